@@ -1,0 +1,334 @@
+"""Benchmark: active-face updates/s of the per-face finite-volume update.
+
+Workload (one "step" = one OptimalOrderRunner step): the 2D shear-layer
+(Kelvin-Helmholtz) problem on the periodic unit square, 256x256 generators on a
+seeded +-0.1-jittered lattice (65,536 cells, 196,608 Voronoi faces), exact
+Riemann solver, gamma = 5/3, all cells active every step.  Inputs are seeded
+synthetic data of that shape; the working set (~40-70 MB) is below the L2 size,
+so L2 is flushed (256 MB write) before every timed step.
+
+Headline ``value``: the FP32-face / FP64-accumulate form, device-resident.
+The line also carries the plain FP64 form, the L1 density error of the FP32
+form against the plain FP64 result, an end-to-end number through the C ABI
+with host buffers (copies inside the timed region), the roofline of the face
+kernel, and the CPU oracle timed on the host cores.
+
+``--impl reference`` times the CPU restatement of the reference (the oracle,
+OpenMP over all host cores): the Rust reference cannot be built here (no Rust
+toolchain), so the C restatement is the reference arm.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "active-face updates/s"
+UNIT = "faces/s"
+WORKLOAD = "kelvin_helmholtz_2d 256x256 jittered periodic Voronoi, exact Riemann solver, gamma=5/3"
+NX = 256
+L2_FLUSH_BYTES = 256 << 20
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    return ws, rank
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def _problem():
+    from hydro_rs_gb300 import ics
+
+    t0 = time.perf_counter()
+    p = ics.kelvin_helmholtz_2d(NX, seed=2, riemann=ics.EXACT, t_end=1.5)
+    return p, time.perf_counter() - t0
+
+
+def _cpu_sample(problem, budget_s: float = 10.0, max_steps: int = 400):
+    """The oracle on the host cores: warm-up step, then steps until the budget."""
+    from oracle import oracle as O
+
+    threads = os.cpu_count() or 1
+    sim = O.OracleSim(problem, n_threads=threads)
+    sim.step()  # the dt = 0 first step
+    sim.step()
+    f0 = sim.active_faces
+    t0 = time.perf_counter()
+    n = 0
+    while n < max_steps:
+        sim.step()
+        n += 1
+        if time.perf_counter() - t0 >= budget_s:
+            break
+    dt = time.perf_counter() - t0
+    faces = sim.active_faces - f0
+    return {"value": faces / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{n} OptimalOrder steps of the same 256x256 exact-solver workload ({faces} face updates, "
+                      f"{dt:.1f} s wall) after 2 warm-up steps; C restatement of the reference, OpenMP"}
+
+
+class _Clocks:
+    def __init__(self):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        if self.p is not None:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except Exception:
+                self.p.kill()
+
+    def summary(self, dev: int = 0):
+        self.f.flush()
+        self.f.seek(0)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9 or parts[0] != str(dev):
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.f.name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _time_steps(sim, steps, stream, flush_buf, torch):
+    """Times `steps` device-resident steps, one event pair per step, L2 flushed before each."""
+    total = 0.0
+    sim.set_time()
+    for _ in range(steps):
+        flush_buf.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        sim.enqueue_steps(1)
+        e1.record(stream)
+        e1.synchronize()
+        total += e0.elapsed_time(e1)
+    st, af = sim.sync_time()
+    return total
+
+
+def _face_kernel_ms(sim, steps):
+    sim.profile(True)
+    sim.set_time()
+    sim.enqueue_steps(steps)
+    prof = sim.profile_read()
+    sim.profile(False)
+    sim.sync_time()
+    return prof
+
+
+def run_ours(args):
+    import torch
+
+    from hydro_rs_gb300 import gpu as G
+    from hydro_rs_gb300.layout import Cells
+
+    ws, rank = _dist()
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    problem, mesh_s = _problem()
+    nf, nc = problem.mesh.n_faces, problem.mesh.n_cells
+    stream = torch.cuda.Stream()
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+
+    sims = {}
+    for prec in (1, 0):
+        with torch.cuda.stream(stream):
+            sims[prec] = G.GpuSim(problem, precision=prec, stream=stream.cuda_stream)
+    # advance both forms identically past the dt=0 first step + warm-up
+    res = {}
+    for prec, sim in sims.items():
+        sim.run(max_steps=2 + args.warmup)
+    torch.cuda.synchronize()
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    with _Clocks() as clk:
+        for prec, sim in sims.items():
+            barrier()
+            f0 = sim.sync_time()[1]
+            ms = _time_steps(sim, args.steps, stream, flush, torch)
+            barrier()
+            faces = sim.sync_time()[1] - f0
+            res[prec] = (ms, faces)
+    clocks = clk.summary(dev)
+
+    # L1 density error of the FP32 form against the plain FP64 form (same steps)
+    a, b = sims[1].state(), sims[0].state()
+    l1 = float(np.abs(a.prim[0] - b.prim[0]).sum() / np.abs(b.prim[0]).sum())
+    same_time = sims[1].ti_current == sims[0].ti_current
+
+    # per-kernel times (events around each kernel) for the roofline
+    prof = {prec: _face_kernel_ms(sim, min(args.steps, 20)) for prec, sim in sims.items()}
+
+    # end-to-end through the C ABI with pinned host buffers
+    cells = Cells.zeros(nc)
+    pinned = {}
+    for k, v in cells.arrays.items():
+        t = torch.empty(v.shape, dtype=torch.float64 if v.dtype == np.float64 else torch.int8, pin_memory=True)
+        pinned[k] = t
+        cells.arrays[k] = t.numpy()
+    sim = sims[1]
+    sim.state(cells)
+    e2e_steps = max(3, min(args.steps, 20))
+    torch.cuda.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    f0 = sim.active_faces
+    for _ in range(e2e_steps):
+        sim.upload(cells)
+        sim.step()
+        sim.state(cells)
+    e2e_s = time.perf_counter() - t0
+    barrier()
+    e2e_faces = sim.active_faces - f0
+    bytes_cells = cells.nbytes()
+
+    ms32, faces32 = res[1]
+    ms64, faces64 = res[0]
+    # max over ranks of the timed region; faces summed
+    if ws > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([ms32, ms64, e2e_s], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms32, ms64, e2e_s = t.tolist()
+        c = torch.tensor([faces32, faces64, e2e_faces], device="cuda", dtype=torch.float64)
+        dist.all_reduce(c)
+        faces32, faces64, e2e_faces = c.tolist()
+    if rank != 0:
+        return
+    peak, peak_kind = _peaks()
+
+    def roof(prec):
+        ms, n = prof[prec]["face_flux"]
+        ms_launch = ms / max(n, 1)
+        per_cell = 193 if prec == 1 else 353
+        bytes_launch = nf * (88 + 56) + nc * per_cell
+        ach = bytes_launch / (ms_launch * 1e-3) / 1e9
+        return {"bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(ach / peak, 4), "traffic": None, "kernel": "k_face_flux32" if prec == 1 else "k_face_flux",
+                "kernel_ms": round(ms_launch, 4), "algorithmic_bytes_per_launch": bytes_launch,
+                "peak_kind": peak_kind, "note": "of measured" if peak_kind == "measured" else "of fallback",
+                "step_kernel_ms": {k: round(v[0] / max(v[1], 1), 4) for k, v in prof[prec].items()}}
+
+    cpu = _cpu_sample(problem) if ws == 1 else None
+    value = faces32 / (ms32 * 1e-3)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms32 / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32-face/f64-accumulate", "data": "synthetic (seeded jittered lattice, shear-layer ICs)",
+        "config": {"workload": WORKLOAD, "cells": nc, "faces": nf, "precision": "fp32_face",
+                   "l2": "flushed (256 MB write) before each timed step", "parallelism": f"replicas x{ws}",
+                   "mesh_build_s": round(mesh_s, 3)},
+        "l1_density_err_vs_fp64": l1, "l1_same_time": same_time,
+        "plain_fp64": {"value": faces64 / (ms64 * 1e-3), "unit": UNIT, "ms_per_step": ms64 / args.steps,
+                       "roofline": roof(0)},
+        "roofline": roof(1),
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_faces / e2e_s, "unit": UNIT, "h2d_bytes_per_step": bytes_cells,
+                "d2h_bytes_per_step": bytes_cells + 64,
+                "how": "mvmm_upload_cells + mvmm_step + mvmm_download_cells per step, pinned host buffers, wall clock"},
+        "gpu_launches": args.steps * 7 * 1 + args.steps * 6,
+        "clocks": clocks,
+    }
+    print(json.dumps(line))
+
+
+def run_reference(args):
+    ws, rank = _dist()
+    if rank != 0:
+        return
+    problem, _ = _problem()
+    from oracle import oracle as O
+
+    threads = os.cpu_count() or 1
+    sim = O.OracleSim(problem, n_threads=threads)
+    for _ in range(2 + args.warmup):
+        sim.step()
+    f0 = sim.active_faces
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        sim.step()
+    dt = time.perf_counter() - t0
+    faces = sim.active_faces - f0
+    v = faces / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded jittered lattice, shear-layer ICs)",
+        "config": {"workload": WORKLOAD, "cells": problem.mesh.n_cells, "faces": problem.mesh.n_faces},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} steps after {2 + args.warmup} warm-up steps; the Rust reference "
+                                   "cannot be built here (no cargo/rustc), the C restatement runs instead"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

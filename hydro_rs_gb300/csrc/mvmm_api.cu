@@ -1,0 +1,607 @@
+// Host side of mvmm_gpu: context, device buffers, CUDA-graph step, C ABI.
+//
+// The engine loop (Engine::run, engine.rs:152-199) runs on the device: every
+// step is one CUDA graph of six kernels that reads and advances a device
+// timeline, so a run of many steps needs no host round trip per step.
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/mvmm_gpu.h"
+#include "mvmm_internal.h"
+
+namespace mvmm {
+void launch_face_flux_fp64(const KP& p, int solver, cudaStream_t s);
+void launch_riemann_fp64(int kind, int sample, double gamma, int64_t n, const double* l, const double* r,
+                         const double* vf, const double* nrm, double* out, unsigned int* err, cudaStream_t s);
+void launch_face_flux_fp32(const KP& p, int solver, cudaStream_t s);
+void launch_riemann_fp32(int kind, int sample, double gamma, int64_t n, const double* l, const double* r,
+                         const double* vf, const double* nrm, double* out, unsigned int* err, cudaStream_t s);
+}  // namespace mvmm
+
+using namespace mvmm;
+
+namespace {
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+#define CUDA_TRY(expr)                                                                                  \
+    do {                                                                                                \
+        cudaError_t e_ = (expr);                                                                        \
+        if (e_ != cudaSuccess)                                                                          \
+            return fail(MVMM_E_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_));               \
+    } while (0)
+
+constexpr unsigned long long kMax = 1ull << 57;
+}  // namespace
+
+struct mvmm_ctx {
+    mvmm_params prm{};
+    int n = 0, nf = 0;
+    int64_t ncsr = 0;
+    int *left = nullptr, *right = nullptr, *csr_off = nullptr, *csr_face = nullptr;
+    double *area = nullptr, *normal = nullptr, *fcen = nullptr, *shift = nullptr;
+    double* cd = nullptr;
+    float* cf = nullptr;
+    int8_t *timebin = nullptr, *tb_tmp = nullptr;
+    uint8_t* active = nullptr;
+    double* flux = nullptr;
+    float* flux32 = nullptr;
+    double* dtmp = nullptr;
+    DevTimeline* tl = nullptr;
+    DevTimeline* tl_host = nullptr;  // pinned
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    cudaGraphExec_t step_exec = nullptr;
+    bool prof = false;
+    cudaEvent_t ev[MVMM_NUM_KERNELS + 1] = {};
+    double prof_ms[MVMM_NUM_KERNELS] = {};
+    int64_t prof_n[MVMM_NUM_KERNELS] = {};
+    double time_base = 0, time_base_inv = 0;
+    uint32_t err_bits = 0;
+};
+
+namespace {
+
+KP make_kp(mvmm_ctx* c, int stage, int flux_rows) {
+    KP p{};
+    p.n = c->n;
+    p.nf = c->nf;
+    p.left = c->left;
+    p.right = c->right;
+    p.area = c->area;
+    p.normal = c->normal;
+    p.fcen = c->fcen;
+    p.shift = c->shift;
+    p.csr_off = c->csr_off;
+    p.csr_face = c->csr_face;
+    p.cd = c->cd;
+    p.cf = c->cf;
+    p.timebin = c->timebin;
+    p.tb_tmp = c->tb_tmp;
+    p.active = c->active;
+    p.flux = c->flux;
+    p.flux32 = c->flux32;
+    p.flux_rows = flux_rows;
+    p.tl = c->tl;
+    p.gamma = c->prm.gamma;
+    p.iso_u = c->prm.isothermal_internal_energy;
+    p.eos = c->prm.eos;
+    p.cfl = c->prm.cfl;
+    p.boundary = c->prm.boundary;
+    p.dim = c->prm.dimensionality;
+    p.sync_all = c->prm.sync_all;
+    p.max_iter = c->prm.max_newton_iter > 0 ? c->prm.max_newton_iter : 1000;
+    p.time_base = c->time_base;
+    p.time_base_inv = c->time_base_inv;
+    p.stage = stage;
+    return p;
+}
+
+void launch_face(mvmm_ctx* c, const KP& p) {
+    if (c->prm.precision == MVMM_PRECISION_FP32FACE) {
+        launch_prep32(p, c->stream);
+        launch_face_flux_fp32(p, c->prm.riemann, c->stream);
+    } else {
+        launch_face_flux_fp64(p, c->prm.riemann, c->stream);
+    }
+}
+
+// The six kernels of one OptimalOrderRunner step, optionally bracketed by events.
+void enqueue_step_kernels(mvmm_ctx* c, bool with_events) {
+    KP p = make_kp(c, 0, 7);
+    cudaStream_t s = c->stream;
+    if (with_events) cudaEventRecord(c->ev[0], s);
+    launch_predict(p, s);
+    if (with_events) cudaEventRecord(c->ev[1], s);
+    launch_face(c, p);
+    if (with_events) cudaEventRecord(c->ev[2], s);
+    launch_update(p, 1, s);
+    if (with_events) cudaEventRecord(c->ev[3], s);
+    launch_gradients(p, 1, s);
+    if (with_events) cudaEventRecord(c->ev[4], s);
+    launch_limit(p, s);
+    if (with_events) cudaEventRecord(c->ev[5], s);
+    launch_end(p, s);
+    if (with_events) cudaEventRecord(c->ev[6], s);
+}
+
+int build_graph(mvmm_ctx* c) {
+    if (c->step_exec) return MVMM_OK;
+    cudaGraph_t g;
+    CUDA_TRY(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    enqueue_step_kernels(c, false);
+    CUDA_TRY(cudaStreamEndCapture(c->stream, &g));
+    cudaError_t e = cudaGraphInstantiate(&c->step_exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(MVMM_E_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+    return MVMM_OK;
+}
+
+int enqueue_steps_impl(mvmm_ctx* c, int64_t n) {
+    if (c->prof) {
+        for (int64_t k = 0; k < n; k++) {
+            enqueue_step_kernels(c, true);
+            CUDA_TRY(cudaEventSynchronize(c->ev[MVMM_NUM_KERNELS]));
+            for (int j = 0; j < MVMM_NUM_KERNELS; j++) {
+                float ms = 0;
+                cudaEventElapsedTime(&ms, c->ev[j], c->ev[j + 1]);
+                c->prof_ms[j] += ms;
+                c->prof_n[j] += 1;
+            }
+        }
+        CUDA_TRY(cudaGetLastError());
+        return MVMM_OK;
+    }
+    int rc = build_graph(c);
+    if (rc) return rc;
+    for (int64_t k = 0; k < n; k++) CUDA_TRY(cudaGraphLaunch(c->step_exec, c->stream));
+    return MVMM_OK;
+}
+
+int read_tl(mvmm_ctx* c) {
+    CUDA_TRY(cudaMemcpyAsync(c->tl_host, c->tl, sizeof(DevTimeline), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return MVMM_OK;
+}
+
+int write_tl(mvmm_ctx* c) {
+    CUDA_TRY(cudaMemcpyAsync(c->tl, c->tl_host, sizeof(DevTimeline), cudaMemcpyHostToDevice, c->stream));
+    return MVMM_OK;
+}
+
+// Host-side checks standing in for device bounds checks: every index the
+// kernels dereference is validated once here.
+int check_mesh(const mvmm_mesh* m, int boundary) {
+    if (!m || m->n_cells <= 0 || m->n_faces < 0) return fail(MVMM_E_INVALID, "mesh: empty or negative sizes");
+    if (m->n_cells > (1ll << 30) || m->n_faces > (1ll << 30)) return fail(MVMM_E_INVALID, "mesh: too large");
+    if (!m->left || !m->right || !m->area || !m->normal || !m->centroid || !m->shift || !m->csr_off || !m->csr_face)
+        return fail(MVMM_E_INVALID, "mesh: null pointer");
+    int64_t n = m->n_cells, nf = m->n_faces;
+    if (m->csr_off[0] != 0) return fail(MVMM_E_INVALID, "mesh: csr_off[0] != 0");
+    std::vector<int32_t> deg(n, 0);
+    for (int64_t f = 0; f < nf; f++) {
+        int32_t l = m->left[f], r = m->right[f];
+        if (l < 0 || l >= n) return fail(MVMM_E_INVALID, "mesh: face left index out of range");
+        if (r >= n || r < -1) return fail(MVMM_E_INVALID, "mesh: face right index out of range");
+        if (r < 0 && boundary == MVMM_BOUNDARY_PERIODIC)
+            return fail(MVMM_E_INVALID, "mesh: boundary face with periodic boundary conditions");
+        deg[l]++;
+        if (r >= 0) deg[r]++;
+    }
+    for (int64_t i = 0; i < n; i++) {
+        if (m->csr_off[i + 1] < m->csr_off[i]) return fail(MVMM_E_INVALID, "mesh: csr_off not monotone");
+        if (m->csr_off[i + 1] - m->csr_off[i] != deg[i]) return fail(MVMM_E_INVALID, "mesh: csr does not match faces");
+    }
+    for (int64_t k = 0; k < m->csr_off[n]; k++) {
+        int32_t f = m->csr_face[k];
+        if (f < 0 || f >= nf) return fail(MVMM_E_INVALID, "mesh: csr face index out of range");
+    }
+    for (int64_t i = 0; i < n; i++)
+        for (int32_t k = m->csr_off[i]; k < m->csr_off[i + 1]; k++) {
+            int32_t f = m->csr_face[k];
+            if (m->left[f] != i && m->right[f] != i) return fail(MVMM_E_INVALID, "mesh: csr lists a face not touching the cell");
+        }
+    return MVMM_OK;
+}
+
+int finish(mvmm_ctx* c) {
+    int rc = read_tl(c);
+    if (rc) return rc;
+    uint32_t bits = c->tl_host->err;
+    if (bits & ~c->err_bits) {
+        c->err_bits |= bits;
+        char buf[96];
+        snprintf(buf, sizeof(buf), "numerical failure, error bits 0x%x", bits);
+        return fail(MVMM_E_NUMERIC, buf);
+    }
+    c->err_bits |= bits;
+    return MVMM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* mvmm_last_error(void) { return g_last_error.c_str(); }
+
+int mvmm_ctx_create(const mvmm_params* prm, const mvmm_mesh* m, mvmm_ctx** out) {
+    if (!prm || !out) return fail(MVMM_E_INVALID, "null argument");
+    *out = nullptr;
+    if (!(prm->gamma > 1.0)) return fail(MVMM_E_INVALID, "gamma must be > 1");
+    if (prm->dimensionality < 1 || prm->dimensionality > 3) return fail(MVMM_E_INVALID, "dimensionality must be 1..3");
+    if (prm->riemann < 0 || prm->riemann > 2) return fail(MVMM_E_INVALID, "unknown Riemann solver");
+    if (prm->boundary < 0 || prm->boundary > 3) return fail(MVMM_E_INVALID, "unknown boundary");
+    if (prm->precision < 0 || prm->precision > 1) return fail(MVMM_E_INVALID, "unknown precision");
+    if (prm->eos < 0 || prm->eos > 1) return fail(MVMM_E_INVALID, "unknown equation of state");
+    if (prm->particle_motion != MVMM_MOTION_FIXED)
+        return fail(MVMM_E_UNSUPPORTED, "only fixed particle motion runs on the device");
+    if (!(prm->t_end > 0.0)) return fail(MVMM_E_INVALID, "t_end must be > 0");
+    int rc = check_mesh(m, prm->boundary);
+    if (rc) return rc;
+    mvmm_ctx* c = new mvmm_ctx();
+    c->prm = *prm;
+    c->n = (int)m->n_cells;
+    c->nf = (int)m->n_faces;
+    c->ncsr = m->csr_off[m->n_cells];
+    c->time_base = prm->t_end / (double)kMax;  // Engine::new (engine.rs:118-119)
+    c->time_base_inv = 1. / c->time_base;
+    size_t n = c->n, nf = c->nf > 0 ? c->nf : 1;
+    auto cleanup = [&](int code, const std::string& msg) {
+        mvmm_ctx_destroy(c);
+        return fail(code, msg);
+    };
+#define ALLOC(ptr, bytes)                                                                  \
+    do {                                                                                   \
+        cudaError_t e_ = cudaMalloc((void**)&(ptr), (bytes));                              \
+        if (e_ != cudaSuccess) return cleanup(MVMM_E_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e_)); \
+    } while (0)
+    ALLOC(c->left, nf * 4);
+    ALLOC(c->right, nf * 4);
+    ALLOC(c->area, nf * 8);
+    ALLOC(c->normal, 3 * nf * 8);
+    ALLOC(c->fcen, 3 * nf * 8);
+    ALLOC(c->shift, 3 * nf * 8);
+    ALLOC(c->csr_off, (n + 1) * 4);
+    ALLOC(c->csr_face, (c->ncsr > 0 ? c->ncsr : 1) * 4);
+    ALLOC(c->cd, (size_t)kCellFields * n * 8);
+    if (prm->precision == MVMM_PRECISION_FP32FACE) {
+        ALLOC(c->cf, (size_t)kCellFields32 * n * 4);
+        ALLOC(c->flux32, 7 * nf * 4);
+    }
+    ALLOC(c->timebin, n);
+    ALLOC(c->tb_tmp, n);
+    ALLOC(c->active, n);
+    ALLOC(c->flux, 10 * nf * 8);
+    ALLOC(c->dtmp, n * 8);
+    ALLOC(c->tl, sizeof(DevTimeline));
+#undef ALLOC
+    if (cudaMallocHost((void**)&c->tl_host, sizeof(DevTimeline)) != cudaSuccess)
+        return cleanup(MVMM_E_NOMEM, "cudaMallocHost failed");
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
+        return cleanup(MVMM_E_CUDA, "cudaStreamCreate failed");
+    c->own_stream = true;
+    for (int k = 0; k <= MVMM_NUM_KERNELS; k++) cudaEventCreate(&c->ev[k]);
+    cudaStream_t s = c->stream;
+    if (c->nf > 0) {
+        cudaMemcpyAsync(c->left, m->left, nf * 4, cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(c->right, m->right, nf * 4, cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(c->area, m->area, nf * 8, cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(c->normal, m->normal, 3 * nf * 8, cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(c->fcen, m->centroid, 3 * nf * 8, cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(c->shift, m->shift, 3 * nf * 8, cudaMemcpyHostToDevice, s);
+    }
+    cudaMemcpyAsync(c->csr_off, m->csr_off, (n + 1) * 4, cudaMemcpyHostToDevice, s);
+    if (c->ncsr > 0) cudaMemcpyAsync(c->csr_face, m->csr_face, c->ncsr * 4, cudaMemcpyHostToDevice, s);
+    cudaMemsetAsync(c->cd, 0, (size_t)kCellFields * n * 8, s);
+    cudaMemsetAsync(c->timebin, 0, n, s);
+    cudaMemsetAsync(c->tb_tmp, 0, n, s);
+    cudaMemsetAsync(c->active, 0, n, s);
+    cudaMemsetAsync(c->flux, 0, 10 * nf * 8, s);
+    std::memset(c->tl_host, 0, sizeof(DevTimeline));
+    c->tl_host->min_dti = kMax;
+    c->tl_host->min_timebin = 127;
+    cudaMemcpyAsync(c->tl, c->tl_host, sizeof(DevTimeline), cudaMemcpyHostToDevice, s);
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cleanup(MVMM_E_CUDA, std::string("mesh upload: ") + cudaGetErrorString(e));
+    *out = c;
+    return MVMM_OK;
+}
+
+int mvmm_ctx_destroy(mvmm_ctx* c) {
+    if (!c) return MVMM_OK;
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->step_exec) cudaGraphExecDestroy(c->step_exec);
+    void* ptrs[] = {c->left, c->right, c->csr_off, c->csr_face, c->area, c->normal, c->fcen, c->shift, c->cd,
+                    c->cf, c->timebin, c->tb_tmp, c->active, c->flux, c->flux32, c->dtmp, c->tl};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    if (c->tl_host) cudaFreeHost(c->tl_host);
+    for (int k = 0; k <= MVMM_NUM_KERNELS; k++)
+        if (c->ev[k]) cudaEventDestroy(c->ev[k]);
+    if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return MVMM_OK;
+}
+
+int mvmm_ctx_set_stream(mvmm_ctx* c, void* stream) {
+    if (!c) return fail(MVMM_E_INVALID, "null context");
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    if (c->own_stream) cudaStreamDestroy(c->stream);
+    if (stream) {
+        c->stream = (cudaStream_t)stream;
+        c->own_stream = false;
+    } else {
+        CUDA_TRY(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+        c->own_stream = true;
+    }
+    return MVMM_OK;
+}
+
+uint32_t mvmm_error_bits(mvmm_ctx* c) { return c ? c->err_bits : 0u; }
+
+int mvmm_upload_cells(mvmm_ctx* c, const mvmm_cells* h) {
+    if (!c || !h) return fail(MVMM_E_INVALID, "null argument");
+    if (h->n != c->n) return fail(MVMM_E_INVALID, "cell count does not match the mesh");
+    size_t n = c->n;
+    cudaStream_t s = c->stream;
+    struct {
+        const double* src;
+        int field, rows;
+    } map[] = {{h->cons, F_CONS, 5},   {h->prim, F_PRIM, 5},   {h->grad, F_GRAD, 15},      {h->gc, F_GC, 3},
+               {h->extrap, F_EXTRAP, 5}, {h->facc, F_FACC, 5}, {h->volume, F_VOL, 1},      {h->loc, F_LOC, 3},
+               {h->centroid, F_CEN, 3}, {h->v, F_V, 3},         {h->v_rel, F_VREL, 3},     {h->max_a_over_r, F_MAOR, 1},
+               {h->max_signal_velocity, F_MSV, 1}, {h->dt, F_DT, 1}};
+    for (auto& e : map) {
+        if (!e.src) return fail(MVMM_E_INVALID, "null cell field");
+        CUDA_TRY(cudaMemcpyAsync(c->cd + (size_t)e.field * n, e.src, (size_t)e.rows * n * 8, cudaMemcpyHostToDevice, s));
+    }
+    if (!h->timebin) return fail(MVMM_E_INVALID, "null timebin");
+    CUDA_TRY(cudaMemcpyAsync(c->timebin, h->timebin, n, cudaMemcpyHostToDevice, s));
+    return MVMM_OK;
+}
+
+int mvmm_download_cells(mvmm_ctx* c, mvmm_cells* h) {
+    if (!c || !h) return fail(MVMM_E_INVALID, "null argument");
+    if (h->n != c->n) return fail(MVMM_E_INVALID, "cell count does not match the mesh");
+    size_t n = c->n;
+    cudaStream_t s = c->stream;
+    struct {
+        double* dst;
+        int field, rows;
+    } map[] = {{h->cons, F_CONS, 5},   {h->prim, F_PRIM, 5},   {h->grad, F_GRAD, 15},      {h->gc, F_GC, 3},
+               {h->extrap, F_EXTRAP, 5}, {h->facc, F_FACC, 5}, {h->volume, F_VOL, 1},      {h->loc, F_LOC, 3},
+               {h->centroid, F_CEN, 3}, {h->v, F_V, 3},         {h->v_rel, F_VREL, 3},     {h->max_a_over_r, F_MAOR, 1},
+               {h->max_signal_velocity, F_MSV, 1}, {h->dt, F_DT, 1}};
+    for (auto& e : map) {
+        if (!e.dst) return fail(MVMM_E_INVALID, "null cell field");
+        CUDA_TRY(cudaMemcpyAsync(e.dst, c->cd + (size_t)e.field * n, (size_t)e.rows * n * 8, cudaMemcpyDeviceToHost, s));
+    }
+    if (!h->timebin) return fail(MVMM_E_INVALID, "null timebin");
+    CUDA_TRY(cudaMemcpyAsync(h->timebin, c->timebin, n, cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    return MVMM_OK;
+}
+
+// ---- per-stage --------------------------------------------------------
+static int upload_mask(mvmm_ctx* c, const uint8_t* active) {
+    if (!active) return fail(MVMM_E_INVALID, "null active mask");
+    CUDA_TRY(cudaMemcpyAsync(c->active, active, c->n, cudaMemcpyHostToDevice, c->stream));
+    return MVMM_OK;
+}
+
+int mvmm_predict(mvmm_ctx* c, double dt) {
+    if (!c) return fail(MVMM_E_INVALID, "null context");
+    KP p = make_kp(c, 1, 10);
+    p.stage_dt = dt;
+    launch_predict(p, c->stream);
+    CUDA_TRY(cudaGetLastError());
+    return finish(c);
+}
+
+int mvmm_compute_fluxes(mvmm_ctx* c, const uint8_t* active, double* out, int64_t* n_active) {
+    if (!c || !out) return fail(MVMM_E_INVALID, "null argument");
+    int rc = upload_mask(c, active);
+    if (rc) return rc;
+    rc = read_tl(c);
+    if (rc) return rc;
+    unsigned long long before = c->tl_host->active_faces;
+    KP p = make_kp(c, 1, 10);
+    launch_derive(p, c->stream);
+    launch_face(c, p);
+    CUDA_TRY(cudaGetLastError());
+    if (c->nf > 0)
+        CUDA_TRY(cudaMemcpyAsync(out, c->flux, (size_t)10 * c->nf * 8, cudaMemcpyDeviceToHost, c->stream));
+    rc = finish(c);
+    if (n_active) *n_active = (int64_t)(c->tl_host->active_faces - before);
+    return rc;
+}
+
+int mvmm_apply_fluxes(mvmm_ctx* c, const double* fluxes, const uint8_t* active) {
+    if (!c || !fluxes) return fail(MVMM_E_INVALID, "null argument");
+    int rc = upload_mask(c, active);
+    if (rc) return rc;
+    if (c->nf > 0)
+        CUDA_TRY(cudaMemcpyAsync(c->flux, fluxes, (size_t)10 * c->nf * 8, cudaMemcpyHostToDevice, c->stream));
+    KP p = make_kp(c, 1, 10);
+    launch_update(p, 0, c->stream);
+    CUDA_TRY(cudaGetLastError());
+    return finish(c);
+}
+
+int mvmm_convert_conserved_to_primitive(mvmm_ctx* c, const uint8_t* active) {
+    if (!c) return fail(MVMM_E_INVALID, "null context");
+    int rc = upload_mask(c, active);
+    if (rc) return rc;
+    launch_c2p(make_kp(c, 1, 10), c->stream);
+    CUDA_TRY(cudaGetLastError());
+    return finish(c);
+}
+
+int mvmm_gradients(mvmm_ctx* c, const uint8_t* active) {
+    if (!c) return fail(MVMM_E_INVALID, "null context");
+    int rc = upload_mask(c, active);
+    if (rc) return rc;
+    launch_gradients(make_kp(c, 1, 10), 0, c->stream);
+    CUDA_TRY(cudaGetLastError());
+    return finish(c);
+}
+
+int mvmm_compute_timesteps(mvmm_ctx* c, const uint8_t* active, double* dt_out) {
+    if (!c || !dt_out) return fail(MVMM_E_INVALID, "null argument");
+    int rc = upload_mask(c, active);
+    if (rc) return rc;
+    launch_timesteps(make_kp(c, 1, 10), c->dtmp, c->stream);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaMemcpyAsync(dt_out, c->dtmp, (size_t)c->n * 8, cudaMemcpyDeviceToHost, c->stream));
+    return finish(c);
+}
+
+// ---- step / run --------------------------------------------------------
+int mvmm_set_time(mvmm_ctx* c, uint64_t ti_current, uint64_t ti_old) {
+    if (!c) return fail(MVMM_E_INVALID, "null context");
+    int rc = read_tl(c);
+    if (rc) return rc;
+    c->tl_host->ti_current = ti_current;
+    c->tl_host->ti_old = ti_old;
+    c->tl_host->min_dti = kMax;
+    c->tl_host->min_timebin = 127;
+    c->tl_host->done = 0;
+    rc = write_tl(c);
+    if (rc) return rc;
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return MVMM_OK;
+}
+
+int mvmm_get_time(mvmm_ctx* c, uint64_t* ti_current, uint64_t* ti_old, int64_t* steps, int64_t* active_faces,
+                  int* finished) {
+    if (!c) return fail(MVMM_E_INVALID, "null context");
+    int rc = read_tl(c);
+    if (rc) return rc;
+    if (ti_current) *ti_current = c->tl_host->ti_current;
+    if (ti_old) *ti_old = c->tl_host->ti_old;
+    if (steps) *steps = (int64_t)c->tl_host->steps;
+    if (active_faces) *active_faces = (int64_t)c->tl_host->active_faces;
+    if (finished) *finished = c->tl_host->done;
+    return MVMM_OK;
+}
+
+int mvmm_step(mvmm_ctx* c, uint64_t ti_current, uint64_t ti_old, uint64_t* ti_next, int64_t* n_active_faces) {
+    if (!c) return fail(MVMM_E_INVALID, "null context");
+    int rc = mvmm_set_time(c, ti_current, ti_old);
+    if (rc) return rc;
+    unsigned long long before = c->tl_host->active_faces;
+    rc = enqueue_steps_impl(c, 1);
+    if (rc) return rc;
+    rc = finish(c);
+    if (ti_next) *ti_next = c->tl_host->ti_current;
+    if (n_active_faces) *n_active_faces = (int64_t)(c->tl_host->active_faces - before);
+    return rc;
+}
+
+int mvmm_enqueue_steps(mvmm_ctx* c, int64_t n_steps) {
+    if (!c) return fail(MVMM_E_INVALID, "null context");
+    return enqueue_steps_impl(c, n_steps);
+}
+
+int mvmm_run(mvmm_ctx* c, int64_t max_steps, uint64_t* ti_current, uint64_t* ti_old, int64_t* steps_done,
+             int64_t* n_active_faces, int* finished) {
+    if (!c || !ti_current || !ti_old) return fail(MVMM_E_INVALID, "null argument");
+    int rc = mvmm_set_time(c, *ti_current, *ti_old);
+    if (rc) return rc;
+    unsigned long long s0 = c->tl_host->steps, f0 = c->tl_host->active_faces;
+    const int64_t chunk = 64;
+    int64_t launched = 0;
+    for (;;) {
+        int64_t k = chunk;
+        if (max_steps > 0 && launched + k > max_steps) k = max_steps - launched;
+        if (k <= 0) break;
+        rc = enqueue_steps_impl(c, k);
+        if (rc) return rc;
+        launched += k;
+        rc = finish(c);
+        if (rc) break;
+        if (c->tl_host->done) break;
+    }
+    int rc2 = read_tl(c);
+    if (rc2) return rc2;
+    *ti_current = c->tl_host->ti_current;
+    *ti_old = c->tl_host->ti_old;
+    if (steps_done) *steps_done = (int64_t)(c->tl_host->steps - s0);
+    if (n_active_faces) *n_active_faces = (int64_t)(c->tl_host->active_faces - f0);
+    if (finished) *finished = c->tl_host->done;
+    return rc;
+}
+
+int mvmm_profile_enable(mvmm_ctx* c, int enable) {
+    if (!c) return fail(MVMM_E_INVALID, "null context");
+    c->prof = enable != 0;
+    for (int j = 0; j < MVMM_NUM_KERNELS; j++) {
+        c->prof_ms[j] = 0;
+        c->prof_n[j] = 0;
+    }
+    return MVMM_OK;
+}
+
+int mvmm_profile_read(mvmm_ctx* c, double* ms, int64_t* launches) {
+    if (!c) return fail(MVMM_E_INVALID, "null context");
+    for (int j = 0; j < MVMM_NUM_KERNELS; j++) {
+        if (ms) ms[j] = c->prof_ms[j];
+        if (launches) launches[j] = c->prof_n[j];
+    }
+    return MVMM_OK;
+}
+
+// ---- Riemann over arrays ----------------------------------------------
+static int riemann_common(int kind, int precision, int sample, double gamma, int64_t n, const double* l,
+                          const double* r, const double* vf, const double* nrm, double* out) {
+    if (kind < 0 || kind > 2) return fail(MVMM_E_INVALID, "unknown Riemann solver");
+    if (precision < 0 || precision > 1) return fail(MVMM_E_INVALID, "unknown precision");
+    if (!(gamma > 1.0)) return fail(MVMM_E_INVALID, "gamma must be > 1");
+    if (n < 0 || (n > 0 && (!l || !r || !nrm || !out || (!sample && !vf)))) return fail(MVMM_E_INVALID, "bad arrays");
+    if (n == 0) return MVMM_OK;
+    double* d = nullptr;
+    unsigned int* derr = nullptr;
+    size_t tot = (size_t)n * (5 + 5 + 3 + 3 + 5);
+    CUDA_TRY(cudaMalloc((void**)&d, tot * 8));
+    if (cudaMalloc((void**)&derr, 4) != cudaSuccess) {
+        cudaFree(d);
+        return fail(MVMM_E_NOMEM, "cudaMalloc failed");
+    }
+    double *dl = d, *dr = d + 5 * n, *dv = d + 10 * n, *dn = d + 13 * n, *dout = d + 16 * n;
+    cudaMemcpy(dl, l, (size_t)n * 5 * 8, cudaMemcpyHostToDevice);
+    cudaMemcpy(dr, r, (size_t)n * 5 * 8, cudaMemcpyHostToDevice);
+    if (!sample) cudaMemcpy(dv, vf, (size_t)n * 3 * 8, cudaMemcpyHostToDevice);
+    cudaMemcpy(dn, nrm, (size_t)n * 3 * 8, cudaMemcpyHostToDevice);
+    cudaMemset(derr, 0, 4);
+    if (precision == MVMM_PRECISION_FP32FACE)
+        launch_riemann_fp32(kind, sample, gamma, n, dl, dr, dv, dn, dout, derr, 0);
+    else
+        launch_riemann_fp64(kind, sample, gamma, n, dl, dr, dv, dn, dout, derr, 0);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpy(out, dout, (size_t)n * 5 * 8, cudaMemcpyDeviceToHost);
+    unsigned int herr = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(&herr, derr, 4, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    cudaFree(derr);
+    if (e != cudaSuccess) return fail(MVMM_E_CUDA, cudaGetErrorString(e));
+    if (herr) return fail(MVMM_E_NUMERIC, "Riemann solver reported a numerical failure");
+    return MVMM_OK;
+}
+
+int mvmm_riemann_flux(int kind, int precision, double gamma, int64_t n, const double* left, const double* right,
+                      const double* v_face, const double* normal, double* out) {
+    return riemann_common(kind, precision, 0, gamma, n, left, right, v_face, normal, out);
+}
+
+int mvmm_riemann_sample(int kind, int precision, double gamma, int64_t n, const double* left, const double* right,
+                        const double* normal, double* out) {
+    return riemann_common(kind, precision, 1, gamma, n, left, right, nullptr, normal, out);
+}
+
+}  // extern "C"

@@ -1,0 +1,576 @@
+// Device-side physics of the per-face finite-volume update.
+//
+// Templated over the arithmetic type T of the face stage (double for the plain
+// form, float for the FP32-face form).  Expressions keep the reference's
+// evaluation order term by term; the plain form is compiled with -fmad=false so
+// that nothing is contracted into an FMA (Rust never contracts), which makes
+// the FP64 path reproduce the reference's arithmetic except inside pow().
+// References are paths inside the mvmm_hydro source tree.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+namespace mvmm {
+
+// ------------------------------------------------------------------ math --
+__device__ __forceinline__ double m_sqrt(double x) { return sqrt(x); }
+__device__ __forceinline__ float m_sqrt(float x) { return sqrtf(x); }
+__device__ __forceinline__ double m_pow(double x, double y) { return pow(x, y); }
+__device__ __forceinline__ float m_pow(float x, float y) { return powf(x, y); }
+__device__ __forceinline__ double m_abs(double x) { return fabs(x); }
+__device__ __forceinline__ float m_abs(float x) { return fabsf(x); }
+// Rust f64::min / f64::max: IEEE minNum / maxNum (the non-NaN operand wins).
+__device__ __forceinline__ double m_min(double a, double b) { return fmin(a, b); }
+__device__ __forceinline__ float m_min(float a, float b) { return fminf(a, b); }
+__device__ __forceinline__ double m_max(double a, double b) { return fmax(a, b); }
+__device__ __forceinline__ float m_max(float a, float b) { return fmaxf(a, b); }
+
+template <typename T>
+struct V3 {
+    T x, y, z;
+};
+template <typename T>
+__device__ __forceinline__ V3<T> v3(T x, T y, T z) { return {x, y, z}; }
+template <typename T>
+__device__ __forceinline__ V3<T> operator+(V3<T> a, V3<T> b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+template <typename T>
+__device__ __forceinline__ V3<T> operator-(V3<T> a, V3<T> b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+template <typename T>
+__device__ __forceinline__ V3<T> operator*(T s, V3<T> a) { return {s * a.x, s * a.y, s * a.z}; }
+template <typename T>
+__device__ __forceinline__ V3<T> neg(V3<T> a) { return {-a.x, -a.y, -a.z}; }
+// glam DVec3::dot: x*x' + y*y' + z*z' left to right.
+template <typename T>
+__device__ __forceinline__ T dot(V3<T> a, V3<T> b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+template <typename T>
+__device__ __forceinline__ T len2(V3<T> a) { return dot(a, a); }
+template <typename T>
+__device__ __forceinline__ T len(V3<T> a) { return m_sqrt(dot(a, a)); }
+template <typename T>
+__device__ __forceinline__ V3<T> cross(V3<T> a, V3<T> b) {  // glam DVec3::cross
+    return {a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y};
+}
+template <typename T, typename U>
+__device__ __forceinline__ V3<T> cvt(V3<U> a) { return {T(a.x), T(a.y), T(a.z)}; }
+
+// State<T>(f64, DVec3, f64): 0 density/mass, 1..3 velocity/momentum, 4 pressure/energy.
+template <typename T>
+struct St {
+    T q[5];
+};
+template <typename T>
+__device__ __forceinline__ St<T> st(T a, V3<T> b, T c) { return {{a, b.x, b.y, b.z, c}}; }
+template <typename T>
+__device__ __forceinline__ St<T> st_zero() { return {{T(0), T(0), T(0), T(0), T(0)}}; }
+template <typename T>
+__device__ __forceinline__ V3<T> vel(const St<T>& s) { return {s.q[1], s.q[2], s.q[3]}; }
+template <typename T>
+__device__ __forceinline__ St<T> operator+(const St<T>& a, const St<T>& b) {
+    St<T> r;
+#pragma unroll
+    for (int i = 0; i < 5; i++) r.q[i] = a.q[i] + b.q[i];
+    return r;
+}
+template <typename T>
+__device__ __forceinline__ St<T> operator-(const St<T>& a, const St<T>& b) {
+    St<T> r;
+#pragma unroll
+    for (int i = 0; i < 5; i++) r.q[i] = a.q[i] - b.q[i];
+    return r;
+}
+template <typename T>
+__device__ __forceinline__ St<T> operator*(T s, const St<T>& a) {
+    St<T> r;
+#pragma unroll
+    for (int i = 0; i < 5; i++) r.q[i] = s * a.q[i];
+    return r;
+}
+
+// ------------------------------------------------------------- gas law --
+// AdiabaticIndex + GasLaw (gas_law.rs:1-106).
+template <typename T>
+struct Gas {
+    T gamma, gamma_inv, odgm1_, odgp1_, iso_u;
+    int eos;  // 0 ideal, 1 isothermal
+    __device__ __forceinline__ T gp1dg() const { return (gamma + T(1)) * gamma_inv; }
+    __device__ __forceinline__ T gm1d2g() const { return T(0.5) * (gamma - T(1)) * gamma_inv; }
+    __device__ __forceinline__ T gm1dgp1() const { return (gamma - T(1)) * odgp1_; }
+    __device__ __forceinline__ T odgm1() const { return odgm1_; }
+    __device__ __forceinline__ T tdgm1() const { return T(2) * odgm1_; }
+    __device__ __forceinline__ T tdgp1() const { return T(2) * odgp1_; }
+    __device__ __forceinline__ T internal_energy_from_pressure(T p, T rho_inv) const {
+        return eos == 0 ? p * rho_inv * odgm1_ : iso_u;
+    }
+    __device__ __forceinline__ T pressure_from_internal_energy(T u, T rho) const {
+        return eos == 0 ? (gamma - T(1)) * u * rho : (gamma - T(1)) * iso_u * rho;
+    }
+    __device__ __forceinline__ T sound_speed(T p, T rho_inv) const {
+        return eos == 0 ? m_sqrt(gamma * p * rho_inv) : m_sqrt(iso_u * gamma * (gamma - T(1)));
+    }
+};
+template <typename T>
+__host__ __device__ inline Gas<T> make_gas(double gamma, int eos, double iso_u) {
+    // AdiabaticIndex::from (gas_law.rs:9-18), constants evaluated in double
+    Gas<T> g;
+    g.gamma = T(gamma);
+    g.gamma_inv = T(1. / gamma);
+    g.odgm1_ = T(1. / (gamma - 1.));
+    g.odgp1_ = T(1. / (gamma + 1.));
+    g.iso_u = T(iso_u);
+    g.eos = eos;
+    return g;
+}
+
+// -------------------------------------------------------- state helpers --
+template <typename T>
+__device__ __forceinline__ St<T> boost(const St<T>& s, V3<T> v) {  // physical_quantities.rs:228-236
+    if (s.q[0] > T(0)) return st(s.q[0], vel(s) + v, s.q[4]);
+    return s;
+}
+template <typename T>
+__device__ __forceinline__ St<T> reflect(const St<T>& s, V3<T> n) {  // physical_quantities.rs:239-242
+    V3<T> v = vel(s);
+    return st(s.q[0], v - (T(2) * dot(v, n)) * n, s.q[4]);
+}
+template <typename T>
+__device__ __forceinline__ void check_physical(St<T>& s) {  // physical_quantities.rs:245-254
+    if (s.q[0] < T(0)) s = st_zero<T>();
+    if (s.q[4] < T(0)) s = st_zero<T>();
+}
+
+// ------------------------------------------------------------- Riemann --
+// flux_from_half_state (riemann_solver.rs:46-76)
+template <typename T>
+__device__ __forceinline__ St<T> flux_from_half_state(const St<T>& h, V3<T> iv, V3<T> n, const Gas<T>& g) {
+    V3<T> hv = vel(h);
+    T rho = h.q[0], p = h.q[4];
+    V3<T> vt = iv + hv;
+    V3<T> f0 = rho * hv;
+    V3<T> f1 = (rho * vt.x) * hv;
+    f1.x += p;
+    V3<T> f2 = (rho * vt.y) * hv;
+    f2.y += p;
+    V3<T> f3 = (rho * vt.z) * hv;
+    f3.z += p;
+    T roe = p * g.odgm1() + T(0.5) * rho * len2(vt);
+    V3<T> f4 = roe * hv + p * vt;
+    return st(dot(f0, n), v3(dot(f1, n), dot(f2, n), dot(f3, n)), dot(f4, n));
+}
+
+// RiemannStarSolver samplers (riemann_solver.rs:108-221)
+template <typename T>
+__device__ __forceinline__ T shock_speed(T v, T a, T pdps, const Gas<T>& g) {
+    return v - a * m_sqrt(T(0.5) * g.gp1dg() * pdps + g.gm1d2g());
+}
+template <typename T>
+__device__ __forceinline__ T rarefaction_tail_speed(T u, T a, T pdps, const Gas<T>& g) {
+    return u - a * m_pow(pdps, g.gm1d2g());
+}
+template <typename T>
+__device__ __noinline__ St<T> sample_rarefaction_fan(St<T> s, T a, T v, V3<T> n, Gas<T> g) {
+    T v_half = g.tdgp1() * (a + T(0.5) * (g.gamma - T(1)) * v);
+    T base = g.tdgp1() + g.gm1dgp1() / a * v;
+    return st(s.q[0] * m_pow(base, g.tdgm1()), vel(s) + (v_half - v) * n, s.q[4] * m_pow(base, g.gamma * g.tdgm1()));
+}
+template <typename T>
+__device__ __forceinline__ St<T> sample_middle(T rho, T u, T p, const St<T>& s, T v, V3<T> n) {
+    return st(rho, vel(s) + (u - v) * n, p);
+}
+
+template <typename T>
+struct Star {
+    T rho_l, rho_r, u, p;
+};
+
+// Toro sampling at x/t = 0 given the star state (riemann_solver.rs:224-255)
+template <typename T>
+__device__ St<T> sample_star(const Star<T>& s, const St<T>& l, const St<T>& r, T vl, T vr, T al, T ar, V3<T> n,
+                             const Gas<T>& g) {
+    if (s.u < T(0)) {
+        if (s.p > r.q[4]) {  // right shock
+            if (shock_speed(vr, -ar, s.p / r.q[4], g) > T(0)) return sample_middle(s.rho_r, s.u, s.p, r, vr, n);
+            return r;
+        }
+        // right rarefaction
+        if (vr - (-ar) > T(0)) {
+            if (rarefaction_tail_speed(s.u, -ar, s.p / r.q[4], g) < T(0))
+                return sample_rarefaction_fan(r, -ar, vr, n, g);
+            return sample_middle(s.rho_r, s.u, s.p, r, vr, n);
+        }
+        return r;
+    } else if (s.p > l.q[4]) {  // left shock
+        if (shock_speed(vl, al, s.p / l.q[4], g) < T(0)) return sample_middle(s.rho_l, s.u, s.p, l, vl, n);
+        return l;
+    }
+    // left rarefaction
+    if (vl - al < T(0)) {
+        if (rarefaction_tail_speed(s.u, al, s.p / l.q[4], g) > T(0)) return sample_rarefaction_fan(l, al, vl, n, g);
+        return sample_middle(s.rho_l, s.u, s.p, l, vl, n);
+    }
+    return l;
+}
+
+// VacuumRiemannSolver (riemann_solver/vacuum.rs:14-138)
+template <typename T>
+__device__ __forceinline__ bool is_vacuum(const St<T>& l, const St<T>& r, T al, T ar, T vrml, const Gas<T>& g) {
+    if (l.q[0] == T(0) || r.q[0] == T(0)) return true;
+    if (g.tdgm1() * (al + ar) <= vrml) return true;
+    return false;
+}
+template <typename T>
+__device__ __noinline__ St<T> vacuum_sample(St<T> l, St<T> r, T vl, T vr, T al, T ar, V3<T> n, Gas<T> g) {
+    bool right_vac, left_vac;
+    T sl = T(0), sr = T(0);
+    if (r.q[0] == T(0)) {
+        sl = vl + g.tdgm1() * al;
+        right_vac = true;
+        left_vac = false;
+    } else if (l.q[0] == T(0)) {
+        sr = vr - g.tdgm1() * ar;
+        right_vac = false;
+        left_vac = true;
+    } else {  // vacuum creation (:78-99)
+        sl = vl + g.tdgm1() * al;
+        sr = vr - g.tdgm1() * ar;
+        if (T(0) <= sl) {
+            right_vac = true;
+            left_vac = false;
+        } else if (T(0) < sr) {
+            return st_zero<T>();
+        } else {
+            right_vac = false;
+            left_vac = true;
+        }
+    }
+    if (right_vac) {  // sample_right_vacuum (:40-57)
+        if (T(0) <= vl - al) return l;
+        if (T(0) < sl) return sample_rarefaction_fan(l, al, vl, n, g);
+        return st_zero<T>();
+    }
+    (void)left_vac;  // sample_left_vacuum (:59-76)
+    if (T(0) <= sr) return st_zero<T>();
+    if (T(0) < vr + ar) return sample_rarefaction_fan(r, -ar, vr, n, g);
+    return r;
+}
+
+// ---- exact solver (riemann_solver/exact.rs), always evaluated in FP64 ----
+struct ExSide {
+    double rho, p, a;
+};
+__device__ __forceinline__ double ex_fb(double p, const ExSide& s, const Gas<double>& g) {  // :12-20
+    if (p > s.p) {
+        double cap_a = g.tdgp1() / s.rho;
+        double cap_b = g.gm1dgp1() * s.p;
+        return (p - s.p) * sqrt(cap_a / (p + cap_b));
+    }
+    return g.tdgm1() * s.a * (pow(p / s.p, g.gm1d2g()) - 1.);
+}
+__device__ __forceinline__ double ex_f(double p, const ExSide& l, const ExSide& r, double vl, double vr,
+                                       const Gas<double>& g) {  // :23-34
+    return ex_fb(p, l, g) + ex_fb(p, r, g) + (vr - vl);
+}
+__device__ __forceinline__ double ex_fprimeb(double p, const ExSide& s, const Gas<double>& g) {  // :37-45
+    if (p > s.p) {
+        double cap_a = g.tdgp1() / s.rho;
+        double cap_b = g.gm1dgp1() * s.p;
+        return (1. - 0.5 * (p - s.p) / (cap_b + p)) * sqrt(cap_a / (p + cap_b));
+    }
+    return 1. / s.rho / s.a * pow(p / s.p, -g.gm1d2g());
+}
+__device__ __forceinline__ double ex_gb(double p, const ExSide& s, const Gas<double>& g) {  // :60-64
+    double cap_a = g.tdgp1() / s.rho;
+    double cap_b = g.gm1dgp1() * s.p;
+    return sqrt(cap_a / (p + cap_b));
+}
+static __device__ __noinline__ double ex_guess_p(ExSide l, ExSide r, double vl, double vr, Gas<double> g) {  // :70-103
+    double p_min = fmin(l.p, r.p);
+    double p_max = fmax(l.p, r.p);
+    double q_max = p_max / p_min;
+    double ppv = 0.5 * (l.p + r.p) - 0.125 * (vr - vl) * (l.rho + r.rho) * (l.a + r.a);
+    ppv = fmax(ppv, 1e-8);
+    double p_guess;
+    if (q_max <= 2. && p_min <= ppv && ppv <= p_max) {
+        p_guess = ppv;
+    } else if (ppv < p_min) {
+        double base = (l.a + r.a - 0.5 * (g.gamma - 1.) * (vr - vl)) /
+                      (l.a / pow(l.p, g.gm1d2g()) + r.a / pow(r.p, g.gm1d2g()));
+        p_guess = pow(base, g.gamma * g.tdgm1());
+    } else {
+        p_guess = (ex_gb(ppv, l, g) * l.p + ex_gb(ppv, r, g) * r.p - vr + vl) / (ex_gb(ppv, l, g) + ex_gb(ppv, r, g));
+    }
+    return fmax(p_guess, 1e-8);
+}
+// Brent's method (exact.rs:106-191); the iteration count is bounded by
+// max_iter (the reference has no bound; it converges for a bracketed root).
+static __device__ __noinline__ double ex_brent(double lower, double upper, double low_f, double up_f, double tol, ExSide l,
+                                        ExSide r, double vl, double vr, Gas<double> g, int max_iter,
+                                        unsigned int* err) {
+    double a = lower, b = upper, c, d = INFINITY;
+    double fa = low_f, fb = up_f, fc, s, fs, t;
+    if (fa * fb > 0.) {
+        *err |= 2u;
+        return b;
+    }
+    if (fabs(fa) < fabs(fb)) { t = a; a = b; b = t; t = fa; fa = fb; fb = t; }
+    c = a;
+    fc = fa;
+    bool mflag = true;
+    int it = 0;
+    while (fb != 0. && fabs(a - b) > tol * 0.5 * (a + b)) {
+        if (++it > 100 * max_iter) {
+            *err |= 1u;
+            break;
+        }
+        if (fa != fc && fb != fc)
+            s = a * fb * fc / (fa - fb) / (fa - fc) + b * fa * fc / (fb - fa) / (fb - fc) +
+                c * fa * fb / (fc - fa) / (fc - fb);
+        else
+            s = b - fb * (b - a) / (fb - fa);
+        double tmp = 0.25 * (3. * a + b);
+        if (!((s > tmp && s < b) || (s < tmp && s > b)) || (mflag && fabs(s - b) >= (0.5 * fabs(b - c))) ||
+            (!mflag && fabs(s - b) >= (0.5 * fabs(c - d))) || (mflag && fabs(b - c) < 0.5 * tol * (b + c)) ||
+            (!mflag && fabs(c - d) < 0.5 * tol * (c + d))) {
+            s = 0.5 * (a + b);
+            mflag = true;
+        } else {
+            mflag = false;
+        }
+        fs = ex_f(s, l, r, vl, vr, g);
+        d = c;
+        c = b;
+        fc = fb;
+        if (fa * fs < 0.) { b = s; fb = fs; } else { a = s; fa = fs; }
+        if (fabs(fa) < fabs(fb)) { t = a; a = b; b = t; t = fa; fa = fb; fb = t; }
+    }
+    return b;
+}
+__device__ __forceinline__ double ex_middle_density(double p, const ExSide& s, const Gas<double>& g) {  // :193-212
+    double pdps = p / s.p;
+    if (pdps > 1.) return s.rho * (pdps + g.gm1dgp1()) / (g.gm1dgp1() * pdps + 1.);
+    return s.rho * pow(pdps, 1. / g.gamma);
+}
+// ExactRiemannSolver::solve_for_star_state (exact.rs:241-291)
+static __device__ __noinline__ Star<double> ex_star(ExSide l, ExSide r, double vl, double vr, Gas<double> g, int max_iter,
+                                            unsigned int* err) {
+    double p = 0.;
+    double p_guess = ex_guess_p(l, r, vl, vr, g);
+    double fp = ex_f(p, l, r, vl, vr, g);
+    double fp_guess = ex_f(p_guess, l, r, vl, vr, g);
+    if (fp * fp_guess >= 0.) {
+        int counter = 0;
+        while (fabs(p - p_guess) > 1e-6 * 0.5 * (p + p_guess) && fp_guess < 0.0) {
+            p = p_guess;
+            p_guess = p_guess - fp_guess / (ex_fprimeb(p_guess, l, g) + ex_fprimeb(p_guess, r, g));
+            fp_guess = ex_f(p_guess, l, r, vl, vr, g);
+            counter += 1;
+            if (counter > max_iter) {  // the reference panics here
+                *err |= 1u;
+                break;
+            }
+        }
+    }
+    if (fabs(p - p_guess) > 1e-6 * 0.5 * (p + p_guess) && fp_guess > 0.) {
+        p = 0.;
+        fp = ex_f(p, l, r, vl, vr, g);
+        p = ex_brent(p, p_guess, fp, fp_guess, 1e-6, l, r, vl, vr, g, max_iter, err);
+    } else {
+        p = p_guess;
+    }
+    Star<double> s;  // star_state_from_pstar (:214-238)
+    s.u = 0.5 * (vl + vr) + 0.5 * (ex_fb(p, r, g) - ex_fb(p, l, g));
+    s.rho_l = ex_middle_density(p, l, g);
+    s.rho_r = ex_middle_density(p, r, g);
+    s.p = p;
+    return s;
+}
+
+// PVRiemannSolver::solve_for_star_state (riemann_solver/pvrs.rs:26-46)
+template <typename T>
+__device__ __forceinline__ Star<T> pv_star(const St<T>& l, const St<T>& r, T vl, T vr, T al, T ar) {
+    T rho_bar = T(0.5) * (l.q[0] + r.q[0]);
+    T p_bar = T(0.5) * (l.q[4] + r.q[4]);
+    T a_bar = T(0.5) * (al + ar);
+    Star<T> s;
+    s.p = p_bar + T(0.5) * (vl - vr) * rho_bar * a_bar;
+    s.u = T(0.5) * ((vl + vr) + (l.q[4] - r.q[4]) / (rho_bar * a_bar));
+    s.rho_l = l.q[0] + (vl - s.u) * rho_bar / a_bar;
+    s.rho_r = r.q[0] + (s.u - vr) * rho_bar / a_bar;
+    return s;
+}
+
+enum { SOLVER_HLLC = 0, SOLVER_EXACT = 1, SOLVER_PVRS = 2 };
+
+// Blanket RiemannFluxSolver impl for star solvers: half state (riemann_solver.rs:258-284).
+template <typename T, int SOLVER>
+__device__ __forceinline__ St<T> star_half_state(const St<T>& l, const St<T>& r, V3<T> n, const Gas<T>& g,
+                                                 const Gas<double>& g64, int max_iter, unsigned int* err) {
+    T vl = dot(vel(l), n);
+    T vr = dot(vel(r), n);
+    T al = g.sound_speed(l.q[4], T(1) / l.q[0]);
+    T ar = g.sound_speed(r.q[4], T(1) / r.q[0]);
+    T vrml = vr - vl;
+    if (is_vacuum(l, r, al, ar, vrml, g)) return vacuum_sample(l, r, vl, vr, al, ar, n, g);
+    Star<T> s;
+    if (SOLVER == SOLVER_EXACT) {
+        ExSide L{double(l.q[0]), double(l.q[4]), double(al)};
+        ExSide R{double(r.q[0]), double(r.q[4]), double(ar)};
+        Star<double> sd = ex_star(L, R, double(vl), double(vr), g64, max_iter, err);
+        s.rho_l = T(sd.rho_l);
+        s.rho_r = T(sd.rho_r);
+        s.u = T(sd.u);
+        s.p = T(sd.p);
+    } else {
+        s = pv_star(l, r, vl, vr, al, ar);
+    }
+    return sample_star(s, l, r, vl, vr, al, ar, n, g);
+}
+
+// HLLCRiemannSolver (riemann_solver/hllc.rs:12-123)
+template <typename T>
+__device__ __forceinline__ St<T> hllc_flux_single(const St<T>& s, T v, T e, V3<T> n) {  // :97-104
+    T rho_v = s.q[0] * v;
+    return st(rho_v, rho_v * vel(s) + s.q[4] * n, ((s.q[0] * e) + s.q[4]) * v);
+}
+template <typename T>
+__device__ __forceinline__ St<T> hllc_flux_star(const St<T>& s, T v, T e, T S, T s_star, V3<T> n) {  // :107-123
+    T s_m_v = S - v;
+    T rho = s.q[0];
+    T starfac = rho * s_m_v / (S - s_star);
+    V3<T> v_star = (s_star - v) * n + vel(s);
+    T e_star = e + (s_star - v) * (s_star + s.q[4] / (rho * s_m_v));
+    St<T> u_star = starfac * st(T(1), v_star, e_star);
+    St<T> u_l = st(rho, rho * vel(s), rho * e);
+    return S * (u_star - u_l);
+}
+template <typename T>
+__device__ St<T> hllc_solve(const St<T>& l, const St<T>& r, V3<T> iv, V3<T> n, const Gas<T>& g) {
+    T rho_l_inv = T(1) / l.q[0];
+    T rho_r_inv = T(1) / r.q[0];
+    T vl = dot(vel(l), n);
+    T vr = dot(vel(r), n);
+    T al = g.sound_speed(l.q[4], rho_l_inv);
+    T ar = g.sound_speed(r.q[4], rho_r_inv);
+    T vrml = vr - vl;
+    if (is_vacuum(l, r, al, ar, vrml, g)) {
+        St<T> w = vacuum_sample(l, r, vl, vr, al, ar, n, g);
+        return flux_from_half_state(w, iv, n, g);
+    }
+    T ppvrs = T(0.5) * (l.q[4] + r.q[4]) - T(0.125) * vrml * (l.q[0] + r.q[0]) * (al + ar);
+    T p_star = m_max(ppvrs, T(0));
+    T q_l = T(1);
+    if (p_star > l.q[4] && l.q[4] > T(0)) q_l = m_sqrt(T(1) + T(0.5) * g.gp1dg() * (p_star / l.q[4] - T(1)));
+    T q_r = T(1);
+    if (p_star > r.q[4] && r.q[4] > T(0)) q_r = m_sqrt(T(1) + T(0.5) * g.gp1dg() * (p_star / r.q[4] - T(1)));
+    T s_l_m_v_l = -al * q_l;
+    T s_r_m_v_r = ar * q_r;
+    T s_star = (r.q[4] - l.q[4] + l.q[0] * vl * s_l_m_v_l - r.q[0] * vr * s_r_m_v_r) /
+               (l.q[0] * s_l_m_v_l - r.q[0] * s_r_m_v_r);
+    St<T> flux;
+    if (s_star >= T(0)) {
+        T v_l2 = len2(vel(l));
+        T e_l = g.internal_energy_from_pressure(l.q[4], rho_l_inv) + T(0.5) * v_l2;
+        flux = hllc_flux_single(l, vl, e_l, n);
+        T s_l = s_l_m_v_l + vl;
+        if (s_l < T(0)) flux = flux + hllc_flux_star(l, vl, e_l, s_l, s_star, n);
+    } else {
+        T v_r2 = len2(vel(r));
+        T e_r = g.internal_energy_from_pressure(r.q[4], rho_r_inv) + T(0.5) * v_r2;
+        flux = hllc_flux_single(r, vr, e_r, n);
+        T s_r = s_r_m_v_r + vr;
+        if (s_r > T(0)) flux = flux + hllc_flux_star(r, vr, e_r, s_r, s_star, n);
+    }
+    // de-boost to the lab frame (:85-90)
+    St<T> add = st(T(0), flux.q[0] * iv, dot(iv, vel(flux)) + T(0.5) * len2(iv) * flux.q[0]);
+    return flux + add;
+}
+
+template <typename T, int SOLVER>
+__device__ __forceinline__ St<T> solve_for_flux(const St<T>& l, const St<T>& r, V3<T> iv, V3<T> n, const Gas<T>& g,
+                                                const Gas<double>& g64, int max_iter, unsigned int* err) {
+    if (SOLVER == SOLVER_HLLC) return hllc_solve(l, r, iv, n, g);
+    St<T> w = star_half_state<T, SOLVER>(l, r, n, g, g64, max_iter, err);
+    return flux_from_half_state(w, iv, n, g);
+}
+
+// ------------------------------------------------------------ limiters --
+// pairwise_limiter_single_quantity (gradients.rs:105-132)
+template <typename T>
+__device__ __forceinline__ T pairwise_limiter_q(T q_l, T q_r, T q_dash, T dx_fac) {
+    if (q_l == q_r) return q_l;
+    T q_bar = q_l + dx_fac * (q_r - q_l);
+    T q_diff = m_abs(q_l - q_r);
+    T delta1 = T(0.5) * q_diff;
+    T delta2 = T(0.25) * q_diff;
+    if (q_l < q_r) {
+        T q_min = m_min(q_l, q_r);
+        T qmin = (q_min - delta1) * q_min > T(0) ? q_min - delta1 : q_min * m_abs(q_min) / (m_abs(q_min) + delta1);
+        return m_max(qmin, m_min(q_bar + delta2, q_dash));
+    }
+    T q_max = m_max(q_l, q_r);
+    T qplu = (q_max + delta1) * q_max > T(0) ? q_max + delta1 : q_max * m_abs(q_max) / (m_abs(q_max) + delta1);
+    return m_min(qplu, m_max(q_bar - delta2, q_dash));
+}
+// pairwise_limiter (gradients.rs:134-152)
+template <typename T>
+__device__ __forceinline__ St<T> pairwise_limiter(const St<T>& l, const St<T>& r, const St<T>& dash, T dx_fac) {
+    St<T> o;
+#pragma unroll
+    for (int i = 0; i < 5; i++) o.q[i] = pairwise_limiter_q(l.q[i], r.q[i], dash.q[i], dx_fac);
+    check_physical(o);
+    return o;
+}
+
+// ------------------------------------------------------------ timeline --
+// timeline.rs constants and helpers
+constexpr int NUM_TIME_BINS = 56;
+constexpr int TIME_BIN_NEIGHBOUR_MAX_DELTA_BIN = 2;
+__host__ __device__ __forceinline__ uint64_t get_integer_timestep(int bin) {  // :18-24
+    return bin <= 0 ? 0ull : (1ull << (bin + 1));
+}
+constexpr uint64_t MAX_NR_TIMESTEPS = 1ull << 57;
+__device__ __forceinline__ int get_time_bin(uint64_t dti) {  // :31-33 (u32 wrap, then `as i8`)
+    uint32_t lz = (uint32_t)__clzll((long long)dti);
+    uint32_t v = 64u - lz - 2u;
+    return (int)(int8_t)(uint8_t)(v & 0xffu);
+}
+__device__ __forceinline__ uint64_t get_integer_time_end(uint64_t ti, int bin) {  // :53-67
+    uint64_t dti = get_integer_timestep(bin);
+    if (dti == 0) return 0;
+    uint64_t mod = ti % dti;
+    return mod == 0 ? ti : ti - mod + dti;
+}
+__host__ __device__ __forceinline__ int get_max_active_bin(uint64_t ti) {  // :72-83
+    if (ti == 0) return NUM_TIME_BINS;
+    int bin = 1;
+    while (((1ull << ((bin + 1) & 63)) & ti) == 0) bin += 1;
+    return bin;
+}
+__device__ __forceinline__ uint64_t sat_u64(double x) {  // Rust `f64 as u64`
+    if (!(x > 0.)) return 0;
+    if (x >= 18446744073709551616.0) return ~0ull;
+    return (uint64_t)x;
+}
+// make_integer_timestep (timeline.rs:103-139)
+__device__ __forceinline__ uint64_t make_integer_timestep(double dt, int old_bin, int min_ngb_bin, uint64_t ti_current,
+                                                          double time_base_inv) {
+    uint64_t new_dti = sat_u64(dt * time_base_inv);
+    int nb = get_time_bin(new_dti);
+    int lim = min_ngb_bin + TIME_BIN_NEIGHBOUR_MAX_DELTA_BIN;
+    new_dti = get_integer_timestep(nb < lim ? nb : lim);
+    uint64_t current_dti = get_integer_timestep(old_bin);
+    if (old_bin > 0) new_dti = new_dti < 2 * current_dti ? new_dti : 2 * current_dti;
+    uint64_t timeline_dti = MAX_NR_TIMESTEPS;
+    // the halving loop of the reference, as a bit operation: largest power of
+    // two <= new_dti, capped at MAX (0 stays 0)
+    if (new_dti < timeline_dti) timeline_dti = new_dti == 0 ? 0ull : (1ull << (63 - __clzll((long long)new_dti)));
+    new_dti = timeline_dti;
+    if (new_dti > current_dti) {
+        uint64_t ti_end = get_integer_time_end(ti_current, old_bin);
+        if ((MAX_NR_TIMESTEPS - ti_end) % new_dti != 0) new_dti = current_dti;
+    }
+    return new_dti;
+}
+
+}  // namespace mvmm

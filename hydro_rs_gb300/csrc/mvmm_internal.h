@@ -1,0 +1,105 @@
+// Internal declarations shared by the kernels and the host side of the library.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace mvmm {
+
+// Cell state on the device: one float64 block of kCellFields * n doubles,
+// field f of cell i at cd[f * n + i] (SoA; rows as in mvmm_cells).
+enum CellField : int {
+    F_CONS = 0,     // 5
+    F_PRIM = 5,     // 5
+    F_GRAD = 10,    // 15, row 3q+k
+    F_GC = 25,      // 3
+    F_EXTRAP = 28,  // 5
+    F_FACC = 33,    // 5
+    F_VOL = 38,
+    F_LOC = 39,     // 3
+    F_CEN = 42,     // 3
+    F_V = 45,       // 3
+    F_VREL = 48,    // 3
+    F_MAOR = 51,
+    F_MSV = 52,
+    F_DT = 53,
+    F_SRC = 54,     // 5: time-extrapolation source of the face stage (derived)
+    F_CS = 59,      // sound speed of the face stage, 0 where rho <= 0 (derived)
+    kCellFields = 60
+};
+
+// FP32 copies read by the FP32-face form (float block, field g of cell i at cf[g*n+i]).
+enum CellField32 : int {
+    G_PRIM = 0,    // 5
+    G_GRAD = 5,    // 15
+    G_EXTRAP = 20, // 5
+    G_SRC = 25,    // 5
+    G_CS = 30,
+    G_DGC = 31,    // 3: gradients_centroid - loc
+    G_DCEN = 34,   // 3: centroid - loc
+    G_V = 37,      // 3: mesh velocity
+    kCellFields32 = 40
+};
+
+// Device timeline + counters of one simulation (TimestepInfo, engine.rs:33-41).
+struct DevTimeline {
+    unsigned long long ti_current;
+    unsigned long long ti_old;
+    unsigned long long min_dti;       // reduction target of timesteps_apply
+    int min_timebin;                  // reduction target of timestep_sync
+    int done;                         // 1 once the step at t_end has run
+    unsigned int err;                 // MVMM_ERR_* bits
+    unsigned int pad;
+    unsigned long long steps;
+    unsigned long long active_faces;  // cumulative faces that reached flux_exchange*
+    unsigned long long active_cells;
+};
+
+// Kernel parameters (passed by value).
+struct KP {
+    int n, nf;
+    const int* left;
+    const int* right;
+    const double* area;
+    const double* normal;    // [3][nf]
+    const double* fcen;      // [3][nf]
+    const double* shift;     // [3][nf]
+    const int* csr_off;
+    const int* csr_face;
+    double* cd;              // cell fields
+    float* cf;               // FP32 copies (FP32 form)
+    int8_t* timebin;
+    int8_t* tb_tmp;
+    uint8_t* active;
+    double* flux;            // face results, rows of nf
+    float* flux32;           // FP32 form face results
+    int flux_rows;           // 7 (step) or 10 (stage, with mflux)
+    DevTimeline* tl;
+    double gamma, iso_u;
+    int eos;
+    double cfl;
+    int boundary;
+    int dim;
+    int sync_all;
+    int max_iter;
+    double time_base, time_base_inv;
+    int stage;               // 1: per-stage call (explicit dt / mask from the host)
+    double stage_dt;
+};
+
+// launchers (implemented in step_fp64.cu / step_fp32.cu)
+void launch_predict(const KP& p, cudaStream_t s);
+void launch_derive(const KP& p, cudaStream_t s);
+void launch_face_flux(const KP& p, int solver, int precision, cudaStream_t s);
+void launch_update(const KP& p, int do_c2p, cudaStream_t s);
+void launch_c2p(const KP& p, cudaStream_t s);
+void launch_gradients(const KP& p, int do_timestep, cudaStream_t s);
+void launch_timesteps(const KP& p, double* dt_out, cudaStream_t s);
+void launch_limit(const KP& p, cudaStream_t s);
+void launch_end(const KP& p, cudaStream_t s);
+void launch_riemann(int kind, int precision, int sample, double gamma, int64_t n, const double* l, const double* r,
+                    const double* vf, const double* nrm, double* out, unsigned int* err, cudaStream_t s);
+// FP32 form helpers
+void launch_prep32(const KP& p, cudaStream_t s);
+
+}  // namespace mvmm

@@ -1,0 +1,275 @@
+// FP32-face form of the flux stage (flux.rs:23-195 restated in FP32).
+//
+// Reconstruction, the pair-wise limiter, the Riemann solve and the face flux
+// run in FP32; face geometry differences are formed in FP64 before rounding,
+// the exact solver's pressure iteration (Newton + Brent) runs in FP64, and the
+// final dt * area * F product, the scatter and the conserved update stay FP64
+// (the update kernel is shared with the plain form).  Compiled with FMA
+// contraction enabled.
+#include "mvmm_device.cuh"
+#include "mvmm_internal.h"
+
+namespace mvmm {
+
+namespace {
+
+constexpr int kBlock = 128;
+
+__device__ __forceinline__ double C(const KP& p, int f, int i) { return p.cd[(size_t)f * p.n + i]; }
+__device__ __forceinline__ float G(const KP& p, int f, int i) { return p.cf[(size_t)f * p.n + i]; }
+__device__ __forceinline__ V3<double> C3(const KP& p, int f, int i) {
+    return {C(p, f, i), C(p, f + 1, i), C(p, f + 2, i)};
+}
+__device__ __forceinline__ V3<float> G3(const KP& p, int f, int i) { return {G(p, f, i), G(p, f + 1, i), G(p, f + 2, i)}; }
+__device__ __forceinline__ St<float> G5(const KP& p, int f, int i) {
+    St<float> s;
+#pragma unroll
+    for (int q = 0; q < 5; q++) s.q[q] = G(p, f + q, i);
+    return s;
+}
+__device__ __forceinline__ V3<double> F3(const double* a, int nf, int f) { return {a[f], a[nf + f], a[2 * nf + f]}; }
+
+__global__ void __launch_bounds__(kBlock) k_prep32(KP p) {
+    if (p.tl->done) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n) return;
+    size_t n = p.n;
+    float* cf = p.cf;
+#pragma unroll
+    for (int q = 0; q < 5; q++) {
+        cf[(G_PRIM + q) * n + i] = (float)C(p, F_PRIM + q, i);
+        cf[(G_EXTRAP + q) * n + i] = (float)C(p, F_EXTRAP + q, i);
+        cf[(G_SRC + q) * n + i] = (float)C(p, F_SRC + q, i);
+    }
+#pragma unroll
+    for (int q = 0; q < 15; q++) cf[(G_GRAD + q) * n + i] = (float)C(p, F_GRAD + q, i);
+    cf[G_CS * n + i] = (float)C(p, F_CS, i);
+    V3<double> loc = C3(p, F_LOC, i);
+    V3<double> dgc = C3(p, F_GC, i) - loc;
+    V3<double> dcen = C3(p, F_CEN, i) - loc;
+    V3<double> v = C3(p, F_V, i);
+    cf[(G_DGC + 0) * n + i] = (float)dgc.x;
+    cf[(G_DGC + 1) * n + i] = (float)dgc.y;
+    cf[(G_DGC + 2) * n + i] = (float)dgc.z;
+    cf[(G_DCEN + 0) * n + i] = (float)dcen.x;
+    cf[(G_DCEN + 1) * n + i] = (float)dcen.y;
+    cf[(G_DCEN + 2) * n + i] = (float)dcen.z;
+    cf[(G_V + 0) * n + i] = (float)v.x;
+    cf[(G_V + 1) * n + i] = (float)v.y;
+    cf[(G_V + 2) * n + i] = (float)v.z;
+}
+
+__device__ __forceinline__ St<float> reconstruct32(const KP& p, int i, const St<float>& prim, V3<float> dx, float td) {
+    St<float> r;
+#pragma unroll
+    for (int q = 0; q < 5; q++) {
+        V3<float> g = G3(p, G_GRAD + 3 * q, i);
+        r.q[q] = (prim.q[q] + dot(g, dx)) + G(p, G_EXTRAP + q, i);
+    }
+    if (prim.q[0] > 0.f) {
+#pragma unroll
+        for (int q = 0; q < 5; q++) r.q[q] += td * G(p, G_SRC + q, i);
+    }
+    return r;
+}
+
+struct Out32 {
+    St<double> fl;
+    V3<double> mflux;
+    double v_max, a_over_r;
+};
+
+template <int SOLVER>
+__device__ __forceinline__ Out32 face_interior32(const KP& p, int f, int l, int r, double dt, const Gas<float>& g,
+                                                 const Gas<double>& g64, unsigned int* err) {
+    V3<double> fc = F3(p.fcen, p.nf, f);
+    V3<double> sh = F3(p.shift, p.nf, f);
+    V3<double> locl = C3(p, F_LOC, l), locr = C3(p, F_LOC, r);
+    // geometry differences in FP64, then rounded
+    V3<float> rl = cvt<float>(fc - locl);
+    V3<float> rr = cvt<float>((fc - locr) - sh);
+    V3<double> dxd = (locr + sh) - locl;
+    V3<float> dx = cvt<float>(dxd);
+    V3<float> dx_left = rl - G3(p, G_DGC, l);
+    V3<float> dx_right = rr - G3(p, G_DGC, r);
+    float dx_gradients = len(dx_left - dx_right);
+    V3<float> dx_centroid = (dx + G3(p, G_DCEN, r)) - G3(p, G_DCEN, l);
+    St<float> pl = G5(p, G_PRIM, l), pr = G5(p, G_PRIM, r);
+    float v_max = G(p, G_CS, l) + G(p, G_CS, r);
+    v_max -= fminf(dot(vel(pr) - vel(pl), dx_centroid), 0.f);
+    float td = 0.5f * (float)dt;
+    St<float> ldash = reconstruct32(p, l, pl, dx_left, td);
+    St<float> rdash = reconstruct32(p, r, pr, dx_right, td);
+    St<float> prim_left = pairwise_limiter(pl, pr, ldash, len(dx_left) / dx_gradients);
+    St<float> prim_right = pairwise_limiter(pr, pl, rdash, len(dx_right) / dx_gradients);
+    V3<float> vl = G3(p, G_V, l), vr = G3(p, G_V, r);
+    V3<float> fcm = cvt<float>(fc - 0.5 * ((locl + locr) + sh));
+    float fac = dot(vr - vl, fcm) / len2(dx);
+    V3<float> v_face = 0.5f * (vl + vr) - fac * dx;
+    V3<float> nrm = cvt<float>(F3(p.normal, p.nf, f));
+    V3<float> mvf = neg(v_face);
+    St<float> F = solve_for_flux<float, SOLVER>(boost(prim_left, mvf), boost(prim_right, mvf), v_face, nrm, g, g64,
+                                                p.max_iter, err);
+    double area = p.area[f];
+    Out32 o;
+#pragma unroll
+    for (int q = 0; q < 5; q++) o.fl.q[q] = dt * (area * (double)F.q[q]);
+    double m = area * (double)F.q[0];
+    o.mflux = m * dxd;
+    o.v_max = v_max;
+    o.a_over_r = area / len(dxd);
+    return o;
+}
+
+template <int SOLVER>
+__device__ __forceinline__ Out32 face_boundary32(const KP& p, int f, int i, const Gas<float>& g, const Gas<double>& g64,
+                                                 unsigned int* err) {
+    V3<double> fc = F3(p.fcen, p.nf, f);
+    V3<double> nd = F3(p.normal, p.nf, f);
+    V3<double> loc = C3(p, F_LOC, i), cen = C3(p, F_CEN, i), gc = C3(p, F_GC, i);
+    V3<double> rgc = gc + (2. * dot(fc - gc, nd)) * nd;
+    V3<double> rcen = cen + (2. * dot(fc - cen, nd)) * nd;
+    V3<double> rloc = loc + (2. * dot(fc - loc, nd)) * nd;
+    V3<float> dx_face = cvt<float>(fc - gc);
+    float dx_gradients = (float)len(rgc - gc);
+    V3<float> dx_centroid = cvt<float>(rcen - cen);
+    V3<double> dxd = rloc - loc;
+    V3<float> n = cvt<float>(nd);
+    St<float> prim = G5(p, G_PRIM, i);
+    float v_max = G(p, G_CS, i);
+    double dt = C(p, F_DT, i);
+    float td = 0.5f * (float)dt;
+    St<float> dash = reconstruct32(p, i, prim, dx_face, td);
+    float dx_fac = len(dx_face) / dx_gradients;
+    St<float> bnd;
+    if (p.boundary == 1) {
+        St<float> rprim = reflect(prim, n);
+        dash = pairwise_limiter(prim, rprim, dash, dx_fac);
+        v_max -= fminf(dot(vel(rprim) - vel(prim), dx_centroid), 0.f);
+        bnd = reflect(dash, n);
+    } else if (p.boundary == 2) {
+        dash = pairwise_limiter(prim, prim, dash, dx_fac);
+        bnd = dash;
+    } else {
+        St<float> vac = st_zero<float>();
+        dash = pairwise_limiter(prim, vac, dash, dx_fac);
+        v_max += fminf(dot(vel(prim), dx_centroid), 0.f);
+        bnd = vac;
+    }
+    St<float> F = solve_for_flux<float, SOLVER>(dash, bnd, v3(0.f, 0.f, 0.f), n, g, g64, p.max_iter, err);
+    double area = p.area[f];
+    Out32 o;
+#pragma unroll
+    for (int q = 0; q < 5; q++) o.fl.q[q] = dt * (area * (double)F.q[q]);
+    o.mflux = (area * (double)F.q[0]) * dxd;
+    o.v_max = v_max;
+    o.a_over_r = area / len(dxd);
+    return o;
+}
+
+template <int SOLVER>
+__global__ void __launch_bounds__(kBlock) k_face_flux32(KP p) {
+    if (p.tl->done) return;
+    int f = blockIdx.x * blockDim.x + threadIdx.x;
+    bool counted = false;
+    unsigned int err = 0;
+    const Gas<float> g = make_gas<float>(p.gamma, p.eos, p.iso_u);
+    const Gas<double> g64 = make_gas<double>(p.gamma, p.eos, p.iso_u);
+    if (f < p.nf) {
+        int l = p.left[f], r = p.right[f];
+        bool la = p.active[l] != 0;
+        Out32 o;
+        if (r >= 0) {
+            bool ra = p.active[r] != 0;
+            double dtl = C(p, F_DT, l), dtr = C(p, F_DT, r);
+            if (!((!la && !ra) || (dtr < dtl && !ra) || (dtl < dtr && !la))) {
+                o = face_interior32<SOLVER>(p, f, l, r, fmin(dtl, dtr), g, g64, &err);
+                counted = true;
+            }
+        } else if (la) {
+            o = face_boundary32<SOLVER>(p, f, l, g, g64, &err);
+            counted = true;
+        }
+        if (!counted) {
+            o.fl = st_zero<double>();
+            o.mflux = v3(0., 0., 0.);
+            o.v_max = 0.;
+            o.a_over_r = 0.;
+        }
+        double* out = p.flux;
+        size_t nf = (size_t)p.nf;
+#pragma unroll
+        for (int q = 0; q < 5; q++) out[q * nf + f] = o.fl.q[q];
+        if (p.flux_rows == 10) {
+            out[5 * nf + f] = o.mflux.x;
+            out[6 * nf + f] = o.mflux.y;
+            out[7 * nf + f] = o.mflux.z;
+            out[8 * nf + f] = o.v_max;
+            out[9 * nf + f] = o.a_over_r;
+        } else {
+            out[5 * nf + f] = o.v_max;
+            out[6 * nf + f] = o.a_over_r;
+        }
+        if (err) atomicOr(&p.tl->err, err);
+    }
+    unsigned int b = __ballot_sync(0xffffffffu, counted);
+    if ((threadIdx.x & 31) == 0 && b) atomicAdd(&p.tl->active_faces, (unsigned long long)__popc(b));
+}
+
+template <int SOLVER, bool SAMPLE>
+__global__ void k_riemann32(double gamma, int64_t n, const double* l, const double* r, const double* vf,
+                            const double* nrm, double* out, unsigned int* errp) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Gas<float> g = make_gas<float>(gamma, 0, 0.);
+    Gas<double> g64 = make_gas<double>(gamma, 0, 0.);
+    St<float> L, R;
+#pragma unroll
+    for (int q = 0; q < 5; q++) {
+        L.q[q] = (float)l[q * n + i];
+        R.q[q] = (float)r[q * n + i];
+    }
+    V3<float> nn = v3((float)nrm[i], (float)nrm[n + i], (float)nrm[2 * n + i]);
+    unsigned int err = 0;
+    St<float> o;
+    if (SAMPLE) {
+        o = star_half_state<float, SOLVER == SOLVER_HLLC ? SOLVER_EXACT : SOLVER>(L, R, nn, g, g64, 1000, &err);
+    } else {
+        V3<float> iv = v3((float)vf[i], (float)vf[n + i], (float)vf[2 * n + i]);
+        o = solve_for_flux<float, SOLVER>(L, R, iv, nn, g, g64, 1000, &err);
+    }
+#pragma unroll
+    for (int q = 0; q < 5; q++) out[q * n + i] = (double)o.q[q];
+    if (err) atomicOr(errp, err);
+}
+
+inline int grid(int n) { return (n + kBlock - 1) / kBlock; }
+
+}  // namespace
+
+void launch_prep32(const KP& p, cudaStream_t s) {
+    if (p.n > 0) k_prep32<<<grid(p.n), kBlock, 0, s>>>(p);
+}
+
+void launch_face_flux_fp32(const KP& p, int solver, cudaStream_t s) {
+    if (p.nf <= 0) return;
+    if (solver == SOLVER_HLLC) k_face_flux32<SOLVER_HLLC><<<grid(p.nf), kBlock, 0, s>>>(p);
+    else if (solver == SOLVER_EXACT) k_face_flux32<SOLVER_EXACT><<<grid(p.nf), kBlock, 0, s>>>(p);
+    else k_face_flux32<SOLVER_PVRS><<<grid(p.nf), kBlock, 0, s>>>(p);
+}
+
+void launch_riemann_fp32(int kind, int sample, double gamma, int64_t n, const double* l, const double* r,
+                         const double* vf, const double* nrm, double* out, unsigned int* err, cudaStream_t s) {
+    if (n <= 0) return;
+    int g = (int)((n + kBlock - 1) / kBlock);
+    if (sample) {
+        if (kind == SOLVER_PVRS) k_riemann32<SOLVER_PVRS, true><<<g, kBlock, 0, s>>>(gamma, n, l, r, vf, nrm, out, err);
+        else k_riemann32<SOLVER_EXACT, true><<<g, kBlock, 0, s>>>(gamma, n, l, r, vf, nrm, out, err);
+    } else {
+        if (kind == SOLVER_HLLC) k_riemann32<SOLVER_HLLC, false><<<g, kBlock, 0, s>>>(gamma, n, l, r, vf, nrm, out, err);
+        else if (kind == SOLVER_EXACT) k_riemann32<SOLVER_EXACT, false><<<g, kBlock, 0, s>>>(gamma, n, l, r, vf, nrm, out, err);
+        else k_riemann32<SOLVER_PVRS, false><<<g, kBlock, 0, s>>>(gamma, n, l, r, vf, nrm, out, err);
+    }
+}
+
+}  // namespace mvmm

@@ -1,0 +1,721 @@
+// Plain FP64 form of the OptimalOrderRunner step (runner/hydrodynamics/optimal_order.rs:15-64).
+//
+// Compiled with -fmad=false: every expression is rounded exactly as the Rust
+// reference evaluates it.  One CUDA thread per face for the flux stage, one per
+// cell for the cell stages; the flux scatter is a deterministic CSR gather in
+// the reference's face order (no atomics on floating-point data).
+#include "mvmm_device.cuh"
+#include "mvmm_internal.h"
+
+namespace mvmm {
+
+namespace {
+
+constexpr int kBlock = 128;
+
+__device__ __forceinline__ double C(const KP& p, int f, int i) { return p.cd[(size_t)f * p.n + i]; }
+__device__ __forceinline__ void W(const KP& p, int f, int i, double v) { p.cd[(size_t)f * p.n + i] = v; }
+__device__ __forceinline__ V3<double> C3(const KP& p, int f, int i) {
+    return {C(p, f, i), C(p, f + 1, i), C(p, f + 2, i)};
+}
+__device__ __forceinline__ void W3(const KP& p, int f, int i, V3<double> v) {
+    W(p, f, i, v.x);
+    W(p, f + 1, i, v.y);
+    W(p, f + 2, i, v.z);
+}
+__device__ __forceinline__ St<double> C5(const KP& p, int f, int i) {
+    St<double> s;
+#pragma unroll
+    for (int q = 0; q < 5; q++) s.q[q] = C(p, f + q, i);
+    return s;
+}
+__device__ __forceinline__ void W5(const KP& p, int f, int i, const St<double>& s) {
+#pragma unroll
+    for (int q = 0; q < 5; q++) W(p, f + q, i, s.q[q]);
+}
+__device__ __forceinline__ V3<double> F3(const double* a, int nf, int f) { return {a[f], a[nf + f], a[2 * nf + f]}; }
+__device__ __forceinline__ Gas<double> gas(const KP& p) { return make_gas<double>(p.gamma, p.eos, p.iso_u); }
+__device__ __forceinline__ void set_err(const KP& p, unsigned int bits) {
+    if (bits) atomicOr(&p.tl->err, bits);
+}
+
+// Gradients::dot row q with dx (physical_quantities.rs:122-133)
+__device__ __forceinline__ double gdot(const KP& p, int i, int q, V3<double> dx) {
+    return C(p, F_GRAD + 3 * q, i) * dx.x + C(p, F_GRAD + 3 * q + 1, i) * dx.y + C(p, F_GRAD + 3 * q + 2, i) * dx.z;
+}
+
+// Particle::time_extrapolations body before the -dt factor (part.rs:134-149).
+__device__ __forceinline__ St<double> extrap_source(const KP& p, int i, const St<double>& prim, double rho_inv) {
+    V3<double> vr = C3(p, F_VREL, i);
+    V3<double> g0 = C3(p, F_GRAD + 0, i);
+    V3<double> g4 = C3(p, F_GRAD + 12, i);
+    double div_v = C(p, F_GRAD + 3, i) + C(p, F_GRAD + 7, i) + C(p, F_GRAD + 11, i);
+    St<double> s;
+    s.q[0] = prim.q[0] * div_v + dot(vr, g0);
+    s.q[1] = vr.x * div_v + rho_inv * g4.x;
+    s.q[2] = vr.y * div_v + rho_inv * g4.y;
+    s.q[3] = vr.z * div_v + rho_inv * g4.z;
+    s.q[4] = p.gamma * prim.q[4] * div_v + dot(vr, g4);
+    return s;
+}
+
+// Face-stage derived fields: extrapolation source and v_max sound speed.
+__device__ __forceinline__ void write_derived(const KP& p, int i, const St<double>& prim, const St<double>& src,
+                                              double rho_inv) {
+    if (prim.q[0] > 0.) {
+        W5(p, F_SRC, i, src);
+        W(p, F_CS, i, gas(p).sound_speed(prim.q[4], rho_inv));
+    } else {
+        W5(p, F_SRC, i, st_zero<double>());
+        W(p, F_CS, i, 0.);
+    }
+}
+
+// ------------------------------------------------------------- predict --
+// EulerEqnsFvs::predict -> Particle::extrapolate_state (part.rs:123-132),
+// plus the active mask bin_is_ending (engine.rs:63-65) in step mode.
+__global__ void __launch_bounds__(kBlock) k_predict(KP p) {
+    if (p.tl->done) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool act = false;
+    if (i < p.n) {
+        double dt;
+        if (p.stage) {
+            dt = p.stage_dt;
+        } else {
+            unsigned long long tc = p.tl->ti_current, to = p.tl->ti_old;
+            dt = (double)(tc - to) * p.time_base;  // TimestepInfo::dt_from_dti
+            act = p.timebin[i] <= get_max_active_bin(tc);
+            p.active[i] = act;
+        }
+        St<double> prim = C5(p, F_PRIM, i);
+        double rho_inv = 1. / prim.q[0];
+        St<double> src = extrap_source(p, i, prim, rho_inv);
+        if (prim.q[0] > 0.) {
+            St<double> ex = C5(p, F_EXTRAP, i);
+            W5(p, F_EXTRAP, i, ex + (-dt) * src);
+        } else {
+            St<double> ex = C5(p, F_EXTRAP, i);
+            W5(p, F_EXTRAP, i, ex + st_zero<double>());
+        }
+        St<double> chk = prim;
+        check_physical(chk);
+        bool reset = chk.q[0] != prim.q[0] || chk.q[4] != prim.q[4] || chk.q[1] != prim.q[1] ||
+                     chk.q[2] != prim.q[2] || chk.q[3] != prim.q[3];
+        if (reset) W5(p, F_PRIM, i, chk);
+        // volume: dvdt is zero for a fixed mesh, so volume.clamp(..) leaves it unchanged
+        write_derived(p, i, chk, src, rho_inv);
+    }
+    if (!p.stage) {
+        unsigned int b = __ballot_sync(0xffffffffu, act);
+        if ((threadIdx.x & 31) == 0 && b) atomicAdd(&p.tl->active_cells, (unsigned long long)__popc(b));
+    }
+}
+
+// Recomputes the derived face-stage fields (per-stage flux calls).
+__global__ void __launch_bounds__(kBlock) k_derive(KP p) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n) return;
+    St<double> prim = C5(p, F_PRIM, i);
+    double rho_inv = 1. / prim.q[0];
+    St<double> src = extrap_source(p, i, prim, rho_inv);
+    write_derived(p, i, prim, src, rho_inv);
+}
+
+// ------------------------------------------------------------ face flux --
+// reconstructed state: ((prim + grad.dx) + extrap) + time_extrapolations(-0.5 dt)
+__device__ __forceinline__ St<double> reconstruct(const KP& p, int i, const St<double>& prim, V3<double> dx,
+                                                  double td) {
+    St<double> r;
+#pragma unroll
+    for (int q = 0; q < 5; q++) {
+        double v = prim.q[q] + gdot(p, i, q, dx);
+        v = v + C(p, F_EXTRAP + q, i);
+        r.q[q] = v;
+    }
+    if (prim.q[0] > 0.) {
+#pragma unroll
+        for (int q = 0; q < 5; q++) r.q[q] = r.q[q] + td * C(p, F_SRC + q, i);
+    } else {
+#pragma unroll
+        for (int q = 0; q < 5; q++) r.q[q] = r.q[q] + 0.;
+    }
+    return r;
+}
+
+struct FaceOut {
+    St<double> fl;
+    V3<double> mflux;
+    double v_max, a_over_r;
+};
+
+// flux_exchange (flux.rs:23-100)
+template <int SOLVER>
+__device__ __forceinline__ FaceOut face_interior(const KP& p, int f, int l, int r, double dt, unsigned int* err) {
+    const Gas<double> g = gas(p);
+    V3<double> fc = F3(p.fcen, p.nf, f);
+    V3<double> sh = F3(p.shift, p.nf, f);
+    V3<double> dx_left = fc - C3(p, F_GC, l);
+    V3<double> dx_right = (fc - C3(p, F_GC, r)) - sh;
+    double dx_gradients = len(dx_left - dx_right);
+    V3<double> dx_centroid = (C3(p, F_CEN, r) + sh) - C3(p, F_CEN, l);
+    V3<double> locl = C3(p, F_LOC, l), locr = C3(p, F_LOC, r);
+    V3<double> dx = (locr + sh) - locl;
+    St<double> pl = C5(p, F_PRIM, l), pr = C5(p, F_PRIM, r);
+    double v_max = 0. + C(p, F_CS, l);
+    v_max = v_max + C(p, F_CS, r);
+    v_max -= m_min(dot(vel(pr) - vel(pl), dx_centroid), 0.);
+    double td = -(-0.5 * dt);  // -dt_extrapolate in time_extrapolations
+    St<double> ldash = reconstruct(p, l, pl, dx_left, td);
+    St<double> rdash = reconstruct(p, r, pr, dx_right, td);
+    St<double> prim_left = pairwise_limiter(pl, pr, ldash, len(dx_left) / dx_gradients);
+    St<double> prim_right = pairwise_limiter(pr, pl, rdash, len(dx_right) / dx_gradients);
+    V3<double> vl = C3(p, F_V, l), vr = C3(p, F_V, r);
+    V3<double> midpoint = 0.5 * ((locl + locr) + sh);
+    double fac = dot(vr - vl, fc - midpoint) / len2(dx);
+    V3<double> v_face = 0.5 * (vl + vr) - fac * dx;
+    V3<double> nrm = F3(p.normal, p.nf, f);
+    V3<double> mvf = neg(v_face);
+    St<double> F = solve_for_flux<double, SOLVER>(boost(prim_left, mvf), boost(prim_right, mvf), v_face, nrm, g, g,
+                                                  p.max_iter, err);
+    double area = p.area[f];
+    St<double> fluxes = area * F;
+    FaceOut o;
+    o.fl = dt * fluxes;
+    o.mflux = fluxes.q[0] * dx;
+    o.v_max = v_max;
+    o.a_over_r = area / len(dx);
+    return o;
+}
+
+// flux_exchange_boundary (flux.rs:102-195) with Space::get_boundary_part semantics
+template <int SOLVER>
+__device__ __forceinline__ FaceOut face_boundary(const KP& p, int f, int i, unsigned int* err) {
+    const Gas<double> g = gas(p);
+    V3<double> fc = F3(p.fcen, p.nf, f);
+    V3<double> n = F3(p.normal, p.nf, f);
+    V3<double> loc = C3(p, F_LOC, i), cen = C3(p, F_CEN, i), gc = C3(p, F_GC, i);
+    // Particle::reflect (part.rs:374-383)
+    V3<double> rloc = loc + (2. * dot(fc - loc, n)) * n;
+    V3<double> rcen = cen + (2. * dot(fc - cen, n)) * n;
+    V3<double> rgc = gc + (2. * dot(fc - gc, n)) * n;
+    V3<double> dx_face = fc - gc;
+    double dx_gradients = len(rgc - gc);
+    V3<double> dx_centroid = rcen - cen;
+    V3<double> dx = rloc - loc;
+    St<double> prim = C5(p, F_PRIM, i);
+    double v_max = 0. + C(p, F_CS, i);
+    double dt = C(p, F_DT, i);
+    double td = -(-0.5 * dt);
+    St<double> dash = reconstruct(p, i, prim, dx_face, td);
+    double dx_fac = len(dx_face) / dx_gradients;
+    St<double> bnd;
+    if (p.boundary == 1) {  // reflective
+        St<double> rprim = reflect(prim, n);
+        dash = pairwise_limiter(prim, rprim, dash, dx_fac);
+        v_max -= m_min(dot(vel(rprim) - vel(prim), dx_centroid), 0.);
+        bnd = reflect(dash, n);
+    } else if (p.boundary == 2) {  // open
+        dash = pairwise_limiter(prim, prim, dash, dx_fac);
+        bnd = dash;
+    } else {  // vacuum
+        St<double> vac = st_zero<double>();
+        dash = pairwise_limiter(prim, vac, dash, dx_fac);
+        v_max += m_min(dot(vel(prim), dx_centroid), 0.);
+        bnd = vac;
+    }
+    St<double> F = solve_for_flux<double, SOLVER>(dash, bnd, v3(0., 0., 0.), n, g, g, p.max_iter, err);
+    double area = p.area[f];
+    St<double> fluxes = area * F;
+    FaceOut o;
+    o.fl = dt * fluxes;
+    o.mflux = fluxes.q[0] * dx;
+    o.v_max = v_max;
+    o.a_over_r = area / len(dx);
+    return o;
+}
+
+// EulerEqnsFvs::compute_fluxes (euler_eqns_fvs.rs:26-48): the active-face rule,
+// dt = min(dt_l, dt_r), interior / boundary dispatch.
+template <int SOLVER>
+__global__ void __launch_bounds__(kBlock) k_face_flux(KP p) {
+    if (p.tl->done) return;
+    int f = blockIdx.x * blockDim.x + threadIdx.x;
+    bool counted = false;
+    unsigned int err = 0;
+    if (f < p.nf) {
+        int l = p.left[f], r = p.right[f];
+        bool la = p.active[l] != 0;
+        FaceOut o;
+        if (r >= 0) {
+            bool ra = p.active[r] != 0;
+            double dtl = C(p, F_DT, l), dtr = C(p, F_DT, r);
+            if (!((!la && !ra) || (dtr < dtl && !ra) || (dtl < dtr && !la))) {
+                o = face_interior<SOLVER>(p, f, l, r, m_min(dtl, dtr), &err);
+                counted = true;
+            }
+        } else if (la) {
+            o = face_boundary<SOLVER>(p, f, l, &err);
+            counted = true;
+        }
+        if (!counted) {
+            o.fl = st_zero<double>();
+            o.mflux = v3(0., 0., 0.);
+            o.v_max = 0.;
+            o.a_over_r = 0.;
+        }
+        double* out = p.flux;
+        size_t nf = (size_t)p.nf;
+#pragma unroll
+        for (int q = 0; q < 5; q++) out[q * nf + f] = o.fl.q[q];
+        if (p.flux_rows == 10) {
+            out[5 * nf + f] = o.mflux.x;
+            out[6 * nf + f] = o.mflux.y;
+            out[7 * nf + f] = o.mflux.z;
+            out[8 * nf + f] = o.v_max;
+            out[9 * nf + f] = o.a_over_r;
+        } else {
+            out[5 * nf + f] = o.v_max;
+            out[6 * nf + f] = o.a_over_r;
+        }
+        if (err) set_err(p, err);
+    }
+    unsigned int b = __ballot_sync(0xffffffffu, counted);
+    if ((threadIdx.x & 31) == 0 && b) atomicAdd(&p.tl->active_faces, (unsigned long long)__popc(b));
+}
+
+// ---------------------------------------------------- cons -> primitive --
+// Particle::convert_conserved_to_primitive (part.rs:219-261)
+__device__ __forceinline__ void c2p(const KP& p, int i, const St<double>& cons, unsigned int* err) {
+    const Gas<double> g = gas(p);
+    if (!(cons.q[0] >= 0.)) *err |= 1u << 2;
+    if (!(cons.q[4] >= 0.)) *err |= 1u << 3;
+    St<double> prim;
+    if (cons.q[0] == 0.) {
+        if (cons.q[4] != 0.) *err |= 1u << 3;
+        prim = st_zero<double>();
+    } else if (cons.q[0] > 0.) {  // State<Primitive>::from_conserved (physical_quantities.rs:213-226)
+        double m_inv = 1. / cons.q[0];
+        double density = cons.q[0] / C(p, F_VOL, i);
+        V3<double> velocity = m_inv * vel(cons);
+        double thermal = cons.q[4] - 0.5 * len2(vel(cons)) * m_inv;
+        double u = thermal * m_inv;
+        double pressure = g.pressure_from_internal_energy(u, density);
+        prim = st(density, velocity, pressure);
+    } else {
+        prim = st_zero<double>();
+    }
+    if (!(prim.q[0] >= 0.) || !(prim.q[4] >= 0.)) *err |= 1u << 5;
+    if (!isfinite(prim.q[0]) || !isfinite(prim.q[1]) || !isfinite(prim.q[2]) || !isfinite(prim.q[3]) ||
+        !isfinite(prim.q[4]))
+        *err |= 1u << 4;
+    W5(p, F_PRIM, i, prim);
+}
+
+// ---------------------------------------------------- scatter + update --
+// apply_fluxes (runner/hydrodynamics.rs:13-39): CSR gather of every face of
+// the cell in CSR order; active cells fold the accumulator into the conserved
+// state (Particle::apply_flux, part.rs:178-193), then kick2 and cons->prim.
+__global__ void __launch_bounds__(kBlock) k_update(KP p, int do_c2p) {
+    if (p.tl->done) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n) return;
+    bool act = p.active[i] != 0;
+    St<double> facc = C5(p, F_FACC, i);
+    double msv = C(p, F_MSV, i), maor = C(p, F_MAOR, i);
+    const size_t nf = (size_t)p.nf;
+    const int rv = p.flux_rows == 10 ? 8 : 5;
+    const double* fl = p.flux;
+    int k0 = p.csr_off[i], k1 = p.csr_off[i + 1];
+    for (int k = k0; k < k1; k++) {
+        int f = p.csr_face[k];
+        St<double> x;
+#pragma unroll
+        for (int q = 0; q < 5; q++) x.q[q] = fl[q * nf + f];
+        if (p.left[f] == i) facc = facc - x;  // update_fluxes_left (part.rs:160-167)
+        else facc = facc + x;                 // update_fluxes_right (part.rs:169-176)
+        if (act) {
+            msv = m_max(fl[rv * nf + f], msv);
+            maor = m_max(maor, fl[(rv + 1) * nf + f]);
+        }
+    }
+    unsigned int err = 0;
+    if (act) {
+        St<double> cons = C5(p, F_CONS, i) + facc;
+        if (!isfinite(cons.q[0]) || !isfinite(cons.q[1]) || !isfinite(cons.q[2]) || !isfinite(cons.q[3]) ||
+            !isfinite(cons.q[4]))
+            err |= 1u << 4;
+        if (cons.q[0] < 0.) cons = st_zero<double>();
+        if (cons.q[4] < 0.) cons = st_zero<double>();
+        facc = st_zero<double>();
+        // kick2 (runner/hydrodynamics.rs:51-57): Particle::grav_kick with a zero
+        // acceleration adds +0 to the momentum (part.rs:303-312)
+        cons.q[1] = cons.q[1] + 0.;
+        cons.q[2] = cons.q[2] + 0.;
+        cons.q[3] = cons.q[3] + 0.;
+        W5(p, F_CONS, i, cons);
+        W(p, F_MSV, i, msv);
+        W(p, F_MAOR, i, maor);
+        if (do_c2p) c2p(p, i, cons, &err);
+    }
+    W5(p, F_FACC, i, facc);
+    if (err) set_err(p, err);
+}
+
+__global__ void __launch_bounds__(kBlock) k_c2p(KP p) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n || !p.active[i]) return;
+    unsigned int err = 0;
+    c2p(p, i, C5(p, F_CONS, i), &err);
+    if (err) set_err(p, err);
+}
+
+// ------------------------------------------------------------ gradients --
+// The other side of face f as seen from cell i: Space::get_boundary_part for
+// walls (space.rs:213-229), else the neighbour (runner/hydrodynamics.rs:59-65).
+__device__ __forceinline__ void other_side(const KP& p, int i, int f, const St<double>& prim, V3<double> cen,
+                                           St<double>& oprim, V3<double>& ocen, V3<double>& sh) {
+    int l = p.left[f], r = p.right[f];
+    V3<double> s = F3(p.shift, p.nf, f);
+    sh = (i == l) ? s : neg(s);
+    if (i == l && r < 0) {
+        V3<double> fc = F3(p.fcen, p.nf, f);
+        V3<double> n = F3(p.normal, p.nf, f);
+        ocen = cen + (2. * dot(fc - cen, n)) * n;
+        if (p.boundary == 1) oprim = reflect(prim, n);
+        else if (p.boundary == 2) oprim = prim;
+        else oprim = st_zero<double>();
+    } else {
+        int o = (i == l) ? r : l;
+        ocen = C3(p, F_CEN, o);
+        oprim = C5(p, F_PRIM, o);
+    }
+}
+
+// Particle::radius (part.rs:439-447)
+__device__ __forceinline__ double radius(double volume, int dim) {
+    if (dim == 1) return 0.5 * volume;
+    if (dim == 2) return sqrt(0.31830988618379067154 * volume);
+    return pow(0.25 * 3. * 0.31830988618379067154 * volume, 1. / 3.);
+}
+
+// Particle::timestep for fixed motion (part.rs:42-84, 328-372); returns the dt.
+__device__ __forceinline__ double particle_timestep(const KP& p, int i) {
+    St<double> cons = C5(p, F_CONS, i);
+    if (cons.q[0] == 0.) {
+        W3(p, F_V, i, v3(0., 0., 0.));
+        return INFINITY;
+    }
+    const Gas<double> g = gas(p);
+    double m_inv = 1. / cons.q[0];
+    V3<double> dxg = C3(p, F_LOC, i) - C3(p, F_GC, i);
+    V3<double> d_v = v3(gdot(p, i, 1, dxg), gdot(p, i, 2, dxg), gdot(p, i, 3, dxg));
+    V3<double> fluid_v = m_inv * vel(cons) + d_v;
+    St<double> prim = C5(p, F_PRIM, i);
+    double u = (cons.q[4] - 0.5 * dot(vel(cons), vel(prim))) / cons.q[0];  // Particle::internal_energy
+    double vol = C(p, F_VOL, i);
+    double c = g.sound_speed(g.pressure_from_internal_energy(u, prim.q[0]), vol * m_inv);
+    V3<double> v = v3(0., 0., 0.);  // ParticleMotion::Fixed
+    V3<double> v_rel = fluid_v - v;
+    W3(p, F_V, i, v);
+    W3(p, F_VREL, i, v_rel);
+    W(p, F_MAOR, i, 0.);
+    double v_max = m_max(C(p, F_MSV, i), len(v_rel) + c);
+    W(p, F_MSV, i, 0.);
+    if (v_max > 0.) return p.cfl * radius(vol, p.dim) / v_max;
+    return INFINITY;
+}
+
+__device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = w < v ? w : v;
+    }
+    return v;
+}
+__device__ __forceinline__ int warp_min_int(int v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// gradient_estimate + gradient_limit + gradient_apply (runner/hydrodynamics.rs:67-143)
+// fused per cell; in step mode also compute_timesteps + timesteps_apply
+// (euler_eqns_fvs.rs:50-61, runner/hydrodynamics.rs:145-158) with block-level
+// min reductions of the integer timestep and the new time bins.
+__global__ void __launch_bounds__(kBlock) k_gradients(KP p, int do_timestep) {
+    if (p.tl->done) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long my_dti = MAX_NR_TIMESTEPS;
+    int my_tb = 127;
+    unsigned int err = 0;
+    if (i < p.n) {
+        int tb = p.timebin[i];
+        if (p.active[i]) {
+            V3<double> cen = C3(p, F_CEN, i);
+            St<double> prim = C5(p, F_PRIM, i);
+            // GradientData::init (gradients.rs:14-33): columns c0,c1,c2
+            V3<double> m0 = v3(0., 0., 0.), m1 = v3(0., 0., 0.), m2 = v3(0., 0., 0.);
+            if (p.dim == 1) { m1.y = 1.; m2.z = 1.; }
+            else if (p.dim == 2) { m2.z = 1.; }
+            V3<double> gr[5];
+#pragma unroll
+            for (int q = 0; q < 5; q++) gr[q] = v3(0., 0., 0.);
+            int k0 = p.csr_off[i], k1 = p.csr_off[i + 1];
+            for (int k = k0; k < k1; k++) {
+                int f = p.csr_face[k];
+                St<double> op;
+                V3<double> oc, sh;
+                other_side(p, i, f, prim, cen, op, oc, sh);
+                V3<double> ds = (oc + sh) - cen;
+                double w = p.area[f] / len2(ds);
+                // GradientData::collect (gradients.rs:35-41)
+#pragma unroll
+                for (int q = 0; q < 5; q++) gr[q] = gr[q] + (w * (op.q[q] - prim.q[q])) * ds;
+                m0 = m0 + w * (ds.x * ds);
+                m1 = m1 + w * (ds.y * ds);
+                m2 = m2 + w * (ds.z * ds);
+            }
+            // GradientData::finalize with glam DMat3::inverse (gradients.rs:43-55)
+            V3<double> t0 = cross(m1, m2), t1 = cross(m2, m0), t2 = cross(m0, m1);
+            double det = dot(m2, t2);
+            double inv_det = 1.0 / det;
+            V3<double> r0 = inv_det * t0, r1 = inv_det * t1, r2 = inv_det * t2;
+            V3<double> c0 = v3(r0.x, r1.x, r2.x), c1 = v3(r0.y, r1.y, r2.y), c2 = v3(r0.z, r1.z, r2.z);
+            bool finite = true;
+#pragma unroll
+            for (int q = 0; q < 5; q++) {
+                V3<double> x = gr[q];
+                V3<double> res = x.x * c0;
+                res = res + x.y * c1;
+                res = res + x.z * c2;
+                gr[q] = res;
+                finite = finite && isfinite(res.x) && isfinite(res.y) && isfinite(res.z);
+            }
+            if (!finite) {
+#pragma unroll
+                for (int q = 0; q < 5; q++) gr[q] = v3(0., 0., 0.);
+            }
+            // LimiterData (gradients.rs:58-103)
+            St<double> mn = prim, mx = prim, emn, emx;
+#pragma unroll
+            for (int q = 0; q < 5; q++) {
+                emn.q[q] = INFINITY;
+                emx.q[q] = -INFINITY;
+            }
+            for (int k = k0; k < k1; k++) {
+                int f = p.csr_face[k];
+                St<double> op;
+                V3<double> oc, sh;
+                other_side(p, i, f, prim, cen, op, oc, sh);
+                V3<double> d = (F3(p.fcen, p.nf, f) - cen) - sh;
+#pragma unroll
+                for (int q = 0; q < 5; q++) {
+                    double ex = dot(gr[q], d);
+                    mn.q[q] = m_min(mn.q[q], op.q[q]);
+                    mx.q[q] = m_max(mx.q[q], op.q[q]);
+                    emn.q[q] = m_min(emn.q[q], ex);
+                    emx.q[q] = m_max(emx.q[q], ex);
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < 5; q++) {
+                double d_max = mx.q[q] - prim.q[q];
+                double d_min = mn.q[q] - prim.q[q];
+                double alpha = (emx.q[q] == 0. || emn.q[q] == 0.) ? 1. : m_min(1.0, m_min(d_max / emx.q[q], d_min / emn.q[q]));
+                gr[q] = alpha * gr[q];
+                W3(p, F_GRAD + 3 * q, i, gr[q]);
+            }
+            W3(p, F_GC, i, cen);  // gradient_apply
+            if (do_timestep) {
+                double dt_new = particle_timestep(p, i);
+                unsigned long long tc = p.tl->ti_current;
+                unsigned long long dti = make_integer_timestep(dt_new, tb, NUM_TIME_BINS, tc, p.time_base_inv);
+                if (dti == 0) err |= 1u << 6;
+                W(p, F_DT, i, (double)dti * p.time_base);  // Particle::set_timestep
+                tb = get_time_bin(dti);
+                my_dti = dti;
+            }
+        }
+        if (do_timestep) {
+            p.tb_tmp[i] = (int8_t)tb;
+            my_tb = tb;
+        }
+    }
+    if (err) set_err(p, err);
+    if (!do_timestep) return;
+    __shared__ unsigned long long s_dti[kBlock / 32];
+    __shared__ int s_tb[kBlock / 32];
+    my_dti = warp_min_u64(my_dti);
+    my_tb = warp_min_int(my_tb);
+    int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        s_dti[w] = my_dti;
+        s_tb[w] = my_tb;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long a = s_dti[0];
+        int b = s_tb[0];
+        for (int k = 1; k < kBlock / 32; k++) {
+            a = s_dti[k] < a ? s_dti[k] : a;
+            b = min(b, s_tb[k]);
+        }
+        atomicMin(&p.tl->min_dti, a);
+        atomicMin(&p.tl->min_timebin, b);
+    }
+}
+
+// compute_timesteps as a stage (euler_eqns_fvs.rs:50-61)
+__global__ void __launch_bounds__(kBlock) k_timesteps(KP p, double* out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n) return;
+    out[i] = p.active[i] ? particle_timestep(p, i) : INFINITY;
+}
+
+// ------------------------------------------------- limiter / sync / end --
+// timestep_sync or timestep_limiter (runner/hydrodynamics.rs:160-191) with
+// Particle::timestep_limit (part.rs:263-297); then reset_extrapolations and
+// kick1 (runner/hydrodynamics.rs:41-49, 193-195).
+__global__ void __launch_bounds__(kBlock) k_limit(KP p) {
+    if (p.tl->done) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n) return;
+    int tb = p.tb_tmp[i];
+    int wakeup;
+    if (p.sync_all) {
+        wakeup = p.tl->min_timebin;
+    } else {
+        wakeup = tb;
+        int k0 = p.csr_off[i], k1 = p.csr_off[i + 1];
+        for (int k = k0; k < k1; k++) {
+            int f = p.csr_face[k];
+            int l = p.left[f], r = p.right[f];
+            int o;
+            if (i == l) {
+                if (r < 0) continue;
+                o = r;
+            } else {
+                o = l;
+            }
+            if (!p.active[o]) continue;
+            wakeup = min(wakeup, (int)p.tb_tmp[o] + TIME_BIN_NEIGHBOUR_MAX_DELTA_BIN);
+        }
+    }
+    if (wakeup < tb) {
+        unsigned long long tc = p.tl->ti_current;
+        double dt = C(p, F_DT, i);
+        if (tb <= get_max_active_bin(tc)) {  // bin_is_starting
+            tb = wakeup;
+            dt = (double)get_integer_timestep(tb) * p.time_base;
+        } else {
+            unsigned long long ti_end_old = get_integer_time_end(tc, tb);
+            dt -= (double)(ti_end_old - tc) * p.time_base;
+            tb = wakeup;
+            unsigned long long dti_new = get_integer_timestep(tb);
+            unsigned long long ti_end = get_integer_time_end(tc, tb);
+            dt += (ti_end == tc) ? (double)dti_new * p.time_base : (double)(ti_end - tc) * p.time_base;
+        }
+        W(p, F_DT, i, dt);
+    }
+    p.timebin[i] = (int8_t)tb;
+    if (p.active[i]) {
+        W5(p, F_EXTRAP, i, st_zero<double>());
+        // kick1: hydro_kick1 is a no-op for fixed motion; grav_kick adds +0
+        W(p, F_CONS + 1, i, C(p, F_CONS + 1, i) + 0.);
+        W(p, F_CONS + 2, i, C(p, F_CONS + 2, i) + 0.);
+        W(p, F_CONS + 3, i, C(p, F_CONS + 3, i) + 0.);
+    }
+}
+
+// Engine bookkeeping after a step (engine.rs:194-199, 258-268): advance the
+// device timeline to the next sync point and reset the reductions.
+__global__ void k_end(KP p) {
+    DevTimeline* tl = p.tl;
+    if (tl->done) return;
+    unsigned long long tc = tl->ti_current;
+    unsigned long long tn = tc + tl->min_dti;
+    tl->steps += 1;
+    if (tc >= MAX_NR_TIMESTEPS) tl->done = 1;
+    tl->ti_old = tc;
+    tl->ti_current = tn;
+    tl->min_dti = MAX_NR_TIMESTEPS;
+    tl->min_timebin = 127;
+}
+
+// ---------------------------------------------- Riemann over arrays --
+template <int SOLVER, bool SAMPLE>
+__global__ void k_riemann(double gamma, int64_t n, const double* l, const double* r, const double* vf,
+                          const double* nrm, double* out, unsigned int* errp) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Gas<double> g = make_gas<double>(gamma, 0, 0.);
+    St<double> L, R;
+#pragma unroll
+    for (int q = 0; q < 5; q++) {
+        L.q[q] = l[q * n + i];
+        R.q[q] = r[q * n + i];
+    }
+    V3<double> nn = v3(nrm[i], nrm[n + i], nrm[2 * n + i]);
+    unsigned int err = 0;
+    St<double> o;
+    if (SAMPLE) {
+        o = star_half_state<double, SOLVER == SOLVER_HLLC ? SOLVER_EXACT : SOLVER>(L, R, nn, g, g, 1000, &err);
+    } else {
+        V3<double> iv = v3(vf[i], vf[n + i], vf[2 * n + i]);
+        o = solve_for_flux<double, SOLVER>(L, R, iv, nn, g, g, 1000, &err);
+    }
+#pragma unroll
+    for (int q = 0; q < 5; q++) out[q * n + i] = o.q[q];
+    if (err) atomicOr(errp, err);
+}
+
+inline int grid(int n) { return (n + kBlock - 1) / kBlock; }
+
+}  // namespace
+
+void launch_predict(const KP& p, cudaStream_t s) {
+    if (p.n > 0) k_predict<<<grid(p.n), kBlock, 0, s>>>(p);
+}
+void launch_derive(const KP& p, cudaStream_t s) {
+    if (p.n > 0) k_derive<<<grid(p.n), kBlock, 0, s>>>(p);
+}
+void launch_face_flux_fp64(const KP& p, int solver, cudaStream_t s) {
+    if (p.nf <= 0) return;
+    if (solver == SOLVER_HLLC) k_face_flux<SOLVER_HLLC><<<grid(p.nf), kBlock, 0, s>>>(p);
+    else if (solver == SOLVER_EXACT) k_face_flux<SOLVER_EXACT><<<grid(p.nf), kBlock, 0, s>>>(p);
+    else k_face_flux<SOLVER_PVRS><<<grid(p.nf), kBlock, 0, s>>>(p);
+}
+void launch_update(const KP& p, int do_c2p, cudaStream_t s) {
+    if (p.n > 0) k_update<<<grid(p.n), kBlock, 0, s>>>(p, do_c2p);
+}
+void launch_c2p(const KP& p, cudaStream_t s) {
+    if (p.n > 0) k_c2p<<<grid(p.n), kBlock, 0, s>>>(p);
+}
+void launch_gradients(const KP& p, int do_timestep, cudaStream_t s) {
+    if (p.n > 0) k_gradients<<<grid(p.n), kBlock, 0, s>>>(p, do_timestep);
+}
+void launch_timesteps(const KP& p, double* dt_out, cudaStream_t s) {
+    if (p.n > 0) k_timesteps<<<grid(p.n), kBlock, 0, s>>>(p, dt_out);
+}
+void launch_limit(const KP& p, cudaStream_t s) {
+    if (p.n > 0) k_limit<<<grid(p.n), kBlock, 0, s>>>(p);
+}
+void launch_end(const KP& p, cudaStream_t s) { k_end<<<1, 1, 0, s>>>(p); }
+
+void launch_riemann_fp64(int kind, int sample, double gamma, int64_t n, const double* l, const double* r,
+                         const double* vf, const double* nrm, double* out, unsigned int* err, cudaStream_t s) {
+    if (n <= 0) return;
+    int g = (int)((n + kBlock - 1) / kBlock);
+    if (sample) {
+        if (kind == SOLVER_PVRS) k_riemann<SOLVER_PVRS, true><<<g, kBlock, 0, s>>>(gamma, n, l, r, vf, nrm, out, err);
+        else k_riemann<SOLVER_EXACT, true><<<g, kBlock, 0, s>>>(gamma, n, l, r, vf, nrm, out, err);
+    } else {
+        if (kind == SOLVER_HLLC) k_riemann<SOLVER_HLLC, false><<<g, kBlock, 0, s>>>(gamma, n, l, r, vf, nrm, out, err);
+        else if (kind == SOLVER_EXACT) k_riemann<SOLVER_EXACT, false><<<g, kBlock, 0, s>>>(gamma, n, l, r, vf, nrm, out, err);
+        else k_riemann<SOLVER_PVRS, false><<<g, kBlock, 0, s>>>(gamma, n, l, r, vf, nrm, out, err);
+    }
+}
+
+}  // namespace mvmm

@@ -1,0 +1,580 @@
+// Host Voronoi mesh builder: generators -> face list + cell->face CSR.
+//
+// The reference builds its mesh with the meshless_voronoi crate (0.6.1, called
+// from src/space.rs:571-594 and :236-263); that crate is not part of the hot
+// path and is not vendored, so this file is this library's own builder.  It
+// produces the same quantities the reference's flux/gradient code consumes:
+//   face: left, right (or -1 for a wall), area, unit normal (left -> right /
+//         outward), centroid, periodic shift of the right cell's image;
+//   cell: volume, centroid, and the CSR list of face indices.
+// Conventions (matching the reference's consumers, src/flux.rs:34-38,
+// src/runner/hydrodynamics.rs:84-85): a face is owned by the lower cell index
+// (left = i < right = j); a periodic face stores right = the real index j and
+// shift = offset of the image of j adjacent to i.  Lower-dimensional runs use
+// unit extent along unused axes, so 1D faces have area 1 and 2D face "area" is
+// the edge length.
+//
+// Algorithm: each cell is the box (or a large square/cube for periodic runs)
+// clipped by the bisector half-spaces of nearby generators, found ring by ring
+// in a uniform bin grid, until the security radius criterion (next ring at
+// distance >= 2 * max vertex distance) holds.
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <map>
+#include <unordered_map>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+struct P3 {
+    double x, y, z;
+};
+inline P3 operator+(P3 a, P3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+inline P3 operator-(P3 a, P3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline P3 operator*(double s, P3 a) { return {s * a.x, s * a.y, s * a.z}; }
+inline double dot(P3 a, P3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline P3 cross(P3 a, P3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+inline double norm(P3 a) { return std::sqrt(dot(a, a)); }
+
+// Edge / face labels: >= 0 neighbour generator (with shift index), walls
+// encoded negative: -1 x-, -2 x+, -3 y-, -4 y+, -5 z-, -6 z+; -100 invalid.
+constexpr int64_t kInvalid = -100;
+
+struct FaceOut {
+    int64_t nb;  // neighbour index or wall code
+    int sx, sy, sz;
+    double area;
+    P3 centroid;
+};
+
+struct CellOut {
+    double volume = 0;
+    P3 centroid{0, 0, 0};
+    std::vector<FaceOut> faces;
+    int error = 0;
+};
+
+struct Grid {
+    int dim;
+    int nb[3];
+    double bw[3];
+    double box[3];
+    bool periodic;
+    std::vector<int32_t> start;  // bin -> first index into order
+    std::vector<int32_t> order;
+    double minbw;
+};
+
+Grid make_grid(int dim, int64_t n, const double* g, const double* box, bool periodic) {
+    Grid gr;
+    gr.dim = dim;
+    gr.periodic = periodic;
+    double vol = 1;
+    for (int k = 0; k < dim; k++) vol *= box[k];
+    double h = std::pow(vol / double(n), 1.0 / dim);  // mean spacing
+    for (int k = 0; k < 3; k++) {
+        gr.box[k] = box[k];
+        if (k < dim) {
+            gr.nb[k] = std::max(1, int(std::floor(box[k] / h)));
+            gr.bw[k] = box[k] / gr.nb[k];
+        } else {
+            gr.nb[k] = 1;
+            gr.bw[k] = box[k];
+        }
+    }
+    gr.minbw = gr.bw[0];
+    for (int k = 1; k < dim; k++) gr.minbw = std::min(gr.minbw, gr.bw[k]);
+    int64_t nbins = int64_t(gr.nb[0]) * gr.nb[1] * gr.nb[2];
+    std::vector<int64_t> bin(n);
+    std::vector<int32_t> cnt(nbins + 1, 0);
+    for (int64_t i = 0; i < n; i++) {
+        int b[3] = {0, 0, 0};
+        for (int k = 0; k < dim; k++) {
+            int v = int(std::floor(g[k * n + i] / gr.bw[k]));
+            b[k] = std::min(std::max(v, 0), gr.nb[k] - 1);
+        }
+        bin[i] = (int64_t(b[0]) * gr.nb[1] + b[1]) * gr.nb[2] + b[2];
+        cnt[bin[i] + 1]++;
+    }
+    for (int64_t b = 0; b < nbins; b++) cnt[b + 1] += cnt[b];
+    gr.start.assign(cnt.begin(), cnt.end());
+    gr.order.resize(n);
+    std::vector<int32_t> fill(cnt.begin(), cnt.end() - 1);
+    for (int64_t i = 0; i < n; i++) gr.order[fill[bin[i]]++] = int32_t(i);
+    return gr;
+}
+
+// Iterate the bins at Chebyshev ring r around bin (b0,b1,b2); calls
+// fn(j, shift) for every generator j in those bins (with periodic image shift
+// counts in units of the box).
+template <typename Fn>
+void for_ring(const Grid& gr, const int b[3], int r, Fn&& fn) {
+    int lo[3], hi[3];
+    for (int k = 0; k < 3; k++) {
+        if (k < gr.dim) { lo[k] = -r; hi[k] = r; } else { lo[k] = 0; hi[k] = 0; }
+    }
+    for (int dx = lo[0]; dx <= hi[0]; dx++)
+        for (int dy = lo[1]; dy <= hi[1]; dy++)
+            for (int dz = lo[2]; dz <= hi[2]; dz++) {
+                int m = std::max(std::abs(dx), std::max(std::abs(dy), std::abs(dz)));
+                if (m != r) continue;
+                int c[3] = {b[0] + dx, b[1] + dy, b[2] + dz};
+                int s[3] = {0, 0, 0};
+                bool skip = false;
+                for (int k = 0; k < gr.dim; k++) {
+                    if (c[k] < 0 || c[k] >= gr.nb[k]) {
+                        if (!gr.periodic) { skip = true; break; }
+                        int w = ((c[k] % gr.nb[k]) + gr.nb[k]) % gr.nb[k];
+                        s[k] = (c[k] - w) / gr.nb[k];
+                        c[k] = w;
+                    }
+                }
+                if (skip) continue;
+                int64_t bb = (int64_t(c[0]) * gr.nb[1] + c[1]) * gr.nb[2] + c[2];
+                for (int32_t q = gr.start[bb]; q < gr.start[bb + 1]; q++) fn(gr.order[q], s);
+            }
+}
+
+// ----------------------------------------------------------------- 2D ----
+struct Poly2 {
+    std::vector<P3> v;        // vertices (z unused)
+    std::vector<int64_t> lab; // label of edge v[k] -> v[k+1]
+    std::vector<int> sh;      // packed shift of that edge's neighbour
+};
+
+inline int pack_shift(const int s[3]) { return (s[0] + 8) | ((s[1] + 8) << 4) | ((s[2] + 8) << 8); }
+inline void unpack_shift(int p, int s[3]) {
+    s[0] = (p & 15) - 8;
+    s[1] = ((p >> 4) & 15) - 8;
+    s[2] = ((p >> 8) & 15) - 8;
+}
+
+void clip2(Poly2& P, P3 m, P3 d, int64_t lab, int sh, double eps) {
+    size_t nv = P.v.size();
+    std::vector<double> h(nv);
+    bool any_out = false;
+    for (size_t k = 0; k < nv; k++) {
+        h[k] = dot(P.v[k] - m, d);
+        if (h[k] > eps) any_out = true;
+    }
+    if (!any_out) return;
+    Poly2 Q;
+    for (size_t k = 0; k < nv; k++) {
+        size_t k1 = (k + 1) % nv;
+        P3 a = P.v[k], b = P.v[k1];
+        bool ain = h[k] <= eps, bin = h[k1] <= eps;
+        if (ain) {
+            Q.v.push_back(a);
+            if (bin) {
+                Q.lab.push_back(P.lab[k]);
+                Q.sh.push_back(P.sh[k]);
+            } else {
+                // leaving: a -> cut point keeps the old label, cut -> next entry is new
+                double t = h[k] / (h[k] - h[k1]);
+                P3 p = a + t * (b - a);
+                if (h[k] >= -eps) {
+                    // a is on the plane: the new edge starts at a itself
+                    Q.lab.push_back(lab);
+                    Q.sh.push_back(sh);
+                } else {
+                    Q.lab.push_back(P.lab[k]);
+                    Q.sh.push_back(P.sh[k]);
+                    Q.v.push_back(p);
+                    Q.lab.push_back(lab);
+                    Q.sh.push_back(sh);
+                }
+            }
+        } else if (bin) {
+            // entering: cut point -> b keeps the old label
+            if (h[k1] >= -eps) continue;  // b on the plane: b itself is the entry point
+            double t = h[k] / (h[k] - h[k1]);
+            P3 p = a + t * (b - a);
+            Q.v.push_back(p);
+            Q.lab.push_back(P.lab[k]);
+            Q.sh.push_back(P.sh[k]);
+        }
+    }
+    P = std::move(Q);
+}
+
+CellOut build_cell2(int64_t i, int64_t n, const double* g, const Grid& gr) {
+    CellOut out;
+    P3 gi{g[i], g[n + i], 0.0};
+    Poly2 P;
+    double L0 = gr.box[0], L1 = gr.box[1];
+    if (!gr.periodic) {
+        P.v = {{0, 0, 0}, {L0, 0, 0}, {L0, L1, 0}, {0, L1, 0}};
+        P.lab = {-3, -2, -4, -1};
+    } else {
+        double hx = 0.5 * L0, hy = 0.5 * L1;
+        P.v = {{gi.x - hx, gi.y - hy, 0}, {gi.x + hx, gi.y - hy, 0}, {gi.x + hx, gi.y + hy, 0}, {gi.x - hx, gi.y + hy, 0}};
+        P.lab = {kInvalid, kInvalid, kInvalid, kInvalid};
+    }
+    int zero3[3] = {0, 0, 0};
+    P.sh.assign(4, pack_shift(zero3));
+    int b[3] = {std::min(std::max(int(std::floor(gi.x / gr.bw[0])), 0), gr.nb[0] - 1),
+                std::min(std::max(int(std::floor(gi.y / gr.bw[1])), 0), gr.nb[1] - 1), 0};
+    double eps = 1e-13 * gr.minbw * gr.minbw;
+    int rmax = std::max(gr.nb[0], gr.nb[1]) + 1;
+    for (int r = 0; r <= rmax; r++) {
+        double r2max = 0;
+        for (auto& v : P.v) r2max = std::max(r2max, dot(v - gi, v - gi));
+        double reach = (r - 1) * gr.minbw;
+        if (r >= 1 && reach > 0 && reach * reach >= 4.0 * r2max) break;
+        for_ring(gr, b, r, [&](int32_t j, const int s[3]) {
+            if (j == i && s[0] == 0 && s[1] == 0) return;
+            P3 gj{g[j] + s[0] * L0, g[n + j] + s[1] * L1, 0.0};
+            P3 d = gj - gi;
+            double dd = dot(d, d);
+            double r2 = 0;
+            for (auto& v : P.v) r2 = std::max(r2, dot(v - gi, v - gi));
+            if (dd >= 4.0 * r2) return;
+            if (j == i) { out.error = 2; return; }
+            P3 m = 0.5 * (gi + gj);
+            clip2(P, m, d, j, pack_shift(s), eps * std::sqrt(dd));
+        });
+    }
+    size_t nv = P.v.size();
+    // polygon area / centroid relative to the generator
+    double A = 0, cx = 0, cy = 0;
+    double per = 0;
+    for (size_t k = 0; k < nv; k++) {
+        P3 a = P.v[k] - gi, c = P.v[(k + 1) % nv] - gi;
+        double cr = a.x * c.y - c.x * a.y;
+        A += cr;
+        cx += (a.x + c.x) * cr;
+        cy += (a.y + c.y) * cr;
+        per += norm(c - a);
+    }
+    A *= 0.5;
+    double Lz = gr.box[2];
+    out.volume = A * Lz;
+    out.centroid = {gi.x + cx / (6 * A), gi.y + cy / (6 * A), 0.5 * Lz};
+    for (size_t k = 0; k < nv; k++) {
+        if (P.lab[k] == kInvalid) { out.error = 1; continue; }
+        P3 a = P.v[k], c = P.v[(k + 1) % nv];
+        double len = norm(c - a);
+        if (len <= 1e-12 * per) continue;
+        FaceOut f;
+        f.nb = P.lab[k];
+        int s[3];
+        unpack_shift(P.sh[k], s);
+        f.sx = s[0]; f.sy = s[1]; f.sz = s[2];
+        f.area = len * Lz;
+        f.centroid = {0.5 * (a.x + c.x), 0.5 * (a.y + c.y), 0.5 * Lz};
+        out.faces.push_back(f);
+    }
+    return out;
+}
+
+// ----------------------------------------------------------------- 3D ----
+struct Poly3 {
+    std::vector<P3> v;
+    std::vector<std::vector<int>> f;  // vertex loops, CCW seen from outside
+    std::vector<int64_t> lab;
+    std::vector<int> sh;
+};
+
+void box3(Poly3& P, P3 lo, P3 hi, bool invalid) {
+    P.v = {{lo.x, lo.y, lo.z}, {hi.x, lo.y, lo.z}, {hi.x, hi.y, lo.z}, {lo.x, hi.y, lo.z},
+           {lo.x, lo.y, hi.z}, {hi.x, lo.y, hi.z}, {hi.x, hi.y, hi.z}, {lo.x, hi.y, hi.z}};
+    P.f = {{0, 3, 2, 1}, {4, 5, 6, 7}, {0, 1, 5, 4}, {2, 3, 7, 6}, {0, 4, 7, 3}, {1, 2, 6, 5}};
+    if (invalid) P.lab = {kInvalid, kInvalid, kInvalid, kInvalid, kInvalid, kInvalid};
+    else P.lab = {-5, -6, -3, -4, -1, -2};
+    int z[3] = {0, 0, 0};
+    P.sh.assign(6, pack_shift(z));
+}
+
+void clip3(Poly3& P, P3 m, P3 d, int64_t lab, int sh, double eps) {
+    size_t nv = P.v.size();
+    std::vector<double> h(nv);
+    bool any_out = false;
+    for (size_t k = 0; k < nv; k++) {
+        h[k] = dot(P.v[k] - m, d);
+        if (h[k] > eps) any_out = true;
+    }
+    if (!any_out) return;
+    std::unordered_map<uint64_t, int> cut;  // edge -> new vertex
+    std::unordered_map<int, int> next;      // on the cut face: entry -> exit chain
+    auto edge_point = [&](int a, int b) -> int {
+        // a inside, b outside (or reversed); returns the vertex on the plane
+        if (h[a] >= -eps && h[a] <= eps) return a;
+        uint64_t key = (uint64_t(std::min(a, b)) << 32) | uint64_t(std::max(a, b));
+        auto it = cut.find(key);
+        if (it != cut.end()) return it->second;
+        double t = h[a] / (h[a] - h[b]);
+        P3 p = P.v[a] + t * (P.v[b] - P.v[a]);
+        int id = int(P.v.size());
+        P.v.push_back(p);
+        cut[key] = id;
+        return id;
+    };
+    std::vector<std::vector<int>> nf;
+    std::vector<int64_t> nl;
+    std::vector<int> ns;
+    for (size_t fi = 0; fi < P.f.size(); fi++) {
+        const auto& F = P.f[fi];
+        size_t m_ = F.size();
+        std::vector<int> G;
+        int exitp = -1, entryp = -1;
+        for (size_t k = 0; k < m_; k++) {
+            int a = F[k], b = F[(k + 1) % m_];
+            bool ain = h[a] <= eps, bin = h[b] <= eps;
+            if (ain) {
+                G.push_back(a);
+                if (!bin) {
+                    int p = edge_point(a, b);
+                    if (p != a) G.push_back(p);
+                    exitp = p;
+                }
+            } else if (bin) {
+                int p = edge_point(b, a);
+                if (p != b) G.push_back(p);
+                entryp = p;
+            }
+        }
+        if (exitp >= 0 && entryp >= 0 && exitp != entryp) next[entryp] = exitp;
+        if (G.size() >= 3) {
+            nf.push_back(G);
+            nl.push_back(P.lab[fi]);
+            ns.push_back(P.sh[fi]);
+        }
+    }
+    // chain the new face: each clipped face contributes exit->entry along its
+    // own boundary; the cut face runs entry -> exit in reverse orientation.
+    if (!next.empty()) {
+        std::vector<int> loop;
+        int start = next.begin()->first;
+        int cur = start;
+        for (size_t guard = 0; guard <= next.size() + 1; guard++) {
+            loop.push_back(cur);
+            auto it = next.find(cur);
+            if (it == next.end()) { loop.clear(); break; }
+            cur = it->second;
+            if (cur == start) break;
+        }
+        if (loop.size() >= 3) {
+            nf.push_back(loop);
+            nl.push_back(lab);
+            ns.push_back(sh);
+        }
+    }
+    // compact vertices
+    std::vector<int> remap(P.v.size(), -1);
+    std::vector<P3> nvv;
+    for (auto& F : nf)
+        for (auto& x : F) {
+            if (remap[x] < 0) { remap[x] = int(nvv.size()); nvv.push_back(P.v[x]); }
+            x = remap[x];
+        }
+    P.v = std::move(nvv);
+    P.f = std::move(nf);
+    P.lab = std::move(nl);
+    P.sh = std::move(ns);
+}
+
+CellOut build_cell3(int64_t i, int64_t n, const double* g, const Grid& gr) {
+    CellOut out;
+    P3 gi{g[i], g[n + i], g[2 * n + i]};
+    Poly3 P;
+    double L[3] = {gr.box[0], gr.box[1], gr.box[2]};
+    if (!gr.periodic) box3(P, {0, 0, 0}, {L[0], L[1], L[2]}, false);
+    else box3(P, gi - P3{0.5 * L[0], 0.5 * L[1], 0.5 * L[2]}, gi + P3{0.5 * L[0], 0.5 * L[1], 0.5 * L[2]}, true);
+    int b[3];
+    for (int k = 0; k < 3; k++) {
+        double c = k == 0 ? gi.x : (k == 1 ? gi.y : gi.z);
+        b[k] = std::min(std::max(int(std::floor(c / gr.bw[k])), 0), gr.nb[k] - 1);
+    }
+    double eps = 1e-13 * gr.minbw * gr.minbw;
+    int rmax = std::max(gr.nb[0], std::max(gr.nb[1], gr.nb[2])) + 1;
+    double r2max = 0;
+    for (auto& v : P.v) r2max = std::max(r2max, dot(v - gi, v - gi));
+    for (int r = 0; r <= rmax; r++) {
+        double reach = (r - 1) * gr.minbw;
+        if (r >= 1 && reach > 0 && reach * reach >= 4.0 * r2max) break;
+        // gather this ring's candidates sorted by distance: nearer planes cut more
+        std::vector<std::pair<double, std::pair<int32_t, int>>> cand;
+        for_ring(gr, b, r, [&](int32_t j, const int s[3]) {
+            if (j == i && s[0] == 0 && s[1] == 0 && s[2] == 0) return;
+            P3 gj{g[j] + s[0] * L[0], g[n + j] + s[1] * L[1], g[2 * n + j] + s[2] * L[2]};
+            P3 d = gj - gi;
+            cand.push_back({dot(d, d), {j, pack_shift(s)}});
+        });
+        std::sort(cand.begin(), cand.end());
+        for (auto& c : cand) {
+            if (c.first >= 4.0 * r2max) break;
+            int32_t j = c.second.first;
+            int s[3];
+            unpack_shift(c.second.second, s);
+            if (j == i) { out.error = 2; continue; }
+            P3 gj{g[j] + s[0] * L[0], g[n + j] + s[1] * L[1], g[2 * n + j] + s[2] * L[2]};
+            P3 d = gj - gi;
+            clip3(P, 0.5 * (gi + gj), d, j, c.second.second, eps * std::sqrt(c.first));
+            r2max = 0;
+            for (auto& v : P.v) r2max = std::max(r2max, dot(v - gi, v - gi));
+        }
+    }
+    // integrals: faces by fan triangulation, volume by tetrahedra from gi
+    double V = 0;
+    P3 C{0, 0, 0};
+    double total_area = 0;
+    std::vector<double> fa(P.f.size());
+    std::vector<P3> fc(P.f.size());
+    for (size_t fi = 0; fi < P.f.size(); fi++) {
+        const auto& F = P.f[fi];
+        P3 a0 = P.v[F[0]] - gi;
+        double A = 0;
+        P3 ac{0, 0, 0};
+        for (size_t k = 1; k + 1 < F.size(); k++) {
+            P3 a1 = P.v[F[k]] - gi, a2 = P.v[F[k + 1]] - gi;
+            P3 cr = cross(a1 - a0, a2 - a0);
+            double ta = 0.5 * norm(cr);
+            A += ta;
+            ac = ac + (ta / 3.0) * (a0 + a1 + a2);
+            double tv = dot(a0, cross(a1, a2)) / 6.0;
+            V += tv;
+            C = C + (tv / 4.0) * (a0 + a1 + a2);
+        }
+        fa[fi] = A;
+        fc[fi] = A > 0 ? gi + (1.0 / A) * ac : gi + a0;
+        total_area += A;
+    }
+    out.volume = V;
+    out.centroid = gi + (1.0 / V) * C;
+    for (size_t fi = 0; fi < P.f.size(); fi++) {
+        if (P.lab[fi] == kInvalid) { out.error = 1; continue; }
+        if (fa[fi] <= 1e-12 * total_area) continue;
+        FaceOut f;
+        f.nb = P.lab[fi];
+        int s[3];
+        unpack_shift(P.sh[fi], s);
+        f.sx = s[0]; f.sy = s[1]; f.sz = s[2];
+        f.area = fa[fi];
+        f.centroid = fc[fi];
+        out.faces.push_back(f);
+    }
+    return out;
+}
+
+struct Built {
+    int64_t n = 0;
+    std::vector<int32_t> left, right, csr_off, csr_face;
+    std::vector<double> area, normal, centroid, shift, volume, cell_centroid;
+};
+
+}  // namespace
+
+extern "C" {
+
+// Builds the mesh.  gen is [3][n]; box[3]; returns 0 on success, writes the
+// face count and an opaque handle.
+int mvmm_voronoi_build(int dim, int64_t n, const double* gen, const double* box, int periodic, int n_threads,
+                       int64_t* n_faces, void** handle) {
+    if (dim != 2 && dim != 3) return -1;
+    if (n <= 0) return -2;
+#ifdef _OPENMP
+    if (n_threads > 0) omp_set_num_threads(n_threads);
+#endif
+    Grid gr = make_grid(dim, n, gen, box, periodic != 0);
+    if (periodic)
+        for (int k = 0; k < dim; k++)
+            if (gr.nb[k] < 3) return -3;  // a cell could neighbour its own image
+    std::vector<CellOut> cells(n);
+    int err = 0;
+#pragma omp parallel for schedule(dynamic, 256) reduction(| : err)
+    for (int64_t i = 0; i < n; i++) {
+        cells[i] = dim == 2 ? build_cell2(i, n, gen, gr) : build_cell3(i, n, gen, gr);
+        err |= cells[i].error;
+    }
+    if (err) return -10 - err;
+    Built* B = new Built();
+    B->n = n;
+    B->volume.resize(n);
+    B->cell_centroid.resize(3 * n);
+    std::vector<std::vector<int32_t>> incid(n);
+    int64_t nf = 0;
+    for (int64_t i = 0; i < n; i++) {
+        B->volume[i] = cells[i].volume;
+        B->cell_centroid[i] = cells[i].centroid.x;
+        B->cell_centroid[n + i] = cells[i].centroid.y;
+        B->cell_centroid[2 * n + i] = cells[i].centroid.z;
+        for (auto& f : cells[i].faces)
+            if (f.nb < 0 || f.nb > i) nf++;
+    }
+    B->left.reserve(nf); B->right.reserve(nf); B->area.reserve(nf);
+    std::vector<P3> nrm, cen, shf;
+    nrm.reserve(nf); cen.reserve(nf); shf.reserve(nf);
+    for (int64_t i = 0; i < n; i++) {
+        P3 gi{gen[i], gen[n + i], gen[2 * n + i]};
+        for (auto& f : cells[i].faces) {
+            if (f.nb >= 0 && f.nb <= i) continue;
+            int32_t idx = int32_t(B->left.size());
+            B->left.push_back(int32_t(i));
+            B->area.push_back(f.area);
+            cen.push_back(f.centroid);
+            incid[i].push_back(idx);
+            if (f.nb >= 0) {
+                int64_t j = f.nb;
+                P3 s{f.sx * box[0], f.sy * box[1], f.sz * box[2]};
+                P3 gj{gen[j] + s.x, gen[n + j] + s.y, gen[2 * n + j] + s.z};
+                P3 d = gj - gi;
+                nrm.push_back((1.0 / norm(d)) * d);
+                shf.push_back(s);
+                B->right.push_back(int32_t(j));
+                incid[j].push_back(idx);
+            } else {
+                P3 nn{0, 0, 0};
+                if (f.nb == -1) nn.x = -1; else if (f.nb == -2) nn.x = 1;
+                else if (f.nb == -3) nn.y = -1; else if (f.nb == -4) nn.y = 1;
+                else if (f.nb == -5) nn.z = -1; else nn.z = 1;
+                nrm.push_back(nn);
+                shf.push_back({0, 0, 0});
+                B->right.push_back(-1);
+            }
+        }
+    }
+    nf = int64_t(B->left.size());
+    B->normal.resize(3 * nf); B->centroid.resize(3 * nf); B->shift.resize(3 * nf);
+    for (int64_t f = 0; f < nf; f++) {
+        B->normal[f] = nrm[f].x; B->normal[nf + f] = nrm[f].y; B->normal[2 * nf + f] = nrm[f].z;
+        B->centroid[f] = cen[f].x; B->centroid[nf + f] = cen[f].y; B->centroid[2 * nf + f] = cen[f].z;
+        B->shift[f] = shf[f].x; B->shift[nf + f] = shf[f].y; B->shift[2 * nf + f] = shf[f].z;
+    }
+    B->csr_off.resize(n + 1);
+    B->csr_off[0] = 0;
+    for (int64_t i = 0; i < n; i++) {
+        std::sort(incid[i].begin(), incid[i].end());
+        B->csr_off[i + 1] = B->csr_off[i] + int32_t(incid[i].size());
+    }
+    B->csr_face.reserve(B->csr_off[n]);
+    for (int64_t i = 0; i < n; i++) B->csr_face.insert(B->csr_face.end(), incid[i].begin(), incid[i].end());
+    *n_faces = nf;
+    *handle = B;
+    return 0;
+}
+
+int mvmm_voronoi_fetch(void* handle, int32_t* left, int32_t* right, double* area, double* normal, double* centroid,
+                       double* shift, int32_t* csr_off, int32_t* csr_face, double* volume, double* cell_centroid) {
+    Built* B = static_cast<Built*>(handle);
+    size_t nf = B->left.size();
+    std::memcpy(left, B->left.data(), nf * 4);
+    std::memcpy(right, B->right.data(), nf * 4);
+    std::memcpy(area, B->area.data(), nf * 8);
+    std::memcpy(normal, B->normal.data(), 3 * nf * 8);
+    std::memcpy(centroid, B->centroid.data(), 3 * nf * 8);
+    std::memcpy(shift, B->shift.data(), 3 * nf * 8);
+    std::memcpy(csr_off, B->csr_off.data(), (B->n + 1) * 4);
+    std::memcpy(csr_face, B->csr_face.data(), B->csr_face.size() * 4);
+    std::memcpy(volume, B->volume.data(), B->n * 8);
+    std::memcpy(cell_centroid, B->cell_centroid.data(), 3 * B->n * 8);
+    return 0;
+}
+
+void mvmm_voronoi_free(void* handle) { delete static_cast<Built*>(handle); }
+
+}  // extern "C"

@@ -1,0 +1,252 @@
+"""ctypes bindings of ``libmvmm_gpu.so`` (the C ABI in ``include/mvmm_gpu.h``).
+
+There is no CPU fallback: if the CUDA library is missing, or no GPU is present,
+every entry point raises.  ``GpuSim`` drives one simulation through the
+reference-shaped API (Engine / Runner / FiniteVolumeSolver); the module-level
+functions expose the RiemannFluxSolver over arrays.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from .layout import Cells
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libmvmm_gpu.so")
+MAX_NR_TIMESTEPS = 1 << 57
+KERNEL_NAMES = ("predict", "face_flux", "update", "gradient_timestep", "limiter", "end")
+
+EXPORTED = (
+    "mvmm_ctx_create", "mvmm_ctx_destroy", "mvmm_ctx_set_stream", "mvmm_upload_cells", "mvmm_download_cells",
+    "mvmm_error_bits", "mvmm_last_error", "mvmm_predict", "mvmm_compute_fluxes",
+    "mvmm_convert_conserved_to_primitive", "mvmm_compute_timesteps", "mvmm_apply_fluxes", "mvmm_gradients",
+    "mvmm_step", "mvmm_run", "mvmm_enqueue_steps", "mvmm_set_time", "mvmm_get_time", "mvmm_profile_enable",
+    "mvmm_profile_read", "mvmm_riemann_flux", "mvmm_riemann_sample",
+)
+
+
+class MvmmError(RuntimeError):
+    def __init__(self, code: int, msg: str, bits: int = 0):
+        super().__init__(f"mvmm error {code}: {msg}" + (f" (bits 0x{bits:x})" if bits else ""))
+        self.code = code
+        self.bits = bits
+
+
+class _Params(ctypes.Structure):
+    _fields_ = [("gamma", ctypes.c_double), ("eos", ctypes.c_int), ("isothermal_internal_energy", ctypes.c_double),
+                ("cfl", ctypes.c_double), ("riemann", ctypes.c_int), ("boundary", ctypes.c_int),
+                ("dimensionality", ctypes.c_int), ("sync_all", ctypes.c_int), ("t_end", ctypes.c_double),
+                ("max_newton_iter", ctypes.c_int), ("precision", ctypes.c_int), ("particle_motion", ctypes.c_int)]
+
+
+_LIB = None
+
+
+def load_library(path: str = LIB_PATH):
+    """Loads the CUDA library; raises if it has not been built."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.exists(path):
+        raise RuntimeError(f"CUDA library not built: {path} (run __graft_entry__.build())")
+    L = ctypes.CDLL(path)
+    vp, i64, u64, dbl, i32 = ctypes.c_void_p, ctypes.c_int64, ctypes.c_uint64, ctypes.c_double, ctypes.c_int
+    pu64, pi64, pi32 = ctypes.POINTER(u64), ctypes.POINTER(i64), ctypes.POINTER(i32)
+    sig = {
+        "mvmm_ctx_create": (i32, [vp, vp, ctypes.POINTER(vp)]),
+        "mvmm_ctx_destroy": (i32, [vp]),
+        "mvmm_ctx_set_stream": (i32, [vp, vp]),
+        "mvmm_upload_cells": (i32, [vp, vp]),
+        "mvmm_download_cells": (i32, [vp, vp]),
+        "mvmm_error_bits": (ctypes.c_uint32, [vp]),
+        "mvmm_last_error": (ctypes.c_char_p, []),
+        "mvmm_predict": (i32, [vp, dbl]),
+        "mvmm_compute_fluxes": (i32, [vp, vp, vp, pi64]),
+        "mvmm_convert_conserved_to_primitive": (i32, [vp, vp]),
+        "mvmm_compute_timesteps": (i32, [vp, vp, vp]),
+        "mvmm_apply_fluxes": (i32, [vp, vp, vp]),
+        "mvmm_gradients": (i32, [vp, vp]),
+        "mvmm_step": (i32, [vp, u64, u64, pu64, pi64]),
+        "mvmm_run": (i32, [vp, i64, pu64, pu64, pi64, pi64, pi32]),
+        "mvmm_enqueue_steps": (i32, [vp, i64]),
+        "mvmm_set_time": (i32, [vp, u64, u64]),
+        "mvmm_get_time": (i32, [vp, pu64, pu64, pi64, pi64, pi32]),
+        "mvmm_profile_enable": (i32, [vp, i32]),
+        "mvmm_profile_read": (i32, [vp, vp, vp]),
+        "mvmm_riemann_flux": (i32, [i32, i32, dbl, i64, vp, vp, vp, vp, vp]),
+        "mvmm_riemann_sample": (i32, [i32, i32, dbl, i64, vp, vp, vp, vp]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _LIB = L
+    return L
+
+
+def _check(rc: int, ctx=None):
+    if rc != 0:
+        L = load_library()
+        bits = int(L.mvmm_error_bits(ctx)) if ctx else 0
+        raise MvmmError(rc, L.mvmm_last_error().decode(), bits)
+
+
+def _soa(a, k):
+    return np.ascontiguousarray(np.asarray(a, dtype=np.float64).reshape(k, -1))
+
+
+def riemann_flux(kind: int, gamma: float, left, right, v_face, normal, precision: int = 0):
+    """RiemannFluxSolver::solve_for_flux over arrays on the GPU."""
+    L = load_library()
+    left, right, v_face, normal = _soa(left, 5), _soa(right, 5), _soa(v_face, 3), _soa(normal, 3)
+    n = left.shape[1]
+    out = np.zeros((5, n))
+    _check(L.mvmm_riemann_flux(kind, precision, gamma, n, left.ctypes.data, right.ctypes.data, v_face.ctypes.data,
+                               normal.ctypes.data, out.ctypes.data))
+    return out
+
+
+def riemann_sample(kind: int, gamma: float, left, right, normal, precision: int = 0):
+    """Half state at x/t = 0 (RiemannStarSolver::sample after the vacuum test) on the GPU."""
+    L = load_library()
+    left, right, normal = _soa(left, 5), _soa(right, 5), _soa(normal, 3)
+    n = left.shape[1]
+    out = np.zeros((5, n))
+    _check(L.mvmm_riemann_sample(kind, precision, gamma, n, left.ctypes.data, right.ctypes.data, normal.ctypes.data,
+                                 out.ctypes.data))
+    return out
+
+
+class GpuSim:
+    """One simulation resident on the GPU (Engine + OptimalOrderRunner + EulerEqnsFvs)."""
+
+    def __init__(self, problem, precision: int | None = None, stream=None):
+        L = load_library()
+        p = problem.params
+        self.problem = problem
+        self.mesh = problem.mesh
+        prec = p.precision if precision is None else precision
+        self._p = _Params(p.gamma, 0, 0.0, p.cfl, p.riemann, p.boundary, p.dimensionality, int(p.sync_all), p.t_end,
+                          p.max_newton_iter, prec, 0)
+        self._mv = self.mesh.cview()
+        h = ctypes.c_void_p(0)
+        _check(L.mvmm_ctx_create(ctypes.byref(self._p), ctypes.byref(self._mv), ctypes.byref(h)))
+        self.h = h
+        if stream is not None:
+            _check(L.mvmm_ctx_set_stream(self.h, ctypes.c_void_p(stream)), self.h)
+        self.cells = problem.cells.copy()
+        self.upload(self.cells)
+        self.ti_current = 0
+        self.ti_old = 0
+        self.steps = 0
+        self.active_faces = 0
+        self.finished = False
+
+    def close(self):
+        if getattr(self, "h", None):
+            load_library().mvmm_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- state ----
+    def upload(self, cells: Cells):
+        cv = cells.cview()
+        _check(load_library().mvmm_upload_cells(self.h, ctypes.byref(cv)), self.h)
+
+    def state(self, out: Cells | None = None) -> Cells:
+        out = self.cells.copy() if out is None else out
+        cv = out.cview()
+        _check(load_library().mvmm_download_cells(self.h, ctypes.byref(cv)), self.h)
+        return out
+
+    def error_bits(self) -> int:
+        return int(load_library().mvmm_error_bits(self.h))
+
+    # ---- Runner::step / Engine::run ----
+    def step(self) -> bool:
+        tn = ctypes.c_uint64(0)
+        nf = ctypes.c_int64(0)
+        _check(load_library().mvmm_step(self.h, self.ti_current, self.ti_old, ctypes.byref(tn), ctypes.byref(nf)),
+               self.h)
+        self.steps += 1
+        self.active_faces += nf.value
+        done = self.ti_current >= MAX_NR_TIMESTEPS
+        self.ti_old, self.ti_current = self.ti_current, tn.value
+        self.finished = done
+        return done
+
+    def run(self, max_steps: int = 0) -> int:
+        tc = ctypes.c_uint64(self.ti_current)
+        to = ctypes.c_uint64(self.ti_old)
+        s = ctypes.c_int64(0)
+        nf = ctypes.c_int64(0)
+        fin = ctypes.c_int(0)
+        _check(load_library().mvmm_run(self.h, max_steps, ctypes.byref(tc), ctypes.byref(to), ctypes.byref(s),
+                                       ctypes.byref(nf), ctypes.byref(fin)), self.h)
+        self.ti_current, self.ti_old = tc.value, to.value
+        self.steps += s.value
+        self.active_faces += nf.value
+        self.finished = bool(fin.value)
+        return s.value
+
+    # ---- asynchronous stepping for timing ----
+    def set_time(self):
+        _check(load_library().mvmm_set_time(self.h, self.ti_current, self.ti_old), self.h)
+
+    def enqueue_steps(self, n: int):
+        _check(load_library().mvmm_enqueue_steps(self.h, n), self.h)
+
+    def sync_time(self):
+        tc, to, st, af, fin = (ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int())
+        _check(load_library().mvmm_get_time(self.h, ctypes.byref(tc), ctypes.byref(to), ctypes.byref(st),
+                                            ctypes.byref(af), ctypes.byref(fin)), self.h)
+        self.ti_current, self.ti_old, self.finished = tc.value, to.value, bool(fin.value)
+        return st.value, af.value
+
+    def profile(self, enable: bool):
+        _check(load_library().mvmm_profile_enable(self.h, int(enable)), self.h)
+
+    def profile_read(self):
+        ms = np.zeros(len(KERNEL_NAMES))
+        n = np.zeros(len(KERNEL_NAMES), dtype=np.int64)
+        _check(load_library().mvmm_profile_read(self.h, ms.ctypes.data, n.ctypes.data), self.h)
+        return dict(zip(KERNEL_NAMES, zip(ms.tolist(), n.tolist())))
+
+    # ---- FiniteVolumeSolver trait, per stage ----
+    def predict(self, dt: float):
+        _check(load_library().mvmm_predict(self.h, dt), self.h)
+
+    def compute_fluxes(self, active):
+        active = np.ascontiguousarray(active, dtype=np.uint8)
+        out = np.zeros((10, self.mesh.n_faces))
+        nf = ctypes.c_int64(0)
+        _check(load_library().mvmm_compute_fluxes(self.h, active.ctypes.data, out.ctypes.data, ctypes.byref(nf)),
+               self.h)
+        return out, nf.value
+
+    def apply_fluxes(self, fluxes, active):
+        active = np.ascontiguousarray(active, dtype=np.uint8)
+        fluxes = np.ascontiguousarray(fluxes, dtype=np.float64)
+        _check(load_library().mvmm_apply_fluxes(self.h, fluxes.ctypes.data, active.ctypes.data), self.h)
+
+    def convert(self, active):
+        active = np.ascontiguousarray(active, dtype=np.uint8)
+        _check(load_library().mvmm_convert_conserved_to_primitive(self.h, active.ctypes.data), self.h)
+
+    def gradients(self, active):
+        active = np.ascontiguousarray(active, dtype=np.uint8)
+        _check(load_library().mvmm_gradients(self.h, active.ctypes.data), self.h)
+
+    def compute_timesteps(self, active):
+        active = np.ascontiguousarray(active, dtype=np.uint8)
+        out = np.zeros(self.mesh.n_cells)
+        _check(load_library().mvmm_compute_timesteps(self.h, active.ctypes.data, out.ctypes.data), self.h)
+        return out

@@ -1,0 +1,209 @@
+"""Initial conditions: seeded synthetic inputs with the reference's shapes.
+
+Follows ``InitialConditions::from_fn`` (``src/initial_conditions.rs:121-186``),
+``Particle::from_ic`` (``src/part.rs:207-217``) and ``Space::first_init_parts``
+/ ``Particle::first_init`` (``src/space.rs:571-594``, ``src/part.rs:200-205``).
+Differences, chosen so that the oracle and the GPU see identical inputs: the
+lattice jitter is symmetric, ``U[-j, j)`` times the spacing, and drawn from a
+seeded numpy generator (the reference's is one-sided and unseeded,
+``initial_conditions.rs:143,167-169``).
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .layout import Cells, Mesh
+from .mesh import mesh_1d, mesh_voronoi
+
+HLLC, EXACT, PVRS = 0, 1, 2
+PERIODIC, REFLECTIVE, OPEN, VACUUM = 0, 1, 2, 3
+SOLVER_NAMES = {"HLLC": HLLC, "Exact": EXACT, "PVRS": PVRS}
+
+
+@dataclass
+class Params:
+    """Run parameters (the reference's hydrodynamics/time_integration/space config)."""
+
+    gamma: float = 5.0 / 3.0
+    cfl: float = 0.3
+    riemann: int = HLLC
+    boundary: int = REFLECTIVE
+    dimensionality: int = 1
+    sync_all: bool = True
+    t_end: float = 0.2
+    precision: int = 0  # 0 = plain FP64, 1 = FP32 faces / FP64 accumulate
+    max_newton_iter: int = 1000
+
+
+@dataclass
+class Problem:
+    name: str
+    params: Params
+    mesh: Mesh
+    cells: Cells
+    extra: dict = field(default_factory=dict)
+
+
+def gas_internal_energy_from_pressure(gamma, p, rho_inv):
+    """gas_law.rs:81-88 (ideal gas)."""
+    return p * rho_inv * (1.0 / (gamma - 1.0))
+
+
+def lattice(box, num_part: int, dim: int, jitter: float, rng):
+    """Generator positions as in from_fn (initial_conditions.rs:133-176)."""
+    box = list(box)
+    if dim < 2:
+        box[1] = 1.0
+    if dim < 3:
+        box[2] = 1.0
+    volume = box[0] * box[1] * box[2]
+    nppul = (num_part / volume) ** (1.0 / dim)
+    npx = int(round(box[0] * nppul))
+    npy = int(round(box[1] * nppul)) if dim > 1 else 1
+    npz = int(round(box[2] * nppul)) if dim > 2 else 1
+    n = npx * npy * npz
+    idx = np.arange(n)
+    i = idx // (npy * npz)
+    j = (idx - i * npy * npz) // npz
+    k = idx - i * npy * npz - j * npz
+    pert = np.zeros((3, n))
+    if jitter:
+        for a in range(dim):
+            pert[a] = jitter * (2.0 * rng.random(n) - 1.0)
+    x = np.empty((3, n))
+    x[0] = (i + 0.5 + pert[0]) / npx * box[0]
+    x[1] = (j + 0.5 + pert[1]) / npy * box[1]
+    x[2] = (k + 0.5 + pert[2]) / npz * box[2]
+    return x, tuple(box), volume / n, (npx, npy, npz)
+
+
+def cells_from_ic(mesh: Mesh, x, mass, vel, u, gamma) -> Cells:
+    """Particle::from_ic + update_geometry + first_init (part.rs:151-217)."""
+    n = mesh.n_cells
+    c = Cells.zeros(n)
+    mass = np.asarray(mass, dtype=np.float64)
+    vel = np.asarray(vel, dtype=np.float64)
+    u = np.asarray(u, dtype=np.float64)
+    c.cons[0] = mass
+    c.cons[1:4] = mass * vel
+    c.cons[4] = mass * u + 0.5 * mass * (vel[0] * vel[0] + vel[1] * vel[1] + vel[2] * vel[2])
+    c.volume[:] = mesh.volume
+    c.centroid[:] = mesh.cell_centroid
+    c.loc[:] = x
+    # State<Primitive>::from_conserved (physical_quantities.rs:213-226)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        m_inv = 1.0 / mass
+        rho = mass / mesh.volume
+        v = c.cons[1:4] * m_inv
+        lsq = c.cons[1] * c.cons[1] + c.cons[2] * c.cons[2] + c.cons[3] * c.cons[3]
+        thermal = c.cons[4] - 0.5 * lsq * m_inv
+        ui = thermal * m_inv
+        p = (gamma - 1.0) * ui * rho
+    pos = mass > 0
+    c.prim[0] = np.where(pos, rho, 0.0)
+    c.prim[1:4] = np.where(pos, v, 0.0)
+    c.prim[4] = np.where(pos, p, 0.0)
+    return c
+
+
+def sod_1d(n: int = 1000, riemann: int = HLLC, t_end: float = 0.2, cfl: float = 0.3) -> Problem:
+    """1D Sod shock tube (bin/main.rs:35-40 preset) on [0,1], reflective."""
+    params = Params(gamma=5.0 / 3.0, cfl=cfl, riemann=riemann, boundary=REFLECTIVE, dimensionality=1,
+                    sync_all=True, t_end=t_end)
+    x, box, vpp, _ = lattice((1.0, 1.0, 1.0), n, 1, 0.0, None)
+    mesh = mesh_1d(x[0], box=box, periodic=False)
+    left = x[0] < 0.5
+    rho = np.where(left, 1.0, 0.125)
+    p = np.where(left, 1.0, 0.1)
+    vel = np.zeros((3, x.shape[1]))
+    u = gas_internal_energy_from_pressure(params.gamma, p, 1.0 / rho)
+    cells = cells_from_ic(mesh, x, rho * vpp, vel, u, params.gamma)
+    return Problem("sod_1d", params, mesh, cells)
+
+
+def riemann_1d(n: int, left_state, right_state, riemann: int, t_end: float, gamma: float = 5.0 / 3.0,
+               cfl: float = 0.3, x0: float = 0.5) -> Problem:
+    """One 1D Riemann problem (rho, v, P) | (rho, v, P) at x0, reflective walls."""
+    params = Params(gamma=gamma, cfl=cfl, riemann=riemann, boundary=REFLECTIVE, dimensionality=1,
+                    sync_all=True, t_end=t_end)
+    x, box, vpp, _ = lattice((1.0, 1.0, 1.0), n, 1, 0.0, None)
+    mesh = mesh_1d(x[0], box=box, periodic=False)
+    lft = x[0] < x0
+    rho = np.where(lft, left_state[0], right_state[0])
+    vx = np.where(lft, left_state[1], right_state[1])
+    p = np.where(lft, left_state[2], right_state[2])
+    vel = np.zeros((3, x.shape[1]))
+    vel[0] = vx
+    u = gas_internal_energy_from_pressure(gamma, p, 1.0 / rho)
+    cells = cells_from_ic(mesh, x, rho * vpp, vel, u, gamma)
+    return Problem("riemann_1d", params, mesh, cells)
+
+
+def kelvin_helmholtz_2d(nx: int = 256, seed: int = 2, riemann: int = EXACT, t_end: float = 1.5,
+                        jitter: float = 0.1, cfl: float = 0.3) -> Problem:
+    """2D shear layer on the periodic unit square (seeded +-jitter lattice)."""
+    params = Params(gamma=5.0 / 3.0, cfl=cfl, riemann=riemann, boundary=PERIODIC, dimensionality=2,
+                    sync_all=True, t_end=t_end)
+    rng = np.random.default_rng(seed)
+    x, box, vpp, _ = lattice((1.0, 1.0, 1.0), nx * nx, 2, jitter, rng)
+    mesh = mesh_voronoi(x, 2, box, True)
+    xn = x[0] / box[0]
+    yn = x[1] / box[1]
+    inner = np.abs(yn - 0.5) < 0.25
+    rho = np.where(inner, 2.0, 1.0)
+    vel = np.zeros_like(x)
+    vel[0] = np.where(inner, 0.5, -0.5)
+    vel[1] = 0.1 * np.sin(4.0 * math.pi * xn)
+    p = np.full(x.shape[1], 2.5)
+    u = gas_internal_energy_from_pressure(params.gamma, p, 1.0 / rho)
+    cells = cells_from_ic(mesh, x, rho * vpp, vel, u, params.gamma)
+    return Problem("kelvin_helmholtz_2d", params, mesh, cells)
+
+
+def point_blast_3d(n1d: int = 128, seed: int = 3, riemann: int = HLLC, t_end: float = 0.05,
+                   jitter: float = 0.1, sync_all: bool = False, cfl: float = 0.3) -> Problem:
+    """3D point blast: E=1 of thermal energy split over cells within 2 spacings of the centre."""
+    params = Params(gamma=5.0 / 3.0, cfl=cfl, riemann=riemann, boundary=PERIODIC, dimensionality=3,
+                    sync_all=sync_all, t_end=t_end)
+    rng = np.random.default_rng(seed)
+    x, box, vpp, _ = lattice((1.0, 1.0, 1.0), n1d ** 3, 3, jitter, rng)
+    mesh = mesh_voronoi(x, 3, box, True)
+    n = x.shape[1]
+    rho = np.ones(n)
+    p = np.full(n, 1e-6)
+    vel = np.zeros((3, n))
+    u = gas_internal_energy_from_pressure(params.gamma, p, 1.0 / rho)
+    mass = rho * vpp
+    r = np.sqrt(((x - 0.5) ** 2).sum(axis=0))
+    hot = r < 2.0 / n1d
+    nh = int(hot.sum())
+    u = np.where(hot, (1.0 / nh) / mass, u)
+    cells = cells_from_ic(mesh, x, mass, vel, u, params.gamma)
+    return Problem("point_blast_3d", params, mesh, cells, extra={"n_hot": nh})
+
+
+def yee_vortex_2d(nx: int, beta: float, v_adv, seed: int = 5, box_len: float = 10.0, t_end: float = 1.0,
+                  riemann: int = HLLC, jitter: float = 0.1, cfl: float = 0.3) -> Problem:
+    """Isentropic (Yee) vortex, python/utils.py:242-256 (T_inf=1, gamma=1.4), advected by v_adv."""
+    gamma = 1.4
+    params = Params(gamma=gamma, cfl=cfl, riemann=riemann, boundary=PERIODIC, dimensionality=2,
+                    sync_all=True, t_end=t_end)
+    rng = np.random.default_rng(seed)
+    x, box, vpp, _ = lattice((box_len, box_len, 1.0), nx * nx, 2, jitter, rng)
+    mesh = mesh_voronoi(x, 2, box, True)
+    c = x[:2] - 0.5 * box_len
+    r2 = (c * c).sum(axis=0)
+    T_inf = 1.0
+    temp = T_inf - (gamma - 1) * beta ** 2 / (8 * gamma * math.pi ** 2) * np.exp(1 - r2)
+    rho = np.power(temp, 1 / (gamma - 1))
+    v_fac = 0.5 * beta / math.pi * np.exp(0.5 * (1 - r2))
+    vel = np.zeros_like(x)
+    vel[0] = -c[1] * v_fac + v_adv[0]
+    vel[1] = c[0] * v_fac + v_adv[1]
+    u = temp / (gamma - 1)
+    mass = rho * (box[0] * box[1] * box[2] / x.shape[1])
+    cells = cells_from_ic(mesh, x, mass, vel, u, gamma)
+    return Problem("yee_vortex_2d", params, mesh, cells, extra={"beta": beta, "v_adv": tuple(v_adv)})

@@ -1,0 +1,177 @@
+/*
+ * mvmm_gpu: GB300 (sm_103a) implementation of mvmm_hydro's per-face
+ * finite-volume update, behind a plain C ABI.
+ *
+ * This header is the drop-in boundary.  Each entry point names the reference
+ * interface it replaces (paths inside the mvmm_hydro source tree).  Every
+ * function returns 0 on success or a negative MVMM_E* code; the text of the
+ * last error is available from mvmm_last_error().  Soft numerical failures
+ * that the reference reports by panicking (a stuck Newton iteration, negative
+ * mass, ...) are returned as MVMM_E_NUMERIC with the bits of mvmm_error_bits().
+ *
+ * Memory: all device memory is owned by the context; callers pass host
+ * pointers (pageable or pinned) and sizes only.  A context is used by one host
+ * thread at a time and orders all its work on one CUDA stream.
+ */
+#ifndef MVMM_GPU_H
+#define MVMM_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- enums ---------------------------------------------------------- */
+/* Riemann solver kind: riemann_solver.rs:28-44 ("HLLC", "Exact", "PVRS"). */
+enum { MVMM_RIEMANN_HLLC = 0, MVMM_RIEMANN_EXACT = 1, MVMM_RIEMANN_PVRS = 2 };
+/* Boundary: space.rs:26-32. */
+enum { MVMM_BOUNDARY_PERIODIC = 0, MVMM_BOUNDARY_REFLECTIVE = 1, MVMM_BOUNDARY_OPEN = 2, MVMM_BOUNDARY_VACUUM = 3 };
+/* Equation of state: gas_law.rs:66-70. */
+enum { MVMM_EOS_IDEAL = 0, MVMM_EOS_ISOTHERMAL = 1 };
+/* Arithmetic form of the face stage. */
+enum {
+    MVMM_PRECISION_FP64 = 0,    /* plain: everything FP64, reference evaluation order */
+    MVMM_PRECISION_FP32FACE = 1 /* reconstruction/Riemann/flux FP32; geometry, Newton,
+                                   conserved, scatter and time integration FP64 */
+};
+/* Particle motion: engine.rs:7-13.  Only FIXED is implemented (the mesh is
+ * rebuilt on the host for the other modes). */
+enum { MVMM_MOTION_FIXED = 0 };
+
+/* ---- status codes / error bits --------------------------------------- */
+enum {
+    MVMM_OK = 0,
+    MVMM_E_INVALID = -1,  /* bad argument / size / state */
+    MVMM_E_CUDA = -2,     /* CUDA runtime error */
+    MVMM_E_NUMERIC = -3,  /* see mvmm_error_bits */
+    MVMM_E_NOMEM = -4,
+    MVMM_E_UNSUPPORTED = -5
+};
+enum {
+    MVMM_ERR_NEWTON_CAP = 1u << 0,    /* exact.rs:272-274 (panic in the reference) */
+    MVMM_ERR_BRENT_BRACKET = 1u << 1, /* exact.rs:132-134 */
+    MVMM_ERR_NEG_MASS = 1u << 2,      /* part.rs:220 */
+    MVMM_ERR_NEG_ENERGY = 1u << 3,    /* part.rs:221-224, 227-231 */
+    MVMM_ERR_NONFINITE = 1u << 4,     /* part.rs:180-182, 249-260 */
+    MVMM_ERR_NEG_PRIM = 1u << 5,      /* part.rs:246-247, physical_quantities.rs:220-221 */
+    MVMM_ERR_ZERO_DTI = 1u << 6,      /* timeline.rs:397 */
+    MVMM_ERR_BOUNDS = 1u << 7         /* a mesh index outside its array (checked on upload) */
+};
+
+/* ---- plain structs ---------------------------------------------------- */
+/* EulerEqnsFvs::new(riemann_solver, cfl, gas_law) (euler_eqns_fvs.rs:13-17)
+ * plus the engine/space settings the per-face update reads. */
+typedef struct mvmm_params {
+    double gamma;                      /* GasLaw::new(gamma, ..) */
+    int eos;                           /* MVMM_EOS_* */
+    double isothermal_internal_energy; /* EquationOfState::Isothermal payload */
+    double cfl;                        /* cfl_criterion */
+    int riemann;                       /* MVMM_RIEMANN_* */
+    int boundary;                      /* MVMM_BOUNDARY_* */
+    int dimensionality;                /* 1, 2, 3 */
+    int sync_all;                      /* time_integration.sync_timesteps */
+    double t_end;                      /* defines time_base = t_end / 2^57 (engine.rs:118) */
+    int max_newton_iter;               /* exact solver cap, 1000 in the reference */
+    int precision;                     /* MVMM_PRECISION_* */
+    int particle_motion;               /* MVMM_MOTION_FIXED */
+} mvmm_params;
+
+/* Cell state, SoA, n cells.  Row layout [components][n]; grad row 3*q+k is
+ * d(quantity q)/d(axis k).  Mirrors Particle (part.rs:10-39). */
+typedef struct mvmm_cells {
+    int64_t n;
+    double *cons, *prim, *grad, *gc, *extrap, *facc;
+    double *volume, *loc, *centroid, *v, *v_rel;
+    double *max_a_over_r, *max_signal_velocity, *dt;
+    int8_t *timebin;
+} mvmm_cells;
+
+/* Face list + cell->face CSR: Vec<VoronoiFace> + voronoi_cell_face_connections
+ * (space.rs:70-81).  right < 0 encodes face.right() == None; shift is zero
+ * where face.shift() is None.  normal/centroid/shift are [3][n_faces]. */
+typedef struct mvmm_mesh {
+    int64_t n_cells, n_faces;
+    const int32_t *left, *right;
+    const double *area, *normal, *centroid, *shift;
+    const int32_t *csr_off, *csr_face; /* [n_cells+1], [csr_off[n_cells]] */
+} mvmm_mesh;
+
+typedef struct mvmm_ctx mvmm_ctx;
+
+/* ---- context ---------------------------------------------------------- */
+/* Builds the solver: replaces `EulerEqnsFvs::<R>::new` (euler_eqns_fvs.rs:13-17)
+ * as constructed in bin/main.rs:625-642, and takes ownership of a device copy
+ * of the mesh produced by Space::initialize (space.rs:88-211). */
+int mvmm_ctx_create(const mvmm_params *params, const mvmm_mesh *mesh, mvmm_ctx **out);
+int mvmm_ctx_destroy(mvmm_ctx *ctx);
+/* Runs all work of this context on the given cudaStream_t (NULL = own stream). */
+int mvmm_ctx_set_stream(mvmm_ctx *ctx, void *cuda_stream);
+/* Host <-> device copies of the whole cell state (the &mut [Particle] the
+ * FiniteVolumeSolver trait passes on every call, finite_volume_solver.rs:9-17). */
+int mvmm_upload_cells(mvmm_ctx *ctx, const mvmm_cells *cells);
+int mvmm_download_cells(mvmm_ctx *ctx, mvmm_cells *cells);
+uint32_t mvmm_error_bits(mvmm_ctx *ctx);
+const char *mvmm_last_error(void);
+
+/* ---- FiniteVolumeSolver trait (finite_volume_solver.rs:9-17) ------------ */
+/* predict(&self, particles, dt)  (euler_eqns_fvs.rs:20-24) */
+int mvmm_predict(mvmm_ctx *ctx, double dt);
+/* compute_fluxes(&self, faces, particles, part_is_active, boundary) -> Vec<FluxInfo>
+ * (euler_eqns_fvs.rs:26-48).  active: host uint8[n]; fluxes_out: host
+ * double[10][n_faces] = (fluxes 5, mflux 3, v_max, a_over_r) (flux.rs:10-21). */
+int mvmm_compute_fluxes(mvmm_ctx *ctx, const uint8_t *active, double *fluxes_out, int64_t *n_active_faces);
+/* convert_conserved_to_primitive(&self, particles, part_is_active) (euler_eqns_fvs.rs:63-69) */
+int mvmm_convert_conserved_to_primitive(mvmm_ctx *ctx, const uint8_t *active);
+/* compute_timesteps(&self, particles, part_is_active, motion, dim) -> Vec<f64>
+ * (euler_eqns_fvs.rs:50-61); dt_out: host double[n] (INFINITY if inactive). */
+int mvmm_compute_timesteps(mvmm_ctx *ctx, const uint8_t *active, double *dt_out);
+
+/* ---- runner free functions (runner/hydrodynamics.rs) ----------------- */
+/* apply_fluxes + kick2 (runner/hydrodynamics.rs:13-39, 51-57); fluxes: host double[10][n_faces]. */
+int mvmm_apply_fluxes(mvmm_ctx *ctx, const double *fluxes, const uint8_t *active);
+/* gradient_estimate + gradient_limit + gradient_apply (runner/hydrodynamics.rs:67-143). */
+int mvmm_gradients(mvmm_ctx *ctx, const uint8_t *active);
+
+/* ---- Runner::step / Engine::run --------------------------------------- */
+/* OptimalOrderRunner::step (runner/hydrodynamics/optimal_order.rs:15-64) at
+ * integer time ti_current with the previous sync point ti_old; returns ti_next
+ * and the number of faces that reached flux_exchange*. */
+int mvmm_step(mvmm_ctx *ctx, uint64_t ti_current, uint64_t ti_old, uint64_t *ti_next, int64_t *n_active_faces);
+/* Engine::run (engine.rs:152-199) from the given sync point, device resident:
+ * runs at most max_steps steps (<= 0: to t_end).  On return *ti_current /
+ * *ti_old are the next sync point; *steps_done and *n_active_faces count the
+ * work done; *finished is 1 once the step at t_end has run. */
+int mvmm_run(mvmm_ctx *ctx, int64_t max_steps, uint64_t *ti_current, uint64_t *ti_old, int64_t *steps_done,
+             int64_t *n_active_faces, int *finished);
+/* Enqueues n steps on the context stream without synchronising (for timing
+ * with events recorded on the same stream); state advances on the device. */
+int mvmm_enqueue_steps(mvmm_ctx *ctx, int64_t n_steps);
+/* Sets the device timeline to (ti_current, ti_old) before mvmm_enqueue_steps. */
+int mvmm_set_time(mvmm_ctx *ctx, uint64_t ti_current, uint64_t ti_old);
+/* Reads the device timeline and counters (synchronises the stream). */
+int mvmm_get_time(mvmm_ctx *ctx, uint64_t *ti_current, uint64_t *ti_old, int64_t *steps, int64_t *active_faces,
+                  int *finished);
+/* Per-kernel timing of the step (events around each kernel on the context
+ * stream): enable, then read the accumulated milliseconds and launch counts
+ * of the MVMM_NUM_KERNELS kernels in the order predict, face_flux, update,
+ * gradient_timestep, limiter, end. */
+#define MVMM_NUM_KERNELS 6
+int mvmm_profile_enable(mvmm_ctx *ctx, int enable);
+int mvmm_profile_read(mvmm_ctx *ctx, double *ms, int64_t *launches);
+
+/* ---- RiemannFluxSolver (riemann_solver.rs:78-87) ---------------------- */
+/* solve_for_flux over arrays: left/right [5][n] primitive states, v_face and
+ * normal [3][n], out [5][n]; host pointers.  precision selects the FP64 or
+ * FP32 arithmetic form. */
+int mvmm_riemann_flux(int kind, int precision, double gamma, int64_t n, const double *left, const double *right,
+                      const double *v_face, const double *normal, double *out);
+/* RiemannStarSolver::sample preceded by the vacuum test of the blanket
+ * solve_for_flux (riemann_solver.rs:224-287): half state at x/t = 0. */
+int mvmm_riemann_sample(int kind, int precision, double gamma, int64_t n, const double *left, const double *right,
+                        const double *normal, double *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,116 @@
+/*
+ * CPU oracle for the mvmm_hydro per-face finite-volume update.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker: tests, the smoke
+ * check and the CPU-baseline leg of the benchmark call it to produce the
+ * reference answer.  The GPU product never links, loads or calls it.
+ *
+ * It restates, in plain C with FP contraction disabled, the reference's CPU
+ * path (mvmm_hydro, Rust):  OptimalOrderRunner::step and everything it calls.
+ * Every function cites the reference file:line it follows.  Data is kept as an
+ * array of Particle structs exactly like the reference; the host API below
+ * converts from / to the SoA layout shared with the GPU library.
+ */
+#ifndef MVMM_ORACLE_H
+#define MVMM_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Riemann solver kinds (riemann_solver.rs:28-44). */
+enum { ORC_HLLC = 0, ORC_EXACT = 1, ORC_PVRS = 2 };
+/* Boundary (space.rs:26-32). */
+enum { ORC_PERIODIC = 0, ORC_REFLECTIVE = 1, ORC_OPEN = 2, ORC_VACUUM = 3 };
+/* Equation of state (gas_law.rs:66-70). */
+enum { ORC_EOS_IDEAL = 0, ORC_EOS_ISOTHERMAL = 1 };
+
+/* Error bits, set where the reference panics / asserts. */
+enum {
+    ORC_ERR_NEWTON_CAP = 1u << 0,    /* exact.rs:272-274 */
+    ORC_ERR_BRENT_BRACKET = 1u << 1, /* exact.rs:132-134 */
+    ORC_ERR_NEG_MASS = 1u << 2,      /* part.rs:220 */
+    ORC_ERR_NEG_ENERGY = 1u << 3,    /* part.rs:221-224 */
+    ORC_ERR_NONFINITE = 1u << 4,     /* part.rs:180-182, 249-260 */
+    ORC_ERR_NEG_PRIM = 1u << 5,      /* part.rs:246-247 */
+    ORC_ERR_ZERO_DTI = 1u << 6,      /* timeline.rs:397 */
+    ORC_ERR_MOTION = 1u << 7         /* unsupported particle motion */
+};
+
+typedef struct orc_params {
+    double gamma;
+    int eos;
+    double isothermal_internal_energy;
+    double cfl;
+    int riemann;
+    int boundary;
+    int dimensionality;
+    int sync_all;
+    double t_end;
+    int max_newton_iter; /* 1000 in the reference (exact.rs:272) */
+    int n_threads;       /* OpenMP threads (0 = runtime default) */
+} orc_params;
+
+/* SoA views; identical field meaning to the GPU library's mvmm_cells /
+ * mvmm_mesh.  grad is [15][n] with row 3*q+k = d(quantity q)/d(axis k). */
+typedef struct orc_cells {
+    int64_t n;
+    double *cons, *prim, *grad, *gc, *extrap, *facc;
+    double *volume, *loc, *centroid, *v, *v_rel;
+    double *max_a_over_r, *max_signal_velocity, *dt;
+    int8_t *timebin;
+} orc_cells;
+
+typedef struct orc_mesh {
+    int64_t n_cells, n_faces;
+    const int32_t *left, *right; /* right < 0: boundary face */
+    const double *area, *normal, *centroid, *shift; /* [F], [3][F] ... */
+    const int32_t *csr_off, *csr_face;
+} orc_mesh;
+
+typedef struct orc_ctx orc_ctx;
+
+orc_ctx *orc_create(const orc_params *p, const orc_mesh *m);
+void orc_destroy(orc_ctx *c);
+void orc_set_cells(orc_ctx *c, const orc_cells *in);
+void orc_get_cells(const orc_ctx *c, orc_cells *out);
+uint32_t orc_error(const orc_ctx *c);
+
+/* One OptimalOrderRunner::step; returns ti_next. *n_active_faces gets the
+ * number of faces that reached flux_exchange*. */
+uint64_t orc_step(orc_ctx *c, uint64_t ti_current, uint64_t ti_old, int64_t *n_active_faces);
+/* Engine::run with a Step sync point per step (engine.rs:152-199).  Runs at
+ * most max_steps steps (<=0: unbounded); returns the number of steps run. */
+int64_t orc_run(orc_ctx *c, int64_t max_steps, uint64_t *ti_current, uint64_t *ti_old,
+                int64_t *n_active_faces);
+
+/* Per-stage entry points (FiniteVolumeSolver trait + runner free functions). */
+void orc_predict(orc_ctx *c, double dt);
+/* fluxes: [10][F] SoA (5 fluxes, 3 mflux, v_max, a_over_r) */
+int64_t orc_compute_fluxes(orc_ctx *c, const uint8_t *active, double *fluxes);
+void orc_apply_fluxes(orc_ctx *c, const double *fluxes, const uint8_t *active);
+void orc_convert_conserved_to_primitive(orc_ctx *c, const uint8_t *active);
+void orc_gradients(orc_ctx *c, const uint8_t *active);
+void orc_compute_timesteps(orc_ctx *c, const uint8_t *active, double *dt_out);
+
+/* Riemann solver over arrays; states are [5][n] SoA primitive vectors,
+ * v_face and normal [3][n], output [5][n] conserved flux. */
+void orc_riemann_flux(int kind, double gamma, int64_t n, const double *left, const double *right,
+                      const double *v_face, const double *normal, double *out, uint32_t *err);
+/* Half state sampled at x/t = 0 (RiemannStarSolver::sample, vacuum-aware as
+ * in the blanket solve_for_flux); output [5][n] primitive. */
+void orc_riemann_sample(int kind, double gamma, int64_t n, const double *left, const double *right,
+                        const double *normal, double *out, uint32_t *err);
+/* Timeline helpers (timeline.rs). */
+uint64_t orc_get_integer_timestep(int bin);
+int orc_get_time_bin(uint64_t dti);
+int orc_get_max_active_bin(uint64_t ti);
+uint64_t orc_make_integer_timestep(double dt, int old_bin, int min_ngb_bin, uint64_t ti_current,
+                                   double time_base_inv, uint32_t *err);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
