@@ -27,6 +27,7 @@ CU_SOURCES = {
     "step_fp64.cu": ["-fmad=false"],
     "step_fp32.cu": ["-fmad=true"],
     "mvmm_api.cu": [],
+    "noalloc.cu": ["-fmad=false"],
 }
 HEADERS = ["mvmm_device.cuh", "mvmm_internal.h"]
 

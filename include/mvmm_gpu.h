@@ -171,6 +171,34 @@ int mvmm_riemann_flux(int kind, int precision, double gamma, int64_t n, const do
 int mvmm_riemann_sample(int kind, int precision, double gamma, int64_t n, const double *left, const double *right,
                         const double *normal, double *out);
 
+/* ---- allocation-free variant ------------------------------------------ */
+/* No counterpart in the reference.  For callers that cannot call cudaMalloc:
+ * a host that owns the device memory budget and hands out slices of it, code
+ * running while its own CUDA graph is captured, or code that must avoid the
+ * implicit device synchronisation of cudaMalloc/cudaFree.  Runs the flux
+ * exchange and scatter of one step (mvmm_compute_fluxes, then
+ * mvmm_apply_fluxes with kick2, then mvmm_convert_conserved_to_primitive for
+ * the active cells) in the plain FP64 form on DEVICE arrays owned by the
+ * caller: device_mesh and device_cells hold device pointers with the layouts
+ * documented above, device_active is a device uint8[n] mask, device_err a
+ * device uint32 the call ORs MVMM_ERR_* bits into (the caller clears it; may be
+ * NULL).  The cell state is updated in place.  Asynchronous on cuda_stream.
+ *
+ * The per-face intermediate results live in one static device array of
+ * MVMM_NOALLOC_MAX_FACES faces (7 doubles each, 3.5 MiB) that every GPU which
+ * loads this library keeps until the process exits.  Meshes with more faces
+ * are rejected with MVMM_E_INVALID.  The array is shared by all calls and
+ * keeps the last call's contents; each call overwrites every entry it reads,
+ * so nothing needs clearing, but calls that overlap on the GPU (different
+ * streams or threads) race on it and must be serialised by the caller.  The
+ * first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture.  No cudaMalloc, cudaFree or allocating library
+ * routine is called. */
+#define MVMM_NOALLOC_MAX_FACES 65536
+int mvmm_flux_update_noalloc(const mvmm_params *params, const mvmm_mesh *device_mesh, mvmm_cells *device_cells,
+                             const uint8_t *device_active, uint32_t *device_err, void *cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif
