@@ -54,11 +54,11 @@ def _peaks():
         return 6800.0, "fallback"
 
 
-def _problem():
+def _problem(nx=NX):
     from hydro_rs_gb300 import ics
 
     t0 = time.perf_counter()
-    p = ics.kelvin_helmholtz_2d(NX, seed=2, riemann=ics.EXACT, t_end=1.5)
+    p = ics.kelvin_helmholtz_2d(nx, seed=2, riemann=ics.EXACT, t_end=1.5)
     return p, time.perf_counter() - t0
 
 
@@ -171,7 +171,7 @@ def run_ours(args):
         import torch.distributed as dist
 
         dist.init_process_group("nccl")
-    problem, mesh_s = _problem()
+    problem, mesh_s = _problem(args.nx)
     nf, nc = problem.mesh.n_faces, problem.mesh.n_cells
     stream = torch.cuda.Stream()
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
@@ -262,13 +262,14 @@ def run_ours(args):
                 "peak_kind": peak_kind, "note": "of measured" if peak_kind == "measured" else "of fallback",
                 "step_kernel_ms": {k: round(v[0] / max(v[1], 1), 4) for k, v in prof[prec].items()}}
 
-    cpu = _cpu_sample(problem) if ws == 1 else None
+    cpu = _cpu_sample(problem) if (ws == 1 and not args.no_cpu) else None
     value = faces32 / (ms32 * 1e-3)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms32 / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32-face/f64-accumulate", "data": "synthetic (seeded jittered lattice, shear-layer ICs)",
-        "config": {"workload": WORKLOAD, "cells": nc, "faces": nf, "precision": "fp32_face",
+        "config": {"workload": WORKLOAD if args.nx == NX else WORKLOAD.replace("256x256", f"{args.nx}x{args.nx}"),
+                   "cells": nc, "faces": nf, "precision": "fp32_face",
                    "l2": "flushed (256 MB write) before each timed step", "parallelism": f"replicas x{ws}",
                    "mesh_build_s": round(mesh_s, 3)},
         "l1_density_err_vs_fp64": l1, "l1_same_time": same_time,
@@ -322,6 +323,8 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--nx", type=int, default=NX, help="lattice side (profiling captures of other sizes)")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg (profiling runs)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":

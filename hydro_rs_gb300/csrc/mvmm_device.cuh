@@ -88,12 +88,60 @@ __device__ __forceinline__ St<T> operator*(T s, const St<T>& a) {
     return r;
 }
 
+// ------------------------------------------------- rational powers --
+// For gamma = m/(m-2) (m integer: 5/3 -> 5, 7/5 -> 7) every exponent the
+// Riemann solvers raise to is k/m for an integer k: gm1d2g = 1/m,
+// tdgm1 = m-2, gamma*tdgm1 = m, 1/gamma = (m-2)/m.  GB300 runs FP64 at a small
+// fraction of its FP32 rate, so instead of a general double pow() these powers
+// are built from y = x^(-1/m), computed by range reduction (x = 2^(q m + r) f),
+// an FP32 seed and two division-free Newton steps y <- y + y (1 - x y^m) / m
+// (quadratic convergence: ~1e-7 -> ~1e-14 -> rounding), plus integer powers by
+// repeated squaring.  Accuracy is a few ulp, the same class as pow() itself.
+
+// x^k for a small integer k >= 0 by repeated squaring
+template <typename T>
+__device__ __forceinline__ T ipow(T x, int k) {
+    T r = T(1);
+    T b = x;
+    while (k) {
+        if (k & 1) r = r * b;
+        k >>= 1;
+        if (k) b = b * b;
+    }
+    return r;
+}
+
+// y = x^(-1/m), r = x^(1/m) for finite normal x > 0; false otherwise.
+__device__ __forceinline__ bool rat_root(double x, int m, double inv_m, double& y, double& r) {
+    long long bits = __double_as_longlong(x);
+    int ex = (int)((bits >> 52) & 0x7ff);
+    if (!(x > 0.0) || ex == 0 || ex == 0x7ff) return false;
+    int e = ex - 1023;
+    int q = e >= 0 ? e / m : -((-e + m - 1) / m);  // floor(e / m)
+    int rr = e - q * m;                             // 0 <= rr < m
+    double xr = __longlong_as_double((bits & 0x000fffffffffffffLL) | ((long long)(rr + 1023) << 52));
+    double yy = (double)exp2f(-log2f((float)xr) * (float)inv_m);
+#pragma unroll
+    for (int it = 0; it < 2; it++) {
+        double t = fma(-xr, ipow(yy, m), 1.0);
+        yy = fma(yy * inv_m, t, yy);
+    }
+    double rs = xr * ipow(yy, m - 1);  // xr^(1/m) = 1/yy; one reciprocal Newton step
+    rs = fma(rs, fma(-rs, yy, 1.0), rs);  // removes the rounding of the power chain
+    y = yy * __longlong_as_double((long long)(1023 - q) << 52);
+    r = rs * __longlong_as_double((long long)(1023 + q) << 52);
+    return true;
+}
+__device__ __forceinline__ float rat_root_f(float x, int m) { return powf(x, 1.0f / (float)m); }
+
 // ------------------------------------------------------------- gas law --
 // AdiabaticIndex + GasLaw (gas_law.rs:1-106).
 template <typename T>
 struct Gas {
     T gamma, gamma_inv, odgm1_, odgp1_, iso_u;
     int eos;  // 0 ideal, 1 isothermal
+    int rm;   // m when gamma == m/(m-2) for an integer m in [3, 15], else 0
+    double inv_m;
     __device__ __forceinline__ T gp1dg() const { return (gamma + T(1)) * gamma_inv; }
     __device__ __forceinline__ T gm1d2g() const { return T(0.5) * (gamma - T(1)) * gamma_inv; }
     __device__ __forceinline__ T gm1dgp1() const { return (gamma - T(1)) * odgp1_; }
@@ -109,7 +157,54 @@ struct Gas {
     __device__ __forceinline__ T sound_speed(T p, T rho_inv) const {
         return eos == 0 ? m_sqrt(gamma * p * rho_inv) : m_sqrt(iso_u * gamma * (gamma - T(1)));
     }
+    // x^gm1d2g, x^-gm1d2g, x^tdgm1, x^(gamma*tdgm1), x^(1/gamma)
+    __device__ __forceinline__ T pow_e1(T x) const;
+    __device__ __forceinline__ T pow_me1(T x) const;
+    __device__ __forceinline__ T pow_tdgm1(T x) const {
+        if (rm && x > T(0)) return ipow(x, rm - 2);
+        return m_pow(x, tdgm1());
+    }
+    __device__ __forceinline__ T pow_gtdgm1(T x) const {
+        if (rm && x > T(0)) return ipow(x, rm);
+        return m_pow(x, gamma * tdgm1());
+    }
+    __device__ __forceinline__ T pow_ginv(T x) const;
 };
+template <>
+__device__ __forceinline__ double Gas<double>::pow_e1(double x) const {
+    double y, r;
+    if (rm && rat_root(x, rm, inv_m, y, r)) return r;
+    return pow(x, gm1d2g());
+}
+template <>
+__device__ __forceinline__ double Gas<double>::pow_me1(double x) const {
+    double y, r;
+    if (rm && rat_root(x, rm, inv_m, y, r)) return y;
+    return pow(x, -gm1d2g());
+}
+template <>
+__device__ __forceinline__ double Gas<double>::pow_ginv(double x) const {
+    double y, r;
+    if (rm && rat_root(x, rm, inv_m, y, r)) return ipow(r, rm - 2);
+    return pow(x, 1. / gamma);
+}
+template <>
+__device__ __forceinline__ float Gas<float>::pow_e1(float x) const { return powf(x, gm1d2g()); }
+template <>
+__device__ __forceinline__ float Gas<float>::pow_me1(float x) const { return powf(x, -gm1d2g()); }
+template <>
+__device__ __forceinline__ float Gas<float>::pow_ginv(float x) const { return powf(x, 1.0f / gamma); }
+
+// m with gamma == m/(m-2) to within 4 ulp (3 <= m <= 15), else 0
+__host__ __device__ inline int rational_gamma(double gamma) {
+    if (!(gamma > 1.0) || !(gamma < 4.0)) return 0;
+    double mm = 2.0 * gamma / (gamma - 1.0);
+    int m = (int)(mm + 0.5);
+    if (m < 3 || m > 15) return 0;
+    double g = (double)m / (double)(m - 2);
+    double d = g > gamma ? g - gamma : gamma - g;
+    return d <= 4.0 * 2.220446049250313e-16 * gamma ? m : 0;
+}
 template <typename T>
 __host__ __device__ inline Gas<T> make_gas(double gamma, int eos, double iso_u) {
     // AdiabaticIndex::from (gas_law.rs:9-18), constants evaluated in double
@@ -120,6 +215,8 @@ __host__ __device__ inline Gas<T> make_gas(double gamma, int eos, double iso_u) 
     g.odgp1_ = T(1. / (gamma + 1.));
     g.iso_u = T(iso_u);
     g.eos = eos;
+    g.rm = rational_gamma(gamma);
+    g.inv_m = g.rm ? 1.0 / g.rm : 0.0;
     return g;
 }
 
@@ -166,13 +263,13 @@ __device__ __forceinline__ T shock_speed(T v, T a, T pdps, const Gas<T>& g) {
 }
 template <typename T>
 __device__ __forceinline__ T rarefaction_tail_speed(T u, T a, T pdps, const Gas<T>& g) {
-    return u - a * m_pow(pdps, g.gm1d2g());
+    return u - a * g.pow_e1(pdps);
 }
 template <typename T>
 __device__ __noinline__ St<T> sample_rarefaction_fan(St<T> s, T a, T v, V3<T> n, Gas<T> g) {
     T v_half = g.tdgp1() * (a + T(0.5) * (g.gamma - T(1)) * v);
     T base = g.tdgp1() + g.gm1dgp1() / a * v;
-    return st(s.q[0] * m_pow(base, g.tdgm1()), vel(s) + (v_half - v) * n, s.q[4] * m_pow(base, g.gamma * g.tdgm1()));
+    return st(s.q[0] * g.pow_tdgm1(base), vel(s) + (v_half - v) * n, s.q[4] * g.pow_gtdgm1(base));
 }
 template <typename T>
 __device__ __forceinline__ St<T> sample_middle(T rho, T u, T p, const St<T>& s, T v, V3<T> n) {
@@ -265,7 +362,7 @@ __device__ __forceinline__ double ex_fb(double p, const ExSide& s, const Gas<dou
         double cap_b = g.gm1dgp1() * s.p;
         return (p - s.p) * sqrt(cap_a / (p + cap_b));
     }
-    return g.tdgm1() * s.a * (pow(p / s.p, g.gm1d2g()) - 1.);
+    return g.tdgm1() * s.a * (g.pow_e1(p / s.p) - 1.);
 }
 __device__ __forceinline__ double ex_f(double p, const ExSide& l, const ExSide& r, double vl, double vr,
                                        const Gas<double>& g) {  // :23-34
@@ -277,7 +374,7 @@ __device__ __forceinline__ double ex_fprimeb(double p, const ExSide& s, const Ga
         double cap_b = g.gm1dgp1() * s.p;
         return (1. - 0.5 * (p - s.p) / (cap_b + p)) * sqrt(cap_a / (p + cap_b));
     }
-    return 1. / s.rho / s.a * pow(p / s.p, -g.gm1d2g());
+    return 1. / s.rho / s.a * g.pow_me1(p / s.p);
 }
 __device__ __forceinline__ double ex_gb(double p, const ExSide& s, const Gas<double>& g) {  // :60-64
     double cap_a = g.tdgp1() / s.rho;
@@ -295,8 +392,8 @@ static __device__ __noinline__ double ex_guess_p(ExSide l, ExSide r, double vl, 
         p_guess = ppv;
     } else if (ppv < p_min) {
         double base = (l.a + r.a - 0.5 * (g.gamma - 1.) * (vr - vl)) /
-                      (l.a / pow(l.p, g.gm1d2g()) + r.a / pow(r.p, g.gm1d2g()));
-        p_guess = pow(base, g.gamma * g.tdgm1());
+                      (l.a / g.pow_e1(l.p) + r.a / g.pow_e1(r.p));
+        p_guess = g.pow_gtdgm1(base);
     } else {
         p_guess = (ex_gb(ppv, l, g) * l.p + ex_gb(ppv, r, g) * r.p - vr + vl) / (ex_gb(ppv, l, g) + ex_gb(ppv, r, g));
     }
@@ -349,7 +446,7 @@ static __device__ __noinline__ double ex_brent(double lower, double upper, doubl
 __device__ __forceinline__ double ex_middle_density(double p, const ExSide& s, const Gas<double>& g) {  // :193-212
     double pdps = p / s.p;
     if (pdps > 1.) return s.rho * (pdps + g.gm1dgp1()) / (g.gm1dgp1() * pdps + 1.);
-    return s.rho * pow(pdps, 1. / g.gamma);
+    return s.rho * g.pow_ginv(pdps);
 }
 // ExactRiemannSolver::solve_for_star_state (exact.rs:241-291)
 static __device__ __noinline__ Star<double> ex_star(ExSide l, ExSide r, double vl, double vr, Gas<double> g, int max_iter,
@@ -386,6 +483,155 @@ static __device__ __noinline__ Star<double> ex_star(ExSide l, ExSide r, double v
     return s;
 }
 
+// Exact star state for the FP32-face form: the same iteration as ex_star
+// (guess_p, Newton while f < 0, else Brent, relative tolerance 1e-6, FP64),
+// evaluated with algebraically equal but cheaper expressions: per-side
+// constants hoisted out of the loop, one m-th root per pressure (shared by
+// both sides: (p/p_s)^(1/m) = p^(1/m) p_s^(-1/m)), rsqrt for the shock branch
+// and a single division in Brent's inverse quadratic interpolation.  Used
+// only when gamma = m/(m-2) (Gas::rm != 0).
+struct ExFast {
+    double rho, p, a, sqA, B, c_rar, ps_rm, ps_r, k_fp;
+};
+__device__ __forceinline__ ExFast ex_fast_side(const ExSide& s, const Gas<double>& g) {
+    ExFast e;
+    e.rho = s.rho;
+    e.p = s.p;
+    e.a = s.a;
+    e.sqA = sqrt(g.tdgp1() / s.rho);
+    e.B = g.gm1dgp1() * s.p;
+    e.c_rar = g.tdgm1() * s.a;
+    double y, r;
+    if (!rat_root(s.p, g.rm, g.inv_m, y, r)) {
+        y = pow(s.p, -g.inv_m);
+        r = pow(s.p, g.inv_m);
+    }
+    e.ps_rm = y;
+    e.ps_r = r;
+    e.k_fp = 1. / (s.rho * s.a);
+    return e;
+}
+struct PRoot {
+    double y, r;  // p^(-1/m), p^(1/m)
+};
+__device__ __forceinline__ PRoot proot(double p, const Gas<double>& g) {
+    PRoot q;
+    if (!rat_root(p, g.rm, g.inv_m, q.y, q.r)) {
+        q.y = pow(p, -g.inv_m);
+        q.r = pow(p, g.inv_m);
+    }
+    return q;
+}
+__device__ __forceinline__ double exf_fb(double p, const ExFast& s, const PRoot& q) {
+    if (p > s.p) return (p - s.p) * s.sqA * rsqrt(p + s.B);
+    return s.c_rar * (q.r * s.ps_rm - 1.);
+}
+__device__ __forceinline__ double exf_fpb(double p, const ExFast& s, const PRoot& q) {
+    if (p > s.p) {
+        double w = rsqrt(p + s.B);
+        return s.sqA * w * (1. - 0.5 * (p - s.p) * (w * w));
+    }
+    return s.k_fp * s.ps_r * q.y;
+}
+__device__ __forceinline__ double exf_f(double p, const ExFast& l, const ExFast& r, double dv, const Gas<double>& g) {
+    PRoot q{0., 0.};
+    if (p <= l.p || p <= r.p) q = proot(p, g);
+    return exf_fb(p, l, q) + exf_fb(p, r, q) + dv;
+}
+static __device__ __noinline__ Star<double> ex_star_fast(ExSide L, ExSide R, double vl, double vr, Gas<double> g,
+                                                        int max_iter, unsigned int* err) {
+    ExFast l = ex_fast_side(L, g), r = ex_fast_side(R, g);
+    double dv = vr - vl;
+    // guess_p (exact.rs:70-103)
+    double p_min = fmin(l.p, r.p), p_max = fmax(l.p, r.p);
+    double ppv = 0.5 * (l.p + r.p) - 0.125 * dv * (l.rho + r.rho) * (l.a + r.a);
+    ppv = fmax(ppv, 1e-8);
+    double p_guess;
+    if (p_max <= 2. * p_min && p_min <= ppv && ppv <= p_max) {
+        p_guess = ppv;
+    } else if (ppv < p_min) {
+        double base = (l.a + r.a - 0.5 * (g.gamma - 1.) * dv) / (l.a * l.ps_rm + r.a * r.ps_rm);
+        p_guess = base > 0. ? ipow(base, g.rm) : pow(base, g.gamma * g.tdgm1());
+    } else {
+        double gl = l.sqA * rsqrt(ppv + l.B), gr = r.sqA * rsqrt(ppv + r.B);
+        p_guess = (gl * l.p + gr * r.p - dv) / (gl + gr);
+    }
+    p_guess = fmax(p_guess, 1e-8);
+    double p = 0.;
+    double fp = exf_f(p, l, r, dv, g);
+    double fpg = exf_f(p_guess, l, r, dv, g);
+    if (fp * fpg >= 0.) {
+        int counter = 0;
+        while (fabs(p - p_guess) > 5e-7 * (p + p_guess) && fpg < 0.0) {
+            p = p_guess;
+            PRoot q{0., 0.};
+            if (p_guess <= l.p || p_guess <= r.p) q = proot(p_guess, g);
+            double fpr = exf_fpb(p_guess, l, q) + exf_fpb(p_guess, r, q);
+            p_guess = p_guess - fpg / fpr;
+            fpg = exf_f(p_guess, l, r, dv, g);
+            if (++counter > max_iter) {
+                *err |= 1u;
+                break;
+            }
+        }
+    }
+    if (fabs(p - p_guess) > 5e-7 * (p + p_guess) && fpg > 0.) {
+        // Brent's method on [0, p_guess] (exact.rs:106-191)
+        double a = 0., b = p_guess, c, d = INFINITY, fa = exf_f(0., l, r, dv, g), fb = fpg, fc, s, fs, t;
+        const double tol = 1e-6;
+        if (fa * fb > 0.) {
+            *err |= 2u;
+        } else {
+            if (fabs(fa) < fabs(fb)) { t = a; a = b; b = t; t = fa; fa = fb; fb = t; }
+            c = a;
+            fc = fa;
+            bool mflag = true;
+            int it = 0;
+            while (fb != 0. && fabs(a - b) > tol * 0.5 * (a + b)) {
+                if (++it > 100 * max_iter) {
+                    *err |= 1u;
+                    break;
+                }
+                if (fa != fc && fb != fc) {
+                    double dab = fa - fb, dac = fa - fc, dbc = fb - fc;
+                    s = (a * fb * fc * dbc - b * fa * fc * dac + c * fa * fb * dab) / (dab * dac * dbc);
+                } else {
+                    s = b - fb * (b - a) / (fb - fa);
+                }
+                double tmp = 0.25 * (3. * a + b);
+                if (!((s > tmp && s < b) || (s < tmp && s > b)) || (mflag && fabs(s - b) >= (0.5 * fabs(b - c))) ||
+                    (!mflag && fabs(s - b) >= (0.5 * fabs(c - d))) || (mflag && fabs(b - c) < 0.5 * tol * (b + c)) ||
+                    (!mflag && fabs(c - d) < 0.5 * tol * (c + d))) {
+                    s = 0.5 * (a + b);
+                    mflag = true;
+                } else {
+                    mflag = false;
+                }
+                fs = exf_f(s, l, r, dv, g);
+                d = c;
+                c = b;
+                fc = fb;
+                if (fa * fs < 0.) { b = s; fb = fs; } else { a = s; fa = fs; }
+                if (fabs(fa) < fabs(fb)) { t = a; a = b; b = t; t = fa; fa = fb; fb = t; }
+            }
+        }
+        p = b;
+    } else {
+        p = p_guess;
+    }
+    // star_state_from_pstar (exact.rs:214-238)
+    PRoot q{0., 0.};
+    if (p <= l.p || p <= r.p) q = proot(p, g);
+    Star<double> st_;
+    st_.u = 0.5 * (vl + vr) + 0.5 * (exf_fb(p, r, q) - exf_fb(p, l, q));
+    double gg = g.gm1dgp1();
+    double pl = p / l.p, pr = p / r.p;
+    st_.rho_l = pl > 1. ? l.rho * (pl + gg) / (gg * pl + 1.) : l.rho * ipow(q.r * l.ps_rm, g.rm - 2);
+    st_.rho_r = pr > 1. ? r.rho * (pr + gg) / (gg * pr + 1.) : r.rho * ipow(q.r * r.ps_rm, g.rm - 2);
+    st_.p = p;
+    return st_;
+}
+
 // PVRiemannSolver::solve_for_star_state (riemann_solver/pvrs.rs:26-46)
 template <typename T>
 __device__ __forceinline__ Star<T> pv_star(const St<T>& l, const St<T>& r, T vl, T vr, T al, T ar) {
@@ -416,7 +662,8 @@ __device__ __forceinline__ St<T> star_half_state(const St<T>& l, const St<T>& r,
     if (SOLVER == SOLVER_EXACT) {
         ExSide L{double(l.q[0]), double(l.q[4]), double(al)};
         ExSide R{double(r.q[0]), double(r.q[4]), double(ar)};
-        Star<double> sd = ex_star(L, R, double(vl), double(vr), g64, max_iter, err);
+        Star<double> sd = (sizeof(T) == 4 && g64.rm) ? ex_star_fast(L, R, double(vl), double(vr), g64, max_iter, err)
+                                                     : ex_star(L, R, double(vl), double(vr), g64, max_iter, err);
         s.rho_l = T(sd.rho_l);
         s.rho_r = T(sd.rho_r);
         s.u = T(sd.u);

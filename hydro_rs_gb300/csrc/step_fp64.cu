@@ -396,7 +396,9 @@ __device__ __forceinline__ void other_side(const KP& p, int i, int f, const St<d
 __device__ __forceinline__ double radius(double volume, int dim) {
     if (dim == 1) return 0.5 * volume;
     if (dim == 2) return sqrt(0.31830988618379067154 * volume);
-    return pow(0.25 * 3. * 0.31830988618379067154 * volume, 1. / 3.);
+    double x = 0.25 * 3. * 0.31830988618379067154 * volume, y, r;
+    if (rat_root(x, 3, 1. / 3., y, r)) return r;  // x^(1/3) (cube root by Newton, see rat_root)
+    return pow(x, 1. / 3.);
 }
 
 // Particle::timestep for fixed motion (part.rs:42-84, 328-372); returns the dt.
