@@ -45,6 +45,12 @@ def _dist():
     return ws, rank
 
 
+def aggregate_replicas(times_ms, faces, all_reduce_max, all_reduce_sum):
+    """Replica scaling (no data-path collective): the job's time is the slowest
+    rank's, its work the sum over ranks."""
+    return all_reduce_max(times_ms), all_reduce_sum(faces)
+
+
 def _peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -240,12 +246,15 @@ def run_ours(args):
     if ws > 1:
         import torch.distributed as dist
 
-        t = torch.tensor([ms32, ms64, e2e_s], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms32, ms64, e2e_s = t.tolist()
-        c = torch.tensor([faces32, faces64, e2e_faces], device="cuda", dtype=torch.float64)
-        dist.all_reduce(c)
-        faces32, faces64, e2e_faces = c.tolist()
+        def red(op):
+            def f(vals):
+                t = torch.tensor(vals, device="cuda", dtype=torch.float64)
+                dist.all_reduce(t, op=op)
+                return t.tolist()
+            return f
+
+        (ms32, ms64, e2e_s), (faces32, faces64, e2e_faces) = aggregate_replicas(
+            [ms32, ms64, e2e_s], [faces32, faces64, e2e_faces], red(dist.ReduceOp.MAX), red(dist.ReduceOp.SUM))
     if rank != 0:
         return
     peak, peak_kind = _peaks()

@@ -1311,6 +1311,22 @@ uint64_t orc_make_integer_timestep(double dt, int old_bin, int min_ngb_bin, uint
     return r;
 }
 
+/* ExactRiemannSolver::solve_for_star_state with explicit wave inputs
+ * (exact.rs:241-291), as called by the reference's regression test
+ * exact.rs:440-460.  out = (rho_l, rho_r, u, p). */
+void orc_exact_star(double gamma, double rho_l, double p_l, double a_l, double rho_r, double p_r, double a_r,
+                    double v_l, double v_r, double *out, uint32_t *err) {
+    adiabatic g = adiabatic_from(gamma);
+    state l = st(rho_l, v3(0., 0., 0.), p_l), r = st(rho_r, v3(0., 0., 0.), p_r);
+    uint32_t e = 0;
+    star_values s = ex_star_state(l, r, v_l, v_r, a_l, a_r, &g, 1000, &e);
+    out[0] = s.rho_l;
+    out[1] = s.rho_r;
+    out[2] = s.u;
+    out[3] = s.p;
+    if (err) *err = e;
+}
+
 /* keep cons_from_primitives referenced (used by the conversion round trip test) */
 void orc_cons_from_primitives(double gamma, const double *prim5, double volume, double *cons5) {
     gaslaw eos;

@@ -103,6 +103,13 @@ void orc_riemann_flux(int kind, double gamma, int64_t n, const double *left, con
  * in the blanket solve_for_flux); output [5][n] primitive. */
 void orc_riemann_sample(int kind, double gamma, int64_t n, const double *left, const double *right,
                         const double *normal, double *out, uint32_t *err);
+/* ExactRiemannSolver::solve_for_star_state with explicit inputs; out[4] =
+ * (rho_l, rho_r, u, p) (exact.rs:241-291). */
+void orc_exact_star(double gamma, double rho_l, double p_l, double a_l, double rho_r, double p_r, double a_r,
+                    double v_l, double v_r, double *out, uint32_t *err);
+/* State conversions (physical_quantities.rs:213-226, 294-304). */
+void orc_cons_from_primitives(double gamma, const double *prim5, double volume, double *cons5);
+void orc_prim_from_conserved(double gamma, const double *cons5, double volume, double *prim5);
 /* Timeline helpers (timeline.rs). */
 uint64_t orc_get_integer_timestep(int bin);
 int orc_get_time_bin(uint64_t dti);

@@ -71,6 +71,7 @@ def lib():
         L.orc_make_integer_timestep.argtypes = [dbl, i32, i32, u64, dbl, ctypes.POINTER(ctypes.c_uint32)]
         L.orc_cons_from_primitives.argtypes = [dbl, vp, dbl, vp]
         L.orc_prim_from_conserved.argtypes = [dbl, vp, dbl, vp]
+        L.orc_exact_star.argtypes = [dbl] + [dbl] * 8 + [vp, ctypes.POINTER(ctypes.c_uint32)]
         _LIB = L
     return _LIB
 
@@ -204,6 +205,14 @@ def prim_from_conserved(gamma, cons5, volume):
     out = np.zeros(5)
     lib().orc_prim_from_conserved(gamma, c.ctypes.data, volume, out.ctypes.data)
     return out
+
+
+def exact_star(gamma, rho_l, p_l, a_l, rho_r, p_r, a_r, v_l, v_r):
+    """(rho_l*, rho_r*, u*, p*) and the error bits of the exact star solver."""
+    out = np.zeros(4)
+    err = ctypes.c_uint32(0)
+    lib().orc_exact_star(gamma, rho_l, p_l, a_l, rho_r, p_r, a_r, v_l, v_r, out.ctypes.data, ctypes.byref(err))
+    return out, err.value
 
 
 def get_integer_timestep(b):

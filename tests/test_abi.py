@@ -1,0 +1,75 @@
+"""The C ABI library loads and exports every symbol its header declares.
+
+No compute call is made here (CPU-only test); argument validation that
+happens on the host before any CUDA call is exercised.
+"""
+import ctypes
+import os
+import re
+
+import pytest
+
+from hydro_rs_gb300 import build as B
+from hydro_rs_gb300 import gpu as G
+from hydro_rs_gb300 import ics
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    txt = open(os.path.join(ROOT, "include", "mvmm_gpu.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(mvmm_[a-z0-9_]+)\s*\(", txt)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    B.build_gpu()
+    return G.load_library()
+
+
+def test_every_declared_symbol_is_exported(lib):
+    syms = declared_symbols()
+    assert len(syms) >= 20
+    for s in syms:
+        assert hasattr(lib, s), s
+    assert set(syms) >= set(G.EXPORTED)
+
+
+def test_invalid_params_rejected_on_host(lib):
+    p = ics.sod_1d(16)
+    prm = G._Params(0.9, 0, 0.0, 0.3, 0, 1, 1, 1, 0.2, 1000, 0, 0)  # gamma <= 1
+    mv = p.mesh.cview()
+    h = ctypes.c_void_p(0)
+    rc = lib.mvmm_ctx_create(ctypes.byref(prm), ctypes.byref(mv), ctypes.byref(h))
+    assert rc == -1 and h.value is None
+    assert b"gamma" in lib.mvmm_last_error()
+    prm = G._Params(5 / 3, 0, 0.0, 0.3, 0, 1, 1, 1, 0.2, 1000, 0, 1)  # moving mesh
+    rc = lib.mvmm_ctx_create(ctypes.byref(prm), ctypes.byref(mv), ctypes.byref(h))
+    assert rc == -5
+
+
+def test_bad_mesh_rejected_on_host(lib):
+    p = ics.sod_1d(16)
+    m = p.mesh
+    m.right[3] = 99  # out of range
+    prm = G._Params(5 / 3, 0, 0.0, 0.3, 0, 1, 1, 1, 0.2, 1000, 0, 0)
+    mv = m.cview()
+    h = ctypes.c_void_p(0)
+    rc = lib.mvmm_ctx_create(ctypes.byref(prm), ctypes.byref(mv), ctypes.byref(h))
+    assert rc == -1 and b"out of range" in lib.mvmm_last_error()
+    # boundary faces with periodic boundary conditions (flux.rs:255-257 is unreachable there)
+    p = ics.sod_1d(16)
+    prm = G._Params(5 / 3, 0, 0.0, 0.3, 0, 0, 1, 1, 0.2, 1000, 0, 0)
+    mv = p.mesh.cview()
+    rc = lib.mvmm_ctx_create(ctypes.byref(prm), ctypes.byref(mv), ctypes.byref(h))
+    assert rc == -1
+
+
+def test_product_does_not_import_the_oracle():
+    pkg = os.path.join(ROOT, "hydro_rs_gb300")
+    for dirpath, _, files in os.walk(pkg):
+        for fn in files:
+            if fn.endswith((".py", ".cu", ".cuh", ".cpp", ".h")):
+                txt = open(os.path.join(dirpath, fn)).read()
+                assert "oracle" not in txt.replace("the oracle", "").replace("The oracle", "") or fn.endswith(".md"), fn
