@@ -112,6 +112,7 @@ __device__ __forceinline__ T ipow(T x, int k) {
 }
 
 // y = x^(-1/m), r = x^(1/m) for finite normal x > 0; false otherwise.
+template <int ITERS = 2>
 __device__ __forceinline__ bool rat_root(double x, int m, double inv_m, double& y, double& r) {
     long long bits = __double_as_longlong(x);
     int ex = (int)((bits >> 52) & 0x7ff);
@@ -122,7 +123,7 @@ __device__ __forceinline__ bool rat_root(double x, int m, double inv_m, double& 
     double xr = __longlong_as_double((bits & 0x000fffffffffffffLL) | ((long long)(rr + 1023) << 52));
     double yy = (double)exp2f(-log2f((float)xr) * (float)inv_m);
 #pragma unroll
-    for (int it = 0; it < 2; it++) {
+    for (int it = 0; it < ITERS; it++) {
         double t = fma(-xr, ipow(yy, m), 1.0);
         yy = fma(yy * inv_m, t, yy);
     }
@@ -484,7 +485,8 @@ static __device__ __noinline__ Star<double> ex_star(ExSide l, ExSide r, double v
 }
 
 // Exact star state for the FP32-face form: the same iteration as ex_star
-// (guess_p, Newton while f < 0, else Brent, relative tolerance 1e-6, FP64),
+// (guess_p, Newton while f < 0, else Brent, relative tolerance 1e-6, FP64;
+// roots to ~1e-13 with one Newton step, as the result is rounded to FP32),
 // evaluated with algebraically equal but cheaper expressions: per-side
 // constants hoisted out of the loop, one m-th root per pressure (shared by
 // both sides: (p/p_s)^(1/m) = p^(1/m) p_s^(-1/m)), rsqrt for the shock branch
@@ -502,7 +504,7 @@ __device__ __forceinline__ ExFast ex_fast_side(const ExSide& s, const Gas<double
     e.B = g.gm1dgp1() * s.p;
     e.c_rar = g.tdgm1() * s.a;
     double y, r;
-    if (!rat_root(s.p, g.rm, g.inv_m, y, r)) {
+    if (!rat_root<1>(s.p, g.rm, g.inv_m, y, r)) {
         y = pow(s.p, -g.inv_m);
         r = pow(s.p, g.inv_m);
     }
@@ -516,7 +518,7 @@ struct PRoot {
 };
 __device__ __forceinline__ PRoot proot(double p, const Gas<double>& g) {
     PRoot q;
-    if (!rat_root(p, g.rm, g.inv_m, q.y, q.r)) {
+    if (!rat_root<1>(p, g.rm, g.inv_m, q.y, q.r)) {
         q.y = pow(p, -g.inv_m);
         q.r = pow(p, g.inv_m);
     }

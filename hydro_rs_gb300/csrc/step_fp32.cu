@@ -117,7 +117,7 @@ __device__ __forceinline__ Out32 face_interior32(const KP& p, int f, int l, int 
     double m = area * (double)F.q[0];
     o.mflux = m * dxd;
     o.v_max = v_max;
-    o.a_over_r = area / len(dxd);
+    o.a_over_r = (double)((float)area / len(dx));  // feeds max_a_over_r only (mesh steering)
     return o;
 }
 
