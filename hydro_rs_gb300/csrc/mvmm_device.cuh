@@ -171,21 +171,26 @@ struct Gas {
     }
     __device__ __forceinline__ T pow_ginv(T x) const;
 };
+// pow(+-0, y) is +0 for y > 0 and +inf for y < 0 (IEEE 754 / C99 F.9.4.4):
+// answered directly, as the exact solver evaluates f(0) on every face.
 template <>
 __device__ __forceinline__ double Gas<double>::pow_e1(double x) const {
     double y, r;
+    if (x == 0.0) return 0.0;
     if (rm && rat_root(x, rm, inv_m, y, r)) return r;
     return pow(x, gm1d2g());
 }
 template <>
 __device__ __forceinline__ double Gas<double>::pow_me1(double x) const {
     double y, r;
+    if (x == 0.0) return INFINITY;
     if (rm && rat_root(x, rm, inv_m, y, r)) return y;
     return pow(x, -gm1d2g());
 }
 template <>
 __device__ __forceinline__ double Gas<double>::pow_ginv(double x) const {
     double y, r;
+    if (x == 0.0) return 0.0;
     if (rm && rat_root(x, rm, inv_m, y, r)) return ipow(r, rm - 2);
     return pow(x, 1. / gamma);
 }
@@ -500,7 +505,10 @@ __device__ __forceinline__ ExFast ex_fast_side(const ExSide& s, const Gas<double
     e.rho = s.rho;
     e.p = s.p;
     e.a = s.a;
-    e.sqA = sqrt(g.tdgp1() / s.rho);
+    // multiplicative per-side constants from the FP32 face-stage inputs (no
+    // cancellation downstream); the p_s roots below stay FP64, they meet
+    // p^(1/m) in (p/p_s)^(1/m) - 1
+    e.sqA = (double)sqrtf((float)g.tdgp1() / (float)s.rho);
     e.B = g.gm1dgp1() * s.p;
     e.c_rar = g.tdgm1() * s.a;
     double y, r;
@@ -510,7 +518,7 @@ __device__ __forceinline__ ExFast ex_fast_side(const ExSide& s, const Gas<double
     }
     e.ps_rm = y;
     e.ps_r = r;
-    e.k_fp = 1. / (s.rho * s.a);
+    e.k_fp = (double)(1.0f / ((float)s.rho * (float)s.a));
     return e;
 }
 struct PRoot {
@@ -518,7 +526,10 @@ struct PRoot {
 };
 __device__ __forceinline__ PRoot proot(double p, const Gas<double>& g) {
     PRoot q;
-    if (!rat_root<1>(p, g.rm, g.inv_m, q.y, q.r)) {
+    if (p == 0.0) {
+        q.y = INFINITY;
+        q.r = 0.0;
+    } else if (!rat_root<1>(p, g.rm, g.inv_m, q.y, q.r)) {
         q.y = pow(p, -g.inv_m);
         q.r = pow(p, g.inv_m);
     }
