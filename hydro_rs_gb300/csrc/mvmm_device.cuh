@@ -645,6 +645,122 @@ static __device__ __noinline__ Star<double> ex_star_fast(ExSide L, ExSide R, dou
     return st_;
 }
 
+// Exact star state for the FP32-face form, split by precision.  GB300 runs
+// FP64 at a small fraction of its FP32 rate, so the reference's search (guess,
+// Newton, bracketing) runs in FP32 only to produce a starting pressure, and
+// the pressure this form uses comes from two FP64 Newton steps on the
+// FP64-evaluated f(p) (exact.rs:23-34): f in FP64 (where the near-root
+// cancellation of f_L + f_R + dv happens), f' from FP32 (an approximate
+// derivative keeps Newton's convergence, at a rate set by its 1e-7 error).
+// From a start within ~1e-5 the two steps leave ~1e-12; lanes stay uniform
+// in the FP64 part.  A face whose FP32 start or FP64 polish is not clean
+// (near vacuum, extreme ratios) is solved by the full FP64 reference
+// iteration instead (ex_star_fast).  Requires gamma = m/(m-2).
+__device__ __forceinline__ double rsqrt64(double x) {  // FP32 seed + one Newton step (~1e-14)
+    double w = (double)rsqrtf((float)x);
+    return w * (1.5 - 0.5 * x * (w * w));
+}
+struct F32Side {
+    float rho, p, a, sqA, B, c_rar, k_fp;
+};
+__device__ __forceinline__ F32Side f32_side(float rho, float p, float a, const Gas<float>& g) {
+    F32Side s;
+    s.rho = rho;
+    s.p = p;
+    s.a = a;
+    s.sqA = sqrtf(g.tdgp1() / rho);
+    s.B = g.gm1dgp1() * p;
+    s.c_rar = g.tdgm1() * a;
+    s.k_fp = 1.f / (rho * a);
+    return s;
+}
+__device__ __forceinline__ void f32_eval(float p, const F32Side& s, float z, float& fb, float& fpb) {
+    if (p > s.p) {
+        float w = rsqrtf(p + s.B);
+        float sw = s.sqA * w;
+        fb = (p - s.p) * sw;
+        fpb = sw * (1.f - 0.5f * (p - s.p) * (w * w));
+    } else {
+        float t = __powf(p / s.p, z);
+        fb = s.c_rar * (t - 1.f);
+        fpb = s.k_fp / t;
+    }
+}
+static __device__ __noinline__ Star<float> ex_star_split(float rl, float pl, float al, float rr, float pr, float ar,
+                                                         float vl, float vr, Gas<float> g, Gas<double> g64,
+                                                         int max_iter, unsigned int* err) {
+    const float z = g.gm1d2g();
+    F32Side L = f32_side(rl, pl, al, g), R = f32_side(rr, pr, ar, g);
+    float dv = vr - vl;
+    // starting pressure: guess_p (exact.rs:70-103) in FP32
+    float p_min = fminf(pl, pr), p_max = fmaxf(pl, pr);
+    float ppv = fmaxf(0.5f * (pl + pr) - 0.125f * dv * (rl + rr) * (al + ar), 1e-8f);
+    float p;
+    if (p_max <= 2.f * p_min && p_min <= ppv && ppv <= p_max) {
+        p = ppv;
+    } else if (ppv < p_min) {
+        float base = (al + ar - 0.5f * (g.gamma - 1.f) * dv) / (al * __powf(pl, -z) + ar * __powf(pr, -z));
+        p = base > 0.f ? ipow(base, g64.rm) : 1e-8f;
+    } else {
+        float gl = L.sqA * rsqrtf(ppv + L.B), gr = R.sqA * rsqrtf(ppv + R.B);
+        p = (gl * pl + gr * pr - dv) / (gl + gr);
+    }
+    p = fmaxf(p, 1e-8f);
+    // Newton in FP32; f is increasing and concave, so a step from above lands
+    // below the root and the iterates then rise monotonically
+    for (int it = 0; it < 12; it++) {
+        float fbl, fpl, fbr, fpr;
+        f32_eval(p, L, z, fbl, fpl);
+        f32_eval(p, R, z, fbr, fpr);
+        float dp = (fbl + fbr + dv) / (fpl + fpr);
+        float pn = p - dp;
+        if (!(pn > 0.f)) pn = 0.1f * p;
+        bool done = fabsf(dp) <= 2e-6f * p;
+        p = pn;
+        if (done) break;
+    }
+    // two FP64 Newton steps on the FP64 f
+    ExFast L64 = ex_fast_side(ExSide{(double)rl, (double)pl, (double)al}, g64);
+    ExFast R64 = ex_fast_side(ExSide{(double)rr, (double)pr, (double)ar}, g64);
+    double P = (double)p, dP = 0.;
+    double dvd = (double)vr - (double)vl;
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+        PRoot q{0., 0.};
+        if (P <= L64.p || P <= R64.p) q = proot(P, g64);
+        double fl = P > L64.p ? (P - L64.p) * L64.sqA * rsqrt64(P + L64.B) : L64.c_rar * (q.r * L64.ps_rm - 1.);
+        double fr = P > R64.p ? (P - R64.p) * R64.sqA * rsqrt64(P + R64.B) : R64.c_rar * (q.r * R64.ps_rm - 1.);
+        float fbl, fpl, fbr, fpr;
+        f32_eval((float)P, L, z, fbl, fpl);
+        f32_eval((float)P, R, z, fbr, fpr);
+        dP = (fl + fr + dvd) * (double)(1.f / (fpl + fpr));
+        P = P - dP;
+    }
+    Star<float> s;
+    if (!(P > 0.) || !isfinite(P) || !(fabs(dP) <= 1e-9 * P)) {
+        Star<double> sd = ex_star_fast(ExSide{(double)rl, (double)pl, (double)al},
+                                       ExSide{(double)rr, (double)pr, (double)ar}, (double)vl, (double)vr, g64,
+                                       max_iter, err);
+        s.rho_l = (float)sd.rho_l;
+        s.rho_r = (float)sd.rho_r;
+        s.u = (float)sd.u;
+        s.p = (float)sd.p;
+        return s;
+    }
+    // star_state_from_pstar (exact.rs:214-238) in FP32 at the polished pressure
+    float ps = (float)P;
+    float fbl, fpl, fbr, fpr;
+    f32_eval(ps, L, z, fbl, fpl);
+    f32_eval(ps, R, z, fbr, fpr);
+    s.u = 0.5f * (vl + vr) + 0.5f * (fbr - fbl);
+    float gg = g.gm1dgp1();
+    float qlr = ps / pl, qrr = ps / pr;
+    s.rho_l = qlr > 1.f ? rl * (qlr + gg) / (gg * qlr + 1.f) : rl * ipow(__powf(qlr, z), g64.rm - 2);
+    s.rho_r = qrr > 1.f ? rr * (qrr + gg) / (gg * qrr + 1.f) : rr * ipow(__powf(qrr, z), g64.rm - 2);
+    s.p = ps;
+    return s;
+}
+
 // PVRiemannSolver::solve_for_star_state (riemann_solver/pvrs.rs:26-46)
 template <typename T>
 __device__ __forceinline__ Star<T> pv_star(const St<T>& l, const St<T>& r, T vl, T vr, T al, T ar) {
@@ -672,11 +788,18 @@ __device__ __forceinline__ St<T> star_half_state(const St<T>& l, const St<T>& r,
     T vrml = vr - vl;
     if (is_vacuum(l, r, al, ar, vrml, g)) return vacuum_sample(l, r, vl, vr, al, ar, n, g);
     Star<T> s;
-    if (SOLVER == SOLVER_EXACT) {
+    if (SOLVER == SOLVER_EXACT && sizeof(T) == 4 && g64.rm) {
+        Star<float> sf = ex_star_split(float(l.q[0]), float(l.q[4]), float(al), float(r.q[0]), float(r.q[4]),
+                                       float(ar), float(vl), float(vr), make_gas<float>(double(g.gamma), g.eos,
+                                       double(g.iso_u)), g64, max_iter, err);
+        s.rho_l = T(sf.rho_l);
+        s.rho_r = T(sf.rho_r);
+        s.u = T(sf.u);
+        s.p = T(sf.p);
+    } else if (SOLVER == SOLVER_EXACT) {
         ExSide L{double(l.q[0]), double(l.q[4]), double(al)};
         ExSide R{double(r.q[0]), double(r.q[4]), double(ar)};
-        Star<double> sd = (sizeof(T) == 4 && g64.rm) ? ex_star_fast(L, R, double(vl), double(vr), g64, max_iter, err)
-                                                     : ex_star(L, R, double(vl), double(vr), g64, max_iter, err);
+        Star<double> sd = ex_star(L, R, double(vl), double(vr), g64, max_iter, err);
         s.rho_l = T(sd.rho_l);
         s.rho_r = T(sd.rho_r);
         s.u = T(sd.u);
