@@ -17,6 +17,7 @@ void launch_face_flux_fp64(const KP& p, int solver, cudaStream_t s);
 void launch_riemann_fp64(int kind, int sample, double gamma, int64_t n, const double* l, const double* r,
                          const double* vf, const double* nrm, double* out, unsigned int* err, cudaStream_t s);
 void launch_face_flux_fp32(const KP& p, int solver, cudaStream_t s);
+void launch_gradients32(const KP& p, cudaStream_t s);
 void launch_riemann_fp32(int kind, int sample, double gamma, int64_t n, const double* l, const double* r,
                          const double* vf, const double* nrm, double* out, unsigned int* err, cudaStream_t s);
 }  // namespace mvmm
@@ -123,7 +124,8 @@ void enqueue_step_kernels(mvmm_ctx* c, bool with_events) {
     if (with_events) cudaEventRecord(c->ev[2], s);
     launch_update(p, 1, s);
     if (with_events) cudaEventRecord(c->ev[3], s);
-    launch_gradients(p, 1, s);
+    if (c->prm.precision == MVMM_PRECISION_FP32FACE) launch_gradients32(p, s);
+    else launch_gradients(p, 1, s);
     if (with_events) cudaEventRecord(c->ev[4], s);
     launch_limit(p, s);
     if (with_events) cudaEventRecord(c->ev[5], s);

@@ -1,0 +1,117 @@
+// Cell-state accessors and per-cell helpers shared by the kernels of both
+// arithmetic forms (each translation unit gets its own copy: the plain form is
+// compiled without FMA contraction, the FP32-face form with it).
+#pragma once
+
+#include "mvmm_device.cuh"
+#include "mvmm_internal.h"
+
+namespace mvmm {
+namespace {
+
+constexpr int kBlock = 128;
+
+__device__ __forceinline__ double C(const KP& p, int f, int i) { return p.cd[(size_t)f * p.n + i]; }
+__device__ __forceinline__ void W(const KP& p, int f, int i, double v) { p.cd[(size_t)f * p.n + i] = v; }
+__device__ __forceinline__ V3<double> C3(const KP& p, int f, int i) {
+    return {C(p, f, i), C(p, f + 1, i), C(p, f + 2, i)};
+}
+__device__ __forceinline__ void W3(const KP& p, int f, int i, V3<double> v) {
+    W(p, f, i, v.x);
+    W(p, f + 1, i, v.y);
+    W(p, f + 2, i, v.z);
+}
+__device__ __forceinline__ St<double> C5(const KP& p, int f, int i) {
+    St<double> s;
+#pragma unroll
+    for (int q = 0; q < 5; q++) s.q[q] = C(p, f + q, i);
+    return s;
+}
+__device__ __forceinline__ void W5(const KP& p, int f, int i, const St<double>& s) {
+#pragma unroll
+    for (int q = 0; q < 5; q++) W(p, f + q, i, s.q[q]);
+}
+__device__ __forceinline__ V3<double> F3(const double* a, int nf, int f) { return {a[f], a[nf + f], a[2 * nf + f]}; }
+__device__ __forceinline__ Gas<double> gas(const KP& p) { return make_gas<double>(p.gamma, p.eos, p.iso_u); }
+__device__ __forceinline__ void set_err(const KP& p, unsigned int bits) {
+    if (bits) atomicOr(&p.tl->err, bits);
+}
+
+// Gradients::dot row q with dx (physical_quantities.rs:122-133)
+__device__ __forceinline__ double gdot(const KP& p, int i, int q, V3<double> dx) {
+    return C(p, F_GRAD + 3 * q, i) * dx.x + C(p, F_GRAD + 3 * q + 1, i) * dx.y + C(p, F_GRAD + 3 * q + 2, i) * dx.z;
+}
+
+// The other side of face f as seen from cell i: Space::get_boundary_part for
+// walls (space.rs:213-229), else the neighbour (runner/hydrodynamics.rs:59-65).
+__device__ __forceinline__ void other_side(const KP& p, int i, int f, const St<double>& prim, V3<double> cen,
+                                           St<double>& oprim, V3<double>& ocen, V3<double>& sh) {
+    int l = p.left[f], r = p.right[f];
+    V3<double> s = F3(p.shift, p.nf, f);
+    sh = (i == l) ? s : neg(s);
+    if (i == l && r < 0) {
+        V3<double> fc = F3(p.fcen, p.nf, f);
+        V3<double> n = F3(p.normal, p.nf, f);
+        ocen = cen + (2. * dot(fc - cen, n)) * n;
+        if (p.boundary == 1) oprim = reflect(prim, n);
+        else if (p.boundary == 2) oprim = prim;
+        else oprim = st_zero<double>();
+    } else {
+        int o = (i == l) ? r : l;
+        ocen = C3(p, F_CEN, o);
+        oprim = C5(p, F_PRIM, o);
+    }
+}
+
+// Particle::radius (part.rs:439-447)
+__device__ __forceinline__ double radius(double volume, int dim) {
+    if (dim == 1) return 0.5 * volume;
+    if (dim == 2) return sqrt(0.31830988618379067154 * volume);
+    double x = 0.25 * 3. * 0.31830988618379067154 * volume, y, r;
+    if (rat_root(x, 3, 1. / 3., y, r)) return r;  // x^(1/3) (cube root by Newton, see rat_root)
+    return pow(x, 1. / 3.);
+}
+
+// Particle::timestep for fixed motion (part.rs:42-84, 328-372); returns the dt.
+__device__ __forceinline__ double particle_timestep(const KP& p, int i) {
+    St<double> cons = C5(p, F_CONS, i);
+    if (cons.q[0] == 0.) {
+        W3(p, F_V, i, v3(0., 0., 0.));
+        return INFINITY;
+    }
+    const Gas<double> g = gas(p);
+    double m_inv = 1. / cons.q[0];
+    V3<double> dxg = C3(p, F_LOC, i) - C3(p, F_GC, i);
+    V3<double> d_v = v3(gdot(p, i, 1, dxg), gdot(p, i, 2, dxg), gdot(p, i, 3, dxg));
+    V3<double> fluid_v = m_inv * vel(cons) + d_v;
+    St<double> prim = C5(p, F_PRIM, i);
+    double u = (cons.q[4] - 0.5 * dot(vel(cons), vel(prim))) / cons.q[0];  // Particle::internal_energy
+    double vol = C(p, F_VOL, i);
+    double c = g.sound_speed(g.pressure_from_internal_energy(u, prim.q[0]), vol * m_inv);
+    V3<double> v = v3(0., 0., 0.);  // ParticleMotion::Fixed
+    V3<double> v_rel = fluid_v - v;
+    W3(p, F_V, i, v);
+    W3(p, F_VREL, i, v_rel);
+    W(p, F_MAOR, i, 0.);
+    double v_max = m_max(C(p, F_MSV, i), len(v_rel) + c);
+    W(p, F_MSV, i, 0.);
+    if (v_max > 0.) return p.cfl * radius(vol, p.dim) / v_max;
+    return INFINITY;
+}
+
+__device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = w < v ? w : v;
+    }
+    return v;
+}
+__device__ __forceinline__ int warp_min_int(int v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+}  // namespace
+}  // namespace mvmm

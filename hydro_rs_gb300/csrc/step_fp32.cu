@@ -6,20 +6,13 @@
 // final dt * area * F product, the scatter and the conserved update stay FP64
 // (the update kernel is shared with the plain form).  Compiled with FMA
 // contraction enabled.
-#include "mvmm_device.cuh"
-#include "mvmm_internal.h"
+#include "mvmm_cellops.cuh"
 
 namespace mvmm {
 
 namespace {
 
-constexpr int kBlock = 128;
-
-__device__ __forceinline__ double C(const KP& p, int f, int i) { return p.cd[(size_t)f * p.n + i]; }
 __device__ __forceinline__ float G(const KP& p, int f, int i) { return p.cf[(size_t)f * p.n + i]; }
-__device__ __forceinline__ V3<double> C3(const KP& p, int f, int i) {
-    return {C(p, f, i), C(p, f + 1, i), C(p, f + 2, i)};
-}
 __device__ __forceinline__ V3<float> G3(const KP& p, int f, int i) { return {G(p, f, i), G(p, f + 1, i), G(p, f + 2, i)}; }
 __device__ __forceinline__ St<float> G5(const KP& p, int f, int i) {
     St<float> s;
@@ -27,8 +20,6 @@ __device__ __forceinline__ St<float> G5(const KP& p, int f, int i) {
     for (int q = 0; q < 5; q++) s.q[q] = G(p, f + q, i);
     return s;
 }
-__device__ __forceinline__ V3<double> F3(const double* a, int nf, int f) { return {a[f], a[nf + f], a[2 * nf + f]}; }
-
 __global__ void __launch_bounds__(kBlock) k_prep32(KP p) {
     if (p.tl->done) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -216,6 +207,126 @@ __global__ void __launch_bounds__(kBlock) k_face_flux32(KP p) {
     if ((threadIdx.x & 31) == 0 && b) atomicAdd(&p.tl->active_faces, (unsigned long long)__popc(b));
 }
 
+// gradient_estimate + gradient_limit + gradient_apply (runner/hydrodynamics.rs:67-143)
+// for the FP32-face form: differences of primitives and positions are formed
+// in FP64 and rounded, the WLS sums, the 3x3 inverse and the cell-wise limiter
+// run in FP32 (these slopes only feed the FP32 reconstruction), and the
+// timestep (Particle::timestep, timesteps_apply) stays FP64 as in the plain form.
+__global__ void __launch_bounds__(kBlock) k_gradients32(KP p) {
+    if (p.tl->done) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long my_dti = MAX_NR_TIMESTEPS;
+    int my_tb = 127;
+    unsigned int err = 0;
+    if (i < p.n) {
+        int tb = p.timebin[i];
+        if (p.active[i]) {
+            V3<double> cen = C3(p, F_CEN, i);
+            St<double> prim = C5(p, F_PRIM, i);
+            float a00 = 0.f, a01 = 0.f, a02 = 0.f, a11 = 0.f, a12 = 0.f, a22 = 0.f;
+            if (p.dim == 1) { a11 = 1.f; a22 = 1.f; }
+            else if (p.dim == 2) { a22 = 1.f; }
+            V3<float> gr[5];
+#pragma unroll
+            for (int q = 0; q < 5; q++) gr[q] = v3(0.f, 0.f, 0.f);
+            int k0 = p.csr_off[i], k1 = p.csr_off[i + 1];
+            for (int k = k0; k < k1; k++) {
+                int f = p.csr_face[k];
+                St<double> op;
+                V3<double> oc, sh;
+                other_side(p, i, f, prim, cen, op, oc, sh);
+                V3<float> ds = cvt<float>((oc + sh) - cen);
+                float w = (float)p.area[f] / len2(ds);
+#pragma unroll
+                for (int q = 0; q < 5; q++) gr[q] = gr[q] + (w * (float)(op.q[q] - prim.q[q])) * ds;
+                a00 += w * ds.x * ds.x;
+                a01 += w * ds.x * ds.y;
+                a02 += w * ds.x * ds.z;
+                a11 += w * ds.y * ds.y;
+                a12 += w * ds.y * ds.z;
+                a22 += w * ds.z * ds.z;
+            }
+            V3<float> m0 = v3(a00, a01, a02), m1 = v3(a01, a11, a12), m2 = v3(a02, a12, a22);
+            V3<float> t0 = cross(m1, m2), t1 = cross(m2, m0), t2 = cross(m0, m1);
+            float inv_det = 1.f / dot(m2, t2);
+            V3<float> r0 = inv_det * t0, r1 = inv_det * t1, r2 = inv_det * t2;
+            bool finite = true;
+#pragma unroll
+            for (int q = 0; q < 5; q++) {
+                V3<float> x = gr[q];
+                gr[q] = v3(dot(r0, x), dot(r1, x), dot(r2, x));  // symmetric inverse: rows = columns
+                finite = finite && isfinite(gr[q].x) && isfinite(gr[q].y) && isfinite(gr[q].z);
+            }
+            if (!finite) {
+#pragma unroll
+                for (int q = 0; q < 5; q++) gr[q] = v3(0.f, 0.f, 0.f);
+            }
+            // LimiterData (gradients.rs:58-103) on differences to this cell's state
+            float dmn[5], dmx[5], emn[5], emx[5];
+#pragma unroll
+            for (int q = 0; q < 5; q++) {
+                dmn[q] = 0.f;
+                dmx[q] = 0.f;
+                emn[q] = INFINITY;
+                emx[q] = -INFINITY;
+            }
+            for (int k = k0; k < k1; k++) {
+                int f = p.csr_face[k];
+                St<double> op;
+                V3<double> oc, sh;
+                other_side(p, i, f, prim, cen, op, oc, sh);
+                V3<float> d = cvt<float>((F3(p.fcen, p.nf, f) - cen) - sh);
+#pragma unroll
+                for (int q = 0; q < 5; q++) {
+                    float ex = dot(gr[q], d);
+                    float dq = (float)(op.q[q] - prim.q[q]);
+                    dmn[q] = fminf(dmn[q], dq);
+                    dmx[q] = fmaxf(dmx[q], dq);
+                    emn[q] = fminf(emn[q], ex);
+                    emx[q] = fmaxf(emx[q], ex);
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < 5; q++) {
+                float alpha = (emx[q] == 0.f || emn[q] == 0.f) ? 1.f : fminf(1.f, fminf(dmx[q] / emx[q], dmn[q] / emn[q]));
+                gr[q] = alpha * gr[q];
+                W3(p, F_GRAD + 3 * q, i, cvt<double>(gr[q]));
+            }
+            W3(p, F_GC, i, cen);
+            double dt_new = particle_timestep(p, i);
+            unsigned long long tc = p.tl->ti_current;
+            unsigned long long dti = make_integer_timestep(dt_new, tb, NUM_TIME_BINS, tc, p.time_base_inv);
+            if (dti == 0) err |= 1u << 6;
+            W(p, F_DT, i, (double)dti * p.time_base);
+            tb = get_time_bin(dti);
+            my_dti = dti;
+        }
+        p.tb_tmp[i] = (int8_t)tb;
+        my_tb = tb;
+    }
+    if (err) set_err(p, err);
+    __shared__ unsigned long long s_dti[kBlock / 32];
+    __shared__ int s_tb[kBlock / 32];
+    my_dti = warp_min_u64(my_dti);
+    my_tb = warp_min_int(my_tb);
+    int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        s_dti[w] = my_dti;
+        s_tb[w] = my_tb;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long a = s_dti[0];
+        int b = s_tb[0];
+        for (int k = 1; k < kBlock / 32; k++) {
+            a = s_dti[k] < a ? s_dti[k] : a;
+            b = min(b, s_tb[k]);
+        }
+        atomicMin(&p.tl->min_dti, a);
+        atomicMin(&p.tl->min_timebin, b);
+    }
+}
+
 template <int SOLVER, bool SAMPLE>
 __global__ void k_riemann32(double gamma, int64_t n, const double* l, const double* r, const double* vf,
                             const double* nrm, double* out, unsigned int* errp) {
@@ -249,6 +360,10 @@ inline int grid(int n) { return (n + kBlock - 1) / kBlock; }
 
 void launch_prep32(const KP& p, cudaStream_t s) {
     if (p.n > 0) k_prep32<<<grid(p.n), kBlock, 0, s>>>(p);
+}
+
+void launch_gradients32(const KP& p, cudaStream_t s) {
+    if (p.n > 0) k_gradients32<<<grid(p.n), kBlock, 0, s>>>(p);
 }
 
 void launch_face_flux_fp32(const KP& p, int solver, cudaStream_t s) {

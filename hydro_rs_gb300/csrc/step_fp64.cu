@@ -4,45 +4,11 @@
 // reference evaluates it.  One CUDA thread per face for the flux stage, one per
 // cell for the cell stages; the flux scatter is a deterministic CSR gather in
 // the reference's face order (no atomics on floating-point data).
-#include "mvmm_device.cuh"
-#include "mvmm_internal.h"
+#include "mvmm_cellops.cuh"
 
 namespace mvmm {
 
 namespace {
-
-constexpr int kBlock = 128;
-
-__device__ __forceinline__ double C(const KP& p, int f, int i) { return p.cd[(size_t)f * p.n + i]; }
-__device__ __forceinline__ void W(const KP& p, int f, int i, double v) { p.cd[(size_t)f * p.n + i] = v; }
-__device__ __forceinline__ V3<double> C3(const KP& p, int f, int i) {
-    return {C(p, f, i), C(p, f + 1, i), C(p, f + 2, i)};
-}
-__device__ __forceinline__ void W3(const KP& p, int f, int i, V3<double> v) {
-    W(p, f, i, v.x);
-    W(p, f + 1, i, v.y);
-    W(p, f + 2, i, v.z);
-}
-__device__ __forceinline__ St<double> C5(const KP& p, int f, int i) {
-    St<double> s;
-#pragma unroll
-    for (int q = 0; q < 5; q++) s.q[q] = C(p, f + q, i);
-    return s;
-}
-__device__ __forceinline__ void W5(const KP& p, int f, int i, const St<double>& s) {
-#pragma unroll
-    for (int q = 0; q < 5; q++) W(p, f + q, i, s.q[q]);
-}
-__device__ __forceinline__ V3<double> F3(const double* a, int nf, int f) { return {a[f], a[nf + f], a[2 * nf + f]}; }
-__device__ __forceinline__ Gas<double> gas(const KP& p) { return make_gas<double>(p.gamma, p.eos, p.iso_u); }
-__device__ __forceinline__ void set_err(const KP& p, unsigned int bits) {
-    if (bits) atomicOr(&p.tl->err, bits);
-}
-
-// Gradients::dot row q with dx (physical_quantities.rs:122-133)
-__device__ __forceinline__ double gdot(const KP& p, int i, int q, V3<double> dx) {
-    return C(p, F_GRAD + 3 * q, i) * dx.x + C(p, F_GRAD + 3 * q + 1, i) * dx.y + C(p, F_GRAD + 3 * q + 2, i) * dx.z;
-}
 
 // Particle::time_extrapolations body before the -dt factor (part.rs:134-149).
 __device__ __forceinline__ St<double> extrap_source(const KP& p, int i, const St<double>& prim, double rho_inv) {
@@ -371,77 +337,6 @@ __global__ void __launch_bounds__(kBlock) k_c2p(KP p) {
 }
 
 // ------------------------------------------------------------ gradients --
-// The other side of face f as seen from cell i: Space::get_boundary_part for
-// walls (space.rs:213-229), else the neighbour (runner/hydrodynamics.rs:59-65).
-__device__ __forceinline__ void other_side(const KP& p, int i, int f, const St<double>& prim, V3<double> cen,
-                                           St<double>& oprim, V3<double>& ocen, V3<double>& sh) {
-    int l = p.left[f], r = p.right[f];
-    V3<double> s = F3(p.shift, p.nf, f);
-    sh = (i == l) ? s : neg(s);
-    if (i == l && r < 0) {
-        V3<double> fc = F3(p.fcen, p.nf, f);
-        V3<double> n = F3(p.normal, p.nf, f);
-        ocen = cen + (2. * dot(fc - cen, n)) * n;
-        if (p.boundary == 1) oprim = reflect(prim, n);
-        else if (p.boundary == 2) oprim = prim;
-        else oprim = st_zero<double>();
-    } else {
-        int o = (i == l) ? r : l;
-        ocen = C3(p, F_CEN, o);
-        oprim = C5(p, F_PRIM, o);
-    }
-}
-
-// Particle::radius (part.rs:439-447)
-__device__ __forceinline__ double radius(double volume, int dim) {
-    if (dim == 1) return 0.5 * volume;
-    if (dim == 2) return sqrt(0.31830988618379067154 * volume);
-    double x = 0.25 * 3. * 0.31830988618379067154 * volume, y, r;
-    if (rat_root(x, 3, 1. / 3., y, r)) return r;  // x^(1/3) (cube root by Newton, see rat_root)
-    return pow(x, 1. / 3.);
-}
-
-// Particle::timestep for fixed motion (part.rs:42-84, 328-372); returns the dt.
-__device__ __forceinline__ double particle_timestep(const KP& p, int i) {
-    St<double> cons = C5(p, F_CONS, i);
-    if (cons.q[0] == 0.) {
-        W3(p, F_V, i, v3(0., 0., 0.));
-        return INFINITY;
-    }
-    const Gas<double> g = gas(p);
-    double m_inv = 1. / cons.q[0];
-    V3<double> dxg = C3(p, F_LOC, i) - C3(p, F_GC, i);
-    V3<double> d_v = v3(gdot(p, i, 1, dxg), gdot(p, i, 2, dxg), gdot(p, i, 3, dxg));
-    V3<double> fluid_v = m_inv * vel(cons) + d_v;
-    St<double> prim = C5(p, F_PRIM, i);
-    double u = (cons.q[4] - 0.5 * dot(vel(cons), vel(prim))) / cons.q[0];  // Particle::internal_energy
-    double vol = C(p, F_VOL, i);
-    double c = g.sound_speed(g.pressure_from_internal_energy(u, prim.q[0]), vol * m_inv);
-    V3<double> v = v3(0., 0., 0.);  // ParticleMotion::Fixed
-    V3<double> v_rel = fluid_v - v;
-    W3(p, F_V, i, v);
-    W3(p, F_VREL, i, v_rel);
-    W(p, F_MAOR, i, 0.);
-    double v_max = m_max(C(p, F_MSV, i), len(v_rel) + c);
-    W(p, F_MSV, i, 0.);
-    if (v_max > 0.) return p.cfl * radius(vol, p.dim) / v_max;
-    return INFINITY;
-}
-
-__device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
-        v = w < v ? w : v;
-    }
-    return v;
-}
-__device__ __forceinline__ int warp_min_int(int v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
-    return v;
-}
-
 // gradient_estimate + gradient_limit + gradient_apply (runner/hydrodynamics.rs:67-143)
 // fused per cell; in step mode also compute_timesteps + timesteps_apply
 // (euler_eqns_fvs.rs:50-61, runner/hydrodynamics.rs:145-158) with block-level
@@ -457,10 +352,12 @@ __global__ void __launch_bounds__(kBlock) k_gradients(KP p, int do_timestep) {
         if (p.active[i]) {
             V3<double> cen = C3(p, F_CEN, i);
             St<double> prim = C5(p, F_PRIM, i);
-            // GradientData::init (gradients.rs:14-33): columns c0,c1,c2
-            V3<double> m0 = v3(0., 0., 0.), m1 = v3(0., 0., 0.), m2 = v3(0., 0., 0.);
-            if (p.dim == 1) { m1.y = 1.; m2.z = 1.; }
-            else if (p.dim == 2) { m2.z = 1.; }
+            // GradientData::init (gradients.rs:14-33).  The WLS matrix is
+            // symmetric term by term (ds.x*ds.y == ds.y*ds.x exactly), so its
+            // six distinct entries are accumulated once: a00 a01 a02 / a11 a12 / a22.
+            double a00 = 0., a01 = 0., a02 = 0., a11 = 0., a12 = 0., a22 = 0.;
+            if (p.dim == 1) { a11 = 1.; a22 = 1.; }
+            else if (p.dim == 2) { a22 = 1.; }
             V3<double> gr[5];
 #pragma unroll
             for (int q = 0; q < 5; q++) gr[q] = v3(0., 0., 0.);
@@ -472,13 +369,27 @@ __global__ void __launch_bounds__(kBlock) k_gradients(KP p, int do_timestep) {
                 other_side(p, i, f, prim, cen, op, oc, sh);
                 V3<double> ds = (oc + sh) - cen;
                 double w = p.area[f] / len2(ds);
-                // GradientData::collect (gradients.rs:35-41)
+                // GradientData::collect (gradients.rs:35-41).  When ds.z is
+                // exactly zero (2D meshes) the z terms add +-0 to entries that
+                // are +0 (or 1), which leaves them unchanged, so they are skipped.
+                bool z = ds.z != 0.;
 #pragma unroll
-                for (int q = 0; q < 5; q++) gr[q] = gr[q] + (w * (op.q[q] - prim.q[q])) * ds;
-                m0 = m0 + w * (ds.x * ds);
-                m1 = m1 + w * (ds.y * ds);
-                m2 = m2 + w * (ds.z * ds);
+                for (int q = 0; q < 5; q++) {
+                    double wdq = w * (op.q[q] - prim.q[q]);
+                    gr[q].x = gr[q].x + wdq * ds.x;
+                    gr[q].y = gr[q].y + wdq * ds.y;
+                    if (z) gr[q].z = gr[q].z + wdq * ds.z;
+                }
+                a00 = a00 + w * (ds.x * ds.x);
+                a01 = a01 + w * (ds.x * ds.y);
+                a11 = a11 + w * (ds.y * ds.y);
+                if (z) {
+                    a02 = a02 + w * (ds.x * ds.z);
+                    a12 = a12 + w * (ds.y * ds.z);
+                    a22 = a22 + w * (ds.z * ds.z);
+                }
             }
+            V3<double> m0 = v3(a00, a01, a02), m1 = v3(a01, a11, a12), m2 = v3(a02, a12, a22);
             // GradientData::finalize with glam DMat3::inverse (gradients.rs:43-55)
             V3<double> t0 = cross(m1, m2), t1 = cross(m2, m0), t2 = cross(m0, m1);
             double det = dot(m2, t2);
