@@ -138,9 +138,12 @@ class _Clocks:
 
 
 def _time_steps(sim, steps, stream, flush_buf, torch):
-    """Times `steps` device-resident steps, one event pair per step, L2 flushed before each."""
-    total = 0.0
+    """Times `steps` device-resident steps with one event pair each and an L2
+    flush before each.  Everything is enqueued first and synchronised once, so
+    the GPU runs flush, step, flush, step, ... without host gaps; only the
+    event-bracketed step times are summed."""
     sim.set_time()
+    evs = []
     for _ in range(steps):
         flush_buf.zero_()
         e0 = torch.cuda.Event(enable_timing=True)
@@ -148,9 +151,10 @@ def _time_steps(sim, steps, stream, flush_buf, torch):
         e0.record(stream)
         sim.enqueue_steps(1)
         e1.record(stream)
-        e1.synchronize()
-        total += e0.elapsed_time(e1)
-    st, af = sim.sync_time()
+        evs.append((e0, e1))
+    torch.cuda.synchronize()
+    total = sum(e0.elapsed_time(e1) for e0, e1 in evs)
+    sim.sync_time()
     return total
 
 
