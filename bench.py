@@ -145,7 +145,8 @@ def _time_steps(sim, steps, stream, flush_buf, torch):
     sim.set_time()
     evs = []
     for _ in range(steps):
-        flush_buf.zero_()
+        with torch.cuda.stream(stream):
+            flush_buf.zero_()  # on the simulation's stream, so it is ordered with the steps
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
