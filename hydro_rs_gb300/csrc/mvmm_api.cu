@@ -493,6 +493,17 @@ int mvmm_get_time(mvmm_ctx* c, uint64_t* ti_current, uint64_t* ti_old, int64_t* 
     return MVMM_OK;
 }
 
+int mvmm_get_stats(mvmm_ctx* c, mvmm_stats* out) {
+    if (!c || !out) return fail(MVMM_E_INVALID, "null argument");
+    int rc = read_tl(c);
+    if (rc) return rc;
+    out->steps = (int64_t)c->tl_host->steps;
+    out->active_faces = (int64_t)c->tl_host->active_faces;
+    out->active_cells = (int64_t)c->tl_host->active_cells;
+    out->fp64_fallback_faces = (int64_t)c->tl_host->fallback_faces;
+    return MVMM_OK;
+}
+
 int mvmm_step(mvmm_ctx* c, uint64_t ti_current, uint64_t ti_old, uint64_t* ti_next, int64_t* n_active_faces) {
     if (!c) return fail(MVMM_E_INVALID, "null context");
     int rc = mvmm_set_time(c, ti_current, ti_old);

@@ -652,8 +652,9 @@ static __device__ __noinline__ Star<double> ex_star_fast(ExSide L, ExSide R, dou
 // FP64-evaluated f(p) (exact.rs:23-34): f in FP64 (where the near-root
 // cancellation of f_L + f_R + dv happens), f' from FP32 (an approximate
 // derivative keeps Newton's convergence, at a rate set by its 1e-7 error).
-// From a start within ~1e-5 the two steps leave ~1e-12; lanes stay uniform
-// in the FP64 part.  A face whose FP32 start or FP64 polish is not clean
+// From a start within ~1e-5 the two steps leave ~1e-12; a last correction
+// above 1e-8 (the FP32 resolution of the result) sends the face to the
+// fallback.  Lanes stay uniform in the FP64 part.  A face whose FP32 start or FP64 polish is not clean
 // (near vacuum, extreme ratios) is solved by the full FP64 reference
 // iteration instead (ex_star_fast).  Requires gamma = m/(m-2).
 __device__ __forceinline__ double rsqrt64(double x) {  // FP32 seed + one Newton step (~1e-14)
@@ -706,19 +707,27 @@ static __device__ __noinline__ Star<float> ex_star_split(float rl, float pl, flo
         p = (gl * pl + gr * pr - dv) / (gl + gr);
     }
     p = fmaxf(p, 1e-8f);
-    // Newton in FP32; f is increasing and concave, so a step from above lands
-    // below the root and the iterates then rise monotonically
-    for (int it = 0; it < 12; it++) {
+    // Newton in FP32 on x = p^(1/m): the rarefaction terms of f are linear in
+    // x (two rarefactions converge in one step) and the shock terms convex, so
+    // after at most one overshoot the iterates approach the root monotonically;
+    // Newton in p crawls where a step lands at small p and (p/p_s)^(1/m) is steep.
+    const int m = g64.rm;
+    const float inv_m = 1.f / (float)m;
+    float x = __powf(p, inv_m);
+    for (int it = 0; it < 16; it++) {
+        float xm1 = ipow(x, m - 1);
+        float pp = xm1 * x;
         float fbl, fpl, fbr, fpr;
-        f32_eval(p, L, z, fbl, fpl);
-        f32_eval(p, R, z, fbr, fpr);
-        float dp = (fbl + fbr + dv) / (fpl + fpr);
-        float pn = p - dp;
-        if (!(pn > 0.f)) pn = 0.1f * p;
-        bool done = fabsf(dp) <= 2e-6f * p;
-        p = pn;
+        f32_eval(pp, L, z, fbl, fpl);
+        f32_eval(pp, R, z, fbr, fpr);
+        float dx = (fbl + fbr + dv) / ((fpl + fpr) * (float)m * xm1);
+        float xn = x - dx;
+        if (!(xn > 0.f)) xn = 0.5f * x;
+        bool done = fabsf(dx) <= 1e-6f * x;
+        x = xn;
         if (done) break;
     }
+    p = ipow(x, m);
     // two FP64 Newton steps on the FP64 f
     ExFast L64 = ex_fast_side(ExSide{(double)rl, (double)pl, (double)al}, g64);
     ExFast R64 = ex_fast_side(ExSide{(double)rr, (double)pr, (double)ar}, g64);
@@ -737,7 +746,8 @@ static __device__ __noinline__ Star<float> ex_star_split(float rl, float pl, flo
         P = P - dP;
     }
     Star<float> s;
-    if (!(P > 0.) || !isfinite(P) || !(fabs(dP) <= 1e-9 * P)) {
+    if (!(P > 0.) || !isfinite(P) || !(fabs(dP) <= 1e-8 * P)) {
+        *err |= 1u << 16;  // counted by the face kernel as a fallback face
         Star<double> sd = ex_star_fast(ExSide{(double)rl, (double)pl, (double)al},
                                        ExSide{(double)rr, (double)pr, (double)ar}, (double)vl, (double)vr, g64,
                                        max_iter, err);

@@ -53,7 +53,12 @@ struct DevTimeline {
     unsigned long long steps;
     unsigned long long active_faces;  // cumulative faces that reached flux_exchange*
     unsigned long long active_cells;
+    unsigned long long fallback_faces;  // FP32-face form: faces solved by the full FP64 iteration
 };
+
+// Internal (not exported) flag a face's Riemann solve sets when the FP32-face
+// form's split exact solver fell back to the full FP64 iteration.
+constexpr unsigned int kInfoFallback = 1u << 16;
 
 // Kernel parameters (passed by value).
 struct KP {

@@ -201,10 +201,12 @@ __global__ void __launch_bounds__(kBlock) k_face_flux32(KP p) {
             out[5 * nf + f] = o.v_max;
             out[6 * nf + f] = o.a_over_r;
         }
-        if (err) atomicOr(&p.tl->err, err);
+        if (err & ~kInfoFallback) atomicOr(&p.tl->err, err & ~kInfoFallback);
     }
     unsigned int b = __ballot_sync(0xffffffffu, counted);
+    unsigned int fb = __ballot_sync(0xffffffffu, (err & kInfoFallback) != 0);
     if ((threadIdx.x & 31) == 0 && b) atomicAdd(&p.tl->active_faces, (unsigned long long)__popc(b));
+    if ((threadIdx.x & 31) == 0 && fb) atomicAdd(&p.tl->fallback_faces, (unsigned long long)__popc(fb));
 }
 
 // gradient_estimate + gradient_limit + gradient_apply (runner/hydrodynamics.rs:67-143)
@@ -351,6 +353,7 @@ __global__ void k_riemann32(double gamma, int64_t n, const double* l, const doub
     }
 #pragma unroll
     for (int q = 0; q < 5; q++) out[q * n + i] = (double)o.q[q];
+    err &= ~kInfoFallback;
     if (err) atomicOr(errp, err);
 }
 

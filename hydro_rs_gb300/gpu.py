@@ -24,7 +24,7 @@ EXPORTED = (
     "mvmm_error_bits", "mvmm_last_error", "mvmm_predict", "mvmm_compute_fluxes",
     "mvmm_convert_conserved_to_primitive", "mvmm_compute_timesteps", "mvmm_apply_fluxes", "mvmm_gradients",
     "mvmm_step", "mvmm_run", "mvmm_enqueue_steps", "mvmm_set_time", "mvmm_get_time", "mvmm_profile_enable",
-    "mvmm_profile_read", "mvmm_riemann_flux", "mvmm_riemann_sample",
+    "mvmm_profile_read", "mvmm_riemann_flux", "mvmm_riemann_sample", "mvmm_get_stats",
 )
 
 
@@ -78,6 +78,7 @@ def load_library(path: str = LIB_PATH):
         "mvmm_profile_read": (i32, [vp, vp, vp]),
         "mvmm_riemann_flux": (i32, [i32, i32, dbl, i64, vp, vp, vp, vp, vp]),
         "mvmm_riemann_sample": (i32, [i32, i32, dbl, i64, vp, vp, vp, vp]),
+        "mvmm_get_stats": (i32, [vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -210,6 +211,11 @@ class GpuSim:
                                             ctypes.byref(af), ctypes.byref(fin)), self.h)
         self.ti_current, self.ti_old, self.finished = tc.value, to.value, bool(fin.value)
         return st.value, af.value
+
+    def stats(self) -> dict:
+        a = np.zeros(4, dtype=np.int64)
+        _check(load_library().mvmm_get_stats(self.h, a.ctypes.data), self.h)
+        return dict(zip(("steps", "active_faces", "active_cells", "fp64_fallback_faces"), a.tolist()))
 
     def profile(self, enable: bool):
         _check(load_library().mvmm_profile_enable(self.h, int(enable)), self.h)

@@ -152,6 +152,15 @@ int mvmm_set_time(mvmm_ctx *ctx, uint64_t ti_current, uint64_t ti_old);
 /* Reads the device timeline and counters (synchronises the stream). */
 int mvmm_get_time(mvmm_ctx *ctx, uint64_t *ti_current, uint64_t *ti_old, int64_t *steps, int64_t *active_faces,
                   int *finished);
+/* Counters of the device timeline since the context was created: steps run,
+ * faces that reached flux_exchange*, active cells, and (FP32-face form with
+ * the exact solver) faces whose pressure came from the full FP64 iteration
+ * instead of the FP32 search + FP64 Newton polish.  Synchronises the stream.
+ * No counterpart in the reference (its status line prints step counts only). */
+typedef struct mvmm_stats {
+    int64_t steps, active_faces, active_cells, fp64_fallback_faces;
+} mvmm_stats;
+int mvmm_get_stats(mvmm_ctx *ctx, mvmm_stats *out);
 /* Per-kernel timing of the step (events around each kernel on the context
  * stream): enable, then read the accumulated milliseconds and launch counts
  * of the MVMM_NUM_KERNELS kernels in the order predict, face_flux, update,
