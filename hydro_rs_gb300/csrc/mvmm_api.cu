@@ -54,6 +54,8 @@ struct mvmm_ctx {
     double* flux = nullptr;
     float* flux32 = nullptr;
     double* dtmp = nullptr;
+    uint8_t* face_act = nullptr;
+    int* face_list = nullptr;
     DevTimeline* tl = nullptr;
     DevTimeline* tl_host = nullptr;  // pinned
     cudaStream_t stream = nullptr;
@@ -101,6 +103,11 @@ KP make_kp(mvmm_ctx* c, int stage, int flux_rows) {
     p.time_base = c->time_base;
     p.time_base_inv = c->time_base_inv;
     p.stage = stage;
+    // hierarchical steps walk a compacted active-face list; synchronised steps
+    // (every face active) and per-stage calls sweep all faces
+    p.use_list = (!stage && !c->prm.sync_all) ? 1 : 0;
+    p.face_act = c->face_act;
+    p.face_list = c->face_list;
     return p;
 }
 
@@ -119,6 +126,7 @@ void enqueue_step_kernels(mvmm_ctx* c, bool with_events) {
     cudaStream_t s = c->stream;
     if (with_events) cudaEventRecord(c->ev[0], s);
     launch_predict(p, s);
+    if (p.use_list) launch_compact(p, s);
     if (with_events) cudaEventRecord(c->ev[1], s);
     launch_face(c, p);
     if (with_events) cudaEventRecord(c->ev[2], s);
@@ -281,6 +289,8 @@ int mvmm_ctx_create(const mvmm_params* prm, const mvmm_mesh* m, mvmm_ctx** out) 
     ALLOC(c->active, n);
     ALLOC(c->flux, 10 * nf * 8);
     ALLOC(c->dtmp, n * 8);
+    ALLOC(c->face_act, nf);
+    ALLOC(c->face_list, nf * 4);
     ALLOC(c->tl, sizeof(DevTimeline));
 #undef ALLOC
     if (cudaMallocHost((void**)&c->tl_host, sizeof(DevTimeline)) != cudaSuccess)
@@ -305,6 +315,7 @@ int mvmm_ctx_create(const mvmm_params* prm, const mvmm_mesh* m, mvmm_ctx** out) 
     cudaMemsetAsync(c->tb_tmp, 0, n, s);
     cudaMemsetAsync(c->active, 0, n, s);
     cudaMemsetAsync(c->flux, 0, 10 * nf * 8, s);
+    cudaMemsetAsync(c->face_act, 0, nf, s);
     std::memset(c->tl_host, 0, sizeof(DevTimeline));
     c->tl_host->min_dti = kMax;
     c->tl_host->min_timebin = 127;
@@ -320,7 +331,7 @@ int mvmm_ctx_destroy(mvmm_ctx* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->step_exec) cudaGraphExecDestroy(c->step_exec);
     void* ptrs[] = {c->left, c->right, c->csr_off, c->csr_face, c->area, c->normal, c->fcen, c->shift, c->cd,
-                    c->cf, c->timebin, c->tb_tmp, c->active, c->flux, c->flux32, c->dtmp, c->tl};
+                    c->cf, c->timebin, c->tb_tmp, c->active, c->flux, c->flux32, c->dtmp, c->face_act, c->face_list, c->tl};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (c->tl_host) cudaFreeHost(c->tl_host);

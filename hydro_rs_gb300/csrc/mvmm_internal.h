@@ -54,6 +54,8 @@ struct DevTimeline {
     unsigned long long active_faces;  // cumulative faces that reached flux_exchange*
     unsigned long long active_cells;
     unsigned long long fallback_faces;  // FP32-face form: faces solved by the full FP64 iteration
+    unsigned int n_list;                // length of this step's active-face list (hierarchical steps)
+    unsigned int pad2;
 };
 
 // Internal (not exported) flag a face's Riemann solve sets when the FP32-face
@@ -90,6 +92,9 @@ struct KP {
     double time_base, time_base_inv;
     int stage;               // 1: per-stage call (explicit dt / mask from the host)
     double stage_dt;
+    int use_list;            // 1: face kernel walks the compacted active-face list
+    uint8_t* face_act;       // per-face flag of this step's active-face rule
+    int* face_list;          // compacted active faces
 };
 
 // launchers (implemented in step_fp64.cu / step_fp32.cu)
@@ -101,6 +106,7 @@ void launch_c2p(const KP& p, cudaStream_t s);
 void launch_gradients(const KP& p, int do_timestep, cudaStream_t s);
 void launch_timesteps(const KP& p, double* dt_out, cudaStream_t s);
 void launch_limit(const KP& p, cudaStream_t s);
+void launch_compact(const KP& p, cudaStream_t s);
 void launch_end(const KP& p, cudaStream_t s);
 void launch_riemann(int kind, int precision, int sample, double gamma, int64_t n, const double* l, const double* r,
                     const double* vf, const double* nrm, double* out, unsigned int* err, cudaStream_t s);

@@ -161,52 +161,58 @@ __device__ __forceinline__ Out32 face_boundary32(const KP& p, int f, int i, cons
 template <int SOLVER>
 __global__ void __launch_bounds__(kBlock) k_face_flux32(KP p) {
     if (p.tl->done) return;
-    int f = blockIdx.x * blockDim.x + threadIdx.x;
-    bool counted = false;
-    unsigned int err = 0;
     const Gas<float> g = make_gas<float>(p.gamma, p.eos, p.iso_u);
     const Gas<double> g64 = make_gas<double>(p.gamma, p.eos, p.iso_u);
-    if (f < p.nf) {
-        int l = p.left[f], r = p.right[f];
-        bool la = p.active[l] != 0;
-        Out32 o;
-        if (r >= 0) {
-            bool ra = p.active[r] != 0;
-            double dtl = C(p, F_DT, l), dtr = C(p, F_DT, r);
-            if (!((!la && !ra) || (dtr < dtl && !ra) || (dtl < dtr && !la))) {
-                o = face_interior32<SOLVER>(p, f, l, r, fmin(dtl, dtr), g, g64, &err);
+    const int n_items = p.use_list ? (int)p.tl->n_list : p.nf;
+    for (int base = blockIdx.x * blockDim.x; base < n_items; base += gridDim.x * blockDim.x) {
+        int idx = base + threadIdx.x;
+        int f = idx < n_items ? (p.use_list ? p.face_list[idx] : idx) : -1;
+        bool counted = false;
+        unsigned int err = 0;
+        if (f >= 0) {
+            int l = p.left[f], r = p.right[f];
+            bool la = p.active[l] != 0;
+            Out32 o;
+            if (r >= 0) {
+                bool ra = p.active[r] != 0;
+                double dtl = C(p, F_DT, l), dtr = C(p, F_DT, r);
+                if (!((!la && !ra) || (dtr < dtl && !ra) || (dtl < dtr && !la))) {
+                    o = face_interior32<SOLVER>(p, f, l, r, fmin(dtl, dtr), g, g64, &err);
+                    counted = true;
+                }
+            } else if (la) {
+                o = face_boundary32<SOLVER>(p, f, l, g, g64, &err);
                 counted = true;
             }
-        } else if (la) {
-            o = face_boundary32<SOLVER>(p, f, l, g, g64, &err);
-            counted = true;
-        }
-        if (!counted) {
-            o.fl = st_zero<double>();
-            o.mflux = v3(0., 0., 0.);
-            o.v_max = 0.;
-            o.a_over_r = 0.;
-        }
-        double* out = p.flux;
-        size_t nf = (size_t)p.nf;
+            if (!counted) {
+                o.fl = st_zero<double>();
+                o.mflux = v3(0., 0., 0.);
+                o.v_max = 0.;
+                o.a_over_r = 0.;
+            }
+            double* out = p.flux;
+            size_t nf = (size_t)p.nf;
 #pragma unroll
-        for (int q = 0; q < 5; q++) out[q * nf + f] = o.fl.q[q];
-        if (p.flux_rows == 10) {
-            out[5 * nf + f] = o.mflux.x;
-            out[6 * nf + f] = o.mflux.y;
-            out[7 * nf + f] = o.mflux.z;
-            out[8 * nf + f] = o.v_max;
-            out[9 * nf + f] = o.a_over_r;
-        } else {
-            out[5 * nf + f] = o.v_max;
-            out[6 * nf + f] = o.a_over_r;
+            for (int q = 0; q < 5; q++) out[q * nf + f] = o.fl.q[q];
+            if (p.flux_rows == 10) {
+                out[5 * nf + f] = o.mflux.x;
+                out[6 * nf + f] = o.mflux.y;
+                out[7 * nf + f] = o.mflux.z;
+                out[8 * nf + f] = o.v_max;
+                out[9 * nf + f] = o.a_over_r;
+            } else {
+                out[5 * nf + f] = o.v_max;
+                out[6 * nf + f] = o.a_over_r;
+            }
+            if (err & ~kInfoFallback) atomicOr(&p.tl->err, err & ~kInfoFallback);
         }
-        if (err & ~kInfoFallback) atomicOr(&p.tl->err, err & ~kInfoFallback);
+        unsigned int fb = __ballot_sync(0xffffffffu, (err & kInfoFallback) != 0);
+        if ((threadIdx.x & 31) == 0 && fb) atomicAdd(&p.tl->fallback_faces, (unsigned long long)__popc(fb));
+        if (!p.use_list) {
+            unsigned int b = __ballot_sync(0xffffffffu, counted);
+            if ((threadIdx.x & 31) == 0 && b) atomicAdd(&p.tl->active_faces, (unsigned long long)__popc(b));
+        }
     }
-    unsigned int b = __ballot_sync(0xffffffffu, counted);
-    unsigned int fb = __ballot_sync(0xffffffffu, (err & kInfoFallback) != 0);
-    if ((threadIdx.x & 31) == 0 && b) atomicAdd(&p.tl->active_faces, (unsigned long long)__popc(b));
-    if ((threadIdx.x & 31) == 0 && fb) atomicAdd(&p.tl->fallback_faces, (unsigned long long)__popc(fb));
 }
 
 // gradient_estimate + gradient_limit + gradient_apply (runner/hydrodynamics.rs:67-143)
@@ -371,9 +377,10 @@ void launch_gradients32(const KP& p, cudaStream_t s) {
 
 void launch_face_flux_fp32(const KP& p, int solver, cudaStream_t s) {
     if (p.nf <= 0) return;
-    if (solver == SOLVER_HLLC) k_face_flux32<SOLVER_HLLC><<<grid(p.nf), kBlock, 0, s>>>(p);
-    else if (solver == SOLVER_EXACT) k_face_flux32<SOLVER_EXACT><<<grid(p.nf), kBlock, 0, s>>>(p);
-    else k_face_flux32<SOLVER_PVRS><<<grid(p.nf), kBlock, 0, s>>>(p);
+    int g = p.use_list ? (grid(p.nf) < 152 * 4 ? grid(p.nf) : 152 * 4) : grid(p.nf);
+    if (solver == SOLVER_HLLC) k_face_flux32<SOLVER_HLLC><<<g, kBlock, 0, s>>>(p);
+    else if (solver == SOLVER_EXACT) k_face_flux32<SOLVER_EXACT><<<g, kBlock, 0, s>>>(p);
+    else k_face_flux32<SOLVER_PVRS><<<g, kBlock, 0, s>>>(p);
 }
 
 void launch_riemann_fp32(int kind, int sample, double gamma, int64_t n, const double* l, const double* r,

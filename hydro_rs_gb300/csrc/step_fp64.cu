@@ -206,48 +206,86 @@ __device__ __forceinline__ FaceOut face_boundary(const KP& p, int f, int i, unsi
 template <int SOLVER>
 __global__ void __launch_bounds__(kBlock) k_face_flux(KP p) {
     if (p.tl->done) return;
+    // all faces (one per thread), or the compacted active-face list (grid-stride)
+    const int n_items = p.use_list ? (int)p.tl->n_list : p.nf;
+    for (int base = blockIdx.x * blockDim.x; base < n_items; base += gridDim.x * blockDim.x) {
+        int idx = base + threadIdx.x;
+        int f = idx < n_items ? (p.use_list ? p.face_list[idx] : idx) : -1;
+        bool counted = false;
+        unsigned int err = 0;
+        if (f >= 0) {
+            int l = p.left[f], r = p.right[f];
+            bool la = p.active[l] != 0;
+            FaceOut o;
+            if (r >= 0) {
+                bool ra = p.active[r] != 0;
+                double dtl = C(p, F_DT, l), dtr = C(p, F_DT, r);
+                if (!((!la && !ra) || (dtr < dtl && !ra) || (dtl < dtr && !la))) {
+                    o = face_interior<SOLVER>(p, f, l, r, m_min(dtl, dtr), &err);
+                    counted = true;
+                }
+            } else if (la) {
+                o = face_boundary<SOLVER>(p, f, l, &err);
+                counted = true;
+            }
+            if (!counted) {
+                o.fl = st_zero<double>();
+                o.mflux = v3(0., 0., 0.);
+                o.v_max = 0.;
+                o.a_over_r = 0.;
+            }
+            double* out = p.flux;
+            size_t nf = (size_t)p.nf;
+#pragma unroll
+            for (int q = 0; q < 5; q++) out[q * nf + f] = o.fl.q[q];
+            if (p.flux_rows == 10) {
+                out[5 * nf + f] = o.mflux.x;
+                out[6 * nf + f] = o.mflux.y;
+                out[7 * nf + f] = o.mflux.z;
+                out[8 * nf + f] = o.v_max;
+                out[9 * nf + f] = o.a_over_r;
+            } else {
+                out[5 * nf + f] = o.v_max;
+                out[6 * nf + f] = o.a_over_r;
+            }
+            if (err) set_err(p, err);
+        }
+        if (!p.use_list) {  // list mode counts the list length in k_end
+            unsigned int b = __ballot_sync(0xffffffffu, counted);
+            if ((threadIdx.x & 31) == 0 && b) atomicAdd(&p.tl->active_faces, (unsigned long long)__popc(b));
+        }
+    }
+}
+
+// Per-time-bin active-face list (hierarchical steps): applies the active-face
+// rule of compute_fluxes (euler_eqns_fvs.rs:35-45) to every face, flags it and
+// appends the active ones to a list with warp-aggregated atomics.  The list
+// order is arbitrary; each face writes only its own result rows, so results do
+// not depend on it.
+__global__ void __launch_bounds__(kBlock) k_compact(KP p) {
+    if (p.tl->done) return;
     int f = blockIdx.x * blockDim.x + threadIdx.x;
-    bool counted = false;
-    unsigned int err = 0;
+    bool act = false;
     if (f < p.nf) {
         int l = p.left[f], r = p.right[f];
         bool la = p.active[l] != 0;
-        FaceOut o;
         if (r >= 0) {
             bool ra = p.active[r] != 0;
             double dtl = C(p, F_DT, l), dtr = C(p, F_DT, r);
-            if (!((!la && !ra) || (dtr < dtl && !ra) || (dtl < dtr && !la))) {
-                o = face_interior<SOLVER>(p, f, l, r, m_min(dtl, dtr), &err);
-                counted = true;
-            }
-        } else if (la) {
-            o = face_boundary<SOLVER>(p, f, l, &err);
-            counted = true;
-        }
-        if (!counted) {
-            o.fl = st_zero<double>();
-            o.mflux = v3(0., 0., 0.);
-            o.v_max = 0.;
-            o.a_over_r = 0.;
-        }
-        double* out = p.flux;
-        size_t nf = (size_t)p.nf;
-#pragma unroll
-        for (int q = 0; q < 5; q++) out[q * nf + f] = o.fl.q[q];
-        if (p.flux_rows == 10) {
-            out[5 * nf + f] = o.mflux.x;
-            out[6 * nf + f] = o.mflux.y;
-            out[7 * nf + f] = o.mflux.z;
-            out[8 * nf + f] = o.v_max;
-            out[9 * nf + f] = o.a_over_r;
+            act = !((!la && !ra) || (dtr < dtl && !ra) || (dtl < dtr && !la));
         } else {
-            out[5 * nf + f] = o.v_max;
-            out[6 * nf + f] = o.a_over_r;
+            act = la;
         }
-        if (err) set_err(p, err);
+        p.face_act[f] = act;
     }
-    unsigned int b = __ballot_sync(0xffffffffu, counted);
-    if ((threadIdx.x & 31) == 0 && b) atomicAdd(&p.tl->active_faces, (unsigned long long)__popc(b));
+    unsigned int b = __ballot_sync(0xffffffffu, act);
+    if (!b) return;
+    int lane = threadIdx.x & 31;
+    int leader = __ffs(b) - 1;
+    unsigned int start = 0;
+    if (lane == leader) start = atomicAdd(&p.tl->n_list, (unsigned int)__popc(b));
+    start = __shfl_sync(0xffffffffu, start, leader);
+    if (act) p.face_list[start + __popc(b & ((1u << lane) - 1u))] = f;
 }
 
 // ---------------------------------------------------- cons -> primitive --
@@ -295,6 +333,8 @@ __global__ void __launch_bounds__(kBlock) k_update(KP p, int do_c2p) {
     int k0 = p.csr_off[i], k1 = p.csr_off[i + 1];
     for (int k = k0; k < k1; k++) {
         int f = p.csr_face[k];
+        // an inactive face carries FluxInfo::zero(): adding it changes nothing
+        if (p.use_list && !p.face_act[f]) continue;
         St<double> x;
 #pragma unroll
         for (int q = 0; q < 5; q++) x.q[q] = fl[q * nf + f];
@@ -555,6 +595,8 @@ __global__ void k_end(KP p) {
     tl->ti_current = tn;
     tl->min_dti = MAX_NR_TIMESTEPS;
     tl->min_timebin = 127;
+    tl->active_faces += tl->n_list;  // list mode: the list is this step's active faces
+    tl->n_list = 0;
 }
 
 // ---------------------------------------------- Riemann over arrays --
@@ -594,11 +636,18 @@ void launch_predict(const KP& p, cudaStream_t s) {
 void launch_derive(const KP& p, cudaStream_t s) {
     if (p.n > 0) k_derive<<<grid(p.n), kBlock, 0, s>>>(p);
 }
+// list mode: a grid of a few waves walks the list (its length is only known on the device)
+inline int face_grid(const KP& p) { return p.use_list ? (grid(p.nf) < 152 * 4 ? grid(p.nf) : 152 * 4) : grid(p.nf); }
+
 void launch_face_flux_fp64(const KP& p, int solver, cudaStream_t s) {
     if (p.nf <= 0) return;
-    if (solver == SOLVER_HLLC) k_face_flux<SOLVER_HLLC><<<grid(p.nf), kBlock, 0, s>>>(p);
-    else if (solver == SOLVER_EXACT) k_face_flux<SOLVER_EXACT><<<grid(p.nf), kBlock, 0, s>>>(p);
-    else k_face_flux<SOLVER_PVRS><<<grid(p.nf), kBlock, 0, s>>>(p);
+    int g = face_grid(p);
+    if (solver == SOLVER_HLLC) k_face_flux<SOLVER_HLLC><<<g, kBlock, 0, s>>>(p);
+    else if (solver == SOLVER_EXACT) k_face_flux<SOLVER_EXACT><<<g, kBlock, 0, s>>>(p);
+    else k_face_flux<SOLVER_PVRS><<<g, kBlock, 0, s>>>(p);
+}
+void launch_compact(const KP& p, cudaStream_t s) {
+    if (p.nf > 0) k_compact<<<grid(p.nf), kBlock, 0, s>>>(p);
 }
 void launch_update(const KP& p, int do_c2p, cudaStream_t s) {
     if (p.n > 0) k_update<<<grid(p.n), kBlock, 0, s>>>(p, do_c2p);
