@@ -34,7 +34,6 @@ sys.path.insert(0, ROOT)
 
 METRIC = "active-face updates/s"
 UNIT = "faces/s"
-WORKLOAD = "kelvin_helmholtz_2d 256x256 jittered periodic Voronoi, exact Riemann solver, gamma=5/3"
 NX = 256
 L2_FLUSH_BYTES = 256 << 20
 
@@ -60,15 +59,31 @@ def _peaks():
         return 6800.0, "fallback"
 
 
-def _problem(nx=NX):
+WORKLOADS = {
+    # the headline: 2D shear layer, 256^2 jittered lattice, exact solver, all cells active
+    "kh2d": "kelvin_helmholtz_2d {n}x{n} jittered periodic Voronoi, exact Riemann solver, gamma=5/3",
+    # 1D Sod shock tube, reflective walls, HLLC, synchronised steps
+    "sod1d": "sod_1d {n} cells, reflective, HLLC, gamma=5/3",
+    # 3D point blast, 128^3 jittered lattice, HLLC, hierarchical time bins
+    "blast3d": "point_blast_3d {n}^3 jittered periodic Voronoi, HLLC, hierarchical time bins, gamma=5/3",
+}
+DEFAULT_N = {"kh2d": NX, "sod1d": 1000, "blast3d": 128}
+
+
+def _problem(nx=NX, workload="kh2d"):
     from hydro_rs_gb300 import ics
 
     t0 = time.perf_counter()
-    p = ics.kelvin_helmholtz_2d(nx, seed=2, riemann=ics.EXACT, t_end=1.5)
+    if workload == "sod1d":
+        p = ics.sod_1d(nx)
+    elif workload == "blast3d":
+        p = ics.point_blast_3d(nx, seed=3, riemann=ics.HLLC, t_end=0.05, sync_all=False)
+    else:
+        p = ics.kelvin_helmholtz_2d(nx, seed=2, riemann=ics.EXACT, t_end=1.5)
     return p, time.perf_counter() - t0
 
 
-def _cpu_sample(problem, budget_s: float = 10.0, max_steps: int = 400):
+def _cpu_sample(problem, label, budget_s: float = 10.0, max_steps: int = 400):
     """The oracle on the host cores: warm-up step, then steps until the budget."""
     from oracle import oracle as O
 
@@ -87,7 +102,7 @@ def _cpu_sample(problem, budget_s: float = 10.0, max_steps: int = 400):
     dt = time.perf_counter() - t0
     faces = sim.active_faces - f0
     return {"value": faces / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{n} OptimalOrder steps of the same 256x256 exact-solver workload ({faces} face updates, "
+            "sample": f"{n} OptimalOrder steps of the same workload ({label}; {faces} face updates, "
                       f"{dt:.1f} s wall) after 2 warm-up steps; C restatement of the reference, OpenMP"}
 
 
@@ -182,7 +197,7 @@ def run_ours(args):
         import torch.distributed as dist
 
         dist.init_process_group("nccl")
-    problem, mesh_s = _problem(args.nx)
+    problem, mesh_s = _problem(args.nx, args.workload)
     nf, nc = problem.mesh.n_faces, problem.mesh.n_cells
     stream = torch.cuda.Stream()
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
@@ -276,17 +291,18 @@ def run_ours(args):
                 "peak_kind": peak_kind, "note": "of measured" if peak_kind == "measured" else "of fallback",
                 "step_kernel_ms": {k: round(v[0] / max(v[1], 1), 4) for k, v in prof[prec].items()}}
 
-    cpu = _cpu_sample(problem) if (ws == 1 and not args.no_cpu) else None
+    cpu = _cpu_sample(problem, WORKLOADS[args.workload].format(n=args.nx)) if (ws == 1 and not args.no_cpu) else None
     value = faces32 / (ms32 * 1e-3)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms32 / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32-face/f64-accumulate", "data": "synthetic (seeded jittered lattice, shear-layer ICs)",
-        "config": {"workload": WORKLOAD if args.nx == NX else WORKLOAD.replace("256x256", f"{args.nx}x{args.nx}"),
+        "config": {"workload": WORKLOADS[args.workload].format(n=args.nx),
                    "cells": nc, "faces": nf, "precision": "fp32_face",
                    "l2": "flushed (256 MB write) before each timed step", "parallelism": f"replicas x{ws}",
                    "mesh_build_s": round(mesh_s, 3)},
         "l1_density_err_vs_fp64": l1, "l1_same_time": same_time,
+        "active_face_fraction": faces32 / (args.steps * nf * ws),
         "plain_fp64": {"value": faces64 / (ms64 * 1e-3), "unit": UNIT, "ms_per_step": ms64 / args.steps,
                        "roofline": roof(0)},
         "roofline": roof(1),
@@ -304,7 +320,7 @@ def run_reference(args):
     ws, rank = _dist()
     if rank != 0:
         return
-    problem, _ = _problem()
+    problem, _ = _problem(args.nx, args.workload)
     from oracle import oracle as O
 
     threads = os.cpu_count() or 1
@@ -322,7 +338,8 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded jittered lattice, shear-layer ICs)",
-        "config": {"workload": WORKLOAD, "cells": problem.mesh.n_cells, "faces": problem.mesh.n_faces},
+        "config": {"workload": WORKLOADS[args.workload].format(n=args.nx), "cells": problem.mesh.n_cells,
+                   "faces": problem.mesh.n_faces},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{args.steps} steps after {2 + args.warmup} warm-up steps; the Rust reference "
                                    "cannot be built here (no cargo/rustc), the C restatement runs instead"},
@@ -337,10 +354,14 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--nx", type=int, default=NX, help="lattice side (profiling captures of other sizes)")
+    ap.add_argument("--workload", default="kh2d", choices=sorted(WORKLOADS),
+                    help="kh2d (the headline), sod1d, blast3d (extra measurements)")
+    ap.add_argument("--nx", type=int, default=None, help="lattice side / cell count (default per workload)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg (profiling runs)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.nx is None:
+        args.nx = DEFAULT_N[args.workload]
     if args.impl == "reference":
         run_reference(args)
     else:
