@@ -54,10 +54,14 @@ struct mvmm_ctx {
     double* flux = nullptr;
     float* flux32 = nullptr;
     double* dtmp = nullptr;
+    int n_inst = 1;
+    int* inst = nullptr;       // per-cell instance (batches only)
+    double* inst_tb = nullptr;  // per-instance time_base, 1/time_base (batches only)
+    double* inst_tbi = nullptr;
     uint8_t* face_act = nullptr;
     int* face_list = nullptr;
-    DevTimeline* tl = nullptr;
-    DevTimeline* tl_host = nullptr;  // pinned
+    DevTimeline* tl = nullptr;       // [n_inst]
+    DevTimeline* tl_host = nullptr;  // pinned [n_inst]
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     cudaGraphExec_t step_exec = nullptr;
@@ -103,9 +107,13 @@ KP make_kp(mvmm_ctx* c, int stage, int flux_rows) {
     p.time_base = c->time_base;
     p.time_base_inv = c->time_base_inv;
     p.stage = stage;
-    // hierarchical steps walk a compacted active-face list; synchronised steps
-    // (every face active) and per-stage calls sweep all faces
-    p.use_list = (!stage && !c->prm.sync_all) ? 1 : 0;
+    p.inst = c->inst;
+    p.n_inst = c->n_inst;
+    p.inst_tb = c->inst_tb;
+    p.inst_tbi = c->inst_tbi;
+    // hierarchical steps of a single simulation walk a compacted active-face
+    // list; synchronised steps, batches and per-stage calls sweep all faces
+    p.use_list = (!stage && !c->prm.sync_all && c->n_inst == 1) ? 1 : 0;
     p.face_act = c->face_act;
     p.face_list = c->face_list;
     return p;
@@ -175,14 +183,25 @@ int enqueue_steps_impl(mvmm_ctx* c, int64_t n) {
 }
 
 int read_tl(mvmm_ctx* c) {
-    CUDA_TRY(cudaMemcpyAsync(c->tl_host, c->tl, sizeof(DevTimeline), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(cudaMemcpyAsync(c->tl_host, c->tl, sizeof(DevTimeline) * c->n_inst, cudaMemcpyDeviceToHost, c->stream));
     CUDA_TRY(cudaStreamSynchronize(c->stream));
     return MVMM_OK;
 }
 
 int write_tl(mvmm_ctx* c) {
-    CUDA_TRY(cudaMemcpyAsync(c->tl, c->tl_host, sizeof(DevTimeline), cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(cudaMemcpyAsync(c->tl, c->tl_host, sizeof(DevTimeline) * c->n_inst, cudaMemcpyHostToDevice, c->stream));
     return MVMM_OK;
+}
+
+bool all_done(const mvmm_ctx* c) {
+    for (int k = 0; k < c->n_inst; k++)
+        if (!c->tl_host[k].done) return false;
+    return true;
+}
+unsigned long long sum_field(const mvmm_ctx* c, unsigned long long DevTimeline::*f) {
+    unsigned long long s = 0;
+    for (int k = 0; k < c->n_inst; k++) s += c->tl_host[k].*f;
+    return s;
 }
 
 // Host-side checks standing in for device bounds checks: every index the
@@ -223,7 +242,8 @@ int check_mesh(const mvmm_mesh* m, int boundary) {
 int finish(mvmm_ctx* c) {
     int rc = read_tl(c);
     if (rc) return rc;
-    uint32_t bits = c->tl_host->err;
+    uint32_t bits = 0;
+    for (int k = 0; k < c->n_inst; k++) bits |= c->tl_host[k].err;
     if (bits & ~c->err_bits) {
         c->err_bits |= bits;
         char buf[96];
@@ -240,7 +260,8 @@ extern "C" {
 
 const char* mvmm_last_error(void) { return g_last_error.c_str(); }
 
-int mvmm_ctx_create(const mvmm_params* prm, const mvmm_mesh* m, mvmm_ctx** out) {
+static int create_impl(const mvmm_params* prm, const mvmm_mesh* m, int64_t n_inst, const int64_t* cell_off,
+                       const double* t_end, mvmm_ctx** out) {
     if (!prm || !out) return fail(MVMM_E_INVALID, "null argument");
     *out = nullptr;
     if (!(prm->gamma > 1.0)) return fail(MVMM_E_INVALID, "gamma must be > 1");
@@ -254,8 +275,26 @@ int mvmm_ctx_create(const mvmm_params* prm, const mvmm_mesh* m, mvmm_ctx** out) 
     if (!(prm->t_end > 0.0)) return fail(MVMM_E_INVALID, "t_end must be > 0");
     int rc = check_mesh(m, prm->boundary);
     if (rc) return rc;
+    std::vector<int32_t> inst_h;
+    if (n_inst > 1) {
+        if (!cell_off || !t_end) return fail(MVMM_E_INVALID, "batch: null offsets or t_end");
+        if (n_inst > (1 << 24)) return fail(MVMM_E_INVALID, "batch: too many instances");
+        if (cell_off[0] != 0 || cell_off[n_inst] != m->n_cells) return fail(MVMM_E_INVALID, "batch: offsets must span the cells");
+        inst_h.resize(m->n_cells);
+        for (int64_t k = 0; k < n_inst; k++) {
+            if (cell_off[k + 1] < cell_off[k]) return fail(MVMM_E_INVALID, "batch: offsets not monotone");
+            if (!(t_end[k] > 0.0)) return fail(MVMM_E_INVALID, "batch: t_end must be > 0");
+            for (int64_t i = cell_off[k]; i < cell_off[k + 1]; i++) inst_h[i] = (int32_t)k;
+        }
+        for (int64_t f = 0; f < m->n_faces; f++)
+            if (m->right[f] >= 0 && inst_h[m->left[f]] != inst_h[m->right[f]])
+                return fail(MVMM_E_INVALID, "batch: a face joins two instances");
+    } else {
+        n_inst = 1;
+    }
     mvmm_ctx* c = new mvmm_ctx();
     c->prm = *prm;
+    c->n_inst = (int)n_inst;
     c->n = (int)m->n_cells;
     c->nf = (int)m->n_faces;
     c->ncsr = m->csr_off[m->n_cells];
@@ -291,9 +330,14 @@ int mvmm_ctx_create(const mvmm_params* prm, const mvmm_mesh* m, mvmm_ctx** out) 
     ALLOC(c->dtmp, n * 8);
     ALLOC(c->face_act, nf);
     ALLOC(c->face_list, nf * 4);
-    ALLOC(c->tl, sizeof(DevTimeline));
+    ALLOC(c->tl, sizeof(DevTimeline) * c->n_inst);
+    if (c->n_inst > 1) {
+        ALLOC(c->inst, n * 4);
+        ALLOC(c->inst_tb, c->n_inst * 8);
+        ALLOC(c->inst_tbi, c->n_inst * 8);
+    }
 #undef ALLOC
-    if (cudaMallocHost((void**)&c->tl_host, sizeof(DevTimeline)) != cudaSuccess)
+    if (cudaMallocHost((void**)&c->tl_host, sizeof(DevTimeline) * c->n_inst) != cudaSuccess)
         return cleanup(MVMM_E_NOMEM, "cudaMallocHost failed");
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
         return cleanup(MVMM_E_CUDA, "cudaStreamCreate failed");
@@ -316,13 +360,59 @@ int mvmm_ctx_create(const mvmm_params* prm, const mvmm_mesh* m, mvmm_ctx** out) 
     cudaMemsetAsync(c->active, 0, n, s);
     cudaMemsetAsync(c->flux, 0, 10 * nf * 8, s);
     cudaMemsetAsync(c->face_act, 0, nf, s);
-    std::memset(c->tl_host, 0, sizeof(DevTimeline));
-    c->tl_host->min_dti = kMax;
-    c->tl_host->min_timebin = 127;
-    cudaMemcpyAsync(c->tl, c->tl_host, sizeof(DevTimeline), cudaMemcpyHostToDevice, s);
+    std::memset(c->tl_host, 0, sizeof(DevTimeline) * c->n_inst);
+    for (int k = 0; k < c->n_inst; k++) {
+        c->tl_host[k].min_dti = kMax;
+        c->tl_host[k].min_timebin = 127;
+    }
+    cudaMemcpyAsync(c->tl, c->tl_host, sizeof(DevTimeline) * c->n_inst, cudaMemcpyHostToDevice, s);
+    std::vector<double> tb, tbi;
+    if (c->n_inst > 1) {
+        tb.resize(c->n_inst);
+        tbi.resize(c->n_inst);
+        for (int k = 0; k < c->n_inst; k++) {
+            tb[k] = t_end[k] / (double)kMax;  // Engine::new per simulation (engine.rs:118-119)
+            tbi[k] = 1. / tb[k];
+        }
+        cudaMemcpyAsync(c->inst, inst_h.data(), n * 4, cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(c->inst_tb, tb.data(), c->n_inst * 8, cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(c->inst_tbi, tbi.data(), c->n_inst * 8, cudaMemcpyHostToDevice, s);
+    }
     cudaError_t e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return cleanup(MVMM_E_CUDA, std::string("mesh upload: ") + cudaGetErrorString(e));
     *out = c;
+    return MVMM_OK;
+}
+
+int mvmm_ctx_create(const mvmm_params* prm, const mvmm_mesh* m, mvmm_ctx** out) {
+    return create_impl(prm, m, 1, nullptr, nullptr, out);
+}
+
+int mvmm_ctx_create_batched(const mvmm_params* prm, const mvmm_mesh* m, int64_t n_instances,
+                            const int64_t* cell_offsets, const double* t_end, mvmm_ctx** out) {
+    if (n_instances < 1) return fail(MVMM_E_INVALID, "batch: n_instances must be >= 1");
+    if (n_instances == 1) {
+        mvmm_params q = *prm;
+        if (t_end) q.t_end = t_end[0];
+        return create_impl(&q, m, 1, nullptr, nullptr, out);
+    }
+    return create_impl(prm, m, n_instances, cell_offsets, t_end, out);
+}
+
+int mvmm_batch_state(mvmm_ctx* c, uint64_t* ti_current, uint64_t* ti_old, int64_t* steps, int64_t* active_faces,
+                     uint32_t* err_bits, int* finished) {
+    if (!c) return fail(MVMM_E_INVALID, "null context");
+    int rc = read_tl(c);
+    if (rc) return rc;
+    for (int k = 0; k < c->n_inst; k++) {
+        const DevTimeline& t = c->tl_host[k];
+        if (ti_current) ti_current[k] = t.ti_current;
+        if (ti_old) ti_old[k] = t.ti_old;
+        if (steps) steps[k] = (int64_t)t.steps;
+        if (active_faces) active_faces[k] = (int64_t)t.active_faces;
+        if (err_bits) err_bits[k] = t.err;
+        if (finished) finished[k] = t.done;
+    }
     return MVMM_OK;
 }
 
@@ -331,7 +421,8 @@ int mvmm_ctx_destroy(mvmm_ctx* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->step_exec) cudaGraphExecDestroy(c->step_exec);
     void* ptrs[] = {c->left, c->right, c->csr_off, c->csr_face, c->area, c->normal, c->fcen, c->shift, c->cd,
-                    c->cf, c->timebin, c->tb_tmp, c->active, c->flux, c->flux32, c->dtmp, c->face_act, c->face_list, c->tl};
+                    c->cf, c->timebin, c->tb_tmp, c->active, c->flux, c->flux32, c->dtmp, c->face_act, c->face_list, c->tl,
+                    c->inst, c->inst_tb, c->inst_tbi};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (c->tl_host) cudaFreeHost(c->tl_host);
@@ -423,7 +514,7 @@ int mvmm_compute_fluxes(mvmm_ctx* c, const uint8_t* active, double* out, int64_t
     if (rc) return rc;
     rc = read_tl(c);
     if (rc) return rc;
-    unsigned long long before = c->tl_host->active_faces;
+    unsigned long long before = sum_field(c, &DevTimeline::active_faces);
     KP p = make_kp(c, 1, 10);
     launch_derive(p, c->stream);
     launch_face(c, p);
@@ -431,7 +522,7 @@ int mvmm_compute_fluxes(mvmm_ctx* c, const uint8_t* active, double* out, int64_t
     if (c->nf > 0)
         CUDA_TRY(cudaMemcpyAsync(out, c->flux, (size_t)10 * c->nf * 8, cudaMemcpyDeviceToHost, c->stream));
     rc = finish(c);
-    if (n_active) *n_active = (int64_t)(c->tl_host->active_faces - before);
+    if (n_active) *n_active = (int64_t)(sum_field(c, &DevTimeline::active_faces) - before);
     return rc;
 }
 
@@ -480,11 +571,13 @@ int mvmm_set_time(mvmm_ctx* c, uint64_t ti_current, uint64_t ti_old) {
     if (!c) return fail(MVMM_E_INVALID, "null context");
     int rc = read_tl(c);
     if (rc) return rc;
-    c->tl_host->ti_current = ti_current;
-    c->tl_host->ti_old = ti_old;
-    c->tl_host->min_dti = kMax;
-    c->tl_host->min_timebin = 127;
-    c->tl_host->done = 0;
+    for (int k = 0; k < c->n_inst; k++) {  // a batch restarts every simulation at the same point
+        c->tl_host[k].ti_current = ti_current;
+        c->tl_host[k].ti_old = ti_old;
+        c->tl_host[k].min_dti = kMax;
+        c->tl_host[k].min_timebin = 127;
+        c->tl_host[k].done = 0;
+    }
     rc = write_tl(c);
     if (rc) return rc;
     CUDA_TRY(cudaStreamSynchronize(c->stream));
@@ -499,8 +592,8 @@ int mvmm_get_time(mvmm_ctx* c, uint64_t* ti_current, uint64_t* ti_old, int64_t* 
     if (ti_current) *ti_current = c->tl_host->ti_current;
     if (ti_old) *ti_old = c->tl_host->ti_old;
     if (steps) *steps = (int64_t)c->tl_host->steps;
-    if (active_faces) *active_faces = (int64_t)c->tl_host->active_faces;
-    if (finished) *finished = c->tl_host->done;
+    if (active_faces) *active_faces = (int64_t)sum_field(c, &DevTimeline::active_faces);
+    if (finished) *finished = all_done(c) ? 1 : 0;
     return MVMM_OK;
 }
 
@@ -508,23 +601,24 @@ int mvmm_get_stats(mvmm_ctx* c, mvmm_stats* out) {
     if (!c || !out) return fail(MVMM_E_INVALID, "null argument");
     int rc = read_tl(c);
     if (rc) return rc;
-    out->steps = (int64_t)c->tl_host->steps;
-    out->active_faces = (int64_t)c->tl_host->active_faces;
-    out->active_cells = (int64_t)c->tl_host->active_cells;
-    out->fp64_fallback_faces = (int64_t)c->tl_host->fallback_faces;
+    out->steps = (int64_t)sum_field(c, &DevTimeline::steps);
+    out->active_faces = (int64_t)sum_field(c, &DevTimeline::active_faces);
+    out->active_cells = (int64_t)sum_field(c, &DevTimeline::active_cells);
+    out->fp64_fallback_faces = (int64_t)sum_field(c, &DevTimeline::fallback_faces);
     return MVMM_OK;
 }
 
 int mvmm_step(mvmm_ctx* c, uint64_t ti_current, uint64_t ti_old, uint64_t* ti_next, int64_t* n_active_faces) {
     if (!c) return fail(MVMM_E_INVALID, "null context");
-    int rc = mvmm_set_time(c, ti_current, ti_old);
+    // a batch continues every simulation from its own device timeline
+    int rc = c->n_inst == 1 ? mvmm_set_time(c, ti_current, ti_old) : read_tl(c);
     if (rc) return rc;
-    unsigned long long before = c->tl_host->active_faces;
+    unsigned long long before = sum_field(c, &DevTimeline::active_faces);
     rc = enqueue_steps_impl(c, 1);
     if (rc) return rc;
     rc = finish(c);
     if (ti_next) *ti_next = c->tl_host->ti_current;
-    if (n_active_faces) *n_active_faces = (int64_t)(c->tl_host->active_faces - before);
+    if (n_active_faces) *n_active_faces = (int64_t)(sum_field(c, &DevTimeline::active_faces) - before);
     return rc;
 }
 
@@ -536,11 +630,12 @@ int mvmm_enqueue_steps(mvmm_ctx* c, int64_t n_steps) {
 int mvmm_run(mvmm_ctx* c, int64_t max_steps, uint64_t* ti_current, uint64_t* ti_old, int64_t* steps_done,
              int64_t* n_active_faces, int* finished) {
     if (!c || !ti_current || !ti_old) return fail(MVMM_E_INVALID, "null argument");
-    int rc = mvmm_set_time(c, *ti_current, *ti_old);
+    int rc = c->n_inst == 1 ? mvmm_set_time(c, *ti_current, *ti_old) : read_tl(c);
     if (rc) return rc;
-    unsigned long long s0 = c->tl_host->steps, f0 = c->tl_host->active_faces;
+    unsigned long long s0 = c->tl_host->steps, f0 = sum_field(c, &DevTimeline::active_faces);
     const int64_t chunk = 64;
     int64_t launched = 0;
+    int numeric = MVMM_OK;
     for (;;) {
         int64_t k = chunk;
         if (max_steps > 0 && launched + k > max_steps) k = max_steps - launched;
@@ -549,16 +644,23 @@ int mvmm_run(mvmm_ctx* c, int64_t max_steps, uint64_t* ti_current, uint64_t* ti_
         if (rc) return rc;
         launched += k;
         rc = finish(c);
+        // a batch runs on when one simulation fails (it stops, see k_end);
+        // the failure is returned at the end, per-simulation bits in mvmm_batch_state
+        if (rc == MVMM_E_NUMERIC && c->n_inst > 1) {
+            numeric = rc;
+            rc = MVMM_OK;
+        }
         if (rc) break;
-        if (c->tl_host->done) break;
+        if (all_done(c)) break;
     }
+    if (!rc && numeric) rc = fail(numeric, "numerical failure in at least one simulation of the batch");
     int rc2 = read_tl(c);
     if (rc2) return rc2;
     *ti_current = c->tl_host->ti_current;
     *ti_old = c->tl_host->ti_old;
     if (steps_done) *steps_done = (int64_t)(c->tl_host->steps - s0);
-    if (n_active_faces) *n_active_faces = (int64_t)(c->tl_host->active_faces - f0);
-    if (finished) *finished = c->tl_host->done;
+    if (n_active_faces) *n_active_faces = (int64_t)(sum_field(c, &DevTimeline::active_faces) - f0);
+    if (finished) *finished = all_done(c) ? 1 : 0;
     return rc;
 }
 

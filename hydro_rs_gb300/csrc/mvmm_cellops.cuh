@@ -33,8 +33,37 @@ __device__ __forceinline__ void W5(const KP& p, int f, int i, const St<double>& 
 }
 __device__ __forceinline__ V3<double> F3(const double* a, int nf, int f) { return {a[f], a[nf + f], a[2 * nf + f]}; }
 __device__ __forceinline__ Gas<double> gas(const KP& p) { return make_gas<double>(p.gamma, p.eos, p.iso_u); }
-__device__ __forceinline__ void set_err(const KP& p, unsigned int bits) {
-    if (bits) atomicOr(&p.tl->err, bits);
+__device__ __forceinline__ int inst_of(const KP& p, int cell) { return p.inst ? p.inst[cell] : 0; }
+__device__ __forceinline__ double tbase(const KP& p, int k) { return p.inst_tb ? p.inst_tb[k] : p.time_base; }
+__device__ __forceinline__ double tbase_inv(const KP& p, int k) { return p.inst_tbi ? p.inst_tbi[k] : p.time_base_inv; }
+__device__ __forceinline__ void set_err(const KP& p, int k, unsigned int bits) {
+    if (bits) atomicOr(&p.tl[k].err, bits);
+}
+// Counter add per instance, aggregated over the lanes of a warp that share an
+// instance (k < 0: the lane contributes nothing).  Every lane of the warp calls it.
+enum { CNT_FACES = 0, CNT_CELLS = 1, CNT_FALLBACK = 2 };
+__device__ __forceinline__ void inst_count(const KP& p, int k, bool flag, int which) {
+    unsigned int grp = __match_any_sync(0xffffffffu, k);
+    unsigned int cnt = __popc(__ballot_sync(0xffffffffu, flag) & grp);
+    if (k >= 0 && cnt && (int)(threadIdx.x & 31) == __ffs(grp) - 1) {
+        DevTimeline* T = p.tl + k;
+        unsigned long long* c = which == CNT_FACES ? &T->active_faces
+                                : which == CNT_CELLS ? &T->active_cells : &T->fallback_faces;
+        atomicAdd(c, (unsigned long long)cnt);
+    }
+}
+// Per-instance minima of the integer timestep and the new time bin
+// (timesteps_apply / timestep_sync reductions).  dti is 0 or a power of two
+// (make_integer_timestep), so its bit index is an order-preserving 32-bit key.
+__device__ __forceinline__ void inst_min_dti_tb(const KP& p, int k, unsigned long long dti, int tb) {
+    unsigned int grp = __match_any_sync(0xffffffffu, k);
+    unsigned int key = dti == 0 ? 0u : (unsigned int)(64 - __clzll((long long)dti));
+    unsigned int kmin = __reduce_min_sync(grp, key);
+    int tbmin = __reduce_min_sync(grp, tb);
+    if (k >= 0 && (int)(threadIdx.x & 31) == __ffs(grp) - 1) {
+        atomicMin(&p.tl[k].min_dti, kmin == 0 ? 0ull : (1ull << (kmin - 1)));
+        atomicMin(&p.tl[k].min_timebin, tbmin);
+    }
 }
 
 // Gradients::dot row q with dx (physical_quantities.rs:122-133)

@@ -92,6 +92,12 @@ struct KP {
     double time_base, time_base_inv;
     int stage;               // 1: per-stage call (explicit dt / mask from the host)
     double stage_dt;
+    // batches: many independent simulations packed into one mesh; each has its
+    // own device timeline tl[k] (k = inst[cell]) and time base
+    const int* inst;         // per-cell instance index, nullptr for a single simulation
+    int n_inst;
+    const double* inst_tb;   // per-instance time_base (nullptr: time_base)
+    const double* inst_tbi;  // per-instance 1 / time_base (nullptr: time_base_inv)
     int use_list;            // 1: face kernel walks the compacted active-face list
     uint8_t* face_act;       // per-face flag of this step's active-face rule
     int* face_list;          // compacted active faces

@@ -21,9 +21,9 @@ __device__ __forceinline__ St<float> G5(const KP& p, int f, int i) {
     return s;
 }
 __global__ void __launch_bounds__(kBlock) k_prep32(KP p) {
-    if (p.tl->done) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
+    if (p.tl[inst_of(p, i)].done) return;
     size_t n = p.n;
     float* cf = p.cf;
 #pragma unroll
@@ -160,16 +160,18 @@ __device__ __forceinline__ Out32 face_boundary32(const KP& p, int f, int i, cons
 
 template <int SOLVER>
 __global__ void __launch_bounds__(kBlock) k_face_flux32(KP p) {
-    if (p.tl->done) return;
+    if (p.use_list && p.tl[0].done) return;
     const Gas<float> g = make_gas<float>(p.gamma, p.eos, p.iso_u);
     const Gas<double> g64 = make_gas<double>(p.gamma, p.eos, p.iso_u);
-    const int n_items = p.use_list ? (int)p.tl->n_list : p.nf;
+    const int n_items = p.use_list ? (int)p.tl[0].n_list : p.nf;
     for (int base = blockIdx.x * blockDim.x; base < n_items; base += gridDim.x * blockDim.x) {
         int idx = base + threadIdx.x;
         int f = idx < n_items ? (p.use_list ? p.face_list[idx] : idx) : -1;
+        int k = f >= 0 ? inst_of(p, p.left[f]) : -1;
+        if (k >= 0 && p.tl[k].done) k = -1;
         bool counted = false;
         unsigned int err = 0;
-        if (f >= 0) {
+        if (k >= 0) {
             int l = p.left[f], r = p.right[f];
             bool la = p.active[l] != 0;
             Out32 o;
@@ -204,14 +206,10 @@ __global__ void __launch_bounds__(kBlock) k_face_flux32(KP p) {
                 out[5 * nf + f] = o.v_max;
                 out[6 * nf + f] = o.a_over_r;
             }
-            if (err & ~kInfoFallback) atomicOr(&p.tl->err, err & ~kInfoFallback);
+            if (err & ~kInfoFallback) set_err(p, k, err & ~kInfoFallback);
         }
-        unsigned int fb = __ballot_sync(0xffffffffu, (err & kInfoFallback) != 0);
-        if ((threadIdx.x & 31) == 0 && fb) atomicAdd(&p.tl->fallback_faces, (unsigned long long)__popc(fb));
-        if (!p.use_list) {
-            unsigned int b = __ballot_sync(0xffffffffu, counted);
-            if ((threadIdx.x & 31) == 0 && b) atomicAdd(&p.tl->active_faces, (unsigned long long)__popc(b));
-        }
+        inst_count(p, k, (err & kInfoFallback) != 0, CNT_FALLBACK);
+        if (!p.use_list) inst_count(p, k, counted, CNT_FACES);
     }
 }
 
@@ -221,12 +219,13 @@ __global__ void __launch_bounds__(kBlock) k_face_flux32(KP p) {
 // run in FP32 (these slopes only feed the FP32 reconstruction), and the
 // timestep (Particle::timestep, timesteps_apply) stays FP64 as in the plain form.
 __global__ void __launch_bounds__(kBlock) k_gradients32(KP p) {
-    if (p.tl->done) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     unsigned long long my_dti = MAX_NR_TIMESTEPS;
     int my_tb = 127;
     unsigned int err = 0;
-    if (i < p.n) {
+    int k = i < p.n ? inst_of(p, i) : -1;
+    if (k >= 0 && p.tl[k].done) k = -1;
+    if (k >= 0) {
         int tb = p.timebin[i];
         if (p.active[i]) {
             V3<double> cen = C3(p, F_CEN, i);
@@ -302,37 +301,18 @@ __global__ void __launch_bounds__(kBlock) k_gradients32(KP p) {
             }
             W3(p, F_GC, i, cen);
             double dt_new = particle_timestep(p, i);
-            unsigned long long tc = p.tl->ti_current;
-            unsigned long long dti = make_integer_timestep(dt_new, tb, NUM_TIME_BINS, tc, p.time_base_inv);
+            unsigned long long tc = p.tl[k].ti_current;
+            unsigned long long dti = make_integer_timestep(dt_new, tb, NUM_TIME_BINS, tc, tbase_inv(p, k));
             if (dti == 0) err |= 1u << 6;
-            W(p, F_DT, i, (double)dti * p.time_base);
+            W(p, F_DT, i, (double)dti * tbase(p, k));
             tb = get_time_bin(dti);
             my_dti = dti;
         }
         p.tb_tmp[i] = (int8_t)tb;
         my_tb = tb;
     }
-    if (err) set_err(p, err);
-    __shared__ unsigned long long s_dti[kBlock / 32];
-    __shared__ int s_tb[kBlock / 32];
-    my_dti = warp_min_u64(my_dti);
-    my_tb = warp_min_int(my_tb);
-    int w = threadIdx.x >> 5;
-    if ((threadIdx.x & 31) == 0) {
-        s_dti[w] = my_dti;
-        s_tb[w] = my_tb;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        unsigned long long a = s_dti[0];
-        int b = s_tb[0];
-        for (int k = 1; k < kBlock / 32; k++) {
-            a = s_dti[k] < a ? s_dti[k] : a;
-            b = min(b, s_tb[k]);
-        }
-        atomicMin(&p.tl->min_dti, a);
-        atomicMin(&p.tl->min_timebin, b);
-    }
+    if (err) set_err(p, k, err);
+    inst_min_dti_tb(p, k, my_dti, my_tb);
 }
 
 template <int SOLVER, bool SAMPLE>

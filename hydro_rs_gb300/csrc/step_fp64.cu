@@ -41,16 +41,17 @@ __device__ __forceinline__ void write_derived(const KP& p, int i, const St<doubl
 // EulerEqnsFvs::predict -> Particle::extrapolate_state (part.rs:123-132),
 // plus the active mask bin_is_ending (engine.rs:63-65) in step mode.
 __global__ void __launch_bounds__(kBlock) k_predict(KP p) {
-    if (p.tl->done) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     bool act = false;
-    if (i < p.n) {
+    int k = i < p.n ? inst_of(p, i) : -1;
+    if (k >= 0 && p.tl[k].done) k = -1;  // a finished simulation of a batch is left untouched
+    if (k >= 0) {
         double dt;
         if (p.stage) {
             dt = p.stage_dt;
         } else {
-            unsigned long long tc = p.tl->ti_current, to = p.tl->ti_old;
-            dt = (double)(tc - to) * p.time_base;  // TimestepInfo::dt_from_dti
+            unsigned long long tc = p.tl[k].ti_current, to = p.tl[k].ti_old;
+            dt = (double)(tc - to) * tbase(p, k);  // TimestepInfo::dt_from_dti
             act = p.timebin[i] <= get_max_active_bin(tc);
             p.active[i] = act;
         }
@@ -72,10 +73,7 @@ __global__ void __launch_bounds__(kBlock) k_predict(KP p) {
         // volume: dvdt is zero for a fixed mesh, so volume.clamp(..) leaves it unchanged
         write_derived(p, i, chk, src, rho_inv);
     }
-    if (!p.stage) {
-        unsigned int b = __ballot_sync(0xffffffffu, act);
-        if ((threadIdx.x & 31) == 0 && b) atomicAdd(&p.tl->active_cells, (unsigned long long)__popc(b));
-    }
+    if (!p.stage) inst_count(p, k, act, CNT_CELLS);
 }
 
 // Recomputes the derived face-stage fields (per-stage flux calls).
@@ -205,15 +203,17 @@ __device__ __forceinline__ FaceOut face_boundary(const KP& p, int f, int i, unsi
 // dt = min(dt_l, dt_r), interior / boundary dispatch.
 template <int SOLVER>
 __global__ void __launch_bounds__(kBlock) k_face_flux(KP p) {
-    if (p.tl->done) return;
+    if (p.use_list && p.tl[0].done) return;
     // all faces (one per thread), or the compacted active-face list (grid-stride)
-    const int n_items = p.use_list ? (int)p.tl->n_list : p.nf;
+    const int n_items = p.use_list ? (int)p.tl[0].n_list : p.nf;
     for (int base = blockIdx.x * blockDim.x; base < n_items; base += gridDim.x * blockDim.x) {
         int idx = base + threadIdx.x;
         int f = idx < n_items ? (p.use_list ? p.face_list[idx] : idx) : -1;
+        int k = f >= 0 ? inst_of(p, p.left[f]) : -1;
+        if (k >= 0 && p.tl[k].done) k = -1;
         bool counted = false;
         unsigned int err = 0;
-        if (f >= 0) {
+        if (k >= 0) {
             int l = p.left[f], r = p.right[f];
             bool la = p.active[l] != 0;
             FaceOut o;
@@ -248,12 +248,9 @@ __global__ void __launch_bounds__(kBlock) k_face_flux(KP p) {
                 out[5 * nf + f] = o.v_max;
                 out[6 * nf + f] = o.a_over_r;
             }
-            if (err) set_err(p, err);
+            if (err) set_err(p, k, err);
         }
-        if (!p.use_list) {  // list mode counts the list length in k_end
-            unsigned int b = __ballot_sync(0xffffffffu, counted);
-            if ((threadIdx.x & 31) == 0 && b) atomicAdd(&p.tl->active_faces, (unsigned long long)__popc(b));
-        }
+        if (!p.use_list) inst_count(p, k, counted, CNT_FACES);  // list mode counts the list in k_end
     }
 }
 
@@ -263,7 +260,7 @@ __global__ void __launch_bounds__(kBlock) k_face_flux(KP p) {
 // order is arbitrary; each face writes only its own result rows, so results do
 // not depend on it.
 __global__ void __launch_bounds__(kBlock) k_compact(KP p) {
-    if (p.tl->done) return;
+    if (p.tl[0].done) return;
     int f = blockIdx.x * blockDim.x + threadIdx.x;
     bool act = false;
     if (f < p.nf) {
@@ -283,7 +280,7 @@ __global__ void __launch_bounds__(kBlock) k_compact(KP p) {
     int lane = threadIdx.x & 31;
     int leader = __ffs(b) - 1;
     unsigned int start = 0;
-    if (lane == leader) start = atomicAdd(&p.tl->n_list, (unsigned int)__popc(b));
+    if (lane == leader) start = atomicAdd(&p.tl[0].n_list, (unsigned int)__popc(b));
     start = __shfl_sync(0xffffffffu, start, leader);
     if (act) p.face_list[start + __popc(b & ((1u << lane) - 1u))] = f;
 }
@@ -321,9 +318,10 @@ __device__ __forceinline__ void c2p(const KP& p, int i, const St<double>& cons, 
 // the cell in CSR order; active cells fold the accumulator into the conserved
 // state (Particle::apply_flux, part.rs:178-193), then kick2 and cons->prim.
 __global__ void __launch_bounds__(kBlock) k_update(KP p, int do_c2p) {
-    if (p.tl->done) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
+    const int k = inst_of(p, i);
+    if (p.tl[k].done) return;
     bool act = p.active[i] != 0;
     St<double> facc = C5(p, F_FACC, i);
     double msv = C(p, F_MSV, i), maor = C(p, F_MAOR, i);
@@ -365,7 +363,7 @@ __global__ void __launch_bounds__(kBlock) k_update(KP p, int do_c2p) {
         if (do_c2p) c2p(p, i, cons, &err);
     }
     W5(p, F_FACC, i, facc);
-    if (err) set_err(p, err);
+    if (err) set_err(p, k, err);
 }
 
 __global__ void __launch_bounds__(kBlock) k_c2p(KP p) {
@@ -373,7 +371,7 @@ __global__ void __launch_bounds__(kBlock) k_c2p(KP p) {
     if (i >= p.n || !p.active[i]) return;
     unsigned int err = 0;
     c2p(p, i, C5(p, F_CONS, i), &err);
-    if (err) set_err(p, err);
+    if (err) set_err(p, inst_of(p, i), err);
 }
 
 // ------------------------------------------------------------ gradients --
@@ -382,12 +380,13 @@ __global__ void __launch_bounds__(kBlock) k_c2p(KP p) {
 // (euler_eqns_fvs.rs:50-61, runner/hydrodynamics.rs:145-158) with block-level
 // min reductions of the integer timestep and the new time bins.
 __global__ void __launch_bounds__(kBlock) k_gradients(KP p, int do_timestep) {
-    if (p.tl->done) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     unsigned long long my_dti = MAX_NR_TIMESTEPS;
     int my_tb = 127;
     unsigned int err = 0;
-    if (i < p.n) {
+    int k = i < p.n ? inst_of(p, i) : -1;
+    if (k >= 0 && p.tl[k].done) k = -1;
+    if (k >= 0) {
         int tb = p.timebin[i];
         if (p.active[i]) {
             V3<double> cen = C3(p, F_CEN, i);
@@ -483,10 +482,10 @@ __global__ void __launch_bounds__(kBlock) k_gradients(KP p, int do_timestep) {
             W3(p, F_GC, i, cen);  // gradient_apply
             if (do_timestep) {
                 double dt_new = particle_timestep(p, i);
-                unsigned long long tc = p.tl->ti_current;
-                unsigned long long dti = make_integer_timestep(dt_new, tb, NUM_TIME_BINS, tc, p.time_base_inv);
+                unsigned long long tc = p.tl[k].ti_current;
+                unsigned long long dti = make_integer_timestep(dt_new, tb, NUM_TIME_BINS, tc, tbase_inv(p, k));
                 if (dti == 0) err |= 1u << 6;
-                W(p, F_DT, i, (double)dti * p.time_base);  // Particle::set_timestep
+                W(p, F_DT, i, (double)dti * tbase(p, k));  // Particle::set_timestep
                 tb = get_time_bin(dti);
                 my_dti = dti;
             }
@@ -496,28 +495,9 @@ __global__ void __launch_bounds__(kBlock) k_gradients(KP p, int do_timestep) {
             my_tb = tb;
         }
     }
-    if (err) set_err(p, err);
+    if (err) set_err(p, k, err);
     if (!do_timestep) return;
-    __shared__ unsigned long long s_dti[kBlock / 32];
-    __shared__ int s_tb[kBlock / 32];
-    my_dti = warp_min_u64(my_dti);
-    my_tb = warp_min_int(my_tb);
-    int w = threadIdx.x >> 5;
-    if ((threadIdx.x & 31) == 0) {
-        s_dti[w] = my_dti;
-        s_tb[w] = my_tb;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        unsigned long long a = s_dti[0];
-        int b = s_tb[0];
-        for (int k = 1; k < kBlock / 32; k++) {
-            a = s_dti[k] < a ? s_dti[k] : a;
-            b = min(b, s_tb[k]);
-        }
-        atomicMin(&p.tl->min_dti, a);
-        atomicMin(&p.tl->min_timebin, b);
-    }
+    inst_min_dti_tb(p, k, my_dti, my_tb);
 }
 
 // compute_timesteps as a stage (euler_eqns_fvs.rs:50-61)
@@ -532,13 +512,15 @@ __global__ void __launch_bounds__(kBlock) k_timesteps(KP p, double* out) {
 // Particle::timestep_limit (part.rs:263-297); then reset_extrapolations and
 // kick1 (runner/hydrodynamics.rs:41-49, 193-195).
 __global__ void __launch_bounds__(kBlock) k_limit(KP p) {
-    if (p.tl->done) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
+    const int k = inst_of(p, i);
+    if (p.tl[k].done) return;
+    const double time_base = tbase(p, k);
     int tb = p.tb_tmp[i];
     int wakeup;
     if (p.sync_all) {
-        wakeup = p.tl->min_timebin;
+        wakeup = p.tl[k].min_timebin;
     } else {
         wakeup = tb;
         int k0 = p.csr_off[i], k1 = p.csr_off[i + 1];
@@ -557,18 +539,18 @@ __global__ void __launch_bounds__(kBlock) k_limit(KP p) {
         }
     }
     if (wakeup < tb) {
-        unsigned long long tc = p.tl->ti_current;
+        unsigned long long tc = p.tl[k].ti_current;
         double dt = C(p, F_DT, i);
         if (tb <= get_max_active_bin(tc)) {  // bin_is_starting
             tb = wakeup;
-            dt = (double)get_integer_timestep(tb) * p.time_base;
+            dt = (double)get_integer_timestep(tb) * time_base;
         } else {
             unsigned long long ti_end_old = get_integer_time_end(tc, tb);
-            dt -= (double)(ti_end_old - tc) * p.time_base;
+            dt -= (double)(ti_end_old - tc) * time_base;
             tb = wakeup;
             unsigned long long dti_new = get_integer_timestep(tb);
             unsigned long long ti_end = get_integer_time_end(tc, tb);
-            dt += (ti_end == tc) ? (double)dti_new * p.time_base : (double)(ti_end - tc) * p.time_base;
+            dt += (ti_end == tc) ? (double)dti_new * time_base : (double)(ti_end - tc) * time_base;
         }
         W(p, F_DT, i, dt);
     }
@@ -585,12 +567,17 @@ __global__ void __launch_bounds__(kBlock) k_limit(KP p) {
 // Engine bookkeeping after a step (engine.rs:194-199, 258-268): advance the
 // device timeline to the next sync point and reset the reductions.
 __global__ void k_end(KP p) {
-    DevTimeline* tl = p.tl;
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= p.n_inst) return;
+    DevTimeline* tl = p.tl + k;
     if (tl->done) return;
     unsigned long long tc = tl->ti_current;
     unsigned long long tn = tc + tl->min_dti;
     tl->steps += 1;
     if (tc >= MAX_NR_TIMESTEPS) tl->done = 1;
+    // a simulation whose step reported a failure stops here (the reference
+    // panics); the other simulations of a batch carry on
+    if (tl->err) tl->done = 1;
     tl->ti_old = tc;
     tl->ti_current = tn;
     tl->min_dti = MAX_NR_TIMESTEPS;
@@ -664,7 +651,7 @@ void launch_timesteps(const KP& p, double* dt_out, cudaStream_t s) {
 void launch_limit(const KP& p, cudaStream_t s) {
     if (p.n > 0) k_limit<<<grid(p.n), kBlock, 0, s>>>(p);
 }
-void launch_end(const KP& p, cudaStream_t s) { k_end<<<1, 1, 0, s>>>(p); }
+void launch_end(const KP& p, cudaStream_t s) { k_end<<<(p.n_inst + 127) / 128, 128, 0, s>>>(p); }
 
 void launch_riemann_fp64(int kind, int sample, double gamma, int64_t n, const double* l, const double* r,
                          const double* vf, const double* nrm, double* out, unsigned int* err, cudaStream_t s) {

@@ -25,6 +25,7 @@ EXPORTED = (
     "mvmm_convert_conserved_to_primitive", "mvmm_compute_timesteps", "mvmm_apply_fluxes", "mvmm_gradients",
     "mvmm_step", "mvmm_run", "mvmm_enqueue_steps", "mvmm_set_time", "mvmm_get_time", "mvmm_profile_enable",
     "mvmm_profile_read", "mvmm_riemann_flux", "mvmm_riemann_sample", "mvmm_get_stats",
+    "mvmm_ctx_create_batched", "mvmm_batch_state",
 )
 
 
@@ -79,6 +80,8 @@ def load_library(path: str = LIB_PATH):
         "mvmm_riemann_flux": (i32, [i32, i32, dbl, i64, vp, vp, vp, vp, vp]),
         "mvmm_riemann_sample": (i32, [i32, i32, dbl, i64, vp, vp, vp, vp]),
         "mvmm_get_stats": (i32, [vp, vp]),
+        "mvmm_ctx_create_batched": (i32, [vp, vp, i64, vp, vp, ctypes.POINTER(vp)]),
+        "mvmm_batch_state": (i32, [vp, vp, vp, vp, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -122,9 +125,12 @@ def riemann_sample(kind: int, gamma: float, left, right, normal, precision: int 
 
 
 class GpuSim:
-    """One simulation resident on the GPU (Engine + OptimalOrderRunner + EulerEqnsFvs)."""
+    """One simulation resident on the GPU (Engine + OptimalOrderRunner + EulerEqnsFvs).
 
-    def __init__(self, problem, precision: int | None = None, stream=None):
+    With ``cell_offsets`` / ``t_end`` (from :func:`hydro_rs_gb300.ics.pack`) the
+    context is a batch of independent simulations stepped together."""
+
+    def __init__(self, problem, precision: int | None = None, stream=None, cell_offsets=None, t_end=None):
         L = load_library()
         p = problem.params
         self.problem = problem
@@ -134,7 +140,15 @@ class GpuSim:
                           p.max_newton_iter, prec, 0)
         self._mv = self.mesh.cview()
         h = ctypes.c_void_p(0)
-        _check(L.mvmm_ctx_create(ctypes.byref(self._p), ctypes.byref(self._mv), ctypes.byref(h)))
+        self.n_instances = 1
+        if cell_offsets is not None:
+            self._off = np.ascontiguousarray(cell_offsets, dtype=np.int64)
+            self._tend = np.ascontiguousarray(t_end, dtype=np.float64)
+            self.n_instances = len(self._off) - 1
+            _check(L.mvmm_ctx_create_batched(ctypes.byref(self._p), ctypes.byref(self._mv), self.n_instances,
+                                             self._off.ctypes.data, self._tend.ctypes.data, ctypes.byref(h)))
+        else:
+            _check(L.mvmm_ctx_create(ctypes.byref(self._p), ctypes.byref(self._mv), ctypes.byref(h)))
         self.h = h
         if stream is not None:
             _check(L.mvmm_ctx_set_stream(self.h, ctypes.c_void_p(stream)), self.h)
@@ -211,6 +225,15 @@ class GpuSim:
                                             ctypes.byref(af), ctypes.byref(fin)), self.h)
         self.ti_current, self.ti_old, self.finished = tc.value, to.value, bool(fin.value)
         return st.value, af.value
+
+    def batch_state(self) -> dict:
+        k = self.n_instances
+        tc, to = np.zeros(k, np.uint64), np.zeros(k, np.uint64)
+        st, af = np.zeros(k, np.int64), np.zeros(k, np.int64)
+        err, fin = np.zeros(k, np.uint32), np.zeros(k, np.int32)
+        _check(load_library().mvmm_batch_state(self.h, tc.ctypes.data, to.ctypes.data, st.ctypes.data, af.ctypes.data,
+                                               err.ctypes.data, fin.ctypes.data), self.h)
+        return {"ti_current": tc, "ti_old": to, "steps": st, "active_faces": af, "err": err, "finished": fin}
 
     def stats(self) -> dict:
         a = np.zeros(4, dtype=np.int64)

@@ -207,3 +207,72 @@ def yee_vortex_2d(nx: int, beta: float, v_adv, seed: int = 5, box_len: float = 1
     mass = rho * (box[0] * box[1] * box[2] / x.shape[1])
     cells = cells_from_ic(mesh, x, mass, vel, u, gamma)
     return Problem("yee_vortex_2d", params, mesh, cells, extra={"beta": beta, "v_adv": tuple(v_adv)})
+
+
+def riemann_batch_1d(n_instances: int = 512, seed: int = 4, n_min: int = 200, n_max: int = 20000,
+                     riemann: int = EXACT, t_end: float = 0.15, gamma: float = 5.0 / 3.0):
+    """Independent 1D Riemann problems: N log-uniform in [n_min, n_max]; rho_L, rho_R
+    log-uniform in [0.1, 10]; P log-uniform in [1e-3, 1e3]; v uniform in [-2, 2];
+    discontinuity at x = 0.5, reflective walls."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n_instances):
+        n = int(round(math.exp(rng.uniform(math.log(n_min), math.log(n_max)))))
+        rho = 10 ** rng.uniform(-1, 1, 2)
+        p = 10 ** rng.uniform(-3, 3, 2)
+        v = rng.uniform(-2, 2, 2)
+        out.append(riemann_1d(n, (rho[0], v[0], p[0]), (rho[1], v[1], p[1]), riemann, t_end, gamma=gamma))
+    return out
+
+
+def pack(problems):
+    """Packs independent problems (same physics parameters) into one mesh union:
+    cells and faces of problem k follow those of problem k-1, with indices
+    offset.  Returns (Problem, cell_offsets, t_end array)."""
+    from .layout import Cells, Mesh
+
+    assert problems
+    p0 = problems[0].params
+    for q in problems[1:]:
+        a, b = q.params, p0
+        assert (a.gamma, a.cfl, a.riemann, a.boundary, a.dimensionality, a.sync_all, a.precision) == \
+            (b.gamma, b.cfl, b.riemann, b.boundary, b.dimensionality, b.sync_all, b.precision), "mixed physics"
+    n = [q.mesh.n_cells for q in problems]
+    f = [q.mesh.n_faces for q in problems]
+    cell_off = np.concatenate([[0], np.cumsum(n)]).astype(np.int64)
+    face_off = np.concatenate([[0], np.cumsum(f)]).astype(np.int64)
+    csr_len = [int(q.mesh.csr_off[-1]) for q in problems]
+    csr_base = np.concatenate([[0], np.cumsum(csr_len)]).astype(np.int64)
+    N, F = int(cell_off[-1]), int(face_off[-1])
+    left = np.concatenate([q.mesh.left + cell_off[k] for k, q in enumerate(problems)]).astype(np.int32)
+    right = np.concatenate([np.where(q.mesh.right >= 0, q.mesh.right + cell_off[k], -1)
+                            for k, q in enumerate(problems)]).astype(np.int32)
+    cat3 = lambda name: np.ascontiguousarray(np.concatenate([getattr(q.mesh, name) for q in problems], axis=1))
+    csr_off = np.concatenate([[0]] + [q.mesh.csr_off[1:] + csr_base[k] for k, q in enumerate(problems)]).astype(np.int32)
+    csr_face = np.concatenate([q.mesh.csr_face + face_off[k] for k, q in enumerate(problems)]).astype(np.int32)
+    mesh = Mesh(n_cells=N, left=left, right=right, area=np.concatenate([q.mesh.area for q in problems]),
+                normal=cat3("normal"), centroid=cat3("centroid"), shift=cat3("shift"), csr_off=csr_off,
+                csr_face=csr_face, volume=np.concatenate([q.mesh.volume for q in problems]),
+                cell_centroid=np.ascontiguousarray(np.concatenate([q.mesh.cell_centroid for q in problems], axis=1)),
+                dimensionality=problems[0].mesh.dimensionality, box=problems[0].mesh.box,
+                periodic=problems[0].mesh.periodic)
+    cells = Cells(n=N)
+    for name, arr in problems[0].cells.arrays.items():
+        axis = 1 if arr.ndim == 2 else 0
+        cells.arrays[name] = np.ascontiguousarray(np.concatenate([q.cells.arrays[name] for q in problems], axis=axis))
+    t_end = np.array([q.params.t_end for q in problems], dtype=np.float64)
+    return Problem("batch", p0, mesh, cells, extra={"n_instances": len(problems)}), cell_off, t_end
+
+
+def unpack_cells(cells, cell_off):
+    """Splits packed cell state back into one Cells per instance."""
+    from .layout import Cells
+
+    out = []
+    for k in range(len(cell_off) - 1):
+        a, b = int(cell_off[k]), int(cell_off[k + 1])
+        c = Cells(n=b - a)
+        for name, arr in cells.arrays.items():
+            c.arrays[name] = np.ascontiguousarray(arr[..., a:b])
+        out.append(c)
+    return out

@@ -105,6 +105,20 @@ typedef struct mvmm_ctx mvmm_ctx;
  * of the mesh produced by Space::initialize (space.rs:88-211). */
 int mvmm_ctx_create(const mvmm_params *params, const mvmm_mesh *mesh, mvmm_ctx **out);
 int mvmm_ctx_destroy(mvmm_ctx *ctx);
+/* Batched context (no counterpart in the reference, which runs one simulation
+ * per process): n_instances independent simulations packed into one mesh.
+ * Cells of instance k are cell_offsets[k] .. cell_offsets[k+1]-1 and no face
+ * may join two instances; each instance has its own integer timeline with
+ * time_base = t_end[k] / 2^57, all share params (gamma, solver, boundary, ...).
+ * Every stage of a step is one launch over all instances; finished instances
+ * are skipped.  mvmm_step / mvmm_run / mvmm_enqueue_steps step every unfinished
+ * instance from its own device timeline (their ti arguments are ignored for a
+ * batch); mvmm_run returns when all are finished. */
+int mvmm_ctx_create_batched(const mvmm_params *params, const mvmm_mesh *mesh, int64_t n_instances,
+                            const int64_t *cell_offsets, const double *t_end, mvmm_ctx **out);
+/* Per-instance timeline state, arrays of n_instances (any may be NULL). */
+int mvmm_batch_state(mvmm_ctx *ctx, uint64_t *ti_current, uint64_t *ti_old, int64_t *steps, int64_t *active_faces,
+                     uint32_t *err_bits, int *finished);
 /* Runs all work of this context on the given cudaStream_t (NULL = own stream). */
 int mvmm_ctx_set_stream(mvmm_ctx *ctx, void *cuda_stream);
 /* Host <-> device copies of the whole cell state (the &mut [Particle] the
