@@ -22,11 +22,21 @@ def _batch(problems, precision=0):
     return sim, packed, off
 
 
+def _run(sim):
+    """Runs to the end; a simulation that fails (PVRS has no pressure floor,
+    pvrs.rs:40, so strong rarefactions can give a negative pressure) stops and
+    is reported per simulation, the call then returns MVMM_E_NUMERIC."""
+    try:
+        sim.run()
+    except G.MvmmError as e:
+        assert e.code == -3
+
+
 @pytest.mark.parametrize("riemann,precision", [(ics.EXACT, 0), (ics.PVRS, 0), (ics.EXACT, 1)])
 def test_batch_equals_alone(gpu_lib, riemann, precision):
     probs = ics.riemann_batch_1d(8, seed=41, n_min=40, n_max=240, riemann=riemann, t_end=0.02)
     sim, packed, off = _batch(probs, precision)
-    sim.run()
+    _run(sim)
     st = sim.batch_state()
     assert st["finished"].all() or (st["err"] != 0).any()
     parts = ics.unpack_cells(sim.state(), off)
@@ -34,7 +44,7 @@ def test_batch_equals_alone(gpu_lib, riemann, precision):
         if st["err"][k]:
             continue
         alone = G.GpuSim(p, precision=precision)
-        alone.run()
+        _run(alone)
         assert alone.finished and alone.steps == st["steps"][k]
         a = alone.state()
         for f in ("cons", "prim", "grad", "dt"):
@@ -46,7 +56,7 @@ def test_batch_equals_alone(gpu_lib, riemann, precision):
 def test_batch_matches_oracle(gpu_lib):
     probs = ics.riemann_batch_1d(4, seed=42, n_min=60, n_max=160, riemann=ics.EXACT, t_end=0.02)
     sim, packed, off = _batch(probs)
-    sim.run()
+    _run(sim)
     parts = ics.unpack_cells(sim.state(), off)
     st = sim.batch_state()
     for k, p in enumerate(probs):
