@@ -71,12 +71,18 @@ def test_batch_matches_oracle(gpu_lib):
 
 
 def test_failed_simulation_stops_alone(gpu_lib):
-    """A host-made failure (negative energy) in one simulation stops it; the others finish unchanged."""
+    """A host-made failure in one simulation stops it; the others finish unchanged.
+
+    The failure: a cell whose kinetic energy exceeds its total energy, so
+    cons->prim yields a negative pressure, which the reference asserts against
+    (physical_quantities.rs:220-221).  (A negative total energy would not do:
+    the reference resets such a cell to vacuum, part.rs:184-191.)"""
     probs = ics.riemann_batch_1d(5, seed=43, n_min=40, n_max=120, riemann=ics.HLLC, t_end=0.02)
     packed, off, te = ics.pack(probs)
     bad = 2
-    packed.cells.cons[4][int(off[bad]) + 3] = -1.0
-    packed.cells.prim[4][int(off[bad]) + 3] = -1.0
+    i = int(off[bad]) + 3
+    c = packed.cells.cons
+    c[1][i] = 4.0 * np.sqrt(2.0 * c[0][i] * c[4][i])
     sim = G.GpuSim(packed, cell_offsets=off, t_end=te)
     with pytest.raises(G.MvmmError):
         sim.run()
