@@ -5,6 +5,7 @@
 // timeline, so a run of many steps needs no host round trip per step.
 #include <cstdio>
 #include <cstdlib>
+#include <algorithm>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -60,6 +61,7 @@ struct mvmm_ctx {
     double* inst_tbi = nullptr;
     uint8_t* face_act = nullptr;
     int* face_list = nullptr;
+    int blk_face = 128, blk_cell = 128;
     DevTimeline* tl = nullptr;       // [n_inst]
     DevTimeline* tl_host = nullptr;  // pinned [n_inst]
     cudaStream_t stream = nullptr;
@@ -116,6 +118,8 @@ KP make_kp(mvmm_ctx* c, int stage, int flux_rows) {
     p.use_list = (!stage && !c->prm.sync_all && c->n_inst == 1) ? 1 : 0;
     p.face_act = c->face_act;
     p.face_list = c->face_list;
+    p.blk_face = c->blk_face;
+    p.blk_cell = c->blk_cell;
     return p;
 }
 
@@ -662,6 +666,83 @@ int mvmm_run(mvmm_ctx* c, int64_t max_steps, uint64_t* ti_current, uint64_t* ti_
     if (n_active_faces) *n_active_faces = (int64_t)(sum_field(c, &DevTimeline::active_faces) - f0);
     if (finished) *finished = all_done(c) ? 1 : 0;
     return rc;
+}
+
+// Chooses the thread-block sizes of the face kernel and of the cell kernels by
+// timing steps of this context's own workload, then puts the state back: the
+// cell state, time bins and timelines are saved to a device copy first.
+int mvmm_autotune(mvmm_ctx* c, int steps, int* blk_face, int* blk_cell) {
+    if (!c || steps < 1) return fail(MVMM_E_INVALID, "bad arguments");
+    int rc = read_tl(c);
+    if (rc) return rc;
+    size_t n = c->n;
+    size_t bytes = (size_t)kCellFields * n * 8;
+    double* save = nullptr;
+    int8_t* save_tb = nullptr;
+    CUDA_TRY(cudaMalloc((void**)&save, bytes));
+    if (cudaMalloc((void**)&save_tb, n) != cudaSuccess) {
+        cudaFree(save);
+        return fail(MVMM_E_NOMEM, "cudaMalloc failed");
+    }
+    std::vector<DevTimeline> tl0(c->tl_host, c->tl_host + c->n_inst);
+    cudaMemcpyAsync(save, c->cd, bytes, cudaMemcpyDeviceToDevice, c->stream);
+    cudaMemcpyAsync(save_tb, c->timebin, n, cudaMemcpyDeviceToDevice, c->stream);
+    const int cand[3] = {64, 128, 256};
+    float best = 1e30f;
+    int bf = c->blk_face, bc = c->blk_cell;
+    bool prof = c->prof;
+    c->prof = false;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+            c->blk_face = cand[i];
+            c->blk_cell = cand[j];
+            if (c->step_exec) {
+                cudaGraphExecDestroy(c->step_exec);
+                c->step_exec = nullptr;
+            }
+            // restore, warm once, time `steps` steps
+            cudaMemcpyAsync(c->cd, save, bytes, cudaMemcpyDeviceToDevice, c->stream);
+            cudaMemcpyAsync(c->timebin, save_tb, n, cudaMemcpyDeviceToDevice, c->stream);
+            std::copy(tl0.begin(), tl0.end(), c->tl_host);
+            write_tl(c);
+            rc = enqueue_steps_impl(c, 1);
+            if (rc) break;
+            cudaEventRecord(e0, c->stream);
+            rc = enqueue_steps_impl(c, steps);
+            if (rc) break;
+            cudaEventRecord(e1, c->stream);
+            cudaEventSynchronize(e1);
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (ms < best) {
+                best = ms;
+                bf = cand[i];
+                bc = cand[j];
+            }
+        }
+    c->blk_face = bf;
+    c->blk_cell = bc;
+    if (c->step_exec) {
+        cudaGraphExecDestroy(c->step_exec);
+        c->step_exec = nullptr;
+    }
+    cudaMemcpyAsync(c->cd, save, bytes, cudaMemcpyDeviceToDevice, c->stream);
+    cudaMemcpyAsync(c->timebin, save_tb, n, cudaMemcpyDeviceToDevice, c->stream);
+    std::copy(tl0.begin(), tl0.end(), c->tl_host);
+    write_tl(c);
+    cudaStreamSynchronize(c->stream);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(save);
+    cudaFree(save_tb);
+    c->prof = prof;
+    if (rc) return rc;
+    if (blk_face) *blk_face = bf;
+    if (blk_cell) *blk_cell = bc;
+    return MVMM_OK;
 }
 
 int mvmm_profile_enable(mvmm_ctx* c, int enable) {

@@ -9,7 +9,8 @@
 namespace mvmm {
 namespace {
 
-constexpr int kBlock = 128;
+constexpr int kBlock = 128;     // default block of the step kernels
+constexpr int kMaxBlock = 256;  // largest block the autotuner may choose
 
 __device__ __forceinline__ double C(const KP& p, int f, int i) { return p.cd[(size_t)f * p.n + i]; }
 __device__ __forceinline__ void W(const KP& p, int f, int i, double v) { p.cd[(size_t)f * p.n + i] = v; }

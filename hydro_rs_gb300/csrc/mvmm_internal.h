@@ -98,6 +98,7 @@ struct KP {
     int n_inst;
     const double* inst_tb;   // per-instance time_base (nullptr: time_base)
     const double* inst_tbi;  // per-instance 1 / time_base (nullptr: time_base_inv)
+    int blk_face, blk_cell;  // thread-block sizes (chosen by mvmm_autotune)
     int use_list;            // 1: face kernel walks the compacted active-face list
     uint8_t* face_act;       // per-face flag of this step's active-face rule
     int* face_list;          // compacted active faces

@@ -20,7 +20,7 @@ __device__ __forceinline__ St<float> G5(const KP& p, int f, int i) {
     for (int q = 0; q < 5; q++) s.q[q] = G(p, f + q, i);
     return s;
 }
-__global__ void __launch_bounds__(kBlock) k_prep32(KP p) {
+__global__ void __launch_bounds__(kMaxBlock) k_prep32(KP p) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
     if (p.tl[inst_of(p, i)].done) return;
@@ -159,7 +159,7 @@ __device__ __forceinline__ Out32 face_boundary32(const KP& p, int f, int i, cons
 }
 
 template <int SOLVER>
-__global__ void __launch_bounds__(kBlock) k_face_flux32(KP p) {
+__global__ void __launch_bounds__(kMaxBlock) k_face_flux32(KP p) {
     if (p.use_list && p.tl[0].done) return;
     const Gas<float> g = make_gas<float>(p.gamma, p.eos, p.iso_u);
     const Gas<double> g64 = make_gas<double>(p.gamma, p.eos, p.iso_u);
@@ -218,7 +218,7 @@ __global__ void __launch_bounds__(kBlock) k_face_flux32(KP p) {
 // in FP64 and rounded, the WLS sums, the 3x3 inverse and the cell-wise limiter
 // run in FP32 (these slopes only feed the FP32 reconstruction), and the
 // timestep (Particle::timestep, timesteps_apply) stays FP64 as in the plain form.
-__global__ void __launch_bounds__(kBlock) k_gradients32(KP p) {
+__global__ void __launch_bounds__(kMaxBlock) k_gradients32(KP p) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     unsigned long long my_dti = MAX_NR_TIMESTEPS;
     int my_tb = 127;
@@ -343,24 +343,25 @@ __global__ void k_riemann32(double gamma, int64_t n, const double* l, const doub
     if (err) atomicOr(errp, err);
 }
 
-inline int grid(int n) { return (n + kBlock - 1) / kBlock; }
+inline int grid(int n, int b = kBlock) { return (n + b - 1) / b; }
 
 }  // namespace
 
 void launch_prep32(const KP& p, cudaStream_t s) {
-    if (p.n > 0) k_prep32<<<grid(p.n), kBlock, 0, s>>>(p);
+    if (p.n > 0) k_prep32<<<grid(p.n, p.blk_cell), p.blk_cell, 0, s>>>(p);
 }
 
 void launch_gradients32(const KP& p, cudaStream_t s) {
-    if (p.n > 0) k_gradients32<<<grid(p.n), kBlock, 0, s>>>(p);
+    if (p.n > 0) k_gradients32<<<grid(p.n, p.blk_cell), p.blk_cell, 0, s>>>(p);
 }
 
 void launch_face_flux_fp32(const KP& p, int solver, cudaStream_t s) {
     if (p.nf <= 0) return;
-    int g = p.use_list ? (grid(p.nf) < 152 * 4 ? grid(p.nf) : 152 * 4) : grid(p.nf);
-    if (solver == SOLVER_HLLC) k_face_flux32<SOLVER_HLLC><<<g, kBlock, 0, s>>>(p);
-    else if (solver == SOLVER_EXACT) k_face_flux32<SOLVER_EXACT><<<g, kBlock, 0, s>>>(p);
-    else k_face_flux32<SOLVER_PVRS><<<g, kBlock, 0, s>>>(p);
+    int g = grid(p.nf, p.blk_face), cap = 152 * 512 / p.blk_face;
+    if (p.use_list && g > cap) g = cap;
+    if (solver == SOLVER_HLLC) k_face_flux32<SOLVER_HLLC><<<g, p.blk_face, 0, s>>>(p);
+    else if (solver == SOLVER_EXACT) k_face_flux32<SOLVER_EXACT><<<g, p.blk_face, 0, s>>>(p);
+    else k_face_flux32<SOLVER_PVRS><<<g, p.blk_face, 0, s>>>(p);
 }
 
 void launch_riemann_fp32(int kind, int sample, double gamma, int64_t n, const double* l, const double* r,

@@ -40,7 +40,7 @@ __device__ __forceinline__ void write_derived(const KP& p, int i, const St<doubl
 // ------------------------------------------------------------- predict --
 // EulerEqnsFvs::predict -> Particle::extrapolate_state (part.rs:123-132),
 // plus the active mask bin_is_ending (engine.rs:63-65) in step mode.
-__global__ void __launch_bounds__(kBlock) k_predict(KP p) {
+__global__ void __launch_bounds__(kMaxBlock) k_predict(KP p) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     bool act = false;
     int k = i < p.n ? inst_of(p, i) : -1;
@@ -77,7 +77,7 @@ __global__ void __launch_bounds__(kBlock) k_predict(KP p) {
 }
 
 // Recomputes the derived face-stage fields (per-stage flux calls).
-__global__ void __launch_bounds__(kBlock) k_derive(KP p) {
+__global__ void __launch_bounds__(kMaxBlock) k_derive(KP p) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
     St<double> prim = C5(p, F_PRIM, i);
@@ -202,7 +202,7 @@ __device__ __forceinline__ FaceOut face_boundary(const KP& p, int f, int i, unsi
 // EulerEqnsFvs::compute_fluxes (euler_eqns_fvs.rs:26-48): the active-face rule,
 // dt = min(dt_l, dt_r), interior / boundary dispatch.
 template <int SOLVER>
-__global__ void __launch_bounds__(kBlock) k_face_flux(KP p) {
+__global__ void __launch_bounds__(kMaxBlock) k_face_flux(KP p) {
     if (p.use_list && p.tl[0].done) return;
     // all faces (one per thread), or the compacted active-face list (grid-stride)
     const int n_items = p.use_list ? (int)p.tl[0].n_list : p.nf;
@@ -259,7 +259,7 @@ __global__ void __launch_bounds__(kBlock) k_face_flux(KP p) {
 // appends the active ones to a list with warp-aggregated atomics.  The list
 // order is arbitrary; each face writes only its own result rows, so results do
 // not depend on it.
-__global__ void __launch_bounds__(kBlock) k_compact(KP p) {
+__global__ void __launch_bounds__(kMaxBlock) k_compact(KP p) {
     if (p.tl[0].done) return;
     int f = blockIdx.x * blockDim.x + threadIdx.x;
     bool act = false;
@@ -317,7 +317,7 @@ __device__ __forceinline__ void c2p(const KP& p, int i, const St<double>& cons, 
 // apply_fluxes (runner/hydrodynamics.rs:13-39): CSR gather of every face of
 // the cell in CSR order; active cells fold the accumulator into the conserved
 // state (Particle::apply_flux, part.rs:178-193), then kick2 and cons->prim.
-__global__ void __launch_bounds__(kBlock) k_update(KP p, int do_c2p) {
+__global__ void __launch_bounds__(kMaxBlock) k_update(KP p, int do_c2p) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
     const int k = inst_of(p, i);
@@ -366,7 +366,7 @@ __global__ void __launch_bounds__(kBlock) k_update(KP p, int do_c2p) {
     if (err) set_err(p, k, err);
 }
 
-__global__ void __launch_bounds__(kBlock) k_c2p(KP p) {
+__global__ void __launch_bounds__(kMaxBlock) k_c2p(KP p) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n || !p.active[i]) return;
     unsigned int err = 0;
@@ -379,7 +379,7 @@ __global__ void __launch_bounds__(kBlock) k_c2p(KP p) {
 // fused per cell; in step mode also compute_timesteps + timesteps_apply
 // (euler_eqns_fvs.rs:50-61, runner/hydrodynamics.rs:145-158) with block-level
 // min reductions of the integer timestep and the new time bins.
-__global__ void __launch_bounds__(kBlock) k_gradients(KP p, int do_timestep) {
+__global__ void __launch_bounds__(kMaxBlock) k_gradients(KP p, int do_timestep) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     unsigned long long my_dti = MAX_NR_TIMESTEPS;
     int my_tb = 127;
@@ -501,7 +501,7 @@ __global__ void __launch_bounds__(kBlock) k_gradients(KP p, int do_timestep) {
 }
 
 // compute_timesteps as a stage (euler_eqns_fvs.rs:50-61)
-__global__ void __launch_bounds__(kBlock) k_timesteps(KP p, double* out) {
+__global__ void __launch_bounds__(kMaxBlock) k_timesteps(KP p, double* out) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
     out[i] = p.active[i] ? particle_timestep(p, i) : INFINITY;
@@ -511,7 +511,7 @@ __global__ void __launch_bounds__(kBlock) k_timesteps(KP p, double* out) {
 // timestep_sync or timestep_limiter (runner/hydrodynamics.rs:160-191) with
 // Particle::timestep_limit (part.rs:263-297); then reset_extrapolations and
 // kick1 (runner/hydrodynamics.rs:41-49, 193-195).
-__global__ void __launch_bounds__(kBlock) k_limit(KP p) {
+__global__ void __launch_bounds__(kMaxBlock) k_limit(KP p) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
     const int k = inst_of(p, i);
@@ -613,43 +613,46 @@ __global__ void k_riemann(double gamma, int64_t n, const double* l, const double
     if (err) atomicOr(errp, err);
 }
 
-inline int grid(int n) { return (n + kBlock - 1) / kBlock; }
+inline int grid(int n, int b = kBlock) { return (n + b - 1) / b; }
 
 }  // namespace
 
 void launch_predict(const KP& p, cudaStream_t s) {
-    if (p.n > 0) k_predict<<<grid(p.n), kBlock, 0, s>>>(p);
+    if (p.n > 0) k_predict<<<grid(p.n, p.blk_cell), p.blk_cell, 0, s>>>(p);
 }
 void launch_derive(const KP& p, cudaStream_t s) {
-    if (p.n > 0) k_derive<<<grid(p.n), kBlock, 0, s>>>(p);
+    if (p.n > 0) k_derive<<<grid(p.n, p.blk_cell), p.blk_cell, 0, s>>>(p);
 }
 // list mode: a grid of a few waves walks the list (its length is only known on the device)
-inline int face_grid(const KP& p) { return p.use_list ? (grid(p.nf) < 152 * 4 ? grid(p.nf) : 152 * 4) : grid(p.nf); }
+inline int face_grid(const KP& p) {
+    int g = grid(p.nf, p.blk_face), cap = 152 * 512 / p.blk_face;
+    return p.use_list && g > cap ? cap : g;
+}
 
 void launch_face_flux_fp64(const KP& p, int solver, cudaStream_t s) {
     if (p.nf <= 0) return;
     int g = face_grid(p);
-    if (solver == SOLVER_HLLC) k_face_flux<SOLVER_HLLC><<<g, kBlock, 0, s>>>(p);
-    else if (solver == SOLVER_EXACT) k_face_flux<SOLVER_EXACT><<<g, kBlock, 0, s>>>(p);
-    else k_face_flux<SOLVER_PVRS><<<g, kBlock, 0, s>>>(p);
+    if (solver == SOLVER_HLLC) k_face_flux<SOLVER_HLLC><<<g, p.blk_face, 0, s>>>(p);
+    else if (solver == SOLVER_EXACT) k_face_flux<SOLVER_EXACT><<<g, p.blk_face, 0, s>>>(p);
+    else k_face_flux<SOLVER_PVRS><<<g, p.blk_face, 0, s>>>(p);
 }
 void launch_compact(const KP& p, cudaStream_t s) {
-    if (p.nf > 0) k_compact<<<grid(p.nf), kBlock, 0, s>>>(p);
+    if (p.nf > 0) k_compact<<<grid(p.nf, p.blk_cell), p.blk_cell, 0, s>>>(p);
 }
 void launch_update(const KP& p, int do_c2p, cudaStream_t s) {
-    if (p.n > 0) k_update<<<grid(p.n), kBlock, 0, s>>>(p, do_c2p);
+    if (p.n > 0) k_update<<<grid(p.n, p.blk_cell), p.blk_cell, 0, s>>>(p, do_c2p);
 }
 void launch_c2p(const KP& p, cudaStream_t s) {
-    if (p.n > 0) k_c2p<<<grid(p.n), kBlock, 0, s>>>(p);
+    if (p.n > 0) k_c2p<<<grid(p.n, p.blk_cell), p.blk_cell, 0, s>>>(p);
 }
 void launch_gradients(const KP& p, int do_timestep, cudaStream_t s) {
-    if (p.n > 0) k_gradients<<<grid(p.n), kBlock, 0, s>>>(p, do_timestep);
+    if (p.n > 0) k_gradients<<<grid(p.n, p.blk_cell), p.blk_cell, 0, s>>>(p, do_timestep);
 }
 void launch_timesteps(const KP& p, double* dt_out, cudaStream_t s) {
-    if (p.n > 0) k_timesteps<<<grid(p.n), kBlock, 0, s>>>(p, dt_out);
+    if (p.n > 0) k_timesteps<<<grid(p.n, p.blk_cell), p.blk_cell, 0, s>>>(p, dt_out);
 }
 void launch_limit(const KP& p, cudaStream_t s) {
-    if (p.n > 0) k_limit<<<grid(p.n), kBlock, 0, s>>>(p);
+    if (p.n > 0) k_limit<<<grid(p.n, p.blk_cell), p.blk_cell, 0, s>>>(p);
 }
 void launch_end(const KP& p, cudaStream_t s) { k_end<<<(p.n_inst + 127) / 128, 128, 0, s>>>(p); }
 

@@ -25,7 +25,7 @@ EXPORTED = (
     "mvmm_convert_conserved_to_primitive", "mvmm_compute_timesteps", "mvmm_apply_fluxes", "mvmm_gradients",
     "mvmm_step", "mvmm_run", "mvmm_enqueue_steps", "mvmm_set_time", "mvmm_get_time", "mvmm_profile_enable",
     "mvmm_profile_read", "mvmm_riemann_flux", "mvmm_riemann_sample", "mvmm_get_stats",
-    "mvmm_ctx_create_batched", "mvmm_batch_state",
+    "mvmm_ctx_create_batched", "mvmm_batch_state", "mvmm_autotune",
 )
 
 
@@ -82,6 +82,7 @@ def load_library(path: str = LIB_PATH):
         "mvmm_get_stats": (i32, [vp, vp]),
         "mvmm_ctx_create_batched": (i32, [vp, vp, i64, vp, vp, ctypes.POINTER(vp)]),
         "mvmm_batch_state": (i32, [vp, vp, vp, vp, vp, vp, vp]),
+        "mvmm_autotune": (i32, [vp, i32, pi32, pi32]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -214,6 +215,10 @@ class GpuSim:
 
     # ---- asynchronous stepping for timing ----
     def set_time(self):
+        """Writes the host's sync point to the device timeline (a batch keeps
+        each simulation's own device timeline, so this is a no-op for it)."""
+        if self.n_instances > 1:
+            return
         _check(load_library().mvmm_set_time(self.h, self.ti_current, self.ti_old), self.h)
 
     def enqueue_steps(self, n: int):
@@ -234,6 +239,12 @@ class GpuSim:
         _check(load_library().mvmm_batch_state(self.h, tc.ctypes.data, to.ctypes.data, st.ctypes.data, af.ctypes.data,
                                                err.ctypes.data, fin.ctypes.data), self.h)
         return {"ti_current": tc, "ti_old": to, "steps": st, "active_faces": af, "err": err, "finished": fin}
+
+    def autotune(self, steps: int = 3):
+        """Picks the thread-block sizes by timing this workload (state is restored)."""
+        bf, bc = ctypes.c_int(0), ctypes.c_int(0)
+        _check(load_library().mvmm_autotune(self.h, steps, ctypes.byref(bf), ctypes.byref(bc)), self.h)
+        return bf.value, bc.value
 
     def stats(self) -> dict:
         a = np.zeros(4, dtype=np.int64)

@@ -175,6 +175,12 @@ typedef struct mvmm_stats {
     int64_t steps, active_faces, active_cells, fp64_fallback_faces;
 } mvmm_stats;
 int mvmm_get_stats(mvmm_ctx *ctx, mvmm_stats *out);
+/* Autotuner (no counterpart in the reference): times `steps` steps of this
+ * context's own workload for each thread-block size of the face kernel and of
+ * the cell kernels (64, 128, 256), keeps the fastest pair and restores the
+ * state it started from (it allocates a temporary device copy of the cell
+ * state).  Returns the chosen sizes. */
+int mvmm_autotune(mvmm_ctx *ctx, int steps, int *blk_face, int *blk_cell);
 /* Per-kernel timing of the step (events around each kernel on the context
  * stream): enable, then read the accumulated milliseconds and launch counts
  * of the MVMM_NUM_KERNELS kernels in the order predict, face_flux, update,

@@ -96,3 +96,23 @@ def test_failed_simulation_stops_alone(gpu_lib):
         alone = G.GpuSim(p)
         alone.run()
         assert np.array_equal(parts[k].cons, alone.state().cons), k
+
+
+def test_autotune_keeps_state_and_results(gpu_lib):
+    """The autotuner restores the state it timed from; block sizes do not change results."""
+    p = ics.kelvin_helmholtz_2d(32, riemann=ics.EXACT)
+    a = G.GpuSim(p, precision=1)
+    b = G.GpuSim(p, precision=1)
+    a.run(max_steps=3)
+    b.run(max_steps=3)
+    before = a.state()
+    bf, bc = a.autotune(2)
+    assert bf in (64, 128, 256) and bc in (64, 128, 256)
+    after = a.state()
+    for f in ("cons", "prim", "grad", "dt"):
+        assert np.array_equal(before.arrays[f], after.arrays[f]), f
+    a.run(max_steps=5)
+    b.run(max_steps=5)
+    assert a.ti_current == b.ti_current
+    for f in ("cons", "prim", "grad"):
+        assert np.array_equal(a.state().arrays[f], b.state().arrays[f]), f
