@@ -68,8 +68,10 @@ WORKLOADS = {
     "blast3d": "point_blast_3d {n}^3 jittered periodic Voronoi, HLLC, hierarchical time bins, gamma=5/3",
     # {n} independent 1D Riemann problems packed in one batch, N log-uniform in [200, 20000]
     "batch1d": "{n} independent 1D Riemann problems (N log-uniform 200..20000), exact solver, one batch, t_end=0.15",
+    # served: Poisson stream (50 req/s) of {n} isentropic-vortex runs, 32^2..512^2, HLLC, t_end=1
+    "serve2d": "{n} served isentropic-vortex requests (Poisson 50/s, 32^2..512^2 periodic Voronoi, HLLC, t_end=1)",
 }
-DEFAULT_N = {"kh2d": NX, "sod1d": 1000, "blast3d": 128, "batch1d": 512}
+DEFAULT_N = {"kh2d": NX, "sod1d": 1000, "blast3d": 128, "batch1d": 512, "serve2d": 60}
 
 
 def _problem(nx=NX, workload="kh2d"):
@@ -362,6 +364,61 @@ def run_ours(args):
     print(json.dumps(line))
 
 
+def run_serve(args):
+    """Config 5: continuous batching of a Poisson request stream (rank 0 only)."""
+    import torch
+
+    from hydro_rs_gb300 import serve
+
+    ws, rank = _dist()
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    if rank != 0:
+        return
+    reqs = serve.poisson_requests(args.nx, rate=50.0, seed=5)
+    srv = serve.Server(budget_bytes=32 << 30, chunk=16, precision=1)
+    t0 = time.perf_counter()
+    for nx in sorted({r.nx for r in reqs}):
+        srv.template(nx)  # host meshes, built once per resolution
+    mesh_s = time.perf_counter() - t0
+    warm = serve.poisson_requests(5, rate=1e6, seed=6, resolutions=sorted({r.nx for r in reqs}))
+    srv.run(warm, realtime=False)  # slots created, graphs captured
+    with _Clocks() as clk:
+        res, wall = srv.run(reqs, realtime=True)
+    clocks = clk.summary(0)
+    summ = serve.latency_summary(res, wall)
+    cpu = None
+    if not args.no_cpu:
+        from oracle import oracle as O
+
+        threads = os.cpu_count() or 1
+        done, t_cpu, faces = 0, 0.0, 0
+        for r in sorted(reqs, key=lambda r: r.nx)[:8]:
+            sim = O.OracleSim(srv.problem_for(r), n_threads=threads)
+            t1 = time.perf_counter()
+            sim.run()
+            t_cpu += time.perf_counter() - t1
+            faces += sim.active_faces
+            done += 1
+            if t_cpu > 20.0:
+                break
+        cpu = {"value": faces / t_cpu, "unit": UNIT, "cores": threads, "kind": "port",
+               "solves_per_s": done / t_cpu,
+               "sample": f"the {done} smallest requests of the stream run one after another to t_end on the oracle "
+                         f"({t_cpu:.1f} s)"}
+    line = {
+        "metric": METRIC, "value": summ["active_faces"] / wall, "unit": UNIT, "n_gpus": 1, "steps": None,
+        "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32-face/f64-accumulate", "data": "synthetic (seeded Poisson request stream, isentropic vortices)",
+        "config": {"workload": WORKLOADS["serve2d"].format(n=args.nx), "hbm_budget_bytes": srv.budget,
+                   "chunk_steps": srv.chunk, "mesh_build_s": round(mesh_s, 2)},
+        "serving": {k: v for k, v in summ.items()} | {"peak_concurrent": srv.peak_running,
+                                                       "slots": len(srv.slots), "slot_bytes": srv.used},
+        "cpu_baseline": cpu, "clocks": clocks,
+    }
+    srv.close()
+    print(json.dumps(line))
+
+
 def run_reference(args):
     ws, rank = _dist()
     if rank != 0:
@@ -410,6 +467,8 @@ def main():
         args.nx = DEFAULT_N[args.workload]
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "serve2d":
+        run_serve(args)
     else:
         run_ours(args)
 

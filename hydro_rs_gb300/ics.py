@@ -185,18 +185,12 @@ def point_blast_3d(n1d: int = 128, seed: int = 3, riemann: int = HLLC, t_end: fl
     return Problem("point_blast_3d", params, mesh, cells, extra={"n_hot": nh})
 
 
-def yee_vortex_2d(nx: int, beta: float, v_adv, seed: int = 5, box_len: float = 10.0, t_end: float = 1.0,
-                  riemann: int = HLLC, jitter: float = 0.1, cfl: float = 0.3) -> Problem:
-    """Isentropic (Yee) vortex, python/utils.py:242-256 (T_inf=1, gamma=1.4), advected by v_adv."""
-    gamma = 1.4
-    params = Params(gamma=gamma, cfl=cfl, riemann=riemann, boundary=PERIODIC, dimensionality=2,
-                    sync_all=True, t_end=t_end)
-    rng = np.random.default_rng(seed)
-    x, box, vpp, _ = lattice((box_len, box_len, 1.0), nx * nx, 2, jitter, rng)
-    mesh = mesh_voronoi(x, 2, box, True)
+def yee_cells(mesh: Mesh, x, beta: float, v_adv, gamma: float = 1.4, box_len: float = 10.0, T_inf: float = 1.0):
+    """Isentropic (Yee) vortex centred in the box plus a uniform advection velocity,
+    python/utils.py:242-256 (Hopkins 2016 appendix A), masses from the nominal
+    per-cell volume as in from_fn."""
     c = x[:2] - 0.5 * box_len
     r2 = (c * c).sum(axis=0)
-    T_inf = 1.0
     temp = T_inf - (gamma - 1) * beta ** 2 / (8 * gamma * math.pi ** 2) * np.exp(1 - r2)
     rho = np.power(temp, 1 / (gamma - 1))
     v_fac = 0.5 * beta / math.pi * np.exp(0.5 * (1 - r2))
@@ -204,8 +198,20 @@ def yee_vortex_2d(nx: int, beta: float, v_adv, seed: int = 5, box_len: float = 1
     vel[0] = -c[1] * v_fac + v_adv[0]
     vel[1] = c[0] * v_fac + v_adv[1]
     u = temp / (gamma - 1)
-    mass = rho * (box[0] * box[1] * box[2] / x.shape[1])
-    cells = cells_from_ic(mesh, x, mass, vel, u, gamma)
+    mass = rho * (box_len * box_len / x.shape[1])
+    return cells_from_ic(mesh, x, mass, vel, u, gamma)
+
+
+def yee_vortex_2d(nx: int, beta: float, v_adv, seed: int = 5, box_len: float = 10.0, t_end: float = 1.0,
+                  riemann: int = HLLC, jitter: float = 0.1, cfl: float = 0.3) -> Problem:
+    """Isentropic vortex on the periodic [0, box_len]^2 (T_inf = 1, gamma = 1.4), advected by v_adv."""
+    gamma = 1.4
+    params = Params(gamma=gamma, cfl=cfl, riemann=riemann, boundary=PERIODIC, dimensionality=2,
+                    sync_all=True, t_end=t_end)
+    rng = np.random.default_rng(seed)
+    x, box, vpp, _ = lattice((box_len, box_len, 1.0), nx * nx, 2, jitter, rng)
+    mesh = mesh_voronoi(x, 2, box, True)
+    cells = yee_cells(mesh, x, beta, v_adv, gamma, box_len)
     return Problem("yee_vortex_2d", params, mesh, cells, extra={"beta": beta, "v_adv": tuple(v_adv)})
 
 
