@@ -83,7 +83,8 @@ class _Slot:
     def __init__(self, gpu, torch, template, precision):
         self.stream = torch.cuda.Stream()
         self.sim = gpu.GpuSim(template, precision=precision, stream=self.stream.cuda_stream)
-        self.nx = template.extra["nx"]
+        # a context's time base is t_end / 2^57, so a slot serves one (resolution, t_end)
+        self.key = (template.extra["nx"], template.params.t_end)
         self.bytes = context_bytes(template.mesh.n_cells, template.mesh.n_faces, precision)
         self.req = None
         self.event = None
@@ -126,15 +127,15 @@ class Server:
         q.params.t_end = r.t_end
         return q
 
-    def _free_slot(self, nx):
+    def _free_slot(self, key):
         for s in self.slots:
-            if s.req is None and s.nx == nx:
+            if s.req is None and s.key == key:
                 return s
         return None
 
     def _admit(self, r: Request, now: float):
         q = self.problem_for(r)
-        s = self._free_slot(r.nx)
+        s = self._free_slot((r.nx, r.t_end))
         if s is None:
             need = context_bytes(q.mesh.n_cells, q.mesh.n_faces, self.precision)
             if self.used + need > self.budget:
@@ -147,11 +148,9 @@ class Server:
                         break
                 else:
                     return False
-            s = _Slot(self.gpu, self.torch, self.template(r.nx), self.precision)
+            s = _Slot(self.gpu, self.torch, q, self.precision)
             self.slots.append(s)
             self.used += s.bytes
-        if s.sim.problem.params.t_end != r.t_end:
-            raise ValueError("a slot serves one t_end")
         s.sim.upload(q.cells)
         s.sim.ti_current = s.sim.ti_old = 0
         s.sim.finished = False
