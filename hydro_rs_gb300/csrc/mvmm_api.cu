@@ -6,6 +6,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -16,11 +17,13 @@
 namespace mvmm {
 void launch_face_flux_fp64(const KP& p, int solver, cudaStream_t s);
 void launch_riemann_fp64(int kind, int sample, double gamma, int64_t n, const double* l, const double* r,
-                         const double* vf, const double* nrm, double* out, unsigned int* err, cudaStream_t s);
+                         const double* vf, const double* nrm, double* out, unsigned int* err, const RSx& x,
+                         cudaStream_t s);
 void launch_face_flux_fp32(const KP& p, int solver, cudaStream_t s);
 void launch_gradients32(const KP& p, cudaStream_t s);
 void launch_riemann_fp32(int kind, int sample, double gamma, int64_t n, const double* l, const double* r,
-                         const double* vf, const double* nrm, double* out, unsigned int* err, cudaStream_t s);
+                         const double* vf, const double* nrm, double* out, unsigned int* err, const RSx& x,
+                         cudaStream_t s);
 }  // namespace mvmm
 
 using namespace mvmm;
@@ -77,6 +80,27 @@ struct mvmm_ctx {
 
 namespace {
 
+RSx solver_settings(const mvmm_params& prm) {
+    RSx x;
+    x.kind = prm.riemann;
+    x.airs_threshold = prm.airs_threshold;
+    for (int k = 0; k < 3; k++) x.adv[k] = prm.advection_velocity[k];
+    return x;
+}
+
+// Settings each solver kind needs (MissingAIRSThreshold, errors.rs; the
+// velocity check of bin/main.rs:637-640).
+int check_solver(int kind, double airs_threshold, const double* adv) {
+    if (kind < MVMM_RIEMANN_HLLC || kind > MVMM_RIEMANN_LINEAR_ADVECTION)
+        return fail(MVMM_E_INVALID, "unknown Riemann solver");
+    if (kind == MVMM_RIEMANN_AIRS && std::isnan(airs_threshold))
+        return fail(MVMM_E_INVALID, "AIRS needs a threshold (airs_threshold is NaN)");
+    if (kind == MVMM_RIEMANN_LINEAR_ADVECTION &&
+        (!adv || !std::isfinite(adv[0]) || !std::isfinite(adv[1]) || !std::isfinite(adv[2])))
+        return fail(MVMM_E_INVALID, "LinearAdvection needs a finite advection_velocity");
+    return MVMM_OK;
+}
+
 KP make_kp(mvmm_ctx* c, int stage, int flux_rows) {
     KP p{};
     p.n = c->n;
@@ -120,6 +144,9 @@ KP make_kp(mvmm_ctx* c, int stage, int flux_rows) {
     p.face_list = c->face_list;
     p.blk_face = c->blk_face;
     p.blk_cell = c->blk_cell;
+    p.rsx = solver_settings(c->prm);
+    // a stage call to mvmm_gradients always estimates gradients
+    p.godunov = (!stage && c->prm.runner == MVMM_RUNNER_GODUNOV) ? 1 : 0;
     return p;
 }
 
@@ -270,7 +297,10 @@ static int create_impl(const mvmm_params* prm, const mvmm_mesh* m, int64_t n_ins
     *out = nullptr;
     if (!(prm->gamma > 1.0)) return fail(MVMM_E_INVALID, "gamma must be > 1");
     if (prm->dimensionality < 1 || prm->dimensionality > 3) return fail(MVMM_E_INVALID, "dimensionality must be 1..3");
-    if (prm->riemann < 0 || prm->riemann > 2) return fail(MVMM_E_INVALID, "unknown Riemann solver");
+    int rs = check_solver(prm->riemann, prm->airs_threshold, prm->advection_velocity);
+    if (rs) return rs;
+    if (prm->runner != MVMM_RUNNER_OPTIMAL_ORDER && prm->runner != MVMM_RUNNER_GODUNOV)
+        return fail(MVMM_E_INVALID, "unknown runner");
     if (prm->boundary < 0 || prm->boundary > 3) return fail(MVMM_E_INVALID, "unknown boundary");
     if (prm->precision < 0 || prm->precision > 1) return fail(MVMM_E_INVALID, "unknown precision");
     if (prm->eos < 0 || prm->eos > 1) return fail(MVMM_E_INVALID, "unknown equation of state");
@@ -766,8 +796,9 @@ int mvmm_profile_read(mvmm_ctx* c, double* ms, int64_t* launches) {
 
 // ---- Riemann over arrays ----------------------------------------------
 static int riemann_common(int kind, int precision, int sample, double gamma, int64_t n, const double* l,
-                          const double* r, const double* vf, const double* nrm, double* out) {
-    if (kind < 0 || kind > 2) return fail(MVMM_E_INVALID, "unknown Riemann solver");
+                          const double* r, const double* vf, const double* nrm, double* out, const RSx& x) {
+    int rs = check_solver(kind, x.airs_threshold, x.adv);
+    if (rs) return rs;
     if (precision < 0 || precision > 1) return fail(MVMM_E_INVALID, "unknown precision");
     if (!(gamma > 1.0)) return fail(MVMM_E_INVALID, "gamma must be > 1");
     if (n < 0 || (n > 0 && (!l || !r || !nrm || !out || (!sample && !vf)))) return fail(MVMM_E_INVALID, "bad arrays");
@@ -787,9 +818,9 @@ static int riemann_common(int kind, int precision, int sample, double gamma, int
     cudaMemcpy(dn, nrm, (size_t)n * 3 * 8, cudaMemcpyHostToDevice);
     cudaMemset(derr, 0, 4);
     if (precision == MVMM_PRECISION_FP32FACE)
-        launch_riemann_fp32(kind, sample, gamma, n, dl, dr, dv, dn, dout, derr, 0);
+        launch_riemann_fp32(kind, sample, gamma, n, dl, dr, dv, dn, dout, derr, x, 0);
     else
-        launch_riemann_fp64(kind, sample, gamma, n, dl, dr, dv, dn, dout, derr, 0);
+        launch_riemann_fp64(kind, sample, gamma, n, dl, dr, dv, dn, dout, derr, x, 0);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemcpy(out, dout, (size_t)n * 5 * 8, cudaMemcpyDeviceToHost);
     unsigned int herr = 0;
@@ -801,14 +832,37 @@ static int riemann_common(int kind, int precision, int sample, double gamma, int
     return MVMM_OK;
 }
 
+// The kind-only forms carry no AIRS threshold or advection velocity.
+static RSx no_settings(int kind) {
+    RSx x;
+    x.kind = kind;
+    x.airs_threshold = NAN;
+    x.adv[0] = x.adv[1] = x.adv[2] = NAN;
+    return x;
+}
+
 int mvmm_riemann_flux(int kind, int precision, double gamma, int64_t n, const double* left, const double* right,
                       const double* v_face, const double* normal, double* out) {
-    return riemann_common(kind, precision, 0, gamma, n, left, right, v_face, normal, out);
+    return riemann_common(kind, precision, 0, gamma, n, left, right, v_face, normal, out, no_settings(kind));
 }
 
 int mvmm_riemann_sample(int kind, int precision, double gamma, int64_t n, const double* left, const double* right,
                         const double* normal, double* out) {
-    return riemann_common(kind, precision, 1, gamma, n, left, right, nullptr, normal, out);
+    return riemann_common(kind, precision, 1, gamma, n, left, right, nullptr, normal, out, no_settings(kind));
+}
+
+int mvmm_riemann_flux_p(const mvmm_params* p, int64_t n, const double* left, const double* right,
+                        const double* v_face, const double* normal, double* out) {
+    if (!p) return fail(MVMM_E_INVALID, "null params");
+    return riemann_common(p->riemann, p->precision, 0, p->gamma, n, left, right, v_face, normal, out,
+                          solver_settings(*p));
+}
+
+int mvmm_riemann_sample_p(const mvmm_params* p, int64_t n, const double* left, const double* right,
+                          const double* normal, double* out) {
+    if (!p) return fail(MVMM_E_INVALID, "null params");
+    return riemann_common(p->riemann, p->precision, 1, p->gamma, n, left, right, nullptr, normal, out,
+                          solver_settings(*p));
 }
 
 }  // extern "C"

@@ -12,6 +12,8 @@
 #include <math.h>
 #include <stdint.h>
 
+#include "mvmm_internal.h"
+
 namespace mvmm {
 
 // ------------------------------------------------------------------ math --
@@ -170,6 +172,13 @@ struct Gas {
         return m_pow(x, gamma * tdgm1());
     }
     __device__ __forceinline__ T pow_ginv(T x) const;
+    // x^(1 / gm1d2g) with the exponent rounded as `1. / beta` is (trrs.rs:28-29):
+    // an integer power when that exponent is the integer m
+    __device__ __forceinline__ T pow_igm1d2g(T x) const {
+        T e = T(1) / gm1d2g();
+        if (rm && e == T(rm)) return ipow(x, rm);
+        return m_pow(x, e);
+    }
 };
 // pow(+-0, y) is +0 for y > 0 and +inf for y < 0 (IEEE 754 / C99 F.9.4.4):
 // answered directly, as the exact solver evaluates f(0) on every face.
@@ -785,20 +794,80 @@ __device__ __forceinline__ Star<T> pv_star(const St<T>& l, const St<T>& r, T vl,
     return s;
 }
 
-enum { SOLVER_HLLC = 0, SOLVER_EXACT = 1, SOLVER_PVRS = 2 };
-
-// Blanket RiemannFluxSolver impl for star solvers: half state (riemann_solver.rs:258-284).
-template <typename T, int SOLVER>
-__device__ __forceinline__ St<T> star_half_state(const St<T>& l, const St<T>& r, V3<T> n, const Gas<T>& g,
-                                                 const Gas<double>& g64, int max_iter, unsigned int* err) {
-    T vl = dot(vel(l), n);
-    T vr = dot(vel(r), n);
-    T al = g.sound_speed(l.q[4], T(1) / l.q[0]);
-    T ar = g.sound_speed(r.q[4], T(1) / r.q[0]);
-    T vrml = vr - vl;
-    if (is_vacuum(l, r, al, ar, vrml, g)) return vacuum_sample(l, r, vl, vr, al, ar, n, g);
+// ExactRiemannSolver::fb, middle_density and star_state_from_pstar
+// (exact.rs:12-20, 193-238) in the face type T, for the star solvers that
+// estimate p* in closed form and take the rest from the exact relations.
+template <typename T>
+__device__ __forceinline__ T xs_fb(T p, T rho, T ps, T a, const Gas<T>& g) {
+    if (p > ps) {
+        T cap_a = g.tdgp1() / rho;
+        T cap_b = g.gm1dgp1() * ps;
+        return (p - ps) * m_sqrt(cap_a / (p + cap_b));
+    }
+    return g.tdgm1() * a * (g.pow_e1(p / ps) - T(1));
+}
+template <typename T>
+__device__ __forceinline__ T xs_middle_density(T p, T rho, T ps, const Gas<T>& g) {
+    T pdps = p / ps;
+    if (pdps > T(1)) return rho * (pdps + g.gm1dgp1()) / (g.gm1dgp1() * pdps + T(1));
+    return rho * g.pow_ginv(pdps);
+}
+template <typename T>
+__device__ __forceinline__ Star<T> star_from_pstar(T ps, const St<T>& l, const St<T>& r, T vl, T vr, T al, T ar,
+                                                   const Gas<T>& g) {
     Star<T> s;
-    if (SOLVER == SOLVER_EXACT && sizeof(T) == 4 && g64.rm) {
+    s.u = T(0.5) * (vl + vr) + T(0.5) * (xs_fb(ps, r.q[0], r.q[4], ar, g) - xs_fb(ps, l.q[0], l.q[4], al, g));
+    s.rho_l = xs_middle_density(ps, l.q[0], l.q[4], g);
+    s.rho_r = xs_middle_density(ps, r.q[0], r.q[4], g);
+    s.p = ps;
+    return s;
+}
+// TSRiemannSolver (riemann_solver/tsrs.rs:18-51): two-shock p* from the PVRS guess
+template <typename T>
+__device__ __forceinline__ Star<T> ts_star(const St<T>& l, const St<T>& r, T vl, T vr, T al, T ar,
+                                           const Gas<T>& g) {
+    T rho_bar = T(0.5) * (l.q[0] + r.q[0]);
+    T p_bar = T(0.5) * (l.q[4] + r.q[4]);
+    T a_bar = T(0.5) * (al + ar);
+    T p_guess = p_bar + T(0.5) * (vl - vr) * rho_bar * a_bar;  // PVRiemannSolver::p_star (pvrs.rs:20-22)
+    T g_l = m_sqrt((g.tdgp1() / l.q[0]) / (p_guess + g.gm1dgp1() * l.q[4]));
+    T g_r = m_sqrt((g.tdgp1() / r.q[0]) / (p_guess + g.gm1dgp1() * r.q[4]));
+    T ps = (g_l * l.q[4] + g_r * r.q[4] - (vr - vl)) / (g_l + g_r);
+    return star_from_pstar(ps, l, r, vl, vr, al, ar, g);
+}
+// TRRiemannSolver (riemann_solver/trrs.rs:14-32): two-rarefaction p*
+template <typename T>
+__device__ __forceinline__ Star<T> tr_star(const St<T>& l, const St<T>& r, T vl, T vr, T al, T ar,
+                                           const Gas<T>& g) {
+    T gm1d2 = T(0.5) * (g.gamma - T(1));
+    T num = al + ar - gm1d2 * (vr - vl);
+    T denom = al * g.pow_me1(l.q[4]) + ar * g.pow_me1(r.q[4]);  // p^-beta
+    T ps = g.pow_igm1d2g(num / denom);
+    return star_from_pstar(ps, l, r, vl, vr, al, ar, g);
+}
+
+// Solver kinds (riemann_solver.rs:28-44, bin/main.rs:625-642).  The face
+// kernels are instantiated for HLLC, EXACT and PVRS; the other kinds share one
+// instantiation (SOLVER_EXTRA) that switches on RSx::kind at run time.
+enum {
+    SOLVER_HLLC = 0,
+    SOLVER_EXACT = 1,
+    SOLVER_PVRS = 2,
+    SOLVER_AIRS = 3,
+    SOLVER_TSRS = 4,
+    SOLVER_TRRS = 5,
+    SOLVER_LINADV = 6,
+    SOLVER_EXTRA = 7
+};
+
+// Exact star state in the face type: FP32 search + FP64 polish for the
+// FP32-face form with a rational gamma, else the FP64 reference iteration.
+template <typename T>
+__device__ __forceinline__ Star<T> exact_star(const St<T>& l, const St<T>& r, T vl, T vr, T al, T ar,
+                                              const Gas<T>& g, const Gas<double>& g64, int max_iter,
+                                              unsigned int* err) {
+    Star<T> s;
+    if (sizeof(T) == 4 && g64.rm) {
         Star<float> sf = ex_star_split(float(l.q[0]), float(l.q[4]), float(al), float(r.q[0]), float(r.q[4]),
                                        float(ar), float(vl), float(vr), make_gas<float>(double(g.gamma), g.eos,
                                        double(g.iso_u)), g64, max_iter, err);
@@ -806,7 +875,7 @@ __device__ __forceinline__ St<T> star_half_state(const St<T>& l, const St<T>& r,
         s.rho_r = T(sf.rho_r);
         s.u = T(sf.u);
         s.p = T(sf.p);
-    } else if (SOLVER == SOLVER_EXACT) {
+    } else {
         ExSide L{double(l.q[0]), double(l.q[4]), double(al)};
         ExSide R{double(r.q[0]), double(r.q[4]), double(ar)};
         Star<double> sd = ex_star(L, R, double(vl), double(vr), g64, max_iter, err);
@@ -814,8 +883,36 @@ __device__ __forceinline__ St<T> star_half_state(const St<T>& l, const St<T>& r,
         s.rho_r = T(sd.rho_r);
         s.u = T(sd.u);
         s.p = T(sd.p);
+    }
+    return s;
+}
+
+// Blanket RiemannFluxSolver impl for star solvers: half state (riemann_solver.rs:258-284).
+template <typename T, int SOLVER>
+__device__ __forceinline__ St<T> star_half_state(const St<T>& l, const St<T>& r, V3<T> n, const Gas<T>& g,
+                                                 const Gas<double>& g64, int max_iter, unsigned int* err,
+                                                 const RSx* x = nullptr) {
+    T vl = dot(vel(l), n);
+    T vr = dot(vel(r), n);
+    T al = g.sound_speed(l.q[4], T(1) / l.q[0]);
+    T ar = g.sound_speed(r.q[4], T(1) / r.q[0]);
+    T vrml = vr - vl;
+    if (is_vacuum(l, r, al, ar, vrml, g)) return vacuum_sample(l, r, vl, vr, al, ar, n, g);
+    const int kind = SOLVER == SOLVER_EXTRA ? x->kind : SOLVER;
+    Star<T> s;
+    if (kind == SOLVER_EXACT) {
+        s = exact_star(l, r, vl, vr, al, ar, g, g64, max_iter, err);
+    } else if (kind == SOLVER_TSRS) {
+        s = ts_star(l, r, vl, vr, al, ar, g);
+    } else if (kind == SOLVER_TRRS) {
+        s = tr_star(l, r, vl, vr, al, ar, g);
     } else {
         s = pv_star(l, r, vl, vr, al, ar);
+        if (kind == SOLVER_AIRS) {  // AIRiemannSolver (airs.rs:18-38)
+            T p_max = m_max(l.q[4], r.q[4]);
+            T p_min = m_min(l.q[4], r.q[4]);
+            if (!(p_max / p_min < T(x->airs_threshold))) s = exact_star(l, r, vl, vr, al, ar, g, g64, max_iter, err);
+        }
     }
     return sample_star(s, l, r, vl, vr, al, ar, n, g);
 }
@@ -879,11 +976,24 @@ __device__ St<T> hllc_solve(const St<T>& l, const St<T>& r, V3<T> iv, V3<T> n, c
     return flux + add;
 }
 
+// LinearAdvectionRiemannSover::solve_for_flux (riemann_solver/linear_advection.rs:17-34):
+// the upwind (density, velocity, pressure) vector times the advection speed
+template <typename T>
+__device__ __forceinline__ St<T> linear_advection_flux(const St<T>& l, const St<T>& r, V3<T> iv, V3<T> n,
+                                                       const RSx& x) {
+    V3<T> va = {T(x.adv[0]), T(x.adv[1]), T(x.adv[2])};
+    T v = dot(va - iv, n);
+    if (v > T(0)) return v * l;
+    return v * r;
+}
+
 template <typename T, int SOLVER>
 __device__ __forceinline__ St<T> solve_for_flux(const St<T>& l, const St<T>& r, V3<T> iv, V3<T> n, const Gas<T>& g,
-                                                const Gas<double>& g64, int max_iter, unsigned int* err) {
+                                                const Gas<double>& g64, int max_iter, unsigned int* err,
+                                                const RSx* x = nullptr) {
     if (SOLVER == SOLVER_HLLC) return hllc_solve(l, r, iv, n, g);
-    St<T> w = star_half_state<T, SOLVER>(l, r, n, g, g64, max_iter, err);
+    if (SOLVER == SOLVER_EXTRA && x->kind == SOLVER_LINADV) return linear_advection_flux(l, r, iv, n, *x);
+    St<T> w = star_half_state<T, SOLVER>(l, r, n, g, g64, max_iter, err, x);
     return flux_from_half_state(w, iv, n, g);
 }
 

@@ -6,6 +6,14 @@
 
 namespace mvmm {
 
+// Run-time solver settings: kind (SOLVER_*), AIRiemannSolver threshold
+// (airs.rs:8-16) and LinearAdvectionRiemannSover velocity (linear_advection.rs:7-15).
+struct RSx {
+    int kind;
+    double airs_threshold;
+    double adv[3];
+};
+
 // Cell state on the device: one float64 block of kCellFields * n doubles,
 // field f of cell i at cd[f * n + i] (SoA; rows as in mvmm_cells).
 enum CellField : int {
@@ -99,6 +107,8 @@ struct KP {
     const double* inst_tb;   // per-instance time_base (nullptr: time_base)
     const double* inst_tbi;  // per-instance 1 / time_base (nullptr: time_base_inv)
     int blk_face, blk_cell;  // thread-block sizes (chosen by mvmm_autotune)
+    RSx rsx;                 // Riemann solver kind and its settings
+    int godunov;             // 1: GodunovHydroRunner (no gradients), 0: OptimalOrderRunner
     int use_list;            // 1: face kernel walks the compacted active-face list
     uint8_t* face_act;       // per-face flag of this step's active-face rule
     int* face_list;          // compacted active faces
@@ -115,8 +125,6 @@ void launch_timesteps(const KP& p, double* dt_out, cudaStream_t s);
 void launch_limit(const KP& p, cudaStream_t s);
 void launch_compact(const KP& p, cudaStream_t s);
 void launch_end(const KP& p, cudaStream_t s);
-void launch_riemann(int kind, int precision, int sample, double gamma, int64_t n, const double* l, const double* r,
-                    const double* vf, const double* nrm, double* out, unsigned int* err, cudaStream_t s);
 // FP32 form helpers
 void launch_prep32(const KP& p, cudaStream_t s);
 

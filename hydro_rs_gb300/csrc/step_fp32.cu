@@ -100,7 +100,7 @@ __device__ __forceinline__ Out32 face_interior32(const KP& p, int f, int l, int 
     V3<float> nrm = cvt<float>(F3(p.normal, p.nf, f));
     V3<float> mvf = neg(v_face);
     St<float> F = solve_for_flux<float, SOLVER>(boost(prim_left, mvf), boost(prim_right, mvf), v_face, nrm, g, g64,
-                                                p.max_iter, err);
+                                                p.max_iter, err, &p.rsx);
     double area = p.area[f];
     Out32 o;
 #pragma unroll
@@ -147,7 +147,7 @@ __device__ __forceinline__ Out32 face_boundary32(const KP& p, int f, int i, cons
         v_max += fminf(dot(vel(prim), dx_centroid), 0.f);
         bnd = vac;
     }
-    St<float> F = solve_for_flux<float, SOLVER>(dash, bnd, v3(0.f, 0.f, 0.f), n, g, g64, p.max_iter, err);
+    St<float> F = solve_for_flux<float, SOLVER>(dash, bnd, v3(0.f, 0.f, 0.f), n, g, g64, p.max_iter, err, &p.rsx);
     double area = p.area[f];
     Out32 o;
 #pragma unroll
@@ -228,6 +228,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_gradients32(KP p) {
     if (k >= 0) {
         int tb = p.timebin[i];
         if (p.active[i]) {
+          if (!p.godunov) {  // GodunovHydroRunner::step has no gradient stage (godunov.rs:14-58)
             V3<double> cen = C3(p, F_CEN, i);
             St<double> prim = C5(p, F_PRIM, i);
             float a00 = 0.f, a01 = 0.f, a02 = 0.f, a11 = 0.f, a12 = 0.f, a22 = 0.f;
@@ -300,6 +301,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_gradients32(KP p) {
                 W3(p, F_GRAD + 3 * q, i, cvt<double>(gr[q]));
             }
             W3(p, F_GC, i, cen);
+          }
             double dt_new = particle_timestep(p, i);
             unsigned long long tc = p.tl[k].ti_current;
             unsigned long long dti = make_integer_timestep(dt_new, tb, NUM_TIME_BINS, tc, tbase_inv(p, k));
@@ -317,7 +319,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_gradients32(KP p) {
 
 template <int SOLVER, bool SAMPLE>
 __global__ void k_riemann32(double gamma, int64_t n, const double* l, const double* r, const double* vf,
-                            const double* nrm, double* out, unsigned int* errp) {
+                            const double* nrm, double* out, unsigned int* errp, RSx x) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     Gas<float> g = make_gas<float>(gamma, 0, 0.);
@@ -332,10 +334,10 @@ __global__ void k_riemann32(double gamma, int64_t n, const double* l, const doub
     unsigned int err = 0;
     St<float> o;
     if (SAMPLE) {
-        o = star_half_state<float, SOLVER == SOLVER_HLLC ? SOLVER_EXACT : SOLVER>(L, R, nn, g, g64, 1000, &err);
+        o = star_half_state<float, SOLVER>(L, R, nn, g, g64, 1000, &err, &x);
     } else {
         V3<float> iv = v3((float)vf[i], (float)vf[n + i], (float)vf[2 * n + i]);
-        o = solve_for_flux<float, SOLVER>(L, R, iv, nn, g, g64, 1000, &err);
+        o = solve_for_flux<float, SOLVER>(L, R, iv, nn, g, g64, 1000, &err, &x);
     }
 #pragma unroll
     for (int q = 0; q < 5; q++) out[q * n + i] = (double)o.q[q];
@@ -361,20 +363,25 @@ void launch_face_flux_fp32(const KP& p, int solver, cudaStream_t s) {
     if (p.use_list && g > cap) g = cap;
     if (solver == SOLVER_HLLC) k_face_flux32<SOLVER_HLLC><<<g, p.blk_face, 0, s>>>(p);
     else if (solver == SOLVER_EXACT) k_face_flux32<SOLVER_EXACT><<<g, p.blk_face, 0, s>>>(p);
-    else k_face_flux32<SOLVER_PVRS><<<g, p.blk_face, 0, s>>>(p);
+    else if (solver == SOLVER_PVRS) k_face_flux32<SOLVER_PVRS><<<g, p.blk_face, 0, s>>>(p);
+    else k_face_flux32<SOLVER_EXTRA><<<g, p.blk_face, 0, s>>>(p);
 }
 
 void launch_riemann_fp32(int kind, int sample, double gamma, int64_t n, const double* l, const double* r,
-                         const double* vf, const double* nrm, double* out, unsigned int* err, cudaStream_t s) {
+                         const double* vf, const double* nrm, double* out, unsigned int* err, const RSx& x,
+                         cudaStream_t s) {
     if (n <= 0) return;
     int g = (int)((n + kBlock - 1) / kBlock);
     if (sample) {
-        if (kind == SOLVER_PVRS) k_riemann32<SOLVER_PVRS, true><<<g, kBlock, 0, s>>>(gamma, n, l, r, vf, nrm, out, err);
-        else k_riemann32<SOLVER_EXACT, true><<<g, kBlock, 0, s>>>(gamma, n, l, r, vf, nrm, out, err);
+        if (kind == SOLVER_PVRS) k_riemann32<SOLVER_PVRS, true><<<g, kBlock, 0, s>>>(gamma, n, l, r, vf, nrm, out, err, x);
+        else if (kind >= SOLVER_AIRS && kind <= SOLVER_TRRS)
+            k_riemann32<SOLVER_EXTRA, true><<<g, kBlock, 0, s>>>(gamma, n, l, r, vf, nrm, out, err, x);
+        else k_riemann32<SOLVER_EXACT, true><<<g, kBlock, 0, s>>>(gamma, n, l, r, vf, nrm, out, err, x);
     } else {
-        if (kind == SOLVER_HLLC) k_riemann32<SOLVER_HLLC, false><<<g, kBlock, 0, s>>>(gamma, n, l, r, vf, nrm, out, err);
-        else if (kind == SOLVER_EXACT) k_riemann32<SOLVER_EXACT, false><<<g, kBlock, 0, s>>>(gamma, n, l, r, vf, nrm, out, err);
-        else k_riemann32<SOLVER_PVRS, false><<<g, kBlock, 0, s>>>(gamma, n, l, r, vf, nrm, out, err);
+        if (kind == SOLVER_HLLC) k_riemann32<SOLVER_HLLC, false><<<g, kBlock, 0, s>>>(gamma, n, l, r, vf, nrm, out, err, x);
+        else if (kind == SOLVER_EXACT) k_riemann32<SOLVER_EXACT, false><<<g, kBlock, 0, s>>>(gamma, n, l, r, vf, nrm, out, err, x);
+        else if (kind == SOLVER_PVRS) k_riemann32<SOLVER_PVRS, false><<<g, kBlock, 0, s>>>(gamma, n, l, r, vf, nrm, out, err, x);
+        else k_riemann32<SOLVER_EXTRA, false><<<g, kBlock, 0, s>>>(gamma, n, l, r, vf, nrm, out, err, x);
     }
 }
 

@@ -141,7 +141,7 @@ __device__ __forceinline__ FaceOut face_interior(const KP& p, int f, int l, int 
     V3<double> nrm = F3(p.normal, p.nf, f);
     V3<double> mvf = neg(v_face);
     St<double> F = solve_for_flux<double, SOLVER>(boost(prim_left, mvf), boost(prim_right, mvf), v_face, nrm, g, g,
-                                                  p.max_iter, err);
+                                                  p.max_iter, err, &p.rsx);
     double area = p.area[f];
     St<double> fluxes = area * F;
     FaceOut o;
@@ -188,7 +188,7 @@ __device__ __forceinline__ FaceOut face_boundary(const KP& p, int f, int i, unsi
         v_max += m_min(dot(vel(prim), dx_centroid), 0.);
         bnd = vac;
     }
-    St<double> F = solve_for_flux<double, SOLVER>(dash, bnd, v3(0., 0., 0.), n, g, g, p.max_iter, err);
+    St<double> F = solve_for_flux<double, SOLVER>(dash, bnd, v3(0., 0., 0.), n, g, g, p.max_iter, err, &p.rsx);
     double area = p.area[f];
     St<double> fluxes = area * F;
     FaceOut o;
@@ -389,6 +389,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_gradients(KP p, int do_timestep) 
     if (k >= 0) {
         int tb = p.timebin[i];
         if (p.active[i]) {
+          if (!p.godunov) {  // GodunovHydroRunner::step has no gradient stage (godunov.rs:14-58)
             V3<double> cen = C3(p, F_CEN, i);
             St<double> prim = C5(p, F_PRIM, i);
             // GradientData::init (gradients.rs:14-33).  The WLS matrix is
@@ -480,6 +481,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_gradients(KP p, int do_timestep) 
                 W3(p, F_GRAD + 3 * q, i, gr[q]);
             }
             W3(p, F_GC, i, cen);  // gradient_apply
+          }
             if (do_timestep) {
                 double dt_new = particle_timestep(p, i);
                 unsigned long long tc = p.tl[k].ti_current;
@@ -589,7 +591,7 @@ __global__ void k_end(KP p) {
 // ---------------------------------------------- Riemann over arrays --
 template <int SOLVER, bool SAMPLE>
 __global__ void k_riemann(double gamma, int64_t n, const double* l, const double* r, const double* vf,
-                          const double* nrm, double* out, unsigned int* errp) {
+                          const double* nrm, double* out, unsigned int* errp, RSx x) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     Gas<double> g = make_gas<double>(gamma, 0, 0.);
@@ -603,10 +605,10 @@ __global__ void k_riemann(double gamma, int64_t n, const double* l, const double
     unsigned int err = 0;
     St<double> o;
     if (SAMPLE) {
-        o = star_half_state<double, SOLVER == SOLVER_HLLC ? SOLVER_EXACT : SOLVER>(L, R, nn, g, g, 1000, &err);
+        o = star_half_state<double, SOLVER>(L, R, nn, g, g, 1000, &err, &x);
     } else {
         V3<double> iv = v3(vf[i], vf[n + i], vf[2 * n + i]);
-        o = solve_for_flux<double, SOLVER>(L, R, iv, nn, g, g, 1000, &err);
+        o = solve_for_flux<double, SOLVER>(L, R, iv, nn, g, g, 1000, &err, &x);
     }
 #pragma unroll
     for (int q = 0; q < 5; q++) out[q * n + i] = o.q[q];
@@ -634,7 +636,8 @@ void launch_face_flux_fp64(const KP& p, int solver, cudaStream_t s) {
     int g = face_grid(p);
     if (solver == SOLVER_HLLC) k_face_flux<SOLVER_HLLC><<<g, p.blk_face, 0, s>>>(p);
     else if (solver == SOLVER_EXACT) k_face_flux<SOLVER_EXACT><<<g, p.blk_face, 0, s>>>(p);
-    else k_face_flux<SOLVER_PVRS><<<g, p.blk_face, 0, s>>>(p);
+    else if (solver == SOLVER_PVRS) k_face_flux<SOLVER_PVRS><<<g, p.blk_face, 0, s>>>(p);
+    else k_face_flux<SOLVER_EXTRA><<<g, p.blk_face, 0, s>>>(p);
 }
 void launch_compact(const KP& p, cudaStream_t s) {
     if (p.nf > 0) k_compact<<<grid(p.nf, p.blk_cell), p.blk_cell, 0, s>>>(p);
@@ -656,17 +659,23 @@ void launch_limit(const KP& p, cudaStream_t s) {
 }
 void launch_end(const KP& p, cudaStream_t s) { k_end<<<(p.n_inst + 127) / 128, 128, 0, s>>>(p); }
 
+// kind: SOLVER_*; sampling is defined for the star solvers, so HLLC and
+// linear advection sample the exact solution.
 void launch_riemann_fp64(int kind, int sample, double gamma, int64_t n, const double* l, const double* r,
-                         const double* vf, const double* nrm, double* out, unsigned int* err, cudaStream_t s) {
+                         const double* vf, const double* nrm, double* out, unsigned int* err, const RSx& x,
+                         cudaStream_t s) {
     if (n <= 0) return;
     int g = (int)((n + kBlock - 1) / kBlock);
     if (sample) {
-        if (kind == SOLVER_PVRS) k_riemann<SOLVER_PVRS, true><<<g, kBlock, 0, s>>>(gamma, n, l, r, vf, nrm, out, err);
-        else k_riemann<SOLVER_EXACT, true><<<g, kBlock, 0, s>>>(gamma, n, l, r, vf, nrm, out, err);
+        if (kind == SOLVER_PVRS) k_riemann<SOLVER_PVRS, true><<<g, kBlock, 0, s>>>(gamma, n, l, r, vf, nrm, out, err, x);
+        else if (kind >= SOLVER_AIRS && kind <= SOLVER_TRRS)
+            k_riemann<SOLVER_EXTRA, true><<<g, kBlock, 0, s>>>(gamma, n, l, r, vf, nrm, out, err, x);
+        else k_riemann<SOLVER_EXACT, true><<<g, kBlock, 0, s>>>(gamma, n, l, r, vf, nrm, out, err, x);
     } else {
-        if (kind == SOLVER_HLLC) k_riemann<SOLVER_HLLC, false><<<g, kBlock, 0, s>>>(gamma, n, l, r, vf, nrm, out, err);
-        else if (kind == SOLVER_EXACT) k_riemann<SOLVER_EXACT, false><<<g, kBlock, 0, s>>>(gamma, n, l, r, vf, nrm, out, err);
-        else k_riemann<SOLVER_PVRS, false><<<g, kBlock, 0, s>>>(gamma, n, l, r, vf, nrm, out, err);
+        if (kind == SOLVER_HLLC) k_riemann<SOLVER_HLLC, false><<<g, kBlock, 0, s>>>(gamma, n, l, r, vf, nrm, out, err, x);
+        else if (kind == SOLVER_EXACT) k_riemann<SOLVER_EXACT, false><<<g, kBlock, 0, s>>>(gamma, n, l, r, vf, nrm, out, err, x);
+        else if (kind == SOLVER_PVRS) k_riemann<SOLVER_PVRS, false><<<g, kBlock, 0, s>>>(gamma, n, l, r, vf, nrm, out, err, x);
+        else k_riemann<SOLVER_EXTRA, false><<<g, kBlock, 0, s>>>(gamma, n, l, r, vf, nrm, out, err, x);
     }
 }
 

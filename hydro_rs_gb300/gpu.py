@@ -25,7 +25,7 @@ EXPORTED = (
     "mvmm_convert_conserved_to_primitive", "mvmm_compute_timesteps", "mvmm_apply_fluxes", "mvmm_gradients",
     "mvmm_step", "mvmm_run", "mvmm_enqueue_steps", "mvmm_set_time", "mvmm_get_time", "mvmm_profile_enable",
     "mvmm_profile_read", "mvmm_riemann_flux", "mvmm_riemann_sample", "mvmm_get_stats",
-    "mvmm_ctx_create_batched", "mvmm_batch_state", "mvmm_autotune",
+    "mvmm_ctx_create_batched", "mvmm_batch_state", "mvmm_autotune", "mvmm_riemann_flux_p", "mvmm_riemann_sample_p",
 )
 
 
@@ -40,7 +40,17 @@ class _Params(ctypes.Structure):
     _fields_ = [("gamma", ctypes.c_double), ("eos", ctypes.c_int), ("isothermal_internal_energy", ctypes.c_double),
                 ("cfl", ctypes.c_double), ("riemann", ctypes.c_int), ("boundary", ctypes.c_int),
                 ("dimensionality", ctypes.c_int), ("sync_all", ctypes.c_int), ("t_end", ctypes.c_double),
-                ("max_newton_iter", ctypes.c_int), ("precision", ctypes.c_int), ("particle_motion", ctypes.c_int)]
+                ("max_newton_iter", ctypes.c_int), ("precision", ctypes.c_int), ("particle_motion", ctypes.c_int),
+                ("runner", ctypes.c_int), ("airs_threshold", ctypes.c_double),
+                ("advection_velocity", ctypes.c_double * 3)]
+
+
+def make_params(p, precision=None) -> _Params:
+    """mvmm_params from an ics.Params (precision overrides p.precision)."""
+    thr, adv = p.solver_extras()
+    prec = p.precision if precision is None else precision
+    return _Params(p.gamma, 0, 0.0, p.cfl, p.riemann, p.boundary, p.dimensionality, int(p.sync_all), p.t_end,
+                   p.max_newton_iter, prec, 0, p.runner, thr, (ctypes.c_double * 3)(*adv))
 
 
 _LIB = None
@@ -79,6 +89,8 @@ def load_library(path: str = LIB_PATH):
         "mvmm_profile_read": (i32, [vp, vp, vp]),
         "mvmm_riemann_flux": (i32, [i32, i32, dbl, i64, vp, vp, vp, vp, vp]),
         "mvmm_riemann_sample": (i32, [i32, i32, dbl, i64, vp, vp, vp, vp]),
+        "mvmm_riemann_flux_p": (i32, [vp, i64, vp, vp, vp, vp, vp]),
+        "mvmm_riemann_sample_p": (i32, [vp, i64, vp, vp, vp, vp]),
         "mvmm_get_stats": (i32, [vp, vp]),
         "mvmm_ctx_create_batched": (i32, [vp, vp, i64, vp, vp, ctypes.POINTER(vp)]),
         "mvmm_batch_state": (i32, [vp, vp, vp, vp, vp, vp, vp]),
@@ -103,25 +115,42 @@ def _soa(a, k):
     return np.ascontiguousarray(np.asarray(a, dtype=np.float64).reshape(k, -1))
 
 
-def riemann_flux(kind: int, gamma: float, left, right, v_face, normal, precision: int = 0):
+def _solver_params(kind, gamma, precision, airs_threshold, velocity):
+    from .ics import Params
+    return make_params(Params(gamma=gamma, riemann=kind, precision=precision, airs_threshold=airs_threshold,
+                              advection_velocity=velocity))
+
+
+def riemann_flux(kind: int, gamma: float, left, right, v_face, normal, precision: int = 0,
+                 airs_threshold=None, velocity=None):
     """RiemannFluxSolver::solve_for_flux over arrays on the GPU."""
     L = load_library()
     left, right, v_face, normal = _soa(left, 5), _soa(right, 5), _soa(v_face, 3), _soa(normal, 3)
     n = left.shape[1]
     out = np.zeros((5, n))
-    _check(L.mvmm_riemann_flux(kind, precision, gamma, n, left.ctypes.data, right.ctypes.data, v_face.ctypes.data,
-                               normal.ctypes.data, out.ctypes.data))
+    if airs_threshold is None and velocity is None:
+        _check(L.mvmm_riemann_flux(kind, precision, gamma, n, left.ctypes.data, right.ctypes.data,
+                                   v_face.ctypes.data, normal.ctypes.data, out.ctypes.data))
+    else:
+        prm = _solver_params(kind, gamma, precision, airs_threshold, velocity)
+        _check(L.mvmm_riemann_flux_p(ctypes.byref(prm), n, left.ctypes.data, right.ctypes.data, v_face.ctypes.data,
+                                     normal.ctypes.data, out.ctypes.data))
     return out
 
 
-def riemann_sample(kind: int, gamma: float, left, right, normal, precision: int = 0):
+def riemann_sample(kind: int, gamma: float, left, right, normal, precision: int = 0, airs_threshold=None):
     """Half state at x/t = 0 (RiemannStarSolver::sample after the vacuum test) on the GPU."""
     L = load_library()
     left, right, normal = _soa(left, 5), _soa(right, 5), _soa(normal, 3)
     n = left.shape[1]
     out = np.zeros((5, n))
-    _check(L.mvmm_riemann_sample(kind, precision, gamma, n, left.ctypes.data, right.ctypes.data, normal.ctypes.data,
-                                 out.ctypes.data))
+    if airs_threshold is None:
+        _check(L.mvmm_riemann_sample(kind, precision, gamma, n, left.ctypes.data, right.ctypes.data,
+                                     normal.ctypes.data, out.ctypes.data))
+    else:
+        prm = _solver_params(kind, gamma, precision, airs_threshold, None)
+        _check(L.mvmm_riemann_sample_p(ctypes.byref(prm), n, left.ctypes.data, right.ctypes.data, normal.ctypes.data,
+                                       out.ctypes.data))
     return out
 
 
@@ -137,8 +166,7 @@ class GpuSim:
         self.problem = problem
         self.mesh = problem.mesh
         prec = p.precision if precision is None else precision
-        self._p = _Params(p.gamma, 0, 0.0, p.cfl, p.riemann, p.boundary, p.dimensionality, int(p.sync_all), p.t_end,
-                          p.max_newton_iter, prec, 0)
+        self._p = make_params(p, prec)
         self._mv = self.mesh.cview()
         h = ctypes.c_void_p(0)
         self.n_instances = 1

@@ -18,9 +18,13 @@ import numpy as np
 from .layout import Cells, Mesh
 from .mesh import mesh_1d, mesh_voronoi
 
-HLLC, EXACT, PVRS = 0, 1, 2
+HLLC, EXACT, PVRS, AIRS, TSRS, TRRS, LINEAR_ADVECTION = 0, 1, 2, 3, 4, 5, 6
 PERIODIC, REFLECTIVE, OPEN, VACUUM = 0, 1, 2, 3
-SOLVER_NAMES = {"HLLC": HLLC, "Exact": EXACT, "PVRS": PVRS}
+OPTIMAL_ORDER, GODUNOV = 0, 1
+# riemann_solver.kind and engine.runner strings (bin/main.rs:625-673)
+SOLVER_NAMES = {"HLLC": HLLC, "Exact": EXACT, "PVRS": PVRS, "AIRS": AIRS, "TSRS": TSRS, "TRRS": TRRS,
+                "LinearAdvection": LINEAR_ADVECTION}
+RUNNER_NAMES = {"OptimalOrder": OPTIMAL_ORDER, "Godunov": GODUNOV}
 
 
 @dataclass
@@ -36,6 +40,15 @@ class Params:
     t_end: float = 0.2
     precision: int = 0  # 0 = plain FP64, 1 = FP32 faces / FP64 accumulate
     max_newton_iter: int = 1000
+    runner: int = OPTIMAL_ORDER
+    airs_threshold: float | None = None       # riemann_solver.threshold (required by AIRS)
+    advection_velocity: tuple | None = None   # riemann_solver.velocity (required by LinearAdvection)
+
+    def solver_extras(self):
+        """(threshold, velocity) as passed to the C structs; NaN marks a missing value."""
+        thr = math.nan if self.airs_threshold is None else float(self.airs_threshold)
+        v = (math.nan,) * 3 if self.advection_velocity is None else tuple(float(x) for x in self.advection_velocity)
+        return thr, v
 
 
 @dataclass

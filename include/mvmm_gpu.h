@@ -23,8 +23,19 @@ extern "C" {
 #endif
 
 /* ---- enums ---------------------------------------------------------- */
-/* Riemann solver kind: riemann_solver.rs:28-44 ("HLLC", "Exact", "PVRS"). */
-enum { MVMM_RIEMANN_HLLC = 0, MVMM_RIEMANN_EXACT = 1, MVMM_RIEMANN_PVRS = 2 };
+/* Riemann solver kind: riemann_solver.rs:28-44 and bin/main.rs:625-642
+ * ("HLLC", "Exact", "PVRS", "AIRS", "TSRS", "TRRS", "LinearAdvection"). */
+enum {
+    MVMM_RIEMANN_HLLC = 0,
+    MVMM_RIEMANN_EXACT = 1,
+    MVMM_RIEMANN_PVRS = 2,
+    MVMM_RIEMANN_AIRS = 3,            /* airs.rs:18-38, needs airs_threshold */
+    MVMM_RIEMANN_TSRS = 4,            /* tsrs.rs:25-51 */
+    MVMM_RIEMANN_TRRS = 5,            /* trrs.rs:14-32 */
+    MVMM_RIEMANN_LINEAR_ADVECTION = 6 /* linear_advection.rs:17-34, needs advection_velocity */
+};
+/* Runner: bin/main.rs:667-673 ("OptimalOrder", "Godunov"). */
+enum { MVMM_RUNNER_OPTIMAL_ORDER = 0, MVMM_RUNNER_GODUNOV = 1 };
 /* Boundary: space.rs:26-32. */
 enum { MVMM_BOUNDARY_PERIODIC = 0, MVMM_BOUNDARY_REFLECTIVE = 1, MVMM_BOUNDARY_OPEN = 2, MVMM_BOUNDARY_VACUUM = 3 };
 /* Equation of state: gas_law.rs:66-70. */
@@ -75,6 +86,9 @@ typedef struct mvmm_params {
     int max_newton_iter;               /* exact solver cap, 1000 in the reference */
     int precision;                     /* MVMM_PRECISION_* */
     int particle_motion;               /* MVMM_MOTION_FIXED */
+    int runner;                        /* MVMM_RUNNER_*: OptimalOrderRunner or GodunovHydroRunner */
+    double airs_threshold;             /* AIRiemannSolver::new(threshold); NaN = missing */
+    double advection_velocity[3];      /* LinearAdvectionRiemannSover::new(velocity) */
 } mvmm_params;
 
 /* Cell state, SoA, n cells.  Row layout [components][n]; grad row 3*q+k is
@@ -196,9 +210,18 @@ int mvmm_profile_read(mvmm_ctx *ctx, double *ms, int64_t *launches);
 int mvmm_riemann_flux(int kind, int precision, double gamma, int64_t n, const double *left, const double *right,
                       const double *v_face, const double *normal, double *out);
 /* RiemannStarSolver::sample preceded by the vacuum test of the blanket
- * solve_for_flux (riemann_solver.rs:224-287): half state at x/t = 0. */
+ * solve_for_flux (riemann_solver.rs:224-287): half state at x/t = 0.
+ * HLLC and LinearAdvection, which are not star solvers, sample the exact
+ * solution.  These two kind-only forms reject AIRS and LinearAdvection, whose
+ * settings they cannot carry. */
 int mvmm_riemann_sample(int kind, int precision, double gamma, int64_t n, const double *left, const double *right,
                         const double *normal, double *out);
+/* The same two calls configured like a context: riemann, precision, gamma,
+ * airs_threshold and advection_velocity are read from params (ideal gas). */
+int mvmm_riemann_flux_p(const mvmm_params *params, int64_t n, const double *left, const double *right,
+                        const double *v_face, const double *normal, double *out);
+int mvmm_riemann_sample_p(const mvmm_params *params, int64_t n, const double *left, const double *right,
+                          const double *normal, double *out);
 
 /* ---- allocation-free variant ------------------------------------------ */
 /* No counterpart in the reference.  For callers that cannot call cudaMalloc:

@@ -303,6 +303,16 @@ static inline double ex_middle_density(double p, state s, const adiabatic *g) { 
     if (pdps > 1.) return s.q[0] * (pdps + gm1dgp1(g)) / (gm1dgp1(g) * pdps + 1.);
     return s.q[0] * pow(pdps, 1. / g->gamma);
 }
+/* ExactRiemannSolver::star_state_from_pstar (exact.rs:214-238) */
+static star_values ex_star_from_pstar(double p, state l, state r, double vl, double vr, double al, double ar,
+                                      const adiabatic *g) {
+    star_values sv;
+    sv.u = 0.5 * (vl + vr) + 0.5 * (ex_fb(p, r, ar, g) - ex_fb(p, l, al, g));
+    sv.rho_l = ex_middle_density(p, l, g);
+    sv.rho_r = ex_middle_density(p, r, g);
+    sv.p = p;
+    return sv;
+}
 static star_values ex_star_state(state l, state r, double vl, double vr, double al, double ar,
                                  const adiabatic *g, int max_iter, uint32_t *err) { /* :241-291 */
     double p = 0.;
@@ -326,13 +336,7 @@ static star_values ex_star_state(state l, state r, double vl, double vr, double 
     } else {
         p = p_guess;
     }
-    /* star_state_from_pstar (:214-238) */
-    star_values sv;
-    sv.u = 0.5 * (vl + vr) + 0.5 * (ex_fb(p, r, ar, g) - ex_fb(p, l, al, g));
-    sv.rho_l = ex_middle_density(p, l, g);
-    sv.rho_r = ex_middle_density(p, r, g);
-    sv.p = p;
-    return sv;
+    return ex_star_from_pstar(p, l, r, vl, vr, al, ar, g);
 }
 
 /* --- PVRS (riemann_solver/pvrs.rs:26-46) --- */
@@ -348,11 +352,55 @@ static star_values pv_star_state(state l, state r, double vl, double vr, double 
     return sv;
 }
 
+/* --- TSRS (riemann_solver/tsrs.rs:18-51) --- */
+static star_values ts_star_state(state l, state r, double vl, double vr, double al, double ar, const adiabatic *g) {
+    /* PVRiemannSolver::p_star(rho_bar, p_bar, a_bar, v_l, v_r) (pvrs.rs:8-22) */
+    double rho_bar = 0.5 * (l.q[0] + r.q[0]);
+    double p_bar = 0.5 * (l.q[4] + r.q[4]);
+    double a_bar = 0.5 * (al + ar);
+    double p_guess = p_bar + 0.5 * (vl - vr) * rho_bar * a_bar;
+    /* TSRiemannSolver::g (tsrs.rs:18-22) */
+    double g_l = sqrt((tdgp1(g) / l.q[0]) / (p_guess + gm1dgp1(g) * l.q[4]));
+    double g_r = sqrt((tdgp1(g) / r.q[0]) / (p_guess + gm1dgp1(g) * r.q[4]));
+    double pstar = (g_l * l.q[4] + g_r * r.q[4] - (vr - vl)) / (g_l + g_r);
+    return ex_star_from_pstar(pstar, l, r, vl, vr, al, ar, g);
+}
+
+/* --- TRRS (riemann_solver/trrs.rs:14-32) --- */
+static star_values tr_star_state(state l, state r, double vl, double vr, double al, double ar, const adiabatic *g) {
+    double beta = gm1d2g(g);
+    double gm1d2 = 0.5 * (g->gamma - 1.);
+    double num = al + ar - gm1d2 * (vr - vl);
+    double denom = al * pow(l.q[4], -beta) + ar * pow(r.q[4], -beta);
+    double pstar = pow(num / denom, 1. / beta);
+    return ex_star_from_pstar(pstar, l, r, vl, vr, al, ar, g);
+}
+
+/* The flux solver of a run: riemann_solver.rs:28-44 and bin/main.rs:625-642
+ * (kind, AIRS threshold, LinearAdvection velocity). */
+typedef struct { int kind; double airs_threshold; vec3 adv; } rsolver;
+
+static star_values star_state(const rsolver *rs, state l, state r, double vl, double vr, double al, double ar,
+                              const adiabatic *g, int max_iter, uint32_t *err) {
+    switch (rs->kind) {
+    case ORC_EXACT: return ex_star_state(l, r, vl, vr, al, ar, g, max_iter, err);
+    case ORC_TSRS: return ts_star_state(l, r, vl, vr, al, ar, g);
+    case ORC_TRRS: return tr_star_state(l, r, vl, vr, al, ar, g);
+    case ORC_AIRS: { /* AIRiemannSolver (airs.rs:18-38) */
+        star_values s = pv_star_state(l, r, vl, vr, al, ar);
+        double p_max = fmax(l.q[4], r.q[4]);
+        double p_min = fmin(l.q[4], r.q[4]);
+        if (p_max / p_min < rs->airs_threshold) return s;
+        return ex_star_state(l, r, vl, vr, al, ar, g, max_iter, err);
+    }
+    default: return pv_star_state(l, r, vl, vr, al, ar);
+    }
+}
+
 /* RiemannStarSolver::sample (riemann_solver.rs:224-255) */
-static state star_sample(int kind, state l, state r, double vl, double vr, double al, double ar, vec3 n,
+static state star_sample(const rsolver *rs, state l, state r, double vl, double vr, double al, double ar, vec3 n,
                          const adiabatic *g, int max_iter, uint32_t *err) {
-    star_values s = kind == ORC_EXACT ? ex_star_state(l, r, vl, vr, al, ar, g, max_iter, err)
-                                      : pv_star_state(l, r, vl, vr, al, ar);
+    star_values s = star_state(rs, l, r, vl, vr, al, ar, g, max_iter, err);
     if (s.u < 0.) {
         if (s.p > r.q[4]) return sample_right_shock_wave(s.rho_r, s.u, s.p, r, vr, ar, n, g);
         return sample_right_rarefaction_wave(s.rho_r, s.u, s.p, r, vr, ar, n, g);
@@ -457,7 +505,7 @@ static state hllc_solve(state l, state r, vec3 iv, vec3 n, const gaslaw *eos) {
 }
 
 /* Blanket RiemannFluxSolver impl for star solvers (riemann_solver.rs:258-287) */
-static state star_half_state(int kind, state l, state r, vec3 n, const gaslaw *eos, int max_iter,
+static state star_half_state(const rsolver *rs, state l, state r, vec3 n, const gaslaw *eos, int max_iter,
                              uint32_t *err) {
     const adiabatic *g = &eos->g;
     double vl = vdot(st_vel(l), n);
@@ -466,13 +514,21 @@ static state star_half_state(int kind, state l, state r, vec3 n, const gaslaw *e
     double ar = sound_speed(eos, r.q[4], 1. / r.q[0]);
     double vrml = vr - vl;
     if (is_vacuum(l, r, al, ar, vrml, g)) return vacuum_sample(l, r, vl, vr, al, ar, n, g);
-    return star_sample(kind, l, r, vl, vr, al, ar, n, g, max_iter, err);
+    return star_sample(rs, l, r, vl, vr, al, ar, n, g, max_iter, err);
 }
 
-static state riemann_solve_for_flux(int kind, state l, state r, vec3 iv, vec3 n, const gaslaw *eos,
+/* LinearAdvectionRiemannSover::solve_for_flux (riemann_solver/linear_advection.rs:17-34) */
+static state linear_advection_flux(const rsolver *rs, state l, state r, vec3 iv, vec3 n) {
+    double v = vdot(vsub(rs->adv, iv), n);
+    state s = v > 0. ? l : r;
+    return st_scale(v, s);
+}
+
+static state riemann_solve_for_flux(const rsolver *rs, state l, state r, vec3 iv, vec3 n, const gaslaw *eos,
                                     int max_iter, uint32_t *err) {
-    if (kind == ORC_HLLC) return hllc_solve(l, r, iv, n, eos);
-    state w = star_half_state(kind, l, r, n, eos, max_iter, err);
+    if (rs->kind == ORC_HLLC) return hllc_solve(l, r, iv, n, eos);
+    if (rs->kind == ORC_LINEAR_ADVECTION) return linear_advection_flux(rs, l, r, iv, n);
+    state w = star_half_state(rs, l, r, n, eos, max_iter, err);
     return flux_from_half_state(w, iv, n, &eos->g);
 }
 
@@ -561,6 +617,7 @@ typedef struct { state fluxes; vec3 mflux; double v_max, a_over_r; } flux_info; 
 struct orc_ctx {
     orc_params p;
     gaslaw eos;
+    rsolver rs;
     int64_t n, nf;
     particle *parts;
     face *faces;
@@ -678,7 +735,7 @@ static flux_info flux_exchange(const orc_ctx *c, const particle *L, const partic
     vec3 v_face = vsub(vscale(0.5, vadd(L->v, R->v)), vscale(fac, dx));
     vec3 mvf = v3(-v_face.x, -v_face.y, -v_face.z);
 
-    state F = riemann_solve_for_flux(c->p.riemann, prim_boost(prim_left, mvf), prim_boost(prim_right, mvf),
+    state F = riemann_solve_for_flux(&c->rs, prim_boost(prim_left, mvf), prim_boost(prim_right, mvf),
                                      v_face, f->normal, eos, c->p.max_newton_iter, err);
     state fluxes = st_scale(f->area, F);
     flux_info fi;
@@ -722,7 +779,7 @@ static flux_info flux_exchange_boundary(const orc_ctx *c, const particle *P, con
         v_max += fmin(vdot(st_vel(P->prim), dx_centroid), 0.);
         bnd = vac;
     }
-    state F = riemann_solve_for_flux(c->p.riemann, dash, bnd, v3(0., 0., 0.), n, eos, c->p.max_newton_iter, err);
+    state F = riemann_solve_for_flux(&c->rs, dash, bnd, v3(0., 0., 0.), n, eos, c->p.max_newton_iter, err);
     state fluxes = st_scale(f->area, F);
     flux_info fi;
     fi.fluxes = st_scale(P->dt, fluxes);
@@ -1086,6 +1143,9 @@ orc_ctx *orc_create(const orc_params *p, const orc_mesh *m) {
     c->eos.g = adiabatic_from(p->gamma);
     c->eos.eos = p->eos;
     c->eos.iso_u = p->isothermal_internal_energy;
+    c->rs.kind = p->riemann;
+    c->rs.airs_threshold = p->airs_threshold;
+    c->rs.adv = v3(p->advection_velocity[0], p->advection_velocity[1], p->advection_velocity[2]);
     c->n = m->n_cells;
     c->nf = m->n_faces;
     c->parts = (particle *)calloc((size_t)c->n, sizeof(particle));
@@ -1181,7 +1241,9 @@ void orc_get_cells(const orc_ctx *c, orc_cells *out) {
     }
 }
 
-/* OptimalOrderRunner::step (runner/hydrodynamics/optimal_order.rs:15-64) */
+/* OptimalOrderRunner::step (runner/hydrodynamics/optimal_order.rs:15-64), or
+ * GodunovHydroRunner::step (runner/hydrodynamics/godunov.rs:14-58): the same
+ * sequence without gradient_estimate / gradient_limit / gradient_apply. */
 uint64_t orc_step(orc_ctx *c, uint64_t ti_current, uint64_t ti_old, int64_t *n_active_faces) {
     int max_bin = get_max_active_bin(ti_current);
     for (int64_t i = 0; i < c->n; i++) c->active[i] = c->parts[i].timebin <= max_bin; /* bin_is_ending */
@@ -1192,7 +1254,7 @@ uint64_t orc_step(orc_ctx *c, uint64_t ti_current, uint64_t ti_old, int64_t *n_a
     apply_fluxes(c, c->fi, c->active);
     kick2(c, c->active);
     convert_c2p(c, c->active);
-    gradients(c, c->active);
+    if (c->p.runner != ORC_RUNNER_GODUNOV) gradients(c, c->active);
     compute_timesteps(c, c->active, c->dts);
     uint64_t ti_next = ti_current + timesteps_apply(c, c->dts, c->active, ti_current);
     if (c->p.sync_all) timestep_sync(c, ti_current);
@@ -1270,34 +1332,49 @@ static inline state soa_state(const double *a, int64_t n, int64_t i) {
     return s;
 }
 
-void orc_riemann_flux(int kind, double gamma, int64_t n, const double *left, const double *right,
-                      const double *v_face, const double *normal, double *out, uint32_t *err) {
+void orc_riemann_flux_ex(int kind, double gamma, double airs_threshold, const double *adv, int64_t n,
+                         const double *left, const double *right, const double *v_face, const double *normal,
+                         double *out, uint32_t *err) {
     gaslaw eos;
     eos.g = adiabatic_from(gamma);
     eos.eos = ORC_EOS_IDEAL;
     eos.iso_u = 0.;
+    rsolver rs = {kind, airs_threshold, adv ? v3(adv[0], adv[1], adv[2]) : v3(0., 0., 0.)};
     uint32_t e = 0;
     for (int64_t i = 0; i < n; i++) {
-        state f = riemann_solve_for_flux(kind, soa_state(left, n, i), soa_state(right, n, i), m_vec(v_face, n, i),
+        state f = riemann_solve_for_flux(&rs, soa_state(left, n, i), soa_state(right, n, i), m_vec(v_face, n, i),
                                          m_vec(normal, n, i), &eos, 1000, &e);
         for (int q = 0; q < 5; q++) out[q * n + i] = f.q[q];
     }
     if (err) *err = e;
 }
 
-void orc_riemann_sample(int kind, double gamma, int64_t n, const double *left, const double *right,
-                        const double *normal, double *out, uint32_t *err) {
+void orc_riemann_flux(int kind, double gamma, int64_t n, const double *left, const double *right,
+                      const double *v_face, const double *normal, double *out, uint32_t *err) {
+    orc_riemann_flux_ex(kind, gamma, 2., NULL, n, left, right, v_face, normal, out, err);
+}
+
+void orc_riemann_sample_ex(int kind, double gamma, double airs_threshold, int64_t n, const double *left,
+                           const double *right, const double *normal, double *out, uint32_t *err) {
     gaslaw eos;
     eos.g = adiabatic_from(gamma);
     eos.eos = ORC_EOS_IDEAL;
     eos.iso_u = 0.;
+    /* HLLC and LinearAdvection are not star solvers: sample the exact solution */
+    int k = (kind == ORC_HLLC || kind == ORC_LINEAR_ADVECTION) ? ORC_EXACT : kind;
+    rsolver rs = {k, airs_threshold, v3(0., 0., 0.)};
     uint32_t e = 0;
     for (int64_t i = 0; i < n; i++) {
-        state w = star_half_state(kind == ORC_HLLC ? ORC_EXACT : kind, soa_state(left, n, i), soa_state(right, n, i),
-                                  m_vec(normal, n, i), &eos, 1000, &e);
+        state w = star_half_state(&rs, soa_state(left, n, i), soa_state(right, n, i), m_vec(normal, n, i), &eos,
+                                  1000, &e);
         for (int q = 0; q < 5; q++) out[q * n + i] = w.q[q];
     }
     if (err) *err = e;
+}
+
+void orc_riemann_sample(int kind, double gamma, int64_t n, const double *left, const double *right,
+                        const double *normal, double *out, uint32_t *err) {
+    orc_riemann_sample_ex(kind, gamma, 2., n, left, right, normal, out, err);
 }
 
 uint64_t orc_get_integer_timestep(int bin) { return get_integer_timestep(bin); }

@@ -20,8 +20,12 @@
 extern "C" {
 #endif
 
-/* Riemann solver kinds (riemann_solver.rs:28-44). */
-enum { ORC_HLLC = 0, ORC_EXACT = 1, ORC_PVRS = 2 };
+/* Riemann solver kinds (riemann_solver.rs:28-44; LinearAdvection from
+ * bin/main.rs:637-640). */
+enum { ORC_HLLC = 0, ORC_EXACT = 1, ORC_PVRS = 2, ORC_AIRS = 3, ORC_TSRS = 4, ORC_TRRS = 5,
+       ORC_LINEAR_ADVECTION = 6 };
+/* Runner (bin/main.rs:667-673). */
+enum { ORC_RUNNER_OPTIMAL_ORDER = 0, ORC_RUNNER_GODUNOV = 1 };
 /* Boundary (space.rs:26-32). */
 enum { ORC_PERIODIC = 0, ORC_REFLECTIVE = 1, ORC_OPEN = 2, ORC_VACUUM = 3 };
 /* Equation of state (gas_law.rs:66-70). */
@@ -51,6 +55,9 @@ typedef struct orc_params {
     double t_end;
     int max_newton_iter; /* 1000 in the reference (exact.rs:272) */
     int n_threads;       /* OpenMP threads (0 = runtime default) */
+    int runner;          /* ORC_RUNNER_* */
+    double airs_threshold;        /* AIRiemannSolver::new(threshold) */
+    double advection_velocity[3]; /* LinearAdvectionRiemannSover::new(velocity) */
 } orc_params;
 
 /* SoA views; identical field meaning to the GPU library's mvmm_cells /
@@ -99,6 +106,13 @@ void orc_compute_timesteps(orc_ctx *c, const uint8_t *active, double *dt_out);
  * v_face and normal [3][n], output [5][n] conserved flux. */
 void orc_riemann_flux(int kind, double gamma, int64_t n, const double *left, const double *right,
                       const double *v_face, const double *normal, double *out, uint32_t *err);
+/* The same with the AIRS threshold and the LinearAdvection velocity (adv[3],
+ * NULL = zero); the plain forms use threshold 2 and zero velocity. */
+void orc_riemann_flux_ex(int kind, double gamma, double airs_threshold, const double *adv, int64_t n,
+                         const double *left, const double *right, const double *v_face, const double *normal,
+                         double *out, uint32_t *err);
+void orc_riemann_sample_ex(int kind, double gamma, double airs_threshold, int64_t n, const double *left,
+                           const double *right, const double *normal, double *out, uint32_t *err);
 /* Half state sampled at x/t = 0 (RiemannStarSolver::sample, vacuum-aware as
  * in the blanket solve_for_flux); output [5][n] primitive. */
 void orc_riemann_sample(int kind, double gamma, int64_t n, const double *left, const double *right,

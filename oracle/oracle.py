@@ -25,7 +25,8 @@ class _Params(ctypes.Structure):
     _fields_ = [("gamma", ctypes.c_double), ("eos", ctypes.c_int), ("isothermal_internal_energy", ctypes.c_double),
                 ("cfl", ctypes.c_double), ("riemann", ctypes.c_int), ("boundary", ctypes.c_int),
                 ("dimensionality", ctypes.c_int), ("sync_all", ctypes.c_int), ("t_end", ctypes.c_double),
-                ("max_newton_iter", ctypes.c_int), ("n_threads", ctypes.c_int)]
+                ("max_newton_iter", ctypes.c_int), ("n_threads", ctypes.c_int), ("runner", ctypes.c_int),
+                ("airs_threshold", ctypes.c_double), ("advection_velocity", ctypes.c_double * 3)]
 
 
 def build() -> str:
@@ -61,6 +62,8 @@ def lib():
         L.orc_compute_timesteps.argtypes = [vp, vp, vp]
         L.orc_riemann_flux.argtypes = [i32, dbl, i64, vp, vp, vp, vp, vp, ctypes.POINTER(ctypes.c_uint32)]
         L.orc_riemann_sample.argtypes = [i32, dbl, i64, vp, vp, vp, vp, ctypes.POINTER(ctypes.c_uint32)]
+        L.orc_riemann_flux_ex.argtypes = [i32, dbl, dbl, vp, i64, vp, vp, vp, vp, vp, ctypes.POINTER(ctypes.c_uint32)]
+        L.orc_riemann_sample_ex.argtypes = [i32, dbl, dbl, i64, vp, vp, vp, vp, ctypes.POINTER(ctypes.c_uint32)]
         L.orc_get_integer_timestep.restype = u64
         L.orc_get_integer_timestep.argtypes = [i32]
         L.orc_get_time_bin.restype = i32
@@ -87,8 +90,9 @@ class OracleSim:
         self.problem = problem
         self.mesh = problem.mesh
         self.cells = problem.cells.copy()
+        thr, adv = p.solver_extras()
         self._p = _Params(p.gamma, 0, 0.0, p.cfl, p.riemann, p.boundary, p.dimensionality, int(p.sync_all),
-                          p.t_end, p.max_newton_iter, n_threads)
+                          p.t_end, p.max_newton_iter, n_threads, p.runner, thr, (ctypes.c_double * 3)(*adv))
         self._mv = self.mesh.cview()
         self.h = lib().orc_create(ctypes.byref(self._p), ctypes.byref(self._mv))
         self._cv = self.cells.cview()
@@ -171,25 +175,26 @@ def _soa(a, k):
     return a
 
 
-def riemann_flux(kind, gamma, left, right, v_face, normal):
+def riemann_flux(kind, gamma, left, right, v_face, normal, airs_threshold=2.0, velocity=None):
     """RiemannFluxSolver::solve_for_flux over arrays ([5][n], [5][n], [3][n], [3][n])."""
     left, right, v_face, normal = _soa(left, 5), _soa(right, 5), _soa(v_face, 3), _soa(normal, 3)
     n = left.shape[1]
     out = np.zeros((5, n))
     err = ctypes.c_uint32(0)
-    lib().orc_riemann_flux(kind, gamma, n, left.ctypes.data, right.ctypes.data, v_face.ctypes.data,
-                           normal.ctypes.data, out.ctypes.data, ctypes.byref(err))
+    adv = np.zeros(3) if velocity is None else np.ascontiguousarray(velocity, dtype=np.float64)
+    lib().orc_riemann_flux_ex(kind, gamma, airs_threshold, adv.ctypes.data, n, left.ctypes.data, right.ctypes.data,
+                              v_face.ctypes.data, normal.ctypes.data, out.ctypes.data, ctypes.byref(err))
     return out, err.value
 
 
-def riemann_sample(kind, gamma, left, right, normal):
+def riemann_sample(kind, gamma, left, right, normal, airs_threshold=2.0):
     """Half state at x/t=0 (vacuum-aware), [5][n]."""
     left, right, normal = _soa(left, 5), _soa(right, 5), _soa(normal, 3)
     n = left.shape[1]
     out = np.zeros((5, n))
     err = ctypes.c_uint32(0)
-    lib().orc_riemann_sample(kind, gamma, n, left.ctypes.data, right.ctypes.data, normal.ctypes.data,
-                             out.ctypes.data, ctypes.byref(err))
+    lib().orc_riemann_sample_ex(kind, gamma, airs_threshold, n, left.ctypes.data, right.ctypes.data,
+                                normal.ctypes.data, out.ctypes.data, ctypes.byref(err))
     return out, err.value
 
 
