@@ -154,13 +154,18 @@ def test_kh_small_parity(gpu_lib, kind):
 
 @pytest.mark.parametrize("kind", [ics.AIRS, ics.TSRS, ics.TRRS])
 def test_fp32_face_l1(gpu_lib, kind):
+    """20 steps on the same integer timeline as the oracle.  (With PVRS star
+    states, which AIRS picks here since the pressure is near uniform, this
+    32x32 shear layer collapses its timestep after about 25 steps in the FP64
+    oracle too; past that point any perturbation is amplified.)"""
     p = ics.kelvin_helmholtz_2d(32, riemann=kind)
     p.params.airs_threshold = 2.0
     orc = O.OracleSim(p)
     gpu = G.GpuSim(p, precision=1)
-    for _ in range(40):
+    for _ in range(20):
         orc.step()
         gpu.step()
+        assert gpu.ti_current == orc.ti_current
     a, b = gpu.state(), orc.state()
     l1 = np.abs(a.prim[0] - b.prim[0]).sum() / np.abs(b.prim[0]).sum()
     assert l1 <= 1e-5, l1
