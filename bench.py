@@ -212,7 +212,7 @@ def run_ours(args):
     import torch
 
     from hydro_rs_gb300 import gpu as G
-    from hydro_rs_gb300.layout import Cells
+    from hydro_rs_gb300.layout import CELL_ROWS, Cells
 
     ws, rank = _dist()
     dev = int(os.environ.get("LOCAL_RANK", "0"))
@@ -274,12 +274,10 @@ def run_ours(args):
     prof = {prec: _face_kernel_ms(sim, min(args.steps, 20)) for prec, sim in sims.items()}
 
     # end-to-end through the C ABI with pinned host buffers
-    cells = Cells.zeros(nc)
-    pinned = {}
-    for k, v in cells.arrays.items():
-        t = torch.empty(v.shape, dtype=torch.float64 if v.dtype == np.float64 else torch.int8, pin_memory=True)
-        pinned[k] = t
-        cells.arrays[k] = t.numpy()
+    # one pinned block in the device's field order: one copy each way per step
+    pinned = (torch.empty(CELL_ROWS * nc, dtype=torch.float64, pin_memory=True),
+              torch.empty(nc, dtype=torch.int8, pin_memory=True))
+    cells = Cells.packed(nc, pinned[0].numpy(), pinned[1].numpy())
     sim = sims[1]
     sim.state(cells)
     e2e_steps = max(3, min(args.steps, 20))
@@ -357,7 +355,7 @@ def run_ours(args):
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_faces / e2e_s, "unit": UNIT, "h2d_bytes_per_step": bytes_cells,
                 "d2h_bytes_per_step": bytes_cells + 64,
-                "how": "mvmm_upload_cells + mvmm_step + mvmm_download_cells per step, pinned host buffers, wall clock"},
+                "how": "mvmm_upload_cells + mvmm_step + mvmm_download_cells per step, one pinned host block in the device field order, wall clock"},
         "gpu_launches": args.steps * 7 * 1 + args.steps * 6,
         "clocks": clocks,
     }

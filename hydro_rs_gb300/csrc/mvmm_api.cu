@@ -21,6 +21,7 @@ void launch_riemann_fp64(int kind, int sample, double gamma, int64_t n, const do
                          cudaStream_t s);
 void launch_face_flux_fp32(const KP& p, int solver, cudaStream_t s);
 void launch_gradients32(const KP& p, cudaStream_t s);
+void launch_geom32(const KP& p, cudaStream_t s);
 void launch_riemann_fp32(int kind, int sample, double gamma, int64_t n, const double* l, const double* r,
                          const double* vf, const double* nrm, double* out, unsigned int* err, const RSx& x,
                          cudaStream_t s);
@@ -57,6 +58,7 @@ struct mvmm_ctx {
     uint8_t* active = nullptr;
     double* flux = nullptr;
     float* flux32 = nullptr;
+    float* geo = nullptr;
     double* dtmp = nullptr;
     int n_inst = 1;
     int* inst = nullptr;       // per-cell instance (batches only)
@@ -120,6 +122,8 @@ KP make_kp(mvmm_ctx* c, int stage, int flux_rows) {
     p.active = c->active;
     p.flux = c->flux;
     p.flux32 = c->flux32;
+    p.geo = c->geo;
+    p.fp32 = c->prm.precision == MVMM_PRECISION_FP32FACE ? 1 : 0;
     p.flux_rows = flux_rows;
     p.tl = c->tl;
     p.gamma = c->prm.gamma;
@@ -356,6 +360,7 @@ static int create_impl(const mvmm_params* prm, const mvmm_mesh* m, int64_t n_ins
     if (prm->precision == MVMM_PRECISION_FP32FACE) {
         ALLOC(c->cf, (size_t)kCellFields32 * n * 4);
         ALLOC(c->flux32, 7 * nf * 4);
+        ALLOC(c->geo, (size_t)kFaceGeom32 * nf * 4);
     }
     ALLOC(c->timebin, n);
     ALLOC(c->tb_tmp, n);
@@ -455,7 +460,8 @@ int mvmm_ctx_destroy(mvmm_ctx* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->step_exec) cudaGraphExecDestroy(c->step_exec);
     void* ptrs[] = {c->left, c->right, c->csr_off, c->csr_face, c->area, c->normal, c->fcen, c->shift, c->cd,
-                    c->cf, c->timebin, c->tb_tmp, c->active, c->flux, c->flux32, c->dtmp, c->face_act, c->face_list, c->tl,
+                    c->cf, c->timebin, c->tb_tmp, c->active, c->flux, c->flux32, c->geo, c->dtmp, c->face_act,
+                    c->face_list, c->tl,
                     c->inst, c->inst_tb, c->inst_tbi};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -495,12 +501,26 @@ int mvmm_upload_cells(mvmm_ctx* c, const mvmm_cells* h) {
                {h->extrap, F_EXTRAP, 5}, {h->facc, F_FACC, 5}, {h->volume, F_VOL, 1},      {h->loc, F_LOC, 3},
                {h->centroid, F_CEN, 3}, {h->v, F_V, 3},         {h->v_rel, F_VREL, 3},     {h->max_a_over_r, F_MAOR, 1},
                {h->max_signal_velocity, F_MSV, 1}, {h->dt, F_DT, 1}};
-    for (auto& e : map) {
-        if (!e.src) return fail(MVMM_E_INVALID, "null cell field");
-        CUDA_TRY(cudaMemcpyAsync(c->cd + (size_t)e.field * n, e.src, (size_t)e.rows * n * 8, cudaMemcpyHostToDevice, s));
+    // rows that lie back to back on the host in the device's field order go
+    // in one copy (a packed host block takes a single copy)
+    const size_t m = sizeof(map) / sizeof(map[0]);
+    for (size_t a = 0; a < m;) {
+        if (!map[a].src) return fail(MVMM_E_INVALID, "null cell field");
+        size_t b = a + 1;
+        int rows = map[a].rows;
+        while (b < m && map[b].src == map[a].src + (size_t)rows * n && map[b].field == map[a].field + rows)
+            rows += map[b++].rows;
+        CUDA_TRY(cudaMemcpyAsync(c->cd + (size_t)map[a].field * n, map[a].src, (size_t)rows * n * 8,
+                                 cudaMemcpyHostToDevice, s));
+        a = b;
     }
     if (!h->timebin) return fail(MVMM_E_INVALID, "null timebin");
     CUDA_TRY(cudaMemcpyAsync(c->timebin, h->timebin, n, cudaMemcpyHostToDevice, s));
+    // positions and centroids may have changed: refresh the FP32 face geometry
+    if (c->prm.precision == MVMM_PRECISION_FP32FACE) {
+        launch_geom32(make_kp(c, 0, 7), s);
+        CUDA_TRY(cudaGetLastError());
+    }
     return MVMM_OK;
 }
 
@@ -516,9 +536,16 @@ int mvmm_download_cells(mvmm_ctx* c, mvmm_cells* h) {
                {h->extrap, F_EXTRAP, 5}, {h->facc, F_FACC, 5}, {h->volume, F_VOL, 1},      {h->loc, F_LOC, 3},
                {h->centroid, F_CEN, 3}, {h->v, F_V, 3},         {h->v_rel, F_VREL, 3},     {h->max_a_over_r, F_MAOR, 1},
                {h->max_signal_velocity, F_MSV, 1}, {h->dt, F_DT, 1}};
-    for (auto& e : map) {
-        if (!e.dst) return fail(MVMM_E_INVALID, "null cell field");
-        CUDA_TRY(cudaMemcpyAsync(e.dst, c->cd + (size_t)e.field * n, (size_t)e.rows * n * 8, cudaMemcpyDeviceToHost, s));
+    const size_t m = sizeof(map) / sizeof(map[0]);
+    for (size_t a = 0; a < m;) {
+        if (!map[a].dst) return fail(MVMM_E_INVALID, "null cell field");
+        size_t b = a + 1;
+        int rows = map[a].rows;
+        while (b < m && map[b].dst == map[a].dst + (size_t)rows * n && map[b].field == map[a].field + rows)
+            rows += map[b++].rows;
+        CUDA_TRY(cudaMemcpyAsync(map[a].dst, c->cd + (size_t)map[a].field * n, (size_t)rows * n * 8,
+                                 cudaMemcpyDeviceToHost, s));
+        a = b;
     }
     if (!h->timebin) return fail(MVMM_E_INVALID, "null timebin");
     CUDA_TRY(cudaMemcpyAsync(h->timebin, c->timebin, n, cudaMemcpyDeviceToHost, s));

@@ -44,9 +44,27 @@ enum CellField32 : int {
     G_SRC = 25,    // 5
     G_CS = 30,
     G_DGC = 31,    // 3: gradients_centroid - loc
-    G_DCEN = 34,   // 3: centroid - loc
+    G_DCEN = 34,   // 3: (unused)
     G_V = 37,      // 3: mesh velocity
     kCellFields32 = 40
+};
+
+// Static face geometry of the FP32-face form (float block, quantity g of face
+// f at geo[g * nf + f]).  Formed in FP64 from the face data and the cells'
+// positions and centroids whenever cells are uploaded (both are fixed on the
+// device for a fixed mesh), then rounded once.  s is the face shift, n the
+// normal; boundary faces (right < 0) use the reflected position / centroid.
+enum FaceGeom32 : int {
+    GE_RL = 0,    // 3: fc - loc_l
+    GE_RR = 3,    // 3: (fc - loc_r) - s                       (interior)
+    GE_DX = 6,    // 3: (loc_r + s) - loc_l; boundary: reflect(loc_l) - loc_l
+    GE_FCM = 9,   // 3: fc - 0.5 ((loc_l + loc_r) + s)         (interior)
+    GE_N = 12,    // 3: n
+    GE_DS = 15,   // 3: (cen_r + s) - cen_l; boundary: reflect(cen_l) - cen_l
+    GE_DL = 18,   // 3: (fc - cen_l) - s   (limiter extrapolation, left cell)
+    GE_DR = 21,   // 3: (fc - cen_r) + s   (limiter extrapolation, right cell)
+    GE_W = 24,    // area / |ds|^2         (WLS weight)
+    kFaceGeom32 = 25
 };
 
 // Device timeline + counters of one simulation (TimestepInfo, engine.rs:33-41).
@@ -87,7 +105,9 @@ struct KP {
     int8_t* tb_tmp;
     uint8_t* active;
     double* flux;            // face results, rows of nf
-    float* flux32;           // FP32 form face results
+    float* flux32;           // FP32 form face results of a step, rows of nf: 5 fluxes, v_max, a_over_r
+    float* geo;              // FP32 form static face geometry (FaceGeom32)
+    int fp32;                // 1: FP32-face form
     int flux_rows;           // 7 (step) or 10 (stage, with mflux)
     DevTimeline* tl;
     double gamma, iso_u;

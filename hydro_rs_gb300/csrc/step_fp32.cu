@@ -1,11 +1,13 @@
 // FP32-face form of the flux stage (flux.rs:23-195 restated in FP32).
 //
 // Reconstruction, the pair-wise limiter, the Riemann solve and the face flux
-// run in FP32; face geometry differences are formed in FP64 before rounding,
-// the exact solver's pressure iteration (Newton + Brent) runs in FP64, and the
-// final dt * area * F product, the scatter and the conserved update stay FP64
-// (the update kernel is shared with the plain form).  Compiled with FMA
-// contraction enabled.
+// run in FP32 on a static FP32 face geometry (differences formed in FP64 once
+// per upload, then rounded); the exact solver's pressure is polished in FP64
+// (full FP64 iteration where the FP32 search does not converge).  A step
+// writes FP32 face fluxes dt * area * F; the scatter and the conserved update
+// accumulate them in FP64 (the update kernel is shared with the plain form),
+// so every face flux leaves one cell and enters the other exactly.  Compiled
+// with FMA contraction enabled.
 #include "mvmm_cellops.cuh"
 
 namespace mvmm {
@@ -37,17 +39,51 @@ __global__ void __launch_bounds__(kMaxBlock) k_prep32(KP p) {
     cf[G_CS * n + i] = (float)C(p, F_CS, i);
     V3<double> loc = C3(p, F_LOC, i);
     V3<double> dgc = C3(p, F_GC, i) - loc;
-    V3<double> dcen = C3(p, F_CEN, i) - loc;
     V3<double> v = C3(p, F_V, i);
     cf[(G_DGC + 0) * n + i] = (float)dgc.x;
     cf[(G_DGC + 1) * n + i] = (float)dgc.y;
     cf[(G_DGC + 2) * n + i] = (float)dgc.z;
-    cf[(G_DCEN + 0) * n + i] = (float)dcen.x;
-    cf[(G_DCEN + 1) * n + i] = (float)dcen.y;
-    cf[(G_DCEN + 2) * n + i] = (float)dcen.z;
     cf[(G_V + 0) * n + i] = (float)v.x;
     cf[(G_V + 1) * n + i] = (float)v.y;
     cf[(G_V + 2) * n + i] = (float)v.z;
+}
+
+__device__ __forceinline__ V3<float> GE3(const KP& p, int g, int f) {
+    const size_t nf = (size_t)p.nf;
+    return {p.geo[g * nf + f], p.geo[(g + 1) * nf + f], p.geo[(g + 2) * nf + f]};
+}
+
+// Static face geometry (FaceGeom32), one thread per face.
+__global__ void __launch_bounds__(kMaxBlock) k_geom32(KP p) {
+    int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= p.nf) return;
+    int l = p.left[f], r = p.right[f];
+    V3<double> fc = F3(p.fcen, p.nf, f), s = F3(p.shift, p.nf, f), n = F3(p.normal, p.nf, f);
+    V3<double> locl = C3(p, F_LOC, l), cenl = C3(p, F_CEN, l);
+    V3<double> z = v3(0., 0., 0.);
+    V3<double> rr = z, fcm = z, dr = z, dx, ds;
+    if (r >= 0) {
+        V3<double> locr = C3(p, F_LOC, r), cenr = C3(p, F_CEN, r);
+        rr = (fc - locr) - s;
+        dx = (locr + s) - locl;
+        fcm = fc - 0.5 * ((locl + locr) + s);
+        ds = (cenr + s) - cenl;
+        dr = (fc - cenr) + s;
+    } else {
+        // Particle::reflect (part.rs:374-383) of the cell's position and centroid
+        dx = (2. * dot(fc - locl, n)) * n;
+        ds = (2. * dot(fc - cenl, n)) * n;
+    }
+    V3<double> vals[8] = {fc - locl, rr, dx, fcm, n, ds, (fc - cenl) - s, dr};
+    float* g = p.geo;
+    const size_t nf = (size_t)p.nf;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        g[(3 * k + 0) * nf + f] = (float)vals[k].x;
+        g[(3 * k + 1) * nf + f] = (float)vals[k].y;
+        g[(3 * k + 2) * nf + f] = (float)vals[k].z;
+    }
+    g[GE_W * nf + f] = (float)(p.area[f] / len2(ds));
 }
 
 __device__ __forceinline__ St<float> reconstruct32(const KP& p, int i, const St<float>& prim, V3<float> dx, float td) {
@@ -65,71 +101,52 @@ __device__ __forceinline__ St<float> reconstruct32(const KP& p, int i, const St<
 }
 
 struct Out32 {
-    St<double> fl;
-    V3<double> mflux;
-    double v_max, a_over_r;
+    St<float> F;     // area-free face flux
+    V3<float> dx;    // generator separation (mflux direction)
+    float v_max, a_over_r;
 };
 
 template <int SOLVER>
-__device__ __forceinline__ Out32 face_interior32(const KP& p, int f, int l, int r, double dt, const Gas<float>& g,
+__device__ __forceinline__ Out32 face_interior32(const KP& p, int f, int l, int r, float dt, const Gas<float>& g,
                                                  const Gas<double>& g64, unsigned int* err) {
-    V3<double> fc = F3(p.fcen, p.nf, f);
-    V3<double> sh = F3(p.shift, p.nf, f);
-    V3<double> locl = C3(p, F_LOC, l), locr = C3(p, F_LOC, r);
-    // geometry differences in FP64, then rounded
-    V3<float> rl = cvt<float>(fc - locl);
-    V3<float> rr = cvt<float>((fc - locr) - sh);
-    V3<double> dxd = (locr + sh) - locl;
-    V3<float> dx = cvt<float>(dxd);
-    V3<float> dx_left = rl - G3(p, G_DGC, l);
-    V3<float> dx_right = rr - G3(p, G_DGC, r);
+    V3<float> dx = GE3(p, GE_DX, f);
+    V3<float> dx_left = GE3(p, GE_RL, f) - G3(p, G_DGC, l);
+    V3<float> dx_right = GE3(p, GE_RR, f) - G3(p, G_DGC, r);
     float dx_gradients = len(dx_left - dx_right);
-    V3<float> dx_centroid = (dx + G3(p, G_DCEN, r)) - G3(p, G_DCEN, l);
+    V3<float> dx_centroid = GE3(p, GE_DS, f);
     St<float> pl = G5(p, G_PRIM, l), pr = G5(p, G_PRIM, r);
     float v_max = G(p, G_CS, l) + G(p, G_CS, r);
     v_max -= fminf(dot(vel(pr) - vel(pl), dx_centroid), 0.f);
-    float td = 0.5f * (float)dt;
+    float td = 0.5f * dt;
     St<float> ldash = reconstruct32(p, l, pl, dx_left, td);
     St<float> rdash = reconstruct32(p, r, pr, dx_right, td);
     St<float> prim_left = pairwise_limiter(pl, pr, ldash, len(dx_left) / dx_gradients);
     St<float> prim_right = pairwise_limiter(pr, pl, rdash, len(dx_right) / dx_gradients);
     V3<float> vl = G3(p, G_V, l), vr = G3(p, G_V, r);
-    V3<float> fcm = cvt<float>(fc - 0.5 * ((locl + locr) + sh));
-    float fac = dot(vr - vl, fcm) / len2(dx);
+    float fac = dot(vr - vl, GE3(p, GE_FCM, f)) / len2(dx);
     V3<float> v_face = 0.5f * (vl + vr) - fac * dx;
-    V3<float> nrm = cvt<float>(F3(p.normal, p.nf, f));
+    V3<float> nrm = GE3(p, GE_N, f);
     V3<float> mvf = neg(v_face);
-    St<float> F = solve_for_flux<float, SOLVER>(boost(prim_left, mvf), boost(prim_right, mvf), v_face, nrm, g, g64,
-                                                p.max_iter, err, &p.rsx);
-    double area = p.area[f];
     Out32 o;
-#pragma unroll
-    for (int q = 0; q < 5; q++) o.fl.q[q] = dt * (area * (double)F.q[q]);
-    double m = area * (double)F.q[0];
-    o.mflux = m * dxd;
+    o.F = solve_for_flux<float, SOLVER>(boost(prim_left, mvf), boost(prim_right, mvf), v_face, nrm, g, g64,
+                                        p.max_iter, err, &p.rsx);
+    o.dx = dx;
     o.v_max = v_max;
-    o.a_over_r = (double)((float)area / len(dx));  // feeds max_a_over_r only (mesh steering)
+    o.a_over_r = (float)p.area[f] / len(dx);  // feeds max_a_over_r only (mesh steering)
     return o;
 }
 
 template <int SOLVER>
-__device__ __forceinline__ Out32 face_boundary32(const KP& p, int f, int i, const Gas<float>& g, const Gas<double>& g64,
-                                                 unsigned int* err) {
-    V3<double> fc = F3(p.fcen, p.nf, f);
-    V3<double> nd = F3(p.normal, p.nf, f);
-    V3<double> loc = C3(p, F_LOC, i), cen = C3(p, F_CEN, i), gc = C3(p, F_GC, i);
-    V3<double> rgc = gc + (2. * dot(fc - gc, nd)) * nd;
-    V3<double> rcen = cen + (2. * dot(fc - cen, nd)) * nd;
-    V3<double> rloc = loc + (2. * dot(fc - loc, nd)) * nd;
-    V3<float> dx_face = cvt<float>(fc - gc);
-    float dx_gradients = (float)len(rgc - gc);
-    V3<float> dx_centroid = cvt<float>(rcen - cen);
-    V3<double> dxd = rloc - loc;
-    V3<float> n = cvt<float>(nd);
+__device__ __forceinline__ Out32 face_boundary32(const KP& p, int f, int i, float dt, const Gas<float>& g,
+                                                 const Gas<double>& g64, unsigned int* err) {
+    V3<float> n = GE3(p, GE_N, f);
+    V3<float> dx_face = GE3(p, GE_RL, f) - G3(p, G_DGC, i);       // fc - gc
+    float dx_gradients = len((2.f * dot(dx_face, n)) * n);        // |reflect(gc) - gc|
+    V3<float> dx_centroid = GE3(p, GE_DS, f);
+    V3<float> dx = GE3(p, GE_DX, f);
     St<float> prim = G5(p, G_PRIM, i);
     float v_max = G(p, G_CS, i);
-    double dt = C(p, F_DT, i);
-    float td = 0.5f * (float)dt;
+    float td = 0.5f * dt;
     St<float> dash = reconstruct32(p, i, prim, dx_face, td);
     float dx_fac = len(dx_face) / dx_gradients;
     St<float> bnd;
@@ -147,14 +164,11 @@ __device__ __forceinline__ Out32 face_boundary32(const KP& p, int f, int i, cons
         v_max += fminf(dot(vel(prim), dx_centroid), 0.f);
         bnd = vac;
     }
-    St<float> F = solve_for_flux<float, SOLVER>(dash, bnd, v3(0.f, 0.f, 0.f), n, g, g64, p.max_iter, err, &p.rsx);
-    double area = p.area[f];
     Out32 o;
-#pragma unroll
-    for (int q = 0; q < 5; q++) o.fl.q[q] = dt * (area * (double)F.q[q]);
-    o.mflux = (area * (double)F.q[0]) * dxd;
+    o.F = solve_for_flux<float, SOLVER>(dash, bnd, v3(0.f, 0.f, 0.f), n, g, g64, p.max_iter, err, &p.rsx);
+    o.dx = dx;
     o.v_max = v_max;
-    o.a_over_r = area / len(dxd);
+    o.a_over_r = (float)p.area[f] / len(dx);
     return o;
 }
 
@@ -164,6 +178,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_face_flux32(KP p) {
     const Gas<float> g = make_gas<float>(p.gamma, p.eos, p.iso_u);
     const Gas<double> g64 = make_gas<double>(p.gamma, p.eos, p.iso_u);
     const int n_items = p.use_list ? (int)p.tl[0].n_list : p.nf;
+    const size_t nf = (size_t)p.nf;
     for (int base = blockIdx.x * blockDim.x; base < n_items; base += gridDim.x * blockDim.x) {
         int idx = base + threadIdx.x;
         int f = idx < n_items ? (p.use_list ? p.face_list[idx] : idx) : -1;
@@ -175,36 +190,40 @@ __global__ void __launch_bounds__(kMaxBlock) k_face_flux32(KP p) {
             int l = p.left[f], r = p.right[f];
             bool la = p.active[l] != 0;
             Out32 o;
+            double dt = 0.;
             if (r >= 0) {
                 bool ra = p.active[r] != 0;
                 double dtl = C(p, F_DT, l), dtr = C(p, F_DT, r);
                 if (!((!la && !ra) || (dtr < dtl && !ra) || (dtl < dtr && !la))) {
-                    o = face_interior32<SOLVER>(p, f, l, r, fmin(dtl, dtr), g, g64, &err);
+                    dt = fmin(dtl, dtr);
+                    o = face_interior32<SOLVER>(p, f, l, r, (float)dt, g, g64, &err);
                     counted = true;
                 }
             } else if (la) {
-                o = face_boundary32<SOLVER>(p, f, l, g, g64, &err);
+                dt = C(p, F_DT, l);
+                o = face_boundary32<SOLVER>(p, f, l, (float)dt, g, g64, &err);
                 counted = true;
             }
-            if (!counted) {
-                o.fl = st_zero<double>();
-                o.mflux = v3(0., 0., 0.);
-                o.v_max = 0.;
-                o.a_over_r = 0.;
-            }
-            double* out = p.flux;
-            size_t nf = (size_t)p.nf;
+            double area = p.area[f];
+            if (p.flux_rows == 7) {
+                // step: FP32 rows dt * area * F, v_max, a_over_r (accumulated in FP64 by the update)
+                float* out = p.flux32;
+                float da = counted ? (float)(dt * area) : 0.f;
 #pragma unroll
-            for (int q = 0; q < 5; q++) out[q * nf + f] = o.fl.q[q];
-            if (p.flux_rows == 10) {
-                out[5 * nf + f] = o.mflux.x;
-                out[6 * nf + f] = o.mflux.y;
-                out[7 * nf + f] = o.mflux.z;
-                out[8 * nf + f] = o.v_max;
-                out[9 * nf + f] = o.a_over_r;
+                for (int q = 0; q < 5; q++) out[q * nf + f] = counted ? da * o.F.q[q] : 0.f;
+                out[5 * nf + f] = counted ? o.v_max : 0.f;
+                out[6 * nf + f] = counted ? o.a_over_r : 0.f;
             } else {
-                out[5 * nf + f] = o.v_max;
-                out[6 * nf + f] = o.a_over_r;
+                // per-stage call: the FluxInfo rows in FP64, mflux included
+                double* out = p.flux;
+#pragma unroll
+                for (int q = 0; q < 5; q++) out[q * nf + f] = counted ? dt * (area * (double)o.F.q[q]) : 0.;
+                double m = counted ? area * (double)o.F.q[0] : 0.;
+                out[5 * nf + f] = m * (double)o.dx.x;
+                out[6 * nf + f] = m * (double)o.dx.y;
+                out[7 * nf + f] = m * (double)o.dx.z;
+                out[8 * nf + f] = counted ? (double)o.v_max : 0.;
+                out[9 * nf + f] = counted ? (double)o.a_over_r : 0.;
             }
             if (err & ~kInfoFallback) set_err(p, k, err & ~kInfoFallback);
         }
@@ -213,10 +232,35 @@ __global__ void __launch_bounds__(kMaxBlock) k_face_flux32(KP p) {
     }
 }
 
+// The other side of face f seen from cell i in the FP32-face form (the FP32
+// counterpart of other_side): its primitive state, the centroid separation ds
+// and the limiter's extrapolation vector, from the static face geometry.
+__device__ __forceinline__ void other_side32(const KP& p, int i, int f, const St<float>& prim, St<float>& op,
+                                             V3<float>& ds, V3<float>& d) {
+    int l = p.left[f], r = p.right[f];
+    if (i == l) {
+        ds = GE3(p, GE_DS, f);
+        d = GE3(p, GE_DL, f);
+        if (r < 0) {  // Space::get_boundary_part (space.rs:213-229)
+            V3<float> n = GE3(p, GE_N, f);
+            if (p.boundary == 1) op = reflect(prim, n);
+            else if (p.boundary == 2) op = prim;
+            else op = st_zero<float>();
+        } else {
+            op = G5(p, G_PRIM, r);
+        }
+    } else {
+        ds = neg(GE3(p, GE_DS, f));
+        d = GE3(p, GE_DR, f);
+        op = G5(p, G_PRIM, l);
+    }
+}
+
 // gradient_estimate + gradient_limit + gradient_apply (runner/hydrodynamics.rs:67-143)
-// for the FP32-face form: differences of primitives and positions are formed
-// in FP64 and rounded, the WLS sums, the 3x3 inverse and the cell-wise limiter
-// run in FP32 (these slopes only feed the FP32 reconstruction), and the
+// for the FP32-face form: primitive differences from the FP32 copies (the
+// update refreshes them for active cells), separations and WLS weights from
+// the static face geometry, the WLS sums, the 3x3 inverse and the cell-wise
+// limiter in FP32 (these slopes only feed the FP32 reconstruction); the
 // timestep (Particle::timestep, timesteps_apply) stays FP64 as in the plain form.
 __global__ void __launch_bounds__(kMaxBlock) k_gradients32(KP p) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -229,8 +273,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_gradients32(KP p) {
         int tb = p.timebin[i];
         if (p.active[i]) {
           if (!p.godunov) {  // GodunovHydroRunner::step has no gradient stage (godunov.rs:14-58)
-            V3<double> cen = C3(p, F_CEN, i);
-            St<double> prim = C5(p, F_PRIM, i);
+            St<float> prim = G5(p, G_PRIM, i);
             float a00 = 0.f, a01 = 0.f, a02 = 0.f, a11 = 0.f, a12 = 0.f, a22 = 0.f;
             if (p.dim == 1) { a11 = 1.f; a22 = 1.f; }
             else if (p.dim == 2) { a22 = 1.f; }
@@ -240,13 +283,12 @@ __global__ void __launch_bounds__(kMaxBlock) k_gradients32(KP p) {
             int k0 = p.csr_off[i], k1 = p.csr_off[i + 1];
             for (int k = k0; k < k1; k++) {
                 int f = p.csr_face[k];
-                St<double> op;
-                V3<double> oc, sh;
-                other_side(p, i, f, prim, cen, op, oc, sh);
-                V3<float> ds = cvt<float>((oc + sh) - cen);
-                float w = (float)p.area[f] / len2(ds);
+                St<float> op;
+                V3<float> ds, d;
+                other_side32(p, i, f, prim, op, ds, d);
+                float w = p.geo[GE_W * (size_t)p.nf + f];
 #pragma unroll
-                for (int q = 0; q < 5; q++) gr[q] = gr[q] + (w * (float)(op.q[q] - prim.q[q])) * ds;
+                for (int q = 0; q < 5; q++) gr[q] = gr[q] + (w * (op.q[q] - prim.q[q])) * ds;
                 a00 += w * ds.x * ds.x;
                 a01 += w * ds.x * ds.y;
                 a02 += w * ds.x * ds.z;
@@ -280,14 +322,13 @@ __global__ void __launch_bounds__(kMaxBlock) k_gradients32(KP p) {
             }
             for (int k = k0; k < k1; k++) {
                 int f = p.csr_face[k];
-                St<double> op;
-                V3<double> oc, sh;
-                other_side(p, i, f, prim, cen, op, oc, sh);
-                V3<float> d = cvt<float>((F3(p.fcen, p.nf, f) - cen) - sh);
+                St<float> op;
+                V3<float> ds, d;
+                other_side32(p, i, f, prim, op, ds, d);
 #pragma unroll
                 for (int q = 0; q < 5; q++) {
                     float ex = dot(gr[q], d);
-                    float dq = (float)(op.q[q] - prim.q[q]);
+                    float dq = op.q[q] - prim.q[q];
                     dmn[q] = fminf(dmn[q], dq);
                     dmx[q] = fmaxf(dmx[q], dq);
                     emn[q] = fminf(emn[q], ex);
@@ -300,6 +341,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_gradients32(KP p) {
                 gr[q] = alpha * gr[q];
                 W3(p, F_GRAD + 3 * q, i, cvt<double>(gr[q]));
             }
+            V3<double> cen = C3(p, F_CEN, i);
             W3(p, F_GC, i, cen);
           }
             double dt_new = particle_timestep(p, i);
@@ -351,6 +393,10 @@ inline int grid(int n, int b = kBlock) { return (n + b - 1) / b; }
 
 void launch_prep32(const KP& p, cudaStream_t s) {
     if (p.n > 0) k_prep32<<<grid(p.n, p.blk_cell), p.blk_cell, 0, s>>>(p);
+}
+
+void launch_geom32(const KP& p, cudaStream_t s) {
+    if (p.nf > 0) k_geom32<<<grid(p.nf, kBlock), kBlock, 0, s>>>(p);
 }
 
 void launch_gradients32(const KP& p, cudaStream_t s) {

@@ -328,6 +328,9 @@ __global__ void __launch_bounds__(kMaxBlock) k_update(KP p, int do_c2p) {
     const size_t nf = (size_t)p.nf;
     const int rv = p.flux_rows == 10 ? 8 : 5;
     const double* fl = p.flux;
+    // the FP32-face form's step writes FP32 rows; they are accumulated in FP64
+    const bool rows32 = p.fp32 && p.flux_rows == 7;
+    const float* fl32 = p.flux32;
     int k0 = p.csr_off[i], k1 = p.csr_off[i + 1];
     for (int k = k0; k < k1; k++) {
         int f = p.csr_face[k];
@@ -335,12 +338,14 @@ __global__ void __launch_bounds__(kMaxBlock) k_update(KP p, int do_c2p) {
         if (p.use_list && !p.face_act[f]) continue;
         St<double> x;
 #pragma unroll
-        for (int q = 0; q < 5; q++) x.q[q] = fl[q * nf + f];
+        for (int q = 0; q < 5; q++) x.q[q] = rows32 ? (double)fl32[q * nf + f] : fl[q * nf + f];
         if (p.left[f] == i) facc = facc - x;  // update_fluxes_left (part.rs:160-167)
         else facc = facc + x;                 // update_fluxes_right (part.rs:169-176)
         if (act) {
-            msv = m_max(fl[rv * nf + f], msv);
-            maor = m_max(maor, fl[(rv + 1) * nf + f]);
+            double vm = rows32 ? (double)fl32[5 * nf + f] : fl[rv * nf + f];
+            double ar = rows32 ? (double)fl32[6 * nf + f] : fl[(rv + 1) * nf + f];
+            msv = m_max(vm, msv);
+            maor = m_max(maor, ar);
         }
     }
     unsigned int err = 0;
@@ -360,7 +365,13 @@ __global__ void __launch_bounds__(kMaxBlock) k_update(KP p, int do_c2p) {
         W5(p, F_CONS, i, cons);
         W(p, F_MSV, i, msv);
         W(p, F_MAOR, i, maor);
-        if (do_c2p) c2p(p, i, cons, &err);
+        if (do_c2p) {
+            c2p(p, i, cons, &err);
+            if (p.fp32) {  // FP32 copies read by the FP32-face form's gradient stage
+#pragma unroll
+                for (int q = 0; q < 5; q++) p.cf[(size_t)(G_PRIM + q) * p.n + i] = (float)C(p, F_PRIM + q, i);
+            }
+        }
     }
     W5(p, F_FACC, i, facc);
     if (err) set_err(p, k, err);

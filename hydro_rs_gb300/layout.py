@@ -45,6 +45,9 @@ CELL_FIELDS = (
 )
 
 
+CELL_ROWS = sum(k for _, k in CELL_FIELDS)
+
+
 class CCells(ctypes.Structure):
     """C view of ``mvmm_cells`` / the oracle's ``orc_cells`` (same layout)."""
 
@@ -83,6 +86,21 @@ class Cells:
         for name, k in CELL_FIELDS:
             c.arrays[name] = np.zeros((k, n) if k > 1 else (n,), dtype=F64)
         c.arrays["timebin"] = np.zeros(n, dtype=np.int8)
+        return c
+
+    @classmethod
+    def packed(cls, n: int, block: np.ndarray, timebin: np.ndarray) -> "Cells":
+        """Fields as views of one float64 block of ``CELL_ROWS * n`` values in
+        ``CELL_FIELDS`` order, the device's own field order, so that
+        ``mvmm_upload_cells`` / ``mvmm_download_cells`` move it in one copy."""
+        assert block.dtype == F64 and block.size == CELL_ROWS * n and timebin.size == n
+        c = cls(n=n)
+        off = 0
+        for name, k in CELL_FIELDS:
+            v = block[off * n:(off + k) * n]
+            c.arrays[name] = v.reshape(k, n) if k > 1 else v
+            off += k
+        c.arrays["timebin"] = timebin
         return c
 
     def __getattr__(self, name):
