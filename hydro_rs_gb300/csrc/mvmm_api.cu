@@ -13,6 +13,7 @@
 
 #include "../../include/mvmm_gpu.h"
 #include "mvmm_internal.h"
+#include "mvmm_device.cuh"
 
 namespace mvmm {
 void launch_face_flux_fp64(const KP& p, int solver, cudaStream_t s);
@@ -149,6 +150,15 @@ KP make_kp(mvmm_ctx* c, int stage, int flux_rows) {
     p.blk_face = c->blk_face;
     p.blk_cell = c->blk_cell;
     p.rsx = solver_settings(c->prm);
+    const Gas<double> g = make_gas<double>(c->prm.gamma, c->prm.eos, c->prm.isothermal_internal_energy);
+    p.gk.gamma = g.gamma;
+    p.gk.gamma_inv = g.gamma_inv;
+    p.gk.odgm1 = g.odgm1_;
+    p.gk.odgp1 = g.odgp1_;
+    p.gk.iso_u = g.iso_u;
+    p.gk.inv_m = g.inv_m;
+    p.gk.eos = g.eos;
+    p.gk.rm = g.rm;
     // a stage call to mvmm_gradients always estimates gradients
     p.godunov = (!stage && c->prm.runner == MVMM_RUNNER_GODUNOV) ? 1 : 0;
     return p;

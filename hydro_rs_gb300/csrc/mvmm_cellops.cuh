@@ -33,7 +33,22 @@ __device__ __forceinline__ void W5(const KP& p, int f, int i, const St<double>& 
     for (int q = 0; q < 5; q++) W(p, f + q, i, s.q[q]);
 }
 __device__ __forceinline__ V3<double> F3(const double* a, int nf, int f) { return {a[f], a[nf + f], a[2 * nf + f]}; }
-__device__ __forceinline__ Gas<double> gas(const KP& p) { return make_gas<double>(p.gamma, p.eos, p.iso_u); }
+// The gas law in type T from the host-evaluated constants; equal to
+// make_gas<T>(p.gamma, p.eos, p.iso_u) member by member.
+template <typename T>
+__device__ __forceinline__ Gas<T> gas_t(const KP& p) {
+    Gas<T> g;
+    g.gamma = T(p.gk.gamma);
+    g.gamma_inv = T(p.gk.gamma_inv);
+    g.odgm1_ = T(p.gk.odgm1);
+    g.odgp1_ = T(p.gk.odgp1);
+    g.iso_u = T(p.gk.iso_u);
+    g.eos = p.gk.eos;
+    g.rm = p.gk.rm;
+    g.inv_m = p.gk.inv_m;
+    return g;
+}
+__device__ __forceinline__ Gas<double> gas(const KP& p) { return gas_t<double>(p); }
 __device__ __forceinline__ int inst_of(const KP& p, int cell) { return p.inst ? p.inst[cell] : 0; }
 __device__ __forceinline__ double tbase(const KP& p, int k) { return p.inst_tb ? p.inst_tb[k] : p.time_base; }
 __device__ __forceinline__ double tbase_inv(const KP& p, int k) { return p.inst_tbi ? p.inst_tbi[k] : p.time_base_inv; }

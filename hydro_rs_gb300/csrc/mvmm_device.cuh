@@ -696,6 +696,20 @@ __device__ __forceinline__ void f32_eval(float p, const F32Side& s, float z, flo
         fpb = s.k_fp / t;
     }
 }
+// One side's term of f at an FP64 pressure P (exact.rs:12-20) for the FP32
+// face inputs of s: the shock branch from the FP32 constants, the rarefaction
+// branch as c (t^(1/m) - 1) with t = P / p_s to ~1e-14 (FP32 reciprocal seed,
+// one Newton step) and t^(1/m) from an FP32 seed refined by one Newton step.
+__device__ __forceinline__ double side_f64(double P, const F32Side& s, int m, float inv_m) {
+    double ps = (double)s.p;
+    if (P > ps) return (P - ps) * (double)s.sqA * rsqrt64(P + (double)s.B);
+    double r0 = (double)(1.f / s.p);
+    double t = P * (r0 * (2.0 - ps * r0));
+    float yf = __powf((float)t, inv_m);
+    double y = (double)yf;
+    y = y - (ipow(y, m) - t) * (double)(inv_m / ipow(yf, m - 1));
+    return (double)s.c_rar * (y - 1.0);
+}
 static __device__ __noinline__ Star<float> ex_star_split(float rl, float pl, float al, float rr, float pr, float ar,
                                                          float vl, float vr, Gas<float> g, Gas<double> g64,
                                                          int max_iter, unsigned int* err) {
@@ -737,25 +751,19 @@ static __device__ __noinline__ Star<float> ex_star_split(float rl, float pl, flo
         if (done) break;
     }
     p = ipow(x, m);
-    // two FP64 Newton steps on the FP64 f
-    ExFast L64 = ex_fast_side(ExSide{(double)rl, (double)pl, (double)al}, g64);
-    ExFast R64 = ex_fast_side(ExSide{(double)rr, (double)pr, (double)ar}, g64);
-    double P = (double)p, dP = 0.;
-    double dvd = (double)vr - (double)vl;
-#pragma unroll
-    for (int k = 0; k < 2; k++) {
-        PRoot q{0., 0.};
-        if (P <= L64.p || P <= R64.p) q = proot(P, g64);
-        double fl = P > L64.p ? (P - L64.p) * L64.sqA * rsqrt64(P + L64.B) : L64.c_rar * (q.r * L64.ps_rm - 1.);
-        double fr = P > R64.p ? (P - R64.p) * R64.sqA * rsqrt64(P + R64.B) : R64.c_rar * (q.r * R64.ps_rm - 1.);
-        float fbl, fpl, fbr, fpr;
-        f32_eval((float)P, L, z, fbl, fpl);
-        f32_eval((float)P, R, z, fbr, fpr);
-        dP = (fl + fr + dvd) * (double)(1.f / (fpl + fpr));
-        P = P - dP;
-    }
+    // one FP64 Newton step: the terms of f from the FP32 face inputs, with the
+    // (P/p_s)^(1/m) - 1 cancellation and the final sum in FP64; f' in FP32
+    double P = (double)p;
+    float fbl, fpl, fbr, fpr;
+    f32_eval(p, L, z, fbl, fpl);
+    f32_eval(p, R, z, fbr, fpr);
+    double fP = ((double)vr - (double)vl) + side_f64(P, L, m, inv_m) + side_f64(P, R, m, inv_m);
+    double dP = fP * (double)(1.f / (fpl + fpr));
+    P = P - dP;
     Star<float> s;
-    if (!(P > 0.) || !isfinite(P) || !(fabs(dP) <= 1e-8 * P)) {
+    // a search that ended more than 1e-4 from the root (after the step the
+    // error is of order dP^2) is redone by the full FP64 iteration
+    if (!(P > 0.) || !isfinite(P) || !(fabs(dP) <= 1e-4 * P)) {
         *err |= 1u << 16;  // counted by the face kernel as a fallback face
         Star<double> sd = ex_star_fast(ExSide{(double)rl, (double)pl, (double)al},
                                        ExSide{(double)rr, (double)pr, (double)ar}, (double)vl, (double)vr, g64,
@@ -768,7 +776,6 @@ static __device__ __noinline__ Star<float> ex_star_split(float rl, float pl, flo
     }
     // star_state_from_pstar (exact.rs:214-238) in FP32 at the polished pressure
     float ps = (float)P;
-    float fbl, fpl, fbr, fpr;
     f32_eval(ps, L, z, fbl, fpl);
     f32_eval(ps, R, z, fbr, fpr);
     s.u = 0.5f * (vl + vr) + 0.5f * (fbr - fbl);
@@ -860,6 +867,10 @@ enum {
     SOLVER_EXTRA = 7
 };
 
+// The FP32 gas law of a face stage (already FP32 in the FP32-face form).
+__device__ __forceinline__ const Gas<float>& gas32(const Gas<float>& g) { return g; }
+__device__ __forceinline__ Gas<float> gas32(const Gas<double>& g) { return make_gas<float>(g.gamma, g.eos, g.iso_u); }
+
 // Exact star state in the face type: FP32 search + FP64 polish for the
 // FP32-face form with a rational gamma, else the FP64 reference iteration.
 template <typename T>
@@ -869,8 +880,7 @@ __device__ __forceinline__ Star<T> exact_star(const St<T>& l, const St<T>& r, T 
     Star<T> s;
     if (sizeof(T) == 4 && g64.rm) {
         Star<float> sf = ex_star_split(float(l.q[0]), float(l.q[4]), float(al), float(r.q[0]), float(r.q[4]),
-                                       float(ar), float(vl), float(vr), make_gas<float>(double(g.gamma), g.eos,
-                                       double(g.iso_u)), g64, max_iter, err);
+                                       float(ar), float(vl), float(vr), gas32(g), g64, max_iter, err);
         s.rho_l = T(sf.rho_l);
         s.rho_r = T(sf.rho_r);
         s.u = T(sf.u);

@@ -14,6 +14,13 @@ struct RSx {
     double adv[3];
 };
 
+// Gas-law constants (AdiabaticIndex::from, gas_law.rs:9-18) evaluated once on
+// the host, so that kernels do not repeat the divisions per thread.
+struct GasK {
+    double gamma, gamma_inv, odgm1, odgp1, iso_u, inv_m;
+    int eos, rm;
+};
+
 // Cell state on the device: one float64 block of kCellFields * n doubles,
 // field f of cell i at cd[f * n + i] (SoA; rows as in mvmm_cells).
 enum CellField : int {
@@ -127,6 +134,7 @@ struct KP {
     const double* inst_tb;   // per-instance time_base (nullptr: time_base)
     const double* inst_tbi;  // per-instance 1 / time_base (nullptr: time_base_inv)
     int blk_face, blk_cell;  // thread-block sizes (chosen by mvmm_autotune)
+    GasK gk;                 // gas-law constants
     RSx rsx;                 // Riemann solver kind and its settings
     int godunov;             // 1: GodunovHydroRunner (no gradients), 0: OptimalOrderRunner
     int use_list;            // 1: face kernel walks the compacted active-face list

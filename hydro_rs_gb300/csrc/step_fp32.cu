@@ -175,8 +175,8 @@ __device__ __forceinline__ Out32 face_boundary32(const KP& p, int f, int i, floa
 template <int SOLVER>
 __global__ void __launch_bounds__(kMaxBlock) k_face_flux32(KP p) {
     if (p.use_list && p.tl[0].done) return;
-    const Gas<float> g = make_gas<float>(p.gamma, p.eos, p.iso_u);
-    const Gas<double> g64 = make_gas<double>(p.gamma, p.eos, p.iso_u);
+    const Gas<float> g = gas_t<float>(p);
+    const Gas<double> g64 = gas_t<double>(p);
     const int n_items = p.use_list ? (int)p.tl[0].n_list : p.nf;
     const size_t nf = (size_t)p.nf;
     for (int base = blockIdx.x * blockDim.x; base < n_items; base += gridDim.x * blockDim.x) {
