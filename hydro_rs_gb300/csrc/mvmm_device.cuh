@@ -696,19 +696,13 @@ __device__ __forceinline__ void f32_eval(float p, const F32Side& s, float z, flo
         fpb = s.k_fp / t;
     }
 }
-// One side's term of f at an FP64 pressure P (exact.rs:12-20) for the FP32
-// face inputs of s: the shock branch from the FP32 constants, the rarefaction
-// branch as c (t^(1/m) - 1) with t = P / p_s to ~1e-14 (FP32 reciprocal seed,
-// one Newton step) and t^(1/m) from an FP32 seed refined by one Newton step.
-__device__ __forceinline__ double side_f64(double P, const F32Side& s, int m, float inv_m) {
-    double ps = (double)s.p;
-    if (P > ps) return (P - ps) * (double)s.sqA * rsqrt64(P + (double)s.B);
-    double r0 = (double)(1.f / s.p);
-    double t = P * (r0 * (2.0 - ps * r0));
-    float yf = __powf((float)t, inv_m);
-    double y = (double)yf;
-    y = y - (ipow(y, m) - t) * (double)(inv_m / ipow(yf, m - 1));
-    return (double)s.c_rar * (y - 1.0);
+// One side's term of f (exact.rs:12-20) in FP32 to a few ulp of the term
+// itself: (p - p_s) sqrt(A / (p + B)) for a shock, and for a rarefaction
+// c ((p/p_s)^(1/m) - 1) = c expm1(log1p((p - p_s) / p_s) / m), which does not
+// lose the digits of t - 1 when p is close to p_s.
+__device__ __forceinline__ float side_acc(float p, const F32Side& s, float inv_m) {
+    if (p > s.p) return (p - s.p) * s.sqA * rsqrtf(p + s.B);
+    return s.c_rar * expm1f(log1pf((p - s.p) / s.p) * inv_m);
 }
 static __device__ __noinline__ Star<float> ex_star_split(float rl, float pl, float al, float rr, float pr, float ar,
                                                          float vl, float vr, Gas<float> g, Gas<double> g64,
@@ -751,15 +745,14 @@ static __device__ __noinline__ Star<float> ex_star_split(float rl, float pl, flo
         if (done) break;
     }
     p = ipow(x, m);
-    // one FP64 Newton step: the terms of f from the FP32 face inputs, with the
-    // (P/p_s)^(1/m) - 1 cancellation and the final sum in FP64; f' in FP32
-    double P = (double)p;
+    // one Newton step with the cancelling sum f = f_l + f_r + (v_r - v_l) in
+    // FP64 over accurate FP32 terms; f' in FP32
     float fbl, fpl, fbr, fpr;
     f32_eval(p, L, z, fbl, fpl);
     f32_eval(p, R, z, fbr, fpr);
-    double fP = ((double)vr - (double)vl) + side_f64(P, L, m, inv_m) + side_f64(P, R, m, inv_m);
+    double fP = ((double)vr - (double)vl) + (double)side_acc(p, L, inv_m) + (double)side_acc(p, R, inv_m);
     double dP = fP * (double)(1.f / (fpl + fpr));
-    P = P - dP;
+    double P = (double)p - dP;
     Star<float> s;
     // a search that ended more than 1e-4 from the root (after the step the
     // error is of order dP^2) is redone by the full FP64 iteration
@@ -776,9 +769,7 @@ static __device__ __noinline__ Star<float> ex_star_split(float rl, float pl, flo
     }
     // star_state_from_pstar (exact.rs:214-238) in FP32 at the polished pressure
     float ps = (float)P;
-    f32_eval(ps, L, z, fbl, fpl);
-    f32_eval(ps, R, z, fbr, fpr);
-    s.u = 0.5f * (vl + vr) + 0.5f * (fbr - fbl);
+    s.u = 0.5f * (vl + vr) + 0.5f * (side_acc(ps, R, inv_m) - side_acc(ps, L, inv_m));
     float gg = g.gm1dgp1();
     float qlr = ps / pl, qrr = ps / pr;
     s.rho_l = qlr > 1.f ? rl * (qlr + gg) / (gg * qlr + 1.f) : rl * ipow(__powf(qlr, z), g64.rm - 2);

@@ -71,7 +71,8 @@ enum FaceGeom32 : int {
     GE_DL = 18,   // 3: (fc - cen_l) - s   (limiter extrapolation, left cell)
     GE_DR = 21,   // 3: (fc - cen_r) + s   (limiter extrapolation, right cell)
     GE_W = 24,    // area / |ds|^2         (WLS weight)
-    kFaceGeom32 = 25
+    GE_A = 25,    // area
+    kFaceGeom32 = 26
 };
 
 // Device timeline + counters of one simulation (TimestepInfo, engine.rs:33-41).

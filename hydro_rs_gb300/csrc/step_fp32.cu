@@ -84,6 +84,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_geom32(KP p) {
         g[(3 * k + 2) * nf + f] = (float)vals[k].z;
     }
     g[GE_W * nf + f] = (float)(p.area[f] / len2(ds));
+    g[GE_A * nf + f] = (float)p.area[f];
 }
 
 __device__ __forceinline__ St<float> reconstruct32(const KP& p, int i, const St<float>& prim, V3<float> dx, float td) {
@@ -132,7 +133,7 @@ __device__ __forceinline__ Out32 face_interior32(const KP& p, int f, int l, int 
                                         p.max_iter, err, &p.rsx);
     o.dx = dx;
     o.v_max = v_max;
-    o.a_over_r = (float)p.area[f] / len(dx);  // feeds max_a_over_r only (mesh steering)
+    o.a_over_r = p.geo[GE_A * (size_t)p.nf + f] / len(dx);  // feeds max_a_over_r only (mesh steering)
     return o;
 }
 
@@ -168,7 +169,7 @@ __device__ __forceinline__ Out32 face_boundary32(const KP& p, int f, int i, floa
     o.F = solve_for_flux<float, SOLVER>(dash, bnd, v3(0.f, 0.f, 0.f), n, g, g64, p.max_iter, err, &p.rsx);
     o.dx = dx;
     o.v_max = v_max;
-    o.a_over_r = (float)p.area[f] / len(dx);
+    o.a_over_r = p.geo[GE_A * (size_t)p.nf + f] / len(dx);
     return o;
 }
 
@@ -204,17 +205,17 @@ __global__ void __launch_bounds__(kMaxBlock) k_face_flux32(KP p) {
                 o = face_boundary32<SOLVER>(p, f, l, (float)dt, g, g64, &err);
                 counted = true;
             }
-            double area = p.area[f];
             if (p.flux_rows == 7) {
                 // step: FP32 rows dt * area * F, v_max, a_over_r (accumulated in FP64 by the update)
                 float* out = p.flux32;
-                float da = counted ? (float)(dt * area) : 0.f;
+                float da = counted ? (float)dt * p.geo[GE_A * nf + f] : 0.f;
 #pragma unroll
                 for (int q = 0; q < 5; q++) out[q * nf + f] = counted ? da * o.F.q[q] : 0.f;
                 out[5 * nf + f] = counted ? o.v_max : 0.f;
                 out[6 * nf + f] = counted ? o.a_over_r : 0.f;
             } else {
                 // per-stage call: the FluxInfo rows in FP64, mflux included
+                double area = p.area[f];
                 double* out = p.flux;
 #pragma unroll
                 for (int q = 0; q < 5; q++) out[q * nf + f] = counted ? dt * (area * (double)o.F.q[q]) : 0.;
