@@ -314,9 +314,27 @@ __device__ __forceinline__ void c2p(const KP& p, int i, const St<double>& cons, 
 }
 
 // ---------------------------------------------------- scatter + update --
+// Error-free FP32 sum (Knuth's TwoSum): hi + lo carries the sum of the FP32
+// addends to ~1e-14 relative, so FP32 face fluxes are accumulated at FP64
+// accuracy without a per-face FP64 conversion.
+struct Sum2 {
+    float hi, lo;
+};
+__device__ __forceinline__ void sum2_add(Sum2& a, float x) {
+    float s = a.hi + x;
+    float bp = s - a.hi;
+    float e = (a.hi - (s - bp)) + (x - bp);
+    a.hi = s;
+    a.lo += e;
+}
+
 // apply_fluxes (runner/hydrodynamics.rs:13-39): CSR gather of every face of
 // the cell in CSR order; active cells fold the accumulator into the conserved
 // state (Particle::apply_flux, part.rs:178-193), then kick2 and cons->prim.
+// ROWS32: the FP32-face form's step rows (FP32 dt * area * F, v_max,
+// a_over_r), summed per cell in FP32 two-sums and added to the FP64
+// accumulator once; otherwise the FP64 rows are folded in face order.
+template <bool ROWS32>
 __global__ void __launch_bounds__(kMaxBlock) k_update(KP p, int do_c2p) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
@@ -326,26 +344,44 @@ __global__ void __launch_bounds__(kMaxBlock) k_update(KP p, int do_c2p) {
     St<double> facc = C5(p, F_FACC, i);
     double msv = C(p, F_MSV, i), maor = C(p, F_MAOR, i);
     const size_t nf = (size_t)p.nf;
-    const int rv = p.flux_rows == 10 ? 8 : 5;
-    const double* fl = p.flux;
-    // the FP32-face form's step writes FP32 rows; they are accumulated in FP64
-    const bool rows32 = p.fp32 && p.flux_rows == 7;
-    const float* fl32 = p.flux32;
     int k0 = p.csr_off[i], k1 = p.csr_off[i + 1];
-    for (int k = k0; k < k1; k++) {
-        int f = p.csr_face[k];
-        // an inactive face carries FluxInfo::zero(): adding it changes nothing
-        if (p.use_list && !p.face_act[f]) continue;
-        St<double> x;
+    if (ROWS32) {
+        const float* fl = p.flux32;
+        Sum2 acc[5];
 #pragma unroll
-        for (int q = 0; q < 5; q++) x.q[q] = rows32 ? (double)fl32[q * nf + f] : fl[q * nf + f];
-        if (p.left[f] == i) facc = facc - x;  // update_fluxes_left (part.rs:160-167)
-        else facc = facc + x;                 // update_fluxes_right (part.rs:169-176)
-        if (act) {
-            double vm = rows32 ? (double)fl32[5 * nf + f] : fl[rv * nf + f];
-            double ar = rows32 ? (double)fl32[6 * nf + f] : fl[(rv + 1) * nf + f];
-            msv = m_max(vm, msv);
-            maor = m_max(maor, ar);
+        for (int q = 0; q < 5; q++) acc[q] = {0.f, 0.f};
+        float vm = -INFINITY, ar = -INFINITY;
+        for (int k = k0; k < k1; k++) {
+            int f = p.csr_face[k];
+            if (p.use_list && !p.face_act[f]) continue;
+            float sg = p.left[f] == i ? -1.f : 1.f;  // update_fluxes_left / _right (part.rs:160-176)
+#pragma unroll
+            for (int q = 0; q < 5; q++) sum2_add(acc[q], sg * fl[q * nf + f]);
+            vm = fmaxf(vm, fl[5 * nf + f]);
+            ar = fmaxf(ar, fl[6 * nf + f]);
+        }
+#pragma unroll
+        for (int q = 0; q < 5; q++) facc.q[q] = facc.q[q] + ((double)acc[q].hi + (double)acc[q].lo);
+        if (act && k1 > k0) {
+            msv = m_max((double)vm, msv);
+            maor = m_max(maor, (double)ar);
+        }
+    } else {
+        const int rv = p.flux_rows == 10 ? 8 : 5;
+        const double* fl = p.flux;
+        for (int k = k0; k < k1; k++) {
+            int f = p.csr_face[k];
+            // an inactive face carries FluxInfo::zero(): adding it changes nothing
+            if (p.use_list && !p.face_act[f]) continue;
+            St<double> x;
+#pragma unroll
+            for (int q = 0; q < 5; q++) x.q[q] = fl[q * nf + f];
+            if (p.left[f] == i) facc = facc - x;  // update_fluxes_left (part.rs:160-167)
+            else facc = facc + x;                 // update_fluxes_right (part.rs:169-176)
+            if (act) {
+                msv = m_max(fl[rv * nf + f], msv);
+                maor = m_max(maor, fl[(rv + 1) * nf + f]);
+            }
         }
     }
     unsigned int err = 0;
@@ -654,7 +690,9 @@ void launch_compact(const KP& p, cudaStream_t s) {
     if (p.nf > 0) k_compact<<<grid(p.nf, p.blk_cell), p.blk_cell, 0, s>>>(p);
 }
 void launch_update(const KP& p, int do_c2p, cudaStream_t s) {
-    if (p.n > 0) k_update<<<grid(p.n, p.blk_cell), p.blk_cell, 0, s>>>(p, do_c2p);
+    if (p.n <= 0) return;
+    if (p.fp32 && p.flux_rows == 7) k_update<true><<<grid(p.n, p.blk_cell), p.blk_cell, 0, s>>>(p, do_c2p);
+    else k_update<false><<<grid(p.n, p.blk_cell), p.blk_cell, 0, s>>>(p, do_c2p);
 }
 void launch_c2p(const KP& p, cudaStream_t s) {
     if (p.n > 0) k_c2p<<<grid(p.n, p.blk_cell), p.blk_cell, 0, s>>>(p);
