@@ -286,13 +286,16 @@ def run_ours(args):
     t0 = time.perf_counter()
     f0 = sim.active_faces
     for _ in range(e2e_steps):
-        sim.upload(cells)
-        try:
-            sim.step()
-        except G.MvmmError as e:
-            if not batch or e.code != -3:
-                raise
-        sim.state(cells)
+        if batch:
+            sim.upload(cells)
+            try:
+                sim.step()
+            except G.MvmmError as e:
+                if e.code != -3:
+                    raise
+            sim.state(cells)
+        else:
+            sim.step_cells(cells)  # upload + step + download in one C call
     e2e_s = time.perf_counter() - t0
     barrier()
     e2e_faces = sim.active_faces - f0
@@ -355,7 +358,9 @@ def run_ours(args):
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_faces / e2e_s, "unit": UNIT, "h2d_bytes_per_step": bytes_cells,
                 "d2h_bytes_per_step": bytes_cells + 64,
-                "how": "mvmm_upload_cells + mvmm_step + mvmm_download_cells per step, one pinned host block in the device field order, wall clock"},
+                "how": ("mvmm_upload_cells + mvmm_step + mvmm_download_cells per step" if batch else
+                        "mvmm_step_cells per step (upload, step and download in one C call)") +
+                       ", one pinned host block in the device field order, wall clock"},
         "gpu_launches": args.steps * 7 * 1 + args.steps * 6,
         "clocks": clocks,
     }

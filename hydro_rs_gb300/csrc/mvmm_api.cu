@@ -75,6 +75,8 @@ struct mvmm_ctx {
     cudaGraphExec_t step_exec = nullptr;
     bool prof = false;
     cudaEvent_t ev[MVMM_NUM_KERNELS + 1] = {};
+    cudaStream_t side = nullptr;              // copies of mvmm_step_cells that overlap the step
+    cudaEvent_t ev_in = nullptr, ev_upd = nullptr, ev_out = nullptr;
     double prof_ms[MVMM_NUM_KERNELS] = {};
     int64_t prof_n[MVMM_NUM_KERNELS] = {};
     double time_base = 0, time_base_inv = 0;
@@ -174,7 +176,9 @@ void launch_face(mvmm_ctx* c, const KP& p) {
 }
 
 // The six kernels of one OptimalOrderRunner step, optionally bracketed by events.
-void enqueue_step_kernels(mvmm_ctx* c, bool with_events) {
+// before_update: an event the update waits for; after_update: recorded after it
+void enqueue_step_kernels(mvmm_ctx* c, bool with_events, cudaEvent_t before_update = nullptr,
+                          cudaEvent_t after_update = nullptr) {
     KP p = make_kp(c, 0, 7);
     cudaStream_t s = c->stream;
     if (with_events) cudaEventRecord(c->ev[0], s);
@@ -183,7 +187,9 @@ void enqueue_step_kernels(mvmm_ctx* c, bool with_events) {
     if (with_events) cudaEventRecord(c->ev[1], s);
     launch_face(c, p);
     if (with_events) cudaEventRecord(c->ev[2], s);
+    if (before_update) cudaStreamWaitEvent(s, before_update, 0);
     launch_update(p, 1, s);
+    if (after_update) cudaEventRecord(after_update, s);
     if (with_events) cudaEventRecord(c->ev[3], s);
     if (c->prm.precision == MVMM_PRECISION_FP32FACE) launch_gradients32(p, s);
     else launch_gradients(p, 1, s);
@@ -479,6 +485,9 @@ int mvmm_ctx_destroy(mvmm_ctx* c) {
     for (int k = 0; k <= MVMM_NUM_KERNELS; k++)
         if (c->ev[k]) cudaEventDestroy(c->ev[k]);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+    if (c->side) cudaStreamDestroy(c->side);
+    for (cudaEvent_t e : {c->ev_in, c->ev_upd, c->ev_out})
+        if (e) cudaEventDestroy(e);
     delete c;
     return MVMM_OK;
 }
@@ -499,68 +508,124 @@ int mvmm_ctx_set_stream(mvmm_ctx* c, void* stream) {
 
 uint32_t mvmm_error_bits(mvmm_ctx* c) { return c ? c->err_bits : 0u; }
 
-int mvmm_upload_cells(mvmm_ctx* c, const mvmm_cells* h) {
-    if (!c || !h) return fail(MVMM_E_INVALID, "null argument");
-    if (h->n != c->n) return fail(MVMM_E_INVALID, "cell count does not match the mesh");
-    size_t n = c->n;
-    cudaStream_t s = c->stream;
-    struct {
-        const double* src;
-        int field, rows;
-    } map[] = {{h->cons, F_CONS, 5},   {h->prim, F_PRIM, 5},   {h->grad, F_GRAD, 15},      {h->gc, F_GC, 3},
-               {h->extrap, F_EXTRAP, 5}, {h->facc, F_FACC, 5}, {h->volume, F_VOL, 1},      {h->loc, F_LOC, 3},
-               {h->centroid, F_CEN, 3}, {h->v, F_V, 3},         {h->v_rel, F_VREL, 3},     {h->max_a_over_r, F_MAOR, 1},
-               {h->max_signal_velocity, F_MSV, 1}, {h->dt, F_DT, 1}};
-    // rows that lie back to back on the host in the device's field order go
-    // in one copy (a packed host block takes a single copy)
-    const size_t m = sizeof(map) / sizeof(map[0]);
-    for (size_t a = 0; a < m;) {
-        if (!map[a].src) return fail(MVMM_E_INVALID, "null cell field");
-        size_t b = a + 1;
-        int rows = map[a].rows;
-        while (b < m && map[b].src == map[a].src + (size_t)rows * n && map[b].field == map[a].field + rows)
-            rows += map[b++].rows;
-        CUDA_TRY(cudaMemcpyAsync(c->cd + (size_t)map[a].field * n, map[a].src, (size_t)rows * n * 8,
-                                 cudaMemcpyHostToDevice, s));
-        a = b;
+}  // extern "C"
+
+namespace {
+// One host array of cell rows and its place in the device block.
+struct RowCopy {
+    double* host;
+    int field, rows;
+};
+// The rows of mvmm_cells in the device's field order; subset: a bit per entry.
+constexpr unsigned kAllRows = 0x3fffu;
+constexpr unsigned kRowsEarlyOut = 0x23u;  // cons, prim, facc: final once the update has run
+constexpr unsigned kRowsLateIn = 0x1821u;  // cons, facc, max_a_over_r, max_signal_velocity: read from the update on
+int row_map(const mvmm_cells* h, unsigned subset, RowCopy* out, size_t* m) {
+    const RowCopy all[14] = {{h->cons, F_CONS, 5},         {h->prim, F_PRIM, 5},     {h->grad, F_GRAD, 15},
+                             {h->gc, F_GC, 3},             {h->extrap, F_EXTRAP, 5}, {h->facc, F_FACC, 5},
+                             {h->volume, F_VOL, 1},        {h->loc, F_LOC, 3},       {h->centroid, F_CEN, 3},
+                             {h->v, F_V, 3},               {h->v_rel, F_VREL, 3},    {h->max_a_over_r, F_MAOR, 1},
+                             {h->max_signal_velocity, F_MSV, 1}, {h->dt, F_DT, 1}};
+    *m = 0;
+    for (int k = 0; k < 14; k++) {
+        if (!all[k].host) return fail(MVMM_E_INVALID, "null cell field");
+        if (subset & (1u << k)) out[(*m)++] = all[k];
     }
     if (!h->timebin) return fail(MVMM_E_INVALID, "null timebin");
-    CUDA_TRY(cudaMemcpyAsync(c->timebin, h->timebin, n, cudaMemcpyHostToDevice, s));
-    // positions and centroids may have changed: refresh the FP32 face geometry
+    return MVMM_OK;
+}
+// Copies rows between the host arrays and the device block; rows that lie
+// back to back on the host in the device's field order go in one copy (a
+// packed host block in that order takes a single copy).
+int copy_rows(mvmm_ctx* c, const RowCopy* map, size_t m, cudaMemcpyKind kind, cudaStream_t s) {
+    const size_t n = c->n;
+    for (size_t a = 0; a < m;) {
+        size_t b = a + 1;
+        int rows = map[a].rows;
+        while (b < m && map[b].host == map[a].host + (size_t)rows * n && map[b].field == map[a].field + rows)
+            rows += map[b++].rows;
+        double* dev = c->cd + (size_t)map[a].field * n;
+        size_t bytes = (size_t)rows * n * 8;
+        if (kind == cudaMemcpyHostToDevice) CUDA_TRY(cudaMemcpyAsync(dev, map[a].host, bytes, kind, s));
+        else CUDA_TRY(cudaMemcpyAsync(map[a].host, dev, bytes, kind, s));
+        a = b;
+    }
+    return MVMM_OK;
+}
+int copy_cells(mvmm_ctx* c, const mvmm_cells* h, unsigned subset, bool timebin, cudaMemcpyKind kind,
+               cudaStream_t s) {
+    if (h->n != c->n) return fail(MVMM_E_INVALID, "cell count does not match the mesh");
+    RowCopy map[14];
+    size_t m = 0;
+    int rc = row_map(h, subset, map, &m);
+    if (rc) return rc;
+    rc = copy_rows(c, map, m, kind, s);
+    if (rc) return rc;
+    if (timebin) {
+        if (kind == cudaMemcpyHostToDevice) CUDA_TRY(cudaMemcpyAsync(c->timebin, h->timebin, c->n, kind, s));
+        else CUDA_TRY(cudaMemcpyAsync(h->timebin, c->timebin, c->n, kind, s));
+    }
+    return MVMM_OK;
+}
+// positions and centroids may have changed: refresh the FP32 face geometry
+int refresh_geometry(mvmm_ctx* c, cudaStream_t s) {
     if (c->prm.precision == MVMM_PRECISION_FP32FACE) {
         launch_geom32(make_kp(c, 0, 7), s);
         CUDA_TRY(cudaGetLastError());
     }
     return MVMM_OK;
 }
+}  // namespace
+
+extern "C" {
+
+int mvmm_upload_cells(mvmm_ctx* c, const mvmm_cells* h) {
+    if (!c || !h) return fail(MVMM_E_INVALID, "null argument");
+    int rc = copy_cells(c, h, kAllRows, true, cudaMemcpyHostToDevice, c->stream);
+    if (rc) return rc;
+    return refresh_geometry(c, c->stream);
+}
 
 int mvmm_download_cells(mvmm_ctx* c, mvmm_cells* h) {
     if (!c || !h) return fail(MVMM_E_INVALID, "null argument");
-    if (h->n != c->n) return fail(MVMM_E_INVALID, "cell count does not match the mesh");
-    size_t n = c->n;
-    cudaStream_t s = c->stream;
-    struct {
-        double* dst;
-        int field, rows;
-    } map[] = {{h->cons, F_CONS, 5},   {h->prim, F_PRIM, 5},   {h->grad, F_GRAD, 15},      {h->gc, F_GC, 3},
-               {h->extrap, F_EXTRAP, 5}, {h->facc, F_FACC, 5}, {h->volume, F_VOL, 1},      {h->loc, F_LOC, 3},
-               {h->centroid, F_CEN, 3}, {h->v, F_V, 3},         {h->v_rel, F_VREL, 3},     {h->max_a_over_r, F_MAOR, 1},
-               {h->max_signal_velocity, F_MSV, 1}, {h->dt, F_DT, 1}};
-    const size_t m = sizeof(map) / sizeof(map[0]);
-    for (size_t a = 0; a < m;) {
-        if (!map[a].dst) return fail(MVMM_E_INVALID, "null cell field");
-        size_t b = a + 1;
-        int rows = map[a].rows;
-        while (b < m && map[b].dst == map[a].dst + (size_t)rows * n && map[b].field == map[a].field + rows)
-            rows += map[b++].rows;
-        CUDA_TRY(cudaMemcpyAsync(map[a].dst, c->cd + (size_t)map[a].field * n, (size_t)rows * n * 8,
-                                 cudaMemcpyDeviceToHost, s));
-        a = b;
-    }
-    if (!h->timebin) return fail(MVMM_E_INVALID, "null timebin");
-    CUDA_TRY(cudaMemcpyAsync(h->timebin, c->timebin, n, cudaMemcpyDeviceToHost, s));
-    CUDA_TRY(cudaStreamSynchronize(s));
+    int rc = copy_cells(c, h, kAllRows, true, cudaMemcpyDeviceToHost, c->stream);
+    if (rc) return rc;
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
     return MVMM_OK;
+}
+
+int mvmm_step_cells(mvmm_ctx* c, const mvmm_cells* in, mvmm_cells* out, uint64_t ti_current, uint64_t ti_old,
+                    uint64_t* ti_next, int64_t* n_active_faces) {
+    if (!c || !in || !out) return fail(MVMM_E_INVALID, "null argument");
+    if (c->n_inst != 1) return fail(MVMM_E_UNSUPPORTED, "mvmm_step_cells steps a single simulation");
+    if (!c->side) {
+        CUDA_TRY(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
+        for (cudaEvent_t* e : {&c->ev_in, &c->ev_upd, &c->ev_out})
+            CUDA_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    }
+    cudaStream_t s = c->stream, s2 = c->side;
+    // what predict and the face stage read, then (side stream) what only the update needs
+    int rc = copy_cells(c, in, kAllRows & ~kRowsLateIn, true, cudaMemcpyHostToDevice, s);
+    if (!rc) rc = copy_cells(c, in, kRowsLateIn, false, cudaMemcpyHostToDevice, s2);
+    if (rc) return rc;
+    CUDA_TRY(cudaEventRecord(c->ev_in, s2));
+    rc = refresh_geometry(c, s);
+    if (rc) return rc;
+    launch_set_time(make_kp(c, 0, 7), ti_current, ti_old, s);
+    enqueue_step_kernels(c, false, c->ev_in, c->ev_upd);
+    // rows final after the update go back while the gradient and limiter stages run
+    CUDA_TRY(cudaStreamWaitEvent(s2, c->ev_upd, 0));
+    rc = copy_cells(c, out, kRowsEarlyOut, false, cudaMemcpyDeviceToHost, s2);
+    if (rc) return rc;
+    CUDA_TRY(cudaEventRecord(c->ev_out, s2));
+    rc = copy_cells(c, out, kAllRows & ~kRowsEarlyOut, true, cudaMemcpyDeviceToHost, s);
+    if (rc) return rc;
+    CUDA_TRY(cudaStreamWaitEvent(s, c->ev_out, 0));
+    CUDA_TRY(cudaGetLastError());
+    rc = finish(c);
+    if (ti_next) *ti_next = c->tl_host->ti_current;
+    if (n_active_faces) *n_active_faces = (int64_t)(c->tl_host->active_faces - c->tl_host->faces_mark);
+    return rc;
 }
 
 // ---- per-stage --------------------------------------------------------

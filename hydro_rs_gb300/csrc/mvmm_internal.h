@@ -90,6 +90,7 @@ struct DevTimeline {
     unsigned long long fallback_faces;  // FP32-face form: faces solved by the full FP64 iteration
     unsigned int n_list;                // length of this step's active-face list (hierarchical steps)
     unsigned int pad2;
+    unsigned long long faces_mark;      // active_faces when the time was last set on the device
 };
 
 // Internal (not exported) flag a face's Riemann solve sets when the FP32-face
@@ -154,6 +155,7 @@ void launch_timesteps(const KP& p, double* dt_out, cudaStream_t s);
 void launch_limit(const KP& p, cudaStream_t s);
 void launch_compact(const KP& p, cudaStream_t s);
 void launch_end(const KP& p, cudaStream_t s);
+void launch_set_time(const KP& p, unsigned long long ti_current, unsigned long long ti_old, cudaStream_t s);
 // FP32 form helpers
 void launch_prep32(const KP& p, cudaStream_t s);
 

@@ -635,6 +635,20 @@ __global__ void k_end(KP p) {
     tl->n_list = 0;
 }
 
+// Sets every simulation's integer time on the device (the counters stay);
+// faces_mark remembers the face counter so the step's own count can be read.
+__global__ void k_set_time(KP p, unsigned long long ti_current, unsigned long long ti_old) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= p.n_inst) return;
+    DevTimeline* tl = p.tl + k;
+    tl->ti_current = ti_current;
+    tl->ti_old = ti_old;
+    tl->min_dti = MAX_NR_TIMESTEPS;
+    tl->min_timebin = 127;
+    tl->done = 0;
+    tl->faces_mark = tl->active_faces;
+}
+
 // ---------------------------------------------- Riemann over arrays --
 template <int SOLVER, bool SAMPLE>
 __global__ void k_riemann(double gamma, int64_t n, const double* l, const double* r, const double* vf,
@@ -707,6 +721,9 @@ void launch_limit(const KP& p, cudaStream_t s) {
     if (p.n > 0) k_limit<<<grid(p.n, p.blk_cell), p.blk_cell, 0, s>>>(p);
 }
 void launch_end(const KP& p, cudaStream_t s) { k_end<<<(p.n_inst + 127) / 128, 128, 0, s>>>(p); }
+void launch_set_time(const KP& p, unsigned long long ti_current, unsigned long long ti_old, cudaStream_t s) {
+    k_set_time<<<(p.n_inst + 127) / 128, 128, 0, s>>>(p, ti_current, ti_old);
+}
 
 // kind: SOLVER_*; sampling is defined for the star solvers, so HLLC and
 // linear advection sample the exact solution.

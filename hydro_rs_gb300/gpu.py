@@ -26,6 +26,7 @@ EXPORTED = (
     "mvmm_step", "mvmm_run", "mvmm_enqueue_steps", "mvmm_set_time", "mvmm_get_time", "mvmm_profile_enable",
     "mvmm_profile_read", "mvmm_riemann_flux", "mvmm_riemann_sample", "mvmm_get_stats",
     "mvmm_ctx_create_batched", "mvmm_batch_state", "mvmm_autotune", "mvmm_riemann_flux_p", "mvmm_riemann_sample_p",
+    "mvmm_step_cells",
 )
 
 
@@ -90,6 +91,7 @@ def load_library(path: str = LIB_PATH):
         "mvmm_riemann_flux": (i32, [i32, i32, dbl, i64, vp, vp, vp, vp, vp]),
         "mvmm_riemann_sample": (i32, [i32, i32, dbl, i64, vp, vp, vp, vp]),
         "mvmm_riemann_flux_p": (i32, [vp, i64, vp, vp, vp, vp, vp]),
+        "mvmm_step_cells": (i32, [vp, vp, vp, u64, u64, pu64, pi64]),
         "mvmm_riemann_sample_p": (i32, [vp, i64, vp, vp, vp, vp]),
         "mvmm_get_stats": (i32, [vp, vp]),
         "mvmm_ctx_create_batched": (i32, [vp, vp, i64, vp, vp, ctypes.POINTER(vp)]),
@@ -220,6 +222,22 @@ class GpuSim:
         nf = ctypes.c_int64(0)
         _check(load_library().mvmm_step(self.h, self.ti_current, self.ti_old, ctypes.byref(tn), ctypes.byref(nf)),
                self.h)
+        self.steps += 1
+        self.active_faces += nf.value
+        done = self.ti_current >= MAX_NR_TIMESTEPS
+        self.ti_old, self.ti_current = self.ti_current, tn.value
+        self.finished = done
+        return done
+
+    def step_cells(self, cells_in: Cells, cells_out: Cells | None = None) -> bool:
+        """One step on host-resident state (mvmm_step_cells): upload, step and
+        download in one call; cells_out defaults to cells_in."""
+        cells_out = cells_in if cells_out is None else cells_out
+        ci, co = cells_in.cview(), cells_out.cview()
+        tn = ctypes.c_uint64(0)
+        nf = ctypes.c_int64(0)
+        _check(load_library().mvmm_step_cells(self.h, ctypes.byref(ci), ctypes.byref(co), self.ti_current,
+                                              self.ti_old, ctypes.byref(tn), ctypes.byref(nf)), self.h)
         self.steps += 1
         self.active_faces += nf.value
         done = self.ti_current >= MAX_NR_TIMESTEPS

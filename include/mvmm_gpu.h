@@ -11,7 +11,8 @@
  *
  * Memory: all device memory is owned by the context; callers pass host
  * pointers (pageable or pinned) and sizes only.  A context is used by one host
- * thread at a time and orders all its work on one CUDA stream.
+ * thread at a time and orders all its work on one CUDA stream (mvmm_step_cells
+ * adds a second stream for overlapped copies and joins it before returning).
  */
 #ifndef MVMM_GPU_H
 #define MVMM_GPU_H
@@ -43,8 +44,11 @@ enum { MVMM_EOS_IDEAL = 0, MVMM_EOS_ISOTHERMAL = 1 };
 /* Arithmetic form of the face stage. */
 enum {
     MVMM_PRECISION_FP64 = 0,    /* plain: everything FP64, reference evaluation order */
-    MVMM_PRECISION_FP32FACE = 1 /* reconstruction/Riemann/flux FP32; geometry, Newton,
-                                   conserved, scatter and time integration FP64 */
+    MVMM_PRECISION_FP32FACE = 1 /* reconstruction, limiter, gradients, Riemann solve and
+                                   face fluxes FP32 (face geometry formed in FP64 and
+                                   rounded once; the exact solver's Newton sum FP64);
+                                   conserved state, flux accumulation, timesteps and the
+                                   integer timeline FP64 */
 };
 /* Particle motion: engine.rs:7-13.  Only FIXED is implemented (the mesh is
  * rebuilt on the host for the other modes). */
@@ -166,6 +170,14 @@ int mvmm_gradients(mvmm_ctx *ctx, const uint8_t *active);
  * integer time ti_current with the previous sync point ti_old; returns ti_next
  * and the number of faces that reached flux_exchange*. */
 int mvmm_step(mvmm_ctx *ctx, uint64_t ti_current, uint64_t ti_old, uint64_t *ti_next, int64_t *n_active_faces);
+/* Runner::step(&mut Space, ..) on host-resident state (runner.rs:6-22): uploads
+ * `in`, runs one step (OptimalOrderRunner or GodunovHydroRunner) and writes the
+ * new state to `out` (which may be `in`) in one call.  Copies of the rows the
+ * update alone reads and of the rows final after it overlap the other stages.
+ * Host arrays laid out back to back in the mvmm_cells field order (pinned for
+ * speed) move in one copy per direction.  Single simulations only. */
+int mvmm_step_cells(mvmm_ctx *ctx, const mvmm_cells *in, mvmm_cells *out, uint64_t ti_current, uint64_t ti_old,
+                    uint64_t *ti_next, int64_t *n_active_faces);
 /* Engine::run (engine.rs:152-199) from the given sync point, device resident:
  * runs at most max_steps steps (<= 0: to t_end).  On return *ti_current /
  * *ti_old are the next sync point; *steps_done and *n_active_faces count the
