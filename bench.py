@@ -198,6 +198,29 @@ def _time_steps(sim, steps, stream, flush_buf, torch):
     return total
 
 
+# Compulsory HBM bytes of the face stage per launch.
+#   plain FP64 (k_face_flux): per active face its indices, area, normal, centroid
+#   and shift (88 B) and the 7 FP64 result rows (56 B); per cell next to an
+#   active face its 44 FP64 face-stage inputs and the active flag (353 B).
+#   FP32-face form (k_prep32 + k_face_flux32): k_prep32 reads 40 FP64 rows and
+#   writes 37 FP32 rows per converted cell (468 B; all cells in synchronised
+#   steps, the cells next to an active face in hierarchical ones); the face
+#   kernel reads per cell the 37 FP32 copies, dt and the flag (157 B) and per
+#   active face the indices, the 26-float static geometry and writes 7 FP32
+#   result rows (140 B).
+def face_stage_bytes(prec, nc, nfa, all_cells):
+    touched = min(nc, 2 * nfa)
+    if prec == 1:
+        return (nc if all_cells else touched) * 468 + touched * 157 + nfa * 140
+    return touched * 353 + nfa * 144
+
+
+# DRAM bytes (read + write) per launch of the face stage from ncu captures at
+# the bench sizes (cold caches, ncu's default cache control): the committed
+# summaries in profiles/ give the commands.  Keyed by (workload, nx, form).
+TRAFFIC = {}
+
+
 def _face_kernel_ms(sim, steps):
     sim.profile(True)
     sim.set_time()
@@ -271,7 +294,12 @@ def run_ours(args):
     same_time = sims[1].ti_current == sims[0].ti_current
 
     # per-kernel times (events around each kernel) for the roofline
-    prof = {prec: _face_kernel_ms(sim, min(args.steps, 20)) for prec, sim in sims.items()}
+    prof, nfa = {}, {}
+    for prec, sim in sims.items():
+        k_prof = min(args.steps, 20)
+        f0 = sim.stats()["active_faces"]
+        prof[prec] = _face_kernel_ms(sim, k_prof)
+        nfa[prec] = (sim.stats()["active_faces"] - f0) / k_prof  # active faces per profiled step
 
     # end-to-end through the C ABI with pinned host buffers
     # one pinned block in the device's field order: one copy each way per step
@@ -330,12 +358,14 @@ def run_ours(args):
     def roof(prec):
         ms, n = prof[prec]["face_flux"]
         ms_launch = ms / max(n, 1)
-        per_cell = 193 if prec == 1 else 353
-        bytes_launch = nf * (88 + 56) + nc * per_cell
+        bytes_launch = face_stage_bytes(prec, nc, nfa[prec], batch or problem.params.sync_all)
         ach = bytes_launch / (ms_launch * 1e-3) / 1e9
+        traffic = TRAFFIC.get((args.workload, args.nx, prec))
         return {"bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(ach / peak, 4), "traffic": None, "kernel": "k_face_flux32" if prec == 1 else "k_face_flux",
-                "kernel_ms": round(ms_launch, 4), "algorithmic_bytes_per_launch": bytes_launch,
+                "frac": round(ach / peak, 4), "traffic": traffic,
+                "kernel": "k_prep32 + k_face_flux32" if prec == 1 else "k_face_flux",
+                "kernel_ms": round(ms_launch, 4), "algorithmic_bytes_per_launch": int(bytes_launch),
+                "active_faces_per_launch": nfa[prec],
                 "peak_kind": peak_kind, "note": "of measured" if peak_kind == "measured" else "of fallback",
                 "step_kernel_ms": {k: round(v[0] / max(v[1], 1), 4) for k, v in prof[prec].items()}}
 

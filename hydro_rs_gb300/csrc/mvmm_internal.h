@@ -141,6 +141,7 @@ struct KP {
     int godunov;             // 1: GodunovHydroRunner (no gradients), 0: OptimalOrderRunner
     int use_list;            // 1: face kernel walks the compacted active-face list
     uint8_t* face_act;       // per-face flag of this step's active-face rule
+    uint8_t* touch;          // list mode, FP32 form: cells next to an active face (prep32 converts only these)
     int* face_list;          // compacted active faces
 };
 

@@ -26,6 +26,10 @@ __global__ void __launch_bounds__(kMaxBlock) k_prep32(KP p) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
     if (p.tl[inst_of(p, i)].done) return;
+    if (p.use_list) {  // hierarchical step: only cells next to an active face are read
+        if (!p.touch[i]) return;
+        p.touch[i] = 0;
+    }
     size_t n = p.n;
     float* cf = p.cf;
 #pragma unroll

@@ -274,6 +274,10 @@ __global__ void __launch_bounds__(kMaxBlock) k_compact(KP p) {
             act = la;
         }
         p.face_act[f] = act;
+        if (act && p.fp32) {  // the FP32 copies of these cells are refreshed by k_prep32
+            p.touch[l] = 1;
+            if (r >= 0) p.touch[r] = 1;
+        }
     }
     unsigned int b = __ballot_sync(0xffffffffu, act);
     if (!b) return;
