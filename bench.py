@@ -68,18 +68,29 @@ WORKLOADS = {
     "blast3d": "point_blast_3d {n}^3 jittered periodic Voronoi, HLLC, hierarchical time bins, gamma=5/3",
     # {n} independent 1D Riemann problems packed in one batch, N log-uniform in [200, 20000]
     "batch1d": "{n} independent 1D Riemann problems (N log-uniform 200..20000), exact solver, one batch, t_end=0.15",
+    # the same batch with the PVRS solver
+    "batch1d_pvrs": "{n} independent 1D Riemann problems (N log-uniform 200..20000), PVRS solver, one batch, "
+                    "t_end=0.15",
     # served: Poisson stream (50 req/s) of {n} isentropic-vortex runs, 32^2..512^2, HLLC, t_end=1
     "serve2d": "{n} served isentropic-vortex requests (Poisson 50/s, 32^2..512^2 periodic Voronoi, HLLC, t_end=1)",
 }
-DEFAULT_N = {"kh2d": NX, "sod1d": 1000, "blast3d": 128, "batch1d": 512, "serve2d": 60}
+DATA = {
+    "kh2d": "synthetic (seeded jittered lattice, shear-layer ICs)",
+    "sod1d": "synthetic (uniform 1D lattice, Sod ICs)",
+    "blast3d": "synthetic (seeded jittered cubic lattice, point-blast ICs)",
+    "batch1d": "synthetic (seeded random 1D Riemann problems)",
+    "batch1d_pvrs": "synthetic (seeded random 1D Riemann problems)",
+}
+DEFAULT_N = {"kh2d": NX, "sod1d": 1000, "blast3d": 128, "batch1d": 512, "batch1d_pvrs": 512, "serve2d": 60}
 
 
 def _problem(nx=NX, workload="kh2d"):
     from hydro_rs_gb300 import ics
 
     t0 = time.perf_counter()
-    if workload == "batch1d":
-        probs = ics.riemann_batch_1d(nx, seed=4, riemann=ics.EXACT, t_end=0.15)
+    if workload in ("batch1d", "batch1d_pvrs"):
+        kind = ics.PVRS if workload == "batch1d_pvrs" else ics.EXACT
+        probs = ics.riemann_batch_1d(nx, seed=4, riemann=kind, t_end=0.15)
         p, off, te = ics.pack(probs)
         p.extra.update(cell_offsets=off, t_end=te, problems=probs)
     elif workload == "sod1d":
@@ -218,7 +229,7 @@ def face_stage_bytes(prec, nc, nfa, all_cells):
 # DRAM bytes (read + write) per launch of the face stage from ncu captures at
 # the bench sizes (cold caches, ncu's default cache control): the committed
 # summaries in profiles/ give the commands.  Keyed by (workload, nx, form).
-TRAFFIC = {}
+TRAFFIC = {("kh2d", 256, 1): 47_873_992, ("kh2d", 256, 0): 40_704_000}  # profiles/face_stage_traffic_kh256.txt
 
 
 def _face_kernel_ms(sim, steps):
@@ -252,13 +263,18 @@ def run_ours(args):
     sims = {}
     batch = problem.extra.get("cell_offsets") is not None
     tuned = {}
+    ctx_s = {}
     for prec in (1, 0):
+        t_ctx = time.perf_counter()
         with torch.cuda.stream(stream):
             if batch:
                 sims[prec] = G.GpuSim(problem, precision=prec, stream=stream.cuda_stream,
                                       cell_offsets=problem.extra["cell_offsets"], t_end=problem.extra["t_end"])
             else:
                 sims[prec] = G.GpuSim(problem, precision=prec, stream=stream.cuda_stream)
+        torch.cuda.synchronize()
+        # mvmm_ctx_create (device allocation + mesh upload) and the first mvmm_upload_cells
+        ctx_s[prec] = time.perf_counter() - t_ctx
         if batch:
             tuned[prec] = sims[prec].autotune(3)
     # advance both forms identically past the dt=0 first step + warm-up
@@ -374,11 +390,12 @@ def run_ours(args):
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms32 / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32-face/f64-accumulate", "data": "synthetic (seeded jittered lattice, shear-layer ICs)",
+        "dtype": "f32-face/f64-accumulate", "data": DATA.get(args.workload, "synthetic, seeded"),
         "config": {"workload": WORKLOADS[args.workload].format(n=args.nx),
                    "cells": nc, "faces": nf, "precision": "fp32_face",
                    "l2": "flushed (256 MB write) before each timed step", "parallelism": f"replicas x{ws}",
-                   "mesh_build_s": round(mesh_s, 3)},
+                   "mesh_build_s": round(mesh_s, 3),
+                   "ctx_create_and_upload_s": {"fp32_face": round(ctx_s[1], 4), "fp64": round(ctx_s[0], 4)}},
         "l1_density_err_vs_fp64": l1, "l1_same_time": same_time,
         "active_face_fraction": faces32 / (args.steps * nf * ws),
         "batch": batch_info,
