@@ -345,6 +345,8 @@ def run_ours(args):
     e2e_faces = sim.active_faces - f0
     bytes_cells = cells.nbytes()
 
+    st32 = sims[1].stats()
+    fallback32 = {"faces": st32["fp64_fallback_faces"], "of_active_faces": st32["active_faces"]}
     ms32, faces32 = res[1]
     ms64, faces64 = res[0]
     batch_info = None
@@ -397,6 +399,7 @@ def run_ours(args):
                    "mesh_build_s": round(mesh_s, 3),
                    "ctx_create_and_upload_s": {"fp32_face": round(ctx_s[1], 4), "fp64": round(ctx_s[0], 4)}},
         "l1_density_err_vs_fp64": l1, "l1_same_time": same_time,
+        "fp64_fallback_faces": fallback32,
         "active_face_fraction": faces32 / (args.steps * nf * ws),
         "batch": batch_info,
         "plain_fp64": {"value": faces64 / (ms64 * 1e-3), "unit": UNIT, "ms_per_step": ms64 / args.steps,
