@@ -66,7 +66,8 @@ struct mvmm_ctx {
     double* inst_tb = nullptr;  // per-instance time_base, 1/time_base (batches only)
     double* inst_tbi = nullptr;
     uint8_t* face_act = nullptr;
-    uint8_t* touch = nullptr;
+    unsigned int* touch = nullptr;
+    int* cell_list = nullptr;
     int* face_list = nullptr;
     int blk_face = 128, blk_cell = 128;
     DevTimeline* tl = nullptr;       // [n_inst]
@@ -150,6 +151,7 @@ KP make_kp(mvmm_ctx* c, int stage, int flux_rows) {
     p.use_list = (!stage && !c->prm.sync_all && c->n_inst == 1) ? 1 : 0;
     p.face_act = c->face_act;
     p.touch = c->touch;
+    p.cell_list = c->cell_list;
     p.face_list = c->face_list;
     p.blk_face = c->blk_face;
     p.blk_cell = c->blk_cell;
@@ -386,7 +388,8 @@ static int create_impl(const mvmm_params* prm, const mvmm_mesh* m, int64_t n_ins
     ALLOC(c->flux, 10 * nf * 8);
     ALLOC(c->dtmp, n * 8);
     ALLOC(c->face_act, nf);
-    ALLOC(c->touch, n);
+    ALLOC(c->touch, n * 4);
+    ALLOC(c->cell_list, n * 4);
     ALLOC(c->face_list, nf * 4);
     ALLOC(c->tl, sizeof(DevTimeline) * c->n_inst);
     if (c->n_inst > 1) {
@@ -418,7 +421,7 @@ static int create_impl(const mvmm_params* prm, const mvmm_mesh* m, int64_t n_ins
     cudaMemsetAsync(c->active, 0, n, s);
     cudaMemsetAsync(c->flux, 0, 10 * nf * 8, s);
     cudaMemsetAsync(c->face_act, 0, nf, s);
-    cudaMemsetAsync(c->touch, 0, n, s);
+    cudaMemsetAsync(c->touch, 0, n * 4, s);
     std::memset(c->tl_host, 0, sizeof(DevTimeline) * c->n_inst);
     for (int k = 0; k < c->n_inst; k++) {
         c->tl_host[k].min_dti = kMax;
@@ -480,7 +483,7 @@ int mvmm_ctx_destroy(mvmm_ctx* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->step_exec) cudaGraphExecDestroy(c->step_exec);
     void* ptrs[] = {c->left, c->right, c->csr_off, c->csr_face, c->area, c->normal, c->fcen, c->shift, c->cd,
-                    c->cf, c->timebin, c->tb_tmp, c->active, c->flux, c->flux32, c->geo, c->dtmp, c->face_act, c->touch,
+                    c->cf, c->timebin, c->tb_tmp, c->active, c->flux, c->flux32, c->geo, c->dtmp, c->face_act, c->touch, c->cell_list,
                     c->face_list, c->tl,
                     c->inst, c->inst_tb, c->inst_tbi};
     for (void* p : ptrs)

@@ -55,6 +55,24 @@ __device__ __forceinline__ double tbase_inv(const KP& p, int k) { return p.inst_
 __device__ __forceinline__ void set_err(const KP& p, int k, unsigned int bits) {
     if (bits) atomicOr(&p.tl[k].err, bits);
 }
+// The cells a cell kernel visits: all cells, or in a hierarchical step the
+// compacted list of active cells and the cells next to an active face (the
+// other cells are left unchanged by every stage after predict).
+__device__ __forceinline__ int cell_items(const KP& p) { return p.use_list ? (int)p.tl[0].n_clist : p.n; }
+__device__ __forceinline__ int cell_at(const KP& p, int idx) { return p.use_list ? p.cell_list[idx] : idx; }
+// Puts cell i on this step's cell list once (want: the lane has a candidate);
+// aggregated over the warp.  Every lane of the warp calls it.
+__device__ __forceinline__ void list_cell_warp(const KP& p, bool want, int i) {
+    want = want && atomicExch(&p.touch[i], 1u) == 0u;
+    unsigned int b = __ballot_sync(0xffffffffu, want);
+    if (!b) return;
+    int lane = threadIdx.x & 31, leader = __ffs(b) - 1;
+    unsigned int start = 0;
+    if (lane == leader) start = atomicAdd(&p.tl[0].n_clist, (unsigned int)__popc(b));
+    start = __shfl_sync(0xffffffffu, start, leader);
+    if (want) p.cell_list[start + __popc(b & ((1u << lane) - 1u))] = i;
+}
+
 // Counter add per instance, aggregated over the lanes of a warp that share an
 // instance (k < 0: the lane contributes nothing).  Every lane of the warp calls it.
 enum { CNT_FACES = 0, CNT_CELLS = 1, CNT_FALLBACK = 2 };

@@ -89,7 +89,7 @@ struct DevTimeline {
     unsigned long long active_cells;
     unsigned long long fallback_faces;  // FP32-face form: faces solved by the full FP64 iteration
     unsigned int n_list;                // length of this step's active-face list (hierarchical steps)
-    unsigned int pad2;
+    unsigned int n_clist;               // length of this step's cell list (hierarchical steps)
     unsigned long long faces_mark;      // active_faces when the time was last set on the device
 };
 
@@ -141,7 +141,8 @@ struct KP {
     int godunov;             // 1: GodunovHydroRunner (no gradients), 0: OptimalOrderRunner
     int use_list;            // 1: face kernel walks the compacted active-face list
     uint8_t* face_act;       // per-face flag of this step's active-face rule
-    uint8_t* touch;          // list mode, FP32 form: cells next to an active face (prep32 converts only these)
+    unsigned int* touch;     // hierarchical steps: 1 for cells on this step's cell list
+    int* cell_list;          // hierarchical steps: active cells and the cells next to an active face
     int* face_list;          // compacted active faces
 };
 
@@ -156,6 +157,7 @@ void launch_timesteps(const KP& p, double* dt_out, cudaStream_t s);
 void launch_limit(const KP& p, cudaStream_t s);
 void launch_compact(const KP& p, cudaStream_t s);
 void launch_end(const KP& p, cudaStream_t s);
+int cell_grid(const KP& p);
 void launch_set_time(const KP& p, unsigned long long ti_current, unsigned long long ti_old, cudaStream_t s);
 // FP32 form helpers
 void launch_prep32(const KP& p, cudaStream_t s);

@@ -22,14 +22,8 @@ __device__ __forceinline__ St<float> G5(const KP& p, int f, int i) {
     for (int q = 0; q < 5; q++) s.q[q] = G(p, f + q, i);
     return s;
 }
-__global__ void __launch_bounds__(kMaxBlock) k_prep32(KP p) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= p.n) return;
+__device__ __forceinline__ void prep32_cell(const KP& p, int i) {
     if (p.tl[inst_of(p, i)].done) return;
-    if (p.use_list) {  // hierarchical step: only cells next to an active face are read
-        if (!p.touch[i]) return;
-        p.touch[i] = 0;
-    }
     size_t n = p.n;
     float* cf = p.cf;
 #pragma unroll
@@ -50,6 +44,12 @@ __global__ void __launch_bounds__(kMaxBlock) k_prep32(KP p) {
     cf[(G_V + 0) * n + i] = (float)v.x;
     cf[(G_V + 1) * n + i] = (float)v.y;
     cf[(G_V + 2) * n + i] = (float)v.z;
+}
+// hierarchical steps convert only the cells on the step's cell list
+__global__ void __launch_bounds__(kMaxBlock) k_prep32(KP p) {
+    const int n_items = cell_items(p);
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n_items; idx += gridDim.x * blockDim.x)
+        prep32_cell(p, cell_at(p, idx));
 }
 
 __device__ __forceinline__ V3<float> GE3(const KP& p, int g, int f) {
@@ -267,12 +267,11 @@ __device__ __forceinline__ void other_side32(const KP& p, int i, int f, const St
 // the static face geometry, the WLS sums, the 3x3 inverse and the cell-wise
 // limiter in FP32 (these slopes only feed the FP32 reconstruction); the
 // timestep (Particle::timestep, timesteps_apply) stays FP64 as in the plain form.
-__global__ void __launch_bounds__(kMaxBlock) k_gradients32(KP p) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void gradients32_cell(const KP& p, int i) {
     unsigned long long my_dti = MAX_NR_TIMESTEPS;
     int my_tb = 127;
     unsigned int err = 0;
-    int k = i < p.n ? inst_of(p, i) : -1;
+    int k = i >= 0 ? inst_of(p, i) : -1;
     if (k >= 0 && p.tl[k].done) k = -1;
     if (k >= 0) {
         int tb = p.timebin[i];
@@ -363,6 +362,14 @@ __global__ void __launch_bounds__(kMaxBlock) k_gradients32(KP p) {
     if (err) set_err(p, k, err);
     inst_min_dti_tb(p, k, my_dti, my_tb);
 }
+__global__ void __launch_bounds__(kMaxBlock) k_gradients32(KP p) {
+    const int n_items = cell_items(p);
+    // warp-uniform trip count: the per-instance reductions need every lane
+    for (int base = blockIdx.x * blockDim.x; base < n_items; base += gridDim.x * blockDim.x) {
+        int idx = base + threadIdx.x;
+        gradients32_cell(p, idx < n_items ? cell_at(p, idx) : -1);
+    }
+}
 
 template <int SOLVER, bool SAMPLE>
 __global__ void k_riemann32(double gamma, int64_t n, const double* l, const double* r, const double* vf,
@@ -397,7 +404,7 @@ inline int grid(int n, int b = kBlock) { return (n + b - 1) / b; }
 }  // namespace
 
 void launch_prep32(const KP& p, cudaStream_t s) {
-    if (p.n > 0) k_prep32<<<grid(p.n, p.blk_cell), p.blk_cell, 0, s>>>(p);
+    if (p.n > 0) k_prep32<<<cell_grid(p), p.blk_cell, 0, s>>>(p);
 }
 
 void launch_geom32(const KP& p, cudaStream_t s) {
@@ -405,7 +412,7 @@ void launch_geom32(const KP& p, cudaStream_t s) {
 }
 
 void launch_gradients32(const KP& p, cudaStream_t s) {
-    if (p.n > 0) k_gradients32<<<grid(p.n, p.blk_cell), p.blk_cell, 0, s>>>(p);
+    if (p.n > 0) k_gradients32<<<cell_grid(p), p.blk_cell, 0, s>>>(p);
 }
 
 void launch_face_flux_fp32(const KP& p, int solver, cudaStream_t s) {

@@ -74,6 +74,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_predict(KP p) {
         write_derived(p, i, chk, src, rho_inv);
     }
     if (!p.stage) inst_count(p, k, act, CNT_CELLS);
+    if (p.use_list) list_cell_warp(p, act, i);
 }
 
 // Recomputes the derived face-stage fields (per-stage flux calls).
@@ -262,23 +263,25 @@ __global__ void __launch_bounds__(kMaxBlock) k_face_flux(KP p) {
 __global__ void __launch_bounds__(kMaxBlock) k_compact(KP p) {
     if (p.tl[0].done) return;
     int f = blockIdx.x * blockDim.x + threadIdx.x;
-    bool act = false;
+    bool act = false, any = false;
     if (f < p.nf) {
         int l = p.left[f], r = p.right[f];
         bool la = p.active[l] != 0;
+        any = la;
         if (r >= 0) {
             bool ra = p.active[r] != 0;
+            any = la || ra;
             double dtl = C(p, F_DT, l), dtr = C(p, F_DT, r);
             act = !((!la && !ra) || (dtr < dtl && !ra) || (dtl < dtr && !la));
         } else {
             act = la;
         }
         p.face_act[f] = act;
-        if (act && p.fp32) {  // the FP32 copies of these cells are refreshed by k_prep32
-            p.touch[l] = 1;
-            if (r >= 0) p.touch[r] = 1;
-        }
     }
+    // both cells of every face with an active side join the cell list: the
+    // faces of active cells, their neighbours' updates and wake-ups
+    list_cell_warp(p, any, f < p.nf ? p.left[f] : 0);
+    list_cell_warp(p, any && p.right[f < p.nf ? f : 0] >= 0, f < p.nf ? p.right[f] : 0);
     unsigned int b = __ballot_sync(0xffffffffu, act);
     if (!b) return;
     int lane = threadIdx.x & 31;
@@ -339,9 +342,7 @@ __device__ __forceinline__ void sum2_add(Sum2& a, float x) {
 // a_over_r), summed per cell in FP32 two-sums and added to the FP64
 // accumulator once; otherwise the FP64 rows are folded in face order.
 template <bool ROWS32>
-__global__ void __launch_bounds__(kMaxBlock) k_update(KP p, int do_c2p) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= p.n) return;
+__device__ __forceinline__ void update_cell(const KP& p, int i, int do_c2p) {
     const int k = inst_of(p, i);
     if (p.tl[k].done) return;
     bool act = p.active[i] != 0;
@@ -416,6 +417,12 @@ __global__ void __launch_bounds__(kMaxBlock) k_update(KP p, int do_c2p) {
     W5(p, F_FACC, i, facc);
     if (err) set_err(p, k, err);
 }
+template <bool ROWS32>
+__global__ void __launch_bounds__(kMaxBlock) k_update(KP p, int do_c2p) {
+    const int n_items = cell_items(p);
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n_items; idx += gridDim.x * blockDim.x)
+        update_cell<ROWS32>(p, cell_at(p, idx), do_c2p);
+}
 
 __global__ void __launch_bounds__(kMaxBlock) k_c2p(KP p) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -430,12 +437,11 @@ __global__ void __launch_bounds__(kMaxBlock) k_c2p(KP p) {
 // fused per cell; in step mode also compute_timesteps + timesteps_apply
 // (euler_eqns_fvs.rs:50-61, runner/hydrodynamics.rs:145-158) with block-level
 // min reductions of the integer timestep and the new time bins.
-__global__ void __launch_bounds__(kMaxBlock) k_gradients(KP p, int do_timestep) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void gradients_cell(const KP& p, int i, int do_timestep) {
     unsigned long long my_dti = MAX_NR_TIMESTEPS;
     int my_tb = 127;
     unsigned int err = 0;
-    int k = i < p.n ? inst_of(p, i) : -1;
+    int k = i >= 0 ? inst_of(p, i) : -1;
     if (k >= 0 && p.tl[k].done) k = -1;
     if (k >= 0) {
         int tb = p.timebin[i];
@@ -552,6 +558,14 @@ __global__ void __launch_bounds__(kMaxBlock) k_gradients(KP p, int do_timestep) 
     if (!do_timestep) return;
     inst_min_dti_tb(p, k, my_dti, my_tb);
 }
+__global__ void __launch_bounds__(kMaxBlock) k_gradients(KP p, int do_timestep) {
+    const int n_items = cell_items(p);
+    // warp-uniform trip count: the per-instance reductions need every lane
+    for (int base = blockIdx.x * blockDim.x; base < n_items; base += gridDim.x * blockDim.x) {
+        int idx = base + threadIdx.x;
+        gradients_cell(p, idx < n_items ? cell_at(p, idx) : -1, do_timestep);
+    }
+}
 
 // compute_timesteps as a stage (euler_eqns_fvs.rs:50-61)
 __global__ void __launch_bounds__(kMaxBlock) k_timesteps(KP p, double* out) {
@@ -564,9 +578,8 @@ __global__ void __launch_bounds__(kMaxBlock) k_timesteps(KP p, double* out) {
 // timestep_sync or timestep_limiter (runner/hydrodynamics.rs:160-191) with
 // Particle::timestep_limit (part.rs:263-297); then reset_extrapolations and
 // kick1 (runner/hydrodynamics.rs:41-49, 193-195).
-__global__ void __launch_bounds__(kMaxBlock) k_limit(KP p) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= p.n) return;
+__device__ __forceinline__ void limit_cell(const KP& p, int i) {
+    if (p.use_list) p.touch[i] = 0;  // the last stage that reads the cell list
     const int k = inst_of(p, i);
     if (p.tl[k].done) return;
     const double time_base = tbase(p, k);
@@ -616,6 +629,11 @@ __global__ void __launch_bounds__(kMaxBlock) k_limit(KP p) {
         W(p, F_CONS + 3, i, C(p, F_CONS + 3, i) + 0.);
     }
 }
+__global__ void __launch_bounds__(kMaxBlock) k_limit(KP p) {
+    const int n_items = cell_items(p);
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n_items; idx += gridDim.x * blockDim.x)
+        limit_cell(p, cell_at(p, idx));
+}
 
 // Engine bookkeeping after a step (engine.rs:194-199, 258-268): advance the
 // device timeline to the next sync point and reset the reductions.
@@ -637,6 +655,7 @@ __global__ void k_end(KP p) {
     tl->min_timebin = 127;
     tl->active_faces += tl->n_list;  // list mode: the list is this step's active faces
     tl->n_list = 0;
+    tl->n_clist = 0;
 }
 
 // Sets every simulation's integer time on the device (the counters stay);
@@ -684,6 +703,14 @@ inline int grid(int n, int b = kBlock) { return (n + b - 1) / b; }
 
 }  // namespace
 
+// Blocks of a cell kernel: one thread per cell, or in a hierarchical step one
+// wave of resident blocks (152 SMs x 2048 threads) striding over the cell list.
+int cell_grid(const KP& p) {
+    int g = grid(p.n, p.blk_cell);
+    int wave = 152 * 2048 / p.blk_cell;
+    return p.use_list && g > wave ? wave : g;
+}
+
 void launch_predict(const KP& p, cudaStream_t s) {
     if (p.n > 0) k_predict<<<grid(p.n, p.blk_cell), p.blk_cell, 0, s>>>(p);
 }
@@ -709,20 +736,20 @@ void launch_compact(const KP& p, cudaStream_t s) {
 }
 void launch_update(const KP& p, int do_c2p, cudaStream_t s) {
     if (p.n <= 0) return;
-    if (p.fp32 && p.flux_rows == 7) k_update<true><<<grid(p.n, p.blk_cell), p.blk_cell, 0, s>>>(p, do_c2p);
-    else k_update<false><<<grid(p.n, p.blk_cell), p.blk_cell, 0, s>>>(p, do_c2p);
+    if (p.fp32 && p.flux_rows == 7) k_update<true><<<cell_grid(p), p.blk_cell, 0, s>>>(p, do_c2p);
+    else k_update<false><<<cell_grid(p), p.blk_cell, 0, s>>>(p, do_c2p);
 }
 void launch_c2p(const KP& p, cudaStream_t s) {
     if (p.n > 0) k_c2p<<<grid(p.n, p.blk_cell), p.blk_cell, 0, s>>>(p);
 }
 void launch_gradients(const KP& p, int do_timestep, cudaStream_t s) {
-    if (p.n > 0) k_gradients<<<grid(p.n, p.blk_cell), p.blk_cell, 0, s>>>(p, do_timestep);
+    if (p.n > 0) k_gradients<<<cell_grid(p), p.blk_cell, 0, s>>>(p, do_timestep);
 }
 void launch_timesteps(const KP& p, double* dt_out, cudaStream_t s) {
     if (p.n > 0) k_timesteps<<<grid(p.n, p.blk_cell), p.blk_cell, 0, s>>>(p, dt_out);
 }
 void launch_limit(const KP& p, cudaStream_t s) {
-    if (p.n > 0) k_limit<<<grid(p.n, p.blk_cell), p.blk_cell, 0, s>>>(p);
+    if (p.n > 0) k_limit<<<cell_grid(p), p.blk_cell, 0, s>>>(p);
 }
 void launch_end(const KP& p, cudaStream_t s) { k_end<<<(p.n_inst + 127) / 128, 128, 0, s>>>(p); }
 void launch_set_time(const KP& p, unsigned long long ti_current, unsigned long long ti_old, cudaStream_t s) {

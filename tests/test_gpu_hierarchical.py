@@ -28,9 +28,31 @@ def test_point_blast_3d_bins(gpu_lib, riemann):
         bins_seen.update(np.unique(orc.state().timebin).tolist())
     assert gpu.active_faces == orc.active_faces
     assert len(bins_seen) >= 2, bins_seen  # the run really is hierarchical
-    errs = compare_cells(gpu.state(), orc.state(), fields=("cons", "prim", "facc", "dt"))
+    a, b = gpu.state(), orc.state()
+    errs = compare_cells(a, b, fields=("cons", "prim", "facc", "dt", "grad", "gc", "extrap"))
     assert max(errs.values()) <= 1e-10, errs
-    t0, t1 = totals(p.cells), totals(gpu.state())
+    assert np.array_equal(a.timebin, b.timebin)
+    t0, t1 = totals(p.cells), totals(a)
+    assert abs(t1[0] - t0[0]) <= 1e-13 and abs(t1[4] - t0[4]) <= 1e-12 * abs(t0[4])
+
+
+def test_point_blast_3d_bins_fp32(gpu_lib):
+    """FP32-face form with hierarchical bins: the compacted face and cell lists
+    (only active cells and their neighbours are visited after predict) give the
+    oracle's timeline, time bins and active faces, and the density within 1e-5 L1."""
+    p = ics.point_blast_3d(8, riemann=ics.HLLC, sync_all=False, t_end=0.05)
+    orc = O.OracleSim(p)
+    gpu = G.GpuSim(p, precision=1)
+    for _ in range(40):
+        orc.step()
+        gpu.step()
+        assert gpu.ti_current == orc.ti_current
+    a, b = gpu.state(), orc.state()
+    assert gpu.active_faces == orc.active_faces
+    assert np.array_equal(a.timebin, b.timebin)
+    l1 = np.abs(a.prim[0] - b.prim[0]).sum() / np.abs(b.prim[0]).sum()
+    assert l1 <= 1e-5, l1
+    t0, t1 = totals(p.cells), totals(a)
     assert abs(t1[0] - t0[0]) <= 1e-13 and abs(t1[4] - t0[4]) <= 1e-12 * abs(t0[4])
 
 
