@@ -67,6 +67,7 @@ struct mvmm_ctx {
     double* inst_tbi = nullptr;
     uint8_t* face_act = nullptr;
     unsigned int* touch = nullptr;
+    uint8_t* fresh = nullptr;
     int* cell_list = nullptr;
     int* face_list = nullptr;
     int blk_face = 128, blk_cell = 128;
@@ -151,6 +152,7 @@ KP make_kp(mvmm_ctx* c, int stage, int flux_rows) {
     p.use_list = (!stage && !c->prm.sync_all && c->n_inst == 1) ? 1 : 0;
     p.face_act = c->face_act;
     p.touch = c->touch;
+    p.fresh = c->fresh;
     p.cell_list = c->cell_list;
     p.face_list = c->face_list;
     p.blk_face = c->blk_face;
@@ -389,6 +391,7 @@ static int create_impl(const mvmm_params* prm, const mvmm_mesh* m, int64_t n_ins
     ALLOC(c->dtmp, n * 8);
     ALLOC(c->face_act, nf);
     ALLOC(c->touch, n * 4);
+    ALLOC(c->fresh, n);
     ALLOC(c->cell_list, n * 4);
     ALLOC(c->face_list, nf * 4);
     ALLOC(c->tl, sizeof(DevTimeline) * c->n_inst);
@@ -422,6 +425,7 @@ static int create_impl(const mvmm_params* prm, const mvmm_mesh* m, int64_t n_ins
     cudaMemsetAsync(c->flux, 0, 10 * nf * 8, s);
     cudaMemsetAsync(c->face_act, 0, nf, s);
     cudaMemsetAsync(c->touch, 0, n * 4, s);
+    cudaMemsetAsync(c->fresh, 0, n, s);
     std::memset(c->tl_host, 0, sizeof(DevTimeline) * c->n_inst);
     for (int k = 0; k < c->n_inst; k++) {
         c->tl_host[k].min_dti = kMax;
@@ -483,7 +487,7 @@ int mvmm_ctx_destroy(mvmm_ctx* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->step_exec) cudaGraphExecDestroy(c->step_exec);
     void* ptrs[] = {c->left, c->right, c->csr_off, c->csr_face, c->area, c->normal, c->fcen, c->shift, c->cd,
-                    c->cf, c->timebin, c->tb_tmp, c->active, c->flux, c->flux32, c->geo, c->dtmp, c->face_act, c->touch, c->cell_list,
+                    c->cf, c->timebin, c->tb_tmp, c->active, c->flux, c->flux32, c->geo, c->dtmp, c->face_act, c->touch, c->cell_list, c->fresh,
                     c->face_list, c->tl,
                     c->inst, c->inst_tb, c->inst_tbi};
     for (void* p : ptrs)
@@ -574,8 +578,16 @@ int copy_cells(mvmm_ctx* c, const mvmm_cells* h, unsigned subset, bool timebin, 
     }
     return MVMM_OK;
 }
+// The cell state changed outside a step: every cell's derived face-stage rows
+// are recomputed by the next predict.
+int mark_stale(mvmm_ctx* c, cudaStream_t s) {
+    CUDA_TRY(cudaMemsetAsync(c->fresh, 0, c->n, s));
+    return MVMM_OK;
+}
 // positions and centroids may have changed: refresh the FP32 face geometry
 int refresh_geometry(mvmm_ctx* c, cudaStream_t s) {
+    int rc = mark_stale(c, s);
+    if (rc) return rc;
     if (c->prm.precision == MVMM_PRECISION_FP32FACE) {
         launch_geom32(make_kp(c, 0, 7), s);
         CUDA_TRY(cudaGetLastError());
@@ -639,11 +651,13 @@ int mvmm_step_cells(mvmm_ctx* c, const mvmm_cells* in, mvmm_cells* out, uint64_t
 static int upload_mask(mvmm_ctx* c, const uint8_t* active) {
     if (!active) return fail(MVMM_E_INVALID, "null active mask");
     CUDA_TRY(cudaMemcpyAsync(c->active, active, c->n, cudaMemcpyHostToDevice, c->stream));
-    return MVMM_OK;
+    return mark_stale(c, c->stream);
 }
 
 int mvmm_predict(mvmm_ctx* c, double dt) {
     if (!c) return fail(MVMM_E_INVALID, "null context");
+    int rs = mark_stale(c, c->stream);
+    if (rs) return rs;
     KP p = make_kp(c, 1, 10);
     p.stage_dt = dt;
     launch_predict(p, c->stream);
@@ -845,6 +859,7 @@ int mvmm_autotune(mvmm_ctx* c, int steps, int* blk_face, int* blk_cell) {
             // restore, warm once, time `steps` steps
             cudaMemcpyAsync(c->cd, save, bytes, cudaMemcpyDeviceToDevice, c->stream);
             cudaMemcpyAsync(c->timebin, save_tb, n, cudaMemcpyDeviceToDevice, c->stream);
+            mark_stale(c, c->stream);
             std::copy(tl0.begin(), tl0.end(), c->tl_host);
             write_tl(c);
             rc = enqueue_steps_impl(c, 1);
@@ -870,6 +885,7 @@ int mvmm_autotune(mvmm_ctx* c, int steps, int* blk_face, int* blk_cell) {
     }
     cudaMemcpyAsync(c->cd, save, bytes, cudaMemcpyDeviceToDevice, c->stream);
     cudaMemcpyAsync(c->timebin, save_tb, n, cudaMemcpyDeviceToDevice, c->stream);
+    mark_stale(c, c->stream);
     std::copy(tl0.begin(), tl0.end(), c->tl_host);
     write_tl(c);
     cudaStreamSynchronize(c->stream);

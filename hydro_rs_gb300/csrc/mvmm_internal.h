@@ -142,6 +142,7 @@ struct KP {
     int use_list;            // 1: face kernel walks the compacted active-face list
     uint8_t* face_act;       // per-face flag of this step's active-face rule
     unsigned int* touch;     // hierarchical steps: 1 for cells on this step's cell list
+    uint8_t* fresh;          // 1: the cell's derived face-stage rows match its prim, grad and v_rel
     int* cell_list;          // hierarchical steps: active cells and the cells next to an active face
     int* face_list;          // compacted active faces
 };

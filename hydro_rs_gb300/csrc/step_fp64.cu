@@ -55,23 +55,33 @@ __global__ void __launch_bounds__(kMaxBlock) k_predict(KP p) {
             act = p.timebin[i] <= get_max_active_bin(tc);
             p.active[i] = act;
         }
-        St<double> prim = C5(p, F_PRIM, i);
-        double rho_inv = 1. / prim.q[0];
-        St<double> src = extrap_source(p, i, prim, rho_inv);
-        if (prim.q[0] > 0.) {
+        if (!p.stage && p.fresh[i]) {
+            // prim, grad and v_rel are unchanged since this cell's source row was
+            // written (it was not active, nothing was uploaded): the same bits
             St<double> ex = C5(p, F_EXTRAP, i);
-            W5(p, F_EXTRAP, i, ex + (-dt) * src);
+            if (C(p, F_PRIM, i) > 0.) W5(p, F_EXTRAP, i, ex + (-dt) * C5(p, F_SRC, i));
+            else W5(p, F_EXTRAP, i, ex + st_zero<double>());
         } else {
-            St<double> ex = C5(p, F_EXTRAP, i);
-            W5(p, F_EXTRAP, i, ex + st_zero<double>());
+            St<double> prim = C5(p, F_PRIM, i);
+            double rho_inv = 1. / prim.q[0];
+            St<double> src = extrap_source(p, i, prim, rho_inv);
+            if (prim.q[0] > 0.) {
+                St<double> ex = C5(p, F_EXTRAP, i);
+                W5(p, F_EXTRAP, i, ex + (-dt) * src);
+            } else {
+                St<double> ex = C5(p, F_EXTRAP, i);
+                W5(p, F_EXTRAP, i, ex + st_zero<double>());
+            }
+            St<double> chk = prim;
+            check_physical(chk);
+            bool reset = chk.q[0] != prim.q[0] || chk.q[4] != prim.q[4] || chk.q[1] != prim.q[1] ||
+                         chk.q[2] != prim.q[2] || chk.q[3] != prim.q[3];
+            if (reset) W5(p, F_PRIM, i, chk);
+            // volume: dvdt is zero for a fixed mesh, so volume.clamp(..) leaves it unchanged
+            write_derived(p, i, chk, src, rho_inv);
+            // a reset prim no longer matches the source row (computed from the old one)
+            if (!p.stage) p.fresh[i] = !reset;
         }
-        St<double> chk = prim;
-        check_physical(chk);
-        bool reset = chk.q[0] != prim.q[0] || chk.q[4] != prim.q[4] || chk.q[1] != prim.q[1] ||
-                     chk.q[2] != prim.q[2] || chk.q[3] != prim.q[3];
-        if (reset) W5(p, F_PRIM, i, chk);
-        // volume: dvdt is zero for a fixed mesh, so volume.clamp(..) leaves it unchanged
-        write_derived(p, i, chk, src, rho_inv);
     }
     if (!p.stage) inst_count(p, k, act, CNT_CELLS);
     if (p.use_list) list_cell_warp(p, act, i);
@@ -391,6 +401,7 @@ __device__ __forceinline__ void update_cell(const KP& p, int i, int do_c2p) {
     }
     unsigned int err = 0;
     if (act) {
+        p.fresh[i] = 0;  // prim (here), grad and v_rel (gradient stage) change
         St<double> cons = C5(p, F_CONS, i) + facc;
         if (!isfinite(cons.q[0]) || !isfinite(cons.q[1]) || !isfinite(cons.q[2]) || !isfinite(cons.q[3]) ||
             !isfinite(cons.q[4]))
