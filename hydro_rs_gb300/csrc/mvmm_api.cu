@@ -65,7 +65,7 @@ struct mvmm_ctx {
     int* inst = nullptr;       // per-cell instance (batches only)
     double* inst_tb = nullptr;  // per-instance time_base, 1/time_base (batches only)
     double* inst_tbi = nullptr;
-    uint8_t* face_act = nullptr;
+    unsigned int* face_stamp = nullptr;
     unsigned int* touch = nullptr;
     uint8_t* fresh = nullptr;
     int* cell_list = nullptr;
@@ -150,7 +150,7 @@ KP make_kp(mvmm_ctx* c, int stage, int flux_rows) {
     // hierarchical steps of a single simulation walk a compacted active-face
     // list; synchronised steps, batches and per-stage calls sweep all faces
     p.use_list = (!stage && !c->prm.sync_all && c->n_inst == 1) ? 1 : 0;
-    p.face_act = c->face_act;
+    p.face_stamp = c->face_stamp;
     p.touch = c->touch;
     p.fresh = c->fresh;
     p.cell_list = c->cell_list;
@@ -389,7 +389,7 @@ static int create_impl(const mvmm_params* prm, const mvmm_mesh* m, int64_t n_ins
     ALLOC(c->active, n);
     ALLOC(c->flux, 10 * nf * 8);
     ALLOC(c->dtmp, n * 8);
-    ALLOC(c->face_act, nf);
+    ALLOC(c->face_stamp, nf * 4);
     ALLOC(c->touch, n * 4);
     ALLOC(c->fresh, n);
     ALLOC(c->cell_list, n * 4);
@@ -423,7 +423,7 @@ static int create_impl(const mvmm_params* prm, const mvmm_mesh* m, int64_t n_ins
     cudaMemsetAsync(c->tb_tmp, 0, n, s);
     cudaMemsetAsync(c->active, 0, n, s);
     cudaMemsetAsync(c->flux, 0, 10 * nf * 8, s);
-    cudaMemsetAsync(c->face_act, 0, nf, s);
+    cudaMemsetAsync(c->face_stamp, 0, nf * 4, s);
     cudaMemsetAsync(c->touch, 0, n * 4, s);
     cudaMemsetAsync(c->fresh, 0, n, s);
     std::memset(c->tl_host, 0, sizeof(DevTimeline) * c->n_inst);
@@ -487,7 +487,7 @@ int mvmm_ctx_destroy(mvmm_ctx* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->step_exec) cudaGraphExecDestroy(c->step_exec);
     void* ptrs[] = {c->left, c->right, c->csr_off, c->csr_face, c->area, c->normal, c->fcen, c->shift, c->cd,
-                    c->cf, c->timebin, c->tb_tmp, c->active, c->flux, c->flux32, c->geo, c->dtmp, c->face_act, c->touch, c->cell_list, c->fresh,
+                    c->cf, c->timebin, c->tb_tmp, c->active, c->flux, c->flux32, c->geo, c->dtmp, c->face_stamp, c->touch, c->cell_list, c->fresh,
                     c->face_list, c->tl,
                     c->inst, c->inst_tb, c->inst_tbi};
     for (void* p : ptrs)
@@ -860,6 +860,8 @@ int mvmm_autotune(mvmm_ctx* c, int steps, int* blk_face, int* blk_cell) {
             cudaMemcpyAsync(c->cd, save, bytes, cudaMemcpyDeviceToDevice, c->stream);
             cudaMemcpyAsync(c->timebin, save_tb, n, cudaMemcpyDeviceToDevice, c->stream);
             mark_stale(c, c->stream);
+            // the restored step counter repeats: clear the face stamps it keys
+            cudaMemsetAsync(c->face_stamp, 0, (size_t)(c->nf > 0 ? c->nf : 1) * 4, c->stream);
             std::copy(tl0.begin(), tl0.end(), c->tl_host);
             write_tl(c);
             rc = enqueue_steps_impl(c, 1);
@@ -886,6 +888,7 @@ int mvmm_autotune(mvmm_ctx* c, int steps, int* blk_face, int* blk_cell) {
     cudaMemcpyAsync(c->cd, save, bytes, cudaMemcpyDeviceToDevice, c->stream);
     cudaMemcpyAsync(c->timebin, save_tb, n, cudaMemcpyDeviceToDevice, c->stream);
     mark_stale(c, c->stream);
+    cudaMemsetAsync(c->face_stamp, 0, (size_t)(c->nf > 0 ? c->nf : 1) * 4, c->stream);
     std::copy(tl0.begin(), tl0.end(), c->tl_host);
     write_tl(c);
     cudaStreamSynchronize(c->stream);

@@ -61,17 +61,23 @@ __device__ __forceinline__ void set_err(const KP& p, int k, unsigned int bits) {
 __device__ __forceinline__ int cell_items(const KP& p) { return p.use_list ? (int)p.tl[0].n_clist : p.n; }
 __device__ __forceinline__ int cell_at(const KP& p, int idx) { return p.use_list ? p.cell_list[idx] : idx; }
 // Puts cell i on this step's cell list once (want: the lane has a candidate);
-// aggregated over the warp.  Every lane of the warp calls it.
-__device__ __forceinline__ void list_cell_warp(const KP& p, bool want, int i) {
+// aggregated over the warp.  Every lane of the warp calls it.  The active
+// cells (predict) come first and are also counted in n_alist.
+__device__ __forceinline__ void list_cell_warp(const KP& p, bool want, int i, bool active_cells = false) {
     want = want && atomicExch(&p.touch[i], 1u) == 0u;
     unsigned int b = __ballot_sync(0xffffffffu, want);
     if (!b) return;
     int lane = threadIdx.x & 31, leader = __ffs(b) - 1;
     unsigned int start = 0;
-    if (lane == leader) start = atomicAdd(&p.tl[0].n_clist, (unsigned int)__popc(b));
+    if (lane == leader) {
+        start = atomicAdd(&p.tl[0].n_clist, (unsigned int)__popc(b));
+        if (active_cells) atomicAdd(&p.tl[0].n_alist, (unsigned int)__popc(b));
+    }
     start = __shfl_sync(0xffffffffu, start, leader);
     if (want) p.cell_list[start + __popc(b & ((1u << lane) - 1u))] = i;
 }
+// The stamp of faces active in this step (hierarchical steps, one simulation).
+__device__ __forceinline__ unsigned int face_stamp_now(const KP& p) { return (unsigned int)p.tl[0].steps + 1u; }
 
 // Counter add per instance, aggregated over the lanes of a warp that share an
 // instance (k < 0: the lane contributes nothing).  Every lane of the warp calls it.

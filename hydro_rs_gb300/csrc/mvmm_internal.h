@@ -83,7 +83,7 @@ struct DevTimeline {
     int min_timebin;                  // reduction target of timestep_sync
     int done;                         // 1 once the step at t_end has run
     unsigned int err;                 // MVMM_ERR_* bits
-    unsigned int pad;
+    unsigned int n_alist;             // hierarchical steps: the first n_alist cells of the list are active
     unsigned long long steps;
     unsigned long long active_faces;  // cumulative faces that reached flux_exchange*
     unsigned long long active_cells;
@@ -140,7 +140,7 @@ struct KP {
     RSx rsx;                 // Riemann solver kind and its settings
     int godunov;             // 1: GodunovHydroRunner (no gradients), 0: OptimalOrderRunner
     int use_list;            // 1: face kernel walks the compacted active-face list
-    uint8_t* face_act;       // per-face flag of this step's active-face rule
+    unsigned int* face_stamp;  // hierarchical steps: steps + 1 for faces active in this step
     unsigned int* touch;     // hierarchical steps: 1 for cells on this step's cell list
     uint8_t* fresh;          // 1: the cell's derived face-stage rows match its prim, grad and v_rel
     int* cell_list;          // hierarchical steps: active cells and the cells next to an active face

@@ -84,7 +84,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_predict(KP p) {
         }
     }
     if (!p.stage) inst_count(p, k, act, CNT_CELLS);
-    if (p.use_list) list_cell_warp(p, act, i);
+    if (p.use_list) list_cell_warp(p, act, i, true);
 }
 
 // Recomputes the derived face-stage fields (per-stage flux calls).
@@ -265,41 +265,54 @@ __global__ void __launch_bounds__(kMaxBlock) k_face_flux(KP p) {
     }
 }
 
-// Per-time-bin active-face list (hierarchical steps): applies the active-face
-// rule of compute_fluxes (euler_eqns_fvs.rs:35-45) to every face, flags it and
-// appends the active ones to a list with warp-aggregated atomics.  The list
-// order is arbitrary; each face writes only its own result rows, so results do
-// not depend on it.
+// Per-time-bin active-face list (hierarchical steps): walks the faces of the
+// active cells (the head of the cell list, written by predict), applies the
+// active-face rule of compute_fluxes (euler_eqns_fvs.rs:35-45), stamps each
+// active face once and appends it to the face list, and puts the other cell of
+// every face of an active cell on the cell list (its update and wake-up).  The
+// work is O(faces of active cells); list orders are arbitrary, and each face
+// writes only its own result rows, so results do not depend on them.
 __global__ void __launch_bounds__(kMaxBlock) k_compact(KP p) {
     if (p.tl[0].done) return;
-    int f = blockIdx.x * blockDim.x + threadIdx.x;
-    bool act = false, any = false;
-    if (f < p.nf) {
-        int l = p.left[f], r = p.right[f];
-        bool la = p.active[l] != 0;
-        any = la;
-        if (r >= 0) {
-            bool ra = p.active[r] != 0;
-            any = la || ra;
-            double dtl = C(p, F_DT, l), dtr = C(p, F_DT, r);
-            act = !((!la && !ra) || (dtr < dtl && !ra) || (dtl < dtr && !la));
-        } else {
-            act = la;
+    const int n_act = (int)p.tl[0].n_alist;
+    const unsigned int stamp = face_stamp_now(p);
+    const int lane = threadIdx.x & 31;
+    for (int base = blockIdx.x * blockDim.x; base < n_act; base += gridDim.x * blockDim.x) {
+        int idx = base + threadIdx.x;
+        int i = idx < n_act ? p.cell_list[idx] : -1;
+        int k0 = i >= 0 ? p.csr_off[i] : 0;
+        int deg = i >= 0 ? p.csr_off[i + 1] - k0 : 0;
+        int max_deg = __reduce_max_sync(0xffffffffu, deg);  // warp-uniform trip count
+        for (int j = 0; j < max_deg; j++) {
+            bool have = j < deg;
+            int f = have ? p.csr_face[k0 + j] : 0;
+            int o = -1;
+            bool act = false;
+            if (have) {
+                int l = p.left[f], r = p.right[f];
+                o = l == i ? r : l;
+                bool la = p.active[l] != 0;
+                if (r >= 0) {
+                    bool ra = p.active[r] != 0;
+                    double dtl = C(p, F_DT, l), dtr = C(p, F_DT, r);
+                    act = !((!la && !ra) || (dtr < dtl && !ra) || (dtl < dtr && !la));
+                } else {
+                    act = la;
+                }
+            }
+            // a face between two active cells is reached twice: the stamp lists it once
+            bool first = act && atomicExch(&p.face_stamp[f], stamp) != stamp;
+            unsigned int b = __ballot_sync(0xffffffffu, first);
+            if (b) {
+                int leader = __ffs(b) - 1;
+                unsigned int start = 0;
+                if (lane == leader) start = atomicAdd(&p.tl[0].n_list, (unsigned int)__popc(b));
+                start = __shfl_sync(0xffffffffu, start, leader);
+                if (first) p.face_list[start + __popc(b & ((1u << lane) - 1u))] = f;
+            }
+            list_cell_warp(p, o >= 0, o >= 0 ? o : 0);
         }
-        p.face_act[f] = act;
     }
-    // both cells of every face with an active side join the cell list: the
-    // faces of active cells, their neighbours' updates and wake-ups
-    list_cell_warp(p, any, f < p.nf ? p.left[f] : 0);
-    list_cell_warp(p, any && p.right[f < p.nf ? f : 0] >= 0, f < p.nf ? p.right[f] : 0);
-    unsigned int b = __ballot_sync(0xffffffffu, act);
-    if (!b) return;
-    int lane = threadIdx.x & 31;
-    int leader = __ffs(b) - 1;
-    unsigned int start = 0;
-    if (lane == leader) start = atomicAdd(&p.tl[0].n_list, (unsigned int)__popc(b));
-    start = __shfl_sync(0xffffffffu, start, leader);
-    if (act) p.face_list[start + __popc(b & ((1u << lane) - 1u))] = f;
 }
 
 // ---------------------------------------------------- cons -> primitive --
@@ -360,6 +373,7 @@ __device__ __forceinline__ void update_cell(const KP& p, int i, int do_c2p) {
     double msv = C(p, F_MSV, i), maor = C(p, F_MAOR, i);
     const size_t nf = (size_t)p.nf;
     int k0 = p.csr_off[i], k1 = p.csr_off[i + 1];
+    const unsigned int stamp = p.use_list ? face_stamp_now(p) : 0u;
     if (ROWS32) {
         const float* fl = p.flux32;
         Sum2 acc[5];
@@ -368,7 +382,7 @@ __device__ __forceinline__ void update_cell(const KP& p, int i, int do_c2p) {
         float vm = -INFINITY, ar = -INFINITY;
         for (int k = k0; k < k1; k++) {
             int f = p.csr_face[k];
-            if (p.use_list && !p.face_act[f]) continue;
+            if (p.use_list && p.face_stamp[f] != stamp) continue;
             float sg = p.left[f] == i ? -1.f : 1.f;  // update_fluxes_left / _right (part.rs:160-176)
 #pragma unroll
             for (int q = 0; q < 5; q++) sum2_add(acc[q], sg * fl[q * nf + f]);
@@ -387,7 +401,7 @@ __device__ __forceinline__ void update_cell(const KP& p, int i, int do_c2p) {
         for (int k = k0; k < k1; k++) {
             int f = p.csr_face[k];
             // an inactive face carries FluxInfo::zero(): adding it changes nothing
-            if (p.use_list && !p.face_act[f]) continue;
+            if (p.use_list && p.face_stamp[f] != stamp) continue;
             St<double> x;
 #pragma unroll
             for (int q = 0; q < 5; q++) x.q[q] = fl[q * nf + f];
@@ -667,6 +681,7 @@ __global__ void k_end(KP p) {
     tl->active_faces += tl->n_list;  // list mode: the list is this step's active faces
     tl->n_list = 0;
     tl->n_clist = 0;
+    tl->n_alist = 0;
 }
 
 // Sets every simulation's integer time on the device (the counters stay);
@@ -743,7 +758,7 @@ void launch_face_flux_fp64(const KP& p, int solver, cudaStream_t s) {
     else k_face_flux<SOLVER_EXTRA><<<g, p.blk_face, 0, s>>>(p);
 }
 void launch_compact(const KP& p, cudaStream_t s) {
-    if (p.nf > 0) k_compact<<<grid(p.nf, p.blk_cell), p.blk_cell, 0, s>>>(p);
+    if (p.nf > 0) k_compact<<<cell_grid(p), p.blk_cell, 0, s>>>(p);
 }
 void launch_update(const KP& p, int do_c2p, cudaStream_t s) {
     if (p.n <= 0) return;
