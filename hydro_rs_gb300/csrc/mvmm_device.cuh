@@ -1051,6 +1051,14 @@ __host__ __device__ __forceinline__ int get_max_active_bin(uint64_t ti) {  // :7
     while (((1ull << ((bin + 1) & 63)) & ti) == 0) bin += 1;
     return bin;
 }
+// get_max_active_bin without the bit loop: the lowest set bit p >= 2 gives
+// bin p - 1; with only bits 0/1 set the loop's shift wraps at bin 63.
+__device__ __forceinline__ int max_active_bin_bits(uint64_t ti) {
+    if (ti == 0) return NUM_TIME_BINS;
+    uint64_t hi = ti & ~3ull;
+    if (hi) return __ffsll((long long)hi) - 2;
+    return (ti & 1ull) ? 63 : 64;
+}
 __device__ __forceinline__ uint64_t sat_u64(double x) {  // Rust `f64 as u64`
     if (!(x > 0.)) return 0;
     if (x >= 18446744073709551616.0) return ~0ull;

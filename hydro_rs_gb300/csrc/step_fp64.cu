@@ -52,7 +52,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_predict(KP p) {
         } else {
             unsigned long long tc = p.tl[k].ti_current, to = p.tl[k].ti_old;
             dt = (double)(tc - to) * tbase(p, k);  // TimestepInfo::dt_from_dti
-            act = p.timebin[i] <= get_max_active_bin(tc);
+            act = p.timebin[i] <= max_active_bin_bits(tc);
             p.active[i] = act;
         }
         if (!p.stage && p.fresh[i]) {
@@ -83,8 +83,10 @@ __global__ void __launch_bounds__(kMaxBlock) k_predict(KP p) {
             if (!p.stage) p.fresh[i] = !reset;
         }
     }
-    if (!p.stage) inst_count(p, k, act, CNT_CELLS);
+    // active cells: counted per warp, or in a hierarchical step as the length
+    // of the list's active head (added by k_end)
     if (p.use_list) list_cell_warp(p, act, i, true);
+    else if (!p.stage) inst_count(p, k, act, CNT_CELLS);
 }
 
 // Recomputes the derived face-stage fields (per-stage flux calls).
@@ -680,6 +682,7 @@ __global__ void k_end(KP p) {
     tl->min_timebin = 127;
     tl->active_faces += tl->n_list;  // list mode: the list is this step's active faces
     tl->n_list = 0;
+    tl->active_cells += tl->n_alist;  // list mode: the active head of the cell list
     tl->n_clist = 0;
     tl->n_alist = 0;
 }
@@ -729,11 +732,12 @@ inline int grid(int n, int b = kBlock) { return (n + b - 1) / b; }
 
 }  // namespace
 
-// Blocks of a cell kernel: one thread per cell, or in a hierarchical step one
-// wave of resident blocks (152 SMs x 2048 threads) striding over the cell list.
+// Blocks of a cell kernel: one thread per cell, or in a hierarchical step half
+// a wave of resident blocks (152 SMs x 1024 threads) striding over the cell
+// list, whose length is known on the device only.
 int cell_grid(const KP& p) {
     int g = grid(p.n, p.blk_cell);
-    int wave = 152 * 2048 / p.blk_cell;
+    int wave = 152 * 1024 / p.blk_cell;
     return p.use_list && g > wave ? wave : g;
 }
 

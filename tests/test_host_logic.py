@@ -95,3 +95,20 @@ def test_negative_energy_is_reported():
     s2 = O.OracleSim(ics.Problem(p.name, p.params, p.mesh, c))
     s2.convert(np.ones(32, np.uint8))
     assert s2.error() & (1 << 3)
+
+
+def test_max_active_bin_closed_form():
+    """The kernels' get_max_active_bin without the bit loop (max_active_bin_bits):
+    lowest set bit p >= 2 gives p - 1, else the loop's wrapped shift gives 63 / 64."""
+    def closed(ti):
+        if ti == 0:
+            return 56
+        hi = ti & ~3
+        if hi:
+            return (hi & -hi).bit_length() - 1 - 1
+        return 63 if ti & 1 else 64
+    rng = np.random.default_rng(0)
+    cases = [0, 1, 2, 3, 4, 5, 6, 8, 12, 1 << 57, (1 << 57) - 4, (1 << 63), (1 << 64) - 1]
+    cases += [int(x) << int(s) for x, s in zip(rng.integers(1, 1 << 20, 300), rng.integers(0, 44, 300))]
+    for ti in cases:
+        assert closed(ti) == O.get_max_active_bin(ti), ti
