@@ -66,6 +66,11 @@ struct mvmm_ctx {
     double* inst_tb = nullptr;  // per-instance time_base, 1/time_base (batches only)
     double* inst_tbi = nullptr;
     unsigned int* face_stamp = nullptr;
+    // moving meshes: face capacity, pending geometry of the rebuilt cells
+    int nf_cap = 0;
+    int64_t ncsr_cap = 0;
+    double *pend_vol = nullptr, *pend_cen = nullptr;
+    bool pending_geometry = false;
     unsigned int* touch = nullptr;
     uint8_t* fresh = nullptr;
     int* cell_list = nullptr;
@@ -169,6 +174,10 @@ KP make_kp(mvmm_ctx* c, int stage, int flux_rows) {
     p.gk.rm = g.rm;
     // a stage call to mvmm_gradients always estimates gradients
     p.godunov = (!stage && c->prm.runner == MVMM_RUNNER_GODUNOV) ? 1 : 0;
+    p.motion = c->prm.particle_motion;
+    for (int a = 0; a < 3; a++) p.box[a] = c->prm.box_size[a];
+    p.new_vol = c->pend_vol;
+    p.new_cen = c->pend_cen;
     return p;
 }
 
@@ -189,6 +198,9 @@ void enqueue_step_kernels(mvmm_ctx* c, bool with_events, cudaEvent_t before_upda
     cudaStream_t s = c->stream;
     if (with_events) cudaEventRecord(c->ev[0], s);
     launch_predict(p, s);
+    if (c->pending_geometry) launch_geometry(p, s);  // after predict, as volume_calculation
+    if (c->prm.particle_motion != MVMM_MOTION_FIXED && c->prm.precision == MVMM_PRECISION_FP32FACE)
+        launch_geom32(p, s);  // generators drifted, centroids updated
     if (p.use_list) launch_compact(p, s);
     if (with_events) cudaEventRecord(c->ev[1], s);
     launch_face(c, p);
@@ -229,6 +241,15 @@ int enqueue_steps_impl(mvmm_ctx* c, int64_t n) {
                 c->prof_ms[j] += ms;
                 c->prof_n[j] += 1;
             }
+        }
+        CUDA_TRY(cudaGetLastError());
+        return MVMM_OK;
+    }
+    if (c->prm.particle_motion != MVMM_MOTION_FIXED) {
+        // the mesh changes between steps: direct launches, the pending geometry once
+        for (int64_t k = 0; k < n; k++) {
+            enqueue_step_kernels(c, false);
+            c->pending_geometry = false;
         }
         CUDA_TRY(cudaGetLastError());
         return MVMM_OK;
@@ -330,8 +351,15 @@ static int create_impl(const mvmm_params* prm, const mvmm_mesh* m, int64_t n_ins
     if (prm->boundary < 0 || prm->boundary > 3) return fail(MVMM_E_INVALID, "unknown boundary");
     if (prm->precision < 0 || prm->precision > 1) return fail(MVMM_E_INVALID, "unknown precision");
     if (prm->eos < 0 || prm->eos > 1) return fail(MVMM_E_INVALID, "unknown equation of state");
-    if (prm->particle_motion != MVMM_MOTION_FIXED)
-        return fail(MVMM_E_UNSUPPORTED, "only fixed particle motion runs on the device");
+    if (prm->particle_motion < MVMM_MOTION_FIXED || prm->particle_motion > MVMM_MOTION_FLUID)
+        return fail(MVMM_E_INVALID, "unknown particle motion");
+    if (prm->particle_motion != MVMM_MOTION_FIXED) {
+        if (prm->boundary != MVMM_BOUNDARY_PERIODIC)
+            return fail(MVMM_E_UNSUPPORTED, "moving meshes need a periodic box (walls reflect or remove generators)");
+        if (n_inst > 1) return fail(MVMM_E_UNSUPPORTED, "moving meshes are stepped one simulation at a time");
+        for (int a = 0; a < prm->dimensionality; a++)
+            if (!(prm->box_size[a] > 0.)) return fail(MVMM_E_INVALID, "moving meshes need box_size > 0");
+    }
     if (!(prm->t_end > 0.0)) return fail(MVMM_E_INVALID, "t_end must be > 0");
     int rc = check_mesh(m, prm->boundary);
     if (rc) return rc;
@@ -379,6 +407,12 @@ static int create_impl(const mvmm_params* prm, const mvmm_mesh* m, int64_t n_ins
     ALLOC(c->csr_off, (n + 1) * 4);
     ALLOC(c->csr_face, (c->ncsr > 0 ? c->ncsr : 1) * 4);
     ALLOC(c->cd, (size_t)kCellFields * n * 8);
+    c->nf_cap = (int)nf;
+    c->ncsr_cap = c->ncsr > 0 ? c->ncsr : 1;
+    if (prm->particle_motion != MVMM_MOTION_FIXED) {
+        ALLOC(c->pend_vol, n * 8);
+        ALLOC(c->pend_cen, 3 * n * 8);
+    }
     if (prm->precision == MVMM_PRECISION_FP32FACE) {
         ALLOC(c->cf, (size_t)kCellFields32 * n * 4);
         ALLOC(c->flux32, 7 * nf * 4);
@@ -488,6 +522,7 @@ int mvmm_ctx_destroy(mvmm_ctx* c) {
     if (c->step_exec) cudaGraphExecDestroy(c->step_exec);
     void* ptrs[] = {c->left, c->right, c->csr_off, c->csr_face, c->area, c->normal, c->fcen, c->shift, c->cd,
                     c->cf, c->timebin, c->tb_tmp, c->active, c->flux, c->flux32, c->geo, c->dtmp, c->face_stamp, c->touch, c->cell_list, c->fresh,
+                    c->pend_vol, c->pend_cen,
                     c->face_list, c->tl,
                     c->inst, c->inst_tb, c->inst_tbi};
     for (void* p : ptrs)
@@ -617,6 +652,8 @@ int mvmm_step_cells(mvmm_ctx* c, const mvmm_cells* in, mvmm_cells* out, uint64_t
                     uint64_t* ti_next, int64_t* n_active_faces) {
     if (!c || !in || !out) return fail(MVMM_E_INVALID, "null argument");
     if (c->n_inst != 1) return fail(MVMM_E_UNSUPPORTED, "mvmm_step_cells steps a single simulation");
+    if (c->prm.particle_motion != MVMM_MOTION_FIXED)
+        return fail(MVMM_E_UNSUPPORTED, "mvmm_step_cells steps a fixed mesh");
     if (!c->side) {
         CUDA_TRY(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
         for (cudaEvent_t* e : {&c->ev_in, &c->ev_upd, &c->ev_out})
@@ -779,14 +816,100 @@ int mvmm_step(mvmm_ctx* c, uint64_t ti_current, uint64_t ti_old, uint64_t* ti_ne
     return rc;
 }
 
+static int reject_moving(mvmm_ctx* c) {
+    if (c->prm.particle_motion != MVMM_MOTION_FIXED)
+        return fail(MVMM_E_UNSUPPORTED, "a moving mesh is stepped from the host: mvmm_drift, mvmm_set_mesh, mvmm_step");
+    return MVMM_OK;
+}
+
 int mvmm_enqueue_steps(mvmm_ctx* c, int64_t n_steps) {
     if (!c) return fail(MVMM_E_INVALID, "null context");
+    int rc = reject_moving(c);
+    if (rc) return rc;
     return enqueue_steps_impl(c, n_steps);
+}
+
+int mvmm_drift(mvmm_ctx* c, double dt) {
+    if (!c) return fail(MVMM_E_INVALID, "null context");
+    if (c->prm.particle_motion == MVMM_MOTION_FIXED) return MVMM_OK;  // v = 0: nothing moves
+    if (!(dt >= 0.)) return fail(MVMM_E_INVALID, "drift: dt must be >= 0");
+    launch_drift(make_kp(c, 0, 7), dt, c->stream);
+    CUDA_TRY(cudaGetLastError());
+    return finish(c);
+}
+
+int mvmm_get_positions(mvmm_ctx* c, double* loc) {
+    if (!c || !loc) return fail(MVMM_E_INVALID, "null argument");
+    CUDA_TRY(cudaMemcpyAsync(loc, c->cd + (size_t)F_LOC * c->n, (size_t)3 * c->n * 8, cudaMemcpyDeviceToHost,
+                             c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return MVMM_OK;
+}
+
+int mvmm_set_mesh(mvmm_ctx* c, const mvmm_mesh* m, const double* volume, const double* centroid) {
+    if (!c || !m || !volume || !centroid) return fail(MVMM_E_INVALID, "null argument");
+    if (c->prm.particle_motion == MVMM_MOTION_FIXED)
+        return fail(MVMM_E_INVALID, "set_mesh: the context was created for a fixed mesh");
+    if (m->n_cells != c->n) return fail(MVMM_E_INVALID, "set_mesh: cell count changed");
+    int rc = check_mesh(m, c->prm.boundary);
+    if (rc) return rc;
+    cudaStream_t s = c->stream;
+    CUDA_TRY(cudaStreamSynchronize(s));
+    int nf = (int)m->n_faces;
+    int64_t ncsr = m->csr_off[m->n_cells];
+    if (nf > c->nf_cap || ncsr > c->ncsr_cap) {
+        // grow with headroom; every face-sized buffer is reallocated
+        int cap = nf > c->nf_cap ? nf + nf / 4 + 16 : c->nf_cap;
+        int64_t ccap = ncsr > c->ncsr_cap ? ncsr + ncsr / 4 + 16 : c->ncsr_cap;
+        struct Buf {
+            void** ptr;
+            size_t bytes;
+        } bufs[] = {{(void**)&c->left, (size_t)cap * 4},       {(void**)&c->right, (size_t)cap * 4},
+                    {(void**)&c->area, (size_t)cap * 8},       {(void**)&c->normal, (size_t)cap * 24},
+                    {(void**)&c->fcen, (size_t)cap * 24},      {(void**)&c->shift, (size_t)cap * 24},
+                    {(void**)&c->flux, (size_t)cap * 80},      {(void**)&c->face_stamp, (size_t)cap * 4},
+                    {(void**)&c->face_list, (size_t)cap * 4},  {(void**)&c->csr_face, (size_t)ccap * 4},
+                    {(void**)&c->flux32, c->flux32 ? (size_t)cap * 28 : 0},
+                    {(void**)&c->geo, c->geo ? (size_t)cap * 4 * kFaceGeom32 : 0}};
+        for (auto& b : bufs) {
+            if (!b.bytes) continue;
+            cudaFree(*b.ptr);
+            *b.ptr = nullptr;
+            if (cudaMalloc(b.ptr, b.bytes) != cudaSuccess) return fail(MVMM_E_NOMEM, "set_mesh: cudaMalloc failed");
+        }
+        CUDA_TRY(cudaMemsetAsync(c->face_stamp, 0, (size_t)cap * 4, s));
+        c->nf_cap = cap;
+        c->ncsr_cap = ccap;
+    }
+    // face rows are [3][nf]: the row stride changes with the face count
+    c->nf = nf;
+    c->ncsr = ncsr;
+    if (nf > 0) {
+        CUDA_TRY(cudaMemcpyAsync(c->left, m->left, (size_t)nf * 4, cudaMemcpyHostToDevice, s));
+        CUDA_TRY(cudaMemcpyAsync(c->right, m->right, (size_t)nf * 4, cudaMemcpyHostToDevice, s));
+        CUDA_TRY(cudaMemcpyAsync(c->area, m->area, (size_t)nf * 8, cudaMemcpyHostToDevice, s));
+        CUDA_TRY(cudaMemcpyAsync(c->normal, m->normal, (size_t)nf * 24, cudaMemcpyHostToDevice, s));
+        CUDA_TRY(cudaMemcpyAsync(c->fcen, m->centroid, (size_t)nf * 24, cudaMemcpyHostToDevice, s));
+        CUDA_TRY(cudaMemcpyAsync(c->shift, m->shift, (size_t)nf * 24, cudaMemcpyHostToDevice, s));
+    }
+    CUDA_TRY(cudaMemcpyAsync(c->csr_off, m->csr_off, (size_t)(c->n + 1) * 4, cudaMemcpyHostToDevice, s));
+    if (ncsr > 0) CUDA_TRY(cudaMemcpyAsync(c->csr_face, m->csr_face, (size_t)ncsr * 4, cudaMemcpyHostToDevice, s));
+    CUDA_TRY(cudaMemcpyAsync(c->pend_vol, volume, (size_t)c->n * 8, cudaMemcpyHostToDevice, s));
+    CUDA_TRY(cudaMemcpyAsync(c->pend_cen, centroid, (size_t)c->n * 24, cudaMemcpyHostToDevice, s));
+    c->pending_geometry = true;
+    if (c->step_exec) {  // kernel parameters hold the face count and pointers
+        cudaGraphExecDestroy(c->step_exec);
+        c->step_exec = nullptr;
+    }
+    CUDA_TRY(cudaStreamSynchronize(s));
+    return MVMM_OK;
 }
 
 int mvmm_run(mvmm_ctx* c, int64_t max_steps, uint64_t* ti_current, uint64_t* ti_old, int64_t* steps_done,
              int64_t* n_active_faces, int* finished) {
     if (!c || !ti_current || !ti_old) return fail(MVMM_E_INVALID, "null argument");
+    int rm = reject_moving(c);
+    if (rm) return rm;
     int rc = c->n_inst == 1 ? mvmm_set_time(c, *ti_current, *ti_old) : read_tl(c);
     if (rc) return rc;
     unsigned long long s0 = c->tl_host->steps, f0 = sum_field(c, &DevTimeline::active_faces);

@@ -141,7 +141,39 @@ __device__ __forceinline__ double radius(double volume, int dim) {
     return pow(x, 1. / 3.);
 }
 
-// Particle::timestep for fixed motion (part.rs:42-84, 328-372); returns the dt.
+// Particle::set_particle_velocity (part.rs:328-372): the velocity the
+// generator drifts with over its next timestep.
+__device__ __forceinline__ V3<double> particle_velocity(const KP& p, int i, V3<double> fluid_v, double sound_speed,
+                                                        double vol) {
+    if (p.motion == 0) return v3(0., 0., 0.);  // Fixed
+    if (p.motion == 3) return fluid_v;         // Fluid
+    V3<double> d = C3(p, F_CEN, i) - C3(p, F_LOC, i);
+    if (p.motion == 1) {  // Steer
+        double abs_d = len(d);
+        double eta = 0.25;
+        double eta_r = eta * radius(vol, p.dim);
+        double xi = 0.99;
+        if (abs_d > 0.9 * eta_r) {
+            double fac = xi * sound_speed / abs_d;
+            if (abs_d < 1.1 * eta_r) fac *= 5. * (abs_d - 0.9 * eta_r) / eta_r;
+            return fluid_v + fac * d;
+        }
+        return fluid_v;
+    }
+    // SteerPakmor
+    double alpha = 2. / (double)p.dim * C(p, F_MAOR, i);
+    double beta = 2.25;
+    double eta = m_max(0., m_min(0.5, 2. / beta * (alpha - 0.75 * beta)));
+    V3<double> dn = (1.0 / len(d)) * d;  // DVec3::normalize: d * length_recip
+    // curl of the velocity gradient (physical_quantities.rs:149-155), grad row 3q+k
+    V3<double> curl = v3(C(p, F_GRAD + 10, i) - C(p, F_GRAD + 8, i), C(p, F_GRAD + 5, i) - C(p, F_GRAD + 9, i),
+                         C(p, F_GRAD + 6, i) - C(p, F_GRAD + 4, i));
+    double v_reg = radius(vol, p.dim) * len(curl);
+    V3<double> vr = (eta * m_max(sound_speed, v_reg)) * dn;
+    return fluid_v + vr;
+}
+
+// Particle::timestep (part.rs:42-84, 328-372); returns the dt.
 __device__ __forceinline__ double particle_timestep(const KP& p, int i) {
     St<double> cons = C5(p, F_CONS, i);
     if (cons.q[0] == 0.) {
@@ -157,7 +189,8 @@ __device__ __forceinline__ double particle_timestep(const KP& p, int i) {
     double u = (cons.q[4] - 0.5 * dot(vel(cons), vel(prim))) / cons.q[0];  // Particle::internal_energy
     double vol = C(p, F_VOL, i);
     double c = g.sound_speed(g.pressure_from_internal_energy(u, prim.q[0]), vol * m_inv);
-    V3<double> v = v3(0., 0., 0.);  // ParticleMotion::Fixed
+    V3<double> v = particle_velocity(p, i, fluid_v, c, vol);
+    if (!isfinite(v.x) || !isfinite(v.y) || !isfinite(v.z)) set_err(p, inst_of(p, i), 1u << 4);  // part.rs:366
     V3<double> v_rel = fluid_v - v;
     W3(p, F_V, i, v);
     W3(p, F_VREL, i, v_rel);

@@ -139,6 +139,10 @@ struct KP {
     GasK gk;                 // gas-law constants
     RSx rsx;                 // Riemann solver kind and its settings
     int godunov;             // 1: GodunovHydroRunner (no gradients), 0: OptimalOrderRunner
+    int motion;              // MVMM_MOTION_*
+    double box[3];           // periodic box (moving meshes)
+    const double* new_vol;   // moving meshes: volume [n] and centroid [3][n] of the
+    const double* new_cen;   //   rebuilt cells, applied to active cells after predict
     int use_list;            // 1: face kernel walks the compacted active-face list
     unsigned int* face_stamp;  // hierarchical steps: steps + 1 for faces active in this step
     unsigned int* touch;     // hierarchical steps: 1 for cells on this step's cell list
@@ -160,6 +164,8 @@ void launch_compact(const KP& p, cudaStream_t s);
 void launch_end(const KP& p, cudaStream_t s);
 int cell_grid(const KP& p);
 void launch_set_time(const KP& p, unsigned long long ti_current, unsigned long long ti_old, cudaStream_t s);
+void launch_drift(const KP& p, double dt, cudaStream_t s);
+void launch_geometry(const KP& p, cudaStream_t s);
 // FP32 form helpers
 void launch_prep32(const KP& p, cudaStream_t s);
 

@@ -650,7 +650,16 @@ __device__ __forceinline__ void limit_cell(const KP& p, int i) {
     p.timebin[i] = (int8_t)tb;
     if (p.active[i]) {
         W5(p, F_EXTRAP, i, st_zero<double>());
-        // kick1: hydro_kick1 is a no-op for fixed motion; grav_kick adds +0
+        if (p.motion != 0) {
+            // Particle::hydro_kick1 (part.rs:87-104): half a kick of the particle
+            // velocity with the pressure gradient over the new timestep
+            double rho = C(p, F_PRIM, i);
+            if (rho > 0.) {
+                double kick_fac = 0.5 * C(p, F_DT, i) / rho;
+                for (int a = 0; a < p.dim; a++) W(p, F_V + a, i, C(p, F_V + a, i) - kick_fac * C(p, F_GRAD + 12 + a, i));
+            }
+        }
+        // kick1: grav_kick adds +0
         W(p, F_CONS + 1, i, C(p, F_CONS + 1, i) + 0.);
         W(p, F_CONS + 2, i, C(p, F_CONS + 2, i) + 0.);
         W(p, F_CONS + 3, i, C(p, F_CONS + 3, i) + 0.);
@@ -685,6 +694,65 @@ __global__ void k_end(KP p) {
     tl->active_cells += tl->n_alist;  // list mode: the active head of the cell list
     tl->n_clist = 0;
     tl->n_alist = 0;
+}
+
+// Space::drift (space.rs:833-854) with Particle::drift (part.rs:107-119) and,
+// for a generator that left the periodic box, Particle::box_wrap (part.rs:449-455,
+// utils.rs:23-32).
+__global__ void __launch_bounds__(kMaxBlock) k_drift(KP p, double dt) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n) return;
+    const int k = inst_of(p, i);
+    if (p.tl[k].done) return;
+    double loc[3], cen[3], gc[3];
+    for (int a = 0; a < 3; a++) {
+        loc[a] = C(p, F_LOC + a, i);
+        cen[a] = C(p, F_CEN + a, i);
+        gc[a] = C(p, F_GC + a, i);
+    }
+    for (int a = 0; a < p.dim; a++) {
+        double v = C(p, F_V + a, i);
+        loc[a] += v * dt;
+        cen[a] += v * dt;
+        gc[a] += v * dt;
+    }
+    if (!isfinite(loc[0]) || !isfinite(loc[1]) || !isfinite(loc[2])) {
+        set_err(p, k, 1u << 4);  // "Infinite x after drift!"
+    } else {
+        bool inside = true;
+        for (int a = 0; a < p.dim; a++) inside = inside && loc[a] >= 0. && loc[a] < p.box[a];
+        if (!inside) {
+            double old[3] = {loc[0], loc[1], loc[2]};
+            for (int a = 0; a < p.dim; a++) {
+                // one box length per pass, as the reference's loops (bounded: a
+                // generator moves less than a cell per step)
+                for (int it = 0; it < 64 && loc[a] < 0.; it++) loc[a] += p.box[a];
+                for (int it = 0; it < 64 && loc[a] >= p.box[a]; it++) loc[a] -= p.box[a];
+            }
+            for (int a = 0; a < 3; a++) {
+                double shift = loc[a] - old[a];
+                gc[a] += shift;
+                cen[a] += shift;
+            }
+        }
+    }
+    for (int a = 0; a < 3; a++) {
+        W(p, F_LOC + a, i, loc[a]);
+        W(p, F_CEN + a, i, cen[a]);
+        W(p, F_GC + a, i, gc[a]);
+    }
+}
+
+// Particle::update_geometry (part.rs:151-158) of the active cells with the
+// rebuilt mesh's volume and centroid (Space::volume_calculation, space.rs:236-263).
+__global__ void __launch_bounds__(kMaxBlock) k_geometry(KP p) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n || !p.active[i]) return;
+    if (p.tl[inst_of(p, i)].done) return;
+    double vol = p.new_vol[i];
+    if (!(vol >= 0.)) set_err(p, inst_of(p, i), 1u << 4);  // assert!(self.volume >= 0.)
+    W(p, F_VOL, i, vol);
+    for (int a = 0; a < 3; a++) W(p, F_CEN + a, i, p.new_cen[(size_t)a * p.n + i]);
 }
 
 // Sets every simulation's integer time on the device (the counters stay);
@@ -782,6 +850,12 @@ void launch_limit(const KP& p, cudaStream_t s) {
     if (p.n > 0) k_limit<<<cell_grid(p), p.blk_cell, 0, s>>>(p);
 }
 void launch_end(const KP& p, cudaStream_t s) { k_end<<<(p.n_inst + 127) / 128, 128, 0, s>>>(p); }
+void launch_drift(const KP& p, double dt, cudaStream_t s) {
+    if (p.n > 0) k_drift<<<grid(p.n, kBlock), kBlock, 0, s>>>(p, dt);
+}
+void launch_geometry(const KP& p, cudaStream_t s) {
+    if (p.n > 0) k_geometry<<<grid(p.n, kBlock), kBlock, 0, s>>>(p);
+}
 void launch_set_time(const KP& p, unsigned long long ti_current, unsigned long long ti_old, cudaStream_t s) {
     k_set_time<<<(p.n_inst + 127) / 128, 128, 0, s>>>(p, ti_current, ti_old);
 }

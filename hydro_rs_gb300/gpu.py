@@ -26,7 +26,7 @@ EXPORTED = (
     "mvmm_step", "mvmm_run", "mvmm_enqueue_steps", "mvmm_set_time", "mvmm_get_time", "mvmm_profile_enable",
     "mvmm_profile_read", "mvmm_riemann_flux", "mvmm_riemann_sample", "mvmm_get_stats",
     "mvmm_ctx_create_batched", "mvmm_batch_state", "mvmm_autotune", "mvmm_riemann_flux_p", "mvmm_riemann_sample_p",
-    "mvmm_step_cells",
+    "mvmm_step_cells", "mvmm_drift", "mvmm_get_positions", "mvmm_set_mesh",
 )
 
 
@@ -43,15 +43,16 @@ class _Params(ctypes.Structure):
                 ("dimensionality", ctypes.c_int), ("sync_all", ctypes.c_int), ("t_end", ctypes.c_double),
                 ("max_newton_iter", ctypes.c_int), ("precision", ctypes.c_int), ("particle_motion", ctypes.c_int),
                 ("runner", ctypes.c_int), ("airs_threshold", ctypes.c_double),
-                ("advection_velocity", ctypes.c_double * 3)]
+                ("advection_velocity", ctypes.c_double * 3), ("box_size", ctypes.c_double * 3)]
 
 
-def make_params(p, precision=None) -> _Params:
-    """mvmm_params from an ics.Params (precision overrides p.precision)."""
+def make_params(p, precision=None, box=(1.0, 1.0, 1.0)) -> _Params:
+    """mvmm_params from an ics.Params (precision overrides p.precision; box: the mesh's box)."""
     thr, adv = p.solver_extras()
     prec = p.precision if precision is None else precision
     return _Params(p.gamma, 0, 0.0, p.cfl, p.riemann, p.boundary, p.dimensionality, int(p.sync_all), p.t_end,
-                   p.max_newton_iter, prec, 0, p.runner, thr, (ctypes.c_double * 3)(*adv))
+                   p.max_newton_iter, prec, p.particle_motion, p.runner, thr, (ctypes.c_double * 3)(*adv),
+                   (ctypes.c_double * 3)(*[float(b) for b in box]))
 
 
 _LIB = None
@@ -92,6 +93,9 @@ def load_library(path: str = LIB_PATH):
         "mvmm_riemann_sample": (i32, [i32, i32, dbl, i64, vp, vp, vp, vp]),
         "mvmm_riemann_flux_p": (i32, [vp, i64, vp, vp, vp, vp, vp]),
         "mvmm_step_cells": (i32, [vp, vp, vp, u64, u64, pu64, pi64]),
+        "mvmm_drift": (i32, [vp, dbl]),
+        "mvmm_get_positions": (i32, [vp, vp]),
+        "mvmm_set_mesh": (i32, [vp, vp, vp, vp]),
         "mvmm_riemann_sample_p": (i32, [vp, i64, vp, vp, vp, vp]),
         "mvmm_get_stats": (i32, [vp, vp]),
         "mvmm_ctx_create_batched": (i32, [vp, vp, i64, vp, vp, ctypes.POINTER(vp)]),
@@ -168,7 +172,7 @@ class GpuSim:
         self.problem = problem
         self.mesh = problem.mesh
         prec = p.precision if precision is None else precision
-        self._p = make_params(p, prec)
+        self._p = make_params(p, prec, problem.mesh.box)
         self._mv = self.mesh.cview()
         h = ctypes.c_void_p(0)
         self.n_instances = 1
@@ -228,6 +232,26 @@ class GpuSim:
         self.ti_old, self.ti_current = self.ti_current, tn.value
         self.finished = done
         return done
+
+    # ---- moving meshes (host-driven: drift, rebuild the Voronoi mesh, step)
+    def drift(self, dt: float):
+        """Space::drift of every generator by v*dt (periodic wrap)."""
+        _check(load_library().mvmm_drift(self.h, float(dt)), self.h)
+
+    def positions(self) -> np.ndarray:
+        loc = np.zeros((3, self.mesh.n_cells))
+        _check(load_library().mvmm_get_positions(self.h, loc.ctypes.data), self.h)
+        return loc
+
+    def set_mesh(self, mesh):
+        """Space::volume_calculation's result: new faces now, new volumes and
+        centroids for the next step's active cells."""
+        self._mv = mesh.cview()
+        self._new_mesh = mesh  # keep the arrays alive while the context copies them
+        vol = np.ascontiguousarray(mesh.volume, dtype=np.float64)
+        cen = np.ascontiguousarray(mesh.cell_centroid, dtype=np.float64)
+        _check(load_library().mvmm_set_mesh(self.h, ctypes.byref(self._mv), vol.ctypes.data, cen.ctypes.data), self.h)
+        self.mesh = mesh
 
     def step_cells(self, cells_in: Cells, cells_out: Cells | None = None) -> bool:
         """One step on host-resident state (mvmm_step_cells): upload, step and

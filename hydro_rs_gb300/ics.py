@@ -21,6 +21,9 @@ from .mesh import mesh_1d, mesh_voronoi
 HLLC, EXACT, PVRS, AIRS, TSRS, TRRS, LINEAR_ADVECTION = 0, 1, 2, 3, 4, 5, 6
 PERIODIC, REFLECTIVE, OPEN, VACUUM = 0, 1, 2, 3
 OPTIMAL_ORDER, GODUNOV = 0, 1
+# engine.particle_motion (engine.rs:7-13)
+FIXED, STEER, STEER_PAKMOR, FLUID = 0, 1, 2, 3
+MOTION_NAMES = {"fixed": FIXED, "steer": STEER, "steer_pakmor": STEER_PAKMOR, "fluid": FLUID}
 # riemann_solver.kind and engine.runner strings (bin/main.rs:625-673)
 SOLVER_NAMES = {"HLLC": HLLC, "Exact": EXACT, "PVRS": PVRS, "AIRS": AIRS, "TSRS": TSRS, "TRRS": TRRS,
                 "LinearAdvection": LINEAR_ADVECTION}
@@ -41,6 +44,7 @@ class Params:
     precision: int = 0  # 0 = plain FP64, 1 = FP32 faces / FP64 accumulate
     max_newton_iter: int = 1000
     runner: int = OPTIMAL_ORDER
+    particle_motion: int = FIXED
     airs_threshold: float | None = None       # riemann_solver.threshold (required by AIRS)
     advection_velocity: tuple | None = None   # riemann_solver.velocity (required by LinearAdvection)
 

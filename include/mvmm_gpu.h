@@ -50,9 +50,11 @@ enum {
                                    conserved state, flux accumulation, timesteps and the
                                    integer timeline FP64 */
 };
-/* Particle motion: engine.rs:7-13.  Only FIXED is implemented (the mesh is
- * rebuilt on the host for the other modes). */
-enum { MVMM_MOTION_FIXED = 0 };
+/* Particle motion: engine.rs:7-13, Particle::set_particle_velocity
+ * (part.rs:328-372).  The moving modes need a periodic box: the host rebuilds
+ * the Voronoi mesh from the drifted generators (mvmm_drift, mvmm_get_positions,
+ * mvmm_set_mesh) before each step. */
+enum { MVMM_MOTION_FIXED = 0, MVMM_MOTION_STEER = 1, MVMM_MOTION_STEER_PAKMOR = 2, MVMM_MOTION_FLUID = 3 };
 
 /* ---- status codes / error bits --------------------------------------- */
 enum {
@@ -89,10 +91,11 @@ typedef struct mvmm_params {
     double t_end;                      /* defines time_base = t_end / 2^57 (engine.rs:118) */
     int max_newton_iter;               /* exact solver cap, 1000 in the reference */
     int precision;                     /* MVMM_PRECISION_* */
-    int particle_motion;               /* MVMM_MOTION_FIXED */
+    int particle_motion;               /* MVMM_MOTION_* */
     int runner;                        /* MVMM_RUNNER_*: OptimalOrderRunner or GodunovHydroRunner */
     double airs_threshold;             /* AIRiemannSolver::new(threshold); NaN = missing */
     double advection_velocity[3];      /* LinearAdvectionRiemannSover::new(velocity) */
+    double box_size[3];                /* Space::box_size; periodic wrap of drifted generators */
 } mvmm_params;
 
 /* Cell state, SoA, n cells.  Row layout [components][n]; grad row 3*q+k is
@@ -170,6 +173,21 @@ int mvmm_gradients(mvmm_ctx *ctx, const uint8_t *active);
  * integer time ti_current with the previous sync point ti_old; returns ti_next
  * and the number of faces that reached flux_exchange*. */
 int mvmm_step(mvmm_ctx *ctx, uint64_t ti_current, uint64_t ti_old, uint64_t *ti_next, int64_t *n_active_faces);
+/* ---- moving meshes ------------------------------------------------------ */
+/* Space::drift (space.rs:833-854, part.rs:107-119): every cell's generator,
+ * centroid and gradients centroid move by v*dt; generators that leave the
+ * periodic box are wrapped (part.rs:449-455).  Engine::run calls it between
+ * sync points (engine.rs:164-176). */
+int mvmm_drift(mvmm_ctx *ctx, double dt);
+/* The generator positions loc [3][n] (what Space::volume_calculation feeds the
+ * Voronoi builder, space.rs:236-263). */
+int mvmm_get_positions(mvmm_ctx *ctx, double *loc);
+/* Space::volume_calculation's result (space.rs:236-263): the new face list and
+ * cell->face CSR replace the mesh now; volume and centroid [3][n] of the new
+ * cells are applied to the active cells of the next step after its predict
+ * stage (Particle::update_geometry, part.rs:151-158). */
+int mvmm_set_mesh(mvmm_ctx *ctx, const mvmm_mesh *mesh, const double *volume, const double *centroid);
+
 /* Runner::step(&mut Space, ..) on host-resident state (runner.rs:6-22): uploads
  * `in`, runs one step (OptimalOrderRunner or GodunovHydroRunner) and writes the
  * new state to `out` (which may be `in`) in one call.  Copies of the rows the

@@ -618,6 +618,9 @@ struct orc_ctx {
     orc_params p;
     gaslaw eos;
     rsolver rs;
+    /* moving meshes: geometry of the rebuilt cells, applied after the next predict */
+    double *pend_vol, *pend_cen;
+    int pending_geometry;
     int64_t n, nf;
     particle *parts;
     face *faces;
@@ -839,6 +842,18 @@ static void apply_flux(particle *pt, uint32_t *err) {
     pt->gravity_mflux = v3(0., 0., 0.);
 }
 
+/* Particle::hydro_kick1 (part.rs:87-104) */
+static void hydro_kick1(particle *pt, int motion, int dim) {
+    if (motion == ORC_MOTION_FIXED) return;
+    double rho = pt->prim.q[0];
+    if (rho > 0.) {
+        double kick_fac = 0.5 * pt->dt / rho;
+        if (dim > 0) pt->v.x -= kick_fac * pt->grad.g[4].x;
+        if (dim > 1) pt->v.y -= kick_fac * pt->grad.g[4].y;
+        if (dim > 2) pt->v.z -= kick_fac * pt->grad.g[4].z;
+    }
+}
+
 /* Particle::grav_kick (part.rs:303-312) */
 static void grav_kick(particle *pt) {
     double mass = pt->cons.q[0];
@@ -1029,8 +1044,37 @@ static inline double radius(const particle *pt, int dim) {
     return pow(0.25 * 3. * 0.31830988618379067154 * pt->volume, 1. / 3.);
 }
 
-/* Particle::timestep (part.rs:42-84), set_particle_velocity for Fixed motion (:328-372) */
-static double particle_timestep(particle *pt, double cfl, const gaslaw *eos, int dim) {
+/* Particle::set_particle_velocity (part.rs:328-372) */
+static vec3 particle_velocity(const particle *pt, vec3 fluid_v, double sound_speed, int motion, int dim) {
+    if (motion == ORC_MOTION_FIXED) return v3(0., 0., 0.);
+    if (motion == ORC_MOTION_FLUID) return fluid_v;
+    vec3 d = vsub(pt->centroid, pt->loc);
+    if (motion == ORC_MOTION_STEER) {
+        double abs_d = vlen(d);
+        double eta = 0.25;
+        double eta_r = eta * radius(pt, dim);
+        double xi = 0.99;
+        if (abs_d > 0.9 * eta_r) {
+            double fac = xi * sound_speed / abs_d;
+            if (abs_d < 1.1 * eta_r) fac *= 5. * (abs_d - 0.9 * eta_r) / eta_r;
+            return vadd(fluid_v, vscale(fac, d));
+        }
+        return fluid_v;
+    }
+    /* SteerPakmor */
+    double alpha = 2. / (double)dim * pt->max_a_over_r;
+    double beta = 2.25;
+    double eta = fmax(0., fmin(0.5, 2. / beta * (alpha - 0.75 * beta)));
+    vec3 dn = vscale(1.0 / vlen(d), d); /* DVec3::normalize */
+    /* Gradients::curl_v (physical_quantities.rs:149-155) */
+    vec3 curl = v3(pt->grad.g[3].y - pt->grad.g[2].z, pt->grad.g[1].z - pt->grad.g[3].x,
+                   pt->grad.g[2].x - pt->grad.g[1].y);
+    double v_reg = radius(pt, dim) * vlen(curl);
+    return vadd(fluid_v, vscale(eta * fmax(sound_speed, v_reg), dn));
+}
+
+/* Particle::timestep (part.rs:42-84) */
+static double particle_timestep(particle *pt, double cfl, const gaslaw *eos, int dim, int motion, uint32_t *err) {
     if (pt->cons.q[0] == 0.) {
         pt->v = v3(0., 0., 0.);
         return INFINITY;
@@ -1042,8 +1086,8 @@ static double particle_timestep(particle *pt, double cfl, const gaslaw *eos, int
     /* Particle::internal_energy (part.rs:314-317) */
     double u = (pt->cons.q[4] - 0.5 * vdot(mom, st_vel(pt->prim))) / pt->cons.q[0];
     double c = sound_speed(eos, gas_pressure_from_internal_energy(eos, u, pt->prim.q[0]), pt->volume * m_inv);
-    /* ParticleMotion::Fixed */
-    pt->v = v3(0., 0., 0.);
+    pt->v = particle_velocity(pt, fluid_v, c, motion, dim);
+    if (!isfinite(pt->v.x) || !isfinite(pt->v.y) || !isfinite(pt->v.z)) *err |= ORC_ERR_NONFINITE; /* :366 */
     pt->v_rel = vsub(fluid_v, pt->v);
     pt->max_a_over_r = 0.;
     double v_max = fmax(pt->max_signal_velocity, vlen(pt->v_rel) + c);
@@ -1053,11 +1097,13 @@ static double particle_timestep(particle *pt, double cfl, const gaslaw *eos, int
 }
 
 static void compute_timesteps(orc_ctx *c, const uint8_t *active, double *out) {
-#pragma omp parallel for schedule(static)
+    uint32_t e = 0;
+#pragma omp parallel for schedule(static) reduction(| : e)
     for (int64_t i = 0; i < c->n; i++) {
         if (!active[i]) { out[i] = INFINITY; continue; }
-        out[i] = particle_timestep(&c->parts[i], c->p.cfl, &c->eos, c->p.dimensionality);
+        out[i] = particle_timestep(&c->parts[i], c->p.cfl, &c->eos, c->p.dimensionality, c->p.particle_motion, &e);
     }
+    c->err |= e;
 }
 
 /* TimestepInfo helpers (engine.rs:55-80) */
@@ -1179,8 +1225,71 @@ orc_ctx *orc_create(const orc_params *p, const orc_mesh *m) {
     return c;
 }
 
+/* Space::drift (space.rs:833-854), Particle::drift (part.rs:107-119), box_wrap (part.rs:449-455) */
+void orc_drift(orc_ctx *c, double dt) {
+    int dim = c->p.dimensionality;
+    for (int64_t i = 0; i < c->n; i++) {
+        particle *pt = &c->parts[i];
+        double *loc[3] = {&pt->loc.x, &pt->loc.y, &pt->loc.z};
+        double *cen[3] = {&pt->centroid.x, &pt->centroid.y, &pt->centroid.z};
+        double *gc[3] = {&pt->gc.x, &pt->gc.y, &pt->gc.z};
+        const double v[3] = {pt->v.x, pt->v.y, pt->v.z};
+        for (int a = 0; a < dim; a++) {
+            *loc[a] += v[a] * dt;
+            *cen[a] += v[a] * dt;
+            *gc[a] += v[a] * dt;
+        }
+        if (!isfinite(pt->loc.x) || !isfinite(pt->loc.y) || !isfinite(pt->loc.z)) {
+            c->err |= ORC_ERR_NONFINITE;
+            continue;
+        }
+        int inside = 1;
+        for (int a = 0; a < dim; a++) inside = inside && *loc[a] >= 0. && *loc[a] < c->p.box_size[a];
+        if (inside) continue;
+        vec3 old = pt->loc;
+        for (int a = 0; a < dim; a++) {
+            while (*loc[a] < 0.) *loc[a] += c->p.box_size[a];
+            while (*loc[a] >= c->p.box_size[a]) *loc[a] -= c->p.box_size[a];
+        }
+        vec3 shift = vsub(pt->loc, old);
+        pt->gc = vadd(pt->gc, shift);
+        pt->centroid = vadd(pt->centroid, shift);
+    }
+}
+
+void orc_set_mesh(orc_ctx *c, const orc_mesh *m, const double *volume, const double *centroid) {
+    free(c->faces);
+    free(c->fi);
+    free(c->csr_face);
+    c->nf = m->n_faces;
+    c->faces = (face *)calloc((size_t)(c->nf > 0 ? c->nf : 1), sizeof(face));
+    for (int64_t f = 0; f < c->nf; f++) {
+        face *fc = &c->faces[f];
+        fc->left = m->left[f];
+        fc->right = m->right[f] < 0 ? -1 : m->right[f];
+        fc->area = m->area[f];
+        fc->normal = m_vec(m->normal, c->nf, f);
+        fc->centroid = m_vec(m->centroid, c->nf, f);
+        fc->shift = m_vec(m->shift, c->nf, f);
+    }
+    memcpy(c->csr_off, m->csr_off, sizeof(int32_t) * (size_t)(c->n + 1));
+    int64_t nc = m->csr_off[c->n];
+    c->csr_face = (int32_t *)malloc(sizeof(int32_t) * (size_t)(nc > 0 ? nc : 1));
+    memcpy(c->csr_face, m->csr_face, sizeof(int32_t) * (size_t)nc);
+    c->fi = (flux_info *)malloc(sizeof(flux_info) * (size_t)(c->nf > 0 ? c->nf : 1));
+    if (!c->pend_vol) {
+        c->pend_vol = (double *)malloc(sizeof(double) * (size_t)c->n);
+        c->pend_cen = (double *)malloc(sizeof(double) * 3 * (size_t)c->n);
+    }
+    memcpy(c->pend_vol, volume, sizeof(double) * (size_t)c->n);
+    memcpy(c->pend_cen, centroid, sizeof(double) * 3 * (size_t)c->n);
+    c->pending_geometry = 1;
+}
+
 void orc_destroy(orc_ctx *c) {
     if (!c) return;
+    free(c->pend_vol);
+    free(c->pend_cen);
     free(c->parts); free(c->faces); free(c->csr_off); free(c->csr_face);
     free(c->fi); free(c->active); free(c->gtmp); free(c->has_g); free(c->dts); free(c->wake);
     free(c);
@@ -1249,6 +1358,16 @@ uint64_t orc_step(orc_ctx *c, uint64_t ti_current, uint64_t ti_old, int64_t *n_a
     for (int64_t i = 0; i < c->n; i++) c->active[i] = c->parts[i].timebin <= max_bin; /* bin_is_ending */
     double dt = dt_from_dti(c, ti_current - ti_old);
     orc_predict(c, dt);
+    if (c->pending_geometry) { /* Space::volume_calculation -> Particle::update_geometry (part.rs:151-158) */
+        for (int64_t i = 0; i < c->n; i++) {
+            if (!c->active[i]) continue;
+            particle *pt = &c->parts[i];
+            pt->volume = c->pend_vol[i];
+            pt->centroid = v3(c->pend_cen[i], c->pend_cen[c->n + i], c->pend_cen[2 * c->n + i]);
+            if (!(pt->volume >= 0.)) c->err |= ORC_ERR_NONFINITE;
+        }
+        c->pending_geometry = 0;
+    }
     int64_t nf = compute_fluxes(c, c->active, c->fi);
     if (n_active_faces) *n_active_faces = nf;
     apply_fluxes(c, c->fi, c->active);
@@ -1264,7 +1383,8 @@ uint64_t orc_step(orc_ctx *c, uint64_t ti_current, uint64_t ti_old, int64_t *n_a
     for (int64_t i = 0; i < c->n; i++) {
         if (!c->active[i]) continue;
         c->parts[i].extrap = st_vacuum();
-        grav_kick(&c->parts[i]); /* hydro_kick1 is a no-op for Fixed motion */
+        hydro_kick1(&c->parts[i], c->p.particle_motion, c->p.dimensionality);
+        grav_kick(&c->parts[i]);
     }
     return ti_next;
 }

@@ -24,6 +24,8 @@ extern "C" {
  * bin/main.rs:637-640). */
 enum { ORC_HLLC = 0, ORC_EXACT = 1, ORC_PVRS = 2, ORC_AIRS = 3, ORC_TSRS = 4, ORC_TRRS = 5,
        ORC_LINEAR_ADVECTION = 6 };
+/* Particle motion (engine.rs:7-13). */
+enum { ORC_MOTION_FIXED = 0, ORC_MOTION_STEER = 1, ORC_MOTION_STEER_PAKMOR = 2, ORC_MOTION_FLUID = 3 };
 /* Runner (bin/main.rs:667-673). */
 enum { ORC_RUNNER_OPTIMAL_ORDER = 0, ORC_RUNNER_GODUNOV = 1 };
 /* Boundary (space.rs:26-32). */
@@ -58,6 +60,8 @@ typedef struct orc_params {
     int runner;          /* ORC_RUNNER_* */
     double airs_threshold;        /* AIRiemannSolver::new(threshold) */
     double advection_velocity[3]; /* LinearAdvectionRiemannSover::new(velocity) */
+    int particle_motion;          /* ORC_MOTION_* (engine.rs:7-13) */
+    double box_size[3];           /* Space::box_size (periodic wrap after a drift) */
 } orc_params;
 
 /* SoA views; identical field meaning to the GPU library's mvmm_cells /
@@ -92,6 +96,14 @@ uint64_t orc_step(orc_ctx *c, uint64_t ti_current, uint64_t ti_old, int64_t *n_a
  * most max_steps steps (<=0: unbounded); returns the number of steps run. */
 int64_t orc_run(orc_ctx *c, int64_t max_steps, uint64_t *ti_current, uint64_t *ti_old,
                 int64_t *n_active_faces);
+
+/* Moving meshes.  Space::drift (space.rs:833-854) of every generator,
+ * centroid and gradients centroid by v*dt with the periodic wrap; and
+ * Space::volume_calculation's result (space.rs:236-263): the new faces and CSR
+ * replace the mesh, volume and centroid [3][n] are applied to the active
+ * cells of the next step after its predict (Particle::update_geometry). */
+void orc_drift(orc_ctx *c, double dt);
+void orc_set_mesh(orc_ctx *c, const orc_mesh *m, const double *volume, const double *centroid);
 
 /* Per-stage entry points (FiniteVolumeSolver trait + runner free functions). */
 void orc_predict(orc_ctx *c, double dt);

@@ -26,7 +26,8 @@ class _Params(ctypes.Structure):
                 ("cfl", ctypes.c_double), ("riemann", ctypes.c_int), ("boundary", ctypes.c_int),
                 ("dimensionality", ctypes.c_int), ("sync_all", ctypes.c_int), ("t_end", ctypes.c_double),
                 ("max_newton_iter", ctypes.c_int), ("n_threads", ctypes.c_int), ("runner", ctypes.c_int),
-                ("airs_threshold", ctypes.c_double), ("advection_velocity", ctypes.c_double * 3)]
+                ("airs_threshold", ctypes.c_double), ("advection_velocity", ctypes.c_double * 3),
+                ("particle_motion", ctypes.c_int), ("box_size", ctypes.c_double * 3)]
 
 
 def build() -> str:
@@ -62,6 +63,8 @@ def lib():
         L.orc_compute_timesteps.argtypes = [vp, vp, vp]
         L.orc_riemann_flux.argtypes = [i32, dbl, i64, vp, vp, vp, vp, vp, ctypes.POINTER(ctypes.c_uint32)]
         L.orc_riemann_sample.argtypes = [i32, dbl, i64, vp, vp, vp, vp, ctypes.POINTER(ctypes.c_uint32)]
+        L.orc_drift.argtypes = [vp, dbl]
+        L.orc_set_mesh.argtypes = [vp, vp, vp, vp]
         L.orc_riemann_flux_ex.argtypes = [i32, dbl, dbl, vp, i64, vp, vp, vp, vp, vp, ctypes.POINTER(ctypes.c_uint32)]
         L.orc_riemann_sample_ex.argtypes = [i32, dbl, dbl, i64, vp, vp, vp, vp, ctypes.POINTER(ctypes.c_uint32)]
         L.orc_get_integer_timestep.restype = u64
@@ -92,7 +95,8 @@ class OracleSim:
         self.cells = problem.cells.copy()
         thr, adv = p.solver_extras()
         self._p = _Params(p.gamma, 0, 0.0, p.cfl, p.riemann, p.boundary, p.dimensionality, int(p.sync_all),
-                          p.t_end, p.max_newton_iter, n_threads, p.runner, thr, (ctypes.c_double * 3)(*adv))
+                          p.t_end, p.max_newton_iter, n_threads, p.runner, thr, (ctypes.c_double * 3)(*adv),
+                          p.particle_motion, (ctypes.c_double * 3)(*[float(b) for b in problem.mesh.box]))
         self._mv = self.mesh.cview()
         self.h = lib().orc_create(ctypes.byref(self._p), ctypes.byref(self._mv))
         self._cv = self.cells.cview()
@@ -139,6 +143,21 @@ class OracleSim:
         cv = out.cview()
         lib().orc_get_cells(self.h, ctypes.byref(cv))
         return out
+
+    # ---- moving meshes ----
+    def drift(self, dt: float):
+        lib().orc_drift(self.h, float(dt))
+
+    def positions(self) -> np.ndarray:
+        return self.state().loc.copy()
+
+    def set_mesh(self, mesh):
+        self._mv = mesh.cview()
+        self._new_mesh = mesh
+        vol = np.ascontiguousarray(mesh.volume, dtype=np.float64)
+        cen = np.ascontiguousarray(mesh.cell_centroid, dtype=np.float64)
+        lib().orc_set_mesh(self.h, ctypes.byref(self._mv), vol.ctypes.data, cen.ctypes.data)
+        self.mesh = mesh
 
     # ---- per-stage (FiniteVolumeSolver trait / runner free functions) ----
     def predict(self, dt: float):

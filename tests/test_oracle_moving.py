@@ -1,0 +1,70 @@
+"""Moving meshes in the CPU oracle (particle motion fluid / steer / steer_pakmor).
+
+The generators drift with the particle velocities of set_particle_velocity
+(part.rs:328-372, hydro_kick1 part.rs:87-104) and the host rebuilds the Voronoi
+mesh before each step (Space::drift / volume_calculation).  The reference has
+no test of this path; it is pinned by properties: a uniform flow carried by
+fluid motion stays uniform (Galilean invariance of the moving-mesh scheme: the
+faces move with the fluid, so no mass crosses them) while its generators move
+by v t, and mass, momentum and energy are conserved to round-off in a periodic
+box for every motion.
+"""
+import numpy as np
+import pytest
+
+from hydro_rs_gb300 import ics
+from hydro_rs_gb300.moving import MovingMeshStepper
+from oracle import oracle as O
+
+
+def _uniform_problem(nx, v=(0.3, -0.2)):
+    p = ics.kelvin_helmholtz_2d(nx, riemann=ics.HLLC, t_end=1.0)
+    loc = p.cells.loc
+    vel = np.zeros((3, loc.shape[1]))
+    vel[0], vel[1] = v
+    u = ics.gas_internal_energy_from_pressure(p.params.gamma, 1.0, 1.0)
+    p.cells = ics.cells_from_ic(p.mesh, loc, 1.0 * p.mesh.volume, vel, u, p.params.gamma)
+    p.params.particle_motion = ics.FLUID
+    return p
+
+
+def test_uniform_flow_fluid_motion():
+    p = _uniform_problem(12)
+    sim = O.OracleSim(p)
+    st = MovingMeshStepper(sim, p.mesh)
+    loc0 = p.cells.loc.copy()
+    t = 0.0
+    for _ in range(6):
+        st.step()
+        assert sim.error() == 0
+    s = sim.state()
+    assert np.allclose(s.prim[0], 1.0, rtol=1e-12, atol=0)
+    assert np.allclose(s.prim[1], 0.3, rtol=0, atol=1e-12)
+    assert np.allclose(s.prim[2], -0.2, rtol=0, atol=1e-12)
+    assert np.allclose(s.prim[4], 1.0, rtol=1e-12, atol=0)
+    # the generators moved with the flow (periodic unit box); t = last drift time
+    t = (sim.ti_old) * p.params.t_end / (1 << 57)
+    d = (s.loc[:2] - loc0[:2] - np.array([[0.3], [-0.2]]) * t + 0.5) % 1.0 - 0.5
+    assert np.abs(d).max() < 1e-12
+    assert t > 0
+
+
+@pytest.mark.parametrize("motion", [ics.FLUID, ics.STEER, ics.STEER_PAKMOR])
+def test_conservation_moving(motion):
+    p = ics.kelvin_helmholtz_2d(16, riemann=ics.HLLC, t_end=1.5)
+    p.params.particle_motion = motion
+    sim = O.OracleSim(p)
+    st = MovingMeshStepper(sim, p.mesh)
+    for _ in range(8):
+        st.step()
+    assert sim.error() == 0
+    s = sim.state()
+    c0, c1 = p.cells.cons.sum(axis=1), s.cons.sum(axis=1)
+    assert abs(c1[0] - c0[0]) <= 1e-13 * c0[0]
+    assert abs(c1[4] - c0[4]) <= 1e-13 * c0[4]
+    for q in (1, 2):
+        assert abs(c1[q] - c0[q]) <= 1e-13 * c0[0]
+    # the mesh moved: generators are no longer at the initial positions, and stay in the box
+    assert np.abs(s.loc - p.cells.loc).max() > 1e-6
+    assert (s.loc[:2] >= 0).all() and (s.loc[:2] < 1).all()
+    assert abs(s.volume.sum() - 1.0) < 1e-12
