@@ -71,6 +71,9 @@ WORKLOADS = {
     # the same batch with the PVRS solver
     "batch1d_pvrs": "{n} independent 1D Riemann problems (N log-uniform 200..20000), PVRS solver, one batch, "
                     "t_end=0.15",
+    # moving mesh: the shear layer with steered generators, host Voronoi rebuild every step
+    "kh2d_moving": "kelvin_helmholtz_2d {n}x{n} jittered periodic Voronoi, exact Riemann solver, gamma=5/3, "
+                   "steered generators (particle_motion=steer), mesh rebuilt on the host every step",
     # served: Poisson stream (50 req/s) of {n} isentropic-vortex runs, 32^2..512^2, HLLC, t_end=1
     "serve2d": "{n} served isentropic-vortex requests (Poisson 50/s, 32^2..512^2 periodic Voronoi, HLLC, t_end=1)",
 }
@@ -81,7 +84,7 @@ DATA = {
     "batch1d": "synthetic (seeded random 1D Riemann problems)",
     "batch1d_pvrs": "synthetic (seeded random 1D Riemann problems)",
 }
-DEFAULT_N = {"kh2d": NX, "sod1d": 1000, "blast3d": 128, "batch1d": 512, "batch1d_pvrs": 512, "serve2d": 60}
+DEFAULT_N = {"kh2d_moving": NX, "kh2d": NX, "sod1d": 1000, "blast3d": 128, "batch1d": 512, "batch1d_pvrs": 512, "serve2d": 60}
 
 
 def _problem(nx=NX, workload="kh2d"):
@@ -474,6 +477,102 @@ def run_serve(args):
     print(json.dumps(line))
 
 
+def run_moving(args):
+    """Moving mesh (drift + per-step host Voronoi + re-upload): each
+    step drifts the generators on the device, reads them back, rebuilds the
+    Voronoi mesh on the host, uploads it and steps.  `value` is active-face
+    updates per second of device step time (CUDA events on the context's
+    stream); `e2e` divides by the wall time of the whole cycle, and `stages_s`
+    gives each part as its own line."""
+    import torch
+
+    from hydro_rs_gb300 import gpu as G
+    from hydro_rs_gb300 import ics
+    from hydro_rs_gb300.moving import MovingMeshStepper
+
+    ws, rank = _dist()
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    if rank != 0:
+        return
+    t0 = time.perf_counter()
+    problem = ics.kelvin_helmholtz_2d(args.nx, seed=2, riemann=ics.EXACT, t_end=1.5)
+    problem.params.particle_motion = ics.STEER
+    mesh_s = time.perf_counter() - t0
+    threads = os.cpu_count() or 1
+    stream = torch.cuda.Stream()
+    res, stages, sims = {}, {}, {}
+    with _Clocks() as clk:
+        for prec in (1, 0):
+            sim = G.GpuSim(problem, precision=prec, stream=stream.cuda_stream)
+            st = MovingMeshStepper(sim, problem.mesh, n_threads=threads)
+            for _ in range(args.warmup):
+                st.step()
+            st.seconds = {k: 0.0 for k in st.seconds}
+            f0, dev_ms = sim.active_faces, 0.0
+            t_wall = time.perf_counter()
+            for _ in range(args.steps):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                # the step's own stream work (drift and mesh upload are their own lines)
+                orig_step = sim.step
+
+                def timed_step(sim=sim, orig=orig_step, e0=e0, e1=e1):
+                    e0.record(stream)
+                    done = orig()
+                    e1.record(stream)
+                    return done
+                sim.step = timed_step
+                st.step()
+                sim.step = orig_step
+                e1.synchronize()
+                dev_ms += e0.elapsed_time(e1)
+            wall = time.perf_counter() - t_wall
+            faces = sim.active_faces - f0
+            res[prec] = (faces, dev_ms, wall)
+            stages[prec] = {k: round(v / args.steps * 1e3, 3) for k, v in st.seconds.items()}
+            sims[prec] = sim
+    a, b = sims[1].state(), sims[0].state()
+    l1 = float(np.abs(a.prim[0] - b.prim[0]).sum() / np.abs(b.prim[0]).sum())
+    same_time = sims[1].ti_current == sims[0].ti_current
+    cpu = None
+    if not args.no_cpu:
+        from oracle import oracle as O
+
+        osim = O.OracleSim(problem, n_threads=threads)
+        ost = MovingMeshStepper(osim, problem.mesh, n_threads=threads)
+        ost.step()
+        f0, t1, n = osim.active_faces, time.perf_counter(), 0
+        while time.perf_counter() - t1 < 10.0 and n < 100:
+            ost.step()
+            n += 1
+        t_cpu = time.perf_counter() - t1
+        cpu = {"value": (osim.active_faces - f0) / t_cpu, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{n} moving-mesh steps of the same workload on the oracle, each with the host Voronoi "
+                         f"rebuild ({t_cpu:.1f} s wall, whole cycle)"}
+    faces32, ms32, wall32 = res[1]
+    faces64, ms64, wall64 = res[0]
+    m = sims[1].mesh  # mvmm_set_mesh uploads the faces, the CSR and the new volumes and centroids
+    mesh_bytes = int(m.n_faces * 88 + (m.n_cells + 1) * 4 + m.csr_face.size * 4 + m.n_cells * 32)
+    line = {
+        "metric": METRIC, "value": faces32 / (ms32 * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms32 / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32-face/f64-accumulate",
+        "data": "synthetic (seeded jittered lattice, shear-layer ICs)",
+        "config": {"workload": WORKLOADS["kh2d_moving"].format(n=args.nx), "cells": problem.mesh.n_cells,
+                   "faces_initial": problem.mesh.n_faces, "precision": "fp32_face",
+                   "l2": "not flushed: the mesh upload before each step rewrites the face arrays",
+                   "parallelism": "replicas x1", "mesh_build_s": round(mesh_s, 3)},
+        "l1_density_err_vs_fp64": l1, "l1_same_time": same_time,
+        "stages_ms_per_step": {"fp32_face": stages[1], "fp64": stages[0]},
+        "plain_fp64": {"value": faces64 / (ms64 * 1e-3), "unit": UNIT, "ms_per_step": ms64 / args.steps},
+        "e2e": {"value": faces32 / wall32, "unit": UNIT,
+                "h2d_bytes_per_step": mesh_bytes, "d2h_bytes_per_step": problem.mesh.n_cells * 24,
+                "how": "whole moving-mesh cycle per step, wall clock: mvmm_drift, mvmm_get_positions, host Voronoi "
+                       "build, mvmm_set_mesh, mvmm_step"},
+        "cpu_baseline": cpu, "clocks": clk.summary(0),
+    }
+    print(json.dumps(line))
+
+
 def run_reference(args):
     ws, rank = _dist()
     if rank != 0:
@@ -524,6 +623,8 @@ def main():
         run_reference(args)
     elif args.workload == "serve2d":
         run_serve(args)
+    elif args.workload == "kh2d_moving":
+        run_moving(args)
     else:
         run_ours(args)
 
