@@ -84,7 +84,7 @@ struct mvmm_ctx {
     bool prof = false;
     cudaEvent_t ev[MVMM_NUM_KERNELS + 1] = {};
     cudaStream_t side = nullptr;              // copies of mvmm_step_cells that overlap the step
-    cudaEvent_t ev_in = nullptr, ev_upd = nullptr, ev_out = nullptr;
+    cudaEvent_t ev_face = nullptr, ev_in = nullptr, ev_upd = nullptr, ev_grad = nullptr, ev_out = nullptr;
     double prof_ms[MVMM_NUM_KERNELS] = {};
     int64_t prof_n[MVMM_NUM_KERNELS] = {};
     double time_base = 0, time_base_inv = 0;
@@ -191,26 +191,39 @@ void launch_face(mvmm_ctx* c, const KP& p) {
 }
 
 // The six kernels of one OptimalOrderRunner step, optionally bracketed by events.
-// before_update: an event the update waits for; after_update: recorded after it
-void enqueue_step_kernels(mvmm_ctx* c, bool with_events, cudaEvent_t before_update = nullptr,
-                          cudaEvent_t after_update = nullptr) {
+// Copies that overlap a step (mvmm_step_cells): events the step waits for
+// before its face stage and before its update, events it records after the
+// update and after the gradient stage, and the FP32 geometry refresh once the
+// positions have arrived.
+struct StepHooks {
+    cudaEvent_t wait_before_face = nullptr;
+    bool geom_before_face = false;
+    cudaEvent_t wait_before_update = nullptr;
+    cudaEvent_t after_update = nullptr;
+    cudaEvent_t after_gradients = nullptr;
+};
+
+void enqueue_step_kernels(mvmm_ctx* c, bool with_events, const StepHooks& h = StepHooks()) {
     KP p = make_kp(c, 0, 7);
     cudaStream_t s = c->stream;
     if (with_events) cudaEventRecord(c->ev[0], s);
     launch_predict(p, s);
     if (c->pending_geometry) launch_geometry(p, s);  // after predict, as volume_calculation
-    if (c->prm.particle_motion != MVMM_MOTION_FIXED && c->prm.precision == MVMM_PRECISION_FP32FACE)
-        launch_geom32(p, s);  // generators drifted, centroids updated
+    if (h.wait_before_face) cudaStreamWaitEvent(s, h.wait_before_face, 0);
+    if ((h.geom_before_face || c->prm.particle_motion != MVMM_MOTION_FIXED) &&
+        c->prm.precision == MVMM_PRECISION_FP32FACE)
+        launch_geom32(p, s);  // generators drifted or uploaded, centroids updated
     if (p.use_list) launch_compact(p, s);
     if (with_events) cudaEventRecord(c->ev[1], s);
     launch_face(c, p);
     if (with_events) cudaEventRecord(c->ev[2], s);
-    if (before_update) cudaStreamWaitEvent(s, before_update, 0);
+    if (h.wait_before_update) cudaStreamWaitEvent(s, h.wait_before_update, 0);
     launch_update(p, 1, s);
-    if (after_update) cudaEventRecord(after_update, s);
+    if (h.after_update) cudaEventRecord(h.after_update, s);
     if (with_events) cudaEventRecord(c->ev[3], s);
     if (c->prm.precision == MVMM_PRECISION_FP32FACE) launch_gradients32(p, s);
     else launch_gradients(p, 1, s);
+    if (h.after_gradients) cudaEventRecord(h.after_gradients, s);
     if (with_events) cudaEventRecord(c->ev[4], s);
     launch_limit(p, s);
     if (with_events) cudaEventRecord(c->ev[5], s);
@@ -532,7 +545,7 @@ int mvmm_ctx_destroy(mvmm_ctx* c) {
         if (c->ev[k]) cudaEventDestroy(c->ev[k]);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     if (c->side) cudaStreamDestroy(c->side);
-    for (cudaEvent_t e : {c->ev_in, c->ev_upd, c->ev_out})
+    for (cudaEvent_t e : {c->ev_face, c->ev_in, c->ev_upd, c->ev_grad, c->ev_out})
         if (e) cudaEventDestroy(e);
     delete c;
     return MVMM_OK;
@@ -564,8 +577,14 @@ struct RowCopy {
 };
 // The rows of mvmm_cells in the device's field order; subset: a bit per entry.
 constexpr unsigned kAllRows = 0x3fffu;
-constexpr unsigned kRowsEarlyOut = 0x23u;  // cons, prim, facc: final once the update has run
-constexpr unsigned kRowsLateIn = 0x1821u;  // cons, facc, max_a_over_r, max_signal_velocity: read from the update on
+// mvmm_step_cells moves the rows in three groups each way, each as soon as the
+// step can use it or has finished with it.
+constexpr unsigned kRowsPredictIn = 0x0416u;  // prim, grad, extrap, v_rel (+ timebin): what predict reads
+constexpr unsigned kRowsFaceIn = 0x23C8u;     // gc, volume, loc, centroid, v, dt: read from the face stage on
+constexpr unsigned kRowsLateIn = 0x1821u;     // cons, facc, max_a_over_r, max_signal_velocity: from the update on
+constexpr unsigned kRowsEarlyOut = 0x0023u;   // cons, prim, facc: final once the update has run
+constexpr unsigned kRowsMidOut = 0x1E0Cu;     // grad, gc, v, v_rel, max_a_over_r, max_signal_velocity: after gradients
+constexpr unsigned kRowsLateOut = 0x21D0u;    // extrap, volume, loc, centroid, dt (+ timebin): after the limiter
 int row_map(const mvmm_cells* h, unsigned subset, RowCopy* out, size_t* m) {
     const RowCopy all[14] = {{h->cons, F_CONS, 5},         {h->prim, F_PRIM, 5},     {h->grad, F_GRAD, 15},
                              {h->gc, F_GC, 3},             {h->extrap, F_EXTRAP, 5}, {h->facc, F_FACC, 5},
@@ -656,25 +675,39 @@ int mvmm_step_cells(mvmm_ctx* c, const mvmm_cells* in, mvmm_cells* out, uint64_t
         return fail(MVMM_E_UNSUPPORTED, "mvmm_step_cells steps a fixed mesh");
     if (!c->side) {
         CUDA_TRY(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
-        for (cudaEvent_t* e : {&c->ev_in, &c->ev_upd, &c->ev_out})
+        for (cudaEvent_t* e : {&c->ev_face, &c->ev_in, &c->ev_upd, &c->ev_grad, &c->ev_out})
             CUDA_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
     }
     cudaStream_t s = c->stream, s2 = c->side;
-    // what predict and the face stage read, then (side stream) what only the update needs
-    int rc = copy_cells(c, in, kAllRows & ~kRowsLateIn, true, cudaMemcpyHostToDevice, s);
-    if (!rc) rc = copy_cells(c, in, kRowsLateIn, false, cudaMemcpyHostToDevice, s2);
+    // host -> device: what predict reads on the step's stream; on the side stream
+    // what the face stage and then the update read, each behind an event
+    int rc = copy_cells(c, in, kRowsPredictIn, true, cudaMemcpyHostToDevice, s);
+    if (!rc) rc = copy_cells(c, in, kRowsFaceIn, false, cudaMemcpyHostToDevice, s2);
+    if (rc) return rc;
+    CUDA_TRY(cudaEventRecord(c->ev_face, s2));
+    rc = copy_cells(c, in, kRowsLateIn, false, cudaMemcpyHostToDevice, s2);
     if (rc) return rc;
     CUDA_TRY(cudaEventRecord(c->ev_in, s2));
-    rc = refresh_geometry(c, s);
+    rc = mark_stale(c, s);
     if (rc) return rc;
     launch_set_time(make_kp(c, 0, 7), ti_current, ti_old, s);
-    enqueue_step_kernels(c, false, c->ev_in, c->ev_upd);
-    // rows final after the update go back while the gradient and limiter stages run
+    StepHooks h;
+    h.wait_before_face = c->ev_face;
+    h.geom_before_face = true;
+    h.wait_before_update = c->ev_in;
+    h.after_update = c->ev_upd;
+    h.after_gradients = c->ev_grad;
+    enqueue_step_kernels(c, false, h);
+    // device -> host on the side stream: the rows final after the update while
+    // the gradient stage runs, those final after it while the limiter runs
     CUDA_TRY(cudaStreamWaitEvent(s2, c->ev_upd, 0));
     rc = copy_cells(c, out, kRowsEarlyOut, false, cudaMemcpyDeviceToHost, s2);
     if (rc) return rc;
+    CUDA_TRY(cudaStreamWaitEvent(s2, c->ev_grad, 0));
+    rc = copy_cells(c, out, kRowsMidOut, false, cudaMemcpyDeviceToHost, s2);
+    if (rc) return rc;
     CUDA_TRY(cudaEventRecord(c->ev_out, s2));
-    rc = copy_cells(c, out, kAllRows & ~kRowsEarlyOut, true, cudaMemcpyDeviceToHost, s);
+    rc = copy_cells(c, out, kRowsLateOut, true, cudaMemcpyDeviceToHost, s);
     if (rc) return rc;
     CUDA_TRY(cudaStreamWaitEvent(s, c->ev_out, 0));
     CUDA_TRY(cudaGetLastError());
