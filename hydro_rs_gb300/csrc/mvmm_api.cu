@@ -72,6 +72,7 @@ struct mvmm_ctx {
     double *pend_vol = nullptr, *pend_cen = nullptr;
     bool pending_geometry = false;
     unsigned int* touch = nullptr;
+    unsigned int* blocks_done = nullptr;
     uint8_t* fresh = nullptr;
     int* cell_list = nullptr;
     int* face_list = nullptr;
@@ -157,6 +158,7 @@ KP make_kp(mvmm_ctx* c, int stage, int flux_rows) {
     p.use_list = (!stage && !c->prm.sync_all && c->n_inst == 1) ? 1 : 0;
     p.face_stamp = c->face_stamp;
     p.touch = c->touch;
+    p.blocks_done = c->blocks_done;
     p.fresh = c->fresh;
     p.cell_list = c->cell_list;
     p.face_list = c->face_list;
@@ -438,6 +440,7 @@ static int create_impl(const mvmm_params* prm, const mvmm_mesh* m, int64_t n_ins
     ALLOC(c->dtmp, n * 8);
     ALLOC(c->face_stamp, nf * 4);
     ALLOC(c->touch, n * 4);
+    ALLOC(c->blocks_done, 4);
     ALLOC(c->fresh, n);
     ALLOC(c->cell_list, n * 4);
     ALLOC(c->face_list, nf * 4);
@@ -472,6 +475,7 @@ static int create_impl(const mvmm_params* prm, const mvmm_mesh* m, int64_t n_ins
     cudaMemsetAsync(c->flux, 0, 10 * nf * 8, s);
     cudaMemsetAsync(c->face_stamp, 0, nf * 4, s);
     cudaMemsetAsync(c->touch, 0, n * 4, s);
+    cudaMemsetAsync(c->blocks_done, 0, 4, s);
     cudaMemsetAsync(c->fresh, 0, n, s);
     std::memset(c->tl_host, 0, sizeof(DevTimeline) * c->n_inst);
     for (int k = 0; k < c->n_inst; k++) {
@@ -534,7 +538,7 @@ int mvmm_ctx_destroy(mvmm_ctx* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->step_exec) cudaGraphExecDestroy(c->step_exec);
     void* ptrs[] = {c->left, c->right, c->csr_off, c->csr_face, c->area, c->normal, c->fcen, c->shift, c->cd,
-                    c->cf, c->timebin, c->tb_tmp, c->active, c->flux, c->flux32, c->geo, c->dtmp, c->face_stamp, c->touch, c->cell_list, c->fresh,
+                    c->cf, c->timebin, c->tb_tmp, c->active, c->flux, c->flux32, c->geo, c->dtmp, c->face_stamp, c->touch, c->blocks_done, c->cell_list, c->fresh,
                     c->pend_vol, c->pend_cen,
                     c->face_list, c->tl,
                     c->inst, c->inst_tb, c->inst_tbi};

@@ -145,6 +145,7 @@ struct KP {
     const double* new_cen;   //   rebuilt cells, applied to active cells after predict
     int use_list;            // 1: face kernel walks the compacted active-face list
     unsigned int* face_stamp;  // hierarchical steps: steps + 1 for faces active in this step
+    unsigned int* blocks_done;  // k_limit blocks finished this step (the last one ends the step)
     unsigned int* touch;     // hierarchical steps: 1 for cells on this step's cell list
     uint8_t* fresh;          // 1: the cell's derived face-stage rows match its prim, grad and v_rel
     int* cell_list;          // hierarchical steps: active cells and the cells next to an active face

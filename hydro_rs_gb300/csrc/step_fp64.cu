@@ -665,17 +665,30 @@ __device__ __forceinline__ void limit_cell(const KP& p, int i) {
         W(p, F_CONS + 3, i, C(p, F_CONS + 3, i) + 0.);
     }
 }
+__device__ __forceinline__ void end_instance(const KP& p, int k);
 __global__ void __launch_bounds__(kMaxBlock) k_limit(KP p) {
     const int n_items = cell_items(p);
     for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n_items; idx += gridDim.x * blockDim.x)
         limit_cell(p, cell_at(p, idx));
+    // the last block to finish does the engine's bookkeeping of the step
+    // (end_instance); no cell data is read there, only the timelines
+    __shared__ bool last;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        last = atomicAdd(p.blocks_done, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (last) {
+        __threadfence();
+        for (int k = threadIdx.x; k < p.n_inst; k += blockDim.x) end_instance(p, k);
+        if (threadIdx.x == 0) *p.blocks_done = 0;
+    }
 }
 
 // Engine bookkeeping after a step (engine.rs:194-199, 258-268): advance the
 // device timeline to the next sync point and reset the reductions.
-__global__ void k_end(KP p) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= p.n_inst) return;
+__device__ __forceinline__ void end_instance(const KP& p, int k) {
     DevTimeline* tl = p.tl + k;
     if (tl->done) return;
     unsigned long long tc = tl->ti_current;
@@ -849,7 +862,8 @@ void launch_timesteps(const KP& p, double* dt_out, cudaStream_t s) {
 void launch_limit(const KP& p, cudaStream_t s) {
     if (p.n > 0) k_limit<<<cell_grid(p), p.blk_cell, 0, s>>>(p);
 }
-void launch_end(const KP& p, cudaStream_t s) { k_end<<<(p.n_inst + 127) / 128, 128, 0, s>>>(p); }
+// the engine bookkeeping runs in the last block of k_limit
+void launch_end(const KP&, cudaStream_t) {}
 void launch_drift(const KP& p, double dt, cudaStream_t s) {
     if (p.n > 0) k_drift<<<grid(p.n, kBlock), kBlock, 0, s>>>(p, dt);
 }
