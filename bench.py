@@ -414,7 +414,8 @@ def run_ours(args):
                 "how": ("mvmm_upload_cells + mvmm_step + mvmm_download_cells per step" if batch else
                         "mvmm_step_cells per step (upload, step and download in one C call)") +
                        ", one pinned host block in the device field order, wall clock"},
-        "gpu_launches": args.steps * 7 * 1 + args.steps * 6,
+        # per step: predict, [compact], [prep32], face, update, gradients, limiter (timed for both forms)
+        "gpu_launches": args.steps * ((6 + 5) + (2 if (not batch and not problem.params.sync_all) else 0)),
         "clocks": clocks,
     }
     print(json.dumps(line))
