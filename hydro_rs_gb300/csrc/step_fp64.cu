@@ -279,13 +279,15 @@ __global__ void __launch_bounds__(kMaxBlock) k_compact(KP p) {
     const int n_act = (int)p.tl[0].n_alist;
     const unsigned int stamp = face_stamp_now(p);
     const int lane = threadIdx.x & 31;
-    for (int base = blockIdx.x * blockDim.x; base < n_act; base += gridDim.x * blockDim.x) {
-        int idx = base + threadIdx.x;
-        int i = idx < n_act ? p.cell_list[idx] : -1;
-        int k0 = i >= 0 ? p.csr_off[i] : 0;
-        int deg = i >= 0 ? p.csr_off[i + 1] - k0 : 0;
-        int max_deg = __reduce_max_sync(0xffffffffu, deg);  // warp-uniform trip count
-        for (int j = 0; j < max_deg; j++) {
+    // one warp per active cell, its lanes over the cell's faces: the face
+    // gathers of a cell are issued together instead of one after another
+    const int n_warps = (gridDim.x * blockDim.x) >> 5;
+    for (int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < n_act; w += n_warps) {
+        const int i = p.cell_list[w];
+        const int k0 = p.csr_off[i];
+        const int deg = p.csr_off[i + 1] - k0;
+        for (int j0 = 0; j0 < deg; j0 += 32) {  // warp-uniform
+            int j = j0 + lane;
             bool have = j < deg;
             int f = have ? p.csr_face[k0 + j] : 0;
             int o = -1;
@@ -366,6 +368,8 @@ __device__ __forceinline__ void sum2_add(Sum2& a, float x) {
 // ROWS32: the FP32-face form's step rows (FP32 dt * area * F, v_max,
 // a_over_r), summed per cell in FP32 two-sums and added to the FP64
 // accumulator once; otherwise the FP64 rows are folded in face order.
+__device__ __forceinline__ void update_finish(const KP& p, int i, int k, bool act, St<double> facc, double msv,
+                                              double maor, int do_c2p);
 template <bool ROWS32>
 __device__ __forceinline__ void update_cell(const KP& p, int i, int do_c2p) {
     const int k = inst_of(p, i);
@@ -415,6 +419,12 @@ __device__ __forceinline__ void update_cell(const KP& p, int i, int do_c2p) {
             }
         }
     }
+    update_finish(p, i, k, act, facc, msv, maor, do_c2p);
+}
+
+// Particle::apply_flux, kick2 and cons->prim of one cell once its faces are summed.
+__device__ __forceinline__ void update_finish(const KP& p, int i, int k, bool act, St<double> facc, double msv,
+                                              double maor, int do_c2p) {
     unsigned int err = 0;
     if (act) {
         p.fresh[i] = 0;  // prim (here), grad and v_rel (gradient stage) change
@@ -444,11 +454,92 @@ __device__ __forceinline__ void update_cell(const KP& p, int i, int do_c2p) {
     W5(p, F_FACC, i, facc);
     if (err) set_err(p, k, err);
 }
+// Hierarchical steps: a warp per listed cell.  The lanes gather the cell's
+// faces together, and every lane then folds them into the accumulator in CSR
+// order from the lanes' registers, so the sum is the one update_cell forms.
+template <bool ROWS32>
+__device__ __forceinline__ void update_cell_warp(const KP& p, int i, int do_c2p, int lane) {
+    const int k = inst_of(p, i);
+    if (p.tl[k].done) return;
+    const bool act = p.active[i] != 0;
+    St<double> facc = C5(p, F_FACC, i);
+    double msv = C(p, F_MSV, i), maor = C(p, F_MAOR, i);
+    const size_t nf = (size_t)p.nf;
+    const int k0 = p.csr_off[i], deg = p.csr_off[i + 1] - k0;
+    const unsigned int stamp = face_stamp_now(p);
+    const int rv = p.flux_rows == 10 ? 8 : 5;
+    Sum2 acc[5];
+#pragma unroll
+    for (int q = 0; q < 5; q++) acc[q] = {0.f, 0.f};
+    float vm32 = -INFINITY, ar32 = -INFINITY;
+    for (int j0 = 0; j0 < deg; j0 += 32) {  // warp-uniform
+        const int j = j0 + lane;
+        int use = 0, lft = 0;
+        double x[7];
+#pragma unroll
+        for (int q = 0; q < 7; q++) x[q] = 0.;
+        if (j < deg) {
+            int f = p.csr_face[k0 + j];
+            use = p.face_stamp[f] == stamp;
+            if (use) {
+                lft = p.left[f] == i;
+                if (ROWS32) {
+#pragma unroll
+                    for (int q = 0; q < 7; q++) x[q] = (double)p.flux32[q * nf + f];
+                } else {
+#pragma unroll
+                    for (int q = 0; q < 5; q++) x[q] = p.flux[q * nf + f];
+                    x[5] = p.flux[rv * nf + f];
+                    x[6] = p.flux[(rv + 1) * nf + f];
+                }
+            }
+        }
+        const int n = min(32, deg - j0);
+        for (int t = 0; t < n; t++) {
+            if (!__shfl_sync(0xffffffffu, use, t)) continue;  // warp-uniform
+            const bool lt = __shfl_sync(0xffffffffu, lft, t) != 0;
+            St<double> y;
+#pragma unroll
+            for (int q = 0; q < 5; q++) y.q[q] = __shfl_sync(0xffffffffu, x[q], t);
+            const double vm = __shfl_sync(0xffffffffu, x[5], t), ar = __shfl_sync(0xffffffffu, x[6], t);
+            if (ROWS32) {
+                const float sg = lt ? -1.f : 1.f;
+#pragma unroll
+                for (int q = 0; q < 5; q++) sum2_add(acc[q], sg * (float)y.q[q]);
+                vm32 = fmaxf(vm32, (float)vm);
+                ar32 = fmaxf(ar32, (float)ar);
+            } else {
+                if (lt) facc = facc - y;  // update_fluxes_left (part.rs:160-167)
+                else facc = facc + y;     // update_fluxes_right (part.rs:169-176)
+                if (act) {
+                    msv = m_max(vm, msv);
+                    maor = m_max(maor, ar);
+                }
+            }
+        }
+    }
+    if (ROWS32) {
+#pragma unroll
+        for (int q = 0; q < 5; q++) facc.q[q] = facc.q[q] + ((double)acc[q].hi + (double)acc[q].lo);
+        if (act && deg > 0) {
+            msv = m_max((double)vm32, msv);
+            maor = m_max(maor, (double)ar32);
+        }
+    }
+    if (lane == 0) update_finish(p, i, k, act, facc, msv, maor, do_c2p);
+}
+
 template <bool ROWS32>
 __global__ void __launch_bounds__(kMaxBlock) k_update(KP p, int do_c2p) {
     const int n_items = cell_items(p);
-    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n_items; idx += gridDim.x * blockDim.x)
-        update_cell<ROWS32>(p, cell_at(p, idx), do_c2p);
+    if (p.use_list) {
+        const int lane = threadIdx.x & 31, n_warps = (gridDim.x * blockDim.x) >> 5;
+        for (int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < n_items; w += n_warps)
+            update_cell_warp<ROWS32>(p, p.cell_list[w], do_c2p, lane);
+    } else {
+        for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n_items; idx += gridDim.x * blockDim.x)
+            update_cell<ROWS32>(p, cell_at(p, idx), do_c2p);
+    }
 }
 
 __global__ void __launch_bounds__(kMaxBlock) k_c2p(KP p) {
@@ -605,31 +696,29 @@ __global__ void __launch_bounds__(kMaxBlock) k_timesteps(KP p, double* out) {
 // timestep_sync or timestep_limiter (runner/hydrodynamics.rs:160-191) with
 // Particle::timestep_limit (part.rs:263-297); then reset_extrapolations and
 // kick1 (runner/hydrodynamics.rs:41-49, 193-195).
-__device__ __forceinline__ void limit_cell(const KP& p, int i) {
+// The neighbour wake-up bin of timestep_limiter (runner/hydrodynamics.rs:165-184):
+// the smallest new bin of an active neighbour plus the allowed difference.
+__device__ __forceinline__ int face_wakeup(const KP& p, int i, int f) {
+    int l = p.left[f], r = p.right[f];
+    int o = i == l ? r : l;
+    if (o < 0 || !p.active[o]) return 1 << 20;
+    return (int)p.tb_tmp[o] + TIME_BIN_NEIGHBOUR_MAX_DELTA_BIN;
+}
+// wakeup < 0: computed here (one thread per cell); else given (warp per cell)
+__device__ __forceinline__ void limit_cell(const KP& p, int i, int wakeup = -1) {
     if (p.use_list) p.touch[i] = 0;  // the last stage that reads the cell list
     const int k = inst_of(p, i);
     if (p.tl[k].done) return;
     const double time_base = tbase(p, k);
     int tb = p.tb_tmp[i];
-    int wakeup;
     if (p.sync_all) {
         wakeup = p.tl[k].min_timebin;
-    } else {
+    } else if (wakeup < 0) {
         wakeup = tb;
         int k0 = p.csr_off[i], k1 = p.csr_off[i + 1];
-        for (int k = k0; k < k1; k++) {
-            int f = p.csr_face[k];
-            int l = p.left[f], r = p.right[f];
-            int o;
-            if (i == l) {
-                if (r < 0) continue;
-                o = r;
-            } else {
-                o = l;
-            }
-            if (!p.active[o]) continue;
-            wakeup = min(wakeup, (int)p.tb_tmp[o] + TIME_BIN_NEIGHBOUR_MAX_DELTA_BIN);
-        }
+        for (int k = k0; k < k1; k++) wakeup = min(wakeup, face_wakeup(p, i, p.csr_face[k]));
+    } else {
+        wakeup = min(wakeup, tb);
     }
     if (wakeup < tb) {
         unsigned long long tc = p.tl[k].ti_current;
@@ -668,8 +757,22 @@ __device__ __forceinline__ void limit_cell(const KP& p, int i) {
 __device__ __forceinline__ void end_instance(const KP& p, int k);
 __global__ void __launch_bounds__(kMaxBlock) k_limit(KP p) {
     const int n_items = cell_items(p);
-    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n_items; idx += gridDim.x * blockDim.x)
-        limit_cell(p, cell_at(p, idx));
+    if (p.use_list && !p.sync_all) {
+        // hierarchical step: a warp per listed cell, its lanes over the faces,
+        // the wake-up bin reduced across the warp (an integer minimum)
+        const int lane = threadIdx.x & 31, n_warps = (gridDim.x * blockDim.x) >> 5;
+        for (int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < n_items; w += n_warps) {
+            const int i = p.cell_list[w];
+            const int k0 = p.csr_off[i], deg = p.csr_off[i + 1] - k0;
+            int wake = 1 << 20;
+            for (int j = lane; j < deg; j += 32) wake = min(wake, face_wakeup(p, i, p.csr_face[k0 + j]));
+            wake = __reduce_min_sync(0xffffffffu, wake);
+            if (lane == 0) limit_cell(p, i, wake);
+        }
+    } else {
+        for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n_items; idx += gridDim.x * blockDim.x)
+            limit_cell(p, cell_at(p, idx));
+    }
     // the last block to finish does the engine's bookkeeping of the step
     // (end_instance); no cell data is read there, only the timelines
     __shared__ bool last;
