@@ -372,8 +372,134 @@ __device__ __forceinline__ void gradients32_cell(const KP& p, int i) {
     if (err) set_err(p, k, err);
     inst_min_dti_tb(p, k, my_dti, my_tb);
 }
+// Hierarchical steps: a warp per listed cell (lanes over the faces, the WLS
+// sums folded in CSR order from the lanes' registers, the limiter's minima and
+// maxima reduced across the warp), as gradients_cell_warp in the plain form.
+__device__ __forceinline__ void gradients32_cell_warp(const KP& p, int i, int lane) {
+    unsigned long long my_dti = MAX_NR_TIMESTEPS;
+    int my_tb = 127;
+    unsigned int err = 0;
+    int k = inst_of(p, i);
+    if (p.tl[k].done) k = -1;
+    if (k >= 0) {
+        int tb = p.timebin[i];
+        if (p.active[i]) {
+          if (!p.godunov) {
+            St<float> prim = G5(p, G_PRIM, i);
+            float a00 = 0.f, a01 = 0.f, a02 = 0.f, a11 = 0.f, a12 = 0.f, a22 = 0.f;
+            if (p.dim == 1) { a11 = 1.f; a22 = 1.f; }
+            else if (p.dim == 2) { a22 = 1.f; }
+            V3<float> gr[5];
+#pragma unroll
+            for (int q = 0; q < 5; q++) gr[q] = v3(0.f, 0.f, 0.f);
+            const int k0 = p.csr_off[i], deg = p.csr_off[i + 1] - k0;
+            for (int j0 = 0; j0 < deg; j0 += 32) {  // warp-uniform
+                float w = 0.f, dq[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+                V3<float> ds = v3(0.f, 0.f, 0.f);
+                if (j0 + lane < deg) {
+                    int f = p.csr_face[k0 + j0 + lane];
+                    St<float> op;
+                    V3<float> d;
+                    other_side32(p, i, f, prim, op, ds, d);
+                    w = p.geo[GE_W * (size_t)p.nf + f];
+#pragma unroll
+                    for (int q = 0; q < 5; q++) dq[q] = op.q[q] - prim.q[q];
+                }
+                const int n = min(32, deg - j0);
+                for (int t = 0; t < n; t++) {
+                    const float wt = __shfl_sync(0xffffffffu, w, t);
+                    const V3<float> dst = v3(__shfl_sync(0xffffffffu, ds.x, t), __shfl_sync(0xffffffffu, ds.y, t),
+                                             __shfl_sync(0xffffffffu, ds.z, t));
+#pragma unroll
+                    for (int q = 0; q < 5; q++) gr[q] = gr[q] + (wt * __shfl_sync(0xffffffffu, dq[q], t)) * dst;
+                    a00 += wt * dst.x * dst.x;
+                    a01 += wt * dst.x * dst.y;
+                    a02 += wt * dst.x * dst.z;
+                    a11 += wt * dst.y * dst.y;
+                    a12 += wt * dst.y * dst.z;
+                    a22 += wt * dst.z * dst.z;
+                }
+            }
+            V3<float> m0 = v3(a00, a01, a02), m1 = v3(a01, a11, a12), m2 = v3(a02, a12, a22);
+            V3<float> t0 = cross(m1, m2), t1 = cross(m2, m0), t2 = cross(m0, m1);
+            float inv_det = 1.f / dot(m2, t2);
+            V3<float> r0 = inv_det * t0, r1 = inv_det * t1, r2 = inv_det * t2;
+            bool finite = true;
+#pragma unroll
+            for (int q = 0; q < 5; q++) {
+                V3<float> x = gr[q];
+                gr[q] = v3(dot(r0, x), dot(r1, x), dot(r2, x));
+                finite = finite && isfinite(gr[q].x) && isfinite(gr[q].y) && isfinite(gr[q].z);
+            }
+            if (!finite) {
+#pragma unroll
+                for (int q = 0; q < 5; q++) gr[q] = v3(0.f, 0.f, 0.f);
+            }
+            float dmn[5], dmx[5], emn[5], emx[5];
+#pragma unroll
+            for (int q = 0; q < 5; q++) {
+                dmn[q] = 0.f;
+                dmx[q] = 0.f;
+                emn[q] = INFINITY;
+                emx[q] = -INFINITY;
+            }
+            for (int j = lane; j < deg; j += 32) {
+                int f = p.csr_face[k0 + j];
+                St<float> op;
+                V3<float> ds, d;
+                other_side32(p, i, f, prim, op, ds, d);
+#pragma unroll
+                for (int q = 0; q < 5; q++) {
+                    float ex = dot(gr[q], d);
+                    float dq = op.q[q] - prim.q[q];
+                    dmn[q] = fminf(dmn[q], dq);
+                    dmx[q] = fmaxf(dmx[q], dq);
+                    emn[q] = fminf(emn[q], ex);
+                    emx[q] = fmaxf(emx[q], ex);
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < 5; q++) {
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    dmn[q] = fminf(dmn[q], __shfl_xor_sync(0xffffffffu, dmn[q], o));
+                    dmx[q] = fmaxf(dmx[q], __shfl_xor_sync(0xffffffffu, dmx[q], o));
+                    emn[q] = fminf(emn[q], __shfl_xor_sync(0xffffffffu, emn[q], o));
+                    emx[q] = fmaxf(emx[q], __shfl_xor_sync(0xffffffffu, emx[q], o));
+                }
+                float alpha = (emx[q] == 0.f || emn[q] == 0.f) ? 1.f : fminf(1.f, fminf(dmx[q] / emx[q], dmn[q] / emn[q]));
+                gr[q] = alpha * gr[q];
+                if (lane == 0) W3(p, F_GRAD + 3 * q, i, cvt<double>(gr[q]));
+            }
+            if (lane == 0) W3(p, F_GC, i, C3(p, F_CEN, i));
+          }
+            if (lane == 0) {
+                double dt_new = particle_timestep(p, i);
+                unsigned long long tc = p.tl[k].ti_current;
+                unsigned long long dti = make_integer_timestep(dt_new, tb, NUM_TIME_BINS, tc, tbase_inv(p, k));
+                if (dti == 0) err |= 1u << 6;
+                W(p, F_DT, i, (double)dti * tbase(p, k));
+                tb = get_time_bin(dti);
+                my_dti = dti;
+            }
+        }
+        if (lane == 0) {
+            p.tb_tmp[i] = (int8_t)tb;
+            my_tb = tb;
+        }
+    }
+    if (err) set_err(p, k, err);
+    inst_min_dti_tb(p, lane == 0 ? k : -1, my_dti, my_tb);
+}
+
 __global__ void __launch_bounds__(kMaxBlock, GRAD32_MINB) k_gradients32(KP p) {
     const int n_items = cell_items(p);
+    if (p.use_list) {
+        const int lane = threadIdx.x & 31, n_warps = (gridDim.x * blockDim.x) >> 5;
+        for (int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < n_items; w += n_warps)
+            gradients32_cell_warp(p, p.cell_list[w], lane);
+        return;
+    }
     // warp-uniform trip count: the per-instance reductions need every lane
     for (int base = blockIdx.x * blockDim.x; base < n_items; base += gridDim.x * blockDim.x) {
         int idx = base + threadIdx.x;

@@ -676,8 +676,159 @@ __device__ __forceinline__ void gradients_cell(const KP& p, int i, int do_timest
     if (!do_timestep) return;
     inst_min_dti_tb(p, k, my_dti, my_tb);
 }
+__device__ __forceinline__ double warp_min_d(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = m_min(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ double warp_max_d(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = m_max(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// Hierarchical steps: a warp per listed cell.  The lanes gather the cell's
+// faces together; the WLS sums are folded in CSR order from the lanes'
+// registers (the sums gradients_cell forms, bit for bit), and the limiter's
+// minima and maxima are warp reductions (fmin / fmax do not depend on order).
+__device__ __forceinline__ void gradients_cell_warp(const KP& p, int i, int do_timestep, int lane) {
+    unsigned long long my_dti = MAX_NR_TIMESTEPS;
+    int my_tb = 127;
+    unsigned int err = 0;
+    int k = inst_of(p, i);
+    if (p.tl[k].done) k = -1;
+    if (k >= 0) {
+        int tb = p.timebin[i];
+        if (p.active[i]) {
+          if (!p.godunov) {
+            V3<double> cen = C3(p, F_CEN, i);
+            St<double> prim = C5(p, F_PRIM, i);
+            double a00 = 0., a01 = 0., a02 = 0., a11 = 0., a12 = 0., a22 = 0.;
+            if (p.dim == 1) { a11 = 1.; a22 = 1.; }
+            else if (p.dim == 2) { a22 = 1.; }
+            V3<double> gr[5];
+#pragma unroll
+            for (int q = 0; q < 5; q++) gr[q] = v3(0., 0., 0.);
+            const int k0 = p.csr_off[i], deg = p.csr_off[i + 1] - k0;
+            for (int j0 = 0; j0 < deg; j0 += 32) {  // warp-uniform
+                double w = 0., dq[5] = {0., 0., 0., 0., 0.};
+                V3<double> ds = v3(0., 0., 0.);
+                if (j0 + lane < deg) {
+                    int f = p.csr_face[k0 + j0 + lane];
+                    St<double> op;
+                    V3<double> oc, sh;
+                    other_side(p, i, f, prim, cen, op, oc, sh);
+                    ds = (oc + sh) - cen;
+                    w = p.area[f] / len2(ds);
+#pragma unroll
+                    for (int q = 0; q < 5; q++) dq[q] = op.q[q] - prim.q[q];
+                }
+                const int n = min(32, deg - j0);
+                for (int t = 0; t < n; t++) {  // GradientData::collect in CSR order
+                    const double wt = __shfl_sync(0xffffffffu, w, t);
+                    const V3<double> dst = v3(__shfl_sync(0xffffffffu, ds.x, t), __shfl_sync(0xffffffffu, ds.y, t),
+                                              __shfl_sync(0xffffffffu, ds.z, t));
+                    const bool z = dst.z != 0.;
+#pragma unroll
+                    for (int q = 0; q < 5; q++) {
+                        double wdq = wt * __shfl_sync(0xffffffffu, dq[q], t);
+                        gr[q].x = gr[q].x + wdq * dst.x;
+                        gr[q].y = gr[q].y + wdq * dst.y;
+                        if (z) gr[q].z = gr[q].z + wdq * dst.z;
+                    }
+                    a00 = a00 + wt * (dst.x * dst.x);
+                    a01 = a01 + wt * (dst.x * dst.y);
+                    a11 = a11 + wt * (dst.y * dst.y);
+                    if (z) {
+                        a02 = a02 + wt * (dst.x * dst.z);
+                        a12 = a12 + wt * (dst.y * dst.z);
+                        a22 = a22 + wt * (dst.z * dst.z);
+                    }
+                }
+            }
+            V3<double> m0 = v3(a00, a01, a02), m1 = v3(a01, a11, a12), m2 = v3(a02, a12, a22);
+            V3<double> t0 = cross(m1, m2), t1 = cross(m2, m0), t2 = cross(m0, m1);
+            double det = dot(m2, t2);
+            double inv_det = 1.0 / det;
+            V3<double> r0 = inv_det * t0, r1 = inv_det * t1, r2 = inv_det * t2;
+            V3<double> c0 = v3(r0.x, r1.x, r2.x), c1 = v3(r0.y, r1.y, r2.y), c2 = v3(r0.z, r1.z, r2.z);
+            bool finite = true;
+#pragma unroll
+            for (int q = 0; q < 5; q++) {
+                V3<double> x = gr[q];
+                V3<double> res = x.x * c0;
+                res = res + x.y * c1;
+                res = res + x.z * c2;
+                gr[q] = res;
+                finite = finite && isfinite(res.x) && isfinite(res.y) && isfinite(res.z);
+            }
+            if (!finite) {
+#pragma unroll
+                for (int q = 0; q < 5; q++) gr[q] = v3(0., 0., 0.);
+            }
+            St<double> mn = prim, mx = prim, emn, emx;
+#pragma unroll
+            for (int q = 0; q < 5; q++) {
+                emn.q[q] = INFINITY;
+                emx.q[q] = -INFINITY;
+            }
+            for (int j = lane; j < deg; j += 32) {
+                int f = p.csr_face[k0 + j];
+                St<double> op;
+                V3<double> oc, sh;
+                other_side(p, i, f, prim, cen, op, oc, sh);
+                V3<double> d = (F3(p.fcen, p.nf, f) - cen) - sh;
+#pragma unroll
+                for (int q = 0; q < 5; q++) {
+                    double ex = dot(gr[q], d);
+                    mn.q[q] = m_min(mn.q[q], op.q[q]);
+                    mx.q[q] = m_max(mx.q[q], op.q[q]);
+                    emn.q[q] = m_min(emn.q[q], ex);
+                    emx.q[q] = m_max(emx.q[q], ex);
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < 5; q++) {
+                mn.q[q] = warp_min_d(mn.q[q]);
+                mx.q[q] = warp_max_d(mx.q[q]);
+                emn.q[q] = warp_min_d(emn.q[q]);
+                emx.q[q] = warp_max_d(emx.q[q]);
+                double d_max = mx.q[q] - prim.q[q];
+                double d_min = mn.q[q] - prim.q[q];
+                double alpha = (emx.q[q] == 0. || emn.q[q] == 0.) ? 1. : m_min(1.0, m_min(d_max / emx.q[q], d_min / emn.q[q]));
+                gr[q] = alpha * gr[q];
+                if (lane == 0) W3(p, F_GRAD + 3 * q, i, gr[q]);
+            }
+            if (lane == 0) W3(p, F_GC, i, cen);  // gradient_apply
+          }
+            if (do_timestep && lane == 0) {
+                double dt_new = particle_timestep(p, i);
+                unsigned long long tc = p.tl[k].ti_current;
+                unsigned long long dti = make_integer_timestep(dt_new, tb, NUM_TIME_BINS, tc, tbase_inv(p, k));
+                if (dti == 0) err |= 1u << 6;
+                W(p, F_DT, i, (double)dti * tbase(p, k));  // Particle::set_timestep
+                tb = get_time_bin(dti);
+                my_dti = dti;
+            }
+        }
+        if (do_timestep && lane == 0) {
+            p.tb_tmp[i] = (int8_t)tb;
+            my_tb = tb;
+        }
+    }
+    if (err) set_err(p, k, err);
+    if (!do_timestep) return;
+    inst_min_dti_tb(p, lane == 0 ? k : -1, my_dti, my_tb);
+}
+
 __global__ void __launch_bounds__(kMaxBlock) k_gradients(KP p, int do_timestep) {
     const int n_items = cell_items(p);
+    if (p.use_list) {
+        const int lane = threadIdx.x & 31, n_warps = (gridDim.x * blockDim.x) >> 5;
+        for (int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < n_items; w += n_warps)
+            gradients_cell_warp(p, p.cell_list[w], do_timestep, lane);
+        return;
+    }
     // warp-uniform trip count: the per-instance reductions need every lane
     for (int base = blockIdx.x * blockDim.x; base < n_items; base += gridDim.x * blockDim.x) {
         int idx = base + threadIdx.x;
