@@ -22,7 +22,7 @@ void launch_riemann_fp64(int kind, int sample, double gamma, int64_t n, const do
                          cudaStream_t s);
 void launch_face_flux_fp32(const KP& p, int solver, cudaStream_t s);
 void launch_gradients32(const KP& p, cudaStream_t s);
-void launch_geom32(const KP& p, cudaStream_t s);
+void launch_geom32(const KP& p, bool check, cudaStream_t s);
 void launch_riemann_fp32(int kind, int sample, double gamma, int64_t n, const double* l, const double* r,
                          const double* vf, const double* nrm, double* out, unsigned int* err, const RSx& x,
                          cudaStream_t s);
@@ -60,6 +60,9 @@ struct mvmm_ctx {
     double* flux = nullptr;
     float* flux32 = nullptr;
     float* geo = nullptr;
+    unsigned long long* geo_pos = nullptr;  // FP32 form: loc and centroid bits of the last geometry build
+    uint8_t* geo_changed = nullptr;
+    bool geo_built = false;  // the FP32 geometry matches the current face arrays
     double* dtmp = nullptr;
     int n_inst = 1;
     int* inst = nullptr;       // per-cell instance (batches only)
@@ -85,11 +88,13 @@ struct mvmm_ctx {
     bool prof = false;
     cudaEvent_t ev[MVMM_NUM_KERNELS + 1] = {};
     cudaStream_t side = nullptr;              // copies of mvmm_step_cells that overlap the step
-    cudaEvent_t ev_face = nullptr, ev_in = nullptr, ev_upd = nullptr, ev_grad = nullptr, ev_out = nullptr;
+    cudaEvent_t ev_pred = nullptr, ev_in = nullptr, ev_upd = nullptr, ev_grad = nullptr, ev_out = nullptr;
     double prof_ms[MVMM_NUM_KERNELS] = {};
     int64_t prof_n[MVMM_NUM_KERNELS] = {};
     double time_base = 0, time_base_inv = 0;
     uint32_t err_bits = 0;
+    int device = 0, n_sms = 1;
+    bool pageable_access = false;  // the device reads and writes pageable host memory
 };
 
 namespace {
@@ -135,6 +140,8 @@ KP make_kp(mvmm_ctx* c, int stage, int flux_rows) {
     p.flux = c->flux;
     p.flux32 = c->flux32;
     p.geo = c->geo;
+    p.geo_pos = c->geo_pos;
+    p.geo_changed = c->geo_changed;
     p.fp32 = c->prm.precision == MVMM_PRECISION_FP32FACE ? 1 : 0;
     p.flux_rows = flux_rows;
     p.tl = c->tl;
@@ -183,6 +190,16 @@ KP make_kp(mvmm_ctx* c, int stage, int flux_rows) {
     return p;
 }
 
+// Brings the FP32 face geometry up to date with the cells' positions and
+// centroids.  A fixed mesh whose geometry was built before rebuilds only the
+// faces of cells whose loc or centroid bits changed; a moving mesh (whose
+// face arrays change) and the first build rebuild every face.
+void update_geom32(mvmm_ctx* c, const KP& p, cudaStream_t s) {
+    if (c->prm.precision != MVMM_PRECISION_FP32FACE) return;
+    launch_geom32(p, c->geo_built && c->prm.particle_motion == MVMM_MOTION_FIXED, s);
+    c->geo_built = true;
+}
+
 void launch_face(mvmm_ctx* c, const KP& p) {
     if (c->prm.precision == MVMM_PRECISION_FP32FACE) {
         launch_prep32(p, c->stream);
@@ -193,12 +210,12 @@ void launch_face(mvmm_ctx* c, const KP& p) {
 }
 
 // The six kernels of one OptimalOrderRunner step, optionally bracketed by events.
-// Copies that overlap a step (mvmm_step_cells): events the step waits for
-// before its face stage and before its update, events it records after the
-// update and after the gradient stage, and the FP32 geometry refresh once the
-// positions have arrived.
+// A step on cells uploaded with it (mvmm_step_cells): predict recomputes every
+// derived row, the FP32 geometry follows the uploaded positions, the update
+// waits for an event (the rows only it reads), and events are recorded after
+// the update and after the gradient stage for the copies back.
 struct StepHooks {
-    cudaEvent_t wait_before_face = nullptr;
+    bool stale_all = false;
     bool geom_before_face = false;
     cudaEvent_t wait_before_update = nullptr;
     cudaEvent_t after_update = nullptr;
@@ -207,14 +224,13 @@ struct StepHooks {
 
 void enqueue_step_kernels(mvmm_ctx* c, bool with_events, const StepHooks& h = StepHooks()) {
     KP p = make_kp(c, 0, 7);
+    p.stale_all = h.stale_all ? 1 : 0;
     cudaStream_t s = c->stream;
     if (with_events) cudaEventRecord(c->ev[0], s);
     launch_predict(p, s);
     if (c->pending_geometry) launch_geometry(p, s);  // after predict, as volume_calculation
-    if (h.wait_before_face) cudaStreamWaitEvent(s, h.wait_before_face, 0);
-    if ((h.geom_before_face || c->prm.particle_motion != MVMM_MOTION_FIXED) &&
-        c->prm.precision == MVMM_PRECISION_FP32FACE)
-        launch_geom32(p, s);  // generators drifted or uploaded, centroids updated
+    if (h.geom_before_face || c->prm.particle_motion != MVMM_MOTION_FIXED)
+        update_geom32(c, p, s);  // generators drifted or uploaded, centroids updated
     if (p.use_list) launch_compact(p, s);
     if (with_events) cudaEventRecord(c->ev[1], s);
     launch_face(c, p);
@@ -432,6 +448,8 @@ static int create_impl(const mvmm_params* prm, const mvmm_mesh* m, int64_t n_ins
         ALLOC(c->cf, (size_t)kCellFields32 * n * 4);
         ALLOC(c->flux32, 7 * nf * 4);
         ALLOC(c->geo, (size_t)kFaceGeom32 * nf * 4);
+        ALLOC(c->geo_pos, 6 * n * 8);
+        ALLOC(c->geo_changed, n);
     }
     ALLOC(c->timebin, n);
     ALLOC(c->tb_tmp, n);
@@ -457,6 +475,14 @@ static int create_impl(const mvmm_params* prm, const mvmm_mesh* m, int64_t n_ins
         return cleanup(MVMM_E_CUDA, "cudaStreamCreate failed");
     c->own_stream = true;
     for (int k = 0; k <= MVMM_NUM_KERNELS; k++) cudaEventCreate(&c->ev[k]);
+    {
+        int pa = 0;
+        if (cudaGetDevice(&c->device) != cudaSuccess ||
+            cudaDeviceGetAttribute(&c->n_sms, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess ||
+            cudaDeviceGetAttribute(&pa, cudaDevAttrPageableMemoryAccess, c->device) != cudaSuccess)
+            return cleanup(MVMM_E_CUDA, "device query failed");
+        c->pageable_access = pa != 0;
+    }
     cudaStream_t s = c->stream;
     if (c->nf > 0) {
         cudaMemcpyAsync(c->left, m->left, nf * 4, cudaMemcpyHostToDevice, s);
@@ -538,7 +564,7 @@ int mvmm_ctx_destroy(mvmm_ctx* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->step_exec) cudaGraphExecDestroy(c->step_exec);
     void* ptrs[] = {c->left, c->right, c->csr_off, c->csr_face, c->area, c->normal, c->fcen, c->shift, c->cd,
-                    c->cf, c->timebin, c->tb_tmp, c->active, c->flux, c->flux32, c->geo, c->dtmp, c->face_stamp, c->touch, c->blocks_done, c->cell_list, c->fresh,
+                    c->cf, c->timebin, c->tb_tmp, c->active, c->flux, c->flux32, c->geo, c->geo_pos, c->geo_changed, c->dtmp, c->face_stamp, c->touch, c->blocks_done, c->cell_list, c->fresh,
                     c->pend_vol, c->pend_cen,
                     c->face_list, c->tl,
                     c->inst, c->inst_tb, c->inst_tbi};
@@ -549,7 +575,7 @@ int mvmm_ctx_destroy(mvmm_ctx* c) {
         if (c->ev[k]) cudaEventDestroy(c->ev[k]);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     if (c->side) cudaStreamDestroy(c->side);
-    for (cudaEvent_t e : {c->ev_face, c->ev_in, c->ev_upd, c->ev_grad, c->ev_out})
+    for (cudaEvent_t e : {c->ev_pred, c->ev_in, c->ev_upd, c->ev_grad, c->ev_out})
         if (e) cudaEventDestroy(e);
     delete c;
     return MVMM_OK;
@@ -584,11 +610,15 @@ constexpr unsigned kAllRows = 0x3fffu;
 // mvmm_step_cells moves the rows in three groups each way, each as soon as the
 // step can use it or has finished with it.
 constexpr unsigned kRowsPredictIn = 0x0416u;  // prim, grad, extrap, v_rel (+ timebin): what predict reads
-constexpr unsigned kRowsFaceIn = 0x23C8u;     // gc, volume, loc, centroid, v, dt: read from the face stage on
-constexpr unsigned kRowsLateIn = 0x1821u;     // cons, facc, max_a_over_r, max_signal_velocity: from the update on
+constexpr unsigned kRowsFaceIn = 0x2388u;     // gc, loc, centroid, v, dt: read from the face stage on
+constexpr unsigned kRowsLateIn = 0x1861u;     // cons, facc, volume, max_a_over_r, max_signal_velocity: from the update on
 constexpr unsigned kRowsEarlyOut = 0x0023u;   // cons, prim, facc: final once the update has run
 constexpr unsigned kRowsMidOut = 0x1E0Cu;     // grad, gc, v, v_rel, max_a_over_r, max_signal_velocity: after gradients
-constexpr unsigned kRowsLateOut = 0x21D0u;    // extrap, volume, loc, centroid, dt (+ timebin): after the limiter
+constexpr unsigned kRowsLateOut = 0x2010u;    // extrap, dt (+ timebin): after the limiter
+// volume, loc, centroid: a step of a fixed mesh reads them and never writes them
+// (the geometry only changes through mvmm_drift / mvmm_set_mesh, which take
+// moving meshes, and mvmm_step_cells steps fixed ones)
+constexpr unsigned kRowsPassThrough = 0x01C0u;
 int row_map(const mvmm_cells* h, unsigned subset, RowCopy* out, size_t* m) {
     const RowCopy all[14] = {{h->cons, F_CONS, 5},         {h->prim, F_PRIM, 5},     {h->grad, F_GRAD, 15},
                              {h->gc, F_GC, 3},             {h->extrap, F_EXTRAP, 5}, {h->facc, F_FACC, 5},
@@ -603,38 +633,154 @@ int row_map(const mvmm_cells* h, unsigned subset, RowCopy* out, size_t* m) {
     if (!h->timebin) return fail(MVMM_E_INVALID, "null timebin");
     return MVMM_OK;
 }
+// Host <-> device transfers of cell rows.  A cudaMemcpyAsync costs a few
+// microseconds of copy-engine setup on top of its bytes (and from pageable
+// memory runs at well under the link's rate), and a row group is up to a dozen
+// separate host arrays, so a group can move in ONE kernel that loads (or
+// stores) the host rows through their device-visible address: the mapping of
+// pinned memory, or the host address itself where the device reads pageable
+// memory through the host page tables.  That kernel holds SM slots for the
+// whole transfer, so pinned rows whose copy overlaps the step's kernels go by
+// the copy engines instead.  Host arrays the device cannot address always go
+// by cudaMemcpyAsync.
+struct Xfer {
+    const char* src;
+    char* dst;
+    long long bytes;
+};
+constexpr int kMaxXfer = 16;
+constexpr long long kXferChunk = 32768;  // bytes a block moves per iteration
+struct XferSet {
+    Xfer x[kMaxXfer];
+    long long chunk_off[kMaxXfer + 1];  // prefix sums of the transfers' chunk counts
+    int m;
+};
+
+// Each block walks whole chunks; a chunk moves in 16-byte units where both
+// addresses and its length allow, else in 8-byte units, else bytes.  Four
+// loads in flight per thread cover the link's latency.
+template <typename U>
+__device__ __forceinline__ void xfer_units(const U* __restrict__ s, U* __restrict__ d, long long nv) {
+    for (long long k0 = threadIdx.x; k0 < nv; k0 += 4 * (long long)blockDim.x) {
+        U v[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const long long k = k0 + (long long)u * blockDim.x;
+            if (k < nv) v[u] = s[k];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const long long k = k0 + (long long)u * blockDim.x;
+            if (k < nv) d[k] = v[u];
+        }
+    }
+}
+__global__ void __launch_bounds__(128) k_xfer(XferSet t) {
+    const long long total = t.chunk_off[t.m];
+    for (long long ch = blockIdx.x; ch < total; ch += gridDim.x) {
+        int j = 0;
+        while (j + 1 < t.m && t.chunk_off[j + 1] <= ch) j++;
+        const long long b0 = (ch - t.chunk_off[j]) * kXferChunk;
+        const long long len = t.x[j].bytes - b0 < kXferChunk ? t.x[j].bytes - b0 : kXferChunk;
+        const char* src = t.x[j].src + b0;
+        char* dst = t.x[j].dst + b0;
+        const unsigned long long a = (unsigned long long)(uintptr_t)src | (uintptr_t)dst | (unsigned long long)len;
+        if ((a & 15) == 0) xfer_units((const uint4*)src, (uint4*)dst, len >> 4);
+        else if ((a & 7) == 0) xfer_units((const unsigned long long*)src, (unsigned long long*)dst, len >> 3);
+        else xfer_units(src, dst, len);
+    }
+}
+
+// The address at which the device reaches host array p, or null; *pinned:
+// page-locked host memory (which the copy engines move at the link's rate).
+const void* device_view(mvmm_ctx* c, const void* p, bool* pinned) {
+    *pinned = false;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    switch (a.type) {
+        case cudaMemoryTypeHost:  // pinned / registered: mapped on a UVA system
+            *pinned = true;
+            return a.devicePointer;
+        case cudaMemoryTypeDevice:
+        case cudaMemoryTypeManaged:
+            return a.device == c->device ? a.devicePointer : nullptr;
+        default:  // unregistered (pageable)
+            return c->pageable_access ? p : nullptr;
+    }
+}
+
+// Moves m (host array, device row) pairs on stream s: in one kernel, except
+// pairs whose host array the device cannot address and, with overlap (the
+// copy runs beside the step's kernels), pairs in pinned memory, which go by
+// cudaMemcpyAsync.
+int transfer(mvmm_ctx* c, const Xfer* pairs, int m, bool h2d, bool overlap, cudaStream_t s) {
+    XferSet t{};
+    t.m = 0;
+    long long chunks = 0;
+    for (int k = 0; k < m; k++) {
+        const Xfer& x = pairs[k];
+        if (x.bytes <= 0) continue;
+        const char* host = h2d ? x.src : (const char*)x.dst;
+        bool pinned = false, pinned_end = false;
+        const char* view = (const char*)device_view(c, host, &pinned);
+        // rows merged from separate arrays must lie in one mapping
+        if (view && (const char*)device_view(c, host + x.bytes - 1, &pinned_end) != view + x.bytes - 1)
+            view = nullptr;
+        if (!view || (overlap && pinned)) {
+            CUDA_TRY(cudaMemcpyAsync(x.dst, x.src, (size_t)x.bytes,
+                                     h2d ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost, s));
+            continue;
+        }
+        Xfer v = x;
+        if (h2d) v.src = (const char*)view;
+        else v.dst = (char*)view;
+        t.x[t.m] = v;
+        t.chunk_off[t.m] = chunks;
+        chunks += (x.bytes + kXferChunk - 1) / kXferChunk;
+        t.m++;
+    }
+    if (t.m == 0) return MVMM_OK;
+    t.chunk_off[t.m] = chunks;
+    const long long cap = 4LL * c->n_sms;
+    k_xfer<<<(unsigned)(chunks < cap ? chunks : cap), 128, 0, s>>>(t);
+    CUDA_TRY(cudaGetLastError());
+    return MVMM_OK;
+}
+
 // Copies rows between the host arrays and the device block; rows that lie
-// back to back on the host in the device's field order go in one copy (a
-// packed host block in that order takes a single copy).
-int copy_rows(mvmm_ctx* c, const RowCopy* map, size_t m, cudaMemcpyKind kind, cudaStream_t s) {
+// back to back on the host in the device's field order form one transfer.
+int copy_rows(mvmm_ctx* c, const RowCopy* map, size_t m, bool timebin, int8_t* tb_host, cudaMemcpyKind kind,
+              bool overlap, cudaStream_t s) {
     const size_t n = c->n;
+    const bool h2d = kind == cudaMemcpyHostToDevice;
+    Xfer x[kMaxXfer];
+    int nx = 0;
     for (size_t a = 0; a < m;) {
         size_t b = a + 1;
         int rows = map[a].rows;
         while (b < m && map[b].host == map[a].host + (size_t)rows * n && map[b].field == map[a].field + rows)
             rows += map[b++].rows;
-        double* dev = c->cd + (size_t)map[a].field * n;
-        size_t bytes = (size_t)rows * n * 8;
-        if (kind == cudaMemcpyHostToDevice) CUDA_TRY(cudaMemcpyAsync(dev, map[a].host, bytes, kind, s));
-        else CUDA_TRY(cudaMemcpyAsync(map[a].host, dev, bytes, kind, s));
+        char* dev = (char*)(c->cd + (size_t)map[a].field * n);
+        char* host = (char*)map[a].host;
+        x[nx++] = {h2d ? host : dev, h2d ? dev : host, (long long)rows * (long long)n * 8};
         a = b;
     }
-    return MVMM_OK;
+    if (timebin) x[nx++] = {h2d ? (char*)tb_host : (char*)c->timebin, h2d ? (char*)c->timebin : (char*)tb_host,
+                            (long long)n};
+    return transfer(c, x, nx, h2d, overlap, s);
 }
+// overlap: the copy runs beside the step's kernels
 int copy_cells(mvmm_ctx* c, const mvmm_cells* h, unsigned subset, bool timebin, cudaMemcpyKind kind,
-               cudaStream_t s) {
+               cudaStream_t s, bool overlap = false) {
     if (h->n != c->n) return fail(MVMM_E_INVALID, "cell count does not match the mesh");
     RowCopy map[14];
     size_t m = 0;
     int rc = row_map(h, subset, map, &m);
     if (rc) return rc;
-    rc = copy_rows(c, map, m, kind, s);
-    if (rc) return rc;
-    if (timebin) {
-        if (kind == cudaMemcpyHostToDevice) CUDA_TRY(cudaMemcpyAsync(c->timebin, h->timebin, c->n, kind, s));
-        else CUDA_TRY(cudaMemcpyAsync(h->timebin, c->timebin, c->n, kind, s));
-    }
-    return MVMM_OK;
+    return copy_rows(c, map, m, timebin, h->timebin, kind, overlap, s);
 }
 // The cell state changed outside a step: every cell's derived face-stage rows
 // are recomputed by the next predict.
@@ -646,10 +792,8 @@ int mark_stale(mvmm_ctx* c, cudaStream_t s) {
 int refresh_geometry(mvmm_ctx* c, cudaStream_t s) {
     int rc = mark_stale(c, s);
     if (rc) return rc;
-    if (c->prm.precision == MVMM_PRECISION_FP32FACE) {
-        launch_geom32(make_kp(c, 0, 7), s);
-        CUDA_TRY(cudaGetLastError());
-    }
+    update_geom32(c, make_kp(c, 0, 7), s);
+    CUDA_TRY(cudaGetLastError());
     return MVMM_OK;
 }
 }  // namespace
@@ -679,24 +823,24 @@ int mvmm_step_cells(mvmm_ctx* c, const mvmm_cells* in, mvmm_cells* out, uint64_t
         return fail(MVMM_E_UNSUPPORTED, "mvmm_step_cells steps a fixed mesh");
     if (!c->side) {
         CUDA_TRY(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
-        for (cudaEvent_t* e : {&c->ev_face, &c->ev_in, &c->ev_upd, &c->ev_grad, &c->ev_out})
+        for (cudaEvent_t* e : {&c->ev_pred, &c->ev_in, &c->ev_upd, &c->ev_grad, &c->ev_out})
             CUDA_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
     }
     cudaStream_t s = c->stream, s2 = c->side;
-    // host -> device: what predict reads on the step's stream; on the side stream
-    // what the face stage and then the update read, each behind an event
-    int rc = copy_cells(c, in, kRowsPredictIn, true, cudaMemcpyHostToDevice, s);
-    if (!rc) rc = copy_cells(c, in, kRowsFaceIn, false, cudaMemcpyHostToDevice, s2);
+    launch_set_time(make_kp(c, 0, 7), ti_current, ti_old, s);
+    // host -> device: the rows predict and the face stage read in one transfer
+    // on the step's own stream, then (copies in one direction share the link)
+    // the rows the update alone reads on the side stream, which land while the
+    // face stage runs
+    int rc = copy_cells(c, in, kRowsPredictIn | kRowsFaceIn, true, cudaMemcpyHostToDevice, s);
     if (rc) return rc;
-    CUDA_TRY(cudaEventRecord(c->ev_face, s2));
-    rc = copy_cells(c, in, kRowsLateIn, false, cudaMemcpyHostToDevice, s2);
+    CUDA_TRY(cudaEventRecord(c->ev_pred, s));
+    CUDA_TRY(cudaStreamWaitEvent(s2, c->ev_pred, 0));
+    rc = copy_cells(c, in, kRowsLateIn, false, cudaMemcpyHostToDevice, s2, true);
     if (rc) return rc;
     CUDA_TRY(cudaEventRecord(c->ev_in, s2));
-    rc = mark_stale(c, s);
-    if (rc) return rc;
-    launch_set_time(make_kp(c, 0, 7), ti_current, ti_old, s);
     StepHooks h;
-    h.wait_before_face = c->ev_face;
+    h.stale_all = true;
     h.geom_before_face = true;
     h.wait_before_update = c->ev_in;
     h.after_update = c->ev_upd;
@@ -705,16 +849,33 @@ int mvmm_step_cells(mvmm_ctx* c, const mvmm_cells* in, mvmm_cells* out, uint64_t
     // device -> host on the side stream: the rows final after the update while
     // the gradient stage runs, those final after it while the limiter runs
     CUDA_TRY(cudaStreamWaitEvent(s2, c->ev_upd, 0));
-    rc = copy_cells(c, out, kRowsEarlyOut, false, cudaMemcpyDeviceToHost, s2);
+    rc = copy_cells(c, out, kRowsEarlyOut, false, cudaMemcpyDeviceToHost, s2, true);
     if (rc) return rc;
     CUDA_TRY(cudaStreamWaitEvent(s2, c->ev_grad, 0));
-    rc = copy_cells(c, out, kRowsMidOut, false, cudaMemcpyDeviceToHost, s2);
+    rc = copy_cells(c, out, kRowsMidOut, false, cudaMemcpyDeviceToHost, s2, true);
     if (rc) return rc;
     CUDA_TRY(cudaEventRecord(c->ev_out, s2));
     rc = copy_cells(c, out, kRowsLateOut, true, cudaMemcpyDeviceToHost, s);
     if (rc) return rc;
     CUDA_TRY(cudaStreamWaitEvent(s, c->ev_out, 0));
     CUDA_TRY(cudaGetLastError());
+    // the rows the step leaves unchanged do not cross the link back: nothing to
+    // do in place, else a host copy from `in` while the step runs (after the
+    // uploads, so that an `out` row that overlaps an `in` row is read first)
+    const size_t n = (size_t)c->n;
+    const struct {
+        const double* src;
+        double* dst;
+        size_t len;
+    } pass[3] = {{in->volume, out->volume, n}, {in->loc, out->loc, 3 * n}, {in->centroid, out->centroid, 3 * n}};
+    static_assert(kRowsPassThrough == ((1u << 6) | (1u << 7) | (1u << 8)), "volume, loc, centroid");
+    bool waited = false;
+    for (const auto& r : pass) {
+        if (r.src == r.dst) continue;
+        if (!waited) CUDA_TRY(cudaEventSynchronize(c->ev_in));
+        waited = true;
+        std::memmove(r.dst, r.src, r.len * sizeof(double));
+    }
     rc = finish(c);
     if (ti_next) *ti_next = c->tl_host->ti_current;
     if (n_active_faces) *n_active_faces = (int64_t)(c->tl_host->active_faces - c->tl_host->faces_mark);
@@ -934,6 +1095,7 @@ int mvmm_set_mesh(mvmm_ctx* c, const mvmm_mesh* m, const double* volume, const d
     CUDA_TRY(cudaMemcpyAsync(c->pend_vol, volume, (size_t)c->n * 8, cudaMemcpyHostToDevice, s));
     CUDA_TRY(cudaMemcpyAsync(c->pend_cen, centroid, (size_t)c->n * 24, cudaMemcpyHostToDevice, s));
     c->pending_geometry = true;
+    c->geo_built = false;  // new face arrays
     if (c->step_exec) {  // kernel parameters hold the face count and pointers
         cudaGraphExecDestroy(c->step_exec);
         c->step_exec = nullptr;

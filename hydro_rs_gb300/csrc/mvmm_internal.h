@@ -116,6 +116,9 @@ struct KP {
     double* flux;            // face results, rows of nf
     float* flux32;           // FP32 form face results of a step, rows of nf: 5 fluxes, v_max, a_over_r
     float* geo;              // FP32 form static face geometry (FaceGeom32)
+    unsigned long long* geo_pos;  // FP32 form: bits of loc and centroid [6][n] the geometry was built from
+    uint8_t* geo_changed;    // FP32 form: 1 for cells whose loc or centroid bits changed since
+    int geo_check;           // 1: k_geom32 rebuilds only the faces of changed cells
     int fp32;                // 1: FP32-face form
     int flux_rows;           // 7 (step) or 10 (stage, with mflux)
     DevTimeline* tl;
@@ -128,6 +131,7 @@ struct KP {
     int max_iter;
     double time_base, time_base_inv;
     int stage;               // 1: per-stage call (explicit dt / mask from the host)
+    int stale_all;           // 1: every cell's state came from the host this step (fresh flags void)
     double stage_dt;
     // batches: many independent simulations packed into one mesh; each has its
     // own device timeline tl[k] (k = inst[cell]) and time base

@@ -16,9 +16,6 @@
 #ifndef FACE32_MINB
 #define FACE32_MINB 3
 #endif
-#ifndef GRAD32_MINB
-#define GRAD32_MINB 1
-#endif
 
 namespace mvmm {
 
@@ -67,11 +64,38 @@ __device__ __forceinline__ V3<float> GE3(const KP& p, int g, int f) {
     return {p.geo[g * nf + f], p.geo[(g + 1) * nf + f], p.geo[(g + 2) * nf + f]};
 }
 
-// Static face geometry (FaceGeom32), one thread per face.
+// Marks the cells whose position or centroid differs, bit for bit, from the
+// one the FP32 face geometry was last built from, and records the new bits
+// (integer compares: no FP64 pipe work).  force: every cell counts as changed.
+__global__ void __launch_bounds__(kMaxBlock) k_geom_check(KP p, int force) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n) return;
+    const size_t n = (size_t)p.n;
+    const unsigned long long* cd = reinterpret_cast<const unsigned long long*>(p.cd);
+    unsigned long long v[6];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        v[a] = cd[(F_LOC + a) * n + i];
+        v[3 + a] = cd[(F_CEN + a) * n + i];
+    }
+    bool changed = force != 0;
+#pragma unroll
+    for (int k = 0; k < 6; k++) changed = changed || v[k] != p.geo_pos[k * n + i];
+    if (changed) {
+#pragma unroll
+        for (int k = 0; k < 6; k++) p.geo_pos[k * n + i] = v[k];
+    }
+    p.geo_changed[i] = changed;
+}
+
+// Static face geometry (FaceGeom32), one thread per face.  With geo_check set
+// only faces next to a changed cell are rebuilt (the face arrays themselves
+// change only with the mesh, which rebuilds every face).
 __global__ void __launch_bounds__(kMaxBlock) k_geom32(KP p) {
     int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= p.nf) return;
     int l = p.left[f], r = p.right[f];
+    if (p.geo_check && !p.geo_changed[l] && (r < 0 || !p.geo_changed[r])) return;
     V3<double> fc = F3(p.fcen, p.nf, f), s = F3(p.shift, p.nf, f), n = F3(p.normal, p.nf, f);
     V3<double> locl = C3(p, F_LOC, l), cenl = C3(p, F_CEN, l);
     V3<double> z = v3(0., 0., 0.);
@@ -492,9 +516,12 @@ __device__ __forceinline__ void gradients32_cell_warp(const KP& p, int i, int la
     inst_min_dti_tb(p, lane == 0 ? k : -1, my_dti, my_tb);
 }
 
-__global__ void __launch_bounds__(kMaxBlock, GRAD32_MINB) k_gradients32(KP p) {
+// LIST: hierarchical step, a warp per listed cell.  The two forms are separate
+// instantiations so that the all-cells kernel keeps its own register budget.
+template <bool LIST>
+__global__ void __launch_bounds__(kMaxBlock) k_gradients32(KP p) {
     const int n_items = cell_items(p);
-    if (p.use_list) {
+    if (LIST) {
         const int lane = threadIdx.x & 31, n_warps = (gridDim.x * blockDim.x) >> 5;
         for (int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < n_items; w += n_warps)
             gradients32_cell_warp(p, p.cell_list[w], lane);
@@ -543,12 +570,17 @@ void launch_prep32(const KP& p, cudaStream_t s) {
     if (p.n > 0) k_prep32<<<cell_grid(p), p.blk_cell, 0, s>>>(p);
 }
 
-void launch_geom32(const KP& p, cudaStream_t s) {
-    if (p.nf > 0) k_geom32<<<grid(p.nf, kBlock), kBlock, 0, s>>>(p);
+void launch_geom32(const KP& p, bool check, cudaStream_t s) {
+    KP q = p;
+    q.geo_check = check ? 1 : 0;
+    if (q.n > 0) k_geom_check<<<grid(q.n, kBlock), kBlock, 0, s>>>(q, check ? 0 : 1);
+    if (q.nf > 0) k_geom32<<<grid(q.nf, kBlock), kBlock, 0, s>>>(q);
 }
 
 void launch_gradients32(const KP& p, cudaStream_t s) {
-    if (p.n > 0) k_gradients32<<<cell_grid(p), p.blk_cell, 0, s>>>(p);
+    if (p.n <= 0) return;
+    if (p.use_list) k_gradients32<true><<<cell_grid(p), p.blk_cell, 0, s>>>(p);
+    else k_gradients32<false><<<cell_grid(p), p.blk_cell, 0, s>>>(p);
 }
 
 void launch_face_flux_fp32(const KP& p, int solver, cudaStream_t s) {

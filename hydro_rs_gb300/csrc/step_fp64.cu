@@ -55,7 +55,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_predict(KP p) {
             act = p.timebin[i] <= max_active_bin_bits(tc);
             p.active[i] = act;
         }
-        if (!p.stage && p.fresh[i]) {
+        if (!p.stage && !p.stale_all && p.fresh[i]) {
             // prim, grad and v_rel are unchanged since this cell's source row was
             // written (it was not active, nothing was uploaded): the same bits
             St<double> ex = C5(p, F_EXTRAP, i);
@@ -529,10 +529,12 @@ __device__ __forceinline__ void update_cell_warp(const KP& p, int i, int do_c2p,
     if (lane == 0) update_finish(p, i, k, act, facc, msv, maor, do_c2p);
 }
 
-template <bool ROWS32>
+// LIST: hierarchical step, a warp per listed cell (a separate instantiation
+// from the all-cells kernel, which keeps its own register budget)
+template <bool ROWS32, bool LIST>
 __global__ void __launch_bounds__(kMaxBlock) k_update(KP p, int do_c2p) {
     const int n_items = cell_items(p);
-    if (p.use_list) {
+    if (LIST) {
         const int lane = threadIdx.x & 31, n_warps = (gridDim.x * blockDim.x) >> 5;
         for (int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < n_items; w += n_warps)
             update_cell_warp<ROWS32>(p, p.cell_list[w], do_c2p, lane);
@@ -821,9 +823,10 @@ __device__ __forceinline__ void gradients_cell_warp(const KP& p, int i, int do_t
     inst_min_dti_tb(p, lane == 0 ? k : -1, my_dti, my_tb);
 }
 
+template <bool LIST>
 __global__ void __launch_bounds__(kMaxBlock) k_gradients(KP p, int do_timestep) {
     const int n_items = cell_items(p);
-    if (p.use_list) {
+    if (LIST) {
         const int lane = threadIdx.x & 31, n_warps = (gridDim.x * blockDim.x) >> 5;
         for (int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < n_items; w += n_warps)
             gradients_cell_warp(p, p.cell_list[w], do_timestep, lane);
@@ -899,10 +902,9 @@ __device__ __forceinline__ void limit_cell(const KP& p, int i, int wakeup = -1) 
                 for (int a = 0; a < p.dim; a++) W(p, F_V + a, i, C(p, F_V + a, i) - kick_fac * C(p, F_GRAD + 12 + a, i));
             }
         }
-        // kick1: grav_kick adds +0
-        W(p, F_CONS + 1, i, C(p, F_CONS + 1, i) + 0.);
-        W(p, F_CONS + 2, i, C(p, F_CONS + 2, i) + 0.);
-        W(p, F_CONS + 3, i, C(p, F_CONS + 3, i) + 0.);
+        // kick1: grav_kick adds +0 to the momentum.  The update of this step
+        // (kick2) already added +0 to it, and (x + 0) + 0 == x + 0 for every
+        // double x, so the row is left as the update wrote it.
     }
 }
 __device__ __forceinline__ void end_instance(const KP& p, int k);
@@ -1101,14 +1103,22 @@ void launch_compact(const KP& p, cudaStream_t s) {
 }
 void launch_update(const KP& p, int do_c2p, cudaStream_t s) {
     if (p.n <= 0) return;
-    if (p.fp32 && p.flux_rows == 7) k_update<true><<<cell_grid(p), p.blk_cell, 0, s>>>(p, do_c2p);
-    else k_update<false><<<cell_grid(p), p.blk_cell, 0, s>>>(p, do_c2p);
+    const bool r32 = p.fp32 && p.flux_rows == 7;
+    if (p.use_list) {
+        if (r32) k_update<true, true><<<cell_grid(p), p.blk_cell, 0, s>>>(p, do_c2p);
+        else k_update<false, true><<<cell_grid(p), p.blk_cell, 0, s>>>(p, do_c2p);
+    } else {
+        if (r32) k_update<true, false><<<cell_grid(p), p.blk_cell, 0, s>>>(p, do_c2p);
+        else k_update<false, false><<<cell_grid(p), p.blk_cell, 0, s>>>(p, do_c2p);
+    }
 }
 void launch_c2p(const KP& p, cudaStream_t s) {
     if (p.n > 0) k_c2p<<<grid(p.n, p.blk_cell), p.blk_cell, 0, s>>>(p);
 }
 void launch_gradients(const KP& p, int do_timestep, cudaStream_t s) {
-    if (p.n > 0) k_gradients<<<cell_grid(p), p.blk_cell, 0, s>>>(p, do_timestep);
+    if (p.n <= 0) return;
+    if (p.use_list) k_gradients<true><<<cell_grid(p), p.blk_cell, 0, s>>>(p, do_timestep);
+    else k_gradients<false><<<cell_grid(p), p.blk_cell, 0, s>>>(p, do_timestep);
 }
 void launch_timesteps(const KP& p, double* dt_out, cudaStream_t s) {
     if (p.n > 0) k_timesteps<<<grid(p.n, p.blk_cell), p.blk_cell, 0, s>>>(p, dt_out);

@@ -261,12 +261,44 @@ def test_step_cells_matches_resident_steps(gpu_lib, precision):
         b.step_cells(host)  # in place on one packed block
         assert a.ti_current == b.ti_current and a.active_faces == b.active_faces
     ref = a.state()
+
+    def same_bits(x, y):  # signed zeros and NaN payloads included
+        x, y = np.ascontiguousarray(x), np.ascontiguousarray(y)
+        return x.dtype == y.dtype and np.array_equal(x.view(np.uint8), y.view(np.uint8))
+
     for k, v in ref.arrays.items():
-        assert np.array_equal(host.arrays[k], v), k
+        assert same_bits(host.arrays[k], v), k
     c = G.GpuSim(p, precision=precision)
     out = p.cells.copy()
     for _ in range(6):
         c.step_cells(split, out)
         split = out.copy()
     for k, v in ref.arrays.items():
-        assert np.array_equal(out.arrays[k], v), k
+        assert same_bits(out.arrays[k], v), k
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_step_cells_sees_moved_positions(gpu_lib, precision):
+    """Positions and centroids changed on the host between mvmm_step_cells calls
+    (a fixed mesh): the FP32 face geometry of the faces next to those cells is
+    rebuilt, so the step equals, bit for bit, that of a context that builds all
+    of its geometry from the same state."""
+    p = ics.kelvin_helmholtz_2d(32, riemann=ics.EXACT)
+    a = G.GpuSim(p, precision=precision)
+    host = p.cells.copy()
+    for _ in range(3):
+        a.step_cells(host)
+    rng = np.random.default_rng(5)
+    moved = rng.choice(p.mesh.n_cells, 40, replace=False)
+    host.loc[:2, moved] += rng.uniform(-1e-4, 1e-4, (2, moved.size))
+    host.centroid[:2, moved] += rng.uniform(-1e-4, 1e-4, (2, moved.size))
+    b = G.GpuSim(p, precision=precision)
+    b.upload(host)
+    b.ti_current, b.ti_old = a.ti_current, a.ti_old
+    out_a, out_b = host.copy(), host.copy()
+    a.step_cells(host, out_a)
+    b.step_cells(host, out_b)
+    assert a.ti_current == b.ti_current
+    for k, v in out_b.arrays.items():
+        x, y = np.ascontiguousarray(out_a.arrays[k]), np.ascontiguousarray(v)
+        assert np.array_equal(x.view(np.uint8), y.view(np.uint8)), k
