@@ -320,19 +320,15 @@ def run_ours(args):
         prof[prec] = _face_kernel_ms(sim, k_prof)
         nfa[prec] = (sim.stats()["active_faces"] - f0) / k_prof  # active faces per profiled step
 
-    # end-to-end through the C ABI with pinned host buffers
-    # one pinned block in the device's field order: one copy each way per step
+    # end-to-end through the C ABI with pinned host buffers: one pinned block in
+    # the device's field order, stepped in place
     pinned = (torch.empty(CELL_ROWS * nc, dtype=torch.float64, pin_memory=True),
               torch.empty(nc, dtype=torch.int8, pin_memory=True))
     cells = Cells.packed(nc, pinned[0].numpy(), pinned[1].numpy())
     sim = sims[1]
     sim.state(cells)
-    e2e_steps = max(3, min(args.steps, 20))
-    torch.cuda.synchronize()
-    barrier()
-    t0 = time.perf_counter()
-    f0 = sim.active_faces
-    for _ in range(e2e_steps):
+
+    def e2e_step():
         if batch:
             sim.upload(cells)
             try:
@@ -343,9 +339,24 @@ def run_ours(args):
             sim.state(cells)
         else:
             sim.step_cells(cells)  # upload + step + download in one C call
+
+    for _ in range(3):  # warm-up (the first call creates the copy stream and the snapshot block)
+        e2e_step()
+    e2e_steps = max(3, min(args.steps, 50))
+    st0 = sim.stats()
+    torch.cuda.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    f0 = sim.active_faces
+    for _ in range(e2e_steps):
+        e2e_step()
     e2e_s = time.perf_counter() - t0
     barrier()
     e2e_faces = sim.active_faces - f0
+    st1 = sim.stats()
+    # bytes the library moved between the host block and the device (counted by it)
+    h2d_step = (st1["host_bytes_in"] - st0["host_bytes_in"]) / e2e_steps
+    d2h_step = (st1["host_bytes_out"] - st0["host_bytes_out"]) / e2e_steps
     bytes_cells = cells.nbytes()
 
     st32 = sims[1].stats()
@@ -409,11 +420,13 @@ def run_ours(args):
                        "roofline": roof(0)},
         "roofline": roof(1),
         "cpu_baseline": cpu,
-        "e2e": {"value": e2e_faces / e2e_s, "unit": UNIT, "h2d_bytes_per_step": bytes_cells,
-                "d2h_bytes_per_step": bytes_cells + 64,
+        "e2e": {"value": e2e_faces / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d_step),
+                "d2h_bytes_per_step": int(d2h_step), "host_block_bytes": bytes_cells, "steps": e2e_steps,
                 "how": ("mvmm_upload_cells + mvmm_step + mvmm_download_cells per step" if batch else
-                        "mvmm_step_cells per step (upload, step and download in one C call)") +
-                       ", one pinned host block in the device field order, wall clock"},
+                        "mvmm_step_cells per step (upload, step and download in one C call; the step's "
+                        "state comes back in place, only the 8 KB chunks it changed)") +
+                       ", one pinned host block in the device field order, wall clock, bytes as counted "
+                       "by the library"},
         # per step: predict, [compact], [prep32], face, update, gradients, limiter (timed for both forms)
         "gpu_launches": args.steps * ((6 + 5) + (2 if (not batch and not problem.params.sync_all) else 0)),
         "clocks": clocks,

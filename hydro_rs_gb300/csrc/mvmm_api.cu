@@ -95,6 +95,12 @@ struct mvmm_ctx {
     uint32_t err_bits = 0;
     int device = 0, n_sms = 1;
     bool pageable_access = false;  // the device reads and writes pageable host memory
+    // mvmm_step_cells: the uploaded rows as they arrived ([54][n] in the block's
+    // field order, and the time bins), and bytes moved between host and device
+    double* snap = nullptr;
+    int8_t* snap_tb = nullptr;
+    unsigned long long* xfer_stored = nullptr;  // device: bytes stored by copies that skip unchanged chunks
+    int64_t host_bytes_in = 0, host_bytes_out = 0;
 };
 
 namespace {
@@ -459,6 +465,7 @@ static int create_impl(const mvmm_params* prm, const mvmm_mesh* m, int64_t n_ins
     ALLOC(c->face_stamp, nf * 4);
     ALLOC(c->touch, n * 4);
     ALLOC(c->blocks_done, 4);
+    ALLOC(c->xfer_stored, 8);
     ALLOC(c->fresh, n);
     ALLOC(c->cell_list, n * 4);
     ALLOC(c->face_list, nf * 4);
@@ -564,7 +571,7 @@ int mvmm_ctx_destroy(mvmm_ctx* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->step_exec) cudaGraphExecDestroy(c->step_exec);
     void* ptrs[] = {c->left, c->right, c->csr_off, c->csr_face, c->area, c->normal, c->fcen, c->shift, c->cd,
-                    c->cf, c->timebin, c->tb_tmp, c->active, c->flux, c->flux32, c->geo, c->geo_pos, c->geo_changed, c->dtmp, c->face_stamp, c->touch, c->blocks_done, c->cell_list, c->fresh,
+                    c->cf, c->timebin, c->tb_tmp, c->active, c->flux, c->flux32, c->geo, c->geo_pos, c->geo_changed, c->snap, c->snap_tb, c->xfer_stored, c->dtmp, c->face_stamp, c->touch, c->blocks_done, c->cell_list, c->fresh,
                     c->pend_vol, c->pend_cen,
                     c->face_list, c->tl,
                     c->inst, c->inst_tb, c->inst_tbi};
@@ -647,20 +654,35 @@ struct Xfer {
     const char* src;
     char* dst;
     long long bytes;
+    char* dst2 = nullptr;        // host -> device: a second device copy (the snapshot), or null
+    const char* ref = nullptr;   // device -> host: a device copy of the host's current content, or null
 };
 constexpr int kMaxXfer = 16;
-constexpr long long kXferChunk = 32768;  // bytes a block moves per iteration
+constexpr long long kXferChunk = 8192;  // bytes a block moves (or compares) at a time
 struct XferSet {
     Xfer x[kMaxXfer];
     long long chunk_off[kMaxXfer + 1];  // prefix sums of the transfers' chunk counts
     int m;
+    unsigned long long* stored;  // bytes stored by transfers with a ref
 };
 
-// Each block walks whole chunks; a chunk moves in 16-byte units where both
-// addresses and its length allow, else in 8-byte units, else bytes.  Four
+__device__ __forceinline__ bool differs(uint4 a, uint4 b) { return a.x != b.x || a.y != b.y || a.z != b.z || a.w != b.w; }
+__device__ __forceinline__ bool differs(unsigned long long a, unsigned long long b) { return a != b; }
+__device__ __forceinline__ bool differs(char a, char b) { return a != b; }
+
+// One chunk in units of U (16, 8 or 1 bytes).  With ref the chunk is stored
+// only if it differs from ref somewhere (the host already holds ref's bytes),
+// and the stored bytes are counted; with d2 it is written twice.  Up to four
 // loads in flight per thread cover the link's latency.
 template <typename U>
-__device__ __forceinline__ void xfer_units(const U* __restrict__ s, U* __restrict__ d, long long nv) {
+__device__ __forceinline__ void xfer_chunk(const U* __restrict__ s, U* __restrict__ d, U* __restrict__ d2,
+                                           const U* __restrict__ ref, long long nv, unsigned long long* stored) {
+    if (ref) {
+        bool diff = false;
+        for (long long k = threadIdx.x; k < nv; k += blockDim.x) diff = diff || differs(s[k], ref[k]);
+        if (!__syncthreads_or(diff)) return;
+        if (threadIdx.x == 0) atomicAdd(stored, (unsigned long long)(nv * (long long)sizeof(U)));
+    }
     for (long long k0 = threadIdx.x; k0 < nv; k0 += 4 * (long long)blockDim.x) {
         U v[4];
 #pragma unroll
@@ -671,23 +693,34 @@ __device__ __forceinline__ void xfer_units(const U* __restrict__ s, U* __restric
 #pragma unroll
         for (int u = 0; u < 4; u++) {
             const long long k = k0 + (long long)u * blockDim.x;
-            if (k < nv) d[k] = v[u];
+            if (k < nv) {
+                d[k] = v[u];
+                if (d2) d2[k] = v[u];
+            }
         }
     }
 }
-__global__ void __launch_bounds__(128) k_xfer(XferSet t) {
+__global__ void __launch_bounds__(256) k_xfer(XferSet t) {
     const long long total = t.chunk_off[t.m];
     for (long long ch = blockIdx.x; ch < total; ch += gridDim.x) {
         int j = 0;
         while (j + 1 < t.m && t.chunk_off[j + 1] <= ch) j++;
+        const Xfer& x = t.x[j];
         const long long b0 = (ch - t.chunk_off[j]) * kXferChunk;
-        const long long len = t.x[j].bytes - b0 < kXferChunk ? t.x[j].bytes - b0 : kXferChunk;
-        const char* src = t.x[j].src + b0;
-        char* dst = t.x[j].dst + b0;
-        const unsigned long long a = (unsigned long long)(uintptr_t)src | (uintptr_t)dst | (unsigned long long)len;
-        if ((a & 15) == 0) xfer_units((const uint4*)src, (uint4*)dst, len >> 4);
-        else if ((a & 7) == 0) xfer_units((const unsigned long long*)src, (unsigned long long*)dst, len >> 3);
-        else xfer_units(src, dst, len);
+        const long long len = x.bytes - b0 < kXferChunk ? x.bytes - b0 : kXferChunk;
+        const char* src = x.src + b0;
+        char* dst = x.dst + b0;
+        char* dst2 = x.dst2 ? x.dst2 + b0 : nullptr;
+        const char* ref = x.ref ? x.ref + b0 : nullptr;
+        const unsigned long long a = (unsigned long long)(uintptr_t)src | (uintptr_t)dst | (uintptr_t)dst2 |
+                                     (uintptr_t)ref | (unsigned long long)len;
+        if ((a & 15) == 0)
+            xfer_chunk((const uint4*)src, (uint4*)dst, (uint4*)dst2, (const uint4*)ref, len >> 4, t.stored);
+        else if ((a & 7) == 0)
+            xfer_chunk((const unsigned long long*)src, (unsigned long long*)dst, (unsigned long long*)dst2,
+                       (const unsigned long long*)ref, len >> 3, t.stored);
+        else
+            xfer_chunk(src, dst, dst2, ref, len, t.stored);
     }
 }
 
@@ -712,13 +745,17 @@ const void* device_view(mvmm_ctx* c, const void* p, bool* pinned) {
     }
 }
 
-// Moves m (host array, device row) pairs on stream s: in one kernel, except
-// pairs whose host array the device cannot address and, with overlap (the
-// copy runs beside the step's kernels), pairs in pinned memory, which go by
-// cudaMemcpyAsync.
-int transfer(mvmm_ctx* c, const Xfer* pairs, int m, bool h2d, bool overlap, cudaStream_t s) {
+// Moves m (host array, device row) pairs on stream s.  Pairs go in one kernel
+// except, by cudaMemcpyAsync, those whose host array the device cannot
+// address and, with overlap (the copy runs beside the step's kernels), plain
+// copies of pinned memory.  A pair with a ref always takes the kernel where
+// the device can address its host array (its bytes mostly need no storing).
+// max_blocks caps the kernel's grid (0: four blocks per SM), so that beside a
+// kernel on the critical path it holds few SM slots.
+int transfer(mvmm_ctx* c, const Xfer* pairs, int m, bool h2d, bool overlap, int max_blocks, cudaStream_t s) {
     XferSet t{};
     t.m = 0;
+    t.stored = c->xfer_stored;
     long long chunks = 0;
     for (int k = 0; k < m; k++) {
         const Xfer& x = pairs[k];
@@ -729,14 +766,19 @@ int transfer(mvmm_ctx* c, const Xfer* pairs, int m, bool h2d, bool overlap, cuda
         // rows merged from separate arrays must lie in one mapping
         if (view && (const char*)device_view(c, host + x.bytes - 1, &pinned_end) != view + x.bytes - 1)
             view = nullptr;
-        if (!view || (overlap && pinned)) {
-            CUDA_TRY(cudaMemcpyAsync(x.dst, x.src, (size_t)x.bytes,
-                                     h2d ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost, s));
+        if (!view || (overlap && pinned && !x.ref)) {
+            const cudaMemcpyKind kind = h2d ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost;
+            CUDA_TRY(cudaMemcpyAsync(x.dst, x.src, (size_t)x.bytes, kind, s));
+            if (x.dst2) CUDA_TRY(cudaMemcpyAsync(x.dst2, x.dst, (size_t)x.bytes, cudaMemcpyDeviceToDevice, s));
+            if (h2d) c->host_bytes_in += x.bytes;
+            else c->host_bytes_out += x.bytes;
             continue;
         }
         Xfer v = x;
-        if (h2d) v.src = (const char*)view;
+        if (h2d) v.src = view;
         else v.dst = (char*)view;
+        if (h2d) c->host_bytes_in += x.bytes;
+        else if (!x.ref) c->host_bytes_out += x.bytes;  // with a ref the kernel counts what it stores
         t.x[t.m] = v;
         t.chunk_off[t.m] = chunks;
         chunks += (x.bytes + kXferChunk - 1) / kXferChunk;
@@ -744,43 +786,105 @@ int transfer(mvmm_ctx* c, const Xfer* pairs, int m, bool h2d, bool overlap, cuda
     }
     if (t.m == 0) return MVMM_OK;
     t.chunk_off[t.m] = chunks;
-    const long long cap = 4LL * c->n_sms;
-    k_xfer<<<(unsigned)(chunks < cap ? chunks : cap), 128, 0, s>>>(t);
+    const long long cap = max_blocks > 0 ? max_blocks : 4LL * c->n_sms;
+    k_xfer<<<(unsigned)(chunks < cap ? chunks : cap), 256, 0, s>>>(t);
     CUDA_TRY(cudaGetLastError());
     return MVMM_OK;
 }
 
+// Options of a row copy.  overlap: it runs beside the step's kernels;
+// max_blocks: the copy kernel's grid cap (0: four blocks per SM).
+// snapshot (host -> device): the rows also go to the snapshot block.
+// in_place (device -> host): the host arrays of `in_place` that `h` shares
+// still hold the bytes of the snapshot, so only what differs is stored.
+struct CopyOpts {
+    bool overlap = false;
+    int max_blocks = 0;
+    bool snapshot = false;
+    const mvmm_cells* in_place = nullptr;
+};
+
+// The host array of field k (row_map order) of h.
+const void* field_ptr(const mvmm_cells* h, int k) {
+    const void* f[14] = {h->cons, h->prim, h->grad, h->gc, h->extrap, h->facc, h->volume,
+                         h->loc, h->centroid, h->v, h->v_rel, h->max_a_over_r, h->max_signal_velocity, h->dt};
+    return f[k];
+}
+
 // Copies rows between the host arrays and the device block; rows that lie
 // back to back on the host in the device's field order form one transfer.
-int copy_rows(mvmm_ctx* c, const RowCopy* map, size_t m, bool timebin, int8_t* tb_host, cudaMemcpyKind kind,
-              bool overlap, cudaStream_t s) {
+int copy_rows(mvmm_ctx* c, const mvmm_cells* h, const RowCopy* map, const int* idx, size_t m, bool timebin,
+              cudaMemcpyKind kind, const CopyOpts& o, cudaStream_t s) {
     const size_t n = c->n;
     const bool h2d = kind == cudaMemcpyHostToDevice;
+    auto diffable = [&](size_t a) {
+        return !h2d && o.in_place && c->snap && field_ptr(h, idx[a]) == field_ptr(o.in_place, idx[a]);
+    };
     Xfer x[kMaxXfer];
     int nx = 0;
     for (size_t a = 0; a < m;) {
         size_t b = a + 1;
         int rows = map[a].rows;
-        while (b < m && map[b].host == map[a].host + (size_t)rows * n && map[b].field == map[a].field + rows)
+        const bool dif = diffable(a);
+        while (b < m && map[b].host == map[a].host + (size_t)rows * n && map[b].field == map[a].field + rows &&
+               diffable(b) == dif)
             rows += map[b++].rows;
         char* dev = (char*)(c->cd + (size_t)map[a].field * n);
+        char* snap = c->snap ? (char*)(c->snap + (size_t)map[a].field * n) : nullptr;
         char* host = (char*)map[a].host;
-        x[nx++] = {h2d ? host : dev, h2d ? dev : host, (long long)rows * (long long)n * 8};
+        Xfer t{h2d ? host : dev, h2d ? dev : host, (long long)rows * (long long)n * 8};
+        if (h2d && o.snapshot) t.dst2 = snap;
+        if (dif) t.ref = snap;
+        x[nx++] = t;
         a = b;
     }
-    if (timebin) x[nx++] = {h2d ? (char*)tb_host : (char*)c->timebin, h2d ? (char*)c->timebin : (char*)tb_host,
-                            (long long)n};
-    return transfer(c, x, nx, h2d, overlap, s);
+    if (timebin) {
+        Xfer t{h2d ? (const char*)h->timebin : (const char*)c->timebin, h2d ? (char*)c->timebin : (char*)h->timebin,
+               (long long)n};
+        if (h2d && o.snapshot) t.dst2 = (char*)c->snap_tb;
+        if (!h2d && o.in_place && c->snap && h->timebin == o.in_place->timebin) t.ref = (const char*)c->snap_tb;
+        x[nx++] = t;
+    }
+    return transfer(c, x, nx, h2d, o.overlap, o.max_blocks, s);
 }
-// overlap: the copy runs beside the step's kernels
+// Device copy of the rows of `subset` (and the time bins) into the snapshot
+// block, on stream s.
+int snapshot_rows(mvmm_ctx* c, unsigned subset, bool timebin, cudaStream_t s) {
+    static const int first[14] = {F_CONS, F_PRIM, F_GRAD, F_GC, F_EXTRAP, F_FACC, F_VOL,
+                                  F_LOC, F_CEN, F_V, F_VREL, F_MAOR, F_MSV, F_DT};
+    static const int rows[14] = {5, 5, 15, 3, 5, 5, 1, 3, 3, 3, 3, 1, 1, 1};
+    const long long n = c->n;
+    XferSet t{};
+    t.stored = c->xfer_stored;
+    long long chunks = 0;
+    auto add = [&](const char* src, char* dst, long long bytes) {
+        t.x[t.m] = Xfer{src, dst, bytes};
+        t.chunk_off[t.m++] = chunks;
+        chunks += (bytes + kXferChunk - 1) / kXferChunk;
+    };
+    for (int k = 0; k < 14; k++) {
+        if (!(subset & (1u << k))) continue;
+        add((const char*)(c->cd + first[k] * n), (char*)(c->snap + first[k] * n), rows[k] * n * 8);
+    }
+    if (timebin) add((const char*)c->timebin, (char*)c->snap_tb, n);
+    if (t.m == 0 || chunks == 0) return MVMM_OK;
+    t.chunk_off[t.m] = chunks;
+    const long long cap = 4LL * c->n_sms;
+    k_xfer<<<(unsigned)(chunks < cap ? chunks : cap), 256, 0, s>>>(t);
+    CUDA_TRY(cudaGetLastError());
+    return MVMM_OK;
+}
 int copy_cells(mvmm_ctx* c, const mvmm_cells* h, unsigned subset, bool timebin, cudaMemcpyKind kind,
-               cudaStream_t s, bool overlap = false) {
+               cudaStream_t s, const CopyOpts& o = CopyOpts()) {
     if (h->n != c->n) return fail(MVMM_E_INVALID, "cell count does not match the mesh");
     RowCopy map[14];
+    int idx[14];
     size_t m = 0;
     int rc = row_map(h, subset, map, &m);
     if (rc) return rc;
-    return copy_rows(c, map, m, timebin, h->timebin, kind, overlap, s);
+    for (int k = 0, j = 0; k < 14; k++)
+        if (subset & (1u << k)) idx[j++] = k;
+    return copy_rows(c, h, map, idx, m, timebin, kind, o, s);
 }
 // The cell state changed outside a step: every cell's derived face-stage rows
 // are recomputed by the next predict.
@@ -826,17 +930,28 @@ int mvmm_step_cells(mvmm_ctx* c, const mvmm_cells* in, mvmm_cells* out, uint64_t
         for (cudaEvent_t* e : {&c->ev_pred, &c->ev_in, &c->ev_upd, &c->ev_grad, &c->ev_out})
             CUDA_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
     }
+    if (!c->snap) {
+        if (cudaMalloc((void**)&c->snap, (size_t)F_SRC * c->n * 8) != cudaSuccess ||
+            cudaMalloc((void**)&c->snap_tb, (size_t)c->n) != cudaSuccess)
+            return fail(MVMM_E_NOMEM, "mvmm_step_cells: cudaMalloc failed");
+    }
     cudaStream_t s = c->stream, s2 = c->side;
     launch_set_time(make_kp(c, 0, 7), ti_current, ti_old, s);
     // host -> device: the rows predict and the face stage read in one transfer
     // on the step's own stream, then (copies in one direction share the link)
     // the rows the update alone reads on the side stream, which land while the
     // face stage runs
-    int rc = copy_cells(c, in, kRowsPredictIn | kRowsFaceIn, true, cudaMemcpyHostToDevice, s);
+    CopyOpts up;
+    up.snapshot = true;  // the uploaded bytes, against which the copies back skip unchanged chunks
+    int rc = copy_cells(c, in, kRowsPredictIn | kRowsFaceIn, true, cudaMemcpyHostToDevice, s, up);
     if (rc) return rc;
     CUDA_TRY(cudaEventRecord(c->ev_pred, s));
     CUDA_TRY(cudaStreamWaitEvent(s2, c->ev_pred, 0));
-    rc = copy_cells(c, in, kRowsLateIn, false, cudaMemcpyHostToDevice, s2, true);
+    up.overlap = true;
+    up.snapshot = false;  // taken on the device once the rows have landed (a short kernel)
+    rc = copy_cells(c, in, kRowsLateIn, false, cudaMemcpyHostToDevice, s2, up);
+    if (rc) return rc;
+    rc = snapshot_rows(c, kRowsLateIn, false, s2);
     if (rc) return rc;
     CUDA_TRY(cudaEventRecord(c->ev_in, s2));
     StepHooks h;
@@ -847,15 +962,24 @@ int mvmm_step_cells(mvmm_ctx* c, const mvmm_cells* in, mvmm_cells* out, uint64_t
     h.after_gradients = c->ev_grad;
     enqueue_step_kernels(c, false, h);
     // device -> host on the side stream: the rows final after the update while
-    // the gradient stage runs, those final after it while the limiter runs
+    // the gradient stage runs, those final after it while the limiter runs.
+    // Arrays that `out` shares with `in` still hold the uploaded bytes: only
+    // the chunks the step changed are stored.
+    CopyOpts back;
+    back.overlap = true;
+    back.max_blocks = 64;  // beside the gradient stage
+    back.in_place = in;
     CUDA_TRY(cudaStreamWaitEvent(s2, c->ev_upd, 0));
-    rc = copy_cells(c, out, kRowsEarlyOut, false, cudaMemcpyDeviceToHost, s2, true);
+    rc = copy_cells(c, out, kRowsEarlyOut, false, cudaMemcpyDeviceToHost, s2, back);
     if (rc) return rc;
     CUDA_TRY(cudaStreamWaitEvent(s2, c->ev_grad, 0));
-    rc = copy_cells(c, out, kRowsMidOut, false, cudaMemcpyDeviceToHost, s2, true);
+    back.max_blocks = 128;  // beside the limiter (which the copies after it wait for)
+    rc = copy_cells(c, out, kRowsMidOut, false, cudaMemcpyDeviceToHost, s2, back);
     if (rc) return rc;
     CUDA_TRY(cudaEventRecord(c->ev_out, s2));
-    rc = copy_cells(c, out, kRowsLateOut, true, cudaMemcpyDeviceToHost, s);
+    back.overlap = false;
+    back.max_blocks = 0;
+    rc = copy_cells(c, out, kRowsLateOut, true, cudaMemcpyDeviceToHost, s, back);
     if (rc) return rc;
     CUDA_TRY(cudaStreamWaitEvent(s, c->ev_out, 0));
     CUDA_TRY(cudaGetLastError());
@@ -997,6 +1121,10 @@ int mvmm_get_stats(mvmm_ctx* c, mvmm_stats* out) {
     out->active_faces = (int64_t)sum_field(c, &DevTimeline::active_faces);
     out->active_cells = (int64_t)sum_field(c, &DevTimeline::active_cells);
     out->fp64_fallback_faces = (int64_t)sum_field(c, &DevTimeline::fallback_faces);
+    unsigned long long stored = 0;
+    CUDA_TRY(cudaMemcpy(&stored, c->xfer_stored, 8, cudaMemcpyDeviceToHost));
+    out->host_bytes_in = c->host_bytes_in;
+    out->host_bytes_out = c->host_bytes_out + (int64_t)stored;
     return MVMM_OK;
 }
 

@@ -317,9 +317,10 @@ class GpuSim:
         return bf.value, bc.value
 
     def stats(self) -> dict:
-        a = np.zeros(4, dtype=np.int64)
+        a = np.zeros(6, dtype=np.int64)
         _check(load_library().mvmm_get_stats(self.h, a.ctypes.data), self.h)
-        return dict(zip(("steps", "active_faces", "active_cells", "fp64_fallback_faces"), a.tolist()))
+        return dict(zip(("steps", "active_faces", "active_cells", "fp64_fallback_faces", "host_bytes_in",
+                         "host_bytes_out"), a.tolist()))
 
     def profile(self, enable: bool):
         _check(load_library().mvmm_profile_enable(self.h, int(enable)), self.h)

@@ -189,11 +189,15 @@ int mvmm_get_positions(mvmm_ctx *ctx, double *loc);
 int mvmm_set_mesh(mvmm_ctx *ctx, const mvmm_mesh *mesh, const double *volume, const double *centroid);
 
 /* Runner::step(&mut Space, ..) on host-resident state (runner.rs:6-22): uploads
- * `in`, runs one step (OptimalOrderRunner or GodunovHydroRunner) and writes the
- * new state to `out` (which may be `in`) in one call.  Copies of the rows the
- * update alone reads and of the rows final after it overlap the other stages.
- * Host arrays laid out back to back in the mvmm_cells field order (pinned for
- * speed) move in one copy per direction.  Single simulations only. */
+ * `in`, runs one step (OptimalOrderRunner or GodunovHydroRunner) of a fixed
+ * mesh and writes the new state to `out` (which may be `in`, wholly or field by
+ * field) in one call.  Copies of the rows the update alone reads and of the
+ * rows final after it overlap the other stages.  Where the device can address
+ * the host arrays (pinned memory, or pageable memory on systems whose GPU uses
+ * the host page tables) the copies run as kernels; arrays `out` shares with
+ * `in` then receive only the 8 KB chunks the step changed.  volume, loc and
+ * centroid, which the step does not change, are not copied back.  Single
+ * simulations only. */
 int mvmm_step_cells(mvmm_ctx *ctx, const mvmm_cells *in, mvmm_cells *out, uint64_t ti_current, uint64_t ti_old,
                     uint64_t *ti_next, int64_t *n_active_faces);
 /* Engine::run (engine.rs:152-199) from the given sync point, device resident:
@@ -217,6 +221,9 @@ int mvmm_get_time(mvmm_ctx *ctx, uint64_t *ti_current, uint64_t *ti_old, int64_t
  * No counterpart in the reference (its status line prints step counts only). */
 typedef struct mvmm_stats {
     int64_t steps, active_faces, active_cells, fp64_fallback_faces;
+    /* bytes moved between host arrays and the device by the cell copies
+     * (mvmm_upload_cells, mvmm_download_cells, mvmm_step_cells) */
+    int64_t host_bytes_in, host_bytes_out;
 } mvmm_stats;
 int mvmm_get_stats(mvmm_ctx *ctx, mvmm_stats *out);
 /* Autotuner (no counterpart in the reference): times `steps` steps of this

@@ -277,6 +277,43 @@ def test_step_cells_matches_resident_steps(gpu_lib, precision):
         assert same_bits(out.arrays[k], v), k
 
 
+def test_step_cells_host_bytes(gpu_lib):
+    """Bytes moved per mvmm_step_cells call: all 54 rows and the time bins go up;
+    47 rows and the time bins come back out of place (volume, loc and centroid
+    never change), and in place only the chunks the step changed, stored into
+    pinned and pageable arrays alike with the same result as a full copy."""
+    import torch
+    from hydro_rs_gb300.layout import CELL_ROWS, Cells
+    p = ics.kelvin_helmholtz_2d(64, riemann=ics.EXACT)
+    n = p.mesh.n_cells
+    sims = [G.GpuSim(p, precision=1) for _ in range(3)]
+    pinned = (torch.empty(CELL_ROWS * n, dtype=torch.float64, pin_memory=True),
+              torch.empty(n, dtype=torch.int8, pin_memory=True))
+    host_pinned = Cells.packed(n, pinned[0].numpy(), pinned[1].numpy())
+    host_pageable = p.cells.copy()
+    for h in (host_pinned, host_pageable):
+        for k, v in p.cells.arrays.items():
+            h.arrays[k][...] = v
+    src = p.cells.copy()
+    for _ in range(4):
+        sims[0].step_cells(host_pinned)
+        sims[1].step_cells(host_pageable)
+        out = p.cells.copy()
+        sims[2].step_cells(src, out)
+        src = out
+    for k, v in out.arrays.items():
+        for h in (host_pinned, host_pageable):
+            x, y = np.ascontiguousarray(h.arrays[k]), np.ascontiguousarray(v)
+            assert np.array_equal(x.view(np.uint8), y.view(np.uint8)), k
+    up, full_back = 4 * (54 * n * 8 + n), 4 * (47 * n * 8 + n)
+    st = [s.stats() for s in sims]
+    assert all(x["host_bytes_in"] - 54 * n * 8 - n == up for x in st)  # the constructor's upload counts too
+    assert st[2]["host_bytes_out"] == full_back
+    for x in st[:2]:
+        # the z rows of this 2D problem and the rows a step resets stay as they were
+        assert 0 < x["host_bytes_out"] < 0.8 * full_back, x
+
+
 @pytest.mark.parametrize("precision", [0, 1])
 def test_step_cells_sees_moved_positions(gpu_lib, precision):
     """Positions and centroids changed on the host between mvmm_step_cells calls
