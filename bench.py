@@ -216,23 +216,29 @@ def _time_steps(sim, steps, stream, flush_buf, torch):
 #   plain FP64 (k_face_flux): per active face its indices, area, normal, centroid
 #   and shift (88 B) and the 7 FP64 result rows (56 B); per cell next to an
 #   active face its 44 FP64 face-stage inputs and the active flag (353 B).
-#   FP32-face form (k_prep32 + k_face_flux32): k_prep32 reads 40 FP64 rows and
-#   writes 37 FP32 rows per converted cell (468 B; all cells in synchronised
-#   steps, the cells next to an active face in hierarchical ones); the face
-#   kernel reads per cell the 37 FP32 copies, dt and the flag (157 B) and per
-#   active face the indices, the 26-float static geometry and writes 7 FP32
-#   result rows (140 B).
+#   FP32-face form: the face kernel reads per cell the 37 FP32 copies, dt and
+#   the flag (157 B) and per active face the indices, the 26-float static
+#   geometry and writes 7 FP32 result rows (140 B).  Steps over all cells write
+#   the FP32 copies in the predict kernel (k_predict32); hierarchical steps run
+#   k_prep32 in the face stage, which reads 40 FP64 rows and writes 37 FP32 rows
+#   per cell next to an active face (468 B).
 def face_stage_bytes(prec, nc, nfa, all_cells):
     touched = min(nc, 2 * nfa)
     if prec == 1:
-        return (nc if all_cells else touched) * 468 + touched * 157 + nfa * 140
+        return (0 if all_cells else touched * 468) + touched * 157 + nfa * 140
     return touched * 353 + nfa * 144
+
+
+def face_stage_kernels(prec, all_cells):
+    if prec == 0:
+        return "k_face_flux"
+    return "k_face_flux32" if all_cells else "k_prep32 + k_face_flux32"
 
 
 # DRAM bytes (read + write) per launch of the face stage from ncu captures at
 # the bench sizes (cold caches, ncu's default cache control): the committed
 # summaries in profiles/ give the commands.  Keyed by (workload, nx, form).
-TRAFFIC = {("kh2d", 256, 1): 47_873_992, ("kh2d", 256, 0): 40_704_000}  # profiles/face_stage_traffic_kh256.txt
+TRAFFIC = {("kh2d", 256, 1): 26_909_440, ("kh2d", 256, 0): 40_748_544}  # profiles/face_stage_traffic_kh256.txt
 
 
 def _face_kernel_ms(sim, steps):
@@ -390,12 +396,13 @@ def run_ours(args):
     def roof(prec):
         ms, n = prof[prec]["face_flux"]
         ms_launch = ms / max(n, 1)
-        bytes_launch = face_stage_bytes(prec, nc, nfa[prec], batch or problem.params.sync_all)
+        all_cells = batch or problem.params.sync_all
+        bytes_launch = face_stage_bytes(prec, nc, nfa[prec], all_cells)
         ach = bytes_launch / (ms_launch * 1e-3) / 1e9
         traffic = TRAFFIC.get((args.workload, args.nx, prec))
         return {"bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(ach / peak, 4), "traffic": traffic,
-                "kernel": "k_prep32 + k_face_flux32" if prec == 1 else "k_face_flux",
+                "kernel": face_stage_kernels(prec, all_cells),
                 "kernel_ms": round(ms_launch, 4), "algorithmic_bytes_per_launch": int(bytes_launch),
                 "active_faces_per_launch": nfa[prec],
                 "peak_kind": peak_kind, "note": "of measured" if peak_kind == "measured" else "of fallback",

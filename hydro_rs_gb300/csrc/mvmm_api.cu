@@ -23,6 +23,7 @@ void launch_riemann_fp64(int kind, int sample, double gamma, int64_t n, const do
 void launch_face_flux_fp32(const KP& p, int solver, cudaStream_t s);
 void launch_gradients32(const KP& p, cudaStream_t s);
 void launch_geom32(const KP& p, bool check, cudaStream_t s);
+void launch_predict32(const KP& p, cudaStream_t s);
 void launch_riemann_fp32(int kind, int sample, double gamma, int64_t n, const double* l, const double* r,
                          const double* vf, const double* nrm, double* out, unsigned int* err, const RSx& x,
                          cudaStream_t s);
@@ -206,9 +207,10 @@ void update_geom32(mvmm_ctx* c, const KP& p, cudaStream_t s) {
     c->geo_built = true;
 }
 
-void launch_face(mvmm_ctx* c, const KP& p) {
+// prepped: the FP32 copies of the cells were written by k_predict32
+void launch_face(mvmm_ctx* c, const KP& p, bool prepped = false) {
     if (c->prm.precision == MVMM_PRECISION_FP32FACE) {
-        launch_prep32(p, c->stream);
+        if (!prepped) launch_prep32(p, c->stream);
         launch_face_flux_fp32(p, c->prm.riemann, c->stream);
     } else {
         launch_face_flux_fp64(p, c->prm.riemann, c->stream);
@@ -233,13 +235,16 @@ void enqueue_step_kernels(mvmm_ctx* c, bool with_events, const StepHooks& h = St
     p.stale_all = h.stale_all ? 1 : 0;
     cudaStream_t s = c->stream;
     if (with_events) cudaEventRecord(c->ev[0], s);
-    launch_predict(p, s);
+    // steps over all cells of the FP32-face form: predict and the FP32 copies in one kernel
+    const bool fused = c->prm.precision == MVMM_PRECISION_FP32FACE && !p.use_list;
+    if (fused) launch_predict32(p, s);
+    else launch_predict(p, s);
     if (c->pending_geometry) launch_geometry(p, s);  // after predict, as volume_calculation
     if (h.geom_before_face || c->prm.particle_motion != MVMM_MOTION_FIXED)
         update_geom32(c, p, s);  // generators drifted or uploaded, centroids updated
     if (p.use_list) launch_compact(p, s);
     if (with_events) cudaEventRecord(c->ev[1], s);
-    launch_face(c, p);
+    launch_face(c, p, fused);
     if (with_events) cudaEventRecord(c->ev[2], s);
     if (h.wait_before_update) cudaStreamWaitEvent(s, h.wait_before_update, 0);
     launch_update(p, 1, s);

@@ -176,7 +176,7 @@ __device__ __forceinline__ V3<double> particle_velocity(const KP& p, int i, V3<d
 // Particle::timestep (part.rs:42-84, 328-372); returns the dt.
 __device__ __forceinline__ double particle_timestep(const KP& p, int i) {
     St<double> cons = C5(p, F_CONS, i);
-    if (cons.q[0] == 0.) {
+    if (is_zero64(cons.q[0])) {
         W3(p, F_V, i, v3(0., 0., 0.));
         return INFINITY;
     }
@@ -190,7 +190,7 @@ __device__ __forceinline__ double particle_timestep(const KP& p, int i) {
     double vol = C(p, F_VOL, i);
     double c = g.sound_speed(g.pressure_from_internal_energy(u, prim.q[0]), vol * m_inv);
     V3<double> v = particle_velocity(p, i, fluid_v, c, vol);
-    if (!isfinite(v.x) || !isfinite(v.y) || !isfinite(v.z)) set_err(p, inst_of(p, i), 1u << 4);  // part.rs:366
+    if (!is_finite64(v.x) || !is_finite64(v.y) || !is_finite64(v.z)) set_err(p, inst_of(p, i), 1u << 4);  // part.rs:366
     V3<double> v_rel = fluid_v - v;
     W3(p, F_V, i, v);
     W3(p, F_VREL, i, v_rel);

@@ -27,6 +27,25 @@ __device__ __forceinline__ float m_abs(float x) { return fabsf(x); }
 __device__ __forceinline__ double m_min(double a, double b) { return fmin(a, b); }
 __device__ __forceinline__ float m_min(float a, float b) { return fminf(a, b); }
 __device__ __forceinline__ double m_max(double a, double b) { return fmax(a, b); }
+
+// Comparisons of a double with zero, and isfinite, evaluated on its bit
+// pattern with integer instructions: the same truth values as the
+// floating-point forms (NaN compares false, -0.0 == 0.0), without occupying
+// the FP64 pipe, which on this GPU runs at 1/64 of the FP32 rate.
+__device__ __forceinline__ unsigned long long mag64(double x) {
+    return (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
+}
+constexpr unsigned long long kInf64 = 0x7ff0000000000000ull;
+__device__ __forceinline__ bool is_nan64(double x) { return mag64(x) > kInf64; }
+__device__ __forceinline__ bool is_finite64(double x) { return mag64(x) < kInf64; }
+__device__ __forceinline__ bool is_zero64(double x) { return mag64(x) == 0; }  // x == 0.
+__device__ __forceinline__ bool lt0_64(double x) {                              // x < 0.
+    return __double_as_longlong(x) < 0 && mag64(x) != 0 && mag64(x) <= kInf64;
+}
+__device__ __forceinline__ bool gt0_64(double x) {  // x > 0.
+    return __double_as_longlong(x) > 0 && mag64(x) <= kInf64;
+}
+__device__ __forceinline__ bool ge0_64(double x) { return !is_nan64(x) && (__double_as_longlong(x) >= 0 || mag64(x) == 0); }
 __device__ __forceinline__ float m_max(float a, float b) { return fmaxf(a, b); }
 
 template <typename T>

@@ -52,6 +52,74 @@ __device__ __forceinline__ void prep32_cell(const KP& p, int i) {
     cf[(G_V + 1) * n + i] = (float)v.y;
     cf[(G_V + 2) * n + i] = (float)v.z;
 }
+// Steps over all cells (synchronised steps, batches): EulerEqnsFvs::predict
+// (Particle::extrapolate_state, part.rs:123-132, with the active mask of
+// engine.rs:63-65) fused with the FP32 copies the face stage reads.  The
+// extrapolation source and the sound speed feed only FP32 arithmetic, so they
+// are formed in FP32 from those copies; the extrapolation itself is state and
+// accumulates in FP64.  Branches as the plain predict: the update of the
+// extrapolation tests the density before check_physical, the face-stage rows
+// the checked state.
+__global__ void __launch_bounds__(kMaxBlock) k_predict32(KP p) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool act = false;
+    int k = i < p.n ? inst_of(p, i) : -1;
+    if (k >= 0 && p.tl[k].done) k = -1;  // a finished simulation of a batch is left untouched
+    if (k >= 0) {
+        const unsigned long long tc = p.tl[k].ti_current, to = p.tl[k].ti_old;
+        const double dt = (double)(tc - to) * tbase(p, k);  // TimestepInfo::dt_from_dti
+        act = p.timebin[i] <= max_active_bin_bits(tc);
+        p.active[i] = act;
+        p.fresh[i] = 0;
+        const size_t n = (size_t)p.n;
+        float* cf = p.cf;
+        const St<double> prim = C5(p, F_PRIM, i);
+        const bool pos = gt0_64(prim.q[0]);
+        const bool reset = lt0_64(prim.q[0]) || lt0_64(prim.q[4]);  // check_physical zeroes the state
+        St<float> w;
+#pragma unroll
+        for (int q = 0; q < 5; q++) w.q[q] = (float)prim.q[q];
+        float gr[15];
+#pragma unroll
+        for (int q = 0; q < 15; q++) gr[q] = (float)C(p, F_GRAD + q, i);
+        const V3<float> vr = cvt<float>(C3(p, F_VREL, i));
+        const Gas<float> g = gas_t<float>(p);
+        const float rho_inv = 1.f / w.q[0];
+        const float div_v = gr[3] + gr[7] + gr[11];
+        const V3<float> g0 = v3(gr[0], gr[1], gr[2]), g4 = v3(gr[12], gr[13], gr[14]);
+        St<float> src;  // Particle::time_extrapolations before the -dt factor (part.rs:134-149)
+        src.q[0] = w.q[0] * div_v + dot(vr, g0);
+        src.q[1] = vr.x * div_v + rho_inv * g4.x;
+        src.q[2] = vr.y * div_v + rho_inv * g4.y;
+        src.q[3] = vr.z * div_v + rho_inv * g4.z;
+        src.q[4] = g.gamma * w.q[4] * div_v + dot(vr, g4);
+        St<double> ex = C5(p, F_EXTRAP, i);
+#pragma unroll
+        for (int q = 0; q < 5; q++) ex.q[q] = pos ? ex.q[q] + (-dt) * (double)src.q[q] : ex.q[q] + 0.;
+        W5(p, F_EXTRAP, i, ex);
+        if (reset) W5(p, F_PRIM, i, st_zero<double>());
+        const bool live = pos && !reset;  // the checked density is positive
+#pragma unroll
+        for (int q = 0; q < 5; q++) {
+            cf[(G_PRIM + q) * n + i] = reset ? 0.f : w.q[q];
+            cf[(G_EXTRAP + q) * n + i] = (float)ex.q[q];
+            cf[(G_SRC + q) * n + i] = live ? src.q[q] : 0.f;
+        }
+#pragma unroll
+        for (int q = 0; q < 15; q++) cf[(G_GRAD + q) * n + i] = gr[q];
+        cf[G_CS * n + i] = live ? g.sound_speed(w.q[4], rho_inv) : 0.f;
+        const V3<double> dgc = C3(p, F_GC, i) - C3(p, F_LOC, i);
+        const V3<double> v = C3(p, F_V, i);
+        cf[(G_DGC + 0) * n + i] = (float)dgc.x;
+        cf[(G_DGC + 1) * n + i] = (float)dgc.y;
+        cf[(G_DGC + 2) * n + i] = (float)dgc.z;
+        cf[(G_V + 0) * n + i] = (float)v.x;
+        cf[(G_V + 1) * n + i] = (float)v.y;
+        cf[(G_V + 2) * n + i] = (float)v.z;
+    }
+    inst_count(p, k, act, CNT_CELLS);
+}
+
 // hierarchical steps convert only the cells on the step's cell list
 __global__ void __launch_bounds__(kMaxBlock) k_prep32(KP p) {
     const int n_items = cell_items(p);
@@ -565,6 +633,10 @@ __global__ void k_riemann32(double gamma, int64_t n, const double* l, const doub
 inline int grid(int n, int b = kBlock) { return (n + b - 1) / b; }
 
 }  // namespace
+
+void launch_predict32(const KP& p, cudaStream_t s) {
+    if (p.n > 0) k_predict32<<<grid(p.n, p.blk_cell), p.blk_cell, 0, s>>>(p);
+}
 
 void launch_prep32(const KP& p, cudaStream_t s) {
     if (p.n > 0) k_prep32<<<cell_grid(p), p.blk_cell, 0, s>>>(p);

@@ -28,7 +28,7 @@ __device__ __forceinline__ St<double> extrap_source(const KP& p, int i, const St
 // Face-stage derived fields: extrapolation source and v_max sound speed.
 __device__ __forceinline__ void write_derived(const KP& p, int i, const St<double>& prim, const St<double>& src,
                                               double rho_inv) {
-    if (prim.q[0] > 0.) {
+    if (gt0_64(prim.q[0])) {
         W5(p, F_SRC, i, src);
         W(p, F_CS, i, gas(p).sound_speed(prim.q[4], rho_inv));
     } else {
@@ -59,23 +59,29 @@ __global__ void __launch_bounds__(kMaxBlock) k_predict(KP p) {
             // prim, grad and v_rel are unchanged since this cell's source row was
             // written (it was not active, nothing was uploaded): the same bits
             St<double> ex = C5(p, F_EXTRAP, i);
-            if (C(p, F_PRIM, i) > 0.) W5(p, F_EXTRAP, i, ex + (-dt) * C5(p, F_SRC, i));
+            if (gt0_64(C(p, F_PRIM, i))) W5(p, F_EXTRAP, i, ex + (-dt) * C5(p, F_SRC, i));
             else W5(p, F_EXTRAP, i, ex + st_zero<double>());
         } else {
             St<double> prim = C5(p, F_PRIM, i);
             double rho_inv = 1. / prim.q[0];
             St<double> src = extrap_source(p, i, prim, rho_inv);
-            if (prim.q[0] > 0.) {
+            if (gt0_64(prim.q[0])) {
                 St<double> ex = C5(p, F_EXTRAP, i);
                 W5(p, F_EXTRAP, i, ex + (-dt) * src);
             } else {
                 St<double> ex = C5(p, F_EXTRAP, i);
                 W5(p, F_EXTRAP, i, ex + st_zero<double>());
             }
+            // check_physical (physical_quantities.rs:245-254) zeroes the state
+            // where density or pressure is negative; compared bitwise, so that
+            // a NaN component also counts as reset, as the float comparison did
             St<double> chk = prim;
-            check_physical(chk);
-            bool reset = chk.q[0] != prim.q[0] || chk.q[4] != prim.q[4] || chk.q[1] != prim.q[1] ||
-                         chk.q[2] != prim.q[2] || chk.q[3] != prim.q[3];
+            if (lt0_64(prim.q[0]) || lt0_64(prim.q[4])) chk = st_zero<double>();
+            bool reset = false;
+#pragma unroll
+            for (int q = 0; q < 5; q++)
+                reset = reset || __double_as_longlong(chk.q[q]) != __double_as_longlong(prim.q[q]) ||
+                        is_nan64(prim.q[q]);
             if (reset) W5(p, F_PRIM, i, chk);
             // volume: dvdt is zero for a fixed mesh, so volume.clamp(..) leaves it unchanged
             write_derived(p, i, chk, src, rho_inv);
@@ -323,13 +329,13 @@ __global__ void __launch_bounds__(kMaxBlock) k_compact(KP p) {
 // Particle::convert_conserved_to_primitive (part.rs:219-261)
 __device__ __forceinline__ void c2p(const KP& p, int i, const St<double>& cons, unsigned int* err) {
     const Gas<double> g = gas(p);
-    if (!(cons.q[0] >= 0.)) *err |= 1u << 2;
-    if (!(cons.q[4] >= 0.)) *err |= 1u << 3;
+    if (!ge0_64(cons.q[0])) *err |= 1u << 2;
+    if (!ge0_64(cons.q[4])) *err |= 1u << 3;
     St<double> prim;
-    if (cons.q[0] == 0.) {
-        if (cons.q[4] != 0.) *err |= 1u << 3;
+    if (is_zero64(cons.q[0])) {
+        if (!is_zero64(cons.q[4])) *err |= 1u << 3;
         prim = st_zero<double>();
-    } else if (cons.q[0] > 0.) {  // State<Primitive>::from_conserved (physical_quantities.rs:213-226)
+    } else if (gt0_64(cons.q[0])) {  // State<Primitive>::from_conserved (physical_quantities.rs:213-226)
         double m_inv = 1. / cons.q[0];
         double density = cons.q[0] / C(p, F_VOL, i);
         V3<double> velocity = m_inv * vel(cons);
@@ -340,9 +346,9 @@ __device__ __forceinline__ void c2p(const KP& p, int i, const St<double>& cons, 
     } else {
         prim = st_zero<double>();
     }
-    if (!(prim.q[0] >= 0.) || !(prim.q[4] >= 0.)) *err |= 1u << 5;
-    if (!isfinite(prim.q[0]) || !isfinite(prim.q[1]) || !isfinite(prim.q[2]) || !isfinite(prim.q[3]) ||
-        !isfinite(prim.q[4]))
+    if (!ge0_64(prim.q[0]) || !ge0_64(prim.q[4])) *err |= 1u << 5;
+    if (!is_finite64(prim.q[0]) || !is_finite64(prim.q[1]) || !is_finite64(prim.q[2]) ||
+        !is_finite64(prim.q[3]) || !is_finite64(prim.q[4]))
         *err |= 1u << 4;
     W5(p, F_PRIM, i, prim);
 }
@@ -429,11 +435,11 @@ __device__ __forceinline__ void update_finish(const KP& p, int i, int k, bool ac
     if (act) {
         p.fresh[i] = 0;  // prim (here), grad and v_rel (gradient stage) change
         St<double> cons = C5(p, F_CONS, i) + facc;
-        if (!isfinite(cons.q[0]) || !isfinite(cons.q[1]) || !isfinite(cons.q[2]) || !isfinite(cons.q[3]) ||
-            !isfinite(cons.q[4]))
+        if (!is_finite64(cons.q[0]) || !is_finite64(cons.q[1]) || !is_finite64(cons.q[2]) ||
+            !is_finite64(cons.q[3]) || !is_finite64(cons.q[4]))
             err |= 1u << 4;
-        if (cons.q[0] < 0.) cons = st_zero<double>();
-        if (cons.q[4] < 0.) cons = st_zero<double>();
+        if (lt0_64(cons.q[0])) cons = st_zero<double>();
+        if (lt0_64(cons.q[4])) cons = st_zero<double>();
         facc = st_zero<double>();
         // kick2 (runner/hydrodynamics.rs:51-57): Particle::grav_kick with a zero
         // acceleration adds +0 to the momentum (part.rs:303-312)
