@@ -238,7 +238,7 @@ def face_stage_kernels(prec, all_cells):
 # DRAM bytes (read + write) per launch of the face stage from ncu captures at
 # the bench sizes (cold caches, ncu's default cache control): the committed
 # summaries in profiles/ give the commands.  Keyed by (workload, nx, form).
-TRAFFIC = {("kh2d", 256, 1): 26_909_440, ("kh2d", 256, 0): 40_748_544}  # profiles/face_stage_traffic_kh256.txt
+TRAFFIC = {("kh2d", 256, 1): 26_908_928, ("kh2d", 256, 0): 40_718_080}  # profiles/face_stage_traffic_kh256.txt
 
 
 def _face_kernel_ms(sim, steps):
@@ -434,8 +434,9 @@ def run_ours(args):
                         "state comes back in place, only the 8 KB chunks it changed)") +
                        ", one pinned host block in the device field order, wall clock, bytes as counted "
                        "by the library"},
-        # per step: predict, [compact], [prep32], face, update, gradients, limiter (timed for both forms)
-        "gpu_launches": args.steps * ((6 + 5) + (2 if (not batch and not problem.params.sync_all) else 0)),
+        # per step, both forms timed: over all cells k_predict32 / k_predict, face, update, gradients,
+        # limiter (5 + 5); hierarchical steps add k_compact to both and k_prep32 to the FP32 form
+        "gpu_launches": args.steps * ((5 + 5) + (3 if (not batch and not problem.params.sync_all) else 0)),
         "clocks": clocks,
     }
     print(json.dumps(line))
