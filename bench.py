@@ -372,7 +372,12 @@ def run_ours(args):
     batch_info = None
     if batch:
         st = sims[1].batch_state()
+        st64 = sims[0].batch_state()
+        # instances stopped by a numerical failure (the reference panics there), after
+        # each form's own number of steps in this process
         batch_info = {"instances": int(len(st["err"])), "flagged_instances": int((st["err"] != 0).sum()),
+                      "flagged_instances_fp64": int((st64["err"] != 0).sum()),
+                      "steps": {"fp32_face": int(st["steps"].max()), "fp64": int(st64["steps"].max())},
                       "finished_instances": int(st["finished"].sum()),
                       "autotuned_blocks": {"fp32_face": tuned.get(1), "fp64": tuned.get(0)},
                       "graph": "each batched step is one CUDA graph launch over all unfinished simulations"}
