@@ -29,7 +29,7 @@ CU_SOURCES = {
     "mvmm_api.cu": [],
     "noalloc.cu": ["-fmad=false"],
 }
-HEADERS = ["mvmm_device.cuh", "mvmm_internal.h", "mvmm_cellops.cuh"]
+HEADERS = ["mvmm_device.cuh", "mvmm_internal.h", "mvmm_cellops.cuh", "bitconv.cuh"]
 
 
 def _nvcc() -> str:

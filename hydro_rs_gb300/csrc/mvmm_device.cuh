@@ -12,6 +12,7 @@
 #include <math.h>
 #include <stdint.h>
 
+#include "bitconv.cuh"
 #include "mvmm_internal.h"
 
 namespace mvmm {
@@ -75,6 +76,13 @@ __device__ __forceinline__ V3<T> cross(V3<T> a, V3<T> b) {  // glam DVec3::cross
 }
 template <typename T, typename U>
 __device__ __forceinline__ V3<T> cvt(V3<U> a) { return {T(a.x), T(a.y), T(a.z)}; }
+// FP64 <-> FP32 conversions of the cell kernels, on the integer pipe
+// (bitconv.cuh): the same values as the conversion instructions, which share
+// the slow FP64 pipe.
+__device__ __forceinline__ float f32(double x) { return bitconv::to_f32_rn(x); }
+__device__ __forceinline__ double f64(float x) { return bitconv::to_f64(x); }
+__device__ __forceinline__ V3<float> f32v(V3<double> a) { return {f32(a.x), f32(a.y), f32(a.z)}; }
+__device__ __forceinline__ V3<double> f64v(V3<float> a) { return {f64(a.x), f64(a.y), f64(a.z)}; }
 
 // State<T>(f64, DVec3, f64): 0 density/mass, 1..3 velocity/momentum, 4 pressure/energy.
 template <typename T>

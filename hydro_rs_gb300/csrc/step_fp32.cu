@@ -35,22 +35,22 @@ __device__ __forceinline__ void prep32_cell(const KP& p, int i) {
     float* cf = p.cf;
 #pragma unroll
     for (int q = 0; q < 5; q++) {
-        cf[(G_PRIM + q) * n + i] = (float)C(p, F_PRIM + q, i);
-        cf[(G_EXTRAP + q) * n + i] = (float)C(p, F_EXTRAP + q, i);
-        cf[(G_SRC + q) * n + i] = (float)C(p, F_SRC + q, i);
+        cf[(G_PRIM + q) * n + i] = f32(C(p, F_PRIM + q, i));
+        cf[(G_EXTRAP + q) * n + i] = f32(C(p, F_EXTRAP + q, i));
+        cf[(G_SRC + q) * n + i] = f32(C(p, F_SRC + q, i));
     }
 #pragma unroll
-    for (int q = 0; q < 15; q++) cf[(G_GRAD + q) * n + i] = (float)C(p, F_GRAD + q, i);
-    cf[G_CS * n + i] = (float)C(p, F_CS, i);
+    for (int q = 0; q < 15; q++) cf[(G_GRAD + q) * n + i] = f32(C(p, F_GRAD + q, i));
+    cf[G_CS * n + i] = f32(C(p, F_CS, i));
     V3<double> loc = C3(p, F_LOC, i);
     V3<double> dgc = C3(p, F_GC, i) - loc;
     V3<double> v = C3(p, F_V, i);
-    cf[(G_DGC + 0) * n + i] = (float)dgc.x;
-    cf[(G_DGC + 1) * n + i] = (float)dgc.y;
-    cf[(G_DGC + 2) * n + i] = (float)dgc.z;
-    cf[(G_V + 0) * n + i] = (float)v.x;
-    cf[(G_V + 1) * n + i] = (float)v.y;
-    cf[(G_V + 2) * n + i] = (float)v.z;
+    cf[(G_DGC + 0) * n + i] = f32(dgc.x);
+    cf[(G_DGC + 1) * n + i] = f32(dgc.y);
+    cf[(G_DGC + 2) * n + i] = f32(dgc.z);
+    cf[(G_V + 0) * n + i] = f32(v.x);
+    cf[(G_V + 1) * n + i] = f32(v.y);
+    cf[(G_V + 2) * n + i] = f32(v.z);
 }
 // Steps over all cells (synchronised steps, batches): EulerEqnsFvs::predict
 // (Particle::extrapolate_state, part.rs:123-132, with the active mask of
@@ -81,8 +81,8 @@ __global__ void __launch_bounds__(kMaxBlock) k_predict32(KP p) {
         for (int q = 0; q < 5; q++) w.q[q] = (float)prim.q[q];
         float gr[15];
 #pragma unroll
-        for (int q = 0; q < 15; q++) gr[q] = (float)C(p, F_GRAD + q, i);
-        const V3<float> vr = cvt<float>(C3(p, F_VREL, i));
+        for (int q = 0; q < 15; q++) gr[q] = f32(C(p, F_GRAD + q, i));
+        const V3<float> vr = f32v(C3(p, F_VREL, i));
         const Gas<float> g = gas_t<float>(p);
         const float rho_inv = 1.f / w.q[0];
         const float div_v = gr[3] + gr[7] + gr[11];
@@ -95,14 +95,14 @@ __global__ void __launch_bounds__(kMaxBlock) k_predict32(KP p) {
         src.q[4] = g.gamma * w.q[4] * div_v + dot(vr, g4);
         St<double> ex = C5(p, F_EXTRAP, i);
 #pragma unroll
-        for (int q = 0; q < 5; q++) ex.q[q] = pos ? ex.q[q] + (-dt) * (double)src.q[q] : ex.q[q] + 0.;
+        for (int q = 0; q < 5; q++) ex.q[q] = pos ? ex.q[q] + (-dt) * f64(src.q[q]) : ex.q[q] + 0.;
         W5(p, F_EXTRAP, i, ex);
         if (reset) W5(p, F_PRIM, i, st_zero<double>());
         const bool live = pos && !reset;  // the checked density is positive
 #pragma unroll
         for (int q = 0; q < 5; q++) {
             cf[(G_PRIM + q) * n + i] = reset ? 0.f : w.q[q];
-            cf[(G_EXTRAP + q) * n + i] = (float)ex.q[q];
+            cf[(G_EXTRAP + q) * n + i] = f32(ex.q[q]);
             cf[(G_SRC + q) * n + i] = live ? src.q[q] : 0.f;
         }
 #pragma unroll
@@ -110,12 +110,12 @@ __global__ void __launch_bounds__(kMaxBlock) k_predict32(KP p) {
         cf[G_CS * n + i] = live ? g.sound_speed(w.q[4], rho_inv) : 0.f;
         const V3<double> dgc = C3(p, F_GC, i) - C3(p, F_LOC, i);
         const V3<double> v = C3(p, F_V, i);
-        cf[(G_DGC + 0) * n + i] = (float)dgc.x;
-        cf[(G_DGC + 1) * n + i] = (float)dgc.y;
-        cf[(G_DGC + 2) * n + i] = (float)dgc.z;
-        cf[(G_V + 0) * n + i] = (float)v.x;
-        cf[(G_V + 1) * n + i] = (float)v.y;
-        cf[(G_V + 2) * n + i] = (float)v.z;
+        cf[(G_DGC + 0) * n + i] = f32(dgc.x);
+        cf[(G_DGC + 1) * n + i] = f32(dgc.y);
+        cf[(G_DGC + 2) * n + i] = f32(dgc.z);
+        cf[(G_V + 0) * n + i] = f32(v.x);
+        cf[(G_V + 1) * n + i] = f32(v.y);
+        cf[(G_V + 2) * n + i] = f32(v.z);
     }
     inst_count(p, k, act, CNT_CELLS);
 }
@@ -185,12 +185,12 @@ __global__ void __launch_bounds__(kMaxBlock) k_geom32(KP p) {
     const size_t nf = (size_t)p.nf;
 #pragma unroll
     for (int k = 0; k < 8; k++) {
-        g[(3 * k + 0) * nf + f] = (float)vals[k].x;
-        g[(3 * k + 1) * nf + f] = (float)vals[k].y;
-        g[(3 * k + 2) * nf + f] = (float)vals[k].z;
+        g[(3 * k + 0) * nf + f] = f32(vals[k].x);
+        g[(3 * k + 1) * nf + f] = f32(vals[k].y);
+        g[(3 * k + 2) * nf + f] = f32(vals[k].z);
     }
-    g[GE_W * nf + f] = (float)(p.area[f] / len2(ds));
-    g[GE_A * nf + f] = (float)p.area[f];
+    g[GE_W * nf + f] = f32(p.area[f] / len2(ds));
+    g[GE_A * nf + f] = f32(p.area[f]);
 }
 
 __device__ __forceinline__ St<float> reconstruct32(const KP& p, int i, const St<float>& prim, V3<float> dx, float td) {
@@ -445,7 +445,7 @@ __device__ __forceinline__ void gradients32_cell(const KP& p, int i) {
             for (int q = 0; q < 5; q++) {
                 float alpha = (emx[q] == 0.f || emn[q] == 0.f) ? 1.f : fminf(1.f, fminf(dmx[q] / emx[q], dmn[q] / emn[q]));
                 gr[q] = alpha * gr[q];
-                W3(p, F_GRAD + 3 * q, i, cvt<double>(gr[q]));
+                W3(p, F_GRAD + 3 * q, i, f64v(gr[q]));
             }
             V3<double> cen = C3(p, F_CEN, i);
             W3(p, F_GC, i, cen);
@@ -561,7 +561,7 @@ __device__ __forceinline__ void gradients32_cell_warp(const KP& p, int i, int la
                 }
                 float alpha = (emx[q] == 0.f || emn[q] == 0.f) ? 1.f : fminf(1.f, fminf(dmx[q] / emx[q], dmn[q] / emn[q]));
                 gr[q] = alpha * gr[q];
-                if (lane == 0) W3(p, F_GRAD + 3 * q, i, cvt<double>(gr[q]));
+                if (lane == 0) W3(p, F_GRAD + 3 * q, i, f64v(gr[q]));
             }
             if (lane == 0) W3(p, F_GC, i, C3(p, F_CEN, i));
           }

@@ -402,10 +402,10 @@ __device__ __forceinline__ void update_cell(const KP& p, int i, int do_c2p) {
             ar = fmaxf(ar, fl[6 * nf + f]);
         }
 #pragma unroll
-        for (int q = 0; q < 5; q++) facc.q[q] = facc.q[q] + ((double)acc[q].hi + (double)acc[q].lo);
+        for (int q = 0; q < 5; q++) facc.q[q] = facc.q[q] + (f64(acc[q].hi) + f64(acc[q].lo));
         if (act && k1 > k0) {
-            msv = m_max((double)vm, msv);
-            maor = m_max(maor, (double)ar);
+            msv = m_max(f64(vm), msv);
+            maor = m_max(maor, f64(ar));
         }
     } else {
         const int rv = p.flux_rows == 10 ? 8 : 5;
@@ -453,7 +453,7 @@ __device__ __forceinline__ void update_finish(const KP& p, int i, int k, bool ac
             c2p(p, i, cons, &err);
             if (p.fp32) {  // FP32 copies read by the FP32-face form's gradient stage
 #pragma unroll
-                for (int q = 0; q < 5; q++) p.cf[(size_t)(G_PRIM + q) * p.n + i] = (float)C(p, F_PRIM + q, i);
+                for (int q = 0; q < 5; q++) p.cf[(size_t)(G_PRIM + q) * p.n + i] = f32(C(p, F_PRIM + q, i));
             }
         }
     }
@@ -526,10 +526,10 @@ __device__ __forceinline__ void update_cell_warp(const KP& p, int i, int do_c2p,
     }
     if (ROWS32) {
 #pragma unroll
-        for (int q = 0; q < 5; q++) facc.q[q] = facc.q[q] + ((double)acc[q].hi + (double)acc[q].lo);
+        for (int q = 0; q < 5; q++) facc.q[q] = facc.q[q] + (f64(acc[q].hi) + f64(acc[q].lo));
         if (act && deg > 0) {
-            msv = m_max((double)vm32, msv);
-            maor = m_max(maor, (double)ar32);
+            msv = m_max(f64(vm32), msv);
+            maor = m_max(maor, f64(ar32));
         }
     }
     if (lane == 0) update_finish(p, i, k, act, facc, msv, maor, do_c2p);
