@@ -106,10 +106,17 @@ def _problem(nx=NX, workload="kh2d"):
 
 
 def _cpu_sample(problem, label, budget_s: float = 10.0, max_steps: int = 400):
-    """The oracle on the host cores: warm-up step, then steps until the budget."""
+    """The oracle on all host cores, and beside it on one core (a shorter sample)."""
+    out = _cpu_sample_threads(problem, label, os.cpu_count() or 1, budget_s, max_steps)
+    one = _cpu_sample_threads(problem, label, 1, budget_s / 3, max_steps)
+    out["one_thread"] = {"value": one["value"], "sample": one["sample"]}
+    return out
+
+
+def _cpu_sample_threads(problem, label, threads, budget_s, max_steps):
+    """The oracle on `threads` host threads: warm-up step, then steps until the budget."""
     from oracle import oracle as O
 
-    threads = os.cpu_count() or 1
     if "problems" in problem.extra:  # a batch: the oracle runs one simulation after another
         faces, dt, n = 0, 0.0, 0
         for q in problem.extra["problems"]:
@@ -141,7 +148,8 @@ def _cpu_sample(problem, label, budget_s: float = 10.0, max_steps: int = 400):
     faces = sim.active_faces - f0
     return {"value": faces / dt, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"{n} OptimalOrder steps of the same workload ({label}; {faces} face updates, "
-                      f"{dt:.1f} s wall) after 2 warm-up steps; C restatement of the reference, OpenMP"}
+                      f"{dt:.1f} s wall) after 2 warm-up steps; C restatement of the reference, OpenMP, "
+                      f"{threads} thread(s)"}
 
 
 class _Clocks:
@@ -227,6 +235,16 @@ def face_stage_bytes(prec, nc, nfa, all_cells):
     if prec == 1:
         return (0 if all_cells else touched * 468) + touched * 157 + nfa * 140
     return touched * 353 + nfa * 144
+
+
+# Compulsory HBM bytes of a whole step, each datum once: 88 B per active face
+# (indices, area, normal, centroid, shift) and per active cell 800 B in the
+# plain form (the flux-stage state read 328, extrapolation write 40, flux
+# accumulator and conserved read+write 160, signal-speed rows 16, c2p 48,
+# gradient write 144, timestep writes 64); the FP32-face form's face stage
+# reads FP32 copies (164 B instead of 328): 636 B.
+STEP_BYTES_FACE = 88
+STEP_BYTES_CELL = {0: 800, 1: 636}
 
 
 def face_stage_kernels(prec, all_cells):
@@ -319,12 +337,14 @@ def run_ours(args):
     same_time = sims[1].ti_current == sims[0].ti_current
 
     # per-kernel times (events around each kernel) for the roofline
-    prof, nfa = {}, {}
+    prof, nfa, nca = {}, {}, {}
     for prec, sim in sims.items():
         k_prof = min(args.steps, 20)
-        f0 = sim.stats()["active_faces"]
+        st0 = sim.stats()
         prof[prec] = _face_kernel_ms(sim, k_prof)
-        nfa[prec] = (sim.stats()["active_faces"] - f0) / k_prof  # active faces per profiled step
+        st1 = sim.stats()
+        nfa[prec] = (st1["active_faces"] - st0["active_faces"]) / k_prof  # active faces per profiled step
+        nca[prec] = (st1["active_cells"] - st0["active_cells"]) / k_prof  # active cells per profiled step
 
     # end-to-end through the C ABI with pinned host buffers: one pinned block in
     # the device's field order, stepped in place
@@ -413,6 +433,15 @@ def run_ours(args):
                 "peak_kind": peak_kind, "note": "of measured" if peak_kind == "measured" else "of fallback",
                 "step_kernel_ms": {k: round(v[0] / max(v[1], 1), 4) for k, v in prof[prec].items()}}
 
+    def step_roof(prec, ms_step):
+        b = STEP_BYTES_FACE * nfa[prec] + STEP_BYTES_CELL[prec] * nca[prec]
+        ach = b / (ms_step * 1e-3) / 1e9
+        return {"bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s", "frac": round(ach / peak, 4),
+                "bytes_per_step": int(b), "active_faces_per_step": nfa[prec], "active_cells_per_step": nca[prec],
+                "bytes_per_face": STEP_BYTES_FACE, "bytes_per_cell": STEP_BYTES_CELL[prec],
+                "note": "whole step (all kernels) over ms_per_step; " +
+                        ("of measured" if peak_kind == "measured" else "of fallback")}
+
     cpu = _cpu_sample(problem, WORKLOADS[args.workload].format(n=args.nx)) if (ws == 1 and not args.no_cpu) else None
     value = faces32 / (ms32 * 1e-3)
     line = {
@@ -430,8 +459,9 @@ def run_ours(args):
         "active_face_fraction": faces32 / (args.steps * nf * ws),
         "batch": batch_info,
         "plain_fp64": {"value": faces64 / (ms64 * 1e-3), "unit": UNIT, "ms_per_step": ms64 / args.steps,
-                       "roofline": roof(0)},
+                       "roofline": roof(0), "step_roofline": step_roof(0, ms64 / args.steps)},
         "roofline": roof(1),
+        "step_roofline": step_roof(1, ms32 / args.steps),
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_faces / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d_step),
                 "d2h_bytes_per_step": int(d2h_step), "host_block_bytes": bytes_cells, "steps": e2e_steps,
@@ -470,6 +500,7 @@ def run_serve(args):
         res, wall = srv.run(reqs, realtime=True)
     clocks = clk.summary(0)
     summ = serve.latency_summary(res, wall)
+    accuracy = _serve_accuracy(srv, reqs, check_oracle=not args.no_cpu)
     cpu = None
     if not args.no_cpu:
         from oracle import oracle as O
@@ -499,10 +530,45 @@ def run_serve(args):
                    "chunk_steps": srv.chunk, "mesh_build_s": round(mesh_s, 2)},
         "serving": {k: v for k, v in summ.items()} | {"peak_concurrent": srv.peak_running,
                                                        "slots": len(srv.slots), "slot_bytes": srv.used},
-        "cpu_baseline": cpu, "clocks": clocks,
+        "accuracy": accuracy, "cpu_baseline": cpu, "clocks": clocks,
     }
     srv.close()
     print(json.dumps(line))
+
+
+def _serve_accuracy(srv, reqs, check_oracle: bool, n_check: int = 3):
+    """L1 density errors of served requests (untimed): the smallest requests solved
+    alone with the server's form (served results are bit-identical to those,
+    tests/test_gpu_serve.py), against the analytic solution (the initial vortex
+    carried by the advection velocity through the periodic box) and against the
+    oracle."""
+    import numpy as np
+
+    from hydro_rs_gb300 import gpu as G
+    from hydro_rs_gb300 import ics
+
+    out = []
+    for r in sorted(reqs, key=lambda r: (r.nx, r.rid))[:n_check]:
+        q = srv.problem_for(r)
+        sim = G.GpuSim(q, precision=srv.precision)
+        sim.run()
+        st = sim.state()
+        sim.close()
+        box = 10.0
+        x = np.array(st.loc, dtype=np.float64)  # the initial state samples the vortex at the generators
+        x[:2] = np.mod(x[:2] - np.asarray(r.v_adv, dtype=np.float64)[:2, None] * r.t_end, box)
+        exact = ics.yee_cells(q.mesh, x, r.beta, r.v_adv).prim[0]
+        row = {"rid": r.rid, "nx": r.nx, "beta": round(r.beta, 3),
+               "l1_vs_analytic": float(np.abs(st.prim[0] - exact).sum() / np.abs(exact).sum())}
+        if check_oracle:
+            from oracle import oracle as O
+
+            o = O.OracleSim(q, n_threads=os.cpu_count() or 1)
+            o.run()
+            ref = o.state().prim[0]
+            row["l1_vs_oracle"] = float(np.abs(st.prim[0] - ref).sum() / np.abs(ref).sum())
+        out.append(row)
+    return out
 
 
 def run_moving(args):
