@@ -246,6 +246,11 @@ def face_stage_bytes(prec, nc, nfa, all_cells):
 STEP_BYTES_FACE = 88
 STEP_BYTES_CELL = {0: 800, 1: 636}
 
+# FP64 flop per face of the plain face kernel (2 DFMA + DMUL + DADD, active
+# threads) from an ncu capture at the bench size: profiles/face_flux_fp64_pipes_kh256.txt.
+FP64_FLOP_PER_FACE = {("kh2d", 256): 1610}
+FP64_DFMA_PER_SM_CLK = 2  # GB300: FP64 at 1/64 of the FP32 rate
+
 
 def face_stage_kernels(prec, all_cells):
     if prec == 0:
@@ -433,6 +438,22 @@ def run_ours(args):
                 "peak_kind": peak_kind, "note": "of measured" if peak_kind == "measured" else "of fallback",
                 "step_kernel_ms": {k: round(v[0] / max(v[1], 1), 4) for k, v in prof[prec].items()}}
 
+    def fp64_roof():
+        # the plain face kernel against the FP64 pipe: flop per face (measured once
+        # by ncu at this size) x active faces / the kernel's event time, against
+        # 2 DFMA (4 flop) per clock per SM at the SM clock sampled during the run
+        fpf = FP64_FLOP_PER_FACE.get((args.workload, args.nx))
+        if fpf is None:
+            return None
+        ms, n = prof[0]["face_flux"]
+        ach = fpf * nfa[0] / (ms / max(n, 1) * 1e-3) / 1e12
+        sm_mhz = (clocks or {}).get("sm_mhz") or 2070.0
+        peak64 = torch.cuda.get_device_properties(dev).multi_processor_count * FP64_DFMA_PER_SM_CLK * 2 * sm_mhz * 1e6 / 1e12
+        return {"bound": "fp64", "achieved": round(ach, 4), "peak": round(peak64, 3), "unit": "TFLOP/s",
+                "frac": round(ach / peak64, 4), "flop_per_face": fpf, "kernel": "k_face_flux",
+                "note": "FP64 pipe 76-79% busy in ncu: warps with few active lanes (the Brent iteration) and "
+                        "non-flop FP64 work hold it"}
+
     def step_roof(prec, ms_step):
         b = STEP_BYTES_FACE * nfa[prec] + STEP_BYTES_CELL[prec] * nca[prec]
         ach = b / (ms_step * 1e-3) / 1e9
@@ -459,7 +480,8 @@ def run_ours(args):
         "active_face_fraction": faces32 / (args.steps * nf * ws),
         "batch": batch_info,
         "plain_fp64": {"value": faces64 / (ms64 * 1e-3), "unit": UNIT, "ms_per_step": ms64 / args.steps,
-                       "roofline": roof(0), "step_roofline": step_roof(0, ms64 / args.steps)},
+                       "roofline": roof(0), "step_roofline": step_roof(0, ms64 / args.steps),
+                       "fp64_roofline": fp64_roof()},
         "roofline": roof(1),
         "step_roofline": step_roof(1, ms32 / args.steps),
         "cpu_baseline": cpu,

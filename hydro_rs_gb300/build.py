@@ -3,7 +3,9 @@
 * ``_build/libmvmm_gpu.so``  - the CUDA library behind ``include/mvmm_gpu.h``,
   compiled for sm_103a only.  ``step_fp64.cu`` is compiled with ``-fmad=false``
   so the plain form never contracts a*b+c (the Rust reference never does);
-  ``step_fp32.cu`` keeps FMA contraction.
+  ``step_fp32.cu`` (the FP32-face form, held to an error bound rather than to
+  the reference's roundings) keeps FMA contraction and uses the approximate
+  FP32 division and square root (``-prec-div=false -prec-sqrt=false``, ~2 ulp).
 * ``_build/libmvmm_mesh.so`` - the host Voronoi mesh builder (g++ / OpenMP).
 
 Sources are compiled in parallel; up-to-date objects are reused.
@@ -25,7 +27,7 @@ NVCC_COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "
 
 CU_SOURCES = {
     "step_fp64.cu": ["-fmad=false"],
-    "step_fp32.cu": ["-fmad=true"],
+    "step_fp32.cu": ["-fmad=true", "-prec-div=false", "-prec-sqrt=false"],
     "mvmm_api.cu": [],
     "noalloc.cu": ["-fmad=false"],
 }

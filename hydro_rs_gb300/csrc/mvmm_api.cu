@@ -86,6 +86,7 @@ struct mvmm_ctx {
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     cudaGraphExec_t step_exec = nullptr;
+    cudaGraphExec_t prof_exec = nullptr;  // the step graph with the per-kernel timing events
     bool prof = false;
     cudaEvent_t ev[MVMM_NUM_KERNELS + 1] = {};
     cudaStream_t side = nullptr;              // copies of mvmm_step_cells that overlap the step
@@ -230,11 +231,15 @@ struct StepHooks {
     cudaEvent_t after_gradients = nullptr;
 };
 
+// The per-kernel timing events; recorded as event nodes when the step is
+// captured into the profiling graph.
+void record_ev(mvmm_ctx* c, int j, cudaStream_t s) { cudaEventRecordWithFlags(c->ev[j], s, cudaEventRecordExternal); }
+
 void enqueue_step_kernels(mvmm_ctx* c, bool with_events, const StepHooks& h = StepHooks()) {
     KP p = make_kp(c, 0, 7);
     p.stale_all = h.stale_all ? 1 : 0;
     cudaStream_t s = c->stream;
-    if (with_events) cudaEventRecord(c->ev[0], s);
+    if (with_events) record_ev(c, 0, s);
     // steps over all cells of the FP32-face form: predict and the FP32 copies in one kernel
     const bool fused = c->prm.precision == MVMM_PRECISION_FP32FACE && !p.use_list;
     if (fused) launch_predict32(p, s);
@@ -243,39 +248,64 @@ void enqueue_step_kernels(mvmm_ctx* c, bool with_events, const StepHooks& h = St
     if (h.geom_before_face || c->prm.particle_motion != MVMM_MOTION_FIXED)
         update_geom32(c, p, s);  // generators drifted or uploaded, centroids updated
     if (p.use_list) launch_compact(p, s);
-    if (with_events) cudaEventRecord(c->ev[1], s);
+    if (with_events) record_ev(c, 1, s);
     launch_face(c, p, fused);
-    if (with_events) cudaEventRecord(c->ev[2], s);
+    if (with_events) record_ev(c, 2, s);
     if (h.wait_before_update) cudaStreamWaitEvent(s, h.wait_before_update, 0);
     launch_update(p, 1, s);
     if (h.after_update) cudaEventRecord(h.after_update, s);
-    if (with_events) cudaEventRecord(c->ev[3], s);
+    if (with_events) record_ev(c, 3, s);
     if (c->prm.precision == MVMM_PRECISION_FP32FACE) launch_gradients32(p, s);
     else launch_gradients(p, 1, s);
     if (h.after_gradients) cudaEventRecord(h.after_gradients, s);
-    if (with_events) cudaEventRecord(c->ev[4], s);
+    if (with_events) record_ev(c, 4, s);
     launch_limit(p, s);
-    if (with_events) cudaEventRecord(c->ev[5], s);
+    if (with_events) record_ev(c, 5, s);
     launch_end(p, s);
-    if (with_events) cudaEventRecord(c->ev[6], s);
+    if (with_events) record_ev(c, 6, s);
 }
 
-int build_graph(mvmm_ctx* c) {
-    if (c->step_exec) return MVMM_OK;
+// The step as a CUDA graph; with_events: the profiling variant, with the
+// per-kernel timing events as event-record nodes.
+int build_graph(mvmm_ctx* c, bool with_events = false) {
+    cudaGraphExec_t* exec = with_events ? &c->prof_exec : &c->step_exec;
+    if (*exec) return MVMM_OK;
     cudaGraph_t g;
     CUDA_TRY(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-    enqueue_step_kernels(c, false);
+    enqueue_step_kernels(c, with_events);
     CUDA_TRY(cudaStreamEndCapture(c->stream, &g));
-    cudaError_t e = cudaGraphInstantiate(&c->step_exec, g, 0);
+    cudaError_t e = cudaGraphInstantiate(exec, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return fail(MVMM_E_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
     return MVMM_OK;
 }
 
+// Kernel parameters hold the face count, the buffers and the block sizes:
+// whatever changes them drops the captured step graphs.
+void drop_graphs(mvmm_ctx* c) {
+    for (cudaGraphExec_t* e : {&c->step_exec, &c->prof_exec})
+        if (*e) {
+            cudaGraphExecDestroy(*e);
+            *e = nullptr;
+        }
+}
+
 int enqueue_steps_impl(mvmm_ctx* c, int64_t n) {
     if (c->prof) {
+        // per-kernel timing: a fixed mesh runs the step as the profiling graph,
+        // so that the events time the kernels, not the host's launches
+        const bool fixed = c->prm.particle_motion == MVMM_MOTION_FIXED;
+        if (fixed) {
+            int rc = build_graph(c, true);
+            if (rc) return rc;
+        }
         for (int64_t k = 0; k < n; k++) {
-            enqueue_step_kernels(c, true);
+            if (fixed) {
+                CUDA_TRY(cudaGraphLaunch(c->prof_exec, c->stream));
+            } else {
+                enqueue_step_kernels(c, true);
+                c->pending_geometry = false;
+            }
             CUDA_TRY(cudaEventSynchronize(c->ev[MVMM_NUM_KERNELS]));
             for (int j = 0; j < MVMM_NUM_KERNELS; j++) {
                 float ms = 0;
@@ -574,7 +604,7 @@ int mvmm_batch_state(mvmm_ctx* c, uint64_t* ti_current, uint64_t* ti_old, int64_
 int mvmm_ctx_destroy(mvmm_ctx* c) {
     if (!c) return MVMM_OK;
     if (c->stream) cudaStreamSynchronize(c->stream);
-    if (c->step_exec) cudaGraphExecDestroy(c->step_exec);
+    drop_graphs(c);
     void* ptrs[] = {c->left, c->right, c->csr_off, c->csr_face, c->area, c->normal, c->fcen, c->shift, c->cd,
                     c->cf, c->timebin, c->tb_tmp, c->active, c->flux, c->flux32, c->geo, c->geo_pos, c->geo_changed, c->snap, c->snap_tb, c->xfer_stored, c->dtmp, c->face_stamp, c->touch, c->blocks_done, c->cell_list, c->fresh,
                     c->pend_vol, c->pend_cen,
@@ -1229,10 +1259,7 @@ int mvmm_set_mesh(mvmm_ctx* c, const mvmm_mesh* m, const double* volume, const d
     CUDA_TRY(cudaMemcpyAsync(c->pend_cen, centroid, (size_t)c->n * 24, cudaMemcpyHostToDevice, s));
     c->pending_geometry = true;
     c->geo_built = false;  // new face arrays
-    if (c->step_exec) {  // kernel parameters hold the face count and pointers
-        cudaGraphExecDestroy(c->step_exec);
-        c->step_exec = nullptr;
-    }
+    drop_graphs(c);  // kernel parameters hold the face count and pointers
     CUDA_TRY(cudaStreamSynchronize(s));
     return MVMM_OK;
 }
@@ -1307,10 +1334,7 @@ int mvmm_autotune(mvmm_ctx* c, int steps, int* blk_face, int* blk_cell) {
         for (int j = 0; j < 3; j++) {
             c->blk_face = cand[i];
             c->blk_cell = cand[j];
-            if (c->step_exec) {
-                cudaGraphExecDestroy(c->step_exec);
-                c->step_exec = nullptr;
-            }
+            drop_graphs(c);
             // restore, warm once, time `steps` steps
             cudaMemcpyAsync(c->cd, save, bytes, cudaMemcpyDeviceToDevice, c->stream);
             cudaMemcpyAsync(c->timebin, save_tb, n, cudaMemcpyDeviceToDevice, c->stream);
@@ -1336,10 +1360,7 @@ int mvmm_autotune(mvmm_ctx* c, int steps, int* blk_face, int* blk_cell) {
         }
     c->blk_face = bf;
     c->blk_cell = bc;
-    if (c->step_exec) {
-        cudaGraphExecDestroy(c->step_exec);
-        c->step_exec = nullptr;
-    }
+    drop_graphs(c);
     cudaMemcpyAsync(c->cd, save, bytes, cudaMemcpyDeviceToDevice, c->stream);
     cudaMemcpyAsync(c->timebin, save_tb, n, cudaMemcpyDeviceToDevice, c->stream);
     mark_stale(c, c->stream);
