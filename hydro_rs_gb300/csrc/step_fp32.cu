@@ -369,6 +369,68 @@ __device__ __forceinline__ void other_side32(const KP& p, int i, int f, const St
 // the static face geometry, the WLS sums, the 3x3 inverse and the cell-wise
 // limiter in FP32 (these slopes only feed the FP32 reconstruction); the
 // timestep (Particle::timestep, timesteps_apply) stays FP64 as in the plain form.
+// Particle::set_particle_velocity (part.rs:328-372) and Particle::timestep
+// (part.rs:42-84) in the FP32-face form.  The thermal energy E - p.v/2 and the
+// position differences are formed in FP64 (they cancel); the fluid velocity,
+// sound speed, mesh velocity, |v_rel|, radius and the CFL ratio in FP32.  gr:
+// the cell's (limited) gradients, rows q = 0..4; v and v_rel are stored in FP64.
+__device__ __forceinline__ float radius32(float volume, int dim) {
+    if (dim == 1) return 0.5f * volume;
+    if (dim == 2) return sqrtf(0.31830988618379067154f * volume);
+    return cbrtf(0.25f * 3.f * 0.31830988618379067154f * volume);
+}
+__device__ __forceinline__ V3<float> particle_velocity32(const KP& p, int i, V3<float> fluid_v, float sound_speed,
+                                                         float vol, const V3<float>* gr) {
+    if (p.motion == 0) return v3(0.f, 0.f, 0.f);  // Fixed
+    if (p.motion == 3) return fluid_v;            // Fluid
+    const V3<float> d = f32v(C3(p, F_CEN, i) - C3(p, F_LOC, i));
+    if (p.motion == 1) {  // Steer
+        const float abs_d = len(d);
+        const float eta_r = 0.25f * radius32(vol, p.dim);
+        if (abs_d > 0.9f * eta_r) {
+            float fac = 0.99f * sound_speed / abs_d;
+            if (abs_d < 1.1f * eta_r) fac *= 5.f * (abs_d - 0.9f * eta_r) / eta_r;
+            return fluid_v + fac * d;
+        }
+        return fluid_v;
+    }
+    // SteerPakmor
+    const float alpha = 2.f / (float)p.dim * f32(C(p, F_MAOR, i));
+    const float beta = 2.25f;
+    const float eta = fmaxf(0.f, fminf(0.5f, 2.f / beta * (alpha - 0.75f * beta)));
+    const V3<float> dn = (1.f / len(d)) * d;
+    // curl of the velocity gradient (physical_quantities.rs:149-155); gr[q] = d(quantity q)/d(x, y, z)
+    const V3<float> curl = v3(gr[3].y - gr[2].z, gr[1].z - gr[3].x, gr[2].x - gr[1].y);
+    const float v_reg = radius32(vol, p.dim) * len(curl);
+    return fluid_v + (eta * fmaxf(sound_speed, v_reg)) * dn;
+}
+__device__ __forceinline__ double particle_timestep32(const KP& p, int i, const V3<float>* gr) {
+    const St<double> cons = C5(p, F_CONS, i);
+    if (is_zero64(cons.q[0])) {
+        W3(p, F_V, i, v3(0., 0., 0.));
+        return INFINITY;
+    }
+    const Gas<float> g = gas_t<float>(p);
+    const float m_inv = 1.f / f32(cons.q[0]);
+    const V3<float> dxg = f32v(C3(p, F_LOC, i) - C3(p, F_GC, i));
+    const V3<float> d_v = v3(dot(gr[1], dxg), dot(gr[2], dxg), dot(gr[3], dxg));
+    const V3<float> fluid_v = m_inv * f32v(vel(cons)) + d_v;
+    const St<double> prim = C5(p, F_PRIM, i);
+    const float u = f32(cons.q[4] - 0.5 * dot(vel(cons), vel(prim))) * m_inv;  // Particle::internal_energy
+    const float vol = f32(C(p, F_VOL, i));
+    const float c = g.sound_speed(g.pressure_from_internal_energy(u, f32(prim.q[0])), vol * m_inv);
+    const V3<float> v = particle_velocity32(p, i, fluid_v, c, vol, gr);
+    if (!isfinite(v.x) || !isfinite(v.y) || !isfinite(v.z)) set_err(p, inst_of(p, i), 1u << 4);  // part.rs:366
+    const V3<float> v_rel = fluid_v - v;
+    W3(p, F_V, i, f64v(v));
+    W3(p, F_VREL, i, f64v(v_rel));
+    W(p, F_MAOR, i, 0.);
+    const float v_max = fmaxf(f32(C(p, F_MSV, i)), len(v_rel) + c);
+    W(p, F_MSV, i, 0.);
+    if (v_max > 0.f) return f64(f32(p.cfl) * radius32(vol, p.dim) / v_max);
+    return INFINITY;
+}
+
 __device__ __forceinline__ void gradients32_cell(const KP& p, int i) {
     unsigned long long my_dti = MAX_NR_TIMESTEPS;
     int my_tb = 127;
@@ -378,14 +440,14 @@ __device__ __forceinline__ void gradients32_cell(const KP& p, int i) {
     if (k >= 0) {
         int tb = p.timebin[i];
         if (p.active[i]) {
+          V3<float> gr[5];
+#pragma unroll
+          for (int q = 0; q < 5; q++) gr[q] = v3(0.f, 0.f, 0.f);
           if (!p.godunov) {  // GodunovHydroRunner::step has no gradient stage (godunov.rs:14-58)
             St<float> prim = G5(p, G_PRIM, i);
             float a00 = 0.f, a01 = 0.f, a02 = 0.f, a11 = 0.f, a12 = 0.f, a22 = 0.f;
             if (p.dim == 1) { a11 = 1.f; a22 = 1.f; }
             else if (p.dim == 2) { a22 = 1.f; }
-            V3<float> gr[5];
-#pragma unroll
-            for (int q = 0; q < 5; q++) gr[q] = v3(0.f, 0.f, 0.f);
             int k0 = p.csr_off[i], k1 = p.csr_off[i + 1];
             for (int k = k0; k < k1; k++) {
                 int f = p.csr_face[k];
@@ -449,8 +511,12 @@ __device__ __forceinline__ void gradients32_cell(const KP& p, int i) {
             }
             V3<double> cen = C3(p, F_CEN, i);
             W3(p, F_GC, i, cen);
+          } else {
+            // no gradient stage: the stored gradients (velocity rows) feed the timestep
+#pragma unroll
+            for (int q = 1; q < 4; q++) gr[q] = f32v(C3(p, F_GRAD + 3 * q, i));
           }
-            double dt_new = particle_timestep(p, i);
+            double dt_new = particle_timestep32(p, i, gr);
             unsigned long long tc = p.tl[k].ti_current;
             unsigned long long dti = make_integer_timestep(dt_new, tb, NUM_TIME_BINS, tc, tbase_inv(p, k));
             if (dti == 0) err |= 1u << 6;
@@ -476,14 +542,14 @@ __device__ __forceinline__ void gradients32_cell_warp(const KP& p, int i, int la
     if (k >= 0) {
         int tb = p.timebin[i];
         if (p.active[i]) {
+          V3<float> gr[5];
+#pragma unroll
+          for (int q = 0; q < 5; q++) gr[q] = v3(0.f, 0.f, 0.f);
           if (!p.godunov) {
             St<float> prim = G5(p, G_PRIM, i);
             float a00 = 0.f, a01 = 0.f, a02 = 0.f, a11 = 0.f, a12 = 0.f, a22 = 0.f;
             if (p.dim == 1) { a11 = 1.f; a22 = 1.f; }
             else if (p.dim == 2) { a22 = 1.f; }
-            V3<float> gr[5];
-#pragma unroll
-            for (int q = 0; q < 5; q++) gr[q] = v3(0.f, 0.f, 0.f);
             const int k0 = p.csr_off[i], deg = p.csr_off[i + 1] - k0;
             for (int j0 = 0; j0 < deg; j0 += 32) {  // warp-uniform
                 float w = 0.f, dq[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
@@ -564,9 +630,12 @@ __device__ __forceinline__ void gradients32_cell_warp(const KP& p, int i, int la
                 if (lane == 0) W3(p, F_GRAD + 3 * q, i, f64v(gr[q]));
             }
             if (lane == 0) W3(p, F_GC, i, C3(p, F_CEN, i));
+          } else {
+#pragma unroll
+            for (int q = 1; q < 4; q++) gr[q] = f32v(C3(p, F_GRAD + 3 * q, i));
           }
             if (lane == 0) {
-                double dt_new = particle_timestep(p, i);
+                double dt_new = particle_timestep32(p, i, gr);
                 unsigned long long tc = p.tl[k].ti_current;
                 unsigned long long dti = make_integer_timestep(dt_new, tb, NUM_TIME_BINS, tc, tbase_inv(p, k));
                 if (dti == 0) err |= 1u << 6;
