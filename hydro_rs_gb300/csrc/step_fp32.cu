@@ -61,27 +61,45 @@ __device__ __forceinline__ void prep32_cell(const KP& p, int i) {
 // extrapolation tests the density before check_physical, the face-stage rows
 // the checked state.
 __global__ void __launch_bounds__(kMaxBlock) k_predict32(KP p) {
+    // two rows of blocks: row 0 forms the extrapolation (and the copies it
+    // reads); row 1 converts the copies nothing here reads (six gradient rows,
+    // gradients_centroid - loc, v), so twice the warps hide the loads' latency
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool main_row = blockIdx.y == 0;
     bool act = false;
     int k = i < p.n ? inst_of(p, i) : -1;
     if (k >= 0 && p.tl[k].done) k = -1;  // a finished simulation of a batch is left untouched
+    const size_t n = (size_t)p.n;
+    float* cf = p.cf;
+    if (k >= 0 && !main_row) {
+#pragma unroll
+        for (int q : {4, 5, 6, 8, 9, 10}) cf[(G_GRAD + q) * n + i] = f32(C(p, F_GRAD + q, i));
+        const V3<double> dgc = C3(p, F_GC, i) - C3(p, F_LOC, i);
+        const V3<double> v = C3(p, F_V, i);
+        cf[(G_DGC + 0) * n + i] = f32(dgc.x);
+        cf[(G_DGC + 1) * n + i] = f32(dgc.y);
+        cf[(G_DGC + 2) * n + i] = f32(dgc.z);
+        cf[(G_V + 0) * n + i] = f32(v.x);
+        cf[(G_V + 1) * n + i] = f32(v.y);
+        cf[(G_V + 2) * n + i] = f32(v.z);
+    }
+    if (!main_row) return;  // block-uniform
     if (k >= 0) {
         const unsigned long long tc = p.tl[k].ti_current, to = p.tl[k].ti_old;
         const double dt = (double)(tc - to) * tbase(p, k);  // TimestepInfo::dt_from_dti
         act = p.timebin[i] <= max_active_bin_bits(tc);
         p.active[i] = act;
         p.fresh[i] = 0;
-        const size_t n = (size_t)p.n;
-        float* cf = p.cf;
         const St<double> prim = C5(p, F_PRIM, i);
         const bool pos = gt0_64(prim.q[0]);
         const bool reset = lt0_64(prim.q[0]) || lt0_64(prim.q[4]);  // check_physical zeroes the state
         St<float> w;
 #pragma unroll
-        for (int q = 0; q < 5; q++) w.q[q] = (float)prim.q[q];
+        for (int q = 0; q < 5; q++) w.q[q] = f32(prim.q[q]);
+        // the gradient rows the source reads: d(rho), the velocity divergence, d(P)
         float gr[15];
 #pragma unroll
-        for (int q = 0; q < 15; q++) gr[q] = f32(C(p, F_GRAD + q, i));
+        for (int q : {0, 1, 2, 3, 7, 11, 12, 13, 14}) gr[q] = f32(C(p, F_GRAD + q, i));
         const V3<float> vr = f32v(C3(p, F_VREL, i));
         const Gas<float> g = gas_t<float>(p);
         const float rho_inv = 1.f / w.q[0];
@@ -106,16 +124,8 @@ __global__ void __launch_bounds__(kMaxBlock) k_predict32(KP p) {
             cf[(G_SRC + q) * n + i] = live ? src.q[q] : 0.f;
         }
 #pragma unroll
-        for (int q = 0; q < 15; q++) cf[(G_GRAD + q) * n + i] = gr[q];
+        for (int q : {0, 1, 2, 3, 7, 11, 12, 13, 14}) cf[(G_GRAD + q) * n + i] = gr[q];
         cf[G_CS * n + i] = live ? g.sound_speed(w.q[4], rho_inv) : 0.f;
-        const V3<double> dgc = C3(p, F_GC, i) - C3(p, F_LOC, i);
-        const V3<double> v = C3(p, F_V, i);
-        cf[(G_DGC + 0) * n + i] = f32(dgc.x);
-        cf[(G_DGC + 1) * n + i] = f32(dgc.y);
-        cf[(G_DGC + 2) * n + i] = f32(dgc.z);
-        cf[(G_V + 0) * n + i] = f32(v.x);
-        cf[(G_V + 1) * n + i] = f32(v.y);
-        cf[(G_V + 2) * n + i] = f32(v.z);
     }
     inst_count(p, k, act, CNT_CELLS);
 }
@@ -704,7 +714,7 @@ inline int grid(int n, int b = kBlock) { return (n + b - 1) / b; }
 }  // namespace
 
 void launch_predict32(const KP& p, cudaStream_t s) {
-    if (p.n > 0) k_predict32<<<grid(p.n, p.blk_cell), p.blk_cell, 0, s>>>(p);
+    if (p.n > 0) k_predict32<<<dim3(grid(p.n, p.blk_cell), 2), p.blk_cell, 0, s>>>(p);
 }
 
 void launch_prep32(const KP& p, cudaStream_t s) {
