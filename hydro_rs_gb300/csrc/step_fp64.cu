@@ -392,14 +392,32 @@ __device__ __forceinline__ void update_cell(const KP& p, int i, int do_c2p) {
 #pragma unroll
         for (int q = 0; q < 5; q++) acc[q] = {0.f, 0.f};
         float vm = -INFINITY, ar = -INFINITY;
-        for (int k = k0; k < k1; k++) {
-            int f = p.csr_face[k];
-            if (p.use_list && p.face_stamp[f] != stamp) continue;
-            float sg = p.left[f] == i ? -1.f : 1.f;  // update_fluxes_left / _right (part.rs:160-176)
+        // faces in batches of 4: a batch's loads are in flight together, and the
+        // batch is then added in CSR order (the same sums as one face at a time)
+        for (int kb = k0; kb < k1; kb += 4) {
+            int ff[4];
+            bool use[4];
 #pragma unroll
-            for (int q = 0; q < 5; q++) sum2_add(acc[q], sg * fl[q * nf + f]);
-            vm = fmaxf(vm, fl[5 * nf + f]);
-            ar = fmaxf(ar, fl[6 * nf + f]);
+            for (int j = 0; j < 4; j++) {
+                use[j] = kb + j < k1;
+                ff[j] = use[j] ? p.csr_face[kb + j] : 0;
+            }
+            float x[4][7], sg[4];
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                if (use[j] && p.use_list) use[j] = p.face_stamp[ff[j]] == stamp;
+                sg[j] = use[j] && p.left[ff[j]] == i ? -1.f : 1.f;  // update_fluxes_left / _right (part.rs:160-176)
+#pragma unroll
+                for (int q = 0; q < 7; q++) x[j][q] = use[j] ? fl[q * nf + ff[j]] : 0.f;
+            }
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                if (!use[j]) continue;
+#pragma unroll
+                for (int q = 0; q < 5; q++) sum2_add(acc[q], sg[j] * x[j][q]);
+                vm = fmaxf(vm, x[j][5]);
+                ar = fmaxf(ar, x[j][6]);
+            }
         }
 #pragma unroll
         for (int q = 0; q < 5; q++) facc.q[q] = facc.q[q] + (f64(acc[q].hi) + f64(acc[q].lo));
