@@ -17,6 +17,7 @@
 
 namespace mvmm {
 void launch_face_flux_fp64(const KP& p, int solver, cudaStream_t s);
+size_t brent_job_bytes();
 void launch_riemann_fp64(int kind, int sample, double gamma, int64_t n, const double* l, const double* r,
                          const double* vf, const double* nrm, double* out, unsigned int* err, const RSx& x,
                          cudaStream_t s);
@@ -72,6 +73,9 @@ struct mvmm_ctx {
     unsigned int* face_stamp = nullptr;
     // moving meshes: face capacity, pending geometry of the rebuilt cells
     int nf_cap = 0;
+    void* brent_jobs = nullptr;  // plain form, exact solver: queued Brent searches of a face launch
+    unsigned int* brent_count = nullptr;
+    int brent_cap = 0;
     int64_t ncsr_cap = 0;
     double *pend_vol = nullptr, *pend_cen = nullptr;
     bool pending_geometry = false;
@@ -104,6 +108,10 @@ struct mvmm_ctx {
     unsigned long long* xfer_stored = nullptr;  // device: bytes stored by copies that skip unchanged chunks
     int64_t host_bytes_in = 0, host_bytes_out = 0;
 };
+
+// Largest Brent queue of the plain exact-solver face kernel (jobs beyond it
+// run their search in the face kernel itself).
+constexpr int64_t kBrentJobsMax = 1 << 22;
 
 namespace {
 
@@ -172,6 +180,9 @@ KP make_kp(mvmm_ctx* c, int stage, int flux_rows) {
     // list; synchronised steps, batches and per-stage calls sweep all faces
     p.use_list = (!stage && !c->prm.sync_all && c->n_inst == 1) ? 1 : 0;
     p.face_stamp = c->face_stamp;
+    p.brent_jobs = c->brent_jobs;
+    p.brent_count = c->brent_count;
+    p.brent_cap = c->brent_cap;
     p.touch = c->touch;
     p.blocks_done = c->blocks_done;
     p.fresh = c->fresh;
@@ -496,6 +507,11 @@ static int create_impl(const mvmm_params* prm, const mvmm_mesh* m, int64_t n_ins
     ALLOC(c->tb_tmp, n);
     ALLOC(c->active, n);
     ALLOC(c->flux, 10 * nf * 8);
+    if (prm->precision == MVMM_PRECISION_FP64 && prm->riemann == MVMM_RIEMANN_EXACT && nf > 0) {
+        c->brent_cap = (int)std::min<int64_t>(nf, kBrentJobsMax);
+        ALLOC(c->brent_jobs, (size_t)c->brent_cap * brent_job_bytes());
+        ALLOC(c->brent_count, sizeof(unsigned int));
+    }
     ALLOC(c->dtmp, n * 8);
     ALLOC(c->face_stamp, nf * 4);
     ALLOC(c->touch, n * 4);
@@ -606,7 +622,7 @@ int mvmm_ctx_destroy(mvmm_ctx* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     drop_graphs(c);
     void* ptrs[] = {c->left, c->right, c->csr_off, c->csr_face, c->area, c->normal, c->fcen, c->shift, c->cd,
-                    c->cf, c->timebin, c->tb_tmp, c->active, c->flux, c->flux32, c->geo, c->geo_pos, c->geo_changed, c->snap, c->snap_tb, c->xfer_stored, c->dtmp, c->face_stamp, c->touch, c->blocks_done, c->cell_list, c->fresh,
+                    c->cf, c->timebin, c->tb_tmp, c->active, c->flux, c->flux32, c->geo, c->geo_pos, c->geo_changed, c->snap, c->snap_tb, c->xfer_stored, c->brent_jobs, c->brent_count, c->dtmp, c->face_stamp, c->touch, c->blocks_done, c->cell_list, c->fresh,
                     c->pend_vol, c->pend_cen,
                     c->face_list, c->tl,
                     c->inst, c->inst_tb, c->inst_tbi};
@@ -1239,6 +1255,14 @@ int mvmm_set_mesh(mvmm_ctx* c, const mvmm_mesh* m, const double* volume, const d
             if (cudaMalloc(b.ptr, b.bytes) != cudaSuccess) return fail(MVMM_E_NOMEM, "set_mesh: cudaMalloc failed");
         }
         CUDA_TRY(cudaMemsetAsync(c->face_stamp, 0, (size_t)cap * 4, s));
+        if (c->brent_jobs) {
+            const int bcap = (int)std::min<int64_t>(cap, kBrentJobsMax);
+            cudaFree(c->brent_jobs);
+            c->brent_jobs = nullptr;
+            if (cudaMalloc(&c->brent_jobs, (size_t)bcap * brent_job_bytes()) != cudaSuccess)
+                return fail(MVMM_E_NOMEM, "set_mesh: cudaMalloc failed");
+            c->brent_cap = bcap;
+        }
         c->nf_cap = cap;
         c->ncsr_cap = ccap;
     }

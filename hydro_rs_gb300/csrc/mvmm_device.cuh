@@ -406,9 +406,17 @@ __device__ __forceinline__ double ex_fb(double p, const ExSide& s, const Gas<dou
     }
     return g.tdgm1() * s.a * (g.pow_e1(p / s.p) - 1.);
 }
+// The two sides' terms are evaluated lower-pressure side first: for a pressure
+// between the two side pressures (the usual case) that side takes the shock
+// branch of fb and the other the rarefaction branch, so the lanes of a warp
+// take the same branches; the terms are then added in the reference's order
+// (left, right), so the value is the same.
 __device__ __forceinline__ double ex_f(double p, const ExSide& l, const ExSide& r, double vl, double vr,
                                        const Gas<double>& g) {  // :23-34
-    return ex_fb(p, l, g) + ex_fb(p, r, g) + (vr - vl);
+    const bool lo_left = l.p <= r.p;
+    const double t_lo = ex_fb(p, lo_left ? l : r, g);
+    const double t_hi = ex_fb(p, lo_left ? r : l, g);
+    return (lo_left ? t_lo : t_hi) + (lo_left ? t_hi : t_lo) + (vr - vl);
 }
 __device__ __forceinline__ double ex_fprimeb(double p, const ExSide& s, const Gas<double>& g) {  // :37-45
     if (p > s.p) {
@@ -490,9 +498,14 @@ __device__ __forceinline__ double ex_middle_density(double p, const ExSide& s, c
     if (pdps > 1.) return s.rho * (pdps + g.gm1dgp1()) / (g.gm1dgp1() * pdps + 1.);
     return s.rho * g.pow_ginv(pdps);
 }
-// ExactRiemannSolver::solve_for_star_state (exact.rs:241-291)
-static __device__ __noinline__ Star<double> ex_star(ExSide l, ExSide r, double vl, double vr, Gas<double> g, int max_iter,
-                                            unsigned int* err) {
+// ExactRiemannSolver::solve_for_star_state (exact.rs:241-291), in two parts
+// around its Brent fallback so that a face kernel can hand the Brent searches
+// to a second kernel (ex_star composes them).  ex_star_pre: guess_p and the
+// Newton iteration; returns true where Brent's method must run on
+// [0, *p_guess] (with f(*p_guess) = *fp_guess), else *p is the pressure.
+static __device__ __noinline__ bool ex_star_pre(ExSide l, ExSide r, double vl, double vr, Gas<double> g, int max_iter,
+                                                unsigned int* err, double* p_out, double* p_guess_out,
+                                                double* fp_guess_out) {
     double p = 0.;
     double p_guess = ex_guess_p(l, r, vl, vr, g);
     double fp = ex_f(p, l, r, vl, vr, g);
@@ -501,7 +514,11 @@ static __device__ __noinline__ Star<double> ex_star(ExSide l, ExSide r, double v
         int counter = 0;
         while (fabs(p - p_guess) > 1e-6 * 0.5 * (p + p_guess) && fp_guess < 0.0) {
             p = p_guess;
-            p_guess = p_guess - fp_guess / (ex_fprimeb(p_guess, l, g) + ex_fprimeb(p_guess, r, g));
+            // f' = f'_l + f'_r, the terms evaluated in ex_f's branch-coherent order
+            const bool lo_left = l.p <= r.p;
+            const double d_lo = ex_fprimeb(p_guess, lo_left ? l : r, g);
+            const double d_hi = ex_fprimeb(p_guess, lo_left ? r : l, g);
+            p_guess = p_guess - fp_guess / ((lo_left ? d_lo : d_hi) + (lo_left ? d_hi : d_lo));
             fp_guess = ex_f(p_guess, l, r, vl, vr, g);
             counter += 1;
             if (counter > max_iter) {  // the reference panics here
@@ -510,19 +527,35 @@ static __device__ __noinline__ Star<double> ex_star(ExSide l, ExSide r, double v
             }
         }
     }
-    if (fabs(p - p_guess) > 1e-6 * 0.5 * (p + p_guess) && fp_guess > 0.) {
-        p = 0.;
-        fp = ex_f(p, l, r, vl, vr, g);
-        p = ex_brent(p, p_guess, fp, fp_guess, 1e-6, l, r, vl, vr, g, max_iter, err);
-    } else {
-        p = p_guess;
-    }
-    Star<double> s;  // star_state_from_pstar (:214-238)
+    *p_guess_out = p_guess;
+    *fp_guess_out = fp_guess;
+    *p_out = p_guess;
+    return fabs(p - p_guess) > 1e-6 * 0.5 * (p + p_guess) && fp_guess > 0.;
+}
+// Brent's method on [0, p_guess] as the reference calls it
+__device__ __forceinline__ double ex_star_brent(double p_guess, double fp_guess, const ExSide& l, const ExSide& r,
+                                                double vl, double vr, const Gas<double>& g, int max_iter,
+                                                unsigned int* err) {
+    double p = 0.;
+    double fp = ex_f(p, l, r, vl, vr, g);
+    return ex_brent(p, p_guess, fp, fp_guess, 1e-6, l, r, vl, vr, g, max_iter, err);
+}
+// star_state_from_pstar (:214-238)
+__device__ __forceinline__ Star<double> ex_star_post(double p, const ExSide& l, const ExSide& r, double vl, double vr,
+                                                     const Gas<double>& g) {
+    Star<double> s;
     s.u = 0.5 * (vl + vr) + 0.5 * (ex_fb(p, r, g) - ex_fb(p, l, g));
     s.rho_l = ex_middle_density(p, l, g);
     s.rho_r = ex_middle_density(p, r, g);
     s.p = p;
     return s;
+}
+static __device__ __noinline__ Star<double> ex_star(ExSide l, ExSide r, double vl, double vr, Gas<double> g, int max_iter,
+                                            unsigned int* err) {
+    double p, p_guess, fp_guess;
+    if (ex_star_pre(l, r, vl, vr, g, max_iter, err, &p, &p_guess, &fp_guess))
+        p = ex_star_brent(p_guess, fp_guess, l, r, vl, vr, g, max_iter, err);
+    return ex_star_post(p, l, r, vl, vr, g);
 }
 
 // Exact star state for the FP32-face form: the same iteration as ex_star

@@ -149,6 +149,9 @@ struct KP {
     const double* new_cen;   //   rebuilt cells, applied to active cells after predict
     int use_list;            // 1: face kernel walks the compacted active-face list
     unsigned int* face_stamp;  // hierarchical steps: steps + 1 for faces active in this step
+    void* brent_jobs;          // plain form, exact solver: the face kernel's queued Brent searches
+    unsigned int* brent_count;  //   (their count this launch)
+    int brent_cap;
     unsigned int* blocks_done;  // k_limit blocks finished this step (the last one ends the step)
     unsigned int* touch;     // hierarchical steps: 1 for cells on this step's cell list
     uint8_t* fresh;          // 1: the cell's derived face-stage rows match its prim, grad and v_rel

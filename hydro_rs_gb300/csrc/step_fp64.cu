@@ -131,11 +131,26 @@ struct FaceOut {
     V3<double> mflux;
     double v_max, a_over_r;
 };
+// A face up to its Riemann solve: the two states handed to the solver (in the
+// face frame), the face velocity and normal, and what the result needs.
+struct FacePre {
+    St<double> l, r;
+    V3<double> iv, n, dx;
+    double dt, area, v_max;
+};
+// ... and from the solver's flux on (flux_exchange, flux.rs:85-99)
+__device__ __forceinline__ FaceOut face_finish(const FacePre& q, const St<double>& F) {
+    St<double> fluxes = q.area * F;
+    FaceOut o;
+    o.fl = q.dt * fluxes;
+    o.mflux = fluxes.q[0] * q.dx;
+    o.v_max = q.v_max;
+    o.a_over_r = q.area / len(q.dx);
+    return o;
+}
 
 // flux_exchange (flux.rs:23-100)
-template <int SOLVER>
-__device__ __forceinline__ FaceOut face_interior(const KP& p, int f, int l, int r, double dt, unsigned int* err) {
-    const Gas<double> g = gas(p);
+__device__ __forceinline__ FacePre face_interior_pre(const KP& p, int f, int l, int r, double dt) {
     V3<double> fc = F3(p.fcen, p.nf, f);
     V3<double> sh = F3(p.shift, p.nf, f);
     V3<double> dx_left = fc - C3(p, F_GC, l);
@@ -157,24 +172,21 @@ __device__ __forceinline__ FaceOut face_interior(const KP& p, int f, int l, int 
     V3<double> midpoint = 0.5 * ((locl + locr) + sh);
     double fac = dot(vr - vl, fc - midpoint) / len2(dx);
     V3<double> v_face = 0.5 * (vl + vr) - fac * dx;
-    V3<double> nrm = F3(p.normal, p.nf, f);
     V3<double> mvf = neg(v_face);
-    St<double> F = solve_for_flux<double, SOLVER>(boost(prim_left, mvf), boost(prim_right, mvf), v_face, nrm, g, g,
-                                                  p.max_iter, err, &p.rsx);
-    double area = p.area[f];
-    St<double> fluxes = area * F;
-    FaceOut o;
-    o.fl = dt * fluxes;
-    o.mflux = fluxes.q[0] * dx;
-    o.v_max = v_max;
-    o.a_over_r = area / len(dx);
-    return o;
+    FacePre q;
+    q.l = boost(prim_left, mvf);
+    q.r = boost(prim_right, mvf);
+    q.iv = v_face;
+    q.n = F3(p.normal, p.nf, f);
+    q.dx = dx;
+    q.dt = dt;
+    q.area = p.area[f];
+    q.v_max = v_max;
+    return q;
 }
 
 // flux_exchange_boundary (flux.rs:102-195) with Space::get_boundary_part semantics
-template <int SOLVER>
-__device__ __forceinline__ FaceOut face_boundary(const KP& p, int f, int i, unsigned int* err) {
-    const Gas<double> g = gas(p);
+__device__ __forceinline__ FacePre face_boundary_pre(const KP& p, int f, int i) {
     V3<double> fc = F3(p.fcen, p.nf, f);
     V3<double> n = F3(p.normal, p.nf, f);
     V3<double> loc = C3(p, F_LOC, i), cen = C3(p, F_CEN, i), gc = C3(p, F_GC, i);
@@ -207,15 +219,55 @@ __device__ __forceinline__ FaceOut face_boundary(const KP& p, int f, int i, unsi
         v_max += m_min(dot(vel(prim), dx_centroid), 0.);
         bnd = vac;
     }
-    St<double> F = solve_for_flux<double, SOLVER>(dash, bnd, v3(0., 0., 0.), n, g, g, p.max_iter, err, &p.rsx);
-    double area = p.area[f];
-    St<double> fluxes = area * F;
-    FaceOut o;
-    o.fl = dt * fluxes;
-    o.mflux = fluxes.q[0] * dx;
-    o.v_max = v_max;
-    o.a_over_r = area / len(dx);
-    return o;
+    FacePre q;
+    q.l = dash;
+    q.r = bnd;
+    q.iv = v3(0., 0., 0.);
+    q.n = n;
+    q.dx = dx;
+    q.dt = dt;
+    q.area = p.area[f];
+    q.v_max = v_max;
+    return q;
+}
+
+// The face rows of a result: 5 fluxes and v_max, a_over_r (step), or the
+// FluxInfo rows with mflux (per-stage calls).
+__device__ __forceinline__ void write_face(const KP& p, int f, const FaceOut& o) {
+    double* out = p.flux;
+    size_t nf = (size_t)p.nf;
+#pragma unroll
+    for (int q = 0; q < 5; q++) out[q * nf + f] = o.fl.q[q];
+    if (p.flux_rows == 10) {
+        out[5 * nf + f] = o.mflux.x;
+        out[6 * nf + f] = o.mflux.y;
+        out[7 * nf + f] = o.mflux.z;
+        out[8 * nf + f] = o.v_max;
+        out[9 * nf + f] = o.a_over_r;
+    } else {
+        out[5 * nf + f] = o.v_max;
+        out[6 * nf + f] = o.a_over_r;
+    }
+}
+
+// The exact solver's Brent searches leave the face kernel for a kernel of
+// their own.  Warps of the face kernel would run them with only the lanes
+// whose PVRS guess landed above the root (about half), holding the FP64 pipe
+// for all 32; queued, they run with full warps.  A job holds the face's
+// Riemann problem after the Newton stage and what the face's result needs.
+struct BrentJob {
+    FacePre q;
+    double vl, vr, al, ar, p_guess, fp_guess;
+    int f, k;
+};
+// The exact solver's flux from the star pressure on (riemann_solver.rs:258-284,
+// exact.rs:214-238), as star_half_state + flux_from_half_state do.
+__device__ __forceinline__ St<double> exact_flux_from_p(double pst, const FacePre& q, double vl, double vr, double al,
+                                                        double ar, const Gas<double>& g) {
+    ExSide L{q.l.q[0], q.l.q[4], al}, R{q.r.q[0], q.r.q[4], ar};
+    Star<double> s = ex_star_post(pst, L, R, vl, vr, g);
+    St<double> w = sample_star(s, q.l, q.r, vl, vr, al, ar, q.n, g);
+    return flux_from_half_state(w, q.iv, q.n, g);
 }
 
 // EulerEqnsFvs::compute_fluxes (euler_eqns_fvs.rs:26-48): the active-face rule,
@@ -223,6 +275,7 @@ __device__ __forceinline__ FaceOut face_boundary(const KP& p, int f, int i, unsi
 template <int SOLVER>
 __global__ void __launch_bounds__(kMaxBlock) k_face_flux(KP p) {
     if (p.use_list && p.tl[0].done) return;
+    const Gas<double> g = gas(p);
     // all faces (one per thread), or the compacted active-face list (grid-stride)
     const int n_items = p.use_list ? (int)p.tl[0].n_list : p.nf;
     for (int base = blockIdx.x * blockDim.x; base < n_items; base += gridDim.x * blockDim.x) {
@@ -235,41 +288,83 @@ __global__ void __launch_bounds__(kMaxBlock) k_face_flux(KP p) {
         if (k >= 0) {
             int l = p.left[f], r = p.right[f];
             bool la = p.active[l] != 0;
-            FaceOut o;
+            FacePre q;
             if (r >= 0) {
                 bool ra = p.active[r] != 0;
                 double dtl = C(p, F_DT, l), dtr = C(p, F_DT, r);
                 if (!((!la && !ra) || (dtr < dtl && !ra) || (dtl < dtr && !la))) {
-                    o = face_interior<SOLVER>(p, f, l, r, m_min(dtl, dtr), &err);
+                    q = face_interior_pre(p, f, l, r, m_min(dtl, dtr));
                     counted = true;
                 }
             } else if (la) {
-                o = face_boundary<SOLVER>(p, f, l, &err);
+                q = face_boundary_pre(p, f, l);
                 counted = true;
             }
+            FaceOut o;
+            bool queued = false;
             if (!counted) {
                 o.fl = st_zero<double>();
                 o.mflux = v3(0., 0., 0.);
                 o.v_max = 0.;
                 o.a_over_r = 0.;
-            }
-            double* out = p.flux;
-            size_t nf = (size_t)p.nf;
-#pragma unroll
-            for (int q = 0; q < 5; q++) out[q * nf + f] = o.fl.q[q];
-            if (p.flux_rows == 10) {
-                out[5 * nf + f] = o.mflux.x;
-                out[6 * nf + f] = o.mflux.y;
-                out[7 * nf + f] = o.mflux.z;
-                out[8 * nf + f] = o.v_max;
-                out[9 * nf + f] = o.a_over_r;
+            } else if (SOLVER == SOLVER_EXACT && p.brent_jobs) {
+                // star_half_state (riemann_solver.rs:258-284) with the exact
+                // star solver, its Brent stage queued when it is needed
+                double vl = dot(vel(q.l), q.n);
+                double vr = dot(vel(q.r), q.n);
+                double al = g.sound_speed(q.l.q[4], 1. / q.l.q[0]);
+                double ar = g.sound_speed(q.r.q[4], 1. / q.r.q[0]);
+                double vrml = vr - vl;
+                St<double> F;
+                if (is_vacuum(q.l, q.r, al, ar, vrml, g)) {
+                    F = flux_from_half_state(vacuum_sample(q.l, q.r, vl, vr, al, ar, q.n, g), q.iv, q.n, g);
+                } else {
+                    ExSide L{q.l.q[0], q.l.q[4], al}, R{q.r.q[0], q.r.q[4], ar};
+                    double pst, pg, fpg;
+                    if (ex_star_pre(L, R, vl, vr, g, p.max_iter, &err, &pst, &pg, &fpg)) {
+                        const unsigned int slot = atomicAdd(p.brent_count, 1u);
+                        if (slot < (unsigned int)p.brent_cap) {
+                            BrentJob& J = reinterpret_cast<BrentJob*>(p.brent_jobs)[slot];
+                            J.q = q;
+                            J.vl = vl;
+                            J.vr = vr;
+                            J.al = al;
+                            J.ar = ar;
+                            J.p_guess = pg;
+                            J.fp_guess = fpg;
+                            J.f = f;
+                            J.k = k;
+                            queued = true;
+                        } else {  // the queue is full: the search runs here
+                            pst = ex_star_brent(pg, fpg, L, R, vl, vr, g, p.max_iter, &err);
+                        }
+                    }
+                    if (!queued) F = exact_flux_from_p(pst, q, vl, vr, al, ar, g);
+                }
+                if (!queued) o = face_finish(q, F);
             } else {
-                out[5 * nf + f] = o.v_max;
-                out[6 * nf + f] = o.a_over_r;
+                o = face_finish(q, solve_for_flux<double, SOLVER>(q.l, q.r, q.iv, q.n, g, g, p.max_iter, &err, &p.rsx));
             }
+            if (!queued) write_face(p, f, o);
             if (err) set_err(p, k, err);
         }
         if (!p.use_list) inst_count(p, k, counted, CNT_FACES);  // list mode counts the list in k_end
+    }
+}
+
+// The queued Brent searches of the exact solver's faces, with full warps;
+// each job then finishes its face (star state, sample, flux) and writes its rows.
+__global__ void __launch_bounds__(kMaxBlock) k_face_brent(KP p) {
+    const Gas<double> g = gas(p);
+    const unsigned int n_jobs = min(*p.brent_count, (unsigned int)p.brent_cap);
+    const BrentJob* jobs = reinterpret_cast<const BrentJob*>(p.brent_jobs);
+    for (unsigned int j = blockIdx.x * blockDim.x + threadIdx.x; j < n_jobs; j += gridDim.x * blockDim.x) {
+        const BrentJob J = jobs[j];
+        unsigned int err = 0;
+        ExSide L{J.q.l.q[0], J.q.l.q[4], J.al}, R{J.q.r.q[0], J.q.r.q[4], J.ar};
+        double pst = ex_star_brent(J.p_guess, J.fp_guess, L, R, J.vl, J.vr, g, p.max_iter, &err);
+        write_face(p, J.f, face_finish(J.q, exact_flux_from_p(pst, J.q, J.vl, J.vr, J.al, J.ar, g)));
+        if (err) set_err(p, J.k, err);
     }
 }
 
@@ -1114,11 +1209,17 @@ inline int face_grid(const KP& p) {
     return p.use_list && g > cap ? cap : g;
 }
 
+size_t brent_job_bytes() { return sizeof(BrentJob); }
 void launch_face_flux_fp64(const KP& p, int solver, cudaStream_t s) {
     if (p.nf <= 0) return;
     int g = face_grid(p);
     if (solver == SOLVER_HLLC) k_face_flux<SOLVER_HLLC><<<g, p.blk_face, 0, s>>>(p);
-    else if (solver == SOLVER_EXACT) k_face_flux<SOLVER_EXACT><<<g, p.blk_face, 0, s>>>(p);
+    else if (solver == SOLVER_EXACT && p.brent_jobs) {
+        cudaMemsetAsync(p.brent_count, 0, sizeof(unsigned int), s);
+        k_face_flux<SOLVER_EXACT><<<g, p.blk_face, 0, s>>>(p);
+        const int blk = 128, jobs_grid = (int)std::min<long long>((p.brent_cap + blk - 1) / blk, 152LL * 16);
+        k_face_brent<<<jobs_grid, blk, 0, s>>>(p);
+    } else if (solver == SOLVER_EXACT) k_face_flux<SOLVER_EXACT><<<g, p.blk_face, 0, s>>>(p);
     else if (solver == SOLVER_PVRS) k_face_flux<SOLVER_PVRS><<<g, p.blk_face, 0, s>>>(p);
     else k_face_flux<SOLVER_EXTRA><<<g, p.blk_face, 0, s>>>(p);
 }
