@@ -441,6 +441,24 @@ __device__ __forceinline__ double particle_timestep32(const KP& p, int i, const 
     return INFINITY;
 }
 
+// The cell's timestep for the integer timeline: FP32 (particle_timestep32),
+// except where dt / time_base lies within ~1e-5 of a power of two, where the
+// FP32 error could move it into the neighbouring time bin: there the FP64
+// particle_timestep decides, as in the plain form.  max_signal_velocity,
+// which the timestep consumes and resets, is put back first.
+__device__ __forceinline__ double cell_timestep32(const KP& p, int i, int k, const V3<float>* gr) {
+    const double msv = C(p, F_MSV, i);
+    const double dt = particle_timestep32(p, i, gr);
+    const unsigned long long b = (unsigned long long)__double_as_longlong(dt * tbase_inv(p, k));
+    const unsigned long long frac = b & ((1ull << 52) - 1ull);  // distance of the mantissa from 1 and from 2
+    const unsigned long long near = 1ull << 35;                 // 2^-17 ~ 7.6e-6
+    if (is_finite64(dt) && (frac < near || frac > (1ull << 52) - near)) {
+        W(p, F_MSV, i, msv);
+        return particle_timestep(p, i);
+    }
+    return dt;
+}
+
 __device__ __forceinline__ void gradients32_cell(const KP& p, int i) {
     unsigned long long my_dti = MAX_NR_TIMESTEPS;
     int my_tb = 127;
@@ -526,7 +544,7 @@ __device__ __forceinline__ void gradients32_cell(const KP& p, int i) {
 #pragma unroll
             for (int q = 1; q < 4; q++) gr[q] = f32v(C3(p, F_GRAD + 3 * q, i));
           }
-            double dt_new = particle_timestep32(p, i, gr);
+            double dt_new = cell_timestep32(p, i, k, gr);
             unsigned long long tc = p.tl[k].ti_current;
             unsigned long long dti = make_integer_timestep(dt_new, tb, NUM_TIME_BINS, tc, tbase_inv(p, k));
             if (dti == 0) err |= 1u << 6;
@@ -645,7 +663,7 @@ __device__ __forceinline__ void gradients32_cell_warp(const KP& p, int i, int la
             for (int q = 1; q < 4; q++) gr[q] = f32v(C3(p, F_GRAD + 3 * q, i));
           }
             if (lane == 0) {
-                double dt_new = particle_timestep32(p, i, gr);
+                double dt_new = cell_timestep32(p, i, k, gr);
                 unsigned long long tc = p.tl[k].ti_current;
                 unsigned long long dti = make_integer_timestep(dt_new, tb, NUM_TIME_BINS, tc, tbase_inv(p, k));
                 if (dti == 0) err |= 1u << 6;
