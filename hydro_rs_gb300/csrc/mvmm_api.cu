@@ -18,6 +18,7 @@
 namespace mvmm {
 void launch_face_flux_fp64(const KP& p, int solver, cudaStream_t s);
 size_t brent_job_bytes();
+void launch_extrap_flush(const KP& p, bool reset, cudaStream_t s);
 void launch_riemann_fp64(int kind, int sample, double gamma, int64_t n, const double* l, const double* r,
                          const double* vf, const double* nrm, double* out, unsigned int* err, const RSx& x,
                          cudaStream_t s);
@@ -73,6 +74,8 @@ struct mvmm_ctx {
     unsigned int* face_stamp = nullptr;
     // moving meshes: face capacity, pending geometry of the rebuilt cells
     int nf_cap = 0;
+    unsigned int* extrap_step = nullptr;  // hierarchical steps: deferred extrapolations (KP::extrap_step)
+    double* dt_log = nullptr;
     void* brent_jobs = nullptr;  // plain form, exact solver: queued Brent searches of a face launch
     unsigned int* brent_count = nullptr;
     int brent_cap = 0;
@@ -180,6 +183,8 @@ KP make_kp(mvmm_ctx* c, int stage, int flux_rows) {
     // list; synchronised steps, batches and per-stage calls sweep all faces
     p.use_list = (!stage && !c->prm.sync_all && c->n_inst == 1) ? 1 : 0;
     p.face_stamp = c->face_stamp;
+    p.extrap_step = c->extrap_step;
+    p.dt_log = c->dt_log;
     p.brent_jobs = c->brent_jobs;
     p.brent_count = c->brent_count;
     p.brent_cap = c->brent_cap;
@@ -513,6 +518,10 @@ static int create_impl(const mvmm_params* prm, const mvmm_mesh* m, int64_t n_ins
         ALLOC(c->brent_count, sizeof(unsigned int));
     }
     ALLOC(c->dtmp, n * 8);
+    if (!prm->sync_all && c->n_inst == 1 && prm->particle_motion == MVMM_MOTION_FIXED) {  // hierarchical steps
+        ALLOC(c->extrap_step, n * 4);
+        ALLOC(c->dt_log, (size_t)kDtLog * 8);
+    }
     ALLOC(c->face_stamp, nf * 4);
     ALLOC(c->touch, n * 4);
     ALLOC(c->blocks_done, 4);
@@ -561,6 +570,7 @@ static int create_impl(const mvmm_params* prm, const mvmm_mesh* m, int64_t n_ins
     cudaMemsetAsync(c->touch, 0, n * 4, s);
     cudaMemsetAsync(c->blocks_done, 0, 4, s);
     cudaMemsetAsync(c->fresh, 0, n, s);
+    if (c->extrap_step) cudaMemsetAsync(c->extrap_step, 0, n * 4, s);  // current at step 0
     std::memset(c->tl_host, 0, sizeof(DevTimeline) * c->n_inst);
     for (int k = 0; k < c->n_inst; k++) {
         c->tl_host[k].min_dti = kMax;
@@ -622,7 +632,7 @@ int mvmm_ctx_destroy(mvmm_ctx* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     drop_graphs(c);
     void* ptrs[] = {c->left, c->right, c->csr_off, c->csr_face, c->area, c->normal, c->fcen, c->shift, c->cd,
-                    c->cf, c->timebin, c->tb_tmp, c->active, c->flux, c->flux32, c->geo, c->geo_pos, c->geo_changed, c->snap, c->snap_tb, c->xfer_stored, c->brent_jobs, c->brent_count, c->dtmp, c->face_stamp, c->touch, c->blocks_done, c->cell_list, c->fresh,
+                    c->cf, c->timebin, c->tb_tmp, c->active, c->flux, c->flux32, c->geo, c->geo_pos, c->geo_changed, c->snap, c->snap_tb, c->xfer_stored, c->brent_jobs, c->brent_count, c->extrap_step, c->dt_log, c->dtmp, c->face_stamp, c->touch, c->blocks_done, c->cell_list, c->fresh,
                     c->pend_vol, c->pend_cen,
                     c->face_list, c->tl,
                     c->inst, c->inst_tb, c->inst_tbi};
@@ -937,6 +947,15 @@ int copy_cells(mvmm_ctx* c, const mvmm_cells* h, unsigned subset, bool timebin, 
         if (subset & (1u << k)) idx[j++] = k;
     return copy_rows(c, h, map, idx, m, timebin, kind, o, s);
 }
+// Hierarchical steps defer the extrapolation of inactive cells: every cell's
+// is made before the state is read or changed as a whole; reset: the state was
+// replaced (uploaded or restored), none is pending.
+int sync_extrap(mvmm_ctx* c, bool reset, cudaStream_t s) {
+    if (!c->extrap_step) return MVMM_OK;
+    launch_extrap_flush(make_kp(c, 0, 7), reset, s);
+    CUDA_TRY(cudaGetLastError());
+    return MVMM_OK;
+}
 // The cell state changed outside a step: every cell's derived face-stage rows
 // are recomputed by the next predict.
 int mark_stale(mvmm_ctx* c, cudaStream_t s) {
@@ -959,12 +978,16 @@ int mvmm_upload_cells(mvmm_ctx* c, const mvmm_cells* h) {
     if (!c || !h) return fail(MVMM_E_INVALID, "null argument");
     int rc = copy_cells(c, h, kAllRows, true, cudaMemcpyHostToDevice, c->stream);
     if (rc) return rc;
+    rc = sync_extrap(c, true, c->stream);
+    if (rc) return rc;
     return refresh_geometry(c, c->stream);
 }
 
 int mvmm_download_cells(mvmm_ctx* c, mvmm_cells* h) {
     if (!c || !h) return fail(MVMM_E_INVALID, "null argument");
-    int rc = copy_cells(c, h, kAllRows, true, cudaMemcpyDeviceToHost, c->stream);
+    int rc = sync_extrap(c, false, c->stream);
+    if (rc) return rc;
+    rc = copy_cells(c, h, kAllRows, true, cudaMemcpyDeviceToHost, c->stream);
     if (rc) return rc;
     CUDA_TRY(cudaStreamSynchronize(c->stream));
     return MVMM_OK;
@@ -995,6 +1018,8 @@ int mvmm_step_cells(mvmm_ctx* c, const mvmm_cells* in, mvmm_cells* out, uint64_t
     CopyOpts up;
     up.snapshot = true;  // the uploaded bytes, against which the copies back skip unchanged chunks
     int rc = copy_cells(c, in, kRowsPredictIn | kRowsFaceIn, true, cudaMemcpyHostToDevice, s, up);
+    if (rc) return rc;
+    rc = sync_extrap(c, true, s);
     if (rc) return rc;
     CUDA_TRY(cudaEventRecord(c->ev_pred, s));
     CUDA_TRY(cudaStreamWaitEvent(s2, c->ev_pred, 0));
@@ -1060,13 +1085,17 @@ int mvmm_step_cells(mvmm_ctx* c, const mvmm_cells* in, mvmm_cells* out, uint64_t
 // ---- per-stage --------------------------------------------------------
 static int upload_mask(mvmm_ctx* c, const uint8_t* active) {
     if (!active) return fail(MVMM_E_INVALID, "null active mask");
+    int rc = sync_extrap(c, false, c->stream);
+    if (rc) return rc;
     CUDA_TRY(cudaMemcpyAsync(c->active, active, c->n, cudaMemcpyHostToDevice, c->stream));
     return mark_stale(c, c->stream);
 }
 
 int mvmm_predict(mvmm_ctx* c, double dt) {
     if (!c) return fail(MVMM_E_INVALID, "null context");
-    int rs = mark_stale(c, c->stream);
+    int rs = sync_extrap(c, false, c->stream);
+    if (rs) return rs;
+    rs = mark_stale(c, c->stream);
     if (rs) return rs;
     KP p = make_kp(c, 1, 10);
     p.stage_dt = dt;
@@ -1344,6 +1373,7 @@ int mvmm_autotune(mvmm_ctx* c, int steps, int* blk_face, int* blk_cell) {
         return fail(MVMM_E_NOMEM, "cudaMalloc failed");
     }
     std::vector<DevTimeline> tl0(c->tl_host, c->tl_host + c->n_inst);
+    sync_extrap(c, false, c->stream);
     cudaMemcpyAsync(save, c->cd, bytes, cudaMemcpyDeviceToDevice, c->stream);
     cudaMemcpyAsync(save_tb, c->timebin, n, cudaMemcpyDeviceToDevice, c->stream);
     const int cand[3] = {64, 128, 256};
@@ -1367,6 +1397,7 @@ int mvmm_autotune(mvmm_ctx* c, int steps, int* blk_face, int* blk_cell) {
             cudaMemsetAsync(c->face_stamp, 0, (size_t)(c->nf > 0 ? c->nf : 1) * 4, c->stream);
             std::copy(tl0.begin(), tl0.end(), c->tl_host);
             write_tl(c);
+            sync_extrap(c, true, c->stream);
             rc = enqueue_steps_impl(c, 1);
             if (rc) break;
             cudaEventRecord(e0, c->stream);
@@ -1391,6 +1422,7 @@ int mvmm_autotune(mvmm_ctx* c, int steps, int* blk_face, int* blk_cell) {
     cudaMemsetAsync(c->face_stamp, 0, (size_t)(c->nf > 0 ? c->nf : 1) * 4, c->stream);
     std::copy(tl0.begin(), tl0.end(), c->tl_host);
     write_tl(c);
+    sync_extrap(c, true, c->stream);
     cudaStreamSynchronize(c->stream);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);

@@ -63,10 +63,11 @@ __device__ __forceinline__ int cell_at(const KP& p, int idx) { return p.use_list
 // Puts cell i on this step's cell list once (want: the lane has a candidate);
 // aggregated over the warp.  Every lane of the warp calls it.  The active
 // cells (predict) come first and are also counted in n_alist.
-__device__ __forceinline__ void list_cell_warp(const KP& p, bool want, int i, bool active_cells = false) {
+// Returns true on the lane that put the cell on the list.
+__device__ __forceinline__ bool list_cell_warp(const KP& p, bool want, int i, bool active_cells = false) {
     want = want && atomicExch(&p.touch[i], 1u) == 0u;
     unsigned int b = __ballot_sync(0xffffffffu, want);
-    if (!b) return;
+    if (!b) return false;
     int lane = threadIdx.x & 31, leader = __ffs(b) - 1;
     unsigned int start = 0;
     if (lane == leader) {
@@ -75,6 +76,7 @@ __device__ __forceinline__ void list_cell_warp(const KP& p, bool want, int i, bo
     }
     start = __shfl_sync(0xffffffffu, start, leader);
     if (want) p.cell_list[start + __popc(b & ((1u << lane) - 1u))] = i;
+    return want;
 }
 // The stamp of faces active in this step (hierarchical steps, one simulation).
 __device__ __forceinline__ unsigned int face_stamp_now(const KP& p) { return (unsigned int)p.tl[0].steps + 1u; }

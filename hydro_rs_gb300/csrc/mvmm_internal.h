@@ -93,6 +93,10 @@ struct DevTimeline {
     unsigned long long faces_mark;      // active_faces when the time was last set on the device
 };
 
+// Steps of dt kept for the deferred extrapolations of hierarchical steps; every
+// kDtLog / 2 steps all cells are brought up to date, so none lags further.
+constexpr int kDtLog = 4096;
+
 // Internal (not exported) flag a face's Riemann solve sets when the FP32-face
 // form's split exact solver fell back to the full FP64 iteration.
 constexpr unsigned int kInfoFallback = 1u << 16;
@@ -149,6 +153,9 @@ struct KP {
     const double* new_cen;   //   rebuilt cells, applied to active cells after predict
     int use_list;            // 1: face kernel walks the compacted active-face list
     unsigned int* face_stamp;  // hierarchical steps: steps + 1 for faces active in this step
+    unsigned int* extrap_step;  // hierarchical steps: the steps whose predict contribution a cell's
+                                //   extrapolation includes (deferred for inactive cells, see k_predict)
+    double* dt_log;             //   the dt of step s at [s % kDtLog]
     void* brent_jobs;          // plain form, exact solver: the face kernel's queued Brent searches
     unsigned int* brent_count;  //   (their count this launch)
     int brent_cap;

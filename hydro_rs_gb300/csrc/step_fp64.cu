@@ -38,6 +38,26 @@ __device__ __forceinline__ void write_derived(const KP& p, int i, const St<doubl
 }
 
 // ------------------------------------------------------------- predict --
+// Hierarchical steps defer the extrapolation of inactive cells whose source
+// row is current: the source, the density test and so each step's addition
+// ex + (-dt) src are fixed until the cell changes, so they are made later, in
+// step order, from the log of the steps' dt: for the cells a step reads (the
+// cells next to its active faces), before a download, and every kDtLog / 2
+// steps for all cells.  Brings cell i up to date before step `upto`.
+__device__ __forceinline__ void extrap_catch_up(const KP& p, int i, unsigned int upto) {
+    const unsigned int from = p.extrap_step[i];
+    if (from >= upto) return;
+    St<double> ex = C5(p, F_EXTRAP, i);
+    if (gt0_64(C(p, F_PRIM, i))) {
+        const St<double> src = C5(p, F_SRC, i);
+        for (unsigned int s = from; s < upto; s++) ex = ex + (-p.dt_log[s % kDtLog]) * src;
+    } else {
+        for (unsigned int s = from; s < upto; s++) ex = ex + st_zero<double>();
+    }
+    W5(p, F_EXTRAP, i, ex);
+    p.extrap_step[i] = upto;
+}
+
 // EulerEqnsFvs::predict -> Particle::extrapolate_state (part.rs:123-132),
 // plus the active mask bin_is_ending (engine.rs:63-65) in step mode.
 __global__ void __launch_bounds__(kMaxBlock) k_predict(KP p) {
@@ -55,13 +75,23 @@ __global__ void __launch_bounds__(kMaxBlock) k_predict(KP p) {
             act = p.timebin[i] <= max_active_bin_bits(tc);
             p.active[i] = act;
         }
-        if (!p.stage && !p.stale_all && p.fresh[i]) {
+        // hierarchical steps: this step's number, for the deferred extrapolations
+        const bool lazy = p.extrap_step != nullptr && !p.stage;
+        const unsigned int s = lazy ? (unsigned int)p.tl[k].steps : 0u;
+        if (lazy && i == 0) p.dt_log[s % kDtLog] = dt;
+        const bool fresh = !p.stage && !p.stale_all && p.fresh[i];
+        if (lazy && fresh && !act && s % (kDtLog / 2) != 0) {
+            // deferred (extrap_catch_up)
+        } else if (fresh) {
             // prim, grad and v_rel are unchanged since this cell's source row was
             // written (it was not active, nothing was uploaded): the same bits
+            if (lazy) extrap_catch_up(p, i, s);
             St<double> ex = C5(p, F_EXTRAP, i);
             if (gt0_64(C(p, F_PRIM, i))) W5(p, F_EXTRAP, i, ex + (-dt) * C5(p, F_SRC, i));
             else W5(p, F_EXTRAP, i, ex + st_zero<double>());
+            if (lazy) p.extrap_step[i] = s + 1;
         } else {
+            if (lazy) extrap_catch_up(p, i, s);
             St<double> prim = C5(p, F_PRIM, i);
             double rho_inv = 1. / prim.q[0];
             St<double> src = extrap_source(p, i, prim, rho_inv);
@@ -87,6 +117,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_predict(KP p) {
             write_derived(p, i, chk, src, rho_inv);
             // a reset prim no longer matches the source row (computed from the old one)
             if (!p.stage) p.fresh[i] = !reset;
+            if (lazy) p.extrap_step[i] = s + 1;
         }
     }
     // active cells: counted per warp, or in a hierarchical step as the length
@@ -415,9 +446,22 @@ __global__ void __launch_bounds__(kMaxBlock) k_compact(KP p) {
                 start = __shfl_sync(0xffffffffu, start, leader);
                 if (first) p.face_list[start + __popc(b & ((1u << lane) - 1u))] = f;
             }
-            list_cell_warp(p, o >= 0, o >= 0 ? o : 0);
+            // a cell newly on the list is read by this step (its faces, its update):
+            // its deferred extrapolation is made now, this step's included
+            if (list_cell_warp(p, o >= 0, o >= 0 ? o : 0) && p.extrap_step)
+                extrap_catch_up(p, o, (unsigned int)p.tl[0].steps + 1u);
         }
     }
+}
+
+// Every cell's deferred extrapolation made (before the state is read as a
+// whole); reset: none is pending (the cells were uploaded).
+__global__ void __launch_bounds__(kMaxBlock) k_extrap_flush(KP p, int reset) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n) return;
+    const unsigned int now = (unsigned int)p.tl[0].steps;
+    if (reset) p.extrap_step[i] = now;
+    else extrap_catch_up(p, i, now);
 }
 
 // ---------------------------------------------------- cons -> primitive --
@@ -1222,6 +1266,9 @@ void launch_face_flux_fp64(const KP& p, int solver, cudaStream_t s) {
     } else if (solver == SOLVER_EXACT) k_face_flux<SOLVER_EXACT><<<g, p.blk_face, 0, s>>>(p);
     else if (solver == SOLVER_PVRS) k_face_flux<SOLVER_PVRS><<<g, p.blk_face, 0, s>>>(p);
     else k_face_flux<SOLVER_EXTRA><<<g, p.blk_face, 0, s>>>(p);
+}
+void launch_extrap_flush(const KP& p, bool reset, cudaStream_t s) {
+    if (p.extrap_step && p.n > 0) k_extrap_flush<<<grid(p.n, kBlock), kBlock, 0, s>>>(p, reset ? 1 : 0);
 }
 void launch_compact(const KP& p, cudaStream_t s) {
     if (p.nf > 0) k_compact<<<cell_grid(p), p.blk_cell, 0, s>>>(p);
