@@ -204,6 +204,7 @@ def _time_steps(sim, steps, stream, flush_buf, torch):
     the GPU runs flush, step, flush, step, ... without host gaps; only the
     event-bracketed step times are summed."""
     sim.set_time()
+    sim.flush_deferred()  # work deferred by earlier steps is not timed ...
     evs = []
     for _ in range(steps):
         with torch.cuda.stream(stream):
@@ -214,6 +215,14 @@ def _time_steps(sim, steps, stream, flush_buf, torch):
         sim.enqueue_steps(1)
         e1.record(stream)
         evs.append((e0, e1))
+    # ... and the work the timed steps deferred is (hierarchical steps extrapolate
+    # inactive cells when a step reads them: what is still pending runs here)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    sim.flush_deferred()
+    e1.record(stream)
+    evs.append((e0, e1))
     torch.cuda.synchronize()
     total = sum(e0.elapsed_time(e1) for e0, e1 in evs)
     sim.sync_time()

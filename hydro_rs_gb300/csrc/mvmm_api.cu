@@ -1235,6 +1235,11 @@ int mvmm_enqueue_steps(mvmm_ctx* c, int64_t n_steps) {
     return enqueue_steps_impl(c, n_steps);
 }
 
+int mvmm_flush_deferred(mvmm_ctx* c) {
+    if (!c) return fail(MVMM_E_INVALID, "null context");
+    return sync_extrap(c, false, c->stream);
+}
+
 int mvmm_drift(mvmm_ctx* c, double dt) {
     if (!c) return fail(MVMM_E_INVALID, "null context");
     if (c->prm.particle_motion == MVMM_MOTION_FIXED) return MVMM_OK;  // v = 0: nothing moves

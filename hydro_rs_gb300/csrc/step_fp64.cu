@@ -44,15 +44,38 @@ __device__ __forceinline__ void write_derived(const KP& p, int i, const St<doubl
 // step order, from the log of the steps' dt: for the cells a step reads (the
 // cells next to its active faces), before a download, and every kDtLog / 2
 // steps for all cells.  Brings cell i up to date before step `upto`.
+// Consecutive steps of the same dt add the same rounded product, so it is
+// formed once per run of equal dt; and an addition that leaves a component
+// unchanged leaves it unchanged for the rest of that run (the same operation on
+// the same bits), which ends the run early for that component: a cell whose
+// source is zero (a uniform neighbourhood) catches up in one addition.
 __device__ __forceinline__ void extrap_catch_up(const KP& p, int i, unsigned int upto) {
     const unsigned int from = p.extrap_step[i];
     if (from >= upto) return;
     St<double> ex = C5(p, F_EXTRAP, i);
     if (gt0_64(C(p, F_PRIM, i))) {
         const St<double> src = C5(p, F_SRC, i);
-        for (unsigned int s = from; s < upto; s++) ex = ex + (-p.dt_log[s % kDtLog]) * src;
+        unsigned int s = from;
+        while (s < upto) {
+            const double dt = p.dt_log[s % kDtLog];
+            const long long dt_bits = __double_as_longlong(dt);
+            unsigned int e = s + 1;
+            while (e < upto && __double_as_longlong(p.dt_log[e % kDtLog]) == dt_bits) e++;
+            const St<double> t = (-dt) * src;
+#pragma unroll
+            for (int q = 0; q < 5; q++) {
+                double x = ex.q[q];
+                for (unsigned int k = s; k < e; k++) {
+                    const double y = x + t.q[q];
+                    if (__double_as_longlong(y) == __double_as_longlong(x)) break;
+                    x = y;
+                }
+                ex.q[q] = x;
+            }
+            s = e;
+        }
     } else {
-        for (unsigned int s = from; s < upto; s++) ex = ex + st_zero<double>();
+        ex = ex + st_zero<double>();  // adding zero twice gives the bits of adding it once
     }
     W5(p, F_EXTRAP, i, ex);
     p.extrap_step[i] = upto;

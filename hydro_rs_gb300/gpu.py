@@ -26,7 +26,7 @@ EXPORTED = (
     "mvmm_step", "mvmm_run", "mvmm_enqueue_steps", "mvmm_set_time", "mvmm_get_time", "mvmm_profile_enable",
     "mvmm_profile_read", "mvmm_riemann_flux", "mvmm_riemann_sample", "mvmm_get_stats",
     "mvmm_ctx_create_batched", "mvmm_batch_state", "mvmm_autotune", "mvmm_riemann_flux_p", "mvmm_riemann_sample_p",
-    "mvmm_step_cells", "mvmm_drift", "mvmm_get_positions", "mvmm_set_mesh",
+    "mvmm_step_cells", "mvmm_drift", "mvmm_get_positions", "mvmm_set_mesh", "mvmm_flush_deferred",
 )
 
 
@@ -94,6 +94,7 @@ def load_library(path: str = LIB_PATH):
         "mvmm_riemann_flux_p": (i32, [vp, i64, vp, vp, vp, vp, vp]),
         "mvmm_step_cells": (i32, [vp, vp, vp, u64, u64, pu64, pi64]),
         "mvmm_drift": (i32, [vp, dbl]),
+        "mvmm_flush_deferred": (i32, [vp]),
         "mvmm_get_positions": (i32, [vp, vp]),
         "mvmm_set_mesh": (i32, [vp, vp, vp, vp]),
         "mvmm_riemann_sample_p": (i32, [vp, i64, vp, vp, vp, vp]),
@@ -309,6 +310,10 @@ class GpuSim:
         _check(load_library().mvmm_batch_state(self.h, tc.ctypes.data, to.ctypes.data, st.ctypes.data, af.ctypes.data,
                                                err.ctypes.data, fin.ctypes.data), self.h)
         return {"ti_current": tc, "ti_old": to, "steps": st, "active_faces": af, "err": err, "finished": fin}
+
+    def flush_deferred(self):
+        """Enqueues the deferred extrapolations of hierarchical steps (no sync)."""
+        _check(load_library().mvmm_flush_deferred(self.h), self.h)
 
     def autotune(self, steps: int = 3):
         """Picks the thread-block sizes by timing this workload (state is restored)."""

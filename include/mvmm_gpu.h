@@ -209,6 +209,14 @@ int mvmm_run(mvmm_ctx *ctx, int64_t max_steps, uint64_t *ti_current, uint64_t *t
 /* Enqueues n steps on the context stream without synchronising (for timing
  * with events recorded on the same stream); state advances on the device. */
 int mvmm_enqueue_steps(mvmm_ctx *ctx, int64_t n_steps);
+/* Hierarchical steps of one simulation on a fixed mesh defer the time
+ * extrapolation of inactive cells (Particle::extrapolate_state, part.rs:123-132)
+ * until a step reads the cell; the state on the device is complete once this
+ * call's work has run.  Enqueued on the context stream without synchronising
+ * (timing with events); mvmm_download_cells and the per-stage calls do it
+ * themselves.  No counterpart in the reference, which extrapolates every cell
+ * each step. */
+int mvmm_flush_deferred(mvmm_ctx *ctx);
 /* Sets the device timeline to (ti_current, ti_old) before mvmm_enqueue_steps. */
 int mvmm_set_time(mvmm_ctx *ctx, uint64_t ti_current, uint64_t ti_old);
 /* Reads the device timeline and counters (synchronises the stream). */
