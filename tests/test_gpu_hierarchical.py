@@ -75,7 +75,7 @@ def test_deferred_extrapolation(gpu_lib):
     completes them after every step and one that leaves them deferred end on
     the same bits, over more steps than the log of step sizes holds (4,096);
     a download in the middle changes nothing; the oracle agrees at t_end."""
-    p = ics.sod_1d(6000, riemann=ics.HLLC, t_end=0.2)
+    p = ics.sod_1d(1500, riemann=ics.HLLC, t_end=0.2)  # 8,193 steps
     p.params.sync_all = False
     lazy, eager = G.GpuSim(p), G.GpuSim(p)
     lazy.run(max_steps=1000)
