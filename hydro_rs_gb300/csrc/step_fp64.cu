@@ -1063,7 +1063,7 @@ __device__ __forceinline__ void limit_cell(const KP& p, int i, int wakeup = -1) 
     if (wakeup < tb) {
         unsigned long long tc = p.tl[k].ti_current;
         double dt = C(p, F_DT, i);
-        if (tb <= get_max_active_bin(tc)) {  // bin_is_starting
+        if (tb <= max_active_bin_bits(tc)) {  // bin_is_starting
             tb = wakeup;
             dt = (double)get_integer_timestep(tb) * time_base;
         } else {
@@ -1319,7 +1319,11 @@ void launch_timesteps(const KP& p, double* dt_out, cudaStream_t s) {
     if (p.n > 0) k_timesteps<<<grid(p.n, p.blk_cell), p.blk_cell, 0, s>>>(p, dt_out);
 }
 void launch_limit(const KP& p, cudaStream_t s) {
-    if (p.n > 0) k_limit<<<cell_grid(p), p.blk_cell, 0, s>>>(p);
+    if (p.n <= 0) return;
+    // steps over all cells: few, full blocks striding over the cells, so that
+    // few blocks take part in the last-block hand-off of the step's bookkeeping
+    if (p.use_list) k_limit<<<cell_grid(p), p.blk_cell, 0, s>>>(p);
+    else k_limit<<<std::min(grid(p.n, 256), 152 * 8), 256, 0, s>>>(p);
 }
 // the engine bookkeeping runs in the last block of k_limit
 void launch_end(const KP&, cudaStream_t) {}
