@@ -731,7 +731,7 @@ __device__ __forceinline__ double rsqrt64(double x) {  // FP32 seed + one Newton
     return w * (1.5 - 0.5 * x * (w * w));
 }
 struct F32Side {
-    float rho, p, a, sqA, B, c_rar, k_fp;
+    float rho, p, a, sqA, B, c_rar, k_fp, ps_rm, k_fp_rm;  // ps_rm = p^(-1/m), k_fp_rm = k_fp / ps_rm
 };
 __device__ __forceinline__ F32Side f32_side(float rho, float p, float a, const Gas<float>& g) {
     F32Side s;
@@ -742,18 +742,23 @@ __device__ __forceinline__ F32Side f32_side(float rho, float p, float a, const G
     s.B = g.gm1dgp1() * p;
     s.c_rar = g.tdgm1() * a;
     s.k_fp = 1.f / (rho * a);
+    s.ps_rm = __powf(p, -g.gm1d2g());
+    s.k_fp_rm = s.k_fp / s.ps_rm;
     return s;
 }
-__device__ __forceinline__ void f32_eval(float p, const F32Side& s, float z, float& fb, float& fpb) {
-    if (p > s.p) {
-        float w = rsqrtf(p + s.B);
+// One side's f term and its derivative (exact.rs:12-20, 37-45) in FP32 at
+// pp = x^m with x known: the rarefaction's (pp/p_s)^(1/m) is x p_s^(-1/m) and
+// its derivative term k_fp / t is k_fp_rm / x (inv_x = 1/x), so the iteration
+// takes no power.
+__device__ __forceinline__ void f32_eval_x(float pp, float x, float inv_x, const F32Side& s, float& fb, float& fpb) {
+    if (pp > s.p) {
+        float w = rsqrtf(pp + s.B);
         float sw = s.sqA * w;
-        fb = (p - s.p) * sw;
-        fpb = sw * (1.f - 0.5f * (p - s.p) * (w * w));
+        fb = (pp - s.p) * sw;
+        fpb = sw * (1.f - 0.5f * (pp - s.p) * (w * w));
     } else {
-        float t = __powf(p / s.p, z);
-        fb = s.c_rar * (t - 1.f);
-        fpb = s.k_fp / t;
+        fb = s.c_rar * fmaf(x, s.ps_rm, -1.f);
+        fpb = s.k_fp_rm * inv_x;
     }
 }
 // One side's term of f (exact.rs:12-20) in FP32 to a few ulp of the term
@@ -764,6 +769,8 @@ __device__ __forceinline__ float side_acc(float p, const F32Side& s, float inv_m
     if (p > s.p) return (p - s.p) * s.sqA * rsqrtf(p + s.B);
     return s.c_rar * expm1f(log1pf((p - s.p) / s.p) * inv_m);
 }
+// M: the gamma's m when known at compile time (5 for 5/3, 7 for 7/5), else 0
+template <int M>
 static __device__ __noinline__ Star<float> ex_star_split(float rl, float pl, float al, float rr, float pr, float ar,
                                                          float vl, float vr, Gas<float> g, Gas<double> g64,
                                                          int max_iter, unsigned int* err) {
@@ -777,8 +784,8 @@ static __device__ __noinline__ Star<float> ex_star_split(float rl, float pl, flo
     if (p_max <= 2.f * p_min && p_min <= ppv && ppv <= p_max) {
         p = ppv;
     } else if (ppv < p_min) {
-        float base = (al + ar - 0.5f * (g.gamma - 1.f) * dv) / (al * __powf(pl, -z) + ar * __powf(pr, -z));
-        p = base > 0.f ? ipow(base, g64.rm) : 1e-8f;
+        float base = (al + ar - 0.5f * (g.gamma - 1.f) * dv) / (al * L.ps_rm + ar * R.ps_rm);
+        p = base > 0.f ? ipow(base, M > 0 ? M : g64.rm) : 1e-8f;
     } else {
         float gl = L.sqA * rsqrtf(ppv + L.B), gr = R.sqA * rsqrtf(ppv + R.B);
         p = (gl * pl + gr * pr - dv) / (gl + gr);
@@ -788,15 +795,16 @@ static __device__ __noinline__ Star<float> ex_star_split(float rl, float pl, flo
     // x (two rarefactions converge in one step) and the shock terms convex, so
     // after at most one overshoot the iterates approach the root monotonically;
     // Newton in p crawls where a step lands at small p and (p/p_s)^(1/m) is steep.
-    const int m = g64.rm;
+    const int m = M > 0 ? M : g64.rm;
     const float inv_m = 1.f / (float)m;
     float x = __powf(p, inv_m);
     for (int it = 0; it < 16; it++) {
         float xm1 = ipow(x, m - 1);
         float pp = xm1 * x;
+        const float inv_x = 1.f / x;
         float fbl, fpl, fbr, fpr;
-        f32_eval(pp, L, z, fbl, fpl);
-        f32_eval(pp, R, z, fbr, fpr);
+        f32_eval_x(pp, x, inv_x, L, fbl, fpl);
+        f32_eval_x(pp, x, inv_x, R, fbr, fpr);
         float dx = (fbl + fbr + dv) / ((fpl + fpr) * (float)m * xm1);
         float xn = x - dx;
         if (!(xn > 0.f)) xn = 0.5f * x;
@@ -808,8 +816,9 @@ static __device__ __noinline__ Star<float> ex_star_split(float rl, float pl, flo
     // one Newton step with the cancelling sum f = f_l + f_r + (v_r - v_l) in
     // FP64 over accurate FP32 terms; f' in FP32
     float fbl, fpl, fbr, fpr;
-    f32_eval(p, L, z, fbl, fpl);
-    f32_eval(p, R, z, fbr, fpr);
+    const float inv_x = 1.f / x;
+    f32_eval_x(p, x, inv_x, L, fbl, fpl);
+    f32_eval_x(p, x, inv_x, R, fbr, fpr);
     double fP = ((double)vr - (double)vl) + (double)side_acc(p, L, inv_m) + (double)side_acc(p, R, inv_m);
     double dP = fP * (double)(1.f / (fpl + fpr));
     double P = (double)p - dP;
@@ -832,8 +841,8 @@ static __device__ __noinline__ Star<float> ex_star_split(float rl, float pl, flo
     s.u = 0.5f * (vl + vr) + 0.5f * (side_acc(ps, R, inv_m) - side_acc(ps, L, inv_m));
     float gg = g.gm1dgp1();
     float qlr = ps / pl, qrr = ps / pr;
-    s.rho_l = qlr > 1.f ? rl * (qlr + gg) / (gg * qlr + 1.f) : rl * ipow(__powf(qlr, z), g64.rm - 2);
-    s.rho_r = qrr > 1.f ? rr * (qrr + gg) / (gg * qrr + 1.f) : rr * ipow(__powf(qrr, z), g64.rm - 2);
+    s.rho_l = qlr > 1.f ? rl * (qlr + gg) / (gg * qlr + 1.f) : rl * ipow(__powf(qlr, z), m - 2);
+    s.rho_r = qrr > 1.f ? rr * (qrr + gg) / (gg * qrr + 1.f) : rr * ipow(__powf(qrr, z), m - 2);
     s.p = ps;
     return s;
 }
@@ -930,8 +939,11 @@ __device__ __forceinline__ Star<T> exact_star(const St<T>& l, const St<T>& r, T 
                                               unsigned int* err) {
     Star<T> s;
     if (sizeof(T) == 4 && g64.rm) {
-        Star<float> sf = ex_star_split(float(l.q[0]), float(l.q[4]), float(al), float(r.q[0]), float(r.q[4]),
-                                       float(ar), float(vl), float(vr), gas32(g), g64, max_iter, err);
+        const float a0 = float(l.q[0]), a1 = float(l.q[4]), a2 = float(al), b0 = float(r.q[0]), b1 = float(r.q[4]),
+                    b2 = float(ar), u0 = float(vl), u1 = float(vr);
+        Star<float> sf = g64.rm == 5   ? ex_star_split<5>(a0, a1, a2, b0, b1, b2, u0, u1, gas32(g), g64, max_iter, err)
+                         : g64.rm == 7 ? ex_star_split<7>(a0, a1, a2, b0, b1, b2, u0, u1, gas32(g), g64, max_iter, err)
+                                       : ex_star_split<0>(a0, a1, a2, b0, b1, b2, u0, u1, gas32(g), g64, max_iter, err);
         s.rho_l = T(sf.rho_l);
         s.rho_r = T(sf.rho_r);
         s.u = T(sf.u);
