@@ -241,6 +241,7 @@ void launch_face(mvmm_ctx* c, const KP& p, bool prepped = false) {
 // the update and after the gradient stage for the copies back.
 struct StepHooks {
     bool stale_all = false;
+    double* snap_late = nullptr;
     bool geom_before_face = false;
     cudaEvent_t wait_before_update = nullptr;
     cudaEvent_t after_update = nullptr;
@@ -254,6 +255,7 @@ void record_ev(mvmm_ctx* c, int j, cudaStream_t s) { cudaEventRecordWithFlags(c-
 void enqueue_step_kernels(mvmm_ctx* c, bool with_events, const StepHooks& h = StepHooks()) {
     KP p = make_kp(c, 0, 7);
     p.stale_all = h.stale_all ? 1 : 0;
+    p.snap_late = h.snap_late;
     cudaStream_t s = c->stream;
     if (with_events) record_ev(c, 0, s);
     // steps over all cells of the FP32-face form: predict and the FP32 copies in one kernel
@@ -857,12 +859,14 @@ int transfer(mvmm_ctx* c, const Xfer* pairs, int m, bool h2d, bool overlap, int 
 // max_blocks: the copy kernel's grid cap (0: four blocks per SM).
 // snapshot (host -> device): the rows also go to the snapshot block.
 // in_place (device -> host): the host arrays of `in_place` that `h` shares
-// still hold the bytes of the snapshot, so only what differs is stored.
+// still hold the bytes of the snapshot, so only what differs is stored;
+// diff_rows: the rows (row_map bits) whose snapshot is current.
 struct CopyOpts {
     bool overlap = false;
     int max_blocks = 0;
     bool snapshot = false;
     const mvmm_cells* in_place = nullptr;
+    unsigned diff_rows = 0x3fffu;
 };
 
 // The host array of field k (row_map order) of h.
@@ -879,7 +883,8 @@ int copy_rows(mvmm_ctx* c, const mvmm_cells* h, const RowCopy* map, const int* i
     const size_t n = c->n;
     const bool h2d = kind == cudaMemcpyHostToDevice;
     auto diffable = [&](size_t a) {
-        return !h2d && o.in_place && c->snap && field_ptr(h, idx[a]) == field_ptr(o.in_place, idx[a]);
+        return !h2d && o.in_place && c->snap && ((o.diff_rows >> idx[a]) & 1u) &&
+               field_ptr(h, idx[a]) == field_ptr(o.in_place, idx[a]);
     };
     Xfer x[kMaxXfer];
     int nx = 0;
@@ -1027,11 +1032,17 @@ int mvmm_step_cells(mvmm_ctx* c, const mvmm_cells* in, mvmm_cells* out, uint64_t
     up.snapshot = false;  // taken on the device once the rows have landed (a short kernel)
     rc = copy_cells(c, in, kRowsLateIn, false, cudaMemcpyHostToDevice, s2, up);
     if (rc) return rc;
-    rc = snapshot_rows(c, kRowsLateIn, false, s2);
-    if (rc) return rc;
+    // their snapshot: with every cell updated every step the update kernel
+    // keeps the bytes it reads; else a device copy, which the update waits for
+    const unsigned late_snap = kRowsLateIn & ~kRowsPassThrough;
+    if (!c->prm.sync_all) {
+        rc = snapshot_rows(c, late_snap, false, s2);
+        if (rc) return rc;
+    }
     CUDA_TRY(cudaEventRecord(c->ev_in, s2));
     StepHooks h;
     h.stale_all = true;
+    if (c->prm.sync_all) h.snap_late = c->snap;
     h.geom_before_face = true;
     h.wait_before_update = c->ev_in;
     h.after_update = c->ev_upd;
@@ -1045,6 +1056,7 @@ int mvmm_step_cells(mvmm_ctx* c, const mvmm_cells* in, mvmm_cells* out, uint64_t
     back.overlap = true;
     back.max_blocks = 64;  // beside the gradient stage
     back.in_place = in;
+    back.diff_rows = kRowsPredictIn | kRowsFaceIn | late_snap;
     CUDA_TRY(cudaStreamWaitEvent(s2, c->ev_upd, 0));
     rc = copy_cells(c, out, kRowsEarlyOut, false, cudaMemcpyDeviceToHost, s2, back);
     if (rc) return rc;

@@ -136,6 +136,8 @@ struct KP {
     double time_base, time_base_inv;
     int stage;               // 1: per-stage call (explicit dt / mask from the host)
     int stale_all;           // 1: every cell's state came from the host this step (fresh flags void)
+    double* snap_late;       // or null: the update keeps the rows it reads first (cons, facc, max_signal_velocity,
+                             //   max_a_over_r) as uploaded, at their field offsets (steps over all cells)
     double stage_dt;
     // batches: many independent simulations packed into one mesh; each has its
     // own device timeline tl[k] (k = inst[cell]) and time base

@@ -545,6 +545,16 @@ __device__ __forceinline__ void update_cell(const KP& p, int i, int do_c2p) {
     bool act = p.active[i] != 0;
     St<double> facc = C5(p, F_FACC, i);
     double msv = C(p, F_MSV, i), maor = C(p, F_MAOR, i);
+    if (p.snap_late) {  // the uploaded bytes of the rows this kernel rewrites, for the copy back's comparison
+        const size_t n = (size_t)p.n;
+#pragma unroll
+        for (int q = 0; q < 5; q++) {
+            p.snap_late[(F_CONS + q) * n + i] = C(p, F_CONS + q, i);
+            p.snap_late[(F_FACC + q) * n + i] = facc.q[q];
+        }
+        p.snap_late[F_MSV * n + i] = msv;
+        p.snap_late[F_MAOR * n + i] = maor;
+    }
     const size_t nf = (size_t)p.nf;
     int k0 = p.csr_off[i], k1 = p.csr_off[i + 1];
     const unsigned int stamp = p.use_list ? face_stamp_now(p) : 0u;

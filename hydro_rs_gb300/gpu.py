@@ -257,8 +257,8 @@ class GpuSim:
     def step_cells(self, cells_in: Cells, cells_out: Cells | None = None) -> bool:
         """One step on host-resident state (mvmm_step_cells): upload, step and
         download in one call; cells_out defaults to cells_in."""
-        cells_out = cells_in if cells_out is None else cells_out
-        ci, co = cells_in.cview(), cells_out.cview()
+        ci = cells_in.cview()
+        co = ci if cells_out is None or cells_out is cells_in else cells_out.cview()
         tn = ctypes.c_uint64(0)
         nf = ctypes.c_int64(0)
         _check(load_library().mvmm_step_cells(self.h, ctypes.byref(ci), ctypes.byref(co), self.ti_current,

@@ -113,11 +113,21 @@ class Cells:
         return Cells(n=self.n, arrays={k: v.copy() for k, v in self.arrays.items()})
 
     def cview(self) -> CCells:
+        """The C struct of pointers to the arrays.  Kept while the same array
+        objects (and the same n) are in place, as building it costs more than
+        a call into the library; the cache holds the arrays, so an array that
+        was replaced cannot hand its address to a new one."""
+        arrs = tuple(self.arrays[name] for name, _ in CELL_FIELDS) + (self.arrays["timebin"],)
+        cached = self.__dict__.get("_cview")
+        if cached is not None and cached[0] == self.n and len(cached[1]) == len(arrs) and \
+                all(a is b for a, b in zip(cached[1], arrs)):
+            return cached[2]
         cv = CCells()
         cv.n = self.n
-        for name, _ in CELL_FIELDS:
-            setattr(cv, name, _ptr(self.arrays[name]))
-        cv.timebin = _ptr(self.arrays["timebin"])
+        for (name, _), a in zip(CELL_FIELDS, arrs):
+            setattr(cv, name, _ptr(a))
+        cv.timebin = _ptr(arrs[-1])
+        self.__dict__["_cview"] = (self.n, arrs, cv)
         return cv
 
     def nbytes(self) -> int:
