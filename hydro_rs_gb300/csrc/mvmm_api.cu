@@ -97,7 +97,9 @@ struct mvmm_ctx {
     bool prof = false;
     cudaEvent_t ev[MVMM_NUM_KERNELS + 1] = {};
     cudaStream_t side = nullptr;              // copies of mvmm_step_cells that overlap the step
-    cudaEvent_t ev_pred = nullptr, ev_in = nullptr, ev_upd = nullptr, ev_grad = nullptr, ev_out = nullptr;
+    cudaStream_t geo_side = nullptr;          // its FP32 face-geometry refresh, beside predict
+    cudaEvent_t ev_pred = nullptr, ev_in = nullptr, ev_upd = nullptr, ev_grad = nullptr, ev_out = nullptr,
+                ev_geo = nullptr;
     double prof_ms[MVMM_NUM_KERNELS] = {};
     int64_t prof_n[MVMM_NUM_KERNELS] = {};
     double time_base = 0, time_base_inv = 0;
@@ -236,13 +238,14 @@ void launch_face(mvmm_ctx* c, const KP& p, bool prepped = false) {
 
 // The six kernels of one OptimalOrderRunner step, optionally bracketed by events.
 // A step on cells uploaded with it (mvmm_step_cells): predict recomputes every
-// derived row, the FP32 geometry follows the uploaded positions, the update
-// waits for an event (the rows only it reads), and events are recorded after
+// derived row, the face stage waits for an event (the FP32 geometry refreshed
+// on a side stream), the update for another (the rows only it reads), and
+// events are recorded after
 // the update and after the gradient stage for the copies back.
 struct StepHooks {
     bool stale_all = false;
     double* snap_late = nullptr;
-    bool geom_before_face = false;
+    cudaEvent_t wait_before_face = nullptr;
     cudaEvent_t wait_before_update = nullptr;
     cudaEvent_t after_update = nullptr;
     cudaEvent_t after_gradients = nullptr;
@@ -263,8 +266,8 @@ void enqueue_step_kernels(mvmm_ctx* c, bool with_events, const StepHooks& h = St
     if (fused) launch_predict32(p, s);
     else launch_predict(p, s);
     if (c->pending_geometry) launch_geometry(p, s);  // after predict, as volume_calculation
-    if (h.geom_before_face || c->prm.particle_motion != MVMM_MOTION_FIXED)
-        update_geom32(c, p, s);  // generators drifted or uploaded, centroids updated
+    if (c->prm.particle_motion != MVMM_MOTION_FIXED) update_geom32(c, p, s);  // generators drifted, centroids updated
+    if (h.wait_before_face) cudaStreamWaitEvent(s, h.wait_before_face, 0);
     if (p.use_list) launch_compact(p, s);
     if (with_events) record_ev(c, 1, s);
     launch_face(c, p, fused);
@@ -645,7 +648,8 @@ int mvmm_ctx_destroy(mvmm_ctx* c) {
         if (c->ev[k]) cudaEventDestroy(c->ev[k]);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     if (c->side) cudaStreamDestroy(c->side);
-    for (cudaEvent_t e : {c->ev_pred, c->ev_in, c->ev_upd, c->ev_grad, c->ev_out})
+    if (c->geo_side) cudaStreamDestroy(c->geo_side);
+    for (cudaEvent_t e : {c->ev_pred, c->ev_in, c->ev_upd, c->ev_grad, c->ev_out, c->ev_geo})
         if (e) cudaEventDestroy(e);
     delete c;
     return MVMM_OK;
@@ -1006,7 +1010,8 @@ int mvmm_step_cells(mvmm_ctx* c, const mvmm_cells* in, mvmm_cells* out, uint64_t
         return fail(MVMM_E_UNSUPPORTED, "mvmm_step_cells steps a fixed mesh");
     if (!c->side) {
         CUDA_TRY(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
-        for (cudaEvent_t* e : {&c->ev_pred, &c->ev_in, &c->ev_upd, &c->ev_grad, &c->ev_out})
+        CUDA_TRY(cudaStreamCreateWithFlags(&c->geo_side, cudaStreamNonBlocking));
+        for (cudaEvent_t* e : {&c->ev_pred, &c->ev_in, &c->ev_upd, &c->ev_grad, &c->ev_out, &c->ev_geo})
             CUDA_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
     }
     if (!c->snap) {
@@ -1028,6 +1033,14 @@ int mvmm_step_cells(mvmm_ctx* c, const mvmm_cells* in, mvmm_cells* out, uint64_t
     if (rc) return rc;
     CUDA_TRY(cudaEventRecord(c->ev_pred, s));
     CUDA_TRY(cudaStreamWaitEvent(s2, c->ev_pred, 0));
+    // the FP32 face geometry follows the uploaded positions and centroids, on a
+    // stream of its own while predict runs (predict does not read it)
+    const bool geo_side = c->prm.precision == MVMM_PRECISION_FP32FACE;
+    if (geo_side) {
+        CUDA_TRY(cudaStreamWaitEvent(c->geo_side, c->ev_pred, 0));
+        update_geom32(c, make_kp(c, 0, 7), c->geo_side);
+        CUDA_TRY(cudaEventRecord(c->ev_geo, c->geo_side));
+    }
     up.overlap = true;
     up.snapshot = false;  // taken on the device once the rows have landed (a short kernel)
     rc = copy_cells(c, in, kRowsLateIn, false, cudaMemcpyHostToDevice, s2, up);
@@ -1043,7 +1056,7 @@ int mvmm_step_cells(mvmm_ctx* c, const mvmm_cells* in, mvmm_cells* out, uint64_t
     StepHooks h;
     h.stale_all = true;
     if (c->prm.sync_all) h.snap_late = c->snap;
-    h.geom_before_face = true;
+    h.wait_before_face = geo_side ? c->ev_geo : nullptr;
     h.wait_before_update = c->ev_in;
     h.after_update = c->ev_upd;
     h.after_gradients = c->ev_grad;
