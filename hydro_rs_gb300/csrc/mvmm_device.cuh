@@ -714,18 +714,17 @@ static __device__ __noinline__ Star<double> ex_star_fast(ExSide L, ExSide R, dou
     return st_;
 }
 
-// Exact star state for the FP32-face form, split by precision.  GB300 runs
-// FP64 at a small fraction of its FP32 rate, so the reference's search (guess,
-// Newton, bracketing) runs in FP32 only to produce a starting pressure, and
-// the pressure this form uses comes from two FP64 Newton steps on the
-// FP64-evaluated f(p) (exact.rs:23-34): f in FP64 (where the near-root
-// cancellation of f_L + f_R + dv happens), f' from FP32 (an approximate
-// derivative keeps Newton's convergence, at a rate set by its 1e-7 error).
-// From a start within ~1e-5 the two steps leave ~1e-12; a last correction
-// above 1e-8 (the FP32 resolution of the result) sends the face to the
-// fallback.  Lanes stay uniform in the FP64 part.  A face whose FP32 start or FP64 polish is not clean
-// (near vacuum, extreme ratios) is solved by the full FP64 reference
-// iteration instead (ex_star_fast).  Requires gamma = m/(m-2).
+// Exact star state for the FP32-face form.  GB300 runs FP64 at a small
+// fraction of its FP32 rate, so the reference's search (guess_p, then Newton
+// on f(p) = f_L + f_R + (v_R - v_L), exact.rs:23-34, 70-103) runs in FP32:
+// Newton on x = p^(1/m) to 1e-6, then one Newton step whose f is the sum of
+// the accurate FP32 terms formed without rounding (a TwoSum pair), which is
+// where the near-root cancellation of f_L + f_R + dv happens; f' from FP32
+// (an approximate derivative keeps Newton's convergence, at a rate set by its
+// 1e-7 error).  A correction above 1e-4 of the pressure (a search that did
+// not converge), a non-finite or non-positive result (near vacuum, extreme
+// ratios) sends the face to the full FP64 reference iteration (ex_star_fast).
+// Requires gamma = m/(m-2).
 __device__ __forceinline__ double rsqrt64(double x) {  // FP32 seed + one Newton step (~1e-14)
     double w = (double)rsqrtf((float)x);
     return w * (1.5 - 0.5 * x * (w * w));
@@ -746,6 +745,20 @@ __device__ __forceinline__ F32Side f32_side(float rho, float p, float a, const G
     s.k_fp_rm = s.k_fp / s.ps_rm;
     return s;
 }
+// Error-free FP32 sum (Knuth's TwoSum): hi + lo carries the sum of the FP32
+// addends to ~1e-14 relative.  The rounded-addition intrinsics keep a product
+// passed in as x from being fused into the first addition.
+struct Sum2 {
+    float hi, lo;
+};
+__device__ __forceinline__ void sum2_add(Sum2& a, float x) {
+    const float s = __fadd_rn(a.hi, x);
+    const float bp = __fsub_rn(s, a.hi);
+    const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bp)), __fsub_rn(x, bp));
+    a.hi = s;
+    a.lo = __fadd_rn(a.lo, e);
+}
+
 // One side's f term and its derivative (exact.rs:12-20, 37-45) in FP32 at
 // pp = x^m with x known: the rarefaction's (pp/p_s)^(1/m) is x p_s^(-1/m) and
 // its derivative term k_fp / t is k_fp_rm / x (inv_x = 1/x), so the iteration
@@ -813,19 +826,23 @@ static __device__ __noinline__ Star<float> ex_star_split(float rl, float pl, flo
         if (done) break;
     }
     p = ipow(x, m);
-    // one Newton step with the cancelling sum f = f_l + f_r + (v_r - v_l) in
-    // FP64 over accurate FP32 terms; f' in FP32
+    // one Newton step with the cancelling sum f = (v_r - v_l) + f_l + f_r of
+    // accurate FP32 terms formed without rounding (a TwoSum pair, rounded once
+    // at the end); f' in FP32
     float fbl, fpl, fbr, fpr;
     const float inv_x = 1.f / x;
     f32_eval_x(p, x, inv_x, L, fbl, fpl);
     f32_eval_x(p, x, inv_x, R, fbr, fpr);
-    double fP = ((double)vr - (double)vl) + (double)side_acc(p, L, inv_m) + (double)side_acc(p, R, inv_m);
-    double dP = fP * (double)(1.f / (fpl + fpr));
-    double P = (double)p - dP;
+    Sum2 f{vr, 0.f};
+    sum2_add(f, -vl);
+    sum2_add(f, side_acc(p, L, inv_m));
+    sum2_add(f, side_acc(p, R, inv_m));
+    const float dP = (f.hi + f.lo) / (fpl + fpr);
+    const float P = p - dP;
     Star<float> s;
     // a search that ended more than 1e-4 from the root (after the step the
     // error is of order dP^2) is redone by the full FP64 iteration
-    if (!(P > 0.) || !isfinite(P) || !(fabs(dP) <= 1e-4 * P)) {
+    if (!(P > 0.f) || !isfinite(P) || !(fabsf(dP) <= 1e-4f * P)) {
         *err |= 1u << 16;  // counted by the face kernel as a fallback face
         Star<double> sd = ex_star_fast(ExSide{(double)rl, (double)pl, (double)al},
                                        ExSide{(double)rr, (double)pr, (double)ar}, (double)vl, (double)vr, g64,
@@ -837,7 +854,7 @@ static __device__ __noinline__ Star<float> ex_star_split(float rl, float pl, flo
         return s;
     }
     // star_state_from_pstar (exact.rs:214-238) in FP32 at the polished pressure
-    float ps = (float)P;
+    const float ps = P;
     s.u = 0.5f * (vl + vr) + 0.5f * (side_acc(ps, R, inv_m) - side_acc(ps, L, inv_m));
     float gg = g.gm1dgp1();
     float qlr = ps / pl, qrr = ps / pr;
@@ -931,7 +948,7 @@ enum {
 __device__ __forceinline__ const Gas<float>& gas32(const Gas<float>& g) { return g; }
 __device__ __forceinline__ Gas<float> gas32(const Gas<double>& g) { return make_gas<float>(g.gamma, g.eos, g.iso_u); }
 
-// Exact star state in the face type: FP32 search + FP64 polish for the
+// Exact star state in the face type: the FP32 search above for the
 // FP32-face form with a rational gamma, else the FP64 reference iteration.
 template <typename T>
 __device__ __forceinline__ Star<T> exact_star(const St<T>& l, const St<T>& r, T vl, T vr, T al, T ar,

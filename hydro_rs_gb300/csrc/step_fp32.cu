@@ -2,8 +2,9 @@
 //
 // Reconstruction, the pair-wise limiter, the Riemann solve and the face flux
 // run in FP32 on a static FP32 face geometry (differences formed in FP64 once
-// per upload, then rounded); the exact solver's pressure is polished in FP64
-// (full FP64 iteration where the FP32 search does not converge).  A step
+// per upload, then rounded); the exact solver's last Newton step sums the
+// cancelling terms without rounding (full FP64 iteration where the FP32 search
+// does not converge).  A step
 // writes FP32 face fluxes dt * area * F; the scatter and the conserved update
 // accumulate them in FP64 (the update kernel is shared with the plain form),
 // so every face flux leaves one cell and enters the other exactly.  Compiled

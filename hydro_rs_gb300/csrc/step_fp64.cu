@@ -516,19 +516,8 @@ __device__ __forceinline__ void c2p(const KP& p, int i, const St<double>& cons, 
 }
 
 // ---------------------------------------------------- scatter + update --
-// Error-free FP32 sum (Knuth's TwoSum): hi + lo carries the sum of the FP32
-// addends to ~1e-14 relative, so FP32 face fluxes are accumulated at FP64
-// accuracy without a per-face FP64 conversion.
-struct Sum2 {
-    float hi, lo;
-};
-__device__ __forceinline__ void sum2_add(Sum2& a, float x) {
-    float s = a.hi + x;
-    float bp = s - a.hi;
-    float e = (a.hi - (s - bp)) + (x - bp);
-    a.hi = s;
-    a.lo += e;
-}
+// FP32 face fluxes are accumulated at FP64 accuracy in Sum2 pairs (TwoSum),
+// without a per-face FP64 conversion.
 
 // apply_fluxes (runner/hydrodynamics.rs:13-39): CSR gather of every face of
 // the cell in CSR order; active cells fold the accumulator into the conserved
