@@ -477,6 +477,15 @@ __device__ __forceinline__ void gradients32_cell(const KP& p, int i) {
             float a00 = 0.f, a01 = 0.f, a02 = 0.f, a11 = 0.f, a12 = 0.f, a22 = 0.f;
             if (p.dim == 1) { a11 = 1.f; a22 = 1.f; }
             else if (p.dim == 2) { a22 = 1.f; }
+            // LimiterData (gradients.rs:58-103) on differences to this cell's
+            // state: the neighbours' differences are gathered here, the
+            // extrapolations (which need the gradient) in a second pass
+            float dmn[5], dmx[5];
+#pragma unroll
+            for (int q = 0; q < 5; q++) {
+                dmn[q] = 0.f;
+                dmx[q] = 0.f;
+            }
             int k0 = p.csr_off[i], k1 = p.csr_off[i + 1];
             for (int k = k0; k < k1; k++) {
                 int f = p.csr_face[k];
@@ -485,7 +494,12 @@ __device__ __forceinline__ void gradients32_cell(const KP& p, int i) {
                 other_side32(p, i, f, prim, op, ds, d);
                 float w = p.geo[GE_W * (size_t)p.nf + f];
 #pragma unroll
-                for (int q = 0; q < 5; q++) gr[q] = gr[q] + (w * (op.q[q] - prim.q[q])) * ds;
+                for (int q = 0; q < 5; q++) {
+                    const float dq = op.q[q] - prim.q[q];
+                    gr[q] = gr[q] + (w * dq) * ds;
+                    dmn[q] = fminf(dmn[q], dq);
+                    dmx[q] = fmaxf(dmx[q], dq);
+                }
                 a00 += w * ds.x * ds.x;
                 a01 += w * ds.x * ds.y;
                 a02 += w * ds.x * ds.z;
@@ -508,26 +522,19 @@ __device__ __forceinline__ void gradients32_cell(const KP& p, int i) {
 #pragma unroll
                 for (int q = 0; q < 5; q++) gr[q] = v3(0.f, 0.f, 0.f);
             }
-            // LimiterData (gradients.rs:58-103) on differences to this cell's state
-            float dmn[5], dmx[5], emn[5], emx[5];
+            float emn[5], emx[5];
 #pragma unroll
             for (int q = 0; q < 5; q++) {
-                dmn[q] = 0.f;
-                dmx[q] = 0.f;
                 emn[q] = INFINITY;
                 emx[q] = -INFINITY;
             }
             for (int k = k0; k < k1; k++) {
-                int f = p.csr_face[k];
-                St<float> op;
-                V3<float> ds, d;
-                other_side32(p, i, f, prim, op, ds, d);
+                const int f = p.csr_face[k];
+                // the limiter's extrapolation vector seen from cell i (as other_side32)
+                const V3<float> d = p.left[f] == i ? GE3(p, GE_DL, f) : GE3(p, GE_DR, f);
 #pragma unroll
                 for (int q = 0; q < 5; q++) {
                     float ex = dot(gr[q], d);
-                    float dq = op.q[q] - prim.q[q];
-                    dmn[q] = fminf(dmn[q], dq);
-                    dmx[q] = fmaxf(dmx[q], dq);
                     emn[q] = fminf(emn[q], ex);
                     emx[q] = fmaxf(emx[q], ex);
                 }
