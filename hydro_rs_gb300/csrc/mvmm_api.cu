@@ -85,6 +85,7 @@ struct mvmm_ctx {
     unsigned int* touch = nullptr;
     unsigned int* blocks_done = nullptr;
     uint8_t* fresh = nullptr;
+    uint8_t* cf_fresh = nullptr;
     int* cell_list = nullptr;
     int* face_list = nullptr;
     int blk_face = 128, blk_cell = 128;
@@ -193,6 +194,7 @@ KP make_kp(mvmm_ctx* c, int stage, int flux_rows) {
     p.touch = c->touch;
     p.blocks_done = c->blocks_done;
     p.fresh = c->fresh;
+    p.cf_fresh = c->cf_fresh;
     p.cell_list = c->cell_list;
     p.face_list = c->face_list;
     p.blk_face = c->blk_face;
@@ -532,6 +534,8 @@ static int create_impl(const mvmm_params* prm, const mvmm_mesh* m, int64_t n_ins
     ALLOC(c->blocks_done, 4);
     ALLOC(c->xfer_stored, 8);
     ALLOC(c->fresh, n);
+    if (prm->precision == MVMM_PRECISION_FP32FACE && prm->particle_motion == MVMM_MOTION_FIXED)
+        ALLOC(c->cf_fresh, n);
     ALLOC(c->cell_list, n * 4);
     ALLOC(c->face_list, nf * 4);
     ALLOC(c->tl, sizeof(DevTimeline) * c->n_inst);
@@ -575,6 +579,7 @@ static int create_impl(const mvmm_params* prm, const mvmm_mesh* m, int64_t n_ins
     cudaMemsetAsync(c->touch, 0, n * 4, s);
     cudaMemsetAsync(c->blocks_done, 0, 4, s);
     cudaMemsetAsync(c->fresh, 0, n, s);
+    if (c->cf_fresh) cudaMemsetAsync(c->cf_fresh, 0, n, s);
     if (c->extrap_step) cudaMemsetAsync(c->extrap_step, 0, n * 4, s);  // current at step 0
     std::memset(c->tl_host, 0, sizeof(DevTimeline) * c->n_inst);
     for (int k = 0; k < c->n_inst; k++) {
@@ -637,7 +642,7 @@ int mvmm_ctx_destroy(mvmm_ctx* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     drop_graphs(c);
     void* ptrs[] = {c->left, c->right, c->csr_off, c->csr_face, c->area, c->normal, c->fcen, c->shift, c->cd,
-                    c->cf, c->timebin, c->tb_tmp, c->active, c->flux, c->flux32, c->geo, c->geo_pos, c->geo_changed, c->snap, c->snap_tb, c->xfer_stored, c->brent_jobs, c->brent_count, c->extrap_step, c->dt_log, c->dtmp, c->face_stamp, c->touch, c->blocks_done, c->cell_list, c->fresh,
+                    c->cf, c->timebin, c->tb_tmp, c->active, c->flux, c->flux32, c->geo, c->geo_pos, c->geo_changed, c->snap, c->snap_tb, c->xfer_stored, c->brent_jobs, c->brent_count, c->extrap_step, c->dt_log, c->dtmp, c->face_stamp, c->touch, c->blocks_done, c->cell_list, c->fresh, c->cf_fresh,
                     c->pend_vol, c->pend_cen,
                     c->face_list, c->tl,
                     c->inst, c->inst_tb, c->inst_tbi};
@@ -969,6 +974,7 @@ int sync_extrap(mvmm_ctx* c, bool reset, cudaStream_t s) {
 // are recomputed by the next predict.
 int mark_stale(mvmm_ctx* c, cudaStream_t s) {
     CUDA_TRY(cudaMemsetAsync(c->fresh, 0, c->n, s));
+    if (c->cf_fresh) CUDA_TRY(cudaMemsetAsync(c->cf_fresh, 0, c->n, s));
     return MVMM_OK;
 }
 // positions and centroids may have changed: refresh the FP32 face geometry

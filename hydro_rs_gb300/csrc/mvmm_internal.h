@@ -164,6 +164,8 @@ struct KP {
     unsigned int* blocks_done;  // k_limit blocks finished this step (the last one ends the step)
     unsigned int* touch;     // hierarchical steps: 1 for cells on this step's cell list
     uint8_t* fresh;          // 1: the cell's derived face-stage rows match its prim, grad and v_rel
+    uint8_t* cf_fresh;       // FP32-face form: 1 where the FP32 copies of the gradients and of
+                             //   gradients_centroid - loc were written with the FP64 rows (or null)
     int* cell_list;          // hierarchical steps: active cells and the cells next to an active face
     int* face_list;          // compacted active faces
 };

@@ -72,7 +72,10 @@ __global__ void __launch_bounds__(kMaxBlock) k_predict32(KP p) {
     if (k >= 0 && p.tl[k].done) k = -1;  // a finished simulation of a batch is left untouched
     const size_t n = (size_t)p.n;
     float* cf = p.cf;
-    if (k >= 0 && !main_row) {
+    // the gradient and gradients_centroid - loc copies of a fixed mesh's cell are
+    // current when the last gradient stage wrote them and nothing was uploaded since
+    const bool cur = k >= 0 && p.cf_fresh && !p.stale_all && p.cf_fresh[i];
+    if (k >= 0 && !main_row && !cur) {
 #pragma unroll
         for (int q : {4, 5, 6, 8, 9, 10}) cf[(G_GRAD + q) * n + i] = f32(C(p, F_GRAD + q, i));
         const V3<double> dgc = C3(p, F_GC, i) - C3(p, F_LOC, i);
@@ -100,7 +103,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_predict32(KP p) {
         // the gradient rows the source reads: d(rho), the velocity divergence, d(P)
         float gr[15];
 #pragma unroll
-        for (int q : {0, 1, 2, 3, 7, 11, 12, 13, 14}) gr[q] = f32(C(p, F_GRAD + q, i));
+        for (int q : {0, 1, 2, 3, 7, 11, 12, 13, 14}) gr[q] = cur ? G(p, G_GRAD + q, i) : f32(C(p, F_GRAD + q, i));
         const V3<float> vr = f32v(C3(p, F_VREL, i));
         const Gas<float> g = gas_t<float>(p);
         const float rho_inv = 1.f / w.q[0];
@@ -124,8 +127,10 @@ __global__ void __launch_bounds__(kMaxBlock) k_predict32(KP p) {
             cf[(G_EXTRAP + q) * n + i] = f32(ex.q[q]);
             cf[(G_SRC + q) * n + i] = live ? src.q[q] : 0.f;
         }
+        if (!cur) {
 #pragma unroll
-        for (int q : {0, 1, 2, 3, 7, 11, 12, 13, 14}) cf[(G_GRAD + q) * n + i] = gr[q];
+            for (int q : {0, 1, 2, 3, 7, 11, 12, 13, 14}) cf[(G_GRAD + q) * n + i] = gr[q];
+        }
         cf[G_CS * n + i] = live ? g.sound_speed(w.q[4], rho_inv) : 0.f;
     }
     inst_count(p, k, act, CNT_CELLS);
@@ -547,6 +552,24 @@ __device__ __forceinline__ void gradients32_cell(const KP& p, int i) {
             }
             V3<double> cen = C3(p, F_CEN, i);
             W3(p, F_GC, i, cen);
+            if (p.cf_fresh) {
+                // the FP32 copies next predict would make from these rows; on a
+                // fixed mesh the timestep sets the mesh velocity to zero
+                const size_t n = (size_t)p.n;
+#pragma unroll
+                for (int q = 0; q < 5; q++) {
+                    p.cf[(G_GRAD + 3 * q + 0) * n + i] = gr[q].x;
+                    p.cf[(G_GRAD + 3 * q + 1) * n + i] = gr[q].y;
+                    p.cf[(G_GRAD + 3 * q + 2) * n + i] = gr[q].z;
+                }
+                const V3<double> dgc = cen - C3(p, F_LOC, i);
+                p.cf[(G_DGC + 0) * n + i] = f32(dgc.x);
+                p.cf[(G_DGC + 1) * n + i] = f32(dgc.y);
+                p.cf[(G_DGC + 2) * n + i] = f32(dgc.z);
+#pragma unroll
+                for (int a = 0; a < 3; a++) p.cf[(G_V + a) * n + i] = 0.f;
+                p.cf_fresh[i] = 1;
+            }
           } else {
             // no gradient stage: the stored gradients (velocity rows) feed the timestep
 #pragma unroll
