@@ -296,6 +296,8 @@ def run_ours(args):
         import torch.distributed as dist
 
         dist.init_process_group("nccl")
+    from hydro_rs_gb300 import ics
+
     problem, mesh_s = _problem(args.nx, args.workload)
     nf, nc = problem.mesh.n_faces, problem.mesh.n_cells
     stream = torch.cuda.Stream()
@@ -303,6 +305,7 @@ def run_ours(args):
 
     sims = {}
     batch = problem.extra.get("cell_offsets") is not None
+    hier = not batch and not problem.params.sync_all  # hierarchical steps of one simulation
     tuned = {}
     ctx_s = {}
     for prec in (1, 0):
@@ -504,8 +507,11 @@ def run_ours(args):
                        ", one pinned host block in the device field order, wall clock, bytes as counted "
                        "by the library"},
         # per step, both forms timed: over all cells k_predict32 / k_predict, face, update, gradients,
-        # limiter (5 + 5); hierarchical steps add k_compact to both and k_prep32 to the FP32 form
-        "gpu_launches": args.steps * ((5 + 5) + (3 if (not batch and not problem.params.sync_all) else 0)),
+        # limiter (5 + 5); the plain form's exact solver adds k_face_brent; hierarchical steps add
+        # k_compact to both and k_prep32 to the FP32 form, and each form's timed region ends with
+        # one k_extrap_flush
+        "gpu_launches": args.steps * ((5 + 5) + (1 if problem.params.riemann == ics.EXACT else 0) +
+                                      (3 if hier else 0)) + (2 if hier else 0),
         "clocks": clocks,
     }
     print(json.dumps(line))
