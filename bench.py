@@ -270,7 +270,7 @@ def face_stage_kernels(prec, all_cells):
 # DRAM bytes (read + write) per launch of the face stage from ncu captures at
 # the bench sizes (cold caches, ncu's default cache control): the committed
 # summaries in profiles/ give the commands.  Keyed by (workload, nx, form).
-TRAFFIC = {("kh2d", 256, 1): 26_908_928, ("kh2d", 256, 0): 40_718_080}  # profiles/face_stage_traffic_kh256.txt
+TRAFFIC = {("kh2d", 256, 1): 26_891_008, ("kh2d", 256, 0): 43_228_672}  # profiles/face_stage_traffic_kh256.txt
 
 
 def _face_kernel_ms(sim, steps):
