@@ -89,23 +89,25 @@ __global__ void __launch_bounds__(kMaxBlock) k_predict(KP p) {
     int k = i < p.n ? inst_of(p, i) : -1;
     if (k >= 0 && p.tl[k].done) k = -1;  // a finished simulation of a batch is left untouched
     if (k >= 0) {
-        double dt;
-        if (p.stage) {
-            dt = p.stage_dt;
-        } else {
-            unsigned long long tc = p.tl[k].ti_current, to = p.tl[k].ti_old;
-            dt = (double)(tc - to) * tbase(p, k);  // TimestepInfo::dt_from_dti
+        unsigned long long tc = 0, to = 0;
+        if (!p.stage) {
+            tc = p.tl[k].ti_current;
+            to = p.tl[k].ti_old;
             act = p.timebin[i] <= max_active_bin_bits(tc);
             p.active[i] = act;
         }
+        // TimestepInfo::dt_from_dti; formed only where it is used, as the FP64
+        // conversion and product cost every cell a hierarchical step defers
+        auto step_dt = [&]() { return p.stage ? p.stage_dt : (double)(tc - to) * tbase(p, k); };
         // hierarchical steps: this step's number, for the deferred extrapolations
         const bool lazy = p.extrap_step != nullptr && !p.stage;
         const unsigned int s = lazy ? (unsigned int)p.tl[k].steps : 0u;
-        if (lazy && i == 0) p.dt_log[s % kDtLog] = dt;
+        if (lazy && i == 0) p.dt_log[s % kDtLog] = step_dt();
         const bool fresh = !p.stage && !p.stale_all && p.fresh[i];
         if (lazy && fresh && !act && s % (kDtLog / 2) != 0) {
             // deferred (extrap_catch_up)
         } else if (fresh) {
+            const double dt = step_dt();
             // prim, grad and v_rel are unchanged since this cell's source row was
             // written (it was not active, nothing was uploaded): the same bits
             if (lazy) extrap_catch_up(p, i, s);
@@ -114,6 +116,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_predict(KP p) {
             else W5(p, F_EXTRAP, i, ex + st_zero<double>());
             if (lazy) p.extrap_step[i] = s + 1;
         } else {
+            const double dt = step_dt();
             if (lazy) extrap_catch_up(p, i, s);
             St<double> prim = C5(p, F_PRIM, i);
             double rho_inv = 1. / prim.q[0];
