@@ -1041,14 +1041,14 @@ int mvmm_step_cells(mvmm_ctx* c, const mvmm_cells* in, mvmm_cells* out, uint64_t
     CUDA_TRY(cudaStreamWaitEvent(s2, c->ev_pred, 0));
     // the FP32 face geometry follows the uploaded positions and centroids, on a
     // stream of its own while predict runs (predict does not read it)
-    const bool geo_side = c->prm.precision == MVMM_PRECISION_FP32FACE;
-    if (geo_side) {
+    const bool fp32_geom = c->prm.precision == MVMM_PRECISION_FP32FACE;
+    if (fp32_geom) {
         CUDA_TRY(cudaStreamWaitEvent(c->geo_side, c->ev_pred, 0));
         update_geom32(c, make_kp(c, 0, 7), c->geo_side);
         CUDA_TRY(cudaEventRecord(c->ev_geo, c->geo_side));
     }
     up.overlap = true;
-    up.snapshot = false;  // taken on the device once the rows have landed (a short kernel)
+    up.snapshot = false;  // taken on the device once the rows have landed (below)
     rc = copy_cells(c, in, kRowsLateIn, false, cudaMemcpyHostToDevice, s2, up);
     if (rc) return rc;
     // their snapshot: with every cell updated every step the update kernel
@@ -1062,7 +1062,7 @@ int mvmm_step_cells(mvmm_ctx* c, const mvmm_cells* in, mvmm_cells* out, uint64_t
     StepHooks h;
     h.stale_all = true;
     if (c->prm.sync_all) h.snap_late = c->snap;
-    h.wait_before_face = geo_side ? c->ev_geo : nullptr;
+    h.wait_before_face = fp32_geom ? c->ev_geo : nullptr;
     h.wait_before_update = c->ev_in;
     h.after_update = c->ev_upd;
     h.after_gradients = c->ev_grad;
