@@ -112,3 +112,21 @@ def test_max_active_bin_closed_form():
     cases += [int(x) << int(s) for x, s in zip(rng.integers(1, 1 << 20, 300), rng.integers(0, 44, 300))]
     for ti in cases:
         assert closed(ti) == O.get_max_active_bin(ti), ti
+
+
+def test_cells_pointer_struct_follows_the_arrays():
+    """Cells.cview keeps its C struct of pointers while the same arrays are in
+    place, and rebuilds it when an array is replaced or n changes."""
+    from hydro_rs_gb300.layout import CELL_ROWS, Cells
+    n = 64
+    c = Cells.packed(n, np.zeros(CELL_ROWS * n), np.zeros(n, dtype=np.int8))
+    a = c.cview()
+    assert c.cview() is a
+    assert a.prim == c.prim.ctypes.data and a.timebin == c.timebin.ctypes.data
+    c.arrays["prim"] = np.ones((5, n))
+    b = c.cview()
+    assert b is not a and b.prim == c.prim.ctypes.data and b.cons == a.cons
+    c.arrays["timebin"] = np.zeros(n, dtype=np.int8)
+    assert c.cview().timebin == c.timebin.ctypes.data
+    d = c.copy()
+    assert d.cview().prim == d.prim.ctypes.data != c.prim.ctypes.data
