@@ -492,18 +492,6 @@ __global__ void __launch_bounds__(kMaxBlock) k_extrap_flush(KP p, int reset) {
 
 // ---------------------------------------------------- cons -> primitive --
 // Particle::convert_conserved_to_primitive (part.rs:219-261)
-// 1/x for a positive normal x within 2^+-100: an FP32 seed (converted on the
-// integer pipe) and two Newton steps in FP64, within an ulp of the quotient.
-// The FP32-face form's conserved -> primitive uses it in place of two IEEE
-// divisions (the FP64 pipe is this form's busiest in the update).
-__device__ __forceinline__ bool recip64(double x, double& r) {
-    const int e = (int)((unsigned int)__double2hiint(x) >> 20) & 0x7ff;  // biased exponent (sign bit 0)
-    if (!(gt0_64(x) && e > 1023 - 100 && e < 1023 + 100)) return false;
-    r = bitconv::to_f64(__frcp_rn(bitconv::to_f32_rn(x)));
-    r = fma(r, fma(-x, r, 1.0), r);
-    r = fma(r, fma(-x, r, 1.0), r);
-    return true;
-}
 __device__ __forceinline__ void c2p(const KP& p, int i, const St<double>& cons, unsigned int* err) {
     const Gas<double> g = gas(p);
     if (!ge0_64(cons.q[0])) *err |= 1u << 2;
@@ -513,14 +501,8 @@ __device__ __forceinline__ void c2p(const KP& p, int i, const St<double>& cons, 
         if (!is_zero64(cons.q[4])) *err |= 1u << 3;
         prim = st_zero<double>();
     } else if (gt0_64(cons.q[0])) {  // State<Primitive>::from_conserved (physical_quantities.rs:213-226)
-        const double vol = C(p, F_VOL, i);
-        double m_inv, density, v_inv;
-        if (p.fp32 && recip64(cons.q[0], m_inv) && recip64(vol, v_inv)) {
-            density = cons.q[0] * v_inv;
-        } else {
-            m_inv = 1. / cons.q[0];
-            density = cons.q[0] / vol;
-        }
+        double m_inv = 1. / cons.q[0];
+        double density = cons.q[0] / C(p, F_VOL, i);
         V3<double> velocity = m_inv * vel(cons);
         double thermal = cons.q[4] - 0.5 * len2(vel(cons)) * m_inv;
         double u = thermal * m_inv;
@@ -642,17 +624,10 @@ __device__ __forceinline__ void update_finish(const KP& p, int i, int k, bool ac
         if (lt0_64(cons.q[4])) cons = st_zero<double>();
         facc = st_zero<double>();
         // kick2 (runner/hydrodynamics.rs:51-57): Particle::grav_kick with a zero
-        // acceleration adds +0 to the momentum (part.rs:303-312).  x + 0 is x
-        // except that -0 becomes +0 (and a NaN is quieted); the FP32-face form
-        // makes that change on the bit pattern, off the FP64 pipe
-        for (int a = 1; a < 4; a++) {
-            if (p.fp32) {
-                const long long b = __double_as_longlong(cons.q[a]);
-                cons.q[a] = b == (long long)0x8000000000000000ull ? 0. : cons.q[a];
-            } else {
-                cons.q[a] = cons.q[a] + 0.;
-            }
-        }
+        // acceleration adds +0 to the momentum (part.rs:303-312)
+        cons.q[1] = cons.q[1] + 0.;
+        cons.q[2] = cons.q[2] + 0.;
+        cons.q[3] = cons.q[3] + 0.;
         W5(p, F_CONS, i, cons);
         W(p, F_MSV, i, msv);
         W(p, F_MAOR, i, maor);
