@@ -620,7 +620,7 @@ def _serve_accuracy(srv, reqs, check_oracle: bool, n_check: int = 3):
 
 
 def run_moving(args):
-    """Moving mesh (drift + per-step host Voronoi + re-upload): each
+    """Moving mesh (drift, a host Voronoi build every step, re-upload): each
     step drifts the generators on the device, reads them back, rebuilds the
     Voronoi mesh on the host, uploads it and steps.  `value` is active-face
     updates per second of device step time (CUDA events on the context's
