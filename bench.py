@@ -7,11 +7,14 @@ Riemann solver, gamma = 5/3, all cells active every step.  Inputs are seeded
 synthetic data of that shape; the working set (~40-70 MB) is below the L2 size,
 so L2 is flushed (256 MB write) before every timed step.
 
-Headline ``value``: the FP32-face / FP64-accumulate form, device-resident.
-The line also carries the plain FP64 form, the L1 density error of the FP32
-form against the plain FP64 result, an end-to-end number through the C ABI
-with host buffers (copies inside the timed region), the roofline of the face
-kernel, and the CPU oracle timed on the host cores.
+Headline ``value``: the plain FP64 drop-in (the reference's arithmetic, the
+same configuration the reference arm runs), device-resident; ``e2e`` the same
+through the C ABI with host buffers (copies inside the timed region).  The
+line also carries the roofline of the face stage (HBM, and FP64 against a
+DGEMM measured here), the FP32-face / FP64-accumulate form under
+``fp32_face`` (its throughput, end-to-end number, roofline and L1 density
+error against the plain FP64 result), and the CPU oracle timed on the host
+cores.
 
 ``--impl reference`` times the CPU restatement of the reference (the oracle,
 OpenMP over all host cores): the Rust reference cannot be built here (no Rust
@@ -36,6 +39,7 @@ METRIC = "active-face updates/s"
 UNIT = "faces/s"
 NX = 256
 L2_FLUSH_BYTES = 256 << 20
+PRECISION_FP64 = "fp64 (the reference's arithmetic: the plain drop-in form)"
 
 
 def _dist():
@@ -261,10 +265,31 @@ FP64_FLOP_PER_FACE = {("kh2d", 256): 1610}
 FP64_DFMA_PER_SM_CLK = 2  # GB300: FP64 at 1/64 of the FP32 rate
 
 
-def face_stage_kernels(prec, all_cells):
+def face_stage_kernels(prec, all_cells, riemann=None):
     if prec == 0:
-        return "k_face_flux"
+        return "k_face_flux + k_face_brent" if riemann == 1 else "k_face_flux"
     return "k_face_flux32" if all_cells else "k_prep32 + k_face_flux32"
+
+
+def _fp64_peak(torch):
+    """FP64 throughput of this GPU measured with cuBLAS DGEMM (TFLOP/s)."""
+    try:
+        n = 4096
+        a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+        b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+        torch.matmul(a, b)
+        best = None
+        for _ in range(5):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            torch.matmul(a, b)
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+            best = ms if best is None else min(best, ms)
+        return 2.0 * n ** 3 / (best * 1e-3) / 1e12
+    except Exception:
+        return None
 
 
 # DRAM bytes (read + write) per launch of the face stage from ncu captures at
@@ -373,45 +398,46 @@ def run_ours(args):
         nca[prec] = (st1["active_cells"] - st0["active_cells"]) / k_prof  # active cells per profiled step
 
     # end-to-end through the C ABI with pinned host buffers: one pinned block in
-    # the device's field order, stepped in place
-    pinned = (torch.empty(CELL_ROWS * nc, dtype=torch.float64, pin_memory=True),
-              torch.empty(nc, dtype=torch.int8, pin_memory=True))
-    cells = Cells.packed(nc, pinned[0].numpy(), pinned[1].numpy())
-    sim = sims[1]
-    sim.state(cells)
+    # the device's field order, stepped in place; both forms
+    def e2e_measure(sim):
+        pinned = (torch.empty(CELL_ROWS * nc, dtype=torch.float64, pin_memory=True),
+                  torch.empty(nc, dtype=torch.int8, pin_memory=True))
+        cells = Cells.packed(nc, pinned[0].numpy(), pinned[1].numpy())
+        sim.state(cells)
 
-    def e2e_step():
-        if batch:
-            sim.upload(cells)
-            try:
-                sim.step()
-            except G.MvmmError as e:
-                if e.code != -3:
-                    raise
-            sim.state(cells)
-        else:
-            sim.step_cells(cells)  # upload + step + download in one C call
+        def e2e_step():
+            if batch:
+                sim.upload(cells)
+                try:
+                    sim.step()
+                except G.MvmmError as e:
+                    if e.code != -3:
+                        raise
+                sim.state(cells)
+            else:
+                sim.step_cells(cells)  # upload + step + download in one C call
 
-    # warm-up: the first call creates the copy stream and the snapshot block, and
-    # the first few run slower while the host block's pages settle
-    for _ in range(3 if batch else 10):
-        e2e_step()
-    e2e_steps = 10 if batch else 50  # a fixed sample (a batch moves ~1 GB per call), whatever --steps is
-    st0 = sim.stats()
-    torch.cuda.synchronize()
-    barrier()
-    t0 = time.perf_counter()
-    f0 = sim.active_faces
-    for _ in range(e2e_steps):
-        e2e_step()
-    e2e_s = time.perf_counter() - t0
-    barrier()
-    e2e_faces = sim.active_faces - f0
-    st1 = sim.stats()
-    # bytes the library moved between the host block and the device (counted by it)
-    h2d_step = (st1["host_bytes_in"] - st0["host_bytes_in"]) / e2e_steps
-    d2h_step = (st1["host_bytes_out"] - st0["host_bytes_out"]) / e2e_steps
-    bytes_cells = cells.nbytes()
+        # warm-up: the first call creates the copy stream and the snapshot block, and
+        # the first few run slower while the host block's pages settle
+        for _ in range(3 if batch else 10):
+            e2e_step()
+        n_steps = 10 if batch else 50  # a fixed sample (a batch moves ~1 GB per call), whatever --steps is
+        st0 = sim.stats()
+        torch.cuda.synchronize()
+        barrier()
+        t0 = time.perf_counter()
+        f0 = sim.active_faces
+        for _ in range(n_steps):
+            e2e_step()
+        secs = time.perf_counter() - t0
+        barrier()
+        st1 = sim.stats()
+        # bytes the library moved between the host block and the device (counted by it)
+        return {"seconds": secs, "faces": sim.active_faces - f0, "steps": n_steps,
+                "h2d": (st1["host_bytes_in"] - st0["host_bytes_in"]) / n_steps,
+                "d2h": (st1["host_bytes_out"] - st0["host_bytes_out"]) / n_steps, "bytes_cells": cells.nbytes()}
+
+    e2e = {prec: e2e_measure(sims[prec]) for prec in (0, 1)}
 
     st32 = sims[1].stats()
     fallback32 = {"faces": st32["fp64_fallback_faces"], "of_active_faces": st32["active_faces"]}
@@ -440,42 +466,58 @@ def run_ours(args):
                 return t.tolist()
             return f
 
-        (ms32, ms64, e2e_s), (faces32, faces64, e2e_faces) = aggregate_replicas(
-            [ms32, ms64, e2e_s], [faces32, faces64, e2e_faces], red(dist.ReduceOp.MAX), red(dist.ReduceOp.SUM))
+        (ms32, ms64, e2e[0]["seconds"], e2e[1]["seconds"]), (faces32, faces64, e2e[0]["faces"], e2e[1]["faces"]) = \
+            aggregate_replicas([ms32, ms64, e2e[0]["seconds"], e2e[1]["seconds"]],
+                               [faces32, faces64, e2e[0]["faces"], e2e[1]["faces"]],
+                               red(dist.ReduceOp.MAX), red(dist.ReduceOp.SUM))
     if rank != 0:
         return
     peak, peak_kind = _peaks()
+    all_cells = batch or problem.params.sync_all
+
+    def kernel_ms(prec):
+        # per-launch milliseconds of each step kernel from event nodes placed
+        # around it in the step graph, less the interval of an empty event pair
+        # (the "end" slot, which holds no kernel: the step's bookkeeping runs in
+        # the limiter's last block)
+        pr = prof[prec]
+        ev_ms = pr["end"][0] / max(pr["end"][1], 1)
+        out = {k: max(v[0] / max(v[1], 1) - ev_ms, 0.0) for k, v in pr.items() if k != "end"}
+        return out, ev_ms
 
     def roof(prec):
-        ms, n = prof[prec]["face_flux"]
-        ms_launch = ms / max(n, 1)
-        all_cells = batch or problem.params.sync_all
+        kms, ev_ms = kernel_ms(prec)
+        ms_launch = kms["face_flux"]
         bytes_launch = face_stage_bytes(prec, nc, nfa[prec], all_cells)
         ach = bytes_launch / (ms_launch * 1e-3) / 1e9
         traffic = TRAFFIC.get((args.workload, args.nx, prec))
         return {"bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(ach / peak, 4), "traffic": traffic,
-                "kernel": face_stage_kernels(prec, all_cells),
+                "kernel": face_stage_kernels(prec, all_cells, problem.params.riemann),
                 "kernel_ms": round(ms_launch, 4), "algorithmic_bytes_per_launch": int(bytes_launch),
                 "active_faces_per_launch": nfa[prec],
                 "peak_kind": peak_kind, "note": "of measured" if peak_kind == "measured" else "of fallback",
-                "step_kernel_ms": {k: round(v[0] / max(v[1], 1), 4) for k, v in prof[prec].items()}}
+                "kernel_ms_source": "CUDA events recorded as graph nodes around each stage of the step graph on "
+                                    "the context stream, minus the interval of an empty event pair "
+                                    f"({ev_ms:.4f} ms)",
+                "step_kernel_ms": {k: round(v, 4) for k, v in kms.items()}}
+
+    fp64_peak = _fp64_peak(torch)
 
     def fp64_roof():
-        # the plain face kernel against the FP64 pipe: flop per face (measured once
-        # by ncu at this size) x active faces / the kernel's event time, against
-        # 2 DFMA (4 flop) per clock per SM at the SM clock sampled during the run
+        # the plain face stage against the FP64 pipe: flop per face (measured once
+        # by ncu at this size) x active faces / the stage's event time, against the
+        # FP64 throughput measured here (cuBLAS DGEMM)
         fpf = FP64_FLOP_PER_FACE.get((args.workload, args.nx))
-        if fpf is None:
+        if fpf is None or fp64_peak is None:
             return None
-        ms, n = prof[0]["face_flux"]
-        ach = fpf * nfa[0] / (ms / max(n, 1) * 1e-3) / 1e12
-        sm_mhz = (clocks or {}).get("sm_mhz") or 2070.0
-        peak64 = torch.cuda.get_device_properties(dev).multi_processor_count * FP64_DFMA_PER_SM_CLK * 2 * sm_mhz * 1e6 / 1e12
-        return {"bound": "fp64", "achieved": round(ach, 4), "peak": round(peak64, 3), "unit": "TFLOP/s",
-                "frac": round(ach / peak64, 4), "flop_per_face": fpf, "kernel": "k_face_flux",
-                "note": "FP64 pipe 76-79% busy in ncu: warps with few active lanes (the Brent iteration) and "
-                        "non-flop FP64 work hold it"}
+        ms = kernel_ms(0)[0]["face_flux"]
+        ach = fpf * nfa[0] / (ms * 1e-3) / 1e12
+        return {"bound": "fp64", "achieved": round(ach, 4), "peak": round(fp64_peak, 3), "unit": "TFLOP/s",
+                "frac": round(ach / fp64_peak, 4), "flop_per_face": fpf, "kernel": face_stage_kernels(0, all_cells,
+                                                                                                problem.params.riemann),
+                "peak_kind": "measured here: torch.matmul float64 4096^3 (cuBLAS DGEMM), best of 5",
+                "note": "flop per face from one ncu capture of the face stage (profiles/)"}
 
     def step_roof(prec, ms_step):
         b = STEP_BYTES_FACE * nfa[prec] + STEP_BYTES_CELL[prec] * nca[prec]
@@ -486,41 +528,48 @@ def run_ours(args):
                 "note": "whole step (all kernels) over ms_per_step; " +
                         ("of measured" if peak_kind == "measured" else "of fallback")}
 
-    cpu = _cpu_sample(problem, WORKLOADS[args.workload].format(n=args.nx)) if (ws == 1 and not args.no_cpu) else None
-    value = faces32 / (ms32 * 1e-3)
-    line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": ms32 / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32-face/f64-accumulate", "data": DATA.get(args.workload, "synthetic, seeded"),
-        "config": {"workload": WORKLOADS[args.workload].format(n=args.nx),
-                   "cells": nc, "faces": nf, "precision": "fp32_face",
-                   "l2": "flushed (256 MB write) before each timed step", "parallelism": f"replicas x{ws}",
-                   "mesh_build_s": round(mesh_s, 3),
-                   "ctx_create_and_upload_s": {"fp32_face": round(ctx_s[1], 4), "fp64": round(ctx_s[0], 4)},
-                   "blocks_face_cell": {"fp32_face": tuned.get(1), "fp64": tuned.get(0)}},
-        "l1_density_err_vs_fp64": l1, "l1_same_time": same_time, "l1_alignment_steps": aligned,
-        "fp64_fallback_faces": fallback32,
-        "active_face_fraction": faces32 / (args.steps * nf * ws),
-        "batch": batch_info,
-        "plain_fp64": {"value": faces64 / (ms64 * 1e-3), "unit": UNIT, "ms_per_step": ms64 / args.steps,
-                       "roofline": roof(0), "step_roofline": step_roof(0, ms64 / args.steps),
-                       "fp64_roofline": fp64_roof()},
-        "roofline": roof(1),
-        "step_roofline": step_roof(1, ms32 / args.steps),
-        "cpu_baseline": cpu,
-        "e2e": {"value": e2e_faces / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d_step),
-                "d2h_bytes_per_step": int(d2h_step), "host_block_bytes": bytes_cells, "steps": e2e_steps,
+    def e2e_line(prec):
+        e = e2e[prec]
+        return {"value": e["faces"] / e["seconds"], "unit": UNIT, "h2d_bytes_per_step": int(e["h2d"]),
+                "d2h_bytes_per_step": int(e["d2h"]), "host_block_bytes": e["bytes_cells"], "steps": e["steps"],
                 "how": ("mvmm_upload_cells + mvmm_step + mvmm_download_cells per step" if batch else
                         "mvmm_step_cells per step (upload, step and download in one C call; the step's "
                         "state comes back in place, only the 8 KB chunks it changed)") +
                        ", one pinned host block in the device field order, wall clock, bytes as counted "
-                       "by the library"},
-        # per step, both forms timed: over all cells k_predict32 / k_predict, face, update, gradients,
+                       "by the library"}
+
+    cpu = _cpu_sample(problem, WORKLOADS[args.workload].format(n=args.nx)) if (ws == 1 and not args.no_cpu) else None
+    value64 = faces64 / (ms64 * 1e-3)
+    value32 = faces32 / (ms32 * 1e-3)
+    exact = problem.params.riemann == ics.EXACT
+    line = {
+        "metric": METRIC, "value": value64, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms64 / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": DATA.get(args.workload, "synthetic, seeded"),
+        "config": {"workload": WORKLOADS[args.workload].format(n=args.nx),
+                   "cells": nc, "faces": nf, "precision": PRECISION_FP64,
+                   "l2": "flushed (256 MB write) before each timed step", "parallelism": f"replicas x{ws}",
+                   "mesh_build_s": round(mesh_s, 3),
+                   "ctx_create_and_upload_s": {"fp64": round(ctx_s[0], 4), "fp32_face": round(ctx_s[1], 4)},
+                   "blocks_face_cell": {"fp64": tuned.get(0), "fp32_face": tuned.get(1)}},
+        "active_face_fraction": faces64 / (args.steps * nf * ws),
+        "batch": batch_info,
+        "roofline": roof(0),
+        "fp64_roofline": fp64_roof(),
+        "step_roofline": step_roof(0, ms64 / args.steps),
+        "e2e": e2e_line(0),
+        "fp32_face": {"value": value32, "unit": UNIT, "ms_per_step": ms32 / args.steps,
+                      "dtype": "f32-face/f64-accumulate", "speedup_vs_fp64": value32 / value64,
+                      "e2e": e2e_line(1),
+                      "l1_density_err_vs_fp64": l1, "l1_same_time": same_time, "l1_alignment_steps": aligned,
+                      "fp64_fallback_faces": fallback32,
+                      "roofline": roof(1), "step_roofline": step_roof(1, ms32 / args.steps)},
+        "cpu_baseline": cpu,
+        # per step, both forms timed: over all cells k_predict / k_predict32, face, update, gradients,
         # limiter (5 + 5); the plain form's exact solver adds k_face_brent; hierarchical steps add
         # k_compact to both and k_prep32 to the FP32 form, and each form's timed region ends with
         # one k_extrap_flush
-        "gpu_launches": args.steps * ((5 + 5) + (1 if problem.params.riemann == ics.EXACT else 0) +
-                                      (3 if hier else 0)) + (2 if hier else 0),
+        "gpu_launches": args.steps * ((5 + 5) + (1 if exact else 0) + (3 if hier else 0)) + (2 if hier else 0),
         "clocks": clocks,
     }
     print(json.dumps(line))
@@ -738,7 +787,7 @@ def run_reference(args):
         "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded jittered lattice, shear-layer ICs)",
         "config": {"workload": WORKLOADS[args.workload].format(n=args.nx), "cells": problem.mesh.n_cells,
-                   "faces": problem.mesh.n_faces},
+                   "faces": problem.mesh.n_faces, "precision": PRECISION_FP64},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{args.steps} steps after {2 + args.warmup} warm-up steps; the Rust reference "
                                    "cannot be built here (no cargo/rustc), the C restatement runs instead"},

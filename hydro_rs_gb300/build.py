@@ -31,7 +31,7 @@ CU_SOURCES = {
     "mvmm_api.cu": [],
     "noalloc.cu": ["-fmad=false"],
 }
-HEADERS = ["mvmm_device.cuh", "mvmm_internal.h", "mvmm_cellops.cuh", "bitconv.cuh"]
+HEADERS = ["mvmm_device.cuh", "mvmm_internal.h", "mvmm_cellops.cuh", "bitconv.cuh", "face64.cuh"]
 
 
 def _nvcc() -> str:

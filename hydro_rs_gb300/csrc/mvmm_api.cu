@@ -50,6 +50,10 @@ int fail(int code, const std::string& msg) {
 constexpr unsigned long long kMax = 1ull << 57;
 }  // namespace
 
+namespace mvmm {
+int report_error(int code, const char* msg) { return fail(code, msg ? msg : ""); }
+}  // namespace mvmm
+
 struct mvmm_ctx {
     mvmm_params prm{};
     int n = 0, nf = 0;
@@ -198,6 +202,7 @@ KP make_kp(mvmm_ctx* c, int stage, int flux_rows) {
     p.cell_list = c->cell_list;
     p.face_list = c->face_list;
     p.blk_face = c->blk_face;
+    p.n_sms = c->n_sms > 0 ? c->n_sms : 1;
     p.blk_cell = c->blk_cell;
     p.rsx = solver_settings(c->prm);
     const Gas<double> g = make_gas<double>(c->prm.gamma, c->prm.eos, c->prm.isothermal_internal_energy);

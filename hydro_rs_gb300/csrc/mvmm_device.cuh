@@ -49,6 +49,12 @@ __device__ __forceinline__ bool gt0_64(double x) {  // x > 0.
 __device__ __forceinline__ bool ge0_64(double x) { return !is_nan64(x) && (__double_as_longlong(x) >= 0 || mag64(x) == 0); }
 __device__ __forceinline__ float m_max(float a, float b) { return fmaxf(a, b); }
 
+// The active-face rule of compute_fluxes (euler_eqns_fvs.rs:35-45) for an
+// interior face: false where the face is skipped.
+__device__ __forceinline__ bool interior_face_active(bool la, bool ra, double dtl, double dtr) {
+    return !((!la && !ra) || (dtr < dtl && !ra) || (dtl < dtr && !la));
+}
+
 template <typename T>
 struct V3 {
     T x, y, z;
@@ -484,12 +490,41 @@ static __device__ __noinline__ double ex_brent(double lower, double upper, doubl
         } else {
             mflag = false;
         }
+        const bool bisected = mflag;
         fs = ex_f(s, l, r, vl, vr, g);
         d = c;
         c = b;
         fc = fb;
+        const bool b_kept = !(fa * fs < 0.);
         if (fa * fs < 0.) { b = s; fb = fs; } else { a = s; fa = fs; }
-        if (fabs(fa) < fabs(fb)) { t = a; a = b; b = t; t = fa; fa = fb; fb = t; }
+        const bool swapped = fabs(fa) < fabs(fb);
+        if (swapped) { t = a; a = b; b = t; t = fa; fa = fb; fb = t; }
+        // A bisection that left b in place (and so set c = b) starts a run in
+        // which every later iteration bisects too: with mflag set and c == b,
+        // the test |b - c| < tol (b + c) / 2 chooses the midpoint whatever the
+        // interpolant.  While each midpoint keeps fa's sign and does not
+        // undercut |fb|, b stays the answer and only a moves, so the run's
+        // midpoints follow from a and b alone.  They are formed without
+        // evaluating f, and f is evaluated at the last (closest to the root)
+        // only: f is increasing in p, so the earlier midpoints, farther from
+        // the root on a's side, have the same sign and a larger magnitude.
+        // Where that check fails the loop resumes as if the run had not been
+        // looked at.  Same iterates, same result, and about a quarter of the
+        // f evaluations where the guess lands above the root (the usual case
+        // for nearly uniform states, where the loop would otherwise bisect
+        // [0, p_guess] down to the tolerance, ~20 evaluations).
+        if (bisected && b_kept && !swapped) {
+            double a2 = a;
+            int k = 0;
+            while (fb != 0. && fabs(a2 - b) > tol * 0.5 * (a2 + b)) {
+                a2 = 0.5 * (a2 + b);
+                k++;
+            }
+            if (k > 0 && it + k <= 100 * max_iter) {
+                const double fl = ex_f(a2, l, r, vl, vr, g);
+                if (fl != 0. && !(fa * fl < 0.) && !(fabs(fl) < fabs(fb))) return b;
+            }
+        }
     }
     return b;
 }

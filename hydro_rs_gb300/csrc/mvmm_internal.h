@@ -146,6 +146,7 @@ struct KP {
     const double* inst_tb;   // per-instance time_base (nullptr: time_base)
     const double* inst_tbi;  // per-instance 1 / time_base (nullptr: time_base_inv)
     int blk_face, blk_cell;  // thread-block sizes (chosen by mvmm_autotune)
+    int n_sms;               // streaming multiprocessors of the context's device (grid sizing)
     GasK gk;                 // gas-law constants
     RSx rsx;                 // Riemann solver kind and its settings
     int godunov;             // 1: GodunovHydroRunner (no gradients), 0: OptimalOrderRunner
@@ -169,6 +170,10 @@ struct KP {
     int* cell_list;          // hierarchical steps: active cells and the cells next to an active face
     int* face_list;          // compacted active faces
 };
+
+// Sets the text mvmm_last_error() returns on this host thread and returns code
+// (implemented in mvmm_api.cu).
+int report_error(int code, const char* msg);
 
 // launchers (implemented in step_fp64.cu / step_fp32.cu)
 void launch_predict(const KP& p, cudaStream_t s);

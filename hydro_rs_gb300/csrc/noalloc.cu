@@ -10,13 +10,17 @@
 // intermediate, the per-face flux results, lives in the file-scope array
 // g_face_scratch below, sized for MVMM_NOALLOC_MAX_FACES faces.
 //
-// Arithmetic is the plain FP64 form (this file is compiled with -fmad=false),
-// so the result equals mvmm_compute_fluxes + mvmm_apply_fluxes +
-// mvmm_convert_conserved_to_primitive on a context.
+// The physics is the plain FP64 form the context kernels use (face64.cuh; this
+// file is compiled with -fmad=false), so the result equals
+// mvmm_compute_fluxes + mvmm_apply_fluxes + mvmm_convert_conserved_to_primitive
+// on a context.  Unlike a context, which validates the mesh on upload, the
+// caller's device arrays are checked by the kernels as they read them: an index
+// outside its array is skipped and reported as MVMM_ERR_BOUNDS.
 #include <mutex>
+#include <string>
 
 #include "../../include/mvmm_gpu.h"
-#include "mvmm_device.cuh"
+#include "face64.cuh"
 
 namespace mvmm {
 namespace {
@@ -47,146 +51,84 @@ __device__ __forceinline__ St<double> R5(const double* a, int n, int i) {
     return s;
 }
 __device__ __forceinline__ Gas<double> gas(const NA& p) { return make_gas<double>(p.gamma, p.eos, p.iso_u); }
-__device__ __forceinline__ double gdot(const NA& p, int i, int q, V3<double> dx) {
-    const double* g = p.c.grad;
-    int n = p.n;
-    return g[(3 * q) * n + i] * dx.x + g[(3 * q + 1) * n + i] * dx.y + g[(3 * q + 2) * n + i] * dx.z;
-}
-// time_extrapolations source (part.rs:134-149) and v_max sound speed, from the cell state
-__device__ __forceinline__ St<double> source(const NA& p, int i, const St<double>& prim) {
-    int n = p.n;
-    const double* g = p.c.grad;
-    V3<double> vr = R3(p.c.v_rel, n, i);
-    V3<double> g0 = v3(g[0 * n + i], g[1 * n + i], g[2 * n + i]);
-    V3<double> g4 = v3(g[12 * n + i], g[13 * n + i], g[14 * n + i]);
-    double div_v = g[3 * n + i] + g[7 * n + i] + g[11 * n + i];
-    double rho_inv = 1. / prim.q[0];
-    St<double> s;
-    s.q[0] = prim.q[0] * div_v + dot(vr, g0);
-    s.q[1] = vr.x * div_v + rho_inv * g4.x;
-    s.q[2] = vr.y * div_v + rho_inv * g4.y;
-    s.q[3] = vr.z * div_v + rho_inv * g4.z;
-    s.q[4] = p.gamma * prim.q[4] * div_v + dot(vr, g4);
-    return s;
-}
-__device__ __forceinline__ double vmax_c(const NA& p, const St<double>& prim) {
-    return prim.q[0] > 0. ? gas(p).sound_speed(prim.q[4], 1. / prim.q[0]) : 0.;
-}
-__device__ __forceinline__ St<double> reconstruct(const NA& p, int i, const St<double>& prim, V3<double> dx, double td) {
-    St<double> r;
-#pragma unroll
-    for (int q = 0; q < 5; q++) r.q[q] = (prim.q[q] + gdot(p, i, q, dx)) + p.c.extrap[q * p.n + i];
-    if (prim.q[0] > 0.) {
-        St<double> s = source(p, i, prim);
-#pragma unroll
-        for (int q = 0; q < 5; q++) r.q[q] = r.q[q] + td * s.q[q];
-    } else {
-#pragma unroll
-        for (int q = 0; q < 5; q++) r.q[q] = r.q[q] + 0.;
-    }
-    return r;
-}
 
-// flux_exchange (flux.rs:23-100)
-template <int SOLVER>
-__device__ void face_interior(const NA& p, int f, int l, int r, double dt, double out[kRows], unsigned int* err) {
-    const Gas<double> g = gas(p);
-    int n = p.n, nf = p.nf;
-    V3<double> fc = R3(p.m.centroid, nf, f);
-    V3<double> sh = R3(p.m.shift, nf, f);
-    V3<double> dx_left = fc - R3(p.c.gc, n, l);
-    V3<double> dx_right = (fc - R3(p.c.gc, n, r)) - sh;
-    double dx_gradients = len(dx_left - dx_right);
-    V3<double> dx_centroid = (R3(p.c.centroid, n, r) + sh) - R3(p.c.centroid, n, l);
-    V3<double> locl = R3(p.c.loc, n, l), locr = R3(p.c.loc, n, r);
-    V3<double> dx = (locr + sh) - locl;
-    St<double> pl = R5(p.c.prim, n, l), pr = R5(p.c.prim, n, r);
-    double v_max = 0. + vmax_c(p, pl);
-    v_max = v_max + vmax_c(p, pr);
-    v_max -= m_min(dot(vel(pr) - vel(pl), dx_centroid), 0.);
-    double td = -(-0.5 * dt);
-    St<double> ldash = reconstruct(p, l, pl, dx_left, td);
-    St<double> rdash = reconstruct(p, r, pr, dx_right, td);
-    St<double> prim_left = pairwise_limiter(pl, pr, ldash, len(dx_left) / dx_gradients);
-    St<double> prim_right = pairwise_limiter(pr, pl, rdash, len(dx_right) / dx_gradients);
-    V3<double> vl = R3(p.c.v, n, l), vr = R3(p.c.v, n, r);
-    V3<double> midpoint = 0.5 * ((locl + locr) + sh);
-    double fac = dot(vr - vl, fc - midpoint) / len2(dx);
-    V3<double> v_face = 0.5 * (vl + vr) - fac * dx;
-    V3<double> mvf = neg(v_face);
-    St<double> F = solve_for_flux<double, SOLVER>(boost(prim_left, mvf), boost(prim_right, mvf), v_face,
-                                                  R3(p.m.normal, nf, f), g, g, p.max_iter, err);
-    double area = p.m.area[f];
-    St<double> fluxes = area * F;
-#pragma unroll
-    for (int q = 0; q < 5; q++) out[q] = dt * fluxes.q[q];
-    out[5] = v_max;
-    out[6] = area / len(dx);
-}
-
-// flux_exchange_boundary (flux.rs:102-195)
-template <int SOLVER>
-__device__ void face_boundary(const NA& p, int f, int i, double out[kRows], unsigned int* err) {
-    const Gas<double> g = gas(p);
-    int n = p.n, nf = p.nf;
-    V3<double> fc = R3(p.m.centroid, nf, f);
-    V3<double> nn = R3(p.m.normal, nf, f);
-    V3<double> loc = R3(p.c.loc, n, i), cen = R3(p.c.centroid, n, i), gc = R3(p.c.gc, n, i);
-    V3<double> rloc = loc + (2. * dot(fc - loc, nn)) * nn;
-    V3<double> rcen = cen + (2. * dot(fc - cen, nn)) * nn;
-    V3<double> rgc = gc + (2. * dot(fc - gc, nn)) * nn;
-    V3<double> dx_face = fc - gc;
-    double dx_gradients = len(rgc - gc);
-    V3<double> dx_centroid = rcen - cen;
-    V3<double> dx = rloc - loc;
-    St<double> prim = R5(p.c.prim, n, i);
-    double v_max = 0. + vmax_c(p, prim);
-    double dt = p.c.dt[i];
-    St<double> dash = reconstruct(p, i, prim, dx_face, -(-0.5 * dt));
-    double dx_fac = len(dx_face) / dx_gradients;
-    St<double> bnd;
-    if (p.boundary == MVMM_BOUNDARY_REFLECTIVE) {
-        St<double> rprim = reflect(prim, nn);
-        dash = pairwise_limiter(prim, rprim, dash, dx_fac);
-        v_max -= m_min(dot(vel(rprim) - vel(prim), dx_centroid), 0.);
-        bnd = reflect(dash, nn);
-    } else if (p.boundary == MVMM_BOUNDARY_OPEN) {
-        dash = pairwise_limiter(prim, prim, dash, dx_fac);
-        bnd = dash;
-    } else {
-        St<double> vac = st_zero<double>();
-        dash = pairwise_limiter(prim, vac, dash, dx_fac);
-        v_max += m_min(dot(vel(prim), dx_centroid), 0.);
-        bnd = vac;
+// The face physics' view of the caller's arrays.  The derived face-stage
+// values a context keeps in rows written by predict (the time-extrapolation
+// source and the v_max sound speed) are formed here from the state, with the
+// same expressions.
+struct AccNA {
+    const NA& p;
+    __device__ __forceinline__ St<double> prim(int i) const { return R5(p.c.prim, p.n, i); }
+    __device__ __forceinline__ V3<double> gc(int i) const { return R3(p.c.gc, p.n, i); }
+    __device__ __forceinline__ V3<double> cen(int i) const { return R3(p.c.centroid, p.n, i); }
+    __device__ __forceinline__ V3<double> loc(int i) const { return R3(p.c.loc, p.n, i); }
+    __device__ __forceinline__ V3<double> v(int i) const { return R3(p.c.v, p.n, i); }
+    __device__ __forceinline__ double dt(int i) const { return p.c.dt[i]; }
+    __device__ __forceinline__ double cs(int i) const {
+        const double rho = p.c.prim[i];
+        return gt0_64(rho) ? gas(p).sound_speed(p.c.prim[4 * p.n + i], 1. / rho) : 0.;
     }
-    St<double> F = solve_for_flux<double, SOLVER>(dash, bnd, v3(0., 0., 0.), nn, g, g, p.max_iter, err);
-    double area = p.m.area[f];
-    St<double> fluxes = area * F;
-#pragma unroll
-    for (int q = 0; q < 5; q++) out[q] = dt * fluxes.q[q];
-    out[5] = v_max;
-    out[6] = area / len(dx);
-}
+    __device__ __forceinline__ double gdot(int i, int q, V3<double> dx) const {
+        const double* g = p.c.grad;
+        const int n = p.n;
+        return g[(3 * q) * n + i] * dx.x + g[(3 * q + 1) * n + i] * dx.y + g[(3 * q + 2) * n + i] * dx.z;
+    }
+    __device__ __forceinline__ double extrap(int i, int q) const { return p.c.extrap[q * p.n + i]; }
+    // Particle::time_extrapolations body before the -dt factor (part.rs:134-149)
+    __device__ __forceinline__ St<double> src(int i, const St<double>& prim) const {
+        const int n = p.n;
+        const double* g = p.c.grad;
+        V3<double> vr = R3(p.c.v_rel, n, i);
+        V3<double> g0 = v3(g[0 * n + i], g[1 * n + i], g[2 * n + i]);
+        V3<double> g4 = v3(g[12 * n + i], g[13 * n + i], g[14 * n + i]);
+        double div_v = g[3 * n + i] + g[7 * n + i] + g[11 * n + i];
+        double rho_inv = 1. / prim.q[0];
+        St<double> s;
+        s.q[0] = prim.q[0] * div_v + dot(vr, g0);
+        s.q[1] = vr.x * div_v + rho_inv * g4.x;
+        s.q[2] = vr.y * div_v + rho_inv * g4.y;
+        s.q[3] = vr.z * div_v + rho_inv * g4.z;
+        s.q[4] = p.gamma * prim.q[4] * div_v + dot(vr, g4);
+        return s;
+    }
+    __device__ __forceinline__ V3<double> fcen(int f) const { return R3(p.m.centroid, p.nf, f); }
+    __device__ __forceinline__ V3<double> shift(int f) const { return R3(p.m.shift, p.nf, f); }
+    __device__ __forceinline__ V3<double> normal(int f) const { return R3(p.m.normal, p.nf, f); }
+    __device__ __forceinline__ double area(int f) const { return p.m.area[f]; }
+    __device__ __forceinline__ int boundary() const { return p.boundary; }
+};
 
 // compute_fluxes (euler_eqns_fvs.rs:26-48) into the static scratch rows
 template <int SOLVER>
 __global__ void __launch_bounds__(kBlock) k_na_face(NA p) {
     int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= p.nf) return;
-    int l = p.m.left[f], r = p.m.right[f];
-    bool la = p.active[l] != 0;
-    double out[kRows] = {0., 0., 0., 0., 0., 0., 0.};
+    const int l = p.m.left[f], r = p.m.right[f];
+    FaceOut o = face_zero();
     unsigned int err = 0;
-    if (r >= 0) {
-        bool ra = p.active[r] != 0;
-        double dtl = p.c.dt[l], dtr = p.c.dt[r];
-        if (!((!la && !ra) || (dtr < dtl && !ra) || (dtl < dtr && !la)))
-            face_interior<SOLVER>(p, f, l, r, m_min(dtl, dtr), out, &err);
-    } else if (la) {
-        face_boundary<SOLVER>(p, f, l, out, &err);
+    if (l < 0 || l >= p.n || r >= p.n || r < -1 || (r < 0 && p.boundary == MVMM_BOUNDARY_PERIODIC)) {
+        err |= MVMM_ERR_BOUNDS;  // the face is skipped
+    } else {
+        const AccNA a{p};
+        const Gas<double> g = gas(p);
+        const bool la = p.active[l] != 0;
+        if (r >= 0) {
+            const bool ra = p.active[r] != 0;
+            const double dtl = p.c.dt[l], dtr = p.c.dt[r];
+            if (interior_face_active(la, ra, dtl, dtr)) {
+                const FacePre q = face_interior_pre(a, f, l, r, m_min(dtl, dtr));
+                o = face_finish(q, solve_for_flux<double, SOLVER>(q.l, q.r, q.iv, q.n, g, g, p.max_iter, &err));
+            }
+        } else if (la) {
+            const FacePre q = face_boundary_pre(a, f, l);
+            o = face_finish(q, solve_for_flux<double, SOLVER>(q.l, q.r, q.iv, q.n, g, g, p.max_iter, &err));
+        }
     }
+    const size_t nf = (size_t)p.nf;
 #pragma unroll
-    for (int q = 0; q < kRows; q++) p.scratch[(size_t)q * p.nf + f] = out[q];
+    for (int q = 0; q < 5; q++) p.scratch[q * nf + f] = o.fl.q[q];
+    p.scratch[5 * nf + f] = o.v_max;
+    p.scratch[6 * nf + f] = o.a_over_r;
     if (err && p.err) atomicOr(p.err, err);
 }
 
@@ -195,56 +137,42 @@ __global__ void __launch_bounds__(kBlock) k_na_face(NA p) {
 __global__ void __launch_bounds__(kBlock) k_na_update(NA p) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
-    int n = p.n;
-    size_t nf = (size_t)p.nf;
-    bool act = p.active[i] != 0;
+    const int n = p.n;
+    const size_t nf = (size_t)p.nf;
+    const bool act = p.active[i] != 0;
+    unsigned int err = 0;
     St<double> facc = R5(p.c.facc, n, i);
     double msv = p.c.max_signal_velocity[i], maor = p.c.max_a_over_r[i];
-    for (int k = p.m.csr_off[i]; k < p.m.csr_off[i + 1]; k++) {
-        int f = p.m.csr_face[k];
-        St<double> x;
+    // the cell's CSR range must lie inside the caller's csr_face[csr_off[n]]
+    const int k0 = p.m.csr_off[i], k1 = p.m.csr_off[i + 1], kend = p.m.csr_off[n];
+    if (k0 < 0 || k1 < k0 || k1 > kend) {
+        err |= MVMM_ERR_BOUNDS;
+    } else {
+        for (int k = k0; k < k1; k++) {
+            const int f = p.m.csr_face[k];
+            if (f < 0 || f >= p.nf) {
+                err |= MVMM_ERR_BOUNDS;
+                continue;
+            }
+            St<double> x;
 #pragma unroll
-        for (int q = 0; q < 5; q++) x.q[q] = p.scratch[q * nf + f];
-        if (p.m.left[f] == i) facc = facc - x;
-        else facc = facc + x;
-        if (act) {
-            msv = m_max(p.scratch[5 * nf + f], msv);
-            maor = m_max(maor, p.scratch[6 * nf + f]);
+            for (int q = 0; q < 5; q++) x.q[q] = p.scratch[q * nf + f];
+            if (p.m.left[f] == i) facc = facc - x;  // update_fluxes_left (part.rs:160-167)
+            else facc = facc + x;                   // update_fluxes_right (part.rs:169-176)
+            if (act) {
+                msv = m_max(p.scratch[5 * nf + f], msv);
+                maor = m_max(maor, p.scratch[6 * nf + f]);
+            }
         }
     }
-    unsigned int err = 0;
     if (act) {
-        St<double> cons = R5(p.c.cons, n, i) + facc;
-        for (int q = 0; q < 5; q++)
-            if (!isfinite(cons.q[q])) err |= MVMM_ERR_NONFINITE;
-        if (cons.q[0] < 0.) cons = st_zero<double>();
-        if (cons.q[4] < 0.) cons = st_zero<double>();
+        const St<double> cons = apply_flux64(R5(p.c.cons, n, i), facc, &err);
         facc = st_zero<double>();
-        cons.q[1] = cons.q[1] + 0.;  // kick2 with zero acceleration
-        cons.q[2] = cons.q[2] + 0.;
-        cons.q[3] = cons.q[3] + 0.;
 #pragma unroll
         for (int q = 0; q < 5; q++) p.c.cons[q * n + i] = cons.q[q];
         p.c.max_signal_velocity[i] = msv;
         p.c.max_a_over_r[i] = maor;
-        // convert_conserved_to_primitive (part.rs:219-261)
-        if (!(cons.q[0] >= 0.)) err |= MVMM_ERR_NEG_MASS;
-        if (!(cons.q[4] >= 0.)) err |= MVMM_ERR_NEG_ENERGY;
-        St<double> prim;
-        if (cons.q[0] == 0.) {
-            if (cons.q[4] != 0.) err |= MVMM_ERR_NEG_ENERGY;
-            prim = st_zero<double>();
-        } else if (cons.q[0] > 0.) {
-            double m_inv = 1. / cons.q[0];
-            double density = cons.q[0] / p.c.volume[i];
-            V3<double> velocity = m_inv * vel(cons);
-            double thermal = cons.q[4] - 0.5 * len2(vel(cons)) * m_inv;
-            double u = thermal * m_inv;
-            prim = st(density, velocity, gas(p).pressure_from_internal_energy(u, density));
-        } else {
-            prim = st_zero<double>();
-        }
-        if (!(prim.q[0] >= 0.) || !(prim.q[4] >= 0.)) err |= MVMM_ERR_NEG_PRIM;
+        const St<double> prim = c2p64(cons, p.c.volume[i], gas(p), &err);
 #pragma unroll
         for (int q = 0; q < 5; q++) p.c.prim[q * n + i] = prim.q[q];
     }
@@ -257,6 +185,10 @@ __global__ void __launch_bounds__(kBlock) k_na_update(NA p) {
 double* g_scratch_addr[kMaxDevices] = {};
 std::mutex g_scratch_mu;
 
+int cuda_fail(const char* what, cudaError_t e) {
+    return report_error(MVMM_E_CUDA, (std::string(what) + ": " + cudaGetErrorString(e)).c_str());
+}
+
 }  // namespace
 }  // namespace mvmm
 
@@ -264,21 +196,33 @@ using namespace mvmm;
 
 extern "C" int mvmm_flux_update_noalloc(const mvmm_params* prm, const mvmm_mesh* dm, mvmm_cells* dc,
                                         const uint8_t* d_active, uint32_t* d_err, void* stream) {
-    if (!prm || !dm || !dc || !d_active) return MVMM_E_INVALID;
-    if (prm->precision != MVMM_PRECISION_FP64 || prm->riemann < 0 || prm->riemann > 2 || !(prm->gamma > 1.) ||
-        prm->boundary < 0 || prm->boundary > 3 || prm->eos < 0 || prm->eos > 1)
-        return MVMM_E_INVALID;
-    if (dm->n_cells <= 0 || dm->n_faces < 0 || dc->n != dm->n_cells) return MVMM_E_INVALID;
-    if (dm->n_faces > MVMM_NOALLOC_MAX_FACES) return MVMM_E_INVALID;  // scratch holds at most this many faces
+    if (!prm || !dm || !dc || !d_active) return report_error(MVMM_E_INVALID, "noalloc: null argument");
+    if (prm->riemann >= MVMM_RIEMANN_AIRS && prm->riemann <= MVMM_RIEMANN_LINEAR_ADVECTION)
+        return report_error(MVMM_E_UNSUPPORTED, "noalloc: only the HLLC, exact and PVRS solvers are supported");
+    if (prm->riemann < 0 || prm->riemann > MVMM_RIEMANN_LINEAR_ADVECTION)
+        return report_error(MVMM_E_INVALID, "noalloc: unknown Riemann solver");
+    if (prm->precision != MVMM_PRECISION_FP64)
+        return report_error(MVMM_E_UNSUPPORTED, "noalloc: only the plain FP64 form is supported");
+    if (!(prm->gamma > 1.)) return report_error(MVMM_E_INVALID, "noalloc: gamma must be > 1");
+    if (prm->boundary < 0 || prm->boundary > 3) return report_error(MVMM_E_INVALID, "noalloc: unknown boundary");
+    if (prm->eos < 0 || prm->eos > 1) return report_error(MVMM_E_INVALID, "noalloc: unknown equation of state");
+    if (dm->n_cells <= 0 || dm->n_faces < 0 || dc->n != dm->n_cells)
+        return report_error(MVMM_E_INVALID, "noalloc: empty mesh or cell count differs from the mesh's");
+    if (dm->n_cells > (1ll << 30)) return report_error(MVMM_E_INVALID, "noalloc: too many cells");
+    if (dm->n_faces > MVMM_NOALLOC_MAX_FACES)  // the scratch array holds at most this many faces
+        return report_error(MVMM_E_INVALID, "noalloc: more faces than MVMM_NOALLOC_MAX_FACES");
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return MVMM_E_CUDA;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_fail("noalloc: cudaGetDevice", e);
+    if (dev < 0 || dev >= kMaxDevices) return report_error(MVMM_E_CUDA, "noalloc: device ordinal above 63");
     double* scratch;
     {
         std::lock_guard<std::mutex> lock(g_scratch_mu);
         if (!g_scratch_addr[dev]) {
             void* ptr = nullptr;
-            cudaError_t e = cudaGetSymbolAddress(&ptr, g_face_scratch);
-            if (e != cudaSuccess || !ptr) return MVMM_E_CUDA;
+            e = cudaGetSymbolAddress(&ptr, g_face_scratch);
+            if (e != cudaSuccess) return cuda_fail("noalloc: cudaGetSymbolAddress", e);
+            if (!ptr) return report_error(MVMM_E_CUDA, "noalloc: cudaGetSymbolAddress returned null");
             g_scratch_addr[dev] = static_cast<double*>(ptr);
         }
         scratch = g_scratch_addr[dev];
@@ -297,12 +241,16 @@ extern "C" int mvmm_flux_update_noalloc(const mvmm_params* prm, const mvmm_mesh*
     p.boundary = prm->boundary;
     p.max_iter = prm->max_newton_iter > 0 ? prm->max_newton_iter : 1000;
     cudaStream_t s = (cudaStream_t)stream;
+    void* args[] = {&p};
+    // cudaLaunchKernel reports this launch's own status (not an earlier error of the thread)
     if (p.nf > 0) {
-        int g = (p.nf + kBlock - 1) / kBlock;
-        if (prm->riemann == MVMM_RIEMANN_HLLC) k_na_face<SOLVER_HLLC><<<g, kBlock, 0, s>>>(p);
-        else if (prm->riemann == MVMM_RIEMANN_EXACT) k_na_face<SOLVER_EXACT><<<g, kBlock, 0, s>>>(p);
-        else k_na_face<SOLVER_PVRS><<<g, kBlock, 0, s>>>(p);
+        const void* fn = prm->riemann == MVMM_RIEMANN_HLLC    ? (const void*)k_na_face<SOLVER_HLLC>
+                         : prm->riemann == MVMM_RIEMANN_EXACT ? (const void*)k_na_face<SOLVER_EXACT>
+                                                              : (const void*)k_na_face<SOLVER_PVRS>;
+        e = cudaLaunchKernel(fn, dim3((p.nf + kBlock - 1) / kBlock), dim3(kBlock), args, 0, s);
+        if (e != cudaSuccess) return cuda_fail("noalloc: face kernel launch", e);
     }
-    k_na_update<<<(p.n + kBlock - 1) / kBlock, kBlock, 0, s>>>(p);
-    return cudaGetLastError() == cudaSuccess ? MVMM_OK : MVMM_E_CUDA;
+    e = cudaLaunchKernel((const void*)k_na_update, dim3((p.n + kBlock - 1) / kBlock), dim3(kBlock), args, 0, s);
+    if (e != cudaSuccess) return cuda_fail("noalloc: update kernel launch", e);
+    return MVMM_OK;
 }

@@ -317,7 +317,7 @@ __global__ void __launch_bounds__(kMaxBlock, FACE32_MINB) k_face_flux32(KP p) {
             if (r >= 0) {
                 bool ra = p.active[r] != 0;
                 double dtl = C(p, F_DT, l), dtr = C(p, F_DT, r);
-                if (!((!la && !ra) || (dtr < dtl && !ra) || (dtl < dtr && !la))) {
+                if (interior_face_active(la, ra, dtl, dtr)) {
                     dt = fmin(dtl, dtr);
                     o = face_interior32<SOLVER>(p, f, l, r, (float)dt, g, g64, &err);
                     counted = true;
@@ -785,7 +785,7 @@ void launch_gradients32(const KP& p, cudaStream_t s) {
 
 void launch_face_flux_fp32(const KP& p, int solver, cudaStream_t s) {
     if (p.nf <= 0) return;
-    int g = grid(p.nf, p.blk_face), cap = 152 * 512 / p.blk_face;
+    int g = grid(p.nf, p.blk_face), cap = p.n_sms * 512 / p.blk_face;
     if (p.use_list && g > cap) g = cap;
     if (solver == SOLVER_HLLC) k_face_flux32<SOLVER_HLLC><<<g, p.blk_face, 0, s>>>(p);
     else if (solver == SOLVER_EXACT) k_face_flux32<SOLVER_EXACT><<<g, p.blk_face, 0, s>>>(p);

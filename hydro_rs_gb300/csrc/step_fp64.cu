@@ -4,6 +4,7 @@
 // reference evaluates it.  One CUDA thread per face for the flux stage, one per
 // cell for the cell stages; the flux scatter is a deterministic CSR gather in
 // the reference's face order (no atomics on floating-point data).
+#include "face64.cuh"
 #include "mvmm_cellops.cuh"
 
 namespace mvmm {
@@ -163,130 +164,26 @@ __global__ void __launch_bounds__(kMaxBlock) k_derive(KP p) {
 }
 
 // ------------------------------------------------------------ face flux --
-// reconstructed state: ((prim + grad.dx) + extrap) + time_extrapolations(-0.5 dt)
-__device__ __forceinline__ St<double> reconstruct(const KP& p, int i, const St<double>& prim, V3<double> dx,
-                                                  double td) {
-    St<double> r;
-#pragma unroll
-    for (int q = 0; q < 5; q++) {
-        double v = prim.q[q] + gdot(p, i, q, dx);
-        v = v + C(p, F_EXTRAP + q, i);
-        r.q[q] = v;
-    }
-    if (prim.q[0] > 0.) {
-#pragma unroll
-        for (int q = 0; q < 5; q++) r.q[q] = r.q[q] + td * C(p, F_SRC + q, i);
-    } else {
-#pragma unroll
-        for (int q = 0; q < 5; q++) r.q[q] = r.q[q] + 0.;
-    }
-    return r;
-}
-
-struct FaceOut {
-    St<double> fl;
-    V3<double> mflux;
-    double v_max, a_over_r;
+// The face physics (face64.cuh) reads the context's cell block: the derived
+// rows predict wrote (time-extrapolation source, sound speed) included.
+struct AccKP {
+    const KP& p;
+    __device__ __forceinline__ St<double> prim(int i) const { return C5(p, F_PRIM, i); }
+    __device__ __forceinline__ V3<double> gc(int i) const { return C3(p, F_GC, i); }
+    __device__ __forceinline__ V3<double> cen(int i) const { return C3(p, F_CEN, i); }
+    __device__ __forceinline__ V3<double> loc(int i) const { return C3(p, F_LOC, i); }
+    __device__ __forceinline__ V3<double> v(int i) const { return C3(p, F_V, i); }
+    __device__ __forceinline__ double dt(int i) const { return C(p, F_DT, i); }
+    __device__ __forceinline__ double cs(int i) const { return C(p, F_CS, i); }
+    __device__ __forceinline__ double gdot(int i, int q, V3<double> dx) const { return mvmm::gdot(p, i, q, dx); }
+    __device__ __forceinline__ double extrap(int i, int q) const { return C(p, F_EXTRAP + q, i); }
+    __device__ __forceinline__ St<double> src(int i, const St<double>&) const { return C5(p, F_SRC, i); }
+    __device__ __forceinline__ V3<double> fcen(int f) const { return F3(p.fcen, p.nf, f); }
+    __device__ __forceinline__ V3<double> shift(int f) const { return F3(p.shift, p.nf, f); }
+    __device__ __forceinline__ V3<double> normal(int f) const { return F3(p.normal, p.nf, f); }
+    __device__ __forceinline__ double area(int f) const { return p.area[f]; }
+    __device__ __forceinline__ int boundary() const { return p.boundary; }
 };
-// A face up to its Riemann solve: the two states handed to the solver (in the
-// face frame), the face velocity and normal, and what the result needs.
-struct FacePre {
-    St<double> l, r;
-    V3<double> iv, n, dx;
-    double dt, area, v_max;
-};
-// ... and from the solver's flux on (flux_exchange, flux.rs:85-99)
-__device__ __forceinline__ FaceOut face_finish(const FacePre& q, const St<double>& F) {
-    St<double> fluxes = q.area * F;
-    FaceOut o;
-    o.fl = q.dt * fluxes;
-    o.mflux = fluxes.q[0] * q.dx;
-    o.v_max = q.v_max;
-    o.a_over_r = q.area / len(q.dx);
-    return o;
-}
-
-// flux_exchange (flux.rs:23-100)
-__device__ __forceinline__ FacePre face_interior_pre(const KP& p, int f, int l, int r, double dt) {
-    V3<double> fc = F3(p.fcen, p.nf, f);
-    V3<double> sh = F3(p.shift, p.nf, f);
-    V3<double> dx_left = fc - C3(p, F_GC, l);
-    V3<double> dx_right = (fc - C3(p, F_GC, r)) - sh;
-    double dx_gradients = len(dx_left - dx_right);
-    V3<double> dx_centroid = (C3(p, F_CEN, r) + sh) - C3(p, F_CEN, l);
-    V3<double> locl = C3(p, F_LOC, l), locr = C3(p, F_LOC, r);
-    V3<double> dx = (locr + sh) - locl;
-    St<double> pl = C5(p, F_PRIM, l), pr = C5(p, F_PRIM, r);
-    double v_max = 0. + C(p, F_CS, l);
-    v_max = v_max + C(p, F_CS, r);
-    v_max -= m_min(dot(vel(pr) - vel(pl), dx_centroid), 0.);
-    double td = -(-0.5 * dt);  // -dt_extrapolate in time_extrapolations
-    St<double> ldash = reconstruct(p, l, pl, dx_left, td);
-    St<double> rdash = reconstruct(p, r, pr, dx_right, td);
-    St<double> prim_left = pairwise_limiter(pl, pr, ldash, len(dx_left) / dx_gradients);
-    St<double> prim_right = pairwise_limiter(pr, pl, rdash, len(dx_right) / dx_gradients);
-    V3<double> vl = C3(p, F_V, l), vr = C3(p, F_V, r);
-    V3<double> midpoint = 0.5 * ((locl + locr) + sh);
-    double fac = dot(vr - vl, fc - midpoint) / len2(dx);
-    V3<double> v_face = 0.5 * (vl + vr) - fac * dx;
-    V3<double> mvf = neg(v_face);
-    FacePre q;
-    q.l = boost(prim_left, mvf);
-    q.r = boost(prim_right, mvf);
-    q.iv = v_face;
-    q.n = F3(p.normal, p.nf, f);
-    q.dx = dx;
-    q.dt = dt;
-    q.area = p.area[f];
-    q.v_max = v_max;
-    return q;
-}
-
-// flux_exchange_boundary (flux.rs:102-195) with Space::get_boundary_part semantics
-__device__ __forceinline__ FacePre face_boundary_pre(const KP& p, int f, int i) {
-    V3<double> fc = F3(p.fcen, p.nf, f);
-    V3<double> n = F3(p.normal, p.nf, f);
-    V3<double> loc = C3(p, F_LOC, i), cen = C3(p, F_CEN, i), gc = C3(p, F_GC, i);
-    // Particle::reflect (part.rs:374-383)
-    V3<double> rloc = loc + (2. * dot(fc - loc, n)) * n;
-    V3<double> rcen = cen + (2. * dot(fc - cen, n)) * n;
-    V3<double> rgc = gc + (2. * dot(fc - gc, n)) * n;
-    V3<double> dx_face = fc - gc;
-    double dx_gradients = len(rgc - gc);
-    V3<double> dx_centroid = rcen - cen;
-    V3<double> dx = rloc - loc;
-    St<double> prim = C5(p, F_PRIM, i);
-    double v_max = 0. + C(p, F_CS, i);
-    double dt = C(p, F_DT, i);
-    double td = -(-0.5 * dt);
-    St<double> dash = reconstruct(p, i, prim, dx_face, td);
-    double dx_fac = len(dx_face) / dx_gradients;
-    St<double> bnd;
-    if (p.boundary == 1) {  // reflective
-        St<double> rprim = reflect(prim, n);
-        dash = pairwise_limiter(prim, rprim, dash, dx_fac);
-        v_max -= m_min(dot(vel(rprim) - vel(prim), dx_centroid), 0.);
-        bnd = reflect(dash, n);
-    } else if (p.boundary == 2) {  // open
-        dash = pairwise_limiter(prim, prim, dash, dx_fac);
-        bnd = dash;
-    } else {  // vacuum
-        St<double> vac = st_zero<double>();
-        dash = pairwise_limiter(prim, vac, dash, dx_fac);
-        v_max += m_min(dot(vel(prim), dx_centroid), 0.);
-        bnd = vac;
-    }
-    FacePre q;
-    q.l = dash;
-    q.r = bnd;
-    q.iv = v3(0., 0., 0.);
-    q.n = n;
-    q.dx = dx;
-    q.dt = dt;
-    q.area = p.area[f];
-    q.v_max = v_max;
-    return q;
-}
 
 // The face rows of a result: 5 fluxes and v_max, a_over_r (step), or the
 // FluxInfo rows with mflux (per-stage calls).
@@ -349,21 +246,18 @@ __global__ void __launch_bounds__(kMaxBlock) k_face_flux(KP p) {
             if (r >= 0) {
                 bool ra = p.active[r] != 0;
                 double dtl = C(p, F_DT, l), dtr = C(p, F_DT, r);
-                if (!((!la && !ra) || (dtr < dtl && !ra) || (dtl < dtr && !la))) {
-                    q = face_interior_pre(p, f, l, r, m_min(dtl, dtr));
+                if (interior_face_active(la, ra, dtl, dtr)) {
+                    q = face_interior_pre(AccKP{p}, f, l, r, m_min(dtl, dtr));
                     counted = true;
                 }
             } else if (la) {
-                q = face_boundary_pre(p, f, l);
+                q = face_boundary_pre(AccKP{p}, f, l);
                 counted = true;
             }
             FaceOut o;
             bool queued = false;
             if (!counted) {
-                o.fl = st_zero<double>();
-                o.mflux = v3(0., 0., 0.);
-                o.v_max = 0.;
-                o.a_over_r = 0.;
+                o = face_zero();
             } else if (SOLVER == SOLVER_EXACT && p.brent_jobs) {
                 // star_half_state (riemann_solver.rs:258-284) with the exact
                 // star solver, its Brent stage queued when it is needed
@@ -457,7 +351,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_compact(KP p) {
                 if (r >= 0) {
                     bool ra = p.active[r] != 0;
                     double dtl = C(p, F_DT, l), dtr = C(p, F_DT, r);
-                    act = !((!la && !ra) || (dtr < dtl && !ra) || (dtl < dtr && !la));
+                    act = interior_face_active(la, ra, dtl, dtr);
                 } else {
                     act = la;
                 }
@@ -493,29 +387,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_extrap_flush(KP p, int reset) {
 // ---------------------------------------------------- cons -> primitive --
 // Particle::convert_conserved_to_primitive (part.rs:219-261)
 __device__ __forceinline__ void c2p(const KP& p, int i, const St<double>& cons, unsigned int* err) {
-    const Gas<double> g = gas(p);
-    if (!ge0_64(cons.q[0])) *err |= 1u << 2;
-    if (!ge0_64(cons.q[4])) *err |= 1u << 3;
-    St<double> prim;
-    if (is_zero64(cons.q[0])) {
-        if (!is_zero64(cons.q[4])) *err |= 1u << 3;
-        prim = st_zero<double>();
-    } else if (gt0_64(cons.q[0])) {  // State<Primitive>::from_conserved (physical_quantities.rs:213-226)
-        double m_inv = 1. / cons.q[0];
-        double density = cons.q[0] / C(p, F_VOL, i);
-        V3<double> velocity = m_inv * vel(cons);
-        double thermal = cons.q[4] - 0.5 * len2(vel(cons)) * m_inv;
-        double u = thermal * m_inv;
-        double pressure = g.pressure_from_internal_energy(u, density);
-        prim = st(density, velocity, pressure);
-    } else {
-        prim = st_zero<double>();
-    }
-    if (!ge0_64(prim.q[0]) || !ge0_64(prim.q[4])) *err |= 1u << 5;
-    if (!is_finite64(prim.q[0]) || !is_finite64(prim.q[1]) || !is_finite64(prim.q[2]) ||
-        !is_finite64(prim.q[3]) || !is_finite64(prim.q[4]))
-        *err |= 1u << 4;
-    W5(p, F_PRIM, i, prim);
+    W5(p, F_PRIM, i, c2p64(cons, C(p, F_VOL, i), gas(p), err));
 }
 
 // ---------------------------------------------------- scatter + update --
@@ -616,18 +488,8 @@ __device__ __forceinline__ void update_finish(const KP& p, int i, int k, bool ac
     unsigned int err = 0;
     if (act) {
         p.fresh[i] = 0;  // prim (here), grad and v_rel (gradient stage) change
-        St<double> cons = C5(p, F_CONS, i) + facc;
-        if (!is_finite64(cons.q[0]) || !is_finite64(cons.q[1]) || !is_finite64(cons.q[2]) ||
-            !is_finite64(cons.q[3]) || !is_finite64(cons.q[4]))
-            err |= 1u << 4;
-        if (lt0_64(cons.q[0])) cons = st_zero<double>();
-        if (lt0_64(cons.q[4])) cons = st_zero<double>();
+        const St<double> cons = apply_flux64(C5(p, F_CONS, i), facc, &err);
         facc = st_zero<double>();
-        // kick2 (runner/hydrodynamics.rs:51-57): Particle::grav_kick with a zero
-        // acceleration adds +0 to the momentum (part.rs:303-312)
-        cons.q[1] = cons.q[1] + 0.;
-        cons.q[2] = cons.q[2] + 0.;
-        cons.q[3] = cons.q[3] + 0.;
         W5(p, F_CONS, i, cons);
         W(p, F_MSV, i, msv);
         W(p, F_MAOR, i, maor);
@@ -1258,11 +1120,11 @@ inline int grid(int n, int b = kBlock) { return (n + b - 1) / b; }
 }  // namespace
 
 // Blocks of a cell kernel: one thread per cell, or in a hierarchical step half
-// a wave of resident blocks (152 SMs x 1024 threads) striding over the cell
+// a wave of resident blocks (the device's SMs x 1024 threads) striding over the cell
 // list, whose length is known on the device only.
 int cell_grid(const KP& p) {
     int g = grid(p.n, p.blk_cell);
-    int wave = 152 * 1024 / p.blk_cell;
+    int wave = p.n_sms * 1024 / p.blk_cell;
     return p.use_list && g > wave ? wave : g;
 }
 
@@ -1274,7 +1136,7 @@ void launch_derive(const KP& p, cudaStream_t s) {
 }
 // list mode: a grid of a few waves walks the list (its length is only known on the device)
 inline int face_grid(const KP& p) {
-    int g = grid(p.nf, p.blk_face), cap = 152 * 512 / p.blk_face;
+    int g = grid(p.nf, p.blk_face), cap = p.n_sms * 512 / p.blk_face;
     return p.use_list && g > cap ? cap : g;
 }
 
@@ -1286,7 +1148,7 @@ void launch_face_flux_fp64(const KP& p, int solver, cudaStream_t s) {
     else if (solver == SOLVER_EXACT && p.brent_jobs) {
         cudaMemsetAsync(p.brent_count, 0, sizeof(unsigned int), s);
         k_face_flux<SOLVER_EXACT><<<g, p.blk_face, 0, s>>>(p);
-        const int blk = 128, jobs_grid = (int)std::min<long long>((p.brent_cap + blk - 1) / blk, 152LL * 16);
+        const int blk = 128, jobs_grid = (int)std::min<long long>((p.brent_cap + blk - 1) / blk, p.n_sms * 16LL);
         k_face_brent<<<jobs_grid, blk, 0, s>>>(p);
     } else if (solver == SOLVER_EXACT) k_face_flux<SOLVER_EXACT><<<g, p.blk_face, 0, s>>>(p);
     else if (solver == SOLVER_PVRS) k_face_flux<SOLVER_PVRS><<<g, p.blk_face, 0, s>>>(p);
@@ -1325,7 +1187,7 @@ void launch_limit(const KP& p, cudaStream_t s) {
     // steps over all cells: few, full blocks striding over the cells, so that
     // few blocks take part in the last-block hand-off of the step's bookkeeping
     if (p.use_list) k_limit<<<cell_grid(p), p.blk_cell, 0, s>>>(p);
-    else k_limit<<<std::min(grid(p.n, 256), 152 * 8), 256, 0, s>>>(p);
+    else k_limit<<<std::min(grid(p.n, 256), p.n_sms * 8), 256, 0, s>>>(p);
 }
 // the engine bookkeeping runs in the last block of k_limit
 void launch_end(const KP&, cudaStream_t) {}

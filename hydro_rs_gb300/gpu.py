@@ -50,7 +50,8 @@ def make_params(p, precision=None, box=(1.0, 1.0, 1.0)) -> _Params:
     """mvmm_params from an ics.Params (precision overrides p.precision; box: the mesh's box)."""
     thr, adv = p.solver_extras()
     prec = p.precision if precision is None else precision
-    return _Params(p.gamma, 0, 0.0, p.cfl, p.riemann, p.boundary, p.dimensionality, int(p.sync_all), p.t_end,
+    return _Params(p.gamma, p.eos, p.isothermal_internal_energy, p.cfl, p.riemann, p.boundary, p.dimensionality,
+                   int(p.sync_all), p.t_end,
                    p.max_newton_iter, prec, p.particle_motion, p.runner, thr, (ctypes.c_double * 3)(*adv),
                    (ctypes.c_double * 3)(*[float(b) for b in box]))
 

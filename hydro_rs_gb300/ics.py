@@ -47,6 +47,8 @@ class Params:
     particle_motion: int = FIXED
     airs_threshold: float | None = None       # riemann_solver.threshold (required by AIRS)
     advection_velocity: tuple | None = None   # riemann_solver.velocity (required by LinearAdvection)
+    eos: int = 0                              # 0 = EquationOfState::Ideal, 1 = Isothermal (gas_law.rs:59-63)
+    isothermal_internal_energy: float = 0.0   # the Isothermal payload
 
     def solver_extras(self):
         """(threshold, velocity) as passed to the C structs; NaN marks a missing value."""
@@ -97,8 +99,11 @@ def lattice(box, num_part: int, dim: int, jitter: float, rng):
     return x, tuple(box), volume / n, (npx, npy, npz)
 
 
-def cells_from_ic(mesh: Mesh, x, mass, vel, u, gamma) -> Cells:
-    """Particle::from_ic + update_geometry + first_init (part.rs:151-217)."""
+def cells_from_ic(mesh: Mesh, x, mass, vel, u, gamma, iso_u=None) -> Cells:
+    """Particle::from_ic + update_geometry + first_init (part.rs:151-217).
+
+    iso_u: the isothermal internal energy of EquationOfState::Isothermal, whose
+    pressure is (gamma - 1) iso_u rho (gas_law.rs:90-97); None for an ideal gas."""
     n = mesh.n_cells
     c = Cells.zeros(n)
     mass = np.asarray(mass, dtype=np.float64)
@@ -118,7 +123,7 @@ def cells_from_ic(mesh: Mesh, x, mass, vel, u, gamma) -> Cells:
         lsq = c.cons[1] * c.cons[1] + c.cons[2] * c.cons[2] + c.cons[3] * c.cons[3]
         thermal = c.cons[4] - 0.5 * lsq * m_inv
         ui = thermal * m_inv
-        p = (gamma - 1.0) * ui * rho
+        p = (gamma - 1.0) * (ui if iso_u is None else iso_u) * rho
     pos = mass > 0
     c.prim[0] = np.where(pos, rho, 0.0)
     c.prim[1:4] = np.where(pos, v, 0.0)
@@ -126,19 +131,28 @@ def cells_from_ic(mesh: Mesh, x, mass, vel, u, gamma) -> Cells:
     return c
 
 
-def sod_1d(n: int = 1000, riemann: int = HLLC, t_end: float = 0.2, cfl: float = 0.3) -> Problem:
-    """1D Sod shock tube (bin/main.rs:35-40 preset) on [0,1], reflective."""
-    params = Params(gamma=5.0 / 3.0, cfl=cfl, riemann=riemann, boundary=REFLECTIVE, dimensionality=1,
+def sod_1d(n: int = 1000, riemann: int = HLLC, t_end: float = 0.2, cfl: float = 0.3,
+           boundary: int = REFLECTIVE, iso_u: float | None = None) -> Problem:
+    """1D Sod shock tube (bin/main.rs:35-40 preset) on [0,1], reflective (or the
+    given wall boundary: open or vacuum).  iso_u: an isothermal gas
+    (EquationOfState::Isothermal) with that internal energy everywhere, so the
+    density jump drives the flow (gas_law.rs:81-106)."""
+    params = Params(gamma=5.0 / 3.0, cfl=cfl, riemann=riemann, boundary=boundary, dimensionality=1,
                     sync_all=True, t_end=t_end)
+    if iso_u is not None:
+        params.eos, params.isothermal_internal_energy = 1, float(iso_u)
     x, box, vpp, _ = lattice((1.0, 1.0, 1.0), n, 1, 0.0, None)
     mesh = mesh_1d(x[0], box=box, periodic=False)
     left = x[0] < 0.5
     rho = np.where(left, 1.0, 0.125)
     p = np.where(left, 1.0, 0.1)
     vel = np.zeros((3, x.shape[1]))
-    u = gas_internal_energy_from_pressure(params.gamma, p, 1.0 / rho)
-    cells = cells_from_ic(mesh, x, rho * vpp, vel, u, params.gamma)
-    return Problem("sod_1d", params, mesh, cells)
+    if iso_u is None:
+        u = gas_internal_energy_from_pressure(params.gamma, p, 1.0 / rho)
+    else:
+        u = np.full(x.shape[1], float(iso_u))  # gas_internal_energy_from_pressure of the isothermal gas
+    cells = cells_from_ic(mesh, x, rho * vpp, vel, u, params.gamma, iso_u=iso_u)
+    return Problem("sod_1d" if iso_u is None else "sod_1d_isothermal", params, mesh, cells)
 
 
 def riemann_1d(n: int, left_state, right_state, riemann: int, t_end: float, gamma: float = 5.0 / 3.0,

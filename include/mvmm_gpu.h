@@ -280,6 +280,11 @@ int mvmm_riemann_sample_p(const mvmm_params *params, int64_t n, const double *le
  * documented above, device_active is a device uint8[n] mask, device_err a
  * device uint32 the call ORs MVMM_ERR_* bits into (the caller clears it; may be
  * NULL).  The cell state is updated in place.  Asynchronous on cuda_stream.
+ * Solvers: HLLC, exact and PVRS (AIRS, TSRS, TRRS and LinearAdvection return
+ * MVMM_E_UNSUPPORTED, as does the FP32-face precision).  The mesh indices are
+ * not validated on the host (the arrays are on the device): the kernels skip
+ * a face or CSR entry whose index lies outside its array and OR
+ * MVMM_ERR_BOUNDS into *device_err instead of reading out of bounds.
  *
  * The per-face intermediate results live in one static device array of
  * MVMM_NOALLOC_MAX_FACES faces (7 doubles each, 3.5 MiB) that every GPU which

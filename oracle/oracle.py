@@ -94,7 +94,8 @@ class OracleSim:
         self.mesh = problem.mesh
         self.cells = problem.cells.copy()
         thr, adv = p.solver_extras()
-        self._p = _Params(p.gamma, 0, 0.0, p.cfl, p.riemann, p.boundary, p.dimensionality, int(p.sync_all),
+        self._p = _Params(p.gamma, p.eos, p.isothermal_internal_energy, p.cfl, p.riemann, p.boundary,
+                          p.dimensionality, int(p.sync_all),
                           p.t_end, p.max_newton_iter, n_threads, p.runner, thr, (ctypes.c_double * 3)(*adv),
                           p.particle_motion, (ctypes.c_double * 3)(*[float(b) for b in problem.mesh.box]))
         self._mv = self.mesh.cview()

@@ -68,3 +68,29 @@ def test_conservation_moving(motion):
     assert np.abs(s.loc - p.cells.loc).max() > 1e-6
     assert (s.loc[:2] >= 0).all() and (s.loc[:2] < 1).all()
     assert abs(s.volume.sum() - 1.0) < 1e-12
+
+
+def test_oracle_galilean_invariance_first_cycle():
+    """tests/test_gallilean_invariance.rs (commented out in the reference) on the
+    oracle: the first gradient estimate and timestep (engine step 0), then the
+    drift, new mesh, flux exchange and cons -> prim of the first step with
+    dt > 0 (engine step 1), boosted by 10 x, within the reference's 1e-10.  The
+    second gradient estimate is not invariant in the reference's arithmetic
+    (see tests/test_gpu_boundaries.py); it is recorded here as departing by
+    more than the rounding of the states it starts from."""
+    from tests.test_gpu_boundaries import _galilean_problem, galilean_differences
+
+    boost = np.array([10.0, 0.0, 0.0])
+    pa, pb = _galilean_problem((0.0, 0.0, 0.0)), _galilean_problem(boost)
+    a, b = O.OracleSim(pa), O.OracleSim(pb)
+    sa, sb = MovingMeshStepper(a, pa.mesh), MovingMeshStepper(b, pb.mesh)
+    sa.step()
+    sb.step()
+    d = galilean_differences(a.state(), b.state(), boost)
+    assert a.ti_current == b.ti_current and max(d.values()) <= 1e-10, d
+    sa.step()
+    sb.step()
+    d = galilean_differences(a.state(), b.state(), boost)
+    grad = d.pop("grad")
+    assert a.ti_current == b.ti_current and max(d.values()) <= 1e-10, d
+    assert max(d.values()) < 1e-13 < grad  # states agree to rounding, the limited gradients do not
