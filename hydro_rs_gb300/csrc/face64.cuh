@@ -161,8 +161,8 @@ __device__ __forceinline__ FacePre face_boundary_pre(const A& a, int f, int i) {
     return q;
 }
 
-// Particle::apply_flux (part.rs:178-193) and kick2 (runner/hydrodynamics.rs:51-57)
-// of an active cell: the conserved state after adding the summed fluxes.
+// Particle::apply_flux (part.rs:178-193) of an active cell: the conserved
+// state after adding the summed fluxes.
 __device__ __forceinline__ St<double> apply_flux64(const St<double>& cons_in, const St<double>& facc,
                                                    unsigned int* err) {
     St<double> cons = cons_in + facc;
@@ -171,11 +171,34 @@ __device__ __forceinline__ St<double> apply_flux64(const St<double>& cons_in, co
         *err |= MVMM_ERR_NONFINITE;
     if (lt0_64(cons.q[0])) cons = st_zero<double>();
     if (lt0_64(cons.q[4])) cons = st_zero<double>();
-    // kick2: Particle::grav_kick with a zero acceleration adds +0 to the momentum (part.rs:303-312)
+    return cons;
+}
+// kick2 / kick1 as the reference's runners run them: Particle::grav_kick with
+// the zero acceleration they leave in a_grav adds +0 to the momentum
+// (part.rs:303-312); the mass and energy additions leave those rows' bits as
+// they are.
+__device__ __forceinline__ St<double> zero_kick64(St<double> cons) {
     cons.q[1] = cons.q[1] + 0.;
     cons.q[2] = cons.q[2] + 0.;
     cons.q[3] = cons.q[3] + 0.;
     return cons;
+}
+// Particle::grav_kick (part.rs:303-312) with acceleration a over half of dt.
+// gravity_mflux is zero whenever a kick runs (apply_flux resets it before
+// kick2, and nothing accumulates into an active cell's after that), so the
+// energy gains (dt/2) a . momentum.
+__device__ __forceinline__ St<double> grav_kick64(const St<double>& cons, double dt, V3<double> a) {
+    const V3<double> k = (0.5 * dt) * a;
+    const double mass = cons.q[0];
+    const V3<double> mom = vel(cons);
+    const V3<double> mflux0 = v3(0., 0., 0.);
+    St<double> out;
+    out.q[0] = cons.q[0] + 0.;
+    out.q[1] = cons.q[1] + k.x * mass;
+    out.q[2] = cons.q[2] + k.y * mass;
+    out.q[3] = cons.q[3] + k.z * mass;
+    out.q[4] = cons.q[4] + dot(k, mom - mflux0);
+    return out;
 }
 
 // Particle::convert_conserved_to_primitive (part.rs:219-261) with

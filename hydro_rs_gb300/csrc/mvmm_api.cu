@@ -203,6 +203,13 @@ KP make_kp(mvmm_ctx* c, int stage, int flux_rows) {
     p.face_list = c->face_list;
     p.blk_face = c->blk_face;
     p.n_sms = c->n_sms > 0 ? c->n_sms : 1;
+    p.grav = c->prm.gravity;
+    p.grav_acc = c->prm.gravity_accelerations ? 1 : 0;
+    p.grav_soft = c->prm.gravity_softening;
+    for (int a = 0; a < 3; a++) {
+        p.grav_avec[a] = c->prm.gravity_acceleration[a];
+        p.grav_pos[a] = c->prm.gravity_position[a];
+    }
     p.blk_cell = c->blk_cell;
     p.rsx = solver_settings(c->prm);
     const Gas<double> g = make_gas<double>(c->prm.gamma, c->prm.eos, c->prm.isothermal_internal_energy);
@@ -460,6 +467,13 @@ static int create_impl(const mvmm_params* prm, const mvmm_mesh* m, int64_t n_ins
         for (int a = 0; a < prm->dimensionality; a++)
             if (!(prm->box_size[a] > 0.)) return fail(MVMM_E_INVALID, "moving meshes need box_size > 0");
     }
+    if (prm->gravity < MVMM_GRAVITY_NONE || prm->gravity > MVMM_GRAVITY_KEPLERIAN)
+        return fail(MVMM_E_INVALID, "unknown gravity solver");
+    if (prm->gravity == MVMM_GRAVITY_SELF && prm->gravity_accelerations)
+        return fail(MVMM_E_UNSUPPORTED, "self-gravity accelerations are not computed (external potentials only)");
+    if ((prm->gravity == MVMM_GRAVITY_SELF || prm->gravity == MVMM_GRAVITY_KEPLERIAN) &&
+        !(prm->gravity_softening >= 0.))
+        return fail(MVMM_E_INVALID, "gravity needs a softening_length >= 0");
     if (!(prm->t_end > 0.0)) return fail(MVMM_E_INVALID, "t_end must be > 0");
     int rc = check_mesh(m, prm->boundary);
     if (rc) return rc;
@@ -1019,6 +1033,8 @@ int mvmm_step_cells(mvmm_ctx* c, const mvmm_cells* in, mvmm_cells* out, uint64_t
     if (c->n_inst != 1) return fail(MVMM_E_UNSUPPORTED, "mvmm_step_cells steps a single simulation");
     if (c->prm.particle_motion != MVMM_MOTION_FIXED)
         return fail(MVMM_E_UNSUPPORTED, "mvmm_step_cells steps a fixed mesh");
+    if (c->prm.gravity_accelerations)  // kick1 rewrites the conserved rows after their copy back has begun
+        return fail(MVMM_E_UNSUPPORTED, "mvmm_step_cells does not apply gravity accelerations");
     if (!c->side) {
         CUDA_TRY(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
         CUDA_TRY(cudaStreamCreateWithFlags(&c->geo_side, cudaStreamNonBlocking));
@@ -1195,6 +1211,33 @@ int mvmm_compute_timesteps(mvmm_ctx* c, const uint8_t* active, double* dt_out) {
     launch_timesteps(make_kp(c, 1, 10), c->dtmp, c->stream);
     CUDA_TRY(cudaGetLastError());
     CUDA_TRY(cudaMemcpyAsync(dt_out, c->dtmp, (size_t)c->n * 8, cudaMemcpyDeviceToHost, c->stream));
+    return finish(c);
+}
+
+// ---- GravitySolver trait -----------------------------------------------
+int mvmm_gravity_timesteps(mvmm_ctx* c, double* dt_out) {
+    if (!c || !dt_out) return fail(MVMM_E_INVALID, "null argument");
+    launch_gravity(make_kp(c, 1, 10), -1, c->dtmp, c->stream);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaMemcpyAsync(dt_out, c->dtmp, (size_t)c->n * 8, cudaMemcpyDeviceToHost, c->stream));
+    return finish(c);
+}
+
+int mvmm_gravity_accelerations(mvmm_ctx* c, double* a_out) {
+    if (!c || !a_out) return fail(MVMM_E_INVALID, "null argument");
+    if (c->prm.gravity == MVMM_GRAVITY_SELF)
+        return fail(MVMM_E_UNSUPPORTED, "self-gravity accelerations are not computed (external potentials only)");
+    const KP p = make_kp(c, 1, 10);
+    for (int a = 0; a < 3; a++) {
+        if (c->prm.gravity == MVMM_GRAVITY_NONE) {
+            CUDA_TRY(cudaMemsetAsync(c->dtmp, 0, (size_t)c->n * 8, c->stream));
+        } else {
+            launch_gravity(p, a, c->dtmp, c->stream);
+            CUDA_TRY(cudaGetLastError());
+        }
+        CUDA_TRY(cudaMemcpyAsync(a_out + (size_t)a * c->n, c->dtmp, (size_t)c->n * 8, cudaMemcpyDeviceToHost,
+                                 c->stream));
+    }
     return finish(c);
 }
 

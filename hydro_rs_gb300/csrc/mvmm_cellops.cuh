@@ -4,6 +4,7 @@
 #pragma once
 
 #include "mvmm_device.cuh"
+#include "mvmm_gpu.h"
 #include "mvmm_internal.h"
 
 namespace mvmm {
@@ -141,6 +142,36 @@ __device__ __forceinline__ double radius(double volume, int dim) {
     double x = 0.25 * 3. * 0.31830988618379067154 * volume, y, r;
     if (rat_root(x, 3, 1. / 3., y, r)) return r;  // x^(1/3) (cube root by Newton, see rat_root)
     return pow(x, 1. / 3.);
+}
+
+// ---- gravity (gravity.rs) ----
+// ExternalPotentialGravity::compute_accelerations at a generator position:
+// Potential::Constant, or KeplerianPotential::acceleration (gravity.rs:125-136).
+__device__ __forceinline__ V3<double> grav_acceleration(const KP& p, V3<double> pos) {
+    if (p.grav == MVMM_GRAVITY_CONSTANT) return v3(p.grav_avec[0], p.grav_avec[1], p.grav_avec[2]);
+    const V3<double> dx = pos - v3(p.grav_pos[0], p.grav_pos[1], p.grav_pos[2]);
+    double r2 = len2(dx);
+    const double r = sqrt(r2);
+    if (r < p.grav_soft) r2 = r2 + p.grav_soft * p.grav_soft;
+    const double d = r * r2;
+    return v3(-dx.x / d, -dx.y / d, -dx.z / d);
+}
+// GravitySolver::compute_timesteps of cell i (gravity.rs:45-53, 71-73, 90-95,
+// 119-123).  Only the Keplerian potential sets a limit: self-gravity's
+// accelerations are zero (the runners never compute them), for which it
+// returns INFINITY, as does the constant potential.
+__device__ __forceinline__ double grav_timestep(const KP& p, int i) {
+    if (p.grav != MVMM_GRAVITY_KEPLERIAN) return INFINITY;
+    // eta * radius (in 2D whatever the dimensionality) / circular_velocity
+    const V3<double> dx = C3(p, F_LOC, i) - v3(p.grav_pos[0], p.grav_pos[1], p.grav_pos[2]);
+    const double r = sqrt(len2(dx));
+    const double r_softened = r < p.grav_soft ? r + p.grav_soft : r;
+    return 0.5 * sqrt(0.31830988618379067154 * C(p, F_VOL, i)) / sqrt(1. / r_softened);
+}
+// The runners take the gravity solver's timestep where it is smaller
+// (runner/hydrodynamics/optimal_order.rs:47-50, godunov.rs:41-44).
+__device__ __forceinline__ double limit_by_gravity(const KP& p, int i, double dt) {
+    return p.grav ? m_min(dt, grav_timestep(p, i)) : dt;
 }
 
 // Particle::set_particle_velocity (part.rs:328-372): the velocity the

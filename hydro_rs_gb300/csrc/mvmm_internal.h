@@ -147,6 +147,11 @@ struct KP {
     const double* inst_tbi;  // per-instance 1 / time_base (nullptr: time_base_inv)
     int blk_face, blk_cell;  // thread-block sizes (chosen by mvmm_autotune)
     int n_sms;               // streaming multiprocessors of the context's device (grid sizing)
+    // gravity solver (gravity.rs): MVMM_GRAVITY_* kind, whether the external
+    // potential's accelerations kick (grav_acc), softening, Constant
+    // acceleration, Keplerian position
+    int grav, grav_acc;
+    double grav_soft, grav_avec[3], grav_pos[3];
     GasK gk;                 // gas-law constants
     RSx rsx;                 // Riemann solver kind and its settings
     int godunov;             // 1: GodunovHydroRunner (no gradients), 0: OptimalOrderRunner
@@ -183,6 +188,7 @@ void launch_update(const KP& p, int do_c2p, cudaStream_t s);
 void launch_c2p(const KP& p, cudaStream_t s);
 void launch_gradients(const KP& p, int do_timestep, cudaStream_t s);
 void launch_timesteps(const KP& p, double* dt_out, cudaStream_t s);
+void launch_gravity(const KP& p, int what, double* out, cudaStream_t s);
 void launch_limit(const KP& p, cudaStream_t s);
 void launch_compact(const KP& p, cudaStream_t s);
 void launch_end(const KP& p, cudaStream_t s);

@@ -166,7 +166,7 @@ __global__ void __launch_bounds__(kBlock) k_na_update(NA p) {
         }
     }
     if (act) {
-        const St<double> cons = apply_flux64(R5(p.c.cons, n, i), facc, &err);
+        const St<double> cons = zero_kick64(apply_flux64(R5(p.c.cons, n, i), facc, &err));  // + kick2
         facc = st_zero<double>();
 #pragma unroll
         for (int q = 0; q < 5; q++) p.c.cons[q * n + i] = cons.q[q];

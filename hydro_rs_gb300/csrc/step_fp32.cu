@@ -575,7 +575,7 @@ __device__ __forceinline__ void gradients32_cell(const KP& p, int i) {
 #pragma unroll
             for (int q = 1; q < 4; q++) gr[q] = f32v(C3(p, F_GRAD + 3 * q, i));
           }
-            double dt_new = cell_timestep32(p, i, k, gr);
+            double dt_new = limit_by_gravity(p, i, cell_timestep32(p, i, k, gr));
             unsigned long long tc = p.tl[k].ti_current;
             unsigned long long dti = make_integer_timestep(dt_new, tb, NUM_TIME_BINS, tc, tbase_inv(p, k));
             if (dti == 0) err |= 1u << 6;
@@ -694,7 +694,7 @@ __device__ __forceinline__ void gradients32_cell_warp(const KP& p, int i, int la
             for (int q = 1; q < 4; q++) gr[q] = f32v(C3(p, F_GRAD + 3 * q, i));
           }
             if (lane == 0) {
-                double dt_new = cell_timestep32(p, i, k, gr);
+                double dt_new = limit_by_gravity(p, i, cell_timestep32(p, i, k, gr));
                 unsigned long long tc = p.tl[k].ti_current;
                 unsigned long long dti = make_integer_timestep(dt_new, tb, NUM_TIME_BINS, tc, tbase_inv(p, k));
                 if (dti == 0) err |= 1u << 6;

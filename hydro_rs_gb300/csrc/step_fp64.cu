@@ -488,7 +488,11 @@ __device__ __forceinline__ void update_finish(const KP& p, int i, int k, bool ac
     unsigned int err = 0;
     if (act) {
         p.fresh[i] = 0;  // prim (here), grad and v_rel (gradient stage) change
-        const St<double> cons = apply_flux64(C5(p, F_CONS, i), facc, &err);
+        St<double> cons = apply_flux64(C5(p, F_CONS, i), facc, &err);
+        // kick2 (runner/hydrodynamics.rs:51-57); accelerations only where the
+        // external potential's are computed (at the runner's "TODO: gravity")
+        cons = p.grav_acc ? grav_kick64(cons, C(p, F_DT, i), grav_acceleration(p, C3(p, F_LOC, i)))
+                          : zero_kick64(cons);
         facc = st_zero<double>();
         W5(p, F_CONS, i, cons);
         W(p, F_MSV, i, msv);
@@ -710,7 +714,7 @@ __device__ __forceinline__ void gradients_cell(const KP& p, int i, int do_timest
             W3(p, F_GC, i, cen);  // gradient_apply
           }
             if (do_timestep) {
-                double dt_new = particle_timestep(p, i);
+                double dt_new = limit_by_gravity(p, i, particle_timestep(p, i));
                 unsigned long long tc = p.tl[k].ti_current;
                 unsigned long long dti = make_integer_timestep(dt_new, tb, NUM_TIME_BINS, tc, tbase_inv(p, k));
                 if (dti == 0) err |= 1u << 6;
@@ -854,7 +858,7 @@ __device__ __forceinline__ void gradients_cell_warp(const KP& p, int i, int do_t
             if (lane == 0) W3(p, F_GC, i, cen);  // gradient_apply
           }
             if (do_timestep && lane == 0) {
-                double dt_new = particle_timestep(p, i);
+                double dt_new = limit_by_gravity(p, i, particle_timestep(p, i));
                 unsigned long long tc = p.tl[k].ti_current;
                 unsigned long long dti = make_integer_timestep(dt_new, tb, NUM_TIME_BINS, tc, tbase_inv(p, k));
                 if (dti == 0) err |= 1u << 6;
@@ -894,6 +898,20 @@ __global__ void __launch_bounds__(kMaxBlock) k_timesteps(KP p, double* out) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
     out[i] = p.active[i] ? particle_timestep(p, i) : INFINITY;
+}
+
+// GravitySolver::compute_timesteps (what < 0) or one component of
+// ExternalPotentialGravity::compute_accelerations (what = 0, 1, 2) for every
+// cell (gravity.rs:45-53, 67-73, 81-95, 110-136).
+__global__ void __launch_bounds__(kMaxBlock) k_gravity(KP p, int what, double* out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n) return;
+    if (what < 0) {
+        out[i] = grav_timestep(p, i);
+    } else {
+        const V3<double> a = grav_acceleration(p, C3(p, F_LOC, i));
+        out[i] = what == 0 ? a.x : what == 1 ? a.y : a.z;
+    }
 }
 
 // ------------------------------------------------- limiter / sync / end --
@@ -954,7 +972,11 @@ __device__ __forceinline__ void limit_cell(const KP& p, int i, int wakeup = -1) 
         }
         // kick1: grav_kick adds +0 to the momentum.  The update of this step
         // (kick2) already added +0 to it, and (x + 0) + 0 == x + 0 for every
-        // double x, so the row is left as the update wrote it.
+        // double x, so the row is left as the update wrote it; only where
+        // the external potential's accelerations are computed does it kick,
+        // over the new dt.
+        if (p.grav_acc)
+            W5(p, F_CONS, i, grav_kick64(C5(p, F_CONS, i), C(p, F_DT, i), grav_acceleration(p, C3(p, F_LOC, i))));
     }
 }
 __device__ __forceinline__ void end_instance(const KP& p, int k);
@@ -1181,6 +1203,9 @@ void launch_gradients(const KP& p, int do_timestep, cudaStream_t s) {
 }
 void launch_timesteps(const KP& p, double* dt_out, cudaStream_t s) {
     if (p.n > 0) k_timesteps<<<grid(p.n, p.blk_cell), p.blk_cell, 0, s>>>(p, dt_out);
+}
+void launch_gravity(const KP& p, int what, double* out, cudaStream_t s) {
+    if (p.n > 0) k_gravity<<<grid(p.n, p.blk_cell), p.blk_cell, 0, s>>>(p, what, out);
 }
 void launch_limit(const KP& p, cudaStream_t s) {
     if (p.n <= 0) return;

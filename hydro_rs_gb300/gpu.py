@@ -27,6 +27,7 @@ EXPORTED = (
     "mvmm_profile_read", "mvmm_riemann_flux", "mvmm_riemann_sample", "mvmm_get_stats",
     "mvmm_ctx_create_batched", "mvmm_batch_state", "mvmm_autotune", "mvmm_riemann_flux_p", "mvmm_riemann_sample_p",
     "mvmm_step_cells", "mvmm_drift", "mvmm_get_positions", "mvmm_set_mesh", "mvmm_flush_deferred",
+    "mvmm_gravity_timesteps", "mvmm_gravity_accelerations",
 )
 
 
@@ -43,7 +44,10 @@ class _Params(ctypes.Structure):
                 ("dimensionality", ctypes.c_int), ("sync_all", ctypes.c_int), ("t_end", ctypes.c_double),
                 ("max_newton_iter", ctypes.c_int), ("precision", ctypes.c_int), ("particle_motion", ctypes.c_int),
                 ("runner", ctypes.c_int), ("airs_threshold", ctypes.c_double),
-                ("advection_velocity", ctypes.c_double * 3), ("box_size", ctypes.c_double * 3)]
+                ("advection_velocity", ctypes.c_double * 3), ("box_size", ctypes.c_double * 3),
+                ("gravity", ctypes.c_int), ("gravity_softening", ctypes.c_double),
+                ("gravity_acceleration", ctypes.c_double * 3), ("gravity_position", ctypes.c_double * 3),
+                ("gravity_accelerations", ctypes.c_int)]
 
 
 def make_params(p, precision=None, box=(1.0, 1.0, 1.0)) -> _Params:
@@ -53,7 +57,7 @@ def make_params(p, precision=None, box=(1.0, 1.0, 1.0)) -> _Params:
     return _Params(p.gamma, p.eos, p.isothermal_internal_energy, p.cfl, p.riemann, p.boundary, p.dimensionality,
                    int(p.sync_all), p.t_end,
                    p.max_newton_iter, prec, p.particle_motion, p.runner, thr, (ctypes.c_double * 3)(*adv),
-                   (ctypes.c_double * 3)(*[float(b) for b in box]))
+                   (ctypes.c_double * 3)(*[float(b) for b in box]), *p.gravity_fields())
 
 
 _LIB = None
@@ -81,6 +85,8 @@ def load_library(path: str = LIB_PATH):
         "mvmm_compute_fluxes": (i32, [vp, vp, vp, pi64]),
         "mvmm_convert_conserved_to_primitive": (i32, [vp, vp]),
         "mvmm_compute_timesteps": (i32, [vp, vp, vp]),
+        "mvmm_gravity_timesteps": (i32, [vp, vp]),
+        "mvmm_gravity_accelerations": (i32, [vp, vp]),
         "mvmm_apply_fluxes": (i32, [vp, vp, vp]),
         "mvmm_gradients": (i32, [vp, vp]),
         "mvmm_step": (i32, [vp, u64, u64, pu64, pi64]),
@@ -366,4 +372,15 @@ class GpuSim:
         active = np.ascontiguousarray(active, dtype=np.uint8)
         out = np.zeros(self.mesh.n_cells)
         _check(load_library().mvmm_compute_timesteps(self.h, active.ctypes.data, out.ctypes.data), self.h)
+        return out
+
+    # ---- GravitySolver trait ----
+    def gravity_timesteps(self):
+        out = np.zeros(self.mesh.n_cells)
+        _check(load_library().mvmm_gravity_timesteps(self.h, out.ctypes.data), self.h)
+        return out
+
+    def gravity_accelerations(self):
+        out = np.zeros((3, self.mesh.n_cells))
+        _check(load_library().mvmm_gravity_accelerations(self.h, out.ctypes.data), self.h)
         return out

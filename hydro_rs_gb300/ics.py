@@ -10,6 +10,7 @@ seeded numpy generator (the reference's is one-sided and unseeded,
 """
 from __future__ import annotations
 
+import ctypes
 import math
 from dataclasses import dataclass, field
 
@@ -19,6 +20,8 @@ from .layout import Cells, Mesh
 from .mesh import mesh_1d, mesh_voronoi
 
 HLLC, EXACT, PVRS, AIRS, TSRS, TRRS, LINEAR_ADVECTION = 0, 1, 2, 3, 4, 5, 6
+# gravity.kind (bin/main.rs:643-662): none, self_gravity, external potential Constant / Keplerian
+GRAVITY_NONE, GRAVITY_SELF, GRAVITY_CONSTANT, GRAVITY_KEPLERIAN = 0, 1, 2, 3
 PERIODIC, REFLECTIVE, OPEN, VACUUM = 0, 1, 2, 3
 OPTIMAL_ORDER, GODUNOV = 0, 1
 # engine.particle_motion (engine.rs:7-13)
@@ -49,6 +52,21 @@ class Params:
     advection_velocity: tuple | None = None   # riemann_solver.velocity (required by LinearAdvection)
     eos: int = 0                              # 0 = EquationOfState::Ideal, 1 = Isothermal (gas_law.rs:59-63)
     isothermal_internal_energy: float = 0.0   # the Isothermal payload
+    # gravity solver (bin/main.rs:643-662): GRAVITY_* kind, softening_length,
+    # Potential::Constant acceleration, KeplerianPotential position, and whether
+    # the external potential's accelerations are computed at the runner's
+    # "TODO: gravity" point (the reference never computes them)
+    gravity: int = 0
+    gravity_softening: float = 0.0
+    gravity_acceleration: tuple = (0.0, 0.0, 0.0)
+    gravity_position: tuple = (0.0, 0.0, 0.0)
+    gravity_accelerations: bool = False
+
+    def gravity_fields(self):
+        """The gravity members of the C parameter structs, in order."""
+        return (int(self.gravity), float(self.gravity_softening),
+                (ctypes.c_double * 3)(*[float(x) for x in self.gravity_acceleration]),
+                (ctypes.c_double * 3)(*[float(x) for x in self.gravity_position]), int(self.gravity_accelerations))
 
     def solver_extras(self):
         """(threshold, velocity) as passed to the C structs; NaN marks a missing value."""

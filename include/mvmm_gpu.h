@@ -96,7 +96,22 @@ typedef struct mvmm_params {
     double airs_threshold;             /* AIRiemannSolver::new(threshold); NaN = missing */
     double advection_velocity[3];      /* LinearAdvectionRiemannSover::new(velocity) */
     double box_size[3];                /* Space::box_size; periodic wrap of drifted generators */
+    /* The gravity solver (bin/main.rs:643-662, gravity.rs).  The runners take
+     * its timestep per cell where smaller (optimal_order.rs:47-50,
+     * godunov.rs:41-44).  They never compute accelerations (the "TODO: gravity"
+     * at optimal_order.rs:33), so a_grav stays zero and the kicks kick2 / kick1
+     * add nothing; gravity_accelerations = 1 computes the external potential's
+     * accelerations at that point instead, and the kicks apply them
+     * (Particle::grav_kick, part.rs:303-312). */
+    int gravity;                     /* MVMM_GRAVITY_* */
+    double gravity_softening;        /* SelfGravity / KeplerianPotential softening_length */
+    double gravity_acceleration[3];  /* Potential::Constant acceleration */
+    double gravity_position[3];      /* KeplerianPotential position */
+    int gravity_accelerations;       /* 0: as the reference; 1: external potentials kick (not for
+                                        MVMM_GRAVITY_SELF, nor through mvmm_step_cells) */
 } mvmm_params;
+/* Gravity solver kind (bin/main.rs:643-662). */
+enum { MVMM_GRAVITY_NONE = 0, MVMM_GRAVITY_SELF = 1, MVMM_GRAVITY_CONSTANT = 2, MVMM_GRAVITY_KEPLERIAN = 3 };
 
 /* Cell state, SoA, n cells.  Row layout [components][n]; grad row 3*q+k is
  * d(quantity q)/d(axis k).  Mirrors Particle (part.rs:10-39). */
@@ -161,6 +176,16 @@ int mvmm_convert_conserved_to_primitive(mvmm_ctx *ctx, const uint8_t *active);
 /* compute_timesteps(&self, particles, part_is_active, motion, dim) -> Vec<f64>
  * (euler_eqns_fvs.rs:50-61); dt_out: host double[n] (INFINITY if inactive). */
 int mvmm_compute_timesteps(mvmm_ctx *ctx, const uint8_t *active, double *dt_out);
+
+/* ---- GravitySolver trait (gravity.rs:6-10) ----------------------------- */
+/* compute_timesteps(&self, particles) -> Vec<f64> (gravity.rs:45-53, 71-73,
+ * 90-95, 119-123): dt_out host double[n]; INFINITY where the solver sets no
+ * limit (self-gravity with zero accelerations, a constant potential). */
+int mvmm_gravity_timesteps(mvmm_ctx *ctx, double *dt_out);
+/* compute_accelerations(&self, particles) of ExternalPotentialGravity
+ * (gravity.rs:67-70, 81-86, 110-136): a_out host double[3][n].  Self-gravity
+ * returns MVMM_E_UNSUPPORTED. */
+int mvmm_gravity_accelerations(mvmm_ctx *ctx, double *a_out);
 
 /* ---- runner free functions (runner/hydrodynamics.rs) ----------------- */
 /* apply_fluxes + kick2 (runner/hydrodynamics.rs:13-39, 51-57); fluxes: host double[10][n_faces]. */

@@ -1096,6 +1096,50 @@ static double particle_timestep(particle *pt, double cfl, const gaslaw *eos, int
     return INFINITY;
 }
 
+/* --- gravity (gravity.rs) --- */
+/* KeplerianPotential::acceleration (gravity.rs:125-136) */
+static vec3 kepler_acceleration(const orc_params *p, vec3 pos) {
+    vec3 dx = vsub(pos, v3(p->gravity_position[0], p->gravity_position[1], p->gravity_position[2]));
+    double r2 = vdot(dx, dx);
+    double r = sqrt(r2);
+    if (r < p->gravity_softening) r2 = r2 + p->gravity_softening * p->gravity_softening;
+    double d = r * r2;
+    return v3(-dx.x / d, -dx.y / d, -dx.z / d);
+}
+/* KeplerianPotential::circular_velocity (gravity.rs:138-147) */
+static double kepler_circular_velocity(const orc_params *p, vec3 pos) {
+    vec3 dx = vsub(pos, v3(p->gravity_position[0], p->gravity_position[1], p->gravity_position[2]));
+    double r = sqrt(vdot(dx, dx));
+    double r_softened = r < p->gravity_softening ? r + p->gravity_softening : r;
+    return sqrt(1. / r_softened);
+}
+/* GravitySolver::compute_timesteps (gravity.rs:45-53, 71-73, 90-95, 119-123) */
+static double gravity_timestep(const orc_ctx *c, const particle *pt) {
+    switch (c->p.gravity) {
+        case ORC_GRAVITY_SELF: {
+            double a2 = vdot(pt->a_grav, pt->a_grav);
+            if (a2 == 0.) return INFINITY;
+            return sqrt(c->p.gravity_softening / sqrt(a2));
+        }
+        case ORC_GRAVITY_KEPLERIAN: /* eta = 0.5, radius in 2D whatever the dimensionality */
+            return 0.5 * radius(pt, 2) / kepler_circular_velocity(&c->p, pt->loc);
+        default:
+            return INFINITY;
+    }
+}
+/* ExternalPotentialGravity::compute_accelerations (gravity.rs:67-70, 81-86) */
+static void gravity_accelerations(orc_ctx *c) {
+    if (c->p.gravity != ORC_GRAVITY_CONSTANT && c->p.gravity != ORC_GRAVITY_KEPLERIAN) return;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < c->n; i++) {
+        particle *pt = &c->parts[i];
+        if (c->p.gravity == ORC_GRAVITY_CONSTANT)
+            pt->a_grav = v3(c->p.gravity_acceleration[0], c->p.gravity_acceleration[1], c->p.gravity_acceleration[2]);
+        else
+            pt->a_grav = kepler_acceleration(&c->p, pt->loc);
+    }
+}
+
 static void compute_timesteps(orc_ctx *c, const uint8_t *active, double *out) {
     uint32_t e = 0;
 #pragma omp parallel for schedule(static) reduction(| : e)
@@ -1104,6 +1148,25 @@ static void compute_timesteps(orc_ctx *c, const uint8_t *active, double *out) {
         out[i] = particle_timestep(&c->parts[i], c->p.cfl, &c->eos, c->p.dimensionality, c->p.particle_motion, &e);
     }
     c->err |= e;
+}
+/* The runners take the gravity solver's timestep per cell where it is smaller
+   (runner/hydrodynamics/optimal_order.rs:47-50, godunov.rs:41-44). */
+static void gravity_timestep_limit(orc_ctx *c, double *dts) {
+    if (c->p.gravity == ORC_GRAVITY_NONE) return;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < c->n; i++) dts[i] = fmin(dts[i], gravity_timestep(c, &c->parts[i]));
+}
+
+void orc_gravity_timesteps(orc_ctx *c, double *dt_out) {
+    for (int64_t i = 0; i < c->n; i++) dt_out[i] = gravity_timestep(c, &c->parts[i]);
+}
+void orc_gravity_accelerations(orc_ctx *c, double *a_out) {
+    gravity_accelerations(c);
+    for (int64_t i = 0; i < c->n; i++) {
+        a_out[i] = c->parts[i].a_grav.x;
+        a_out[c->n + i] = c->parts[i].a_grav.y;
+        a_out[2 * c->n + i] = c->parts[i].a_grav.z;
+    }
 }
 
 /* TimestepInfo helpers (engine.rs:55-80) */
@@ -1371,10 +1434,16 @@ uint64_t orc_step(orc_ctx *c, uint64_t ti_current, uint64_t ti_old, int64_t *n_a
     int64_t nf = compute_fluxes(c, c->active, c->fi);
     if (n_active_faces) *n_active_faces = nf;
     apply_fluxes(c, c->fi, c->active);
+    /* "TODO: gravity" (runner/hydrodynamics/optimal_order.rs:33): the
+       reference computes no accelerations here, so a_grav stays zero; with
+       gravity_accelerations set the external potential's accelerations are
+       computed at this point */
+    if (c->p.gravity_accelerations) gravity_accelerations(c);
     kick2(c, c->active);
     convert_c2p(c, c->active);
     if (c->p.runner != ORC_RUNNER_GODUNOV) gradients(c, c->active);
     compute_timesteps(c, c->active, c->dts);
+    gravity_timestep_limit(c, c->dts);
     uint64_t ti_next = ti_current + timesteps_apply(c, c->dts, c->active, ti_current);
     if (c->p.sync_all) timestep_sync(c, ti_current);
     else timestep_limiter(c, c->active, ti_current);
@@ -1439,6 +1508,7 @@ void orc_apply_fluxes(orc_ctx *c, const double *in, const uint8_t *active) {
         fi->a_over_r = in[9 * nf + f];
     }
     apply_fluxes(c, c->fi, active);
+    if (c->p.gravity_accelerations) gravity_accelerations(c);
     kick2(c, active);
 }
 

@@ -62,7 +62,16 @@ typedef struct orc_params {
     double advection_velocity[3]; /* LinearAdvectionRiemannSover::new(velocity) */
     int particle_motion;          /* ORC_MOTION_* (engine.rs:7-13) */
     double box_size[3];           /* Space::box_size (periodic wrap after a drift) */
+    /* gravity solver (bin/main.rs:643-662, gravity.rs) */
+    int gravity;                     /* ORC_GRAVITY_* */
+    double gravity_softening;        /* SelfGravity / KeplerianPotential softening_length */
+    double gravity_acceleration[3];  /* Potential::Constant acceleration */
+    double gravity_position[3];      /* KeplerianPotential position */
+    int gravity_accelerations;       /* 1: compute_accelerations at the runner's "TODO: gravity"
+                                        point (external potentials), 0: never (the reference) */
 } orc_params;
+
+enum { ORC_GRAVITY_NONE = 0, ORC_GRAVITY_SELF = 1, ORC_GRAVITY_CONSTANT = 2, ORC_GRAVITY_KEPLERIAN = 3 };
 
 /* SoA views; identical field meaning to the GPU library's mvmm_cells /
  * mvmm_mesh.  grad is [15][n] with row 3*q+k = d(quantity q)/d(axis k). */
@@ -84,6 +93,10 @@ typedef struct orc_mesh {
 typedef struct orc_ctx orc_ctx;
 
 orc_ctx *orc_create(const orc_params *p, const orc_mesh *m);
+/* GravitySolver::compute_timesteps / compute_accelerations (gravity.rs):
+ * dt_out [n]; a_out [3][n] (also stored as the cells' accelerations). */
+void orc_gravity_timesteps(orc_ctx *c, double *dt_out);
+void orc_gravity_accelerations(orc_ctx *c, double *a_out);
 void orc_destroy(orc_ctx *c);
 void orc_set_cells(orc_ctx *c, const orc_cells *in);
 void orc_get_cells(const orc_ctx *c, orc_cells *out);

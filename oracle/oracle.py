@@ -27,7 +27,10 @@ class _Params(ctypes.Structure):
                 ("dimensionality", ctypes.c_int), ("sync_all", ctypes.c_int), ("t_end", ctypes.c_double),
                 ("max_newton_iter", ctypes.c_int), ("n_threads", ctypes.c_int), ("runner", ctypes.c_int),
                 ("airs_threshold", ctypes.c_double), ("advection_velocity", ctypes.c_double * 3),
-                ("particle_motion", ctypes.c_int), ("box_size", ctypes.c_double * 3)]
+                ("particle_motion", ctypes.c_int), ("box_size", ctypes.c_double * 3),
+                ("gravity", ctypes.c_int), ("gravity_softening", ctypes.c_double),
+                ("gravity_acceleration", ctypes.c_double * 3), ("gravity_position", ctypes.c_double * 3),
+                ("gravity_accelerations", ctypes.c_int)]
 
 
 def build() -> str:
@@ -78,6 +81,8 @@ def lib():
         L.orc_cons_from_primitives.argtypes = [dbl, vp, dbl, vp]
         L.orc_prim_from_conserved.argtypes = [dbl, vp, dbl, vp]
         L.orc_exact_star.argtypes = [dbl] + [dbl] * 8 + [vp, ctypes.POINTER(ctypes.c_uint32)]
+        L.orc_gravity_timesteps.argtypes = [vp, vp]
+        L.orc_gravity_accelerations.argtypes = [vp, vp]
         _LIB = L
     return _LIB
 
@@ -97,7 +102,8 @@ class OracleSim:
         self._p = _Params(p.gamma, p.eos, p.isothermal_internal_energy, p.cfl, p.riemann, p.boundary,
                           p.dimensionality, int(p.sync_all),
                           p.t_end, p.max_newton_iter, n_threads, p.runner, thr, (ctypes.c_double * 3)(*adv),
-                          p.particle_motion, (ctypes.c_double * 3)(*[float(b) for b in problem.mesh.box]))
+                          p.particle_motion, (ctypes.c_double * 3)(*[float(b) for b in problem.mesh.box]),
+                          *p.gravity_fields())
         self._mv = self.mesh.cview()
         self.h = lib().orc_create(ctypes.byref(self._p), ctypes.byref(self._mv))
         self._cv = self.cells.cview()
@@ -187,6 +193,16 @@ class OracleSim:
         active = np.ascontiguousarray(active, dtype=np.uint8)
         out = np.zeros(self.mesh.n_cells)
         lib().orc_compute_timesteps(self.h, active.ctypes.data, out.ctypes.data)
+        return out
+
+    def gravity_timesteps(self):
+        out = np.zeros(self.mesh.n_cells)
+        lib().orc_gravity_timesteps(self.h, out.ctypes.data)
+        return out
+
+    def gravity_accelerations(self):
+        out = np.zeros((3, self.mesh.n_cells))
+        lib().orc_gravity_accelerations(self.h, out.ctypes.data)
         return out
 
 
