@@ -567,6 +567,51 @@ static __device__ __noinline__ bool ex_star_pre(ExSide l, ExSide r, double vl, d
     *p_out = p_guess;
     return fabs(p - p_guess) > 1e-6 * 0.5 * (p + p_guess) && fp_guess > 0.;
 }
+// The same in two parts, so that a face kernel can queue the Newton searches
+// as well as the Brent searches and each runs with full warps.  ex_star_start:
+// guess_p and the function values at 0 and at the guess (exact.rs:244-254);
+// returns which stage follows: EX_DONE (the pressure is the guess), EX_NEWTON
+// (the Newton loop from p = 0, exact.rs:255-275) or EX_BRENT (Brent's method
+// on [0, p_guess], exact.rs:278-283).  The tests are ex_star_pre's with p = 0.
+enum { EX_DONE = 0, EX_NEWTON = 1, EX_BRENT = 2 };
+static __device__ __noinline__ int ex_star_start(ExSide l, ExSide r, double vl, double vr, Gas<double> g,
+                                                 double* p_guess_out, double* fp_guess_out) {
+    const double p = 0.;
+    const double p_guess = ex_guess_p(l, r, vl, vr, g);
+    const double fp = ex_f(p, l, r, vl, vr, g);
+    const double fp_guess = ex_f(p_guess, l, r, vl, vr, g);
+    *p_guess_out = p_guess;
+    *fp_guess_out = fp_guess;
+    const bool apart = fabs(p - p_guess) > 1e-6 * 0.5 * (p + p_guess);
+    if (fp * fp_guess >= 0. && apart && fp_guess < 0.0) return EX_NEWTON;
+    return apart && fp_guess > 0. ? EX_BRENT : EX_DONE;
+}
+// The Newton loop of ex_star_pre from p = 0, p_guess, f(p_guess); returns true
+// where Brent's method must follow (on [0, *p_guess], f = *fp_guess), else the
+// pressure is *p_guess.
+static __device__ __noinline__ bool ex_newton(ExSide l, ExSide r, double vl, double vr, Gas<double> g, int max_iter,
+                                              unsigned int* err, double* p_guess_io, double* fp_guess_io) {
+    double p = 0.;
+    double p_guess = *p_guess_io;
+    double fp_guess = *fp_guess_io;
+    int counter = 0;
+    while (fabs(p - p_guess) > 1e-6 * 0.5 * (p + p_guess) && fp_guess < 0.0) {
+        p = p_guess;
+        const bool lo_left = l.p <= r.p;
+        const double d_lo = ex_fprimeb(p_guess, lo_left ? l : r, g);
+        const double d_hi = ex_fprimeb(p_guess, lo_left ? r : l, g);
+        p_guess = p_guess - fp_guess / ((lo_left ? d_lo : d_hi) + (lo_left ? d_hi : d_lo));
+        fp_guess = ex_f(p_guess, l, r, vl, vr, g);
+        counter += 1;
+        if (counter > max_iter) {  // the reference panics here
+            *err |= 1u;
+            break;
+        }
+    }
+    *p_guess_io = p_guess;
+    *fp_guess_io = fp_guess;
+    return fabs(p - p_guess) > 1e-6 * 0.5 * (p + p_guess) && fp_guess > 0.;
+}
 // Brent's method on [0, p_guess] as the reference calls it
 __device__ __forceinline__ double ex_star_brent(double p_guess, double fp_guess, const ExSide& l, const ExSide& r,
                                                 double vl, double vr, const Gas<double>& g, int max_iter,

@@ -260,7 +260,8 @@ __global__ void __launch_bounds__(kMaxBlock) k_face_flux(KP p) {
                 o = face_zero();
             } else if (SOLVER == SOLVER_EXACT && p.brent_jobs) {
                 // star_half_state (riemann_solver.rs:258-284) with the exact
-                // star solver, its Brent stage queued when it is needed
+                // star solver: its Newton and Brent stages are queued, each for
+                // a kernel of its own that finishes the face
                 double vl = dot(vel(q.l), q.n);
                 double vr = dot(vel(q.r), q.n);
                 double al = g.sound_speed(q.l.q[4], 1. / q.l.q[0]);
@@ -271,11 +272,15 @@ __global__ void __launch_bounds__(kMaxBlock) k_face_flux(KP p) {
                     F = flux_from_half_state(vacuum_sample(q.l, q.r, vl, vr, al, ar, q.n, g), q.iv, q.n, g);
                 } else {
                     ExSide L{q.l.q[0], q.l.q[4], al}, R{q.r.q[0], q.r.q[4], ar};
-                    double pst, pg, fpg;
-                    if (ex_star_pre(L, R, vl, vr, g, p.max_iter, &err, &pst, &pg, &fpg)) {
-                        const unsigned int slot = atomicAdd(p.brent_count, 1u);
+                    double pg, fpg;
+                    const int next = ex_star_start(L, R, vl, vr, g, &pg, &fpg);
+                    double pst = pg;
+                    if (next != EX_DONE) {
+                        // queue 0: Brent searches; queue 1: Newton searches
+                        const int qi = next == EX_NEWTON ? 1 : 0;
+                        const unsigned int slot = atomicAdd(p.brent_count + qi, 1u);
                         if (slot < (unsigned int)p.brent_cap) {
-                            BrentJob& J = reinterpret_cast<BrentJob*>(p.brent_jobs)[slot];
+                            BrentJob& J = reinterpret_cast<BrentJob*>(p.brent_jobs)[(size_t)qi * p.brent_cap + slot];
                             J.q = q;
                             J.vl = vl;
                             J.vr = vr;
@@ -287,7 +292,8 @@ __global__ void __launch_bounds__(kMaxBlock) k_face_flux(KP p) {
                             J.k = k;
                             queued = true;
                         } else {  // the queue is full: the search runs here
-                            pst = ex_star_brent(pg, fpg, L, R, vl, vr, g, p.max_iter, &err);
+                            const bool brent = next == EX_BRENT || ex_newton(L, R, vl, vr, g, p.max_iter, &err, &pg, &fpg);
+                            pst = brent ? ex_star_brent(pg, fpg, L, R, vl, vr, g, p.max_iter, &err) : pg;
                         }
                     }
                     if (!queued) F = exact_flux_from_p(pst, q, vl, vr, al, ar, g);
@@ -314,6 +320,27 @@ __global__ void __launch_bounds__(kMaxBlock) k_face_brent(KP p) {
         unsigned int err = 0;
         ExSide L{J.q.l.q[0], J.q.l.q[4], J.al}, R{J.q.r.q[0], J.q.r.q[4], J.ar};
         double pst = ex_star_brent(J.p_guess, J.fp_guess, L, R, J.vl, J.vr, g, p.max_iter, &err);
+        write_face(p, J.f, face_finish(J.q, exact_flux_from_p(pst, J.q, J.vl, J.vr, J.al, J.ar, g)));
+        if (err) set_err(p, J.k, err);
+    }
+}
+
+// The queued Newton searches (the second queue): every job runs the Newton
+// loop from the guess (exact.rs:255-275), then, where the loop ends above the
+// root, Brent's method as ex_star_pre's caller would, and finishes its face.
+// The lanes of a warp take the same steps: 2-3 Newton iterations each on the
+// nearly uniform states of a smooth flow.
+__global__ void __launch_bounds__(kMaxBlock) k_face_newton(KP p) {
+    const Gas<double> g = gas(p);
+    const unsigned int n_jobs = min(p.brent_count[1], (unsigned int)p.brent_cap);
+    const BrentJob* jobs = reinterpret_cast<const BrentJob*>(p.brent_jobs) + p.brent_cap;
+    for (unsigned int j = blockIdx.x * blockDim.x + threadIdx.x; j < n_jobs; j += gridDim.x * blockDim.x) {
+        const BrentJob J = jobs[j];
+        unsigned int err = 0;
+        ExSide L{J.q.l.q[0], J.q.l.q[4], J.al}, R{J.q.r.q[0], J.q.r.q[4], J.ar};
+        double pg = J.p_guess, fpg = J.fp_guess;
+        const bool brent = ex_newton(L, R, J.vl, J.vr, g, p.max_iter, &err, &pg, &fpg);
+        const double pst = brent ? ex_star_brent(pg, fpg, L, R, J.vl, J.vr, g, p.max_iter, &err) : pg;
         write_face(p, J.f, face_finish(J.q, exact_flux_from_p(pst, J.q, J.vl, J.vr, J.al, J.ar, g)));
         if (err) set_err(p, J.k, err);
     }
@@ -1168,9 +1195,10 @@ void launch_face_flux_fp64(const KP& p, int solver, cudaStream_t s) {
     int g = face_grid(p);
     if (solver == SOLVER_HLLC) k_face_flux<SOLVER_HLLC><<<g, p.blk_face, 0, s>>>(p);
     else if (solver == SOLVER_EXACT && p.brent_jobs) {
-        cudaMemsetAsync(p.brent_count, 0, sizeof(unsigned int), s);
+        cudaMemsetAsync(p.brent_count, 0, 2 * sizeof(unsigned int), s);
         k_face_flux<SOLVER_EXACT><<<g, p.blk_face, 0, s>>>(p);
         const int blk = 128, jobs_grid = (int)std::min<long long>((p.brent_cap + blk - 1) / blk, p.n_sms * 16LL);
+        k_face_newton<<<jobs_grid, blk, 0, s>>>(p);
         k_face_brent<<<jobs_grid, blk, 0, s>>>(p);
     } else if (solver == SOLVER_EXACT) k_face_flux<SOLVER_EXACT><<<g, p.blk_face, 0, s>>>(p);
     else if (solver == SOLVER_PVRS) k_face_flux<SOLVER_PVRS><<<g, p.blk_face, 0, s>>>(p);

@@ -85,8 +85,11 @@ def test_gravity_solver_entry_points(gpu_lib, case):
     if fin.any():
         assert rel_err(tg[fin], to[fin]) <= 1e-14
     ag, ao = gpu.gravity_accelerations(), orc.gravity_accelerations()
+    # a generator at the Keplerian centre gets -0 / 0 (gravity.rs:133-135), NaN on both sides
+    ok = np.isfinite(ao)
+    assert np.array_equal(np.isfinite(ag), ok)
     for a in range(3):
-        assert rel_err(ag[a], ao[a]) <= 1e-14, a
+        assert rel_err(ag[a][ok[a]], ao[a][ok[a]]) <= 1e-14, a
 
 
 def test_gravity_rejections(gpu_lib):
