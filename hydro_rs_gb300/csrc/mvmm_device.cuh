@@ -424,6 +424,15 @@ __device__ __forceinline__ double ex_f(double p, const ExSide& l, const ExSide& 
     const double t_hi = ex_fb(p, lo_left ? r : l, g);
     return (lo_left ? t_lo : t_hi) + (lo_left ? t_hi : t_lo) + (vr - vl);
 }
+// ex_f at p = 0, where a side with p_s > 0 takes the rarefaction branch with
+// (0 / p_s)^e = 0: its term is (2/(gamma-1)) a (0 - 1), the same bits without
+// the division and the power.
+__device__ __forceinline__ double ex_fb0(const ExSide& s, const Gas<double>& g) {
+    return gt0_64(s.p) ? g.tdgm1() * s.a * (0. - 1.) : ex_fb(0., s, g);
+}
+__device__ __forceinline__ double ex_f0(const ExSide& l, const ExSide& r, double vl, double vr, const Gas<double>& g) {
+    return ex_fb0(l, g) + ex_fb0(r, g) + (vr - vl);
+}
 __device__ __forceinline__ double ex_fprimeb(double p, const ExSide& s, const Gas<double>& g) {  // :37-45
     if (p > s.p) {
         double cap_a = g.tdgp1() / s.rho;
@@ -503,27 +512,22 @@ static __device__ __noinline__ double ex_brent(double lower, double upper, doubl
         // which every later iteration bisects too: with mflag set and c == b,
         // the test |b - c| < tol (b + c) / 2 chooses the midpoint whatever the
         // interpolant.  While each midpoint keeps fa's sign and does not
-        // undercut |fb|, b stays the answer and only a moves, so the run's
-        // midpoints follow from a and b alone.  They are formed without
-        // evaluating f, and f is evaluated at the last (closest to the root)
-        // only: f is increasing in p, so the earlier midpoints, farther from
-        // the root on a's side, have the same sign and a larger magnitude.
-        // Where that check fails the loop resumes as if the run had not been
-        // looked at.  Same iterates, same result, and about a quarter of the
-        // f evaluations where the guess lands above the root (the usual case
-        // for nearly uniform states, where the loop would otherwise bisect
-        // [0, p_guess] down to the tolerance, ~20 evaluations).
-        if (bisected && b_kept && !swapped) {
-            double a2 = a;
-            int k = 0;
-            while (fb != 0. && fabs(a2 - b) > tol * 0.5 * (a2 + b)) {
-                a2 = 0.5 * (a2 + b);
-                k++;
-            }
-            if (k > 0 && it + k <= 100 * max_iter) {
-                const double fl = ex_f(a2, l, r, vl, vr, g);
-                if (fl != 0. && !(fa * fl < 0.) && !(fabs(fl) < fabs(fb))) return b;
-            }
+        // undercut |fb|, b stays the answer and only a moves until the bracket
+        // is within the tolerance, and the loop returns b.  f is increasing in
+        // p, so that holds for every midpoint if it holds at one point closer
+        // to b on a's side than all of them: every midpoint is 0.5 (a_j + b)
+        // with |a_j - b| > tol (a_j + b) / 2 and a_j, b in [0, p_guess], so it
+        // lies more than tol b / 4 from b, and the point tol b / 8 from b
+        // towards a is closer.  f is evaluated there once; where the check
+        // fails the loop resumes as if the run had not been looked at.  Same
+        // iterates, same result, and the ~20 evaluations of the run (the usual
+        // case for nearly uniform states, whose guess lands above the root)
+        // become one.
+        if (bisected && b_kept && !swapped && fb != 0. && fabs(a - b) > tol * 0.5 * (a + b) &&
+            it + 64 <= 100 * max_iter) {
+            const double s_chk = b + copysign(0.125 * tol * fabs(b), a - b);
+            const double fl = ex_f(s_chk, l, r, vl, vr, g);
+            if (fl != 0. && !(fa * fl < 0.) && !(fabs(fl) < fabs(fb))) return b;
         }
     }
     return b;
@@ -543,7 +547,7 @@ static __device__ __noinline__ bool ex_star_pre(ExSide l, ExSide r, double vl, d
                                                 double* fp_guess_out) {
     double p = 0.;
     double p_guess = ex_guess_p(l, r, vl, vr, g);
-    double fp = ex_f(p, l, r, vl, vr, g);
+    double fp = ex_f0(l, r, vl, vr, g);  // p = 0
     double fp_guess = ex_f(p_guess, l, r, vl, vr, g);
     if (fp * fp_guess >= 0.) {
         int counter = 0;
@@ -575,13 +579,14 @@ static __device__ __noinline__ bool ex_star_pre(ExSide l, ExSide r, double vl, d
 // on [0, p_guess], exact.rs:278-283).  The tests are ex_star_pre's with p = 0.
 enum { EX_DONE = 0, EX_NEWTON = 1, EX_BRENT = 2 };
 static __device__ __noinline__ int ex_star_start(ExSide l, ExSide r, double vl, double vr, Gas<double> g,
-                                                 double* p_guess_out, double* fp_guess_out) {
+                                                 double* p_guess_out, double* fp_guess_out, double* fp0_out) {
     const double p = 0.;
     const double p_guess = ex_guess_p(l, r, vl, vr, g);
-    const double fp = ex_f(p, l, r, vl, vr, g);
+    const double fp = ex_f0(l, r, vl, vr, g);  // p = 0
     const double fp_guess = ex_f(p_guess, l, r, vl, vr, g);
     *p_guess_out = p_guess;
     *fp_guess_out = fp_guess;
+    *fp0_out = fp;
     const bool apart = fabs(p - p_guess) > 1e-6 * 0.5 * (p + p_guess);
     if (fp * fp_guess >= 0. && apart && fp_guess < 0.0) return EX_NEWTON;
     return apart && fp_guess > 0. ? EX_BRENT : EX_DONE;
@@ -617,8 +622,15 @@ __device__ __forceinline__ double ex_star_brent(double p_guess, double fp_guess,
                                                 double vl, double vr, const Gas<double>& g, int max_iter,
                                                 unsigned int* err) {
     double p = 0.;
-    double fp = ex_f(p, l, r, vl, vr, g);
+    double fp = ex_f0(l, r, vl, vr, g);  // p = 0
     return ex_brent(p, p_guess, fp, fp_guess, 1e-6, l, r, vl, vr, g, max_iter, err);
+}
+// The same with f(0) as ex_star_start formed it (the reference evaluates it
+// again here, on the same inputs: the same value)
+__device__ __forceinline__ double ex_star_brent0(double p_guess, double fp_guess, double fp0, const ExSide& l,
+                                                 const ExSide& r, double vl, double vr, const Gas<double>& g,
+                                                 int max_iter, unsigned int* err) {
+    return ex_brent(0., p_guess, fp0, fp_guess, 1e-6, l, r, vl, vr, g, max_iter, err);
 }
 // star_state_from_pstar (:214-238)
 __device__ __forceinline__ Star<double> ex_star_post(double p, const ExSide& l, const ExSide& r, double vl, double vr,

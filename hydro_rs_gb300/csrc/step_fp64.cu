@@ -211,7 +211,7 @@ __device__ __forceinline__ void write_face(const KP& p, int f, const FaceOut& o)
 // Riemann problem after the Newton stage and what the face's result needs.
 struct BrentJob {
     FacePre q;
-    double vl, vr, al, ar, p_guess, fp_guess;
+    double vl, vr, al, ar, p_guess, fp_guess, fp0;  // fp0 = f(0)
     int f, k;
 };
 // The exact solver's flux from the star pressure on (riemann_solver.rs:258-284,
@@ -272,8 +272,8 @@ __global__ void __launch_bounds__(kMaxBlock) k_face_flux(KP p) {
                     F = flux_from_half_state(vacuum_sample(q.l, q.r, vl, vr, al, ar, q.n, g), q.iv, q.n, g);
                 } else {
                     ExSide L{q.l.q[0], q.l.q[4], al}, R{q.r.q[0], q.r.q[4], ar};
-                    double pg, fpg;
-                    const int next = ex_star_start(L, R, vl, vr, g, &pg, &fpg);
+                    double pg, fpg, fp0;
+                    const int next = ex_star_start(L, R, vl, vr, g, &pg, &fpg, &fp0);
                     double pst = pg;
                     if (next != EX_DONE) {
                         // queue 0: Brent searches; queue 1: Newton searches
@@ -288,12 +288,13 @@ __global__ void __launch_bounds__(kMaxBlock) k_face_flux(KP p) {
                             J.ar = ar;
                             J.p_guess = pg;
                             J.fp_guess = fpg;
+                            J.fp0 = fp0;
                             J.f = f;
                             J.k = k;
                             queued = true;
                         } else {  // the queue is full: the search runs here
                             const bool brent = next == EX_BRENT || ex_newton(L, R, vl, vr, g, p.max_iter, &err, &pg, &fpg);
-                            pst = brent ? ex_star_brent(pg, fpg, L, R, vl, vr, g, p.max_iter, &err) : pg;
+                            pst = brent ? ex_star_brent0(pg, fpg, fp0, L, R, vl, vr, g, p.max_iter, &err) : pg;
                         }
                     }
                     if (!queued) F = exact_flux_from_p(pst, q, vl, vr, al, ar, g);
@@ -319,7 +320,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_face_brent(KP p) {
         const BrentJob J = jobs[j];
         unsigned int err = 0;
         ExSide L{J.q.l.q[0], J.q.l.q[4], J.al}, R{J.q.r.q[0], J.q.r.q[4], J.ar};
-        double pst = ex_star_brent(J.p_guess, J.fp_guess, L, R, J.vl, J.vr, g, p.max_iter, &err);
+        double pst = ex_star_brent0(J.p_guess, J.fp_guess, J.fp0, L, R, J.vl, J.vr, g, p.max_iter, &err);
         write_face(p, J.f, face_finish(J.q, exact_flux_from_p(pst, J.q, J.vl, J.vr, J.al, J.ar, g)));
         if (err) set_err(p, J.k, err);
     }
@@ -340,7 +341,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_face_newton(KP p) {
         ExSide L{J.q.l.q[0], J.q.l.q[4], J.al}, R{J.q.r.q[0], J.q.r.q[4], J.ar};
         double pg = J.p_guess, fpg = J.fp_guess;
         const bool brent = ex_newton(L, R, J.vl, J.vr, g, p.max_iter, &err, &pg, &fpg);
-        const double pst = brent ? ex_star_brent(pg, fpg, L, R, J.vl, J.vr, g, p.max_iter, &err) : pg;
+        const double pst = brent ? ex_star_brent0(pg, fpg, J.fp0, L, R, J.vl, J.vr, g, p.max_iter, &err) : pg;
         write_face(p, J.f, face_finish(J.q, exact_flux_from_p(pst, J.q, J.vl, J.vr, J.al, J.ar, g)));
         if (err) set_err(p, J.k, err);
     }
