@@ -668,6 +668,74 @@ def _serve_accuracy(srv, reqs, check_oracle: bool, n_check: int = 3):
     return out
 
 
+def run_batch_to_end(args):
+    """The batched configuration as named: every simulation of the batch run to
+    its t_end = 0.15, both forms from the same initial state, the whole run
+    timed (mvmm_run: one CUDA graph launch per batched step until every
+    simulation has finished or been stopped by a numerical failure).  The
+    forms are compared per simulation at t_end, the same simulated time."""
+    import torch
+
+    from hydro_rs_gb300 import gpu as G
+    from hydro_rs_gb300 import ics
+
+    ws, rank = _dist()
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    problem, mesh_s = _problem(args.nx, args.workload)
+    off, te = problem.extra["cell_offsets"], problem.extra["t_end"]
+    res = {}
+    with _Clocks() as clk:
+        for prec in (0, 1):
+            sim = G.GpuSim(problem, precision=prec, cell_offsets=off, t_end=te)
+            tuned = sim.autotune(3)  # block sizes on the live state, which it restores
+            f0 = sim.stats()["active_faces"]
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            try:
+                sim.run()
+            except G.MvmmError as e:  # stopped simulations are reported per instance
+                if e.code != -3:
+                    raise
+            torch.cuda.synchronize()
+            secs = time.perf_counter() - t0
+            st = sim.batch_state()
+            res[prec] = {"seconds": secs, "faces": sim.stats()["active_faces"] - f0, "state": st,
+                         "cells": ics.unpack_cells(sim.state(), off), "blocks": tuned}
+            sim.close()
+    clocks = clk.summary(0)
+    if rank != 0:
+        return
+    ok = (res[0]["state"]["err"] == 0) & (res[1]["state"]["err"] == 0)
+    l1 = []
+    for k in np.nonzero(ok)[0]:
+        a, b = res[1]["cells"][k].prim[0], res[0]["cells"][k].prim[0]
+        l1.append(float(np.abs(a - b).sum() / np.abs(b).sum()))
+    l1 = np.array(l1)
+
+    def form(prec):
+        r = res[prec]
+        return {"value": r["faces"] / r["seconds"], "unit": UNIT, "seconds": round(r["seconds"], 3),
+                "face_updates": int(r["faces"]), "max_steps": int(r["state"]["steps"].max()),
+                "finished": int(r["state"]["finished"].sum()), "flagged": int((r["state"]["err"] != 0).sum()),
+                "blocks_face_cell": r["blocks"]}
+
+    line = {
+        "metric": METRIC, "value": res[0]["faces"] / res[0]["seconds"], "unit": UNIT, "n_gpus": 1,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": DATA.get(args.workload, "synthetic, seeded"),
+        "config": {"workload": WORKLOADS[args.workload].format(n=args.nx) + ", the whole run",
+                   "cells": problem.mesh.n_cells, "faces": problem.mesh.n_faces, "precision": PRECISION_FP64,
+                   "mesh_build_s": round(mesh_s, 3), "timing": "wall clock around mvmm_run to completion"},
+        "fp64": form(0), "fp32_face": form(1),
+        "fp32_face_speedup": (res[1]["faces"] / res[1]["seconds"]) / (res[0]["faces"] / res[0]["seconds"]),
+        "l1_density_err_fp32_vs_fp64_at_t_end": {"instances": int(ok.sum()), "median": float(np.median(l1)),
+                                                 "max": float(np.max(l1))} if l1.size else None,
+        "same_flagged_instances": bool(np.array_equal(res[0]["state"]["err"] != 0, res[1]["state"]["err"] != 0)),
+        "clocks": clocks,
+    }
+    print(json.dumps(line))
+
+
 def run_moving(args):
     """Moving mesh (drift, a host Voronoi build every step, re-upload): each
     step drifts the generators on the device, reads them back, rebuilds the
@@ -806,6 +874,8 @@ def main():
                     help="kh2d (the headline), sod1d, blast3d (extra measurements)")
     ap.add_argument("--nx", type=int, default=None, help="lattice side / cell count (default per workload)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg (profiling runs)")
+    ap.add_argument("--to-end", action="store_true",
+                    help="batch workloads: time the whole run, every simulation to its t_end, in both forms")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.nx is None:
@@ -816,6 +886,8 @@ def main():
         run_serve(args)
     elif args.workload == "kh2d_moving":
         run_moving(args)
+    elif args.to_end and args.workload in ("batch1d", "batch1d_pvrs"):
+        run_batch_to_end(args)
     else:
         run_ours(args)
 

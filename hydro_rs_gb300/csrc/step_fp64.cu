@@ -310,13 +310,49 @@ __global__ void __launch_bounds__(kMaxBlock) k_face_flux(KP p) {
     }
 }
 
+// The queued searches run a tile of kJobTile jobs per block at a time, the
+// tile ordered by the branches f takes at the guess: for each side whether the
+// guess lies above its pressure (the shock branch of fb and fprimeb, else the
+// rarefaction branch with its power).  On the nearly uniform states of a smooth
+// flow the guess, the star pressure and both side pressures differ in their
+// last digits only, so which branches a face takes is close to random, and a
+// warp of unsorted faces would run both branches of every evaluation.  A tile
+// sorted by that key (a counting sort in shared memory) fills most warps with
+// faces that take the same branches; each face's arithmetic is unchanged.
+constexpr int kJobTile = 128;
+__device__ __forceinline__ int job_branch_key(const BrentJob& J) {
+    const double pl = J.q.l.q[4], pr = J.q.r.q[4];
+    const double lo = fmin(pl, pr), hi = fmax(pl, pr);
+    return (J.p_guess > lo ? 1 : 0) + (J.p_guess > hi ? 1 : 0);
+}
+// The index of the job this thread runs in the tile starting at base (or -1).
+__device__ __forceinline__ int sorted_job(const BrentJob* jobs, unsigned int base, unsigned int n_jobs, int* s_count,
+                                          int* s_order) {
+    const unsigned int j = base + threadIdx.x;
+    const int key = j < n_jobs ? job_branch_key(jobs[j]) : 3;
+    if (threadIdx.x < 4) s_count[threadIdx.x] = 0;
+    __syncthreads();
+    const int rank = atomicAdd(&s_count[key], 1);
+    __syncthreads();
+    int start = 0;
+    for (int k = 0; k < key; k++) start += s_count[k];
+    s_order[start + rank] = key < 3 ? (int)j : -1;
+    __syncthreads();
+    const int mine = s_order[threadIdx.x];
+    __syncthreads();  // the arrays are reused by the next tile
+    return mine;
+}
+
 // The queued Brent searches of the exact solver's faces, with full warps;
 // each job then finishes its face (star state, sample, flux) and writes its rows.
-__global__ void __launch_bounds__(kMaxBlock) k_face_brent(KP p) {
+__global__ void __launch_bounds__(kJobTile) k_face_brent(KP p) {
+    __shared__ int s_count[4], s_order[kJobTile];
     const Gas<double> g = gas(p);
     const unsigned int n_jobs = min(*p.brent_count, (unsigned int)p.brent_cap);
     const BrentJob* jobs = reinterpret_cast<const BrentJob*>(p.brent_jobs);
-    for (unsigned int j = blockIdx.x * blockDim.x + threadIdx.x; j < n_jobs; j += gridDim.x * blockDim.x) {
+    for (unsigned int base = blockIdx.x * kJobTile; base < n_jobs; base += gridDim.x * kJobTile) {
+        const int j = sorted_job(jobs, base, n_jobs, s_count, s_order);
+        if (j < 0) continue;
         const BrentJob J = jobs[j];
         unsigned int err = 0;
         ExSide L{J.q.l.q[0], J.q.l.q[4], J.al}, R{J.q.r.q[0], J.q.r.q[4], J.ar};
@@ -329,13 +365,14 @@ __global__ void __launch_bounds__(kMaxBlock) k_face_brent(KP p) {
 // The queued Newton searches (the second queue): every job runs the Newton
 // loop from the guess (exact.rs:255-275), then, where the loop ends above the
 // root, Brent's method as ex_star_pre's caller would, and finishes its face.
-// The lanes of a warp take the same steps: 2-3 Newton iterations each on the
-// nearly uniform states of a smooth flow.
-__global__ void __launch_bounds__(kMaxBlock) k_face_newton(KP p) {
+__global__ void __launch_bounds__(kJobTile) k_face_newton(KP p) {
+    __shared__ int s_count[4], s_order[kJobTile];
     const Gas<double> g = gas(p);
     const unsigned int n_jobs = min(p.brent_count[1], (unsigned int)p.brent_cap);
     const BrentJob* jobs = reinterpret_cast<const BrentJob*>(p.brent_jobs) + p.brent_cap;
-    for (unsigned int j = blockIdx.x * blockDim.x + threadIdx.x; j < n_jobs; j += gridDim.x * blockDim.x) {
+    for (unsigned int base = blockIdx.x * kJobTile; base < n_jobs; base += gridDim.x * kJobTile) {
+        const int j = sorted_job(jobs, base, n_jobs, s_count, s_order);
+        if (j < 0) continue;
         const BrentJob J = jobs[j];
         unsigned int err = 0;
         ExSide L{J.q.l.q[0], J.q.l.q[4], J.al}, R{J.q.r.q[0], J.q.r.q[4], J.ar};
@@ -1198,9 +1235,9 @@ void launch_face_flux_fp64(const KP& p, int solver, cudaStream_t s) {
     else if (solver == SOLVER_EXACT && p.brent_jobs) {
         cudaMemsetAsync(p.brent_count, 0, 2 * sizeof(unsigned int), s);
         k_face_flux<SOLVER_EXACT><<<g, p.blk_face, 0, s>>>(p);
-        const int blk = 128, jobs_grid = (int)std::min<long long>((p.brent_cap + blk - 1) / blk, p.n_sms * 16LL);
-        k_face_newton<<<jobs_grid, blk, 0, s>>>(p);
-        k_face_brent<<<jobs_grid, blk, 0, s>>>(p);
+        const int jobs_grid = (int)std::min<long long>((p.brent_cap + kJobTile - 1) / kJobTile, p.n_sms * 16LL);
+        k_face_newton<<<jobs_grid, kJobTile, 0, s>>>(p);
+        k_face_brent<<<jobs_grid, kJobTile, 0, s>>>(p);
     } else if (solver == SOLVER_EXACT) k_face_flux<SOLVER_EXACT><<<g, p.blk_face, 0, s>>>(p);
     else if (solver == SOLVER_PVRS) k_face_flux<SOLVER_PVRS><<<g, p.blk_face, 0, s>>>(p);
     else k_face_flux<SOLVER_EXTRA><<<g, p.blk_face, 0, s>>>(p);
