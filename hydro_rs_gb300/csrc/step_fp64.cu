@@ -672,6 +672,23 @@ __global__ void __launch_bounds__(kMaxBlock) k_c2p(KP p) {
 }
 
 // ------------------------------------------------------------ gradients --
+// LimiterData::limit_single_quantity (gradients.rs:85-91):
+// min(1, d_max / e_max, d_min / e_min), or 1 where an extrapolation bound is 0.
+// A ratio that is at least 1 cannot lower the minimum with 1, so its IEEE
+// division is skipped where that follows from a comparison (e_max > 0 and
+// d_max >= e_max; e_min < 0 and d_min <= e_min): in a smooth flow most cells are
+// not limited and take neither division.  The value is the same, NaN ratios
+// (which fmin passes over) included.
+__device__ __forceinline__ double limit_factor(double d_max, double d_min, double e_max, double e_min) {
+    if (e_max == 0. || e_min == 0.) return 1.;
+    const bool max_ge1 = e_max > 0. && d_max >= e_max;
+    const bool min_ge1 = e_min < 0. && d_min <= e_min;
+    if (max_ge1 && min_ge1) return 1.;
+    if (max_ge1) return m_min(1.0, d_min / e_min);
+    if (min_ge1) return m_min(1.0, d_max / e_max);
+    return m_min(1.0, m_min(d_max / e_max, d_min / e_min));
+}
+
 // gradient_estimate + gradient_limit + gradient_apply (runner/hydrodynamics.rs:67-143)
 // fused per cell; in step mode also compute_timesteps + timesteps_apply
 // (euler_eqns_fvs.rs:50-61, runner/hydrodynamics.rs:145-158) with block-level
@@ -772,7 +789,7 @@ __device__ __forceinline__ void gradients_cell(const KP& p, int i, int do_timest
             for (int q = 0; q < 5; q++) {
                 double d_max = mx.q[q] - prim.q[q];
                 double d_min = mn.q[q] - prim.q[q];
-                double alpha = (emx.q[q] == 0. || emn.q[q] == 0.) ? 1. : m_min(1.0, m_min(d_max / emx.q[q], d_min / emn.q[q]));
+                const double alpha = limit_factor(d_max, d_min, emx.q[q], emn.q[q]);
                 gr[q] = alpha * gr[q];
                 W3(p, F_GRAD + 3 * q, i, gr[q]);
             }
@@ -916,7 +933,7 @@ __device__ __forceinline__ void gradients_cell_warp(const KP& p, int i, int do_t
                 emx.q[q] = warp_max_d(emx.q[q]);
                 double d_max = mx.q[q] - prim.q[q];
                 double d_min = mn.q[q] - prim.q[q];
-                double alpha = (emx.q[q] == 0. || emn.q[q] == 0.) ? 1. : m_min(1.0, m_min(d_max / emx.q[q], d_min / emn.q[q]));
+                const double alpha = limit_factor(d_max, d_min, emx.q[q], emn.q[q]);
                 gr[q] = alpha * gr[q];
                 if (lane == 0) W3(p, F_GRAD + 3 * q, i, gr[q]);
             }
