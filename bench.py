@@ -267,7 +267,7 @@ FP64_DFMA_PER_SM_CLK = 2  # GB300: FP64 at 1/64 of the FP32 rate
 
 def face_stage_kernels(prec, all_cells, riemann=None):
     if prec == 0:
-        return "k_face_flux + k_face_brent" if riemann == 1 else "k_face_flux"
+        return "k_face_flux + k_face_newton + k_face_brent" if riemann == 1 else "k_face_flux"
     return "k_face_flux32" if all_cells else "k_prep32 + k_face_flux32"
 
 
@@ -566,10 +566,10 @@ def run_ours(args):
                       "roofline": roof(1), "step_roofline": step_roof(1, ms32 / args.steps)},
         "cpu_baseline": cpu,
         # per step, both forms timed: over all cells k_predict / k_predict32, face, update, gradients,
-        # limiter (5 + 5); the plain form's exact solver adds k_face_brent; hierarchical steps add
-        # k_compact to both and k_prep32 to the FP32 form, and each form's timed region ends with
-        # one k_extrap_flush
-        "gpu_launches": args.steps * ((5 + 5) + (1 if exact else 0) + (3 if hier else 0)) + (2 if hier else 0),
+        # limiter (5 + 5); the plain form's exact solver adds k_face_newton and k_face_brent;
+        # hierarchical steps add k_compact to both and k_prep32 to the FP32 form, and each form's
+        # timed region ends with one k_extrap_flush
+        "gpu_launches": args.steps * ((5 + 5) + (2 if exact else 0) + (3 if hier else 0)) + (2 if hier else 0),
         "clocks": clocks,
     }
     print(json.dumps(line))
