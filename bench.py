@@ -324,6 +324,7 @@ def run_ours(args):
     from hydro_rs_gb300 import ics
 
     problem, mesh_s = _problem(args.nx, args.workload)
+    problem.params.limiter_frame = args.limiter_frame
     nf, nc = problem.mesh.n_faces, problem.mesh.n_cells
     stream = torch.cuda.Stream()
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
@@ -550,6 +551,7 @@ def run_ours(args):
                    "cells": nc, "faces": nf, "precision": PRECISION_FP64,
                    "l2": "flushed (256 MB write) before each timed step", "parallelism": f"replicas x{ws}",
                    "mesh_build_s": round(mesh_s, 3),
+                   **({"limiter_frame": "flux_exchange's (not the reference's)"} if args.limiter_frame else {}),
                    "ctx_create_and_upload_s": {"fp64": round(ctx_s[0], 4), "fp32_face": round(ctx_s[1], 4)},
                    "blocks_face_cell": {"fp64": tuned.get(0), "fp32_face": tuned.get(1)}},
         "active_face_fraction": faces64 / (args.steps * nf * ws),
@@ -682,6 +684,7 @@ def run_batch_to_end(args):
     ws, rank = _dist()
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     problem, mesh_s = _problem(args.nx, args.workload)
+    problem.params.limiter_frame = args.limiter_frame
     off, te = problem.extra["cell_offsets"], problem.extra["t_end"]
     res = {}
     with _Clocks() as clk:
@@ -874,6 +877,8 @@ def main():
                     help="kh2d (the headline), sod1d, blast3d (extra measurements)")
     ap.add_argument("--nx", type=int, default=None, help="lattice side / cell count (default per workload)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg (profiling runs)")
+    ap.add_argument("--limiter-frame", type=int, default=0, choices=[0, 1],
+                    help="1: the cell-wise limiter's face offsets in flux_exchange's frame (not the reference's)")
     ap.add_argument("--to-end", action="store_true",
                     help="batch workloads: time the whole run, every simulation to its t_end, in both forms")
     args = ap.parse_args()

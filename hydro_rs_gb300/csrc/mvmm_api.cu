@@ -205,6 +205,7 @@ KP make_kp(mvmm_ctx* c, int stage, int flux_rows) {
     p.n_sms = c->n_sms > 0 ? c->n_sms : 1;
     p.grav = c->prm.gravity;
     p.grav_acc = c->prm.gravity_accelerations ? 1 : 0;
+    p.limiter_frame = c->prm.limiter_frame ? 1 : 0;
     p.grav_soft = c->prm.gravity_softening;
     for (int a = 0; a < 3; a++) {
         p.grav_avec[a] = c->prm.gravity_acceleration[a];

@@ -68,8 +68,8 @@ enum FaceGeom32 : int {
     GE_FCM = 9,   // 3: fc - 0.5 ((loc_l + loc_r) + s)         (interior)
     GE_N = 12,    // 3: n
     GE_DS = 15,   // 3: (cen_r + s) - cen_l; boundary: reflect(cen_l) - cen_l
-    GE_DL = 18,   // 3: (fc - cen_l) - s   (limiter extrapolation, left cell)
-    GE_DR = 21,   // 3: (fc - cen_r) + s   (limiter extrapolation, right cell)
+    GE_DL = 18,   // 3: (fc - cen_l) - s   (limiter extrapolation, left cell; fc - cen_l with limiter_frame)
+    GE_DR = 21,   // 3: (fc - cen_r) + s   (limiter extrapolation, right cell; (fc - cen_r) - s with limiter_frame)
     GE_W = 24,    // area / |ds|^2         (WLS weight)
     GE_A = 25,    // area
     kFaceGeom32 = 26
@@ -152,6 +152,7 @@ struct KP {
     // acceleration, Keplerian position
     int grav, grav_acc;
     double grav_soft, grav_avec[3], grav_pos[3];
+    int limiter_frame;       // 1: the cell-wise limiter's face offsets in flux_exchange's frame
     GasK gk;                 // gas-law constants
     RSx rsx;                 // Riemann solver kind and its settings
     int godunov;             // 1: GodunovHydroRunner (no gradients), 0: OptimalOrderRunner

@@ -190,13 +190,16 @@ __global__ void __launch_bounds__(kMaxBlock) k_geom32(KP p) {
         dx = (locr + s) - locl;
         fcm = fc - 0.5 * ((locl + locr) + s);
         ds = (cenr + s) - cenl;
-        dr = (fc - cenr) + s;
+        // the right cell's limiter offset: the reference's (fc - cen_r) + s, or with
+        // limiter_frame flux_exchange's (fc - cen_r) - s
+        dr = p.limiter_frame ? (fc - cenr) - s : (fc - cenr) + s;
     } else {
         // Particle::reflect (part.rs:374-383) of the cell's position and centroid
         dx = (2. * dot(fc - locl, n)) * n;
         ds = (2. * dot(fc - cenl, n)) * n;
     }
-    V3<double> vals[8] = {fc - locl, rr, dx, fcm, n, ds, (fc - cenl) - s, dr};
+    const V3<double> dl = p.limiter_frame ? fc - cenl : (fc - cenl) - s;  // the left cell's
+    V3<double> vals[8] = {fc - locl, rr, dx, fcm, n, ds, dl, dr};
     float* g = p.geo;
     const size_t nf = (size_t)p.nf;
 #pragma unroll

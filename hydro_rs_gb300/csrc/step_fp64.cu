@@ -672,6 +672,18 @@ __global__ void __launch_bounds__(kMaxBlock) k_c2p(KP p) {
 }
 
 // ------------------------------------------------------------ gradients --
+// The cell-wise limiter's extrapolation from cell i to face f (sh: the face
+// shift as seen from i, other_side).  The reference's offset is face centroid -
+// centroid - sh (runner/hydrodynamics.rs:119); with limiter_frame set it is taken
+// in flux_exchange's frame (flux.rs:33-35), where the face centroid is the left
+// cell's: face centroid - centroid for the left cell, + sh (that is, - shift)
+// for the right one.
+__device__ __forceinline__ V3<double> limiter_offset(const KP& p, int i, int f, V3<double> cen, V3<double> sh) {
+    const V3<double> d = F3(p.fcen, p.nf, f) - cen;
+    if (!p.limiter_frame) return d - sh;
+    return i == p.left[f] ? d : d + sh;
+}
+
 // LimiterData::limit_single_quantity (gradients.rs:85-91):
 // min(1, d_max / e_max, d_min / e_min), or 1 where an extrapolation bound is 0.
 // A ratio that is at least 1 cannot lower the minimum with 1, so its IEEE
@@ -775,7 +787,7 @@ __device__ __forceinline__ void gradients_cell(const KP& p, int i, int do_timest
                 St<double> op;
                 V3<double> oc, sh;
                 other_side(p, i, f, prim, cen, op, oc, sh);
-                V3<double> d = (F3(p.fcen, p.nf, f) - cen) - sh;
+                V3<double> d = limiter_offset(p, i, f, cen, sh);
 #pragma unroll
                 for (int q = 0; q < 5; q++) {
                     double ex = dot(gr[q], d);
@@ -915,7 +927,7 @@ __device__ __forceinline__ void gradients_cell_warp(const KP& p, int i, int do_t
                 St<double> op;
                 V3<double> oc, sh;
                 other_side(p, i, f, prim, cen, op, oc, sh);
-                V3<double> d = (F3(p.fcen, p.nf, f) - cen) - sh;
+                V3<double> d = limiter_offset(p, i, f, cen, sh);
 #pragma unroll
                 for (int q = 0; q < 5; q++) {
                     double ex = dot(gr[q], d);

@@ -47,7 +47,7 @@ class _Params(ctypes.Structure):
                 ("advection_velocity", ctypes.c_double * 3), ("box_size", ctypes.c_double * 3),
                 ("gravity", ctypes.c_int), ("gravity_softening", ctypes.c_double),
                 ("gravity_acceleration", ctypes.c_double * 3), ("gravity_position", ctypes.c_double * 3),
-                ("gravity_accelerations", ctypes.c_int)]
+                ("gravity_accelerations", ctypes.c_int), ("limiter_frame", ctypes.c_int)]
 
 
 def make_params(p, precision=None, box=(1.0, 1.0, 1.0)) -> _Params:

@@ -61,12 +61,18 @@ class Params:
     gravity_acceleration: tuple = (0.0, 0.0, 0.0)
     gravity_position: tuple = (0.0, 0.0, 0.0)
     gravity_accelerations: bool = False
+    # 1: the cell-wise limiter's face offsets in flux_exchange's frame instead of
+    # the reference's (runner/hydrodynamics.rs:119, which across a periodic seam
+    # are a box length long); not the reference's arithmetic
+    limiter_frame: int = 0
 
     def gravity_fields(self):
-        """The gravity members of the C parameter structs, in order."""
+        """The members of the C parameter structs after box_size, in order: the
+        gravity solver's, then limiter_frame."""
         return (int(self.gravity), float(self.gravity_softening),
                 (ctypes.c_double * 3)(*[float(x) for x in self.gravity_acceleration]),
-                (ctypes.c_double * 3)(*[float(x) for x in self.gravity_position]), int(self.gravity_accelerations))
+                (ctypes.c_double * 3)(*[float(x) for x in self.gravity_position]), int(self.gravity_accelerations),
+                int(self.limiter_frame))
 
     def solver_extras(self):
         """(threshold, velocity) as passed to the C structs; NaN marks a missing value."""

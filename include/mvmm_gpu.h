@@ -109,6 +109,15 @@ typedef struct mvmm_params {
     double gravity_position[3];      /* KeplerianPotential position */
     int gravity_accelerations;       /* 0: as the reference; 1: external potentials kick (not for
                                         MVMM_GRAVITY_SELF, nor through mvmm_step_cells) */
+    /* The cell-wise limiter's extrapolation to a face.  0 (the reference,
+     * runner/hydrodynamics.rs:119): face centroid - centroid - shift for the
+     * left cell, + shift for the right one.  flux_exchange puts the face
+     * centroid in the left cell's frame (flux.rs:33-35), so across a periodic
+     * seam those offsets are a box length long and the limiter misbehaves
+     * there (a shear layer stops advancing its time).  1: the offsets in
+     * flux_exchange's frame, face centroid - centroid (left) and face centroid
+     * - shift - centroid (right); not the reference's arithmetic. */
+    int limiter_frame;
 } mvmm_params;
 /* Gravity solver kind (bin/main.rs:643-662). */
 enum { MVMM_GRAVITY_NONE = 0, MVMM_GRAVITY_SELF = 1, MVMM_GRAVITY_CONSTANT = 2, MVMM_GRAVITY_KEPLERIAN = 3 };

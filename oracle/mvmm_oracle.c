@@ -1002,7 +1002,13 @@ static void gradients(orc_ctx *c, const uint8_t *active) {
         for (int32_t k = c->csr_off[i]; k < c->csr_off[i + 1]; k++) {
             const face *f = &c->faces[c->csr_face[k]];
             vec3 shift = (i == f->left) ? f->shift : v3(-f->shift.x, -f->shift.y, -f->shift.z);
-            state ex = gr_dot(g, vsub(vsub(f->centroid, centroid), shift));
+            /* the reference's offset: face centroid - centroid - shift (runner/hydrodynamics.rs:119); with
+               limiter_frame set, the frame flux_exchange uses (flux.rs:33-35): the face centroid is in the
+               left cell's frame, so the right cell's offset is face centroid - shift - centroid */
+            vec3 off = vsub(f->centroid, centroid);
+            if (!c->p.limiter_frame) off = vsub(off, shift);
+            else if (i != f->left) off = vadd(off, shift);
+            state ex = gr_dot(g, off);
             state op;
             if (f->left == i && f->right < 0) {
                 particle o = boundary_part(c, pt, f);

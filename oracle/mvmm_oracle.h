@@ -69,6 +69,7 @@ typedef struct orc_params {
     double gravity_position[3];      /* KeplerianPotential position */
     int gravity_accelerations;       /* 1: compute_accelerations at the runner's "TODO: gravity"
                                         point (external potentials), 0: never (the reference) */
+    int limiter_frame;               /* 0: the reference's cell-wise limiter offsets; 1: flux_exchange's frame */
 } orc_params;
 
 enum { ORC_GRAVITY_NONE = 0, ORC_GRAVITY_SELF = 1, ORC_GRAVITY_CONSTANT = 2, ORC_GRAVITY_KEPLERIAN = 3 };

@@ -30,7 +30,7 @@ class _Params(ctypes.Structure):
                 ("particle_motion", ctypes.c_int), ("box_size", ctypes.c_double * 3),
                 ("gravity", ctypes.c_int), ("gravity_softening", ctypes.c_double),
                 ("gravity_acceleration", ctypes.c_double * 3), ("gravity_position", ctypes.c_double * 3),
-                ("gravity_accelerations", ctypes.c_int)]
+                ("gravity_accelerations", ctypes.c_int), ("limiter_frame", ctypes.c_int)]
 
 
 def build() -> str:
