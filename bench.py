@@ -259,10 +259,10 @@ def face_stage_bytes(prec, nc, nfa, all_cells):
 STEP_BYTES_FACE = 88
 STEP_BYTES_CELL = {0: 800, 1: 636}
 
-# FP64 flop per face of the plain face kernel (2 DFMA + DMUL + DADD, active
-# threads) from an ncu capture at the bench size: profiles/face_flux_fp64_pipes_kh256.txt.
-FP64_FLOP_PER_FACE = {("kh2d", 256): 1610}
-FP64_DFMA_PER_SM_CLK = 2  # GB300: FP64 at 1/64 of the FP32 rate
+# FP64 flop per face of the plain face stage (k_face_flux + k_face_newton +
+# k_face_brent; 2 DFMA + DMUL + DADD over active threads) from an ncu capture
+# at the bench size: profiles/face_stage_fp64_exact_pipes_kh256.txt.
+FP64_FLOP_PER_FACE = {("kh2d", 256): 1483}
 
 
 def face_stage_kernels(prec, all_cells, riemann=None):
