@@ -117,6 +117,10 @@ struct mvmm_ctx {
     int8_t* snap_tb = nullptr;
     unsigned long long* xfer_stored = nullptr;  // device: bytes stored by copies that skip unchanged chunks
     int64_t host_bytes_in = 0, host_bytes_out = 0;
+    // mvmm_step_cells_changed: 1 for cells a kernel rewrote since their rows
+    // were last stored (KP::dirty), and the listed cells' indices
+    uint8_t* dirty = nullptr;
+    int* chg_list = nullptr;
 };
 
 // Largest Brent queue of the plain exact-solver face kernel (jobs beyond it
@@ -206,6 +210,7 @@ KP make_kp(mvmm_ctx* c, int stage, int flux_rows) {
     p.grav = c->prm.gravity;
     p.grav_acc = c->prm.gravity_accelerations ? 1 : 0;
     p.limiter_frame = c->prm.limiter_frame ? 1 : 0;
+    p.dirty = c->dirty;
     p.grav_soft = c->prm.gravity_softening;
     for (int a = 0; a < 3; a++) {
         p.grav_avec[a] = c->prm.gravity_acceleration[a];
@@ -664,7 +669,7 @@ int mvmm_ctx_destroy(mvmm_ctx* c) {
     drop_graphs(c);
     void* ptrs[] = {c->left, c->right, c->csr_off, c->csr_face, c->area, c->normal, c->fcen, c->shift, c->cd,
                     c->cf, c->timebin, c->tb_tmp, c->active, c->flux, c->flux32, c->geo, c->geo_pos, c->geo_changed, c->snap, c->snap_tb, c->xfer_stored, c->brent_jobs, c->brent_count, c->extrap_step, c->dt_log, c->dtmp, c->face_stamp, c->touch, c->blocks_done, c->cell_list, c->fresh, c->cf_fresh,
-                    c->pend_vol, c->pend_cen,
+                    c->pend_vol, c->pend_cen, c->dirty, c->chg_list,
                     c->face_list, c->tl,
                     c->inst, c->inst_tb, c->inst_tbi};
     for (void* p : ptrs)
@@ -1131,6 +1136,167 @@ int mvmm_step_cells(mvmm_ctx* c, const mvmm_cells* in, mvmm_cells* out, uint64_t
         std::memmove(r.dst, r.src, r.len * sizeof(double));
     }
     rc = finish(c);
+    if (ti_next) *ti_next = c->tl_host->ti_current;
+    if (n_active_faces) *n_active_faces = (int64_t)(c->tl_host->active_faces - c->tl_host->faces_mark);
+    return rc;
+}
+
+}  // extern "C"
+
+namespace {
+// ---- host-resident state moved where it changes -------------------------
+// The host rows of mvmm_cells at the addresses the device reaches them by:
+// row r of the device block (r < F_SRC, the block's field order) and the
+// time bins.
+struct HostRows {
+    double* row[F_SRC];
+    int8_t* tb;
+};
+// volume, loc and centroid: a step of a fixed mesh never writes them
+constexpr int kKeptFirst = F_VOL, kKeptEnd = F_V;
+constexpr long long kStoredCellBytes = (long long)(F_SRC - (kKeptEnd - kKeptFirst)) * 8 + 1;
+
+int host_rows(mvmm_ctx* c, const mvmm_cells* h, HostRows* out) {
+    RowCopy map[14];
+    size_t m = 0;
+    int rc = row_map(h, kAllRows, map, &m);
+    if (rc) return rc;
+    const size_t n = (size_t)c->n;
+    auto view = [&](const void* p, size_t bytes) -> char* {
+        bool pinned = false, pinned_end = false;
+        const char* v = (const char*)device_view(c, p, &pinned);
+        if (v && (const char*)device_view(c, (const char*)p + bytes - 1, &pinned_end) != v + bytes - 1) v = nullptr;
+        return (char*)v;
+    };
+    const char* why = "mvmm_step_cells_changed: the device cannot address a cell array (pin it)";
+    for (size_t k = 0; k < m; k++) {
+        double* v = (double*)view(map[k].host, (size_t)map[k].rows * n * 8);
+        if (!v) return fail(MVMM_E_UNSUPPORTED, why);
+        for (int j = 0; j < map[k].rows; j++) out->row[map[k].field + j] = v + (size_t)j * n;
+    }
+    out->tb = (int8_t*)view(h->timebin, n);
+    if (!out->tb) return fail(MVMM_E_UNSUPPORTED, why);
+    return MVMM_OK;
+}
+
+// The listed cells' rows (blockIdx.y: the row, F_SRC the time bin) from the
+// host arrays.  Their derived rows are recomputed by the next predict, and no
+// deferred extrapolation is pending for them.  Indices were checked on the host.
+__global__ void __launch_bounds__(256) k_gather_cells(HostRows h, const int* __restrict__ list, int m, KP p) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= m) return;
+    const int i = list[j];
+    const int r = blockIdx.y;
+    if (r < F_SRC) {
+        p.cd[(size_t)r * p.n + i] = h.row[r][i];
+    } else {
+        p.timebin[i] = h.tb[i];
+        p.fresh[i] = 0;
+        if (p.cf_fresh) p.cf_fresh[i] = 0;
+        if (p.extrap_step) p.extrap_step[i] = (unsigned int)p.tl[0].steps;
+    }
+}
+
+// Rows [A, B) of cell i to the host, eight loads in flight before their stores.
+template <int A, int B>
+__device__ __forceinline__ void store_rows(const HostRows& h, const double* __restrict__ cd, size_t n, int i) {
+#pragma unroll
+    for (int r0 = A; r0 < B; r0 += 8) {
+        double v[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+            if (r0 + u < B) v[u] = cd[(size_t)(r0 + u) * n + i];
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+            if (r0 + u < B) h.row[r0 + u][i] = v[u];
+    }
+}
+
+// Stores the rows of the cells a kernel marked since the last store, a warp
+// per 32 consecutive cells (whole 256-byte segments of each row) wherever one
+// of them is marked, and clears the marks; counts the bytes into the timeline.
+__global__ void __launch_bounds__(256) k_store_dirty(HostRows h, KP p) {
+    const int lane = threadIdx.x & 31;
+    const int n_warps = (int)((gridDim.x * blockDim.x) >> 5);
+    const int groups = (p.n + 31) >> 5;
+    for (int w = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); w < groups; w += n_warps) {
+        const int i = (w << 5) + lane;
+        const bool in = i < p.n;
+        if (!__any_sync(0xffffffffu, in && p.dirty[i])) continue;
+        if (in) {
+            store_rows<0, kKeptFirst>(h, p.cd, (size_t)p.n, i);
+            store_rows<kKeptEnd, F_SRC>(h, p.cd, (size_t)p.n, i);
+            h.tb[i] = p.timebin[i];
+            p.dirty[i] = 0;
+        }
+        if (lane == 0) {
+            const int cells = min(32, p.n - (w << 5));
+            atomicAdd(&p.tl[0].host_stored, (unsigned long long)cells * (unsigned long long)kStoredCellBytes);
+        }
+    }
+}
+}  // namespace
+
+extern "C" {
+
+int mvmm_step_cells_changed(mvmm_ctx* c, mvmm_cells* cells, const int32_t* changed, int64_t n_changed,
+                            uint64_t ti_current, uint64_t ti_old, uint64_t* ti_next, int64_t* n_active_faces,
+                            int64_t* bytes_stored) {
+    if (!c || !cells) return fail(MVMM_E_INVALID, "null argument");
+    if (c->n_inst != 1) return fail(MVMM_E_UNSUPPORTED, "mvmm_step_cells_changed steps a single simulation");
+    if (c->prm.particle_motion != MVMM_MOTION_FIXED)
+        return fail(MVMM_E_UNSUPPORTED, "mvmm_step_cells_changed steps a fixed mesh");
+    if (cells->n != c->n) return fail(MVMM_E_INVALID, "cell count does not match the mesh");
+    if (changed && (n_changed < 0 || n_changed > c->n))
+        return fail(MVMM_E_INVALID, "n_changed must lie in [0, n_cells]");
+    if (changed)
+        for (int64_t k = 0; k < n_changed; k++)
+            if (changed[k] < 0 || changed[k] >= c->n) return fail(MVMM_E_INVALID, "changed: cell index out of range");
+    HostRows h;
+    int rc = host_rows(c, cells, &h);
+    if (rc) return rc;
+    cudaStream_t s = c->stream;
+    if (!c->dirty) {
+        if (cudaMalloc((void**)&c->dirty, (size_t)c->n) != cudaSuccess ||
+            cudaMalloc((void**)&c->chg_list, (size_t)c->n * 4) != cudaSuccess)
+            return fail(MVMM_E_NOMEM, "mvmm_step_cells_changed: cudaMalloc failed");
+        CUDA_TRY(cudaMemsetAsync(c->dirty, 0, (size_t)c->n, s));
+        drop_graphs(c);  // the captured kernels' parameters now carry the marks
+    }
+    launch_set_time(make_kp(c, 0, 7), ti_current, ti_old, s);
+    CUDA_TRY(cudaMemsetAsync(&c->tl->host_stored, 0, sizeof(unsigned long long), s));
+    if (!changed) {
+        // every cell: the arrays become the device's mirror
+        rc = copy_cells(c, cells, kAllRows, true, cudaMemcpyHostToDevice, s);
+        if (rc) return rc;
+        rc = sync_extrap(c, true, s);
+        if (rc) return rc;
+        rc = refresh_geometry(c, s);
+        if (rc) return rc;
+        CUDA_TRY(cudaMemsetAsync(c->dirty, 0, (size_t)c->n, s));
+    } else if (n_changed > 0) {
+        CUDA_TRY(cudaMemcpyAsync(c->chg_list, changed, (size_t)n_changed * 4, cudaMemcpyHostToDevice, s));
+        const KP p = make_kp(c, 0, 7);
+        k_gather_cells<<<dim3((unsigned)((n_changed + 255) / 256), F_SRC + 1), 256, 0, s>>>(h, c->chg_list,
+                                                                                          (int)n_changed, p);
+        CUDA_TRY(cudaGetLastError());
+        update_geom32(c, p, s);  // the faces of cells whose position or centroid changed
+        CUDA_TRY(cudaGetLastError());
+        c->host_bytes_in += n_changed * ((int64_t)F_SRC * 8 + 1);
+    }
+    rc = enqueue_steps_impl(c, 1);
+    if (rc) return rc;
+    // the deferred extrapolations are made (and marked where their bits change),
+    // so that the host rows hold the state after the step
+    rc = sync_extrap(c, false, s);
+    if (rc) return rc;
+    const long long blocks = std::min<long long>(((long long)c->n + 255) / 256, 16LL * c->n_sms);
+    k_store_dirty<<<(unsigned)blocks, 256, 0, s>>>(h, make_kp(c, 0, 7));
+    CUDA_TRY(cudaGetLastError());
+    rc = finish(c);
+    const unsigned long long stored = c->tl_host->host_stored;
+    c->host_bytes_out += (int64_t)stored;
+    if (bytes_stored) *bytes_stored = (int64_t)stored;
     if (ti_next) *ti_next = c->tl_host->ti_current;
     if (n_active_faces) *n_active_faces = (int64_t)(c->tl_host->active_faces - c->tl_host->faces_mark);
     return rc;

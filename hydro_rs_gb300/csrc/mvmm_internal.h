@@ -91,6 +91,7 @@ struct DevTimeline {
     unsigned int n_list;                // length of this step's active-face list (hierarchical steps)
     unsigned int n_clist;               // length of this step's cell list (hierarchical steps)
     unsigned long long faces_mark;      // active_faces when the time was last set on the device
+    unsigned long long host_stored;     // bytes the current mvmm_step_cells_changed call stored into host arrays
 };
 
 // Steps of dt kept for the deferred extrapolations of hierarchical steps; every
@@ -153,6 +154,8 @@ struct KP {
     int grav, grav_acc;
     double grav_soft, grav_avec[3], grav_pos[3];
     int limiter_frame;       // 1: the cell-wise limiter's face offsets in flux_exchange's frame
+    uint8_t* dirty;          // or null: 1 for cells whose host rows a kernel rewrote since the
+                             //   last mvmm_step_cells_changed stored them (that call's copies back)
     GasK gk;                 // gas-law constants
     RSx rsx;                 // Riemann solver kind and its settings
     int godunov;             // 1: GodunovHydroRunner (no gradients), 0: OptimalOrderRunner

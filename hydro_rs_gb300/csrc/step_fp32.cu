@@ -119,6 +119,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_predict32(KP p) {
 #pragma unroll
         for (int q = 0; q < 5; q++) ex.q[q] = pos ? ex.q[q] + (-dt) * f64(src.q[q]) : ex.q[q] + 0.;
         W5(p, F_EXTRAP, i, ex);
+        mark_dirty(p, i);
         if (reset) W5(p, F_PRIM, i, st_zero<double>());
         const bool live = pos && !reset;  // the checked density is positive
 #pragma unroll
@@ -477,6 +478,7 @@ __device__ __forceinline__ void gradients32_cell(const KP& p, int i) {
     if (k >= 0) {
         int tb = p.timebin[i];
         if (p.active[i]) {
+            mark_dirty(p, i);
           V3<float> gr[5];
 #pragma unroll
           for (int q = 0; q < 5; q++) gr[q] = v3(0.f, 0.f, 0.f);
@@ -604,6 +606,7 @@ __device__ __forceinline__ void gradients32_cell_warp(const KP& p, int i, int la
     if (k >= 0) {
         int tb = p.timebin[i];
         if (p.active[i]) {
+            mark_dirty(p, i);
           V3<float> gr[5];
 #pragma unroll
           for (int q = 0; q < 5; q++) gr[q] = v3(0.f, 0.f, 0.f);

@@ -78,6 +78,13 @@ __device__ __forceinline__ void extrap_catch_up(const KP& p, int i, unsigned int
     } else {
         ex = ex + st_zero<double>();  // adding zero twice gives the bits of adding it once
     }
+    if (p.dirty) {  // only a change of bits makes the host's copy stale
+        bool changed = false;
+#pragma unroll
+        for (int q = 0; q < 5; q++)
+            changed = changed || __double_as_longlong(ex.q[q]) != __double_as_longlong(C(p, F_EXTRAP + q, i));
+        if (changed) p.dirty[i] = 1;
+    }
     W5(p, F_EXTRAP, i, ex);
     p.extrap_step[i] = upto;
 }
@@ -116,9 +123,11 @@ __global__ void __launch_bounds__(kMaxBlock) k_predict(KP p) {
             if (gt0_64(C(p, F_PRIM, i))) W5(p, F_EXTRAP, i, ex + (-dt) * C5(p, F_SRC, i));
             else W5(p, F_EXTRAP, i, ex + st_zero<double>());
             if (lazy) p.extrap_step[i] = s + 1;
+            mark_dirty(p, i);
         } else {
             const double dt = step_dt();
             if (lazy) extrap_catch_up(p, i, s);
+            mark_dirty(p, i);
             St<double> prim = C5(p, F_PRIM, i);
             double rho_inv = 1. / prim.q[0];
             St<double> src = extrap_source(p, i, prim, rho_inv);
@@ -551,6 +560,7 @@ __device__ __forceinline__ void update_cell(const KP& p, int i, int do_c2p) {
 __device__ __forceinline__ void update_finish(const KP& p, int i, int k, bool act, St<double> facc, double msv,
                                               double maor, int do_c2p) {
     unsigned int err = 0;
+    mark_dirty(p, i);  // the pending fluxes at least
     if (act) {
         p.fresh[i] = 0;  // prim (here), grad and v_rel (gradient stage) change
         St<double> cons = apply_flux64(C5(p, F_CONS, i), facc, &err);
@@ -714,6 +724,7 @@ __device__ __forceinline__ void gradients_cell(const KP& p, int i, int do_timest
     if (k >= 0) {
         int tb = p.timebin[i];
         if (p.active[i]) {
+            mark_dirty(p, i);
           if (!p.godunov) {  // GodunovHydroRunner::step has no gradient stage (godunov.rs:14-58)
             V3<double> cen = C3(p, F_CEN, i);
             St<double> prim = C5(p, F_PRIM, i);
@@ -850,6 +861,7 @@ __device__ __forceinline__ void gradients_cell_warp(const KP& p, int i, int do_t
     if (k >= 0) {
         int tb = p.timebin[i];
         if (p.active[i]) {
+            mark_dirty(p, i);
           if (!p.godunov) {
             V3<double> cen = C3(p, F_CEN, i);
             St<double> prim = C5(p, F_PRIM, i);
@@ -1025,6 +1037,7 @@ __device__ __forceinline__ void limit_cell(const KP& p, int i, int wakeup = -1) 
     if (p.use_list) p.touch[i] = 0;  // the last stage that reads the cell list
     const int k = inst_of(p, i);
     if (p.tl[k].done) return;
+    mark_dirty(p, i);  // time bin, dt, extrapolations
     const double time_base = tbase(p, k);
     int tb = p.tb_tmp[i];
     if (p.sync_all) {

@@ -27,7 +27,7 @@ EXPORTED = (
     "mvmm_profile_read", "mvmm_riemann_flux", "mvmm_riemann_sample", "mvmm_get_stats",
     "mvmm_ctx_create_batched", "mvmm_batch_state", "mvmm_autotune", "mvmm_riemann_flux_p", "mvmm_riemann_sample_p",
     "mvmm_step_cells", "mvmm_drift", "mvmm_get_positions", "mvmm_set_mesh", "mvmm_flush_deferred",
-    "mvmm_gravity_timesteps", "mvmm_gravity_accelerations",
+    "mvmm_gravity_timesteps", "mvmm_gravity_accelerations", "mvmm_step_cells_changed",
 )
 
 
@@ -100,6 +100,7 @@ def load_library(path: str = LIB_PATH):
         "mvmm_riemann_sample": (i32, [i32, i32, dbl, i64, vp, vp, vp, vp]),
         "mvmm_riemann_flux_p": (i32, [vp, i64, vp, vp, vp, vp, vp]),
         "mvmm_step_cells": (i32, [vp, vp, vp, u64, u64, pu64, pi64]),
+        "mvmm_step_cells_changed": (i32, [vp, vp, vp, i64, u64, u64, pu64, pi64, pi64]),
         "mvmm_drift": (i32, [vp, dbl]),
         "mvmm_flush_deferred": (i32, [vp]),
         "mvmm_get_positions": (i32, [vp, vp]),
@@ -276,6 +277,31 @@ class GpuSim:
         self.ti_old, self.ti_current = self.ti_current, tn.value
         self.finished = done
         return done
+
+    def step_cells_changed(self, cells: Cells, changed=None) -> int:
+        """One step on host-resident state that moves only what changed
+        (mvmm_step_cells_changed): ``cells`` holds what the previous call left,
+        but for the cells listed in ``changed`` (None: upload every cell); the
+        cells the step rewrote are written back into ``cells``.  Returns the
+        bytes written back."""
+        cv = cells.cview()
+        if changed is None:
+            ptr, m = None, 0
+        else:
+            idx = np.ascontiguousarray(changed, dtype=np.int32)
+            ptr, m = idx.ctypes.data, idx.size
+        tn = ctypes.c_uint64(0)
+        nf = ctypes.c_int64(0)
+        stored = ctypes.c_int64(0)
+        _check(load_library().mvmm_step_cells_changed(self.h, ctypes.byref(cv), ptr, m, self.ti_current,
+                                                      self.ti_old, ctypes.byref(tn), ctypes.byref(nf),
+                                                      ctypes.byref(stored)), self.h)
+        self.steps += 1
+        self.active_faces += nf.value
+        done = self.ti_current >= MAX_NR_TIMESTEPS
+        self.ti_old, self.ti_current = self.ti_current, tn.value
+        self.finished = done
+        return stored.value
 
     def run(self, max_steps: int = 0) -> int:
         tc = ctypes.c_uint64(self.ti_current)

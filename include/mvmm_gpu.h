@@ -234,6 +234,23 @@ int mvmm_set_mesh(mvmm_ctx *ctx, const mvmm_mesh *mesh, const double *volume, co
  * simulations only. */
 int mvmm_step_cells(mvmm_ctx *ctx, const mvmm_cells *in, mvmm_cells *out, uint64_t ti_current, uint64_t ti_old,
                     uint64_t *ti_next, int64_t *n_active_faces);
+/* Runner::step(&mut Space, ..) on host-resident state (runner.rs:6-22) that
+ * moves only what changed.  The context keeps a device mirror of `cells`:
+ * `cells` must hold what the previous call left in it, except for the
+ * n_changed cells listed in `changed`, whose rows (every field and the time
+ * bin) the caller may have rewritten; those are read from the host, one step
+ * runs, and the cells the step rewrote (a hierarchical step: the active cells,
+ * their neighbours and the cells whose extrapolation moved) are written back
+ * into `cells` in place, 32 consecutive cells at a time, all rows but volume,
+ * loc and centroid, which a fixed mesh keeps.  changed = NULL uploads every
+ * cell: the first call, and any call whose arrays the previous call did not
+ * leave.  The device must address the arrays (pinned memory, or pageable
+ * memory where the GPU uses the host page tables); else MVMM_E_UNSUPPORTED.
+ * *bytes_stored (or NULL): the bytes this call wrote into `cells`.  Single
+ * simulations of a fixed mesh. */
+int mvmm_step_cells_changed(mvmm_ctx *ctx, mvmm_cells *cells, const int32_t *changed, int64_t n_changed,
+                            uint64_t ti_current, uint64_t ti_old, uint64_t *ti_next, int64_t *n_active_faces,
+                            int64_t *bytes_stored);
 /* Engine::run (engine.rs:152-199) from the given sync point, device resident:
  * runs at most max_steps steps (<= 0: to t_end).  On return *ti_current /
  * *ti_old are the next sync point; *steps_done and *n_active_faces count the
