@@ -80,7 +80,7 @@ struct mvmm_ctx {
     int nf_cap = 0;
     unsigned int* extrap_step = nullptr;  // hierarchical steps: deferred extrapolations (KP::extrap_step)
     double* dt_log = nullptr;
-    void* brent_jobs = nullptr;  // plain form, exact solver: queued Brent searches of a face launch
+    void* brent_jobs = nullptr;  // plain form, exact solver: the queued jobs of a face launch
     unsigned int* brent_count = nullptr;
     int brent_cap = 0;
     int64_t ncsr_cap = 0;
@@ -545,10 +545,11 @@ static int create_impl(const mvmm_params* prm, const mvmm_mesh* m, int64_t n_ins
     ALLOC(c->active, n);
     ALLOC(c->flux, 10 * nf * 8);
     if (prm->precision == MVMM_PRECISION_FP64 && prm->riemann == MVMM_RIEMANN_EXACT && nf > 0) {
-        // two queues of brent_cap jobs (Brent searches, Newton searches) and their counts
+        // kExactQueues queues of brent_cap jobs (Brent searches, Newton searches,
+        // faces to finish) and their counts
         c->brent_cap = (int)std::min<int64_t>(nf, kBrentJobsMax);
-        ALLOC(c->brent_jobs, 2 * (size_t)c->brent_cap * brent_job_bytes());
-        ALLOC(c->brent_count, 2 * sizeof(unsigned int));
+        ALLOC(c->brent_jobs, kExactQueues * (size_t)c->brent_cap * brent_job_bytes());
+        ALLOC(c->brent_count, (kExactQueues + 1) * sizeof(unsigned int));  // + k_face_brent's job counter
     }
     ALLOC(c->dtmp, n * 8);
     if (!prm->sync_all && c->n_inst == 1 && prm->particle_motion == MVMM_MOTION_FIXED) {  // hierarchical steps
@@ -1540,7 +1541,7 @@ int mvmm_set_mesh(mvmm_ctx* c, const mvmm_mesh* m, const double* volume, const d
             const int bcap = (int)std::min<int64_t>(cap, kBrentJobsMax);
             cudaFree(c->brent_jobs);
             c->brent_jobs = nullptr;
-            if (cudaMalloc(&c->brent_jobs, 2 * (size_t)bcap * brent_job_bytes()) != cudaSuccess)
+            if (cudaMalloc(&c->brent_jobs, kExactQueues * (size_t)bcap * brent_job_bytes()) != cudaSuccess)
                 return fail(MVMM_E_NOMEM, "set_mesh: cudaMalloc failed");
             c->brent_cap = bcap;
         }

@@ -532,6 +532,111 @@ static __device__ __noinline__ double ex_brent(double lower, double upper, doubl
     }
     return b;
 }
+// ex_brent's loop one evaluation of f at a time, so that a kernel can hand a
+// lane whose search has ended the next search while the other lanes of its
+// warp go on.  start() and step() leave either done set (the root in b, the
+// error bits in err) or the next point to evaluate in x; the points, and so
+// the iterates and the result, are ex_brent's: x is its s, or the point of its
+// forced-bisection check (phase 1).
+struct BrentMachine {
+    double a, b, c, d, fa, fb, fc, x, tol;
+    int it, max_it;
+    bool mflag, bisected, done;
+    int phase;  // 0: x is the iteration's s; 1: x is the check point
+    unsigned int err;
+
+    __device__ __forceinline__ void start(double lower, double upper, double low_f, double up_f, double tol_,
+                                          int max_iter) {
+        a = lower;
+        b = upper;
+        d = INFINITY;
+        fa = low_f;
+        fb = up_f;
+        tol = tol_;
+        max_it = 100 * max_iter;
+        err = 0;
+        done = false;
+        phase = 0;
+        if (fa * fb > 0.) {
+            err |= 2u;
+            done = true;
+            return;
+        }
+        if (fabs(fa) < fabs(fb)) swap_ab();
+        c = a;
+        fc = fa;
+        mflag = true;
+        it = 0;
+        next_s();
+    }
+    __device__ __forceinline__ void swap_ab() {
+        double t = a;
+        a = b;
+        b = t;
+        t = fa;
+        fa = fb;
+        fb = t;
+    }
+    // the loop test, then the iteration's s (or done)
+    __device__ __forceinline__ void next_s() {
+        if (!(fb != 0. && fabs(a - b) > tol * 0.5 * (a + b))) {
+            done = true;
+            return;
+        }
+        if (++it > max_it) {
+            err |= 1u;
+            done = true;
+            return;
+        }
+        double s;
+        if (fa != fc && fb != fc)
+            s = a * fb * fc / (fa - fb) / (fa - fc) + b * fa * fc / (fb - fa) / (fb - fc) +
+                c * fa * fb / (fc - fa) / (fc - fb);
+        else
+            s = b - fb * (b - a) / (fb - fa);
+        double tmp = 0.25 * (3. * a + b);
+        if (!((s > tmp && s < b) || (s < tmp && s > b)) || (mflag && fabs(s - b) >= (0.5 * fabs(b - c))) ||
+            (!mflag && fabs(s - b) >= (0.5 * fabs(c - d))) || (mflag && fabs(b - c) < 0.5 * tol * (b + c)) ||
+            (!mflag && fabs(c - d) < 0.5 * tol * (c + d))) {
+            s = 0.5 * (a + b);
+            mflag = true;
+        } else {
+            mflag = false;
+        }
+        bisected = mflag;
+        x = s;
+        phase = 0;
+    }
+    // f(x) given
+    __device__ __forceinline__ void step(double fx) {
+        if (phase == 1) {
+            if (fx != 0. && !(fa * fx < 0.) && !(fabs(fx) < fabs(fb))) done = true;
+            else next_s();
+            return;
+        }
+        const double s = x, fs = fx;
+        d = c;
+        c = b;
+        fc = fb;
+        const bool b_kept = !(fa * fs < 0.);
+        if (fa * fs < 0.) {
+            b = s;
+            fb = fs;
+        } else {
+            a = s;
+            fa = fs;
+        }
+        const bool swapped = fabs(fa) < fabs(fb);
+        if (swapped) swap_ab();
+        if (bisected && b_kept && !swapped && fb != 0. && fabs(a - b) > tol * 0.5 * (a + b) && it + 64 <= max_it) {
+            x = b + copysign(0.125 * tol * fabs(b), a - b);
+            phase = 1;
+        } else {
+            next_s();
+        }
+    }
+};
+
 __device__ __forceinline__ double ex_middle_density(double p, const ExSide& s, const Gas<double>& g) {  // :193-212
     double pdps = p / s.p;
     if (pdps > 1.) return s.rho * (pdps + g.gm1dgp1()) / (g.gm1dgp1() * pdps + 1.);

@@ -98,6 +98,11 @@ struct DevTimeline {
 // kDtLog / 2 steps all cells are brought up to date, so none lags further.
 constexpr int kDtLog = 4096;
 
+// Job queues of the plain form's exact solver (KP::brent_jobs): Brent
+// searches, Newton searches, and faces whose star pressure is the guess; each
+// holds brent_cap jobs.
+constexpr int kExactQueues = 3;
+
 // Internal (not exported) flag a face's Riemann solve sets when the FP32-face
 // form's split exact solver fell back to the full FP64 iteration.
 constexpr unsigned int kInfoFallback = 1u << 16;
@@ -168,8 +173,8 @@ struct KP {
     unsigned int* extrap_step;  // hierarchical steps: the steps whose predict contribution a cell's
                                 //   extrapolation includes (deferred for inactive cells, see k_predict)
     double* dt_log;             //   the dt of step s at [s % kDtLog]
-    void* brent_jobs;          // plain form, exact solver: the face kernel's queued Brent searches
-    unsigned int* brent_count;  //   (their count this launch)
+    void* brent_jobs;          // plain form, exact solver: the face kernel's queued jobs (kExactQueues
+    unsigned int* brent_count;  //   queues of brent_cap) and their counts this launch
     int brent_cap;
     unsigned int* blocks_done;  // k_limit blocks finished this step (the last one ends the step)
     unsigned int* touch;     // hierarchical steps: 1 for cells on this step's cell list

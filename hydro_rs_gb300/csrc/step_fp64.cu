@@ -213,11 +213,12 @@ __device__ __forceinline__ void write_face(const KP& p, int f, const FaceOut& o)
     }
 }
 
-// The exact solver's Brent searches leave the face kernel for a kernel of
-// their own.  Warps of the face kernel would run them with only the lanes
-// whose PVRS guess landed above the root (about half), holding the FP64 pipe
-// for all 32; queued, they run with full warps.  A job holds the face's
-// Riemann problem after the Newton stage and what the face's result needs.
+// The exact solver's searches and the rest of its faces leave the face kernel
+// for kernels of their own.  Warps of the face kernel would run each with only
+// the lanes whose guess took that path, holding the FP64 pipe for all 32;
+// queued, they run with full warps.  A job holds the face's Riemann problem
+// after the guess and what the face's result needs; p_guess becomes the star
+// pressure once the search has run.
 struct BrentJob {
     FacePre q;
     double vl, vr, al, ar, p_guess, fp_guess, fp0;  // fp0 = f(0)
@@ -284,27 +285,25 @@ __global__ void __launch_bounds__(kMaxBlock) k_face_flux(KP p) {
                     double pg, fpg, fp0;
                     const int next = ex_star_start(L, R, vl, vr, g, &pg, &fpg, &fp0);
                     double pst = pg;
-                    if (next != EX_DONE) {
-                        // queue 0: Brent searches; queue 1: Newton searches
-                        const int qi = next == EX_NEWTON ? 1 : 0;
-                        const unsigned int slot = atomicAdd(p.brent_count + qi, 1u);
-                        if (slot < (unsigned int)p.brent_cap) {
-                            BrentJob& J = reinterpret_cast<BrentJob*>(p.brent_jobs)[(size_t)qi * p.brent_cap + slot];
-                            J.q = q;
-                            J.vl = vl;
-                            J.vr = vr;
-                            J.al = al;
-                            J.ar = ar;
-                            J.p_guess = pg;
-                            J.fp_guess = fpg;
-                            J.fp0 = fp0;
-                            J.f = f;
-                            J.k = k;
-                            queued = true;
-                        } else {  // the queue is full: the search runs here
-                            const bool brent = next == EX_BRENT || ex_newton(L, R, vl, vr, g, p.max_iter, &err, &pg, &fpg);
-                            pst = brent ? ex_star_brent0(pg, fpg, fp0, L, R, vl, vr, g, p.max_iter, &err) : pg;
-                        }
+                    // queue 0: Brent searches; 1: Newton searches; 2: the guess is the pressure
+                    const int qi = next == EX_BRENT ? 0 : next == EX_NEWTON ? 1 : 2;
+                    const unsigned int slot = atomicAdd(p.brent_count + qi, 1u);
+                    if (slot < (unsigned int)p.brent_cap) {
+                        BrentJob& J = reinterpret_cast<BrentJob*>(p.brent_jobs)[(size_t)qi * p.brent_cap + slot];
+                        J.q = q;
+                        J.vl = vl;
+                        J.vr = vr;
+                        J.al = al;
+                        J.ar = ar;
+                        J.p_guess = pg;
+                        J.fp_guess = fpg;
+                        J.fp0 = fp0;
+                        J.f = f;
+                        J.k = k;
+                        queued = true;
+                    } else if (next != EX_DONE) {  // the queue is full: the search runs here
+                        const bool brent = next == EX_BRENT || ex_newton(L, R, vl, vr, g, p.max_iter, &err, &pg, &fpg);
+                        pst = brent ? ex_star_brent0(pg, fpg, fp0, L, R, vl, vr, g, p.max_iter, &err) : pg;
                     }
                     if (!queued) F = exact_flux_from_p(pst, q, vl, vr, al, ar, g);
                 }
@@ -319,26 +318,30 @@ __global__ void __launch_bounds__(kMaxBlock) k_face_flux(KP p) {
     }
 }
 
-// The queued searches run a tile of kJobTile jobs per block at a time, the
-// tile ordered by the branches f takes at the guess: for each side whether the
-// guess lies above its pressure (the shock branch of fb and fprimeb, else the
-// rarefaction branch with its power).  On the nearly uniform states of a smooth
-// flow the guess, the star pressure and both side pressures differ in their
-// last digits only, so which branches a face takes is close to random, and a
-// warp of unsorted faces would run both branches of every evaluation.  A tile
-// sorted by that key (a counting sort in shared memory) fills most warps with
-// faces that take the same branches; each face's arithmetic is unchanged.
+// The queued jobs run a tile of kJobTile jobs per block at a time, the tile
+// ordered by the branches the job's pressure (the guess in a search, the star
+// pressure when the face is finished) takes: for each side whether it lies
+// above the side's pressure (the shock branch of fb, fprimeb and the middle
+// density, else the rarefaction branch with its power).  On the nearly uniform
+// states of a smooth flow the guess, the star pressure and both side pressures
+// differ in their last digits only, so which branches a face takes is close to
+// random, and a warp of unsorted faces would run both branches of every
+// evaluation.  A tile sorted by that key (a counting sort in shared memory)
+// fills most warps with faces that take the same branches; each face's
+// arithmetic is unchanged.
 constexpr int kJobTile = 128;
 __device__ __forceinline__ int job_branch_key(const BrentJob& J) {
     const double pl = J.q.l.q[4], pr = J.q.r.q[4];
     const double lo = fmin(pl, pr), hi = fmax(pl, pr);
     return (J.p_guess > lo ? 1 : 0) + (J.p_guess > hi ? 1 : 0);
 }
-// The index of the job this thread runs in the tile starting at base (or -1).
-__device__ __forceinline__ int sorted_job(const BrentJob* jobs, unsigned int base, unsigned int n_jobs, int* s_count,
+// The index of the job this thread runs in the tile starting at base (or -1);
+// job(t) is job t of the n_jobs the kernel runs.
+template <class Job>
+__device__ __forceinline__ int sorted_job(const Job& job, unsigned int base, unsigned int n_jobs, int* s_count,
                                           int* s_order) {
     const unsigned int j = base + threadIdx.x;
-    const int key = j < n_jobs ? job_branch_key(jobs[j]) : 3;
+    const int key = j < n_jobs ? job_branch_key(job(j)) : 3;
     if (threadIdx.x < 4) s_count[threadIdx.x] = 0;
     __syncthreads();
     const int rank = atomicAdd(&s_count[key], 1);
@@ -351,45 +354,119 @@ __device__ __forceinline__ int sorted_job(const BrentJob* jobs, unsigned int bas
     __syncthreads();  // the arrays are reused by the next tile
     return mine;
 }
+__device__ __forceinline__ BrentJob* queue_jobs(const KP& p, int qi) {
+    return reinterpret_cast<BrentJob*>(p.brent_jobs) + (size_t)qi * p.brent_cap;
+}
+__device__ __forceinline__ unsigned int queue_count(const KP& p, int qi) {
+    return min(p.brent_count[qi], (unsigned int)p.brent_cap);
+}
 
-// The queued Brent searches of the exact solver's faces, with full warps;
-// each job then finishes its face (star state, sample, flux) and writes its rows.
+// The queued Brent searches of the exact solver's faces.  Searches end after
+// different numbers of evaluations, so a warp that ran one search per lane
+// would hold the FP64 pipe for all 32 lanes until its longest search ended.
+// Here every lane runs its search one evaluation of f at a time
+// (BrentMachine) and, when it ends, takes the next job of the queue (a
+// warp-aggregated fetch from a counter), so the warps stay full until the queue
+// runs dry.  Each job's star pressure goes back into its p_guess for
+// k_face_finish.
+__device__ __forceinline__ void brent_start(const BrentJob& J, const Gas<double>& g, int max_iter, BrentMachine& m,
+                                            ExSide& L, ExSide& R, double& vl, double& vr, int& k) {
+    L = ExSide{J.q.l.q[0], J.q.l.q[4], J.al};
+    R = ExSide{J.q.r.q[0], J.q.r.q[4], J.ar};
+    vl = J.vl;
+    vr = J.vr;
+    k = J.k;
+    m.start(0., J.p_guess, J.fp0, J.fp_guess, 1e-6, max_iter);  // ex_star_brent0
+}
 __global__ void __launch_bounds__(kJobTile) k_face_brent(KP p) {
-    __shared__ int s_count[4], s_order[kJobTile];
     const Gas<double> g = gas(p);
-    const unsigned int n_jobs = min(*p.brent_count, (unsigned int)p.brent_cap);
-    const BrentJob* jobs = reinterpret_cast<const BrentJob*>(p.brent_jobs);
-    for (unsigned int base = blockIdx.x * kJobTile; base < n_jobs; base += gridDim.x * kJobTile) {
-        const int j = sorted_job(jobs, base, n_jobs, s_count, s_order);
-        if (j < 0) continue;
-        const BrentJob J = jobs[j];
-        unsigned int err = 0;
-        ExSide L{J.q.l.q[0], J.q.l.q[4], J.al}, R{J.q.r.q[0], J.q.r.q[4], J.ar};
-        double pst = ex_star_brent0(J.p_guess, J.fp_guess, J.fp0, L, R, J.vl, J.vr, g, p.max_iter, &err);
-        write_face(p, J.f, face_finish(J.q, exact_flux_from_p(pst, J.q, J.vl, J.vr, J.al, J.ar, g)));
-        if (err) set_err(p, J.k, err);
+    const unsigned int n_jobs = queue_count(p, 0);
+    BrentJob* jobs = queue_jobs(p, 0);
+    unsigned int* next = p.brent_count + kExactQueues;  // jobs handed out
+    const unsigned int lane = threadIdx.x & 31;
+    int j = -1, k = 0;
+    bool dry = false;
+    BrentMachine m;
+    ExSide L, R;
+    double vl = 0., vr = 0.;
+    while (true) {
+        // lanes without a search take jobs until each holds one that needs f, or the queue is dry
+        while (true) {
+            const unsigned int need = __ballot_sync(0xffffffffu, j < 0 && !dry);
+            if (!need) break;
+            const int leader = __ffs(need) - 1;
+            unsigned int base = 0;
+            if ((int)lane == leader) base = atomicAdd(next, (unsigned int)__popc(need));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (need & (1u << lane)) {
+                const unsigned int t = base + (unsigned int)__popc(need & ((1u << lane) - 1u));
+                if (t < n_jobs) {
+                    j = (int)t;
+                    brent_start(jobs[j], g, p.max_iter, m, L, R, vl, vr, k);
+                    if (m.done) {
+                        jobs[j].p_guess = m.b;
+                        if (m.err) set_err(p, k, m.err);
+                        j = -1;
+                    }
+                } else {
+                    dry = true;
+                }
+            }
+        }
+        if (!__any_sync(0xffffffffu, j >= 0)) break;
+        if (j >= 0) {
+            m.step(ex_f(m.x, L, R, vl, vr, g));
+            if (m.done) {
+                jobs[j].p_guess = m.b;
+                if (m.err) set_err(p, k, m.err);
+                j = -1;
+            }
+        }
     }
 }
 
 // The queued Newton searches (the second queue): every job runs the Newton
 // loop from the guess (exact.rs:255-275), then, where the loop ends above the
-// root, Brent's method as ex_star_pre's caller would, and finishes its face.
+// root, Brent's method as ex_star_pre's caller would; the star pressure goes
+// back into its p_guess.
 __global__ void __launch_bounds__(kJobTile) k_face_newton(KP p) {
     __shared__ int s_count[4], s_order[kJobTile];
     const Gas<double> g = gas(p);
-    const unsigned int n_jobs = min(p.brent_count[1], (unsigned int)p.brent_cap);
-    const BrentJob* jobs = reinterpret_cast<const BrentJob*>(p.brent_jobs) + p.brent_cap;
+    const unsigned int n_jobs = queue_count(p, 1);
+    BrentJob* jobs = queue_jobs(p, 1);
+    auto job = [&](unsigned int t) -> const BrentJob& { return jobs[t]; };
     for (unsigned int base = blockIdx.x * kJobTile; base < n_jobs; base += gridDim.x * kJobTile) {
-        const int j = sorted_job(jobs, base, n_jobs, s_count, s_order);
+        const int j = sorted_job(job, base, n_jobs, s_count, s_order);
         if (j < 0) continue;
         const BrentJob J = jobs[j];
         unsigned int err = 0;
         ExSide L{J.q.l.q[0], J.q.l.q[4], J.al}, R{J.q.r.q[0], J.q.r.q[4], J.ar};
         double pg = J.p_guess, fpg = J.fp_guess;
         const bool brent = ex_newton(L, R, J.vl, J.vr, g, p.max_iter, &err, &pg, &fpg);
-        const double pst = brent ? ex_star_brent0(pg, fpg, J.fp0, L, R, J.vl, J.vr, g, p.max_iter, &err) : pg;
-        write_face(p, J.f, face_finish(J.q, exact_flux_from_p(pst, J.q, J.vl, J.vr, J.al, J.ar, g)));
+        jobs[j].p_guess = brent ? ex_star_brent0(pg, fpg, J.fp0, L, R, J.vl, J.vr, g, p.max_iter, &err) : pg;
         if (err) set_err(p, J.k, err);
+    }
+}
+
+// Every queued face from its star pressure on (star state, sample, flux), the
+// three queues one after another: apart from the searches, the faces of a warp
+// run the same code, where in the face kernel only its lanes whose guess was the
+// pressure would have run it.
+__global__ void __launch_bounds__(kJobTile) k_face_finish(KP p) {
+    __shared__ int s_count[4], s_order[kJobTile];
+    const Gas<double> g = gas(p);
+    const unsigned int n0 = queue_count(p, 0), n1 = queue_count(p, 1), n2 = queue_count(p, 2);
+    const unsigned int n_jobs = n0 + n1 + n2;
+    const BrentJob* jobs = queue_jobs(p, 0);
+    const size_t cap = (size_t)p.brent_cap;
+    auto job = [&](unsigned int t) -> const BrentJob& {
+        return t < n0 ? jobs[t] : t < n0 + n1 ? jobs[cap + (t - n0)] : jobs[2 * cap + (t - n0 - n1)];
+    };
+    for (unsigned int base = blockIdx.x * kJobTile; base < n_jobs; base += gridDim.x * kJobTile) {
+        const int t = sorted_job(job, base, n_jobs, s_count, s_order);
+        if (t < 0) continue;
+        const BrentJob J = job((unsigned int)t);
+        write_face(p, J.f, face_finish(J.q, exact_flux_from_p(J.p_guess, J.q, J.vl, J.vr, J.al, J.ar, g)));
     }
 }
 
@@ -1270,16 +1347,28 @@ inline int face_grid(const KP& p) {
 }
 
 size_t brent_job_bytes() { return sizeof(BrentJob); }
+// k_face_brent's lanes draw jobs until the queue is dry: as many blocks as fit
+// on the device at once
+int brent_pool_grid(const KP& p) {
+    static int per_sm = 0;
+    if (per_sm == 0 && (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_face_brent, kJobTile, 0) !=
+                            cudaSuccess || per_sm < 1))
+        per_sm = 1;
+    return p.n_sms * per_sm;
+}
 void launch_face_flux_fp64(const KP& p, int solver, cudaStream_t s) {
     if (p.nf <= 0) return;
     int g = face_grid(p);
     if (solver == SOLVER_HLLC) k_face_flux<SOLVER_HLLC><<<g, p.blk_face, 0, s>>>(p);
     else if (solver == SOLVER_EXACT && p.brent_jobs) {
-        cudaMemsetAsync(p.brent_count, 0, 2 * sizeof(unsigned int), s);
+        cudaMemsetAsync(p.brent_count, 0, (kExactQueues + 1) * sizeof(unsigned int), s);
         k_face_flux<SOLVER_EXACT><<<g, p.blk_face, 0, s>>>(p);
         const int jobs_grid = (int)std::min<long long>((p.brent_cap + kJobTile - 1) / kJobTile, p.n_sms * 16LL);
         k_face_newton<<<jobs_grid, kJobTile, 0, s>>>(p);
-        k_face_brent<<<jobs_grid, kJobTile, 0, s>>>(p);
+        k_face_brent<<<brent_pool_grid(p), kJobTile, 0, s>>>(p);
+        const int finish_grid =
+            (int)std::min<long long>((kExactQueues * (long long)p.brent_cap + kJobTile - 1) / kJobTile, p.n_sms * 16LL);
+        k_face_finish<<<finish_grid, kJobTile, 0, s>>>(p);
     } else if (solver == SOLVER_EXACT) k_face_flux<SOLVER_EXACT><<<g, p.blk_face, 0, s>>>(p);
     else if (solver == SOLVER_PVRS) k_face_flux<SOLVER_PVRS><<<g, p.blk_face, 0, s>>>(p);
     else k_face_flux<SOLVER_EXTRA><<<g, p.blk_face, 0, s>>>(p);
