@@ -123,10 +123,6 @@ struct mvmm_ctx {
     int* chg_list = nullptr;
 };
 
-// Largest Brent queue of the plain exact-solver face kernel (jobs beyond it
-// run their search in the face kernel itself).
-constexpr int64_t kBrentJobsMax = 1 << 22;
-
 namespace {
 
 RSx solver_settings(const mvmm_params& prm) {
@@ -546,8 +542,9 @@ static int create_impl(const mvmm_params* prm, const mvmm_mesh* m, int64_t n_ins
     ALLOC(c->flux, 10 * nf * 8);
     if (prm->precision == MVMM_PRECISION_FP64 && prm->riemann == MVMM_RIEMANN_EXACT && nf > 0) {
         // kExactQueues queues of brent_cap jobs (Brent searches, Newton searches,
-        // faces to finish) and their counts
-        c->brent_cap = (int)std::min<int64_t>(nf, kBrentJobsMax);
+        // faces to finish) and their counts; a job per face in each, so that
+        // the face kernel never runs a search or a flux itself
+        c->brent_cap = (int)nf;
         ALLOC(c->brent_jobs, kExactQueues * (size_t)c->brent_cap * brent_job_bytes());
         ALLOC(c->brent_count, (kExactQueues + 1) * sizeof(unsigned int));  // + k_face_brent's job counter
     }
@@ -1214,8 +1211,11 @@ __device__ __forceinline__ void store_rows(const HostRows& h, const double* __re
 }
 
 // Stores the rows of the cells a kernel marked since the last store, a warp
-// per 32 consecutive cells (whole 256-byte segments of each row) wherever one
-// of them is marked, and clears the marks; counts the bytes into the timeline.
+// per 32 consecutive cells (whole 256-byte segments of each row): all their
+// rows wherever one of them is marked kDirtyAll, else their extrapolation rows
+// wherever one is marked kDirtyExtrap (inactive cells of a hierarchical step
+// whose time extrapolation moved).  Clears the marks; counts the bytes into
+// the timeline.
 __global__ void __launch_bounds__(256) k_store_dirty(HostRows h, KP p) {
     const int lane = threadIdx.x & 31;
     const int n_warps = (int)((gridDim.x * blockDim.x) >> 5);
@@ -1223,16 +1223,23 @@ __global__ void __launch_bounds__(256) k_store_dirty(HostRows h, KP p) {
     for (int w = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); w < groups; w += n_warps) {
         const int i = (w << 5) + lane;
         const bool in = i < p.n;
-        if (!__any_sync(0xffffffffu, in && p.dirty[i])) continue;
+        const uint8_t d = in ? p.dirty[i] : 0;
+        const bool all = __any_sync(0xffffffffu, (d & kDirtyAll) != 0);
+        if (!__any_sync(0xffffffffu, d != 0)) continue;
         if (in) {
-            store_rows<0, kKeptFirst>(h, p.cd, (size_t)p.n, i);
-            store_rows<kKeptEnd, F_SRC>(h, p.cd, (size_t)p.n, i);
-            h.tb[i] = p.timebin[i];
+            if (all) {
+                store_rows<0, kKeptFirst>(h, p.cd, (size_t)p.n, i);
+                store_rows<kKeptEnd, F_SRC>(h, p.cd, (size_t)p.n, i);
+                h.tb[i] = p.timebin[i];
+            } else {
+                store_rows<F_EXTRAP, F_EXTRAP + 5>(h, p.cd, (size_t)p.n, i);
+            }
             p.dirty[i] = 0;
         }
         if (lane == 0) {
             const int cells = min(32, p.n - (w << 5));
-            atomicAdd(&p.tl[0].host_stored, (unsigned long long)cells * (unsigned long long)kStoredCellBytes);
+            const unsigned long long per = all ? (unsigned long long)kStoredCellBytes : 5ull * 8ull;
+            atomicAdd(&p.tl[0].host_stored, (unsigned long long)cells * per);
         }
     }
 }
@@ -1538,7 +1545,7 @@ int mvmm_set_mesh(mvmm_ctx* c, const mvmm_mesh* m, const double* volume, const d
         }
         CUDA_TRY(cudaMemsetAsync(c->face_stamp, 0, (size_t)cap * 4, s));
         if (c->brent_jobs) {
-            const int bcap = (int)std::min<int64_t>(cap, kBrentJobsMax);
+            const int bcap = (int)cap;
             cudaFree(c->brent_jobs);
             c->brent_jobs = nullptr;
             if (cudaMalloc(&c->brent_jobs, kExactQueues * (size_t)bcap * brent_job_bytes()) != cudaSuccess)

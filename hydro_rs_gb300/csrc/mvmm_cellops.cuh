@@ -52,9 +52,11 @@ __device__ __forceinline__ Gas<T> gas_t(const KP& p) {
 __device__ __forceinline__ Gas<double> gas(const KP& p) { return gas_t<double>(p); }
 __device__ __forceinline__ int inst_of(const KP& p, int cell) { return p.inst ? p.inst[cell] : 0; }
 // A kernel rewrote rows of cell i that the host holds (mvmm_step_cells_changed
-// copies back only the chunks of such cells).
-__device__ __forceinline__ void mark_dirty(const KP& p, int i) {
-    if (p.dirty) p.dirty[i] = 1;
+// copies back only such cells): its extrapolations only (kDirtyExtrap), or any
+// of its rows (kDirtyAll).  One thread, or the lanes of one warp with the same
+// bits, marks a cell in a kernel.
+__device__ __forceinline__ void mark_dirty(const KP& p, int i, uint8_t bits = kDirtyAll) {
+    if (p.dirty) p.dirty[i] |= bits;
 }
 __device__ __forceinline__ double tbase(const KP& p, int k) { return p.inst_tb ? p.inst_tb[k] : p.time_base; }
 __device__ __forceinline__ double tbase_inv(const KP& p, int k) { return p.inst_tbi ? p.inst_tbi[k] : p.time_base_inv; }

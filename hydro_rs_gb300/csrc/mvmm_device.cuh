@@ -637,6 +637,58 @@ struct BrentMachine {
     }
 };
 
+// ex_newton's loop one evaluation of f at a time (as BrentMachine for
+// ex_brent): start() and step() leave either done set (the pressure in pg,
+// brent set where Brent's method must follow on [0, pg], the error bits in
+// err) or the next point to evaluate in x.
+struct NewtonMachine {
+    double p, pg, fpg, x;
+    int counter, max_iter;
+    bool done, brent;
+    unsigned int err;
+
+    __device__ __forceinline__ void start(double p_guess, double fp_guess, int max_iter_, const ExSide& l,
+                                          const ExSide& r, const Gas<double>& g) {
+        p = 0.;
+        pg = p_guess;
+        fpg = fp_guess;
+        counter = 0;
+        max_iter = max_iter_;
+        err = 0;
+        done = false;
+        brent = false;
+        next_x(l, r, g);
+    }
+    __device__ __forceinline__ void end() {
+        brent = fabs(p - pg) > 1e-6 * 0.5 * (p + pg) && fpg > 0.;
+        done = true;
+    }
+    // the loop test, then the next iterate (or done)
+    __device__ __forceinline__ void next_x(const ExSide& l, const ExSide& r, const Gas<double>& g) {
+        if (!(fabs(p - pg) > 1e-6 * 0.5 * (p + pg) && fpg < 0.0)) {
+            end();
+            return;
+        }
+        p = pg;
+        const bool lo_left = l.p <= r.p;
+        const double d_lo = ex_fprimeb(pg, lo_left ? l : r, g);
+        const double d_hi = ex_fprimeb(pg, lo_left ? r : l, g);
+        pg = pg - fpg / ((lo_left ? d_lo : d_hi) + (lo_left ? d_hi : d_lo));
+        x = pg;
+    }
+    // f(x) given
+    __device__ __forceinline__ void step(double fx, const ExSide& l, const ExSide& r, const Gas<double>& g) {
+        fpg = fx;
+        counter += 1;
+        if (counter > max_iter) {  // the reference panics here
+            err |= 1u;
+            end();
+            return;
+        }
+        next_x(l, r, g);
+    }
+};
+
 __device__ __forceinline__ double ex_middle_density(double p, const ExSide& s, const Gas<double>& g) {  // :193-212
     double pdps = p / s.p;
     if (pdps > 1.) return s.rho * (pdps + g.gm1dgp1()) / (g.gm1dgp1() * pdps + 1.);

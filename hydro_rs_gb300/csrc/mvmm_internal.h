@@ -103,6 +103,9 @@ constexpr int kDtLog = 4096;
 // holds brent_cap jobs.
 constexpr int kExactQueues = 3;
 
+// KP::dirty marks: the cell's extrapolation rows changed, or any of its rows.
+constexpr uint8_t kDirtyExtrap = 1, kDirtyAll = 2;
+
 // Internal (not exported) flag a face's Riemann solve sets when the FP32-face
 // form's split exact solver fell back to the full FP64 iteration.
 constexpr unsigned int kInfoFallback = 1u << 16;

@@ -119,7 +119,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_predict32(KP p) {
 #pragma unroll
         for (int q = 0; q < 5; q++) ex.q[q] = pos ? ex.q[q] + (-dt) * f64(src.q[q]) : ex.q[q] + 0.;
         W5(p, F_EXTRAP, i, ex);
-        mark_dirty(p, i);
+        mark_dirty(p, i, reset ? kDirtyAll : kDirtyExtrap);
         if (reset) W5(p, F_PRIM, i, st_zero<double>());
         const bool live = pos && !reset;  // the checked density is positive
 #pragma unroll

@@ -83,7 +83,7 @@ __device__ __forceinline__ void extrap_catch_up(const KP& p, int i, unsigned int
 #pragma unroll
         for (int q = 0; q < 5; q++)
             changed = changed || __double_as_longlong(ex.q[q]) != __double_as_longlong(C(p, F_EXTRAP + q, i));
-        if (changed) p.dirty[i] = 1;
+        if (changed) p.dirty[i] |= kDirtyExtrap;
     }
     W5(p, F_EXTRAP, i, ex);
     p.extrap_step[i] = upto;
@@ -123,11 +123,11 @@ __global__ void __launch_bounds__(kMaxBlock) k_predict(KP p) {
             if (gt0_64(C(p, F_PRIM, i))) W5(p, F_EXTRAP, i, ex + (-dt) * C5(p, F_SRC, i));
             else W5(p, F_EXTRAP, i, ex + st_zero<double>());
             if (lazy) p.extrap_step[i] = s + 1;
-            mark_dirty(p, i);
+            mark_dirty(p, i, kDirtyExtrap);
         } else {
             const double dt = step_dt();
             if (lazy) extrap_catch_up(p, i, s);
-            mark_dirty(p, i);
+            mark_dirty(p, i, kDirtyExtrap);
             St<double> prim = C5(p, F_PRIM, i);
             double rho_inv = 1. / prim.q[0];
             St<double> src = extrap_source(p, i, prim, rho_inv);
@@ -148,7 +148,10 @@ __global__ void __launch_bounds__(kMaxBlock) k_predict(KP p) {
             for (int q = 0; q < 5; q++)
                 reset = reset || __double_as_longlong(chk.q[q]) != __double_as_longlong(prim.q[q]) ||
                         is_nan64(prim.q[q]);
-            if (reset) W5(p, F_PRIM, i, chk);
+            if (reset) {
+                W5(p, F_PRIM, i, chk);
+                mark_dirty(p, i);
+            }
             // volume: dvdt is zero for a fixed mesh, so volume.clamp(..) leaves it unchanged
             write_derived(p, i, chk, src, rho_inv);
             // a reset prim no longer matches the source row (computed from the old one)
@@ -236,7 +239,8 @@ __device__ __forceinline__ St<double> exact_flux_from_p(double pst, const FacePr
 
 // EulerEqnsFvs::compute_fluxes (euler_eqns_fvs.rs:26-48): the active-face rule,
 // dt = min(dt_l, dt_r), interior / boundary dispatch.
-template <int SOLVER>
+// QUEUE (the exact solver with its job queues): every face's solve is queued.
+template <int SOLVER, bool QUEUE = false>
 __global__ void __launch_bounds__(kMaxBlock) k_face_flux(KP p) {
     if (p.use_list && p.tl[0].done) return;
     const Gas<double> g = gas(p);
@@ -268,7 +272,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_face_flux(KP p) {
             bool queued = false;
             if (!counted) {
                 o = face_zero();
-            } else if (SOLVER == SOLVER_EXACT && p.brent_jobs) {
+            } else if constexpr (QUEUE) {
                 // star_half_state (riemann_solver.rs:258-284) with the exact
                 // star solver: its Newton and Brent stages are queued, each for
                 // a kernel of its own that finishes the face
@@ -284,28 +288,22 @@ __global__ void __launch_bounds__(kMaxBlock) k_face_flux(KP p) {
                     ExSide L{q.l.q[0], q.l.q[4], al}, R{q.r.q[0], q.r.q[4], ar};
                     double pg, fpg, fp0;
                     const int next = ex_star_start(L, R, vl, vr, g, &pg, &fpg, &fp0);
-                    double pst = pg;
-                    // queue 0: Brent searches; 1: Newton searches; 2: the guess is the pressure
+                    // queue 0: Brent searches; 1: Newton searches; 2: the guess is the pressure.
+                    // Each queue holds a job per face (brent_cap >= nf): none overflows.
                     const int qi = next == EX_BRENT ? 0 : next == EX_NEWTON ? 1 : 2;
                     const unsigned int slot = atomicAdd(p.brent_count + qi, 1u);
-                    if (slot < (unsigned int)p.brent_cap) {
-                        BrentJob& J = reinterpret_cast<BrentJob*>(p.brent_jobs)[(size_t)qi * p.brent_cap + slot];
-                        J.q = q;
-                        J.vl = vl;
-                        J.vr = vr;
-                        J.al = al;
-                        J.ar = ar;
-                        J.p_guess = pg;
-                        J.fp_guess = fpg;
-                        J.fp0 = fp0;
-                        J.f = f;
-                        J.k = k;
-                        queued = true;
-                    } else if (next != EX_DONE) {  // the queue is full: the search runs here
-                        const bool brent = next == EX_BRENT || ex_newton(L, R, vl, vr, g, p.max_iter, &err, &pg, &fpg);
-                        pst = brent ? ex_star_brent0(pg, fpg, fp0, L, R, vl, vr, g, p.max_iter, &err) : pg;
-                    }
-                    if (!queued) F = exact_flux_from_p(pst, q, vl, vr, al, ar, g);
+                    BrentJob& J = reinterpret_cast<BrentJob*>(p.brent_jobs)[(size_t)qi * p.brent_cap + slot];
+                    J.q = q;
+                    J.vl = vl;
+                    J.vr = vr;
+                    J.al = al;
+                    J.ar = ar;
+                    J.p_guess = pg;
+                    J.fp_guess = fpg;
+                    J.fp0 = fp0;
+                    J.f = f;
+                    J.k = k;
+                    queued = true;
                 }
                 if (!queued) o = face_finish(q, F);
             } else {
@@ -445,6 +443,100 @@ __global__ void __launch_bounds__(kJobTile) k_face_newton(KP p) {
         const bool brent = ex_newton(L, R, J.vl, J.vr, g, p.max_iter, &err, &pg, &fpg);
         jobs[j].p_guess = brent ? ex_star_brent0(pg, fpg, J.fp0, L, R, J.vl, J.vr, g, p.max_iter, &err) : pg;
         if (err) set_err(p, J.k, err);
+    }
+}
+
+// Both search queues in one pool: Newton jobs first, then Brent jobs.  A lane
+// runs its search one evaluation of f at a time (NewtonMachine, then
+// BrentMachine where the Newton loop ends above the root, as k_face_newton; or
+// BrentMachine alone, as k_face_brent) and, when it ends, takes the next job,
+// so the warps stay full until both queues run dry.  Each job's star pressure
+// goes back into its p_guess for k_face_finish.
+struct SearchLane {
+    int j = -1;        // job (index into the combined queue), or -1
+    int k = 0;         // its simulation
+    bool newton = false;
+    unsigned int err = 0;
+    ExSide L, R;
+    double vl = 0., vr = 0., fp0 = 0.;
+    NewtonMachine nm;
+    BrentMachine bm;
+};
+__device__ __forceinline__ bool search_lane_done(const SearchLane& s) { return s.newton ? s.nm.done : s.bm.done; }
+// Newton done: Brent follows where its loop ended above the root
+__device__ __forceinline__ void search_after_newton(SearchLane& s, int max_iter) {
+    s.err |= s.nm.err;
+    if (s.nm.brent) {
+        s.newton = false;
+        s.bm.start(0., s.nm.pg, s.fp0, s.nm.fpg, 1e-6, max_iter);  // ex_star_brent0
+    }
+}
+__device__ __forceinline__ double search_result(SearchLane& s) {
+    if (s.newton) return s.nm.pg;
+    s.err |= s.bm.err;
+    return s.bm.b;
+}
+__global__ void __launch_bounds__(kJobTile) k_face_search(KP p) {
+    const Gas<double> g = gas(p);
+    const unsigned int n1 = queue_count(p, 1), n0 = queue_count(p, 0);
+    const unsigned int n_jobs = n1 + n0;
+    BrentJob* newton_jobs = queue_jobs(p, 1);
+    BrentJob* brent_jobs = queue_jobs(p, 0);
+    unsigned int* next = p.brent_count + kExactQueues;  // jobs handed out
+    const unsigned int lane = threadIdx.x & 31;
+    auto job = [&](unsigned int t) -> BrentJob& { return t < n1 ? newton_jobs[t] : brent_jobs[t - n1]; };
+    SearchLane s;
+    bool dry = false;
+    auto retire = [&]() {
+        job((unsigned int)s.j).p_guess = search_result(s);
+        if (s.err) set_err(p, s.k, s.err);
+        s.j = -1;
+    };
+    while (true) {
+        // lanes without a search take jobs until each holds one that needs f, or the queues are dry
+        while (true) {
+            const unsigned int need = __ballot_sync(0xffffffffu, s.j < 0 && !dry);
+            if (!need) break;
+            const int leader = __ffs(need) - 1;
+            unsigned int base = 0;
+            if ((int)lane == leader) base = atomicAdd(next, (unsigned int)__popc(need));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (need & (1u << lane)) {
+                const unsigned int t = base + (unsigned int)__popc(need & ((1u << lane) - 1u));
+                if (t < n_jobs) {
+                    const BrentJob& J = job(t);
+                    s.j = (int)t;
+                    s.k = J.k;
+                    s.err = 0;
+                    s.L = ExSide{J.q.l.q[0], J.q.l.q[4], J.al};
+                    s.R = ExSide{J.q.r.q[0], J.q.r.q[4], J.ar};
+                    s.vl = J.vl;
+                    s.vr = J.vr;
+                    s.fp0 = J.fp0;
+                    s.newton = t < n1;
+                    if (s.newton) {
+                        s.nm.start(J.p_guess, J.fp_guess, p.max_iter, s.L, s.R, g);
+                        if (s.nm.done) search_after_newton(s, p.max_iter);
+                    } else {
+                        s.bm.start(0., J.p_guess, J.fp0, J.fp_guess, 1e-6, p.max_iter);  // ex_star_brent0
+                    }
+                    if (search_lane_done(s)) retire();
+                } else {
+                    dry = true;
+                }
+            }
+        }
+        if (!__any_sync(0xffffffffu, s.j >= 0)) break;
+        if (s.j >= 0) {
+            const double fx = ex_f(s.newton ? s.nm.x : s.bm.x, s.L, s.R, s.vl, s.vr, g);
+            if (s.newton) {
+                s.nm.step(fx, s.L, s.R, g);
+                if (s.nm.done) search_after_newton(s, p.max_iter);
+            } else {
+                s.bm.step(fx);
+            }
+            if (search_lane_done(s)) retire();
+        }
     }
 }
 
@@ -1347,12 +1439,12 @@ inline int face_grid(const KP& p) {
 }
 
 size_t brent_job_bytes() { return sizeof(BrentJob); }
-// k_face_brent's lanes draw jobs until the queue is dry: as many blocks as fit
+// The pools' lanes draw jobs until the queues are dry: as many blocks as fit
 // on the device at once
-int brent_pool_grid(const KP& p) {
-    static int per_sm = 0;
-    if (per_sm == 0 && (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_face_brent, kJobTile, 0) !=
-                            cudaSuccess || per_sm < 1))
+template <class K>
+int pool_grid(const KP& p, K kernel) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kJobTile, 0) != cudaSuccess || per_sm < 1)
         per_sm = 1;
     return p.n_sms * per_sm;
 }
@@ -1362,10 +1454,8 @@ void launch_face_flux_fp64(const KP& p, int solver, cudaStream_t s) {
     if (solver == SOLVER_HLLC) k_face_flux<SOLVER_HLLC><<<g, p.blk_face, 0, s>>>(p);
     else if (solver == SOLVER_EXACT && p.brent_jobs) {
         cudaMemsetAsync(p.brent_count, 0, (kExactQueues + 1) * sizeof(unsigned int), s);
-        k_face_flux<SOLVER_EXACT><<<g, p.blk_face, 0, s>>>(p);
-        const int jobs_grid = (int)std::min<long long>((p.brent_cap + kJobTile - 1) / kJobTile, p.n_sms * 16LL);
-        k_face_newton<<<jobs_grid, kJobTile, 0, s>>>(p);
-        k_face_brent<<<brent_pool_grid(p), kJobTile, 0, s>>>(p);
+        k_face_flux<SOLVER_EXACT, true><<<g, p.blk_face, 0, s>>>(p);
+        k_face_search<<<pool_grid(p, k_face_search), kJobTile, 0, s>>>(p);
         const int finish_grid =
             (int)std::min<long long>((kExactQueues * (long long)p.brent_cap + kJobTile - 1) / kJobTile, p.n_sms * 16LL);
         k_face_finish<<<finish_grid, kJobTile, 0, s>>>(p);

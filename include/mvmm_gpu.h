@@ -239,10 +239,11 @@ int mvmm_step_cells(mvmm_ctx *ctx, const mvmm_cells *in, mvmm_cells *out, uint64
  * `cells` must hold what the previous call left in it, except for the
  * n_changed cells listed in `changed`, whose rows (every field and the time
  * bin) the caller may have rewritten; those are read from the host, one step
- * runs, and the cells the step rewrote (a hierarchical step: the active cells,
- * their neighbours and the cells whose extrapolation moved) are written back
- * into `cells` in place, 32 consecutive cells at a time, all rows but volume,
- * loc and centroid, which a fixed mesh keeps.  changed = NULL uploads every
+ * runs, and the cells the step rewrote are written back into `cells` in place,
+ * 32 consecutive cells at a time: all rows but volume, loc and centroid (which
+ * a fixed mesh keeps) where one of them changed more than its extrapolations
+ * (a hierarchical step: the active cells and their neighbours), else the
+ * extrapolation rows where those moved.  changed = NULL uploads every
  * cell: the first call, and any call whose arrays the previous call did not
  * leave.  The device must address the arrays (pinned memory, or pageable
  * memory where the GPU uses the host page tables); else MVMM_E_UNSUPPORTED.
