@@ -84,7 +84,10 @@ def test_changed_cells_are_read(gpu_lib, precision):
     edit = rng.choice(n, 60, replace=False)
     host.cons[4, edit] *= 1.5
     host.prim[4, edit] *= 1.5
-    host.cons[1, edit[:20]] += 1e-3
+    kick = edit[:20]  # a small velocity, its kinetic energy added to the energy
+    host.cons[1, kick] += 1e-4 * host.cons[0, kick]
+    host.cons[4, kick] += 0.5e-8 * host.cons[0, kick]
+    host.prim[1, kick] += 1e-4
     moved = edit[:10]
     host.loc[:, moved] += rng.uniform(-1e-4, 1e-4, (3, moved.size))
     host.centroid[:, moved] += rng.uniform(-1e-4, 1e-4, (3, moved.size))
