@@ -719,11 +719,17 @@ def run_batch_to_end(args):
             f0 = sim.stats()["active_faces"]
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            try:
-                sim.run()
-            except G.MvmmError as e:  # stopped simulations are reported per instance
-                if e.code != -3:
-                    raise
+            while not sim.finished:  # chunks of steps, with progress on stderr
+                try:
+                    sim.run(max_steps=4096)
+                except G.MvmmError as e:  # a stopped simulation is reported per instance; the others run on
+                    if e.code != -3:
+                        raise
+                st = sim.batch_state()
+                sim.finished = bool(st["finished"].all())
+                print(f"[to-end] form {prec}: {int(st['finished'].sum())} of {len(st['finished'])} finished, "
+                      f"{int(st['steps'].max())} steps, {time.perf_counter() - t0:.1f} s", file=sys.stderr,
+                      flush=True)
             torch.cuda.synchronize()
             secs = time.perf_counter() - t0
             st = sim.batch_state()

@@ -546,7 +546,7 @@ static int create_impl(const mvmm_params* prm, const mvmm_mesh* m, int64_t n_ins
         // the face kernel never runs a search or a flux itself
         c->brent_cap = (int)nf;
         ALLOC(c->brent_jobs, kExactQueues * (size_t)c->brent_cap * brent_job_bytes());
-        ALLOC(c->brent_count, (kExactQueues + 1) * sizeof(unsigned int));  // + k_face_brent's job counter
+        ALLOC(c->brent_count, (kExactQueues + 1) * sizeof(unsigned int));  // + k_face_search's job counter
     }
     ALLOC(c->dtmp, n * 8);
     if (!prm->sync_all && c->n_inst == 1 && prm->particle_motion == MVMM_MOTION_FIXED) {  // hierarchical steps

@@ -331,30 +331,31 @@ struct Star {
 
 // Toro sampling at x/t = 0 given the star state (riemann_solver.rs:224-255)
 template <typename T>
+// The reference's two sides (u < 0: the right side, with -a_R; else the left)
+// are written once for the side x/t = 0 falls on: that side's state, velocity,
+// middle density and signed sound speed are selected, and its comparisons carry
+// the side's sign (right: shock speed > 0, head speed v - a > 0, tail speed < 0
+// as sg * x < 0 or > 0 with sg = -1), so the lanes of a warp run one code path
+// whichever side each samples.  Each comparison and value is the one the
+// reference forms on that side.
 __device__ St<T> sample_star(const Star<T>& s, const St<T>& l, const St<T>& r, T vl, T vr, T al, T ar, V3<T> n,
                              const Gas<T>& g) {
-    if (s.u < T(0)) {
-        if (s.p > r.q[4]) {  // right shock
-            if (shock_speed(vr, -ar, s.p / r.q[4], g) > T(0)) return sample_middle(s.rho_r, s.u, s.p, r, vr, n);
-            return r;
-        }
-        // right rarefaction
-        if (vr - (-ar) > T(0)) {
-            if (rarefaction_tail_speed(s.u, -ar, s.p / r.q[4], g) < T(0))
-                return sample_rarefaction_fan(r, -ar, vr, n, g);
-            return sample_middle(s.rho_r, s.u, s.p, r, vr, n);
-        }
-        return r;
-    } else if (s.p > l.q[4]) {  // left shock
-        if (shock_speed(vl, al, s.p / l.q[4], g) < T(0)) return sample_middle(s.rho_l, s.u, s.p, l, vl, n);
-        return l;
+    const bool right = s.u < T(0);
+    const St<T> w = right ? r : l;
+    const T v = right ? vr : vl;
+    const T a = right ? -ar : al;
+    const T rho = right ? s.rho_r : s.rho_l;
+    const T sg = right ? T(-1) : T(1);
+    if (s.p > w.q[4]) {  // shock
+        if (sg * shock_speed(v, a, s.p / w.q[4], g) < T(0)) return sample_middle(rho, s.u, s.p, w, v, n);
+        return w;
     }
-    // left rarefaction
-    if (vl - al < T(0)) {
-        if (rarefaction_tail_speed(s.u, al, s.p / l.q[4], g) > T(0)) return sample_rarefaction_fan(l, al, vl, n, g);
-        return sample_middle(s.rho_l, s.u, s.p, l, vl, n);
+    // rarefaction
+    if (sg * (v - a) < T(0)) {
+        if (sg * rarefaction_tail_speed(s.u, a, s.p / w.q[4], g) > T(0)) return sample_rarefaction_fan(w, a, v, n, g);
+        return sample_middle(rho, s.u, s.p, w, v, n);
     }
-    return l;
+    return w;
 }
 
 // VacuumRiemannSolver (riemann_solver/vacuum.rs:14-138)
@@ -637,9 +638,10 @@ struct BrentMachine {
     }
 };
 
-// ex_newton's loop one evaluation of f at a time (as BrentMachine for
-// ex_brent): start() and step() leave either done set (the pressure in pg,
-// brent set where Brent's method must follow on [0, pg], the error bits in
+// The Newton loop of ex_star_pre (exact.rs:255-275) from p = 0, the guess and
+// f(guess), one evaluation of f at a time (as BrentMachine for ex_brent):
+// start() and step() leave either done set (the pressure in pg, brent set where
+// Brent's method must follow on [0, pg] with f(pg) = fpg, the error bits in
 // err) or the next point to evaluate in x.
 struct NewtonMachine {
     double p, pg, fpg, x;
@@ -748,32 +750,6 @@ static __device__ __noinline__ int ex_star_start(ExSide l, ExSide r, double vl, 
     if (fp * fp_guess >= 0. && apart && fp_guess < 0.0) return EX_NEWTON;
     return apart && fp_guess > 0. ? EX_BRENT : EX_DONE;
 }
-// The Newton loop of ex_star_pre from p = 0, p_guess, f(p_guess); returns true
-// where Brent's method must follow (on [0, *p_guess], f = *fp_guess), else the
-// pressure is *p_guess.
-static __device__ __noinline__ bool ex_newton(ExSide l, ExSide r, double vl, double vr, Gas<double> g, int max_iter,
-                                              unsigned int* err, double* p_guess_io, double* fp_guess_io) {
-    double p = 0.;
-    double p_guess = *p_guess_io;
-    double fp_guess = *fp_guess_io;
-    int counter = 0;
-    while (fabs(p - p_guess) > 1e-6 * 0.5 * (p + p_guess) && fp_guess < 0.0) {
-        p = p_guess;
-        const bool lo_left = l.p <= r.p;
-        const double d_lo = ex_fprimeb(p_guess, lo_left ? l : r, g);
-        const double d_hi = ex_fprimeb(p_guess, lo_left ? r : l, g);
-        p_guess = p_guess - fp_guess / ((lo_left ? d_lo : d_hi) + (lo_left ? d_hi : d_lo));
-        fp_guess = ex_f(p_guess, l, r, vl, vr, g);
-        counter += 1;
-        if (counter > max_iter) {  // the reference panics here
-            *err |= 1u;
-            break;
-        }
-    }
-    *p_guess_io = p_guess;
-    *fp_guess_io = fp_guess;
-    return fabs(p - p_guess) > 1e-6 * 0.5 * (p + p_guess) && fp_guess > 0.;
-}
 // Brent's method on [0, p_guess] as the reference calls it
 __device__ __forceinline__ double ex_star_brent(double p_guess, double fp_guess, const ExSide& l, const ExSide& r,
                                                 double vl, double vr, const Gas<double>& g, int max_iter,
@@ -781,13 +757,6 @@ __device__ __forceinline__ double ex_star_brent(double p_guess, double fp_guess,
     double p = 0.;
     double fp = ex_f0(l, r, vl, vr, g);  // p = 0
     return ex_brent(p, p_guess, fp, fp_guess, 1e-6, l, r, vl, vr, g, max_iter, err);
-}
-// The same with f(0) as ex_star_start formed it (the reference evaluates it
-// again here, on the same inputs: the same value)
-__device__ __forceinline__ double ex_star_brent0(double p_guess, double fp_guess, double fp0, const ExSide& l,
-                                                 const ExSide& r, double vl, double vr, const Gas<double>& g,
-                                                 int max_iter, unsigned int* err) {
-    return ex_brent(0., p_guess, fp0, fp_guess, 1e-6, l, r, vl, vr, g, max_iter, err);
 }
 // star_state_from_pstar (:214-238)
 __device__ __forceinline__ Star<double> ex_star_post(double p, const ExSide& l, const ExSide& r, double vl, double vr,

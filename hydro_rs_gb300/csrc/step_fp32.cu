@@ -317,24 +317,31 @@ __global__ void __launch_bounds__(kMaxBlock, FACE32_MINB) k_face_flux32(KP p) {
             int l = p.left[f], r = p.right[f];
             bool la = p.active[l] != 0;
             Out32 o;
+            // The timesteps are non-negative doubles, which order as their bit
+            // patterns (the sign bit cleared, so that -0 ties with +0): the
+            // active-face rule and fmin(dt_l, dt_r) on the integer pipe, and dt
+            // rounded to FP32 there too (to_f32_rn), keep this kernel off the
+            // FP64 pipe.
             double dt = 0.;
             if (r >= 0) {
                 bool ra = p.active[r] != 0;
-                double dtl = C(p, F_DT, l), dtr = C(p, F_DT, r);
-                if (interior_face_active(la, ra, dtl, dtr)) {
-                    dt = fmin(dtl, dtr);
-                    o = face_interior32<SOLVER>(p, f, l, r, (float)dt, g, g64, &err);
+                const double dtl = C(p, F_DT, l), dtr = C(p, F_DT, r);
+                const long long kl = __double_as_longlong(dtl) & 0x7fffffffffffffffLL;
+                const long long kr = __double_as_longlong(dtr) & 0x7fffffffffffffffLL;
+                if (!((!la && !ra) || (kr < kl && !ra) || (kl < kr && !la))) {  // interior_face_active
+                    dt = kl <= kr ? dtl : dtr;
+                    o = face_interior32<SOLVER>(p, f, l, r, f32(dt), g, g64, &err);
                     counted = true;
                 }
             } else if (la) {
                 dt = C(p, F_DT, l);
-                o = face_boundary32<SOLVER>(p, f, l, (float)dt, g, g64, &err);
+                o = face_boundary32<SOLVER>(p, f, l, f32(dt), g, g64, &err);
                 counted = true;
             }
             if (p.flux_rows == 7) {
                 // step: FP32 rows dt * area * F, v_max, a_over_r (accumulated in FP64 by the update)
                 float* out = p.flux32;
-                float da = counted ? (float)dt * p.geo[GE_A * nf + f] : 0.f;
+                float da = counted ? f32(dt) * p.geo[GE_A * nf + f] : 0.f;
 #pragma unroll
                 for (int q = 0; q < 5; q++) out[q * nf + f] = counted ? da * o.F.q[q] : 0.f;
                 out[5 * nf + f] = counted ? o.v_max : 0.f;

@@ -229,11 +229,37 @@ struct BrentJob {
 };
 // The exact solver's flux from the star pressure on (riemann_solver.rs:258-284,
 // exact.rs:214-238), as star_half_state + flux_from_half_state do.
+// The two sides of sample_star are written once, for the side x/t = 0 falls
+// on: that side's state, velocity and signed sound speed are selected, and its
+// comparisons carry the side's sign, so the lanes of a warp run one code path
+// whichever side each samples.  Every comparison and value is the one
+// sample_star forms on that side, and only that side's middle density
+// (star_state_from_pstar forms both; sample_star reads one) is formed.
 __device__ __forceinline__ St<double> exact_flux_from_p(double pst, const FacePre& q, double vl, double vr, double al,
                                                         double ar, const Gas<double>& g) {
-    ExSide L{q.l.q[0], q.l.q[4], al}, R{q.r.q[0], q.r.q[4], ar};
-    Star<double> s = ex_star_post(pst, L, R, vl, vr, g);
-    St<double> w = sample_star(s, q.l, q.r, vl, vr, al, ar, q.n, g);
+    const ExSide L{q.l.q[0], q.l.q[4], al}, R{q.r.q[0], q.r.q[4], ar};
+    // star_state_from_pstar's u, its two terms in ex_f's branch-coherent order
+    const bool lo_left = L.p <= R.p;
+    const double t_lo = ex_fb(pst, lo_left ? L : R, g);
+    const double t_hi = ex_fb(pst, lo_left ? R : L, g);
+    const double u = 0.5 * (vl + vr) + 0.5 * ((lo_left ? t_hi : t_lo) - (lo_left ? t_lo : t_hi));
+    // sample_star (riemann_solver.rs:224-255): u < 0 samples the right side
+    const bool right = u < 0.;
+    const St<double> s = right ? q.r : q.l;
+    const ExSide S = right ? R : L;
+    const double v = right ? vr : vl;
+    const double a = right ? -ar : al;  // the sampler's signed sound speed
+    const double sg = right ? -1. : 1.;
+    St<double> w;
+    if (pst > s.q[4]) {  // shock
+        const double sp = shock_speed(v, a, pst / s.q[4], g);
+        w = sg * sp < 0. ? sample_middle(ex_middle_density(pst, S, g), u, pst, s, v, q.n) : s;
+    } else if (sg * (v - a) < 0.) {  // rarefaction whose head lies on the other side of x/t = 0
+        if (sg * rarefaction_tail_speed(u, a, pst / s.q[4], g) > 0.) w = sample_rarefaction_fan(s, a, v, q.n, g);
+        else w = sample_middle(ex_middle_density(pst, S, g), u, pst, s, v, q.n);
+    } else {
+        w = s;
+    }
     return flux_from_half_state(w, q.iv, q.n, g);
 }
 
@@ -241,7 +267,7 @@ __device__ __forceinline__ St<double> exact_flux_from_p(double pst, const FacePr
 // dt = min(dt_l, dt_r), interior / boundary dispatch.
 // QUEUE (the exact solver with its job queues): every face's solve is queued.
 template <int SOLVER, bool QUEUE = false>
-__global__ void __launch_bounds__(kMaxBlock) k_face_flux(KP p) {
+__global__ void __launch_bounds__(kMaxBlock, (QUEUE ? 2 : 0)) k_face_flux(KP p) {
     if (p.use_list && p.tl[0].done) return;
     const Gas<double> g = gas(p);
     // all faces (one per thread), or the compacted active-face list (grid-stride)
@@ -359,99 +385,15 @@ __device__ __forceinline__ unsigned int queue_count(const KP& p, int qi) {
     return min(p.brent_count[qi], (unsigned int)p.brent_cap);
 }
 
-// The queued Brent searches of the exact solver's faces.  Searches end after
-// different numbers of evaluations, so a warp that ran one search per lane
-// would hold the FP64 pipe for all 32 lanes until its longest search ended.
-// Here every lane runs its search one evaluation of f at a time
-// (BrentMachine) and, when it ends, takes the next job of the queue (a
-// warp-aggregated fetch from a counter), so the warps stay full until the queue
-// runs dry.  Each job's star pressure goes back into its p_guess for
-// k_face_finish.
-__device__ __forceinline__ void brent_start(const BrentJob& J, const Gas<double>& g, int max_iter, BrentMachine& m,
-                                            ExSide& L, ExSide& R, double& vl, double& vr, int& k) {
-    L = ExSide{J.q.l.q[0], J.q.l.q[4], J.al};
-    R = ExSide{J.q.r.q[0], J.q.r.q[4], J.ar};
-    vl = J.vl;
-    vr = J.vr;
-    k = J.k;
-    m.start(0., J.p_guess, J.fp0, J.fp_guess, 1e-6, max_iter);  // ex_star_brent0
-}
-__global__ void __launch_bounds__(kJobTile) k_face_brent(KP p) {
-    const Gas<double> g = gas(p);
-    const unsigned int n_jobs = queue_count(p, 0);
-    BrentJob* jobs = queue_jobs(p, 0);
-    unsigned int* next = p.brent_count + kExactQueues;  // jobs handed out
-    const unsigned int lane = threadIdx.x & 31;
-    int j = -1, k = 0;
-    bool dry = false;
-    BrentMachine m;
-    ExSide L, R;
-    double vl = 0., vr = 0.;
-    while (true) {
-        // lanes without a search take jobs until each holds one that needs f, or the queue is dry
-        while (true) {
-            const unsigned int need = __ballot_sync(0xffffffffu, j < 0 && !dry);
-            if (!need) break;
-            const int leader = __ffs(need) - 1;
-            unsigned int base = 0;
-            if ((int)lane == leader) base = atomicAdd(next, (unsigned int)__popc(need));
-            base = __shfl_sync(0xffffffffu, base, leader);
-            if (need & (1u << lane)) {
-                const unsigned int t = base + (unsigned int)__popc(need & ((1u << lane) - 1u));
-                if (t < n_jobs) {
-                    j = (int)t;
-                    brent_start(jobs[j], g, p.max_iter, m, L, R, vl, vr, k);
-                    if (m.done) {
-                        jobs[j].p_guess = m.b;
-                        if (m.err) set_err(p, k, m.err);
-                        j = -1;
-                    }
-                } else {
-                    dry = true;
-                }
-            }
-        }
-        if (!__any_sync(0xffffffffu, j >= 0)) break;
-        if (j >= 0) {
-            m.step(ex_f(m.x, L, R, vl, vr, g));
-            if (m.done) {
-                jobs[j].p_guess = m.b;
-                if (m.err) set_err(p, k, m.err);
-                j = -1;
-            }
-        }
-    }
-}
-
-// The queued Newton searches (the second queue): every job runs the Newton
-// loop from the guess (exact.rs:255-275), then, where the loop ends above the
-// root, Brent's method as ex_star_pre's caller would; the star pressure goes
-// back into its p_guess.
-__global__ void __launch_bounds__(kJobTile) k_face_newton(KP p) {
-    __shared__ int s_count[4], s_order[kJobTile];
-    const Gas<double> g = gas(p);
-    const unsigned int n_jobs = queue_count(p, 1);
-    BrentJob* jobs = queue_jobs(p, 1);
-    auto job = [&](unsigned int t) -> const BrentJob& { return jobs[t]; };
-    for (unsigned int base = blockIdx.x * kJobTile; base < n_jobs; base += gridDim.x * kJobTile) {
-        const int j = sorted_job(job, base, n_jobs, s_count, s_order);
-        if (j < 0) continue;
-        const BrentJob J = jobs[j];
-        unsigned int err = 0;
-        ExSide L{J.q.l.q[0], J.q.l.q[4], J.al}, R{J.q.r.q[0], J.q.r.q[4], J.ar};
-        double pg = J.p_guess, fpg = J.fp_guess;
-        const bool brent = ex_newton(L, R, J.vl, J.vr, g, p.max_iter, &err, &pg, &fpg);
-        jobs[j].p_guess = brent ? ex_star_brent0(pg, fpg, J.fp0, L, R, J.vl, J.vr, g, p.max_iter, &err) : pg;
-        if (err) set_err(p, J.k, err);
-    }
-}
-
-// Both search queues in one pool: Newton jobs first, then Brent jobs.  A lane
-// runs its search one evaluation of f at a time (NewtonMachine, then
-// BrentMachine where the Newton loop ends above the root, as k_face_newton; or
-// BrentMachine alone, as k_face_brent) and, when it ends, takes the next job,
-// so the warps stay full until both queues run dry.  Each job's star pressure
-// goes back into its p_guess for k_face_finish.
+// Both search queues in one pool: Newton jobs first, then Brent jobs.
+// Searches end after different numbers of evaluations, so a warp that ran one
+// search per lane would hold the FP64 pipe for all 32 lanes until its longest
+// search ended.  Here a lane runs its search one evaluation of f at a time
+// (NewtonMachine, then BrentMachine on [0, p] where the Newton loop ends above
+// the root; or BrentMachine alone, from the guess and f(0) the face kernel
+// formed) and, when it ends, takes the next job (a warp-aggregated fetch from a
+// counter), so the warps stay full until both queues run dry.  Each job's star
+// pressure goes back into its p_guess for k_face_finish.
 struct SearchLane {
     int j = -1;        // job (index into the combined queue), or -1
     int k = 0;         // its simulation
@@ -468,7 +410,7 @@ __device__ __forceinline__ void search_after_newton(SearchLane& s, int max_iter)
     s.err |= s.nm.err;
     if (s.nm.brent) {
         s.newton = false;
-        s.bm.start(0., s.nm.pg, s.fp0, s.nm.fpg, 1e-6, max_iter);  // ex_star_brent0
+        s.bm.start(0., s.nm.pg, s.fp0, s.nm.fpg, 1e-6, max_iter);  // Brent on [0, p], f(0) as formed
     }
 }
 __device__ __forceinline__ double search_result(SearchLane& s) {
@@ -476,7 +418,39 @@ __device__ __forceinline__ double search_result(SearchLane& s) {
     s.err |= s.bm.err;
     return s.bm.b;
 }
-__global__ void __launch_bounds__(kJobTile) k_face_search(KP p) {
+// The searches' evaluations of f are regrouped across the block: the lanes of
+// a warp holding different jobs would take different branches of fb (shock or
+// rarefaction on each side, depending on where x lies against the two side
+// pressures) and run both.  Each round every lane with a search posts its x and
+// its job's sides in shared memory, the block sorts the posts by that branch
+// pattern (a counting sort), each thread evaluates ex_f for the post at its
+// place, and the owner reads its value back: the same function on the same
+// data, so the same bits, with most warps on one pattern.
+constexpr int kSearchBlock = 256;
+struct EvalPost {
+    double x, vl, vr;
+    ExSide L, R;
+};
+__device__ __forceinline__ int ex_f_key(double x, const ExSide& L, const ExSide& R) {
+    const double lo = fmin(L.p, R.p), hi = fmax(L.p, R.p);
+    return (x > lo ? 1 : 0) + (x > hi ? 1 : 0);
+}
+// The index of the post this thread evaluates (key 3: no post), posts sorted by key.
+__device__ __forceinline__ int block_sorted(int key, int* s_count, int* s_order) {
+    if (threadIdx.x < 4) s_count[threadIdx.x] = 0;
+    __syncthreads();
+    const int rank = atomicAdd(&s_count[key], 1);
+    __syncthreads();
+    int start = 0;
+    for (int k = 0; k < key; k++) start += s_count[k];
+    s_order[start + rank] = key < 3 ? (int)threadIdx.x : -1;
+    __syncthreads();
+    return s_order[threadIdx.x];
+}
+__global__ void __launch_bounds__(kSearchBlock) k_face_search(KP p) {
+    __shared__ EvalPost s_post[kSearchBlock];
+    __shared__ double s_res[kSearchBlock];
+    __shared__ int s_count[4], s_order[kSearchBlock];
     const Gas<double> g = gas(p);
     const unsigned int n1 = queue_count(p, 1), n0 = queue_count(p, 0);
     const unsigned int n_jobs = n1 + n0;
@@ -518,7 +492,7 @@ __global__ void __launch_bounds__(kJobTile) k_face_search(KP p) {
                         s.nm.start(J.p_guess, J.fp_guess, p.max_iter, s.L, s.R, g);
                         if (s.nm.done) search_after_newton(s, p.max_iter);
                     } else {
-                        s.bm.start(0., J.p_guess, J.fp0, J.fp_guess, 1e-6, p.max_iter);  // ex_star_brent0
+                        s.bm.start(0., J.p_guess, J.fp0, J.fp_guess, 1e-6, p.max_iter);  // on [0, guess]
                     }
                     if (search_lane_done(s)) retire();
                 } else {
@@ -526,9 +500,22 @@ __global__ void __launch_bounds__(kJobTile) k_face_search(KP p) {
                 }
             }
         }
-        if (!__any_sync(0xffffffffu, s.j >= 0)) break;
-        if (s.j >= 0) {
-            const double fx = ex_f(s.newton ? s.nm.x : s.bm.x, s.L, s.R, s.vl, s.vr, g);
+        const bool has = s.j >= 0;
+        if (!__syncthreads_or(has)) break;  // block-uniform: every lane's search has ended, the queues are dry
+        int key = 3;
+        if (has) {
+            const double x = s.newton ? s.nm.x : s.bm.x;
+            s_post[threadIdx.x] = EvalPost{x, s.vl, s.vr, s.L, s.R};
+            key = ex_f_key(x, s.L, s.R);
+        }
+        const int o = block_sorted(key, s_count, s_order);
+        if (o >= 0) {
+            const EvalPost e = s_post[o];
+            s_res[o] = ex_f(e.x, e.L, e.R, e.vl, e.vr, g);
+        }
+        __syncthreads();
+        if (has) {
+            const double fx = s_res[threadIdx.x];
             if (s.newton) {
                 s.nm.step(fx, s.L, s.R, g);
                 if (s.nm.done) search_after_newton(s, p.max_iter);
@@ -1442,9 +1429,9 @@ size_t brent_job_bytes() { return sizeof(BrentJob); }
 // The pools' lanes draw jobs until the queues are dry: as many blocks as fit
 // on the device at once
 template <class K>
-int pool_grid(const KP& p, K kernel) {
+int pool_grid(const KP& p, K kernel, int block) {
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kJobTile, 0) != cudaSuccess || per_sm < 1)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0) != cudaSuccess || per_sm < 1)
         per_sm = 1;
     return p.n_sms * per_sm;
 }
@@ -1455,7 +1442,7 @@ void launch_face_flux_fp64(const KP& p, int solver, cudaStream_t s) {
     else if (solver == SOLVER_EXACT && p.brent_jobs) {
         cudaMemsetAsync(p.brent_count, 0, (kExactQueues + 1) * sizeof(unsigned int), s);
         k_face_flux<SOLVER_EXACT, true><<<g, p.blk_face, 0, s>>>(p);
-        k_face_search<<<pool_grid(p, k_face_search), kJobTile, 0, s>>>(p);
+        k_face_search<<<pool_grid(p, k_face_search, kSearchBlock), kSearchBlock, 0, s>>>(p);
         const int finish_grid =
             (int)std::min<long long>((kExactQueues * (long long)p.brent_cap + kJobTile - 1) / kJobTile, p.n_sms * 16LL);
         k_face_finish<<<finish_grid, kJobTile, 0, s>>>(p);
