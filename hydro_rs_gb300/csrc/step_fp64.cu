@@ -267,7 +267,7 @@ __device__ __forceinline__ St<double> exact_flux_from_p(double pst, const FacePr
 // dt = min(dt_l, dt_r), interior / boundary dispatch.
 // QUEUE (the exact solver with its job queues): every face's solve is queued.
 template <int SOLVER, bool QUEUE = false>
-__global__ void __launch_bounds__(kMaxBlock, (QUEUE ? 2 : 0)) k_face_flux(KP p) {
+__global__ void __launch_bounds__(kMaxBlock) k_face_flux(KP p) {
     if (p.use_list && p.tl[0].done) return;
     const Gas<double> g = gas(p);
     // all faces (one per thread), or the compacted active-face list (grid-stride)
