@@ -232,10 +232,15 @@ struct Out32 {
     V3<float> dx;    // generator separation (mflux direction)
     float v_max, a_over_r;
 };
+// A face up to its Riemann solve: the two states handed to the solver (in the
+// face frame), the face velocity and normal, and what the result needs.
+struct Pre32 {
+    St<float> l, r;
+    V3<float> iv, n, dx;
+    float v_max, a_over_r;
+};
 
-template <int SOLVER>
-__device__ __forceinline__ Out32 face_interior32(const KP& p, int f, int l, int r, float dt, const Gas<float>& g,
-                                                 const Gas<double>& g64, unsigned int* err) {
+__device__ __forceinline__ Pre32 face_interior32_pre(const KP& p, int f, int l, int r, float dt) {
     V3<float> dx = GE3(p, GE_DX, f);
     V3<float> dx_left = GE3(p, GE_RL, f) - G3(p, G_DGC, l);
     V3<float> dx_right = GE3(p, GE_RR, f) - G3(p, G_DGC, r);
@@ -252,20 +257,18 @@ __device__ __forceinline__ Out32 face_interior32(const KP& p, int f, int l, int 
     V3<float> vl = G3(p, G_V, l), vr = G3(p, G_V, r);
     float fac = dot(vr - vl, GE3(p, GE_FCM, f)) / len2(dx);
     V3<float> v_face = 0.5f * (vl + vr) - fac * dx;
-    V3<float> nrm = GE3(p, GE_N, f);
     V3<float> mvf = neg(v_face);
-    Out32 o;
-    o.F = solve_for_flux<float, SOLVER>(boost(prim_left, mvf), boost(prim_right, mvf), v_face, nrm, g, g64,
-                                        p.max_iter, err, &p.rsx);
-    o.dx = dx;
-    o.v_max = v_max;
-    o.a_over_r = p.geo[GE_A * (size_t)p.nf + f] / len(dx);  // feeds max_a_over_r only (mesh steering)
-    return o;
+    Pre32 q;
+    q.l = boost(prim_left, mvf);
+    q.r = boost(prim_right, mvf);
+    q.iv = v_face;
+    q.n = GE3(p, GE_N, f);
+    q.dx = dx;
+    q.v_max = v_max;
+    q.a_over_r = p.geo[GE_A * (size_t)p.nf + f] / len(dx);  // feeds max_a_over_r only (mesh steering)
+    return q;
 }
-
-template <int SOLVER>
-__device__ __forceinline__ Out32 face_boundary32(const KP& p, int f, int i, float dt, const Gas<float>& g,
-                                                 const Gas<double>& g64, unsigned int* err) {
+__device__ __forceinline__ Pre32 face_boundary32_pre(const KP& p, int f, int i, float dt) {
     V3<float> n = GE3(p, GE_N, f);
     V3<float> dx_face = GE3(p, GE_RL, f) - G3(p, G_DGC, i);       // fc - gc
     float dx_gradients = len((2.f * dot(dx_face, n)) * n);        // |reflect(gc) - gc|
@@ -291,14 +294,26 @@ __device__ __forceinline__ Out32 face_boundary32(const KP& p, int f, int i, floa
         v_max += fminf(dot(vel(prim), dx_centroid), 0.f);
         bnd = vac;
     }
+    Pre32 q;
+    q.l = dash;
+    q.r = bnd;
+    q.iv = v3(0.f, 0.f, 0.f);
+    q.n = n;
+    q.dx = dx;
+    q.v_max = v_max;
+    q.a_over_r = p.geo[GE_A * (size_t)p.nf + f] / len(dx);
+    return q;
+}
+template <int SOLVER>
+__device__ __forceinline__ Out32 face_solve32(const KP& p, const Pre32& q, const Gas<float>& g,
+                                              const Gas<double>& g64, unsigned int* err) {
     Out32 o;
-    o.F = solve_for_flux<float, SOLVER>(dash, bnd, v3(0.f, 0.f, 0.f), n, g, g64, p.max_iter, err, &p.rsx);
-    o.dx = dx;
-    o.v_max = v_max;
-    o.a_over_r = p.geo[GE_A * (size_t)p.nf + f] / len(dx);
+    o.F = solve_for_flux<float, SOLVER>(q.l, q.r, q.iv, q.n, g, g64, p.max_iter, err, &p.rsx);
+    o.dx = q.dx;
+    o.v_max = q.v_max;
+    o.a_over_r = q.a_over_r;
     return o;
 }
-
 template <int SOLVER>
 __global__ void __launch_bounds__(kMaxBlock, FACE32_MINB) k_face_flux32(KP p) {
     if (p.use_list && p.tl[0].done) return;
@@ -330,12 +345,12 @@ __global__ void __launch_bounds__(kMaxBlock, FACE32_MINB) k_face_flux32(KP p) {
                 const long long kr = __double_as_longlong(dtr) & 0x7fffffffffffffffLL;
                 if (!((!la && !ra) || (kr < kl && !ra) || (kl < kr && !la))) {  // interior_face_active
                     dt = kl <= kr ? dtl : dtr;
-                    o = face_interior32<SOLVER>(p, f, l, r, f32(dt), g, g64, &err);
+                    o = face_solve32<SOLVER>(p, face_interior32_pre(p, f, l, r, f32(dt)), g, g64, &err);
                     counted = true;
                 }
             } else if (la) {
                 dt = C(p, F_DT, l);
-                o = face_boundary32<SOLVER>(p, f, l, f32(dt), g, g64, &err);
+                o = face_solve32<SOLVER>(p, face_boundary32_pre(p, f, l, f32(dt)), g, g64, &err);
                 counted = true;
             }
             if (p.flux_rows == 7) {
@@ -363,6 +378,101 @@ __global__ void __launch_bounds__(kMaxBlock, FACE32_MINB) k_face_flux32(KP p) {
         }
         inst_count(p, k, (err & kInfoFallback) != 0, CNT_FALLBACK);
         if (!p.use_list) inst_count(p, k, counted, CNT_FACES);
+    }
+}
+
+// Steps of the FP32-face form run the face stage as two kernels joined by the
+// faces' reconstructed states, so that neither holds the registers of both the
+// reconstruction (two cells' gathers, the limiter) and the Riemann solve:
+// k_face_rec32 writes per face the two states handed to the solver, the face
+// velocity and dt * area (-1: the face is not active, -2: its simulation has
+// finished), and the rows v_max and a_over_r; k_face_riemann32 solves and
+// writes the flux rows.  The arithmetic is the fused kernel's.
+__global__ void __launch_bounds__(kMaxBlock, 4) k_face_rec32(KP p) {
+    if (p.use_list && p.tl[0].done) return;
+    const int n_items = p.use_list ? (int)p.tl[0].n_list : p.nf;
+    const size_t nf = (size_t)p.nf;
+    for (int base = blockIdx.x * blockDim.x; base < n_items; base += gridDim.x * blockDim.x) {
+        int idx = base + threadIdx.x;
+        int f = idx < n_items ? (p.use_list ? p.face_list[idx] : idx) : -1;
+        int k = f >= 0 ? inst_of(p, p.left[f]) : -1;
+        if (k >= 0 && p.tl[k].done) k = -1;
+        bool counted = false;
+        if (f >= 0) {
+            float* hs = p.hs32;
+            if (k >= 0) {
+                int l = p.left[f], r = p.right[f];
+                bool la = p.active[l] != 0;
+                Pre32 q;
+                double dt = 0.;
+                if (r >= 0) {
+                    bool ra = p.active[r] != 0;
+                    const double dtl = C(p, F_DT, l), dtr = C(p, F_DT, r);
+                    const long long kl = __double_as_longlong(dtl) & 0x7fffffffffffffffLL;
+                    const long long kr = __double_as_longlong(dtr) & 0x7fffffffffffffffLL;
+                    if (!((!la && !ra) || (kr < kl && !ra) || (kl < kr && !la))) {  // interior_face_active
+                        dt = kl <= kr ? dtl : dtr;
+                        q = face_interior32_pre(p, f, l, r, f32(dt));
+                        counted = true;
+                    }
+                } else if (la) {
+                    dt = C(p, F_DT, l);
+                    q = face_boundary32_pre(p, f, l, f32(dt));
+                    counted = true;
+                }
+                if (counted) {
+#pragma unroll
+                    for (int c = 0; c < 5; c++) {
+                        hs[c * nf + f] = q.l.q[c];
+                        hs[(5 + c) * nf + f] = q.r.q[c];
+                    }
+                    hs[10 * nf + f] = q.iv.x;
+                    hs[11 * nf + f] = q.iv.y;
+                    hs[12 * nf + f] = q.iv.z;
+                }
+                hs[13 * nf + f] = counted ? f32(dt) * p.geo[GE_A * nf + f] : -1.f;
+                p.flux32[5 * nf + f] = counted ? q.v_max : 0.f;
+                p.flux32[6 * nf + f] = counted ? q.a_over_r : 0.f;
+            } else {
+                hs[13 * nf + f] = -2.f;
+            }
+        }
+        if (!p.use_list) inst_count(p, k, counted, CNT_FACES);
+    }
+}
+template <int SOLVER>
+__global__ void __launch_bounds__(kMaxBlock, FACE32_MINB) k_face_riemann32(KP p) {
+    if (p.use_list && p.tl[0].done) return;
+    const Gas<float> g = gas_t<float>(p);
+    const Gas<double> g64 = gas_t<double>(p);
+    const int n_items = p.use_list ? (int)p.tl[0].n_list : p.nf;
+    const size_t nf = (size_t)p.nf;
+    for (int base = blockIdx.x * blockDim.x; base < n_items; base += gridDim.x * blockDim.x) {
+        int idx = base + threadIdx.x;
+        int f = idx < n_items ? (p.use_list ? p.face_list[idx] : idx) : -1;
+        const float da = f >= 0 ? p.hs32[13 * nf + f] : -2.f;
+        unsigned int err = 0;
+        int k = -1;
+        if (da >= 0.f) {
+            const float* hs = p.hs32;
+            Pre32 q;
+#pragma unroll
+            for (int c = 0; c < 5; c++) {
+                q.l.q[c] = hs[c * nf + f];
+                q.r.q[c] = hs[(5 + c) * nf + f];
+            }
+            q.iv = v3(hs[10 * nf + f], hs[11 * nf + f], hs[12 * nf + f]);
+            q.n = GE3(p, GE_N, f);
+            const St<float> F = solve_for_flux<float, SOLVER>(q.l, q.r, q.iv, q.n, g, g64, p.max_iter, &err, &p.rsx);
+#pragma unroll
+            for (int c = 0; c < 5; c++) p.flux32[c * nf + f] = da * F.q[c];
+            k = inst_of(p, p.left[f]);
+            if (err & ~kInfoFallback) set_err(p, k, err & ~kInfoFallback);
+        } else if (da == -1.f) {
+#pragma unroll
+            for (int c = 0; c < 5; c++) p.flux32[c * nf + f] = 0.f;
+        }
+        inst_count(p, k, (err & kInfoFallback) != 0, CNT_FALLBACK);
     }
 }
 
@@ -800,6 +910,14 @@ void launch_face_flux_fp32(const KP& p, int solver, cudaStream_t s) {
     if (p.nf <= 0) return;
     int g = grid(p.nf, p.blk_face), cap = p.n_sms * 512 / p.blk_face;
     if (p.use_list && g > cap) g = cap;
+    if (p.flux_rows == 7 && p.hs32) {  // a step: the face stage in two kernels
+        k_face_rec32<<<g, p.blk_face, 0, s>>>(p);
+        if (solver == SOLVER_HLLC) k_face_riemann32<SOLVER_HLLC><<<g, p.blk_face, 0, s>>>(p);
+        else if (solver == SOLVER_EXACT) k_face_riemann32<SOLVER_EXACT><<<g, p.blk_face, 0, s>>>(p);
+        else if (solver == SOLVER_PVRS) k_face_riemann32<SOLVER_PVRS><<<g, p.blk_face, 0, s>>>(p);
+        else k_face_riemann32<SOLVER_EXTRA><<<g, p.blk_face, 0, s>>>(p);
+        return;
+    }
     if (solver == SOLVER_HLLC) k_face_flux32<SOLVER_HLLC><<<g, p.blk_face, 0, s>>>(p);
     else if (solver == SOLVER_EXACT) k_face_flux32<SOLVER_EXACT><<<g, p.blk_face, 0, s>>>(p);
     else if (solver == SOLVER_PVRS) k_face_flux32<SOLVER_PVRS><<<g, p.blk_face, 0, s>>>(p);
