@@ -263,15 +263,15 @@ def face_stage_bytes(prec, nc, nfa, all_cells):
 STEP_BYTES_FACE = 88
 STEP_BYTES_CELL = {0: 800, 1: 636}
 
-# FP64 flop per face of the plain face stage (k_face_flux + k_face_newton +
-# k_face_brent; 2 DFMA + DMUL + DADD over active threads) from an ncu capture
+# FP64 flop per face of the plain face stage (k_face_flux + k_face_search +
+# k_face_finish; 2 DFMA + DMUL + DADD over active threads) from an ncu capture
 # at the bench size: profiles/face_stage_fp64_exact_pipes_kh256.txt.
-FP64_FLOP_PER_FACE = {("kh2d", 256): 1483}
+FP64_FLOP_PER_FACE = {("kh2d", 256): 1506}
 
 
 def face_stage_kernels(prec, all_cells, riemann=None):
     if prec == 0:
-        return "k_face_flux + k_face_newton + k_face_brent + k_face_finish" if riemann == 1 else "k_face_flux"
+        return "k_face_flux + k_face_search + k_face_finish" if riemann == 1 else "k_face_flux"
     return "k_face_flux32" if all_cells else "k_prep32 + k_face_flux32"
 
 
@@ -593,10 +593,10 @@ def run_ours(args):
                       "roofline": roof(1), "step_roofline": step_roof(1, ms32 / args.steps)},
         "cpu_baseline": cpu,
         # per step, both forms timed: over all cells k_predict / k_predict32, face, update, gradients,
-        # limiter (5 + 5); the plain form's exact solver adds k_face_newton, k_face_brent and k_face_finish;
+        # limiter (5 + 5); the plain form's exact solver adds k_face_search and k_face_finish;
         # hierarchical steps add k_compact to both and k_prep32 to the FP32 form, and each form's
         # timed region ends with one k_extrap_flush
-        "gpu_launches": args.steps * ((5 + 5) + (3 if exact else 0) + (3 if hier else 0)) + (2 if hier else 0),
+        "gpu_launches": args.steps * ((5 + 5) + (2 if exact else 0) + (3 if hier else 0)) + (2 if hier else 0),
         "clocks": clocks,
     }
     print(json.dumps(line))

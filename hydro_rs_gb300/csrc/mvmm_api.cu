@@ -67,7 +67,6 @@ struct mvmm_ctx {
     double* flux = nullptr;
     float* flux32 = nullptr;
     float* geo = nullptr;
-    float* hs32 = nullptr;  // FP32 form: reconstructed face states of a step (KP::hs32)
     unsigned long long* geo_pos = nullptr;  // FP32 form: loc and centroid bits of the last geometry build
     uint8_t* geo_changed = nullptr;
     bool geo_built = false;  // the FP32 geometry matches the current face arrays
@@ -167,7 +166,6 @@ KP make_kp(mvmm_ctx* c, int stage, int flux_rows) {
     p.flux = c->flux;
     p.flux32 = c->flux32;
     p.geo = c->geo;
-    p.hs32 = c->hs32;
     p.geo_pos = c->geo_pos;
     p.geo_changed = c->geo_changed;
     p.fp32 = c->prm.precision == MVMM_PRECISION_FP32FACE ? 1 : 0;
@@ -535,7 +533,6 @@ static int create_impl(const mvmm_params* prm, const mvmm_mesh* m, int64_t n_ins
         ALLOC(c->cf, (size_t)kCellFields32 * n * 4);
         ALLOC(c->flux32, 7 * nf * 4);
         ALLOC(c->geo, (size_t)kFaceGeom32 * nf * 4);
-        ALLOC(c->hs32, (size_t)kHalfRows32 * nf * 4);
         ALLOC(c->geo_pos, 6 * n * 8);
         ALLOC(c->geo_changed, n);
     }
@@ -669,7 +666,7 @@ int mvmm_ctx_destroy(mvmm_ctx* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     drop_graphs(c);
     void* ptrs[] = {c->left, c->right, c->csr_off, c->csr_face, c->area, c->normal, c->fcen, c->shift, c->cd,
-                    c->cf, c->timebin, c->tb_tmp, c->active, c->flux, c->flux32, c->geo, c->hs32, c->geo_pos, c->geo_changed, c->snap, c->snap_tb, c->xfer_stored, c->brent_jobs, c->brent_count, c->extrap_step, c->dt_log, c->dtmp, c->face_stamp, c->touch, c->blocks_done, c->cell_list, c->fresh, c->cf_fresh,
+                    c->cf, c->timebin, c->tb_tmp, c->active, c->flux, c->flux32, c->geo, c->geo_pos, c->geo_changed, c->snap, c->snap_tb, c->xfer_stored, c->brent_jobs, c->brent_count, c->extrap_step, c->dt_log, c->dtmp, c->face_stamp, c->touch, c->blocks_done, c->cell_list, c->fresh, c->cf_fresh,
                     c->pend_vol, c->pend_cen, c->dirty, c->chg_list,
                     c->face_list, c->tl,
                     c->inst, c->inst_tb, c->inst_tbi};
@@ -1539,8 +1536,7 @@ int mvmm_set_mesh(mvmm_ctx* c, const mvmm_mesh* m, const double* volume, const d
                     {(void**)&c->flux, (size_t)cap * 80},      {(void**)&c->face_stamp, (size_t)cap * 4},
                     {(void**)&c->face_list, (size_t)cap * 4},  {(void**)&c->csr_face, (size_t)ccap * 4},
                     {(void**)&c->flux32, c->flux32 ? (size_t)cap * 28 : 0},
-                    {(void**)&c->geo, c->geo ? (size_t)cap * 4 * kFaceGeom32 : 0},
-                    {(void**)&c->hs32, c->hs32 ? (size_t)cap * 4 * kHalfRows32 : 0}};
+                    {(void**)&c->geo, c->geo ? (size_t)cap * 4 * kFaceGeom32 : 0}};
         for (auto& b : bufs) {
             if (!b.bytes) continue;
             cudaFree(*b.ptr);

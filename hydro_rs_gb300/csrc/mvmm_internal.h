@@ -103,10 +103,6 @@ constexpr int kDtLog = 4096;
 // holds brent_cap jobs.
 constexpr int kExactQueues = 3;
 
-// Rows of KP::hs32: the solver's left and right states (5 + 5), the face
-// velocity (3), dt * area (or -1: the face is not active; -2: no result).
-constexpr int kHalfRows32 = 14;
-
 // KP::dirty marks: the cell's extrapolation rows changed, or any of its rows.
 constexpr uint8_t kDirtyExtrap = 1, kDirtyAll = 2;
 
@@ -133,8 +129,6 @@ struct KP {
     double* flux;            // face results, rows of nf
     float* flux32;           // FP32 form face results of a step, rows of nf: 5 fluxes, v_max, a_over_r
     float* geo;              // FP32 form static face geometry (FaceGeom32)
-    float* hs32;             // FP32 form steps: the faces' reconstructed states between k_face_rec32 and
-                             //   k_face_riemann32 (kHalfRows32 rows of nf)
     unsigned long long* geo_pos;  // FP32 form: bits of loc and centroid [6][n] the geometry was built from
     uint8_t* geo_changed;    // FP32 form: 1 for cells whose loc or centroid bits changed since
     int geo_check;           // 1: k_geom32 rebuilds only the faces of changed cells

@@ -381,101 +381,6 @@ __global__ void __launch_bounds__(kMaxBlock, FACE32_MINB) k_face_flux32(KP p) {
     }
 }
 
-// Steps of the FP32-face form run the face stage as two kernels joined by the
-// faces' reconstructed states, so that neither holds the registers of both the
-// reconstruction (two cells' gathers, the limiter) and the Riemann solve:
-// k_face_rec32 writes per face the two states handed to the solver, the face
-// velocity and dt * area (-1: the face is not active, -2: its simulation has
-// finished), and the rows v_max and a_over_r; k_face_riemann32 solves and
-// writes the flux rows.  The arithmetic is the fused kernel's.
-__global__ void __launch_bounds__(kMaxBlock, 4) k_face_rec32(KP p) {
-    if (p.use_list && p.tl[0].done) return;
-    const int n_items = p.use_list ? (int)p.tl[0].n_list : p.nf;
-    const size_t nf = (size_t)p.nf;
-    for (int base = blockIdx.x * blockDim.x; base < n_items; base += gridDim.x * blockDim.x) {
-        int idx = base + threadIdx.x;
-        int f = idx < n_items ? (p.use_list ? p.face_list[idx] : idx) : -1;
-        int k = f >= 0 ? inst_of(p, p.left[f]) : -1;
-        if (k >= 0 && p.tl[k].done) k = -1;
-        bool counted = false;
-        if (f >= 0) {
-            float* hs = p.hs32;
-            if (k >= 0) {
-                int l = p.left[f], r = p.right[f];
-                bool la = p.active[l] != 0;
-                Pre32 q;
-                double dt = 0.;
-                if (r >= 0) {
-                    bool ra = p.active[r] != 0;
-                    const double dtl = C(p, F_DT, l), dtr = C(p, F_DT, r);
-                    const long long kl = __double_as_longlong(dtl) & 0x7fffffffffffffffLL;
-                    const long long kr = __double_as_longlong(dtr) & 0x7fffffffffffffffLL;
-                    if (!((!la && !ra) || (kr < kl && !ra) || (kl < kr && !la))) {  // interior_face_active
-                        dt = kl <= kr ? dtl : dtr;
-                        q = face_interior32_pre(p, f, l, r, f32(dt));
-                        counted = true;
-                    }
-                } else if (la) {
-                    dt = C(p, F_DT, l);
-                    q = face_boundary32_pre(p, f, l, f32(dt));
-                    counted = true;
-                }
-                if (counted) {
-#pragma unroll
-                    for (int c = 0; c < 5; c++) {
-                        hs[c * nf + f] = q.l.q[c];
-                        hs[(5 + c) * nf + f] = q.r.q[c];
-                    }
-                    hs[10 * nf + f] = q.iv.x;
-                    hs[11 * nf + f] = q.iv.y;
-                    hs[12 * nf + f] = q.iv.z;
-                }
-                hs[13 * nf + f] = counted ? f32(dt) * p.geo[GE_A * nf + f] : -1.f;
-                p.flux32[5 * nf + f] = counted ? q.v_max : 0.f;
-                p.flux32[6 * nf + f] = counted ? q.a_over_r : 0.f;
-            } else {
-                hs[13 * nf + f] = -2.f;
-            }
-        }
-        if (!p.use_list) inst_count(p, k, counted, CNT_FACES);
-    }
-}
-template <int SOLVER>
-__global__ void __launch_bounds__(kMaxBlock, FACE32_MINB) k_face_riemann32(KP p) {
-    if (p.use_list && p.tl[0].done) return;
-    const Gas<float> g = gas_t<float>(p);
-    const Gas<double> g64 = gas_t<double>(p);
-    const int n_items = p.use_list ? (int)p.tl[0].n_list : p.nf;
-    const size_t nf = (size_t)p.nf;
-    for (int base = blockIdx.x * blockDim.x; base < n_items; base += gridDim.x * blockDim.x) {
-        int idx = base + threadIdx.x;
-        int f = idx < n_items ? (p.use_list ? p.face_list[idx] : idx) : -1;
-        const float da = f >= 0 ? p.hs32[13 * nf + f] : -2.f;
-        unsigned int err = 0;
-        int k = -1;
-        if (da >= 0.f) {
-            const float* hs = p.hs32;
-            Pre32 q;
-#pragma unroll
-            for (int c = 0; c < 5; c++) {
-                q.l.q[c] = hs[c * nf + f];
-                q.r.q[c] = hs[(5 + c) * nf + f];
-            }
-            q.iv = v3(hs[10 * nf + f], hs[11 * nf + f], hs[12 * nf + f]);
-            q.n = GE3(p, GE_N, f);
-            const St<float> F = solve_for_flux<float, SOLVER>(q.l, q.r, q.iv, q.n, g, g64, p.max_iter, &err, &p.rsx);
-#pragma unroll
-            for (int c = 0; c < 5; c++) p.flux32[c * nf + f] = da * F.q[c];
-            k = inst_of(p, p.left[f]);
-            if (err & ~kInfoFallback) set_err(p, k, err & ~kInfoFallback);
-        } else if (da == -1.f) {
-#pragma unroll
-            for (int c = 0; c < 5; c++) p.flux32[c * nf + f] = 0.f;
-        }
-        inst_count(p, k, (err & kInfoFallback) != 0, CNT_FALLBACK);
-    }
-}
-
 // The other side of face f seen from cell i in the FP32-face form (the FP32
 // counterpart of other_side): its primitive state, the centroid separation ds
 // and the limiter's extrapolation vector, from the static face geometry.
@@ -910,14 +815,6 @@ void launch_face_flux_fp32(const KP& p, int solver, cudaStream_t s) {
     if (p.nf <= 0) return;
     int g = grid(p.nf, p.blk_face), cap = p.n_sms * 512 / p.blk_face;
     if (p.use_list && g > cap) g = cap;
-    if (p.flux_rows == 7 && p.hs32) {  // a step: the face stage in two kernels
-        k_face_rec32<<<g, p.blk_face, 0, s>>>(p);
-        if (solver == SOLVER_HLLC) k_face_riemann32<SOLVER_HLLC><<<g, p.blk_face, 0, s>>>(p);
-        else if (solver == SOLVER_EXACT) k_face_riemann32<SOLVER_EXACT><<<g, p.blk_face, 0, s>>>(p);
-        else if (solver == SOLVER_PVRS) k_face_riemann32<SOLVER_PVRS><<<g, p.blk_face, 0, s>>>(p);
-        else k_face_riemann32<SOLVER_EXTRA><<<g, p.blk_face, 0, s>>>(p);
-        return;
-    }
     if (solver == SOLVER_HLLC) k_face_flux32<SOLVER_HLLC><<<g, p.blk_face, 0, s>>>(p);
     else if (solver == SOLVER_EXACT) k_face_flux32<SOLVER_EXACT><<<g, p.blk_face, 0, s>>>(p);
     else if (solver == SOLVER_PVRS) k_face_flux32<SOLVER_PVRS><<<g, p.blk_face, 0, s>>>(p);
