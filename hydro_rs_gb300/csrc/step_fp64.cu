@@ -871,6 +871,23 @@ __device__ __forceinline__ double limit_factor(double d_max, double d_min, doubl
 // fused per cell; in step mode also compute_timesteps + timesteps_apply
 // (euler_eqns_fvs.rs:50-61, runner/hydrodynamics.rs:145-158) with block-level
 // min reductions of the integer timestep and the new time bins.
+// The place in the block's tile (0 .. blockDim - 1) of the item this thread
+// takes, items sorted by key (0 .. kDegKeys - 1; kDegKeys: no item, -1 back),
+// by a counting sort in shared memory.
+constexpr int kDegKeys = 32;
+__device__ __forceinline__ int tile_sorted(int key, int* s_count, int* s_order) {
+    for (int k = threadIdx.x; k <= kDegKeys; k += blockDim.x) s_count[k] = 0;
+    __syncthreads();
+    const int rank = atomicAdd(&s_count[key], 1);
+    __syncthreads();
+    int start = 0;
+    for (int k = 0; k < key; k++) start += s_count[k];
+    s_order[start + rank] = key < kDegKeys ? (int)threadIdx.x : -1;
+    __syncthreads();
+    const int mine = s_order[threadIdx.x];
+    __syncthreads();  // the arrays are reused by the next tile
+    return mine;
+}
 __device__ __forceinline__ void gradients_cell(const KP& p, int i, int do_timestep) {
     unsigned long long my_dti = MAX_NR_TIMESTEPS;
     int my_tb = 127;
@@ -1148,10 +1165,19 @@ __global__ void __launch_bounds__(kMaxBlock) k_gradients(KP p, int do_timestep) 
             gradients_cell_warp(p, p.cell_list[w], do_timestep, lane);
         return;
     }
-    // warp-uniform trip count: the per-instance reductions need every lane
+    // The cells' loops over their faces have as many trips as the cell has
+    // faces (5-8 on a 2D Voronoi mesh), and a warp runs until its cell with the
+    // most faces is done: each tile of cells is ordered by face count (a
+    // counting sort in shared memory), so that a warp's cells have about the
+    // same number.  Each cell's arithmetic is unchanged.  Block-uniform trip
+    // count: the per-instance reductions need every lane, the sort every thread.
+    __shared__ int s_count[kDegKeys + 1], s_order[kMaxBlock];
     for (int base = blockIdx.x * blockDim.x; base < n_items; base += gridDim.x * blockDim.x) {
-        int idx = base + threadIdx.x;
-        gradients_cell(p, idx < n_items ? cell_at(p, idx) : -1, do_timestep);
+        const int idx = base + threadIdx.x;
+        const int i = idx < n_items ? cell_at(p, idx) : -1;
+        const int key = i < 0 ? kDegKeys : min(p.csr_off[i + 1] - p.csr_off[i], kDegKeys - 1);
+        const int t = tile_sorted(key, s_count, s_order);
+        gradients_cell(p, t < 0 ? -1 : cell_at(p, base + t), do_timestep);
     }
 }
 
