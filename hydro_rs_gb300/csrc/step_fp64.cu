@@ -427,6 +427,10 @@ __device__ __forceinline__ double search_result(SearchLane& s) {
 // place, and the owner reads its value back: the same function on the same
 // data, so the same bits, with most warps on one pattern.
 constexpr int kSearchBlock = 256;
+struct EvalPost {
+    double x, vl, vr;
+    ExSide L, R;
+};
 __device__ __forceinline__ int ex_f_key(double x, const ExSide& L, const ExSide& R) {
     const double lo = fmin(L.p, R.p), hi = fmax(L.p, R.p);
     return (x > lo ? 1 : 0) + (x > hi ? 1 : 0);
@@ -443,14 +447,8 @@ __device__ __forceinline__ int block_sorted(int key, int* s_count, int* s_order)
     __syncthreads();
     return s_order[threadIdx.x];
 }
-// Each search's state lives in a shared-memory slot, owned for fetching by one
-// thread of the block; every round the slots are processed twice in sorted
-// orders, so that the lanes of a warp run the same code: once for f, sorted
-// by fb's branch pattern at x, once for the machines' steps, sorted by kind
-// (a Newton step, a Brent step, the check of a forced-bisection run).
-__global__ void __launch_bounds__(kSearchBlock, 2) k_face_search(KP p) {
-    extern __shared__ __align__(16) unsigned char s_dyn[];
-    SearchLane* slot = reinterpret_cast<SearchLane*>(s_dyn);
+__global__ void __launch_bounds__(kSearchBlock) k_face_search(KP p) {
+    __shared__ EvalPost s_post[kSearchBlock];
     __shared__ double s_res[kSearchBlock];
     __shared__ int s_count[4], s_order[kSearchBlock];
     const Gas<double> g = gas(p);
@@ -461,18 +459,17 @@ __global__ void __launch_bounds__(kSearchBlock, 2) k_face_search(KP p) {
     unsigned int* next = p.brent_count + kExactQueues;  // jobs handed out
     const unsigned int lane = threadIdx.x & 31;
     auto job = [&](unsigned int t) -> BrentJob& { return t < n1 ? newton_jobs[t] : brent_jobs[t - n1]; };
-    auto retire = [&](SearchLane& s) {
+    SearchLane s;
+    bool dry = false;
+    auto retire = [&]() {
         job((unsigned int)s.j).p_guess = search_result(s);
         if (s.err) set_err(p, s.k, s.err);
         s.j = -1;
     };
-    SearchLane& mine = slot[threadIdx.x];
-    mine.j = -1;
-    bool dry = false;
     while (true) {
-        // threads whose slot is empty take jobs until each holds one that needs f, or the queues are dry
+        // lanes without a search take jobs until each holds one that needs f, or the queues are dry
         while (true) {
-            const unsigned int need = __ballot_sync(0xffffffffu, mine.j < 0 && !dry);
+            const unsigned int need = __ballot_sync(0xffffffffu, s.j < 0 && !dry);
             if (!need) break;
             const int leader = __ffs(need) - 1;
             unsigned int base = 0;
@@ -482,7 +479,6 @@ __global__ void __launch_bounds__(kSearchBlock, 2) k_face_search(KP p) {
                 const unsigned int t = base + (unsigned int)__popc(need & ((1u << lane) - 1u));
                 if (t < n_jobs) {
                     const BrentJob& J = job(t);
-                    SearchLane s;
                     s.j = (int)t;
                     s.k = J.k;
                     s.err = 0;
@@ -498,43 +494,38 @@ __global__ void __launch_bounds__(kSearchBlock, 2) k_face_search(KP p) {
                     } else {
                         s.bm.start(0., J.p_guess, J.fp0, J.fp_guess, 1e-6, p.max_iter);  // on [0, guess]
                     }
-                    if (search_lane_done(s)) retire(s);
-                    mine = s;
+                    if (search_lane_done(s)) retire();
                 } else {
                     dry = true;
                 }
             }
         }
-        const bool has = mine.j >= 0;
-        if (!__syncthreads_or(has)) break;  // block-uniform: every search has ended, the queues are dry
-        // f at each slot's point, the slots sorted by fb's branch pattern
+        const bool has = s.j >= 0;
+        if (!__syncthreads_or(has)) break;  // block-uniform: every lane's search has ended, the queues are dry
         int key = 3;
-        if (has) key = ex_f_key(mine.newton ? mine.nm.x : mine.bm.x, mine.L, mine.R);
-        int o = block_sorted(key, s_count, s_order);
+        if (has) {
+            const double x = s.newton ? s.nm.x : s.bm.x;
+            s_post[threadIdx.x] = EvalPost{x, s.vl, s.vr, s.L, s.R};
+            key = ex_f_key(x, s.L, s.R);
+        }
+        const int o = block_sorted(key, s_count, s_order);
         if (o >= 0) {
-            const SearchLane& e = slot[o];
-            s_res[o] = ex_f(e.newton ? e.nm.x : e.bm.x, e.L, e.R, e.vl, e.vr, g);
+            const EvalPost e = s_post[o];
+            s_res[o] = ex_f(e.x, e.L, e.R, e.vl, e.vr, g);
         }
         __syncthreads();
-        // the machines' steps, the slots sorted by kind
-        key = !has ? 3 : mine.newton ? 0 : mine.bm.phase == 0 ? 1 : 2;
-        o = block_sorted(key, s_count, s_order);
-        if (o >= 0) {
-            SearchLane s = slot[o];
-            const double fx = s_res[o];
+        if (has) {
+            const double fx = s_res[threadIdx.x];
             if (s.newton) {
                 s.nm.step(fx, s.L, s.R, g);
                 if (s.nm.done) search_after_newton(s, p.max_iter);
             } else {
                 s.bm.step(fx);
             }
-            if (search_lane_done(s)) retire(s);
-            slot[o] = s;
+            if (search_lane_done(s)) retire();
         }
-        __syncthreads();
     }
 }
-constexpr size_t kSearchSmem = sizeof(SearchLane) * kSearchBlock;
 
 // Every queued face from its star pressure on (star state, sample, flux), the
 // three queues one after another: apart from the searches, the faces of a warp
@@ -1477,10 +1468,7 @@ void launch_face_flux_fp64(const KP& p, int solver, cudaStream_t s) {
     else if (solver == SOLVER_EXACT && p.brent_jobs) {
         cudaMemsetAsync(p.brent_count, 0, (kExactQueues + 1) * sizeof(unsigned int), s);
         k_face_flux<SOLVER_EXACT, true><<<g, p.blk_face, 0, s>>>(p);
-        static const cudaError_t smem_ok =  // the slots take more than the default 48 KB
-            cudaFuncSetAttribute(k_face_search, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSearchSmem);
-        (void)smem_ok;
-        k_face_search<<<pool_grid(p, k_face_search, kSearchBlock, kSearchSmem), kSearchBlock, kSearchSmem, s>>>(p);
+        k_face_search<<<pool_grid(p, k_face_search, kSearchBlock, 0), kSearchBlock, 0, s>>>(p);
         const int finish_grid =
             (int)std::min<long long>((kExactQueues * (long long)p.brent_cap + kJobTile - 1) / kJobTile, p.n_sms * 16LL);
         k_face_finish<<<finish_grid, kJobTile, 0, s>>>(p);
