@@ -402,15 +402,18 @@ __device__ __noinline__ St<T> vacuum_sample(St<T> l, St<T> r, T vl, T vr, T al, 
 }
 
 // ---- exact solver (riemann_solver/exact.rs), always evaluated in FP64 ----
+// One side of the exact solver's Riemann problem: density, pressure, sound
+// speed, and the shock terms A = 2/((gamma+1) rho), B = (gamma-1)/(gamma+1) p
+// (exact.rs:14-15, 39-40, 61-62), formed once per face instead of at every
+// evaluation of fb, fb' and gb (the same operations on the same inputs).
 struct ExSide {
-    double rho, p, a;
+    double rho, p, a, A, B;
 };
+__device__ __forceinline__ ExSide ex_side(double rho, double p, double a, const Gas<double>& g) {
+    return ExSide{rho, p, a, g.tdgp1() / rho, g.gm1dgp1() * p};
+}
 __device__ __forceinline__ double ex_fb(double p, const ExSide& s, const Gas<double>& g) {  // :12-20
-    if (p > s.p) {
-        double cap_a = g.tdgp1() / s.rho;
-        double cap_b = g.gm1dgp1() * s.p;
-        return (p - s.p) * sqrt(cap_a / (p + cap_b));
-    }
+    if (p > s.p) return (p - s.p) * sqrt(s.A / (p + s.B));
     return g.tdgm1() * s.a * (g.pow_e1(p / s.p) - 1.);
 }
 // The two sides' terms are evaluated lower-pressure side first: for a pressure
@@ -435,17 +438,11 @@ __device__ __forceinline__ double ex_f0(const ExSide& l, const ExSide& r, double
     return ex_fb0(l, g) + ex_fb0(r, g) + (vr - vl);
 }
 __device__ __forceinline__ double ex_fprimeb(double p, const ExSide& s, const Gas<double>& g) {  // :37-45
-    if (p > s.p) {
-        double cap_a = g.tdgp1() / s.rho;
-        double cap_b = g.gm1dgp1() * s.p;
-        return (1. - 0.5 * (p - s.p) / (cap_b + p)) * sqrt(cap_a / (p + cap_b));
-    }
+    if (p > s.p) return (1. - 0.5 * (p - s.p) / (s.B + p)) * sqrt(s.A / (p + s.B));
     return 1. / s.rho / s.a * g.pow_me1(p / s.p);
 }
 __device__ __forceinline__ double ex_gb(double p, const ExSide& s, const Gas<double>& g) {  // :60-64
-    double cap_a = g.tdgp1() / s.rho;
-    double cap_b = g.gm1dgp1() * s.p;
-    return sqrt(cap_a / (p + cap_b));
+    return sqrt(s.A / (p + s.B));
 }
 static __device__ __noinline__ double ex_guess_p(ExSide l, ExSide r, double vl, double vr, Gas<double> g) {  // :70-103
     double p_min = fmin(l.p, r.p);
@@ -1062,8 +1059,8 @@ static __device__ __noinline__ Star<float> ex_star_split(float rl, float pl, flo
     // error is of order dP^2) is redone by the full FP64 iteration
     if (!(P > 0.f) || !isfinite(P) || !(fabsf(dP) <= 1e-4f * P)) {
         *err |= 1u << 16;  // counted by the face kernel as a fallback face
-        Star<double> sd = ex_star_fast(ExSide{(double)rl, (double)pl, (double)al},
-                                       ExSide{(double)rr, (double)pr, (double)ar}, (double)vl, (double)vr, g64,
+        Star<double> sd = ex_star_fast(ex_side((double)rl, (double)pl, (double)al, g64),
+                                       ex_side((double)rr, (double)pr, (double)ar, g64), (double)vl, (double)vr, g64,
                                        max_iter, err);
         s.rho_l = (float)sd.rho_l;
         s.rho_r = (float)sd.rho_r;
@@ -1184,8 +1181,8 @@ __device__ __forceinline__ Star<T> exact_star(const St<T>& l, const St<T>& r, T 
         s.u = T(sf.u);
         s.p = T(sf.p);
     } else {
-        ExSide L{double(l.q[0]), double(l.q[4]), double(al)};
-        ExSide R{double(r.q[0]), double(r.q[4]), double(ar)};
+        ExSide L = ex_side(double(l.q[0]), double(l.q[4]), double(al), g64);
+        ExSide R = ex_side(double(r.q[0]), double(r.q[4]), double(ar), g64);
         Star<double> sd = ex_star(L, R, double(vl), double(vr), g64, max_iter, err);
         s.rho_l = T(sd.rho_l);
         s.rho_r = T(sd.rho_r);

@@ -237,7 +237,7 @@ struct BrentJob {
 // (star_state_from_pstar forms both; sample_star reads one) is formed.
 __device__ __forceinline__ St<double> exact_flux_from_p(double pst, const FacePre& q, double vl, double vr, double al,
                                                         double ar, const Gas<double>& g) {
-    const ExSide L{q.l.q[0], q.l.q[4], al}, R{q.r.q[0], q.r.q[4], ar};
+    const ExSide L = ex_side(q.l.q[0], q.l.q[4], al, g), R = ex_side(q.r.q[0], q.r.q[4], ar, g);
     // star_state_from_pstar's u, its two terms in ex_f's branch-coherent order
     const bool lo_left = L.p <= R.p;
     const double t_lo = ex_fb(pst, lo_left ? L : R, g);
@@ -314,7 +314,7 @@ __global__ void __launch_bounds__(QUEUE ? kQueueBlock : kMaxBlock, QUEUE ? 6 : 0
                 if (is_vacuum(q.l, q.r, al, ar, vrml, g)) {
                     F = flux_from_half_state(vacuum_sample(q.l, q.r, vl, vr, al, ar, q.n, g), q.iv, q.n, g);
                 } else {
-                    ExSide L{q.l.q[0], q.l.q[4], al}, R{q.r.q[0], q.r.q[4], ar};
+                    const ExSide L = ex_side(q.l.q[0], q.l.q[4], al, g), R = ex_side(q.r.q[0], q.r.q[4], ar, g);
                     double pg, fpg, fp0;
                     const int next = ex_star_start(L, R, vl, vr, g, &pg, &fpg, &fp0);
                     // queue 0: Brent searches; 1: Newton searches; 2: the guess is the pressure.
@@ -485,8 +485,8 @@ __global__ void __launch_bounds__(kSearchBlock) k_face_search(KP p) {
                     s.j = (int)t;
                     s.k = J.k;
                     s.err = 0;
-                    s.L = ExSide{J.q.l.q[0], J.q.l.q[4], J.al};
-                    s.R = ExSide{J.q.r.q[0], J.q.r.q[4], J.ar};
+                    s.L = ex_side(J.q.l.q[0], J.q.l.q[4], J.al, g);
+                    s.R = ex_side(J.q.r.q[0], J.q.r.q[4], J.ar, g);
                     s.vl = J.vl;
                     s.vr = J.vr;
                     s.fp0 = J.fp0;
