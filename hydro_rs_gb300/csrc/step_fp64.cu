@@ -434,9 +434,11 @@ struct EvalPost {
     double x, vl, vr;
     ExSide L, R;
 };
+// (Only the grouping depends on it, so it compares bit patterns on the integer
+// pipe, which order non-negative doubles as their values.)
 __device__ __forceinline__ int ex_f_key(double x, const ExSide& L, const ExSide& R) {
-    const double lo = fmin(L.p, R.p), hi = fmax(L.p, R.p);
-    return (x > lo ? 1 : 0) + (x > hi ? 1 : 0);
+    const long long a = __double_as_longlong(L.p), b = __double_as_longlong(R.p), k = __double_as_longlong(x);
+    return (k > min(a, b) ? 1 : 0) + (k > max(a, b) ? 1 : 0);
 }
 // The index of the post this thread evaluates (key 3: no post), posts sorted by key.
 __device__ __forceinline__ int block_sorted(int key, int* s_count, int* s_order) {
@@ -956,7 +958,7 @@ __device__ __forceinline__ void gradients_cell(const KP& p, int i, int do_timest
                 res = res + x.y * c1;
                 res = res + x.z * c2;
                 gr[q] = res;
-                finite = finite && isfinite(res.x) && isfinite(res.y) && isfinite(res.z);
+                finite = finite && is_finite64(res.x) && is_finite64(res.y) && is_finite64(res.z);
             }
             if (!finite) {
 #pragma unroll
@@ -1098,7 +1100,7 @@ __device__ __forceinline__ void gradients_cell_warp(const KP& p, int i, int do_t
                 res = res + x.y * c1;
                 res = res + x.z * c2;
                 gr[q] = res;
-                finite = finite && isfinite(res.x) && isfinite(res.y) && isfinite(res.z);
+                finite = finite && is_finite64(res.x) && is_finite64(res.y) && is_finite64(res.z);
             }
             if (!finite) {
 #pragma unroll
