@@ -265,12 +265,11 @@ __device__ __forceinline__ St<double> exact_flux_from_p(double pst, const FacePr
 
 // EulerEqnsFvs::compute_fluxes (euler_eqns_fvs.rs:26-48): the active-face rule,
 // dt = min(dt_l, dt_r), interior / boundary dispatch.
-// QUEUE (the exact solver with its job queues): every face's solve is queued;
-// that variant runs in blocks of kQueueBlock threads, 6 of them resident per
-// SM (168 registers; a budget of 128 for 8 blocks measured slower).
-constexpr int kQueueBlock = 64;
+// QUEUE (the exact solver with its job queues): every face's solve is queued.
+// (Register budgets of 128 and 168 for more resident warps measured slower
+// than the compiler's own 170.)
 template <int SOLVER, bool QUEUE = false>
-__global__ void __launch_bounds__(QUEUE ? kQueueBlock : kMaxBlock, QUEUE ? 6 : 0) k_face_flux(KP p) {
+__global__ void __launch_bounds__(kMaxBlock) k_face_flux(KP p) {
     if (p.use_list && p.tl[0].done) return;
     const Gas<double> g = gas(p);
     // all faces (one per thread), or the compacted active-face list (grid-stride)
@@ -1472,9 +1471,7 @@ void launch_face_flux_fp64(const KP& p, int solver, cudaStream_t s) {
     if (solver == SOLVER_HLLC) k_face_flux<SOLVER_HLLC><<<g, p.blk_face, 0, s>>>(p);
     else if (solver == SOLVER_EXACT && p.brent_jobs) {
         cudaMemsetAsync(p.brent_count, 0, (kExactQueues + 1) * sizeof(unsigned int), s);
-        int gq = grid(p.nf, kQueueBlock);
-        if (p.use_list) gq = std::min(gq, p.n_sms * 512 / kQueueBlock);
-        k_face_flux<SOLVER_EXACT, true><<<gq, kQueueBlock, 0, s>>>(p);
+        k_face_flux<SOLVER_EXACT, true><<<g, p.blk_face, 0, s>>>(p);
         k_face_search<<<pool_grid(p, k_face_search, kSearchBlock, 0), kSearchBlock, 0, s>>>(p);
         const int finish_grid =
             (int)std::min<long long>((kExactQueues * (long long)p.brent_cap + kJobTile - 1) / kJobTile, p.n_sms * 16LL);
