@@ -798,14 +798,33 @@ __device__ __forceinline__ void update_cell_warp(const KP& p, int i, int do_c2p,
                 vm32 = fmaxf(vm32, (float)vm);
                 ar32 = fmaxf(ar32, (float)ar);
             } else {
-                if (lt) facc = facc - y;  // update_fluxes_left (part.rs:160-167)
-                else facc = facc + y;     // update_fluxes_right (part.rs:169-176)
-                if (act) {
+                // a lane per sum: lanes 0-4 the accumulator rows, 5 max_signal_velocity,
+                // 6 max_a_over_r, each folded face by face as the reference does
+                if (lane < 5) {
+                    double yq = y.q[0], fq = facc.q[0];
+#pragma unroll
+                    for (int q = 1; q < 5; q++)
+                        if (lane == q) {
+                            yq = y.q[q];
+                            fq = facc.q[q];
+                        }
+                    fq = lt ? fq - yq : fq + yq;  // update_fluxes_left / _right (part.rs:160-176)
+#pragma unroll
+                    for (int q = 0; q < 5; q++)
+                        if (lane == q) facc.q[q] = fq;
+                } else if (act && lane == 5) {
                     msv = m_max(vm, msv);
+                } else if (act && lane == 6) {
                     maor = m_max(maor, ar);
                 }
             }
         }
+    }
+    if (!ROWS32) {  // the sums to every lane
+#pragma unroll
+        for (int q = 0; q < 5; q++) facc.q[q] = __shfl_sync(0xffffffffu, facc.q[q], q);
+        msv = __shfl_sync(0xffffffffu, msv, 5);
+        maor = __shfl_sync(0xffffffffu, maor, 6);
     }
     if (ROWS32) {
 #pragma unroll
@@ -1042,13 +1061,23 @@ __device__ __forceinline__ void gradients_cell_warp(const KP& p, int i, int do_t
           if (!p.godunov) {
             V3<double> cen = C3(p, F_CEN, i);
             St<double> prim = C5(p, F_PRIM, i);
-            double a00 = 0., a01 = 0., a02 = 0., a11 = 0., a12 = 0., a22 = 0.;
-            if (p.dim == 1) { a11 = 1.; a22 = 1.; }
-            else if (p.dim == 2) { a22 = 1.; }
-            V3<double> gr[5];
-#pragma unroll
-            for (int q = 0; q < 5; q++) gr[q] = v3(0., 0., 0.);
+            // GradientData::collect in CSR order, a lane per accumulator: lanes
+            // 0-14 the 15 gradient sums (quantity lane / 3, axis lane % 3),
+            // lanes 15-20 the six matrix entries a00 a01 a11 a02 a12 a22.  Every
+            // lane forms its term as the reference does, t = (u v) x with
+            // (u, v, x) = (w, dq, ds_axis) or (ds_a, ds_b, w) (w (ds_a ds_b) in the
+            // reference: the same product), and adds it to its sum face by face,
+            // so each sum is the reference's; one warp instruction then carries
+            // all 21 sums instead of every lane forming all of them.
             const int k0 = p.csr_off[i], deg = p.csr_off[i + 1] - k0;
+            const bool grad_lane = lane < 15;
+            const int gq = lane / 3, gax = lane % 3;            // gradient lanes
+            const int me = lane - 15;                            // matrix lanes: entry
+            const int ma = me == 0 || me == 1 || me == 3 ? 0 : me == 5 ? 2 : 1;  // a00 a01 a11 a02 a12 a22:
+            const int mb = me == 0 ? 0 : me == 1 || me == 2 ? 1 : 2;              //   first and second axis
+            const bool zdep = grad_lane ? gax == 2 : me >= 3;    // a term the reference skips where ds.z == 0
+            double acc = 0.;
+            if (!grad_lane && ((p.dim == 1 && (me == 2 || me == 5)) || (p.dim == 2 && me == 5))) acc = 1.;
             for (int j0 = 0; j0 < deg; j0 += 32) {  // warp-uniform
                 double w = 0., dq[5] = {0., 0., 0., 0., 0.};
                 V3<double> ds = v3(0., 0., 0.);
@@ -1063,28 +1092,32 @@ __device__ __forceinline__ void gradients_cell_warp(const KP& p, int i, int do_t
                     for (int q = 0; q < 5; q++) dq[q] = op.q[q] - prim.q[q];
                 }
                 const int n = min(32, deg - j0);
-                for (int t = 0; t < n; t++) {  // GradientData::collect in CSR order
+                for (int t = 0; t < n; t++) {
                     const double wt = __shfl_sync(0xffffffffu, w, t);
-                    const V3<double> dst = v3(__shfl_sync(0xffffffffu, ds.x, t), __shfl_sync(0xffffffffu, ds.y, t),
-                                              __shfl_sync(0xffffffffu, ds.z, t));
-                    const bool z = dst.z != 0.;
+                    const double dx = __shfl_sync(0xffffffffu, ds.x, t), dy = __shfl_sync(0xffffffffu, ds.y, t),
+                                 dz = __shfl_sync(0xffffffffu, ds.z, t);
+                    double dqt = 0.;
 #pragma unroll
                     for (int q = 0; q < 5; q++) {
-                        double wdq = wt * __shfl_sync(0xffffffffu, dq[q], t);
-                        gr[q].x = gr[q].x + wdq * dst.x;
-                        gr[q].y = gr[q].y + wdq * dst.y;
-                        if (z) gr[q].z = gr[q].z + wdq * dst.z;
+                        const double v = __shfl_sync(0xffffffffu, dq[q], t);
+                        if (q == gq) dqt = v;
                     }
-                    a00 = a00 + wt * (dst.x * dst.x);
-                    a01 = a01 + wt * (dst.x * dst.y);
-                    a11 = a11 + wt * (dst.y * dst.y);
-                    if (z) {
-                        a02 = a02 + wt * (dst.x * dst.z);
-                        a12 = a12 + wt * (dst.y * dst.z);
-                        a22 = a22 + wt * (dst.z * dst.z);
-                    }
+                    const bool z = dz != 0.;
+                    const double da = ma == 0 ? dx : ma == 1 ? dy : dz, db = mb == 0 ? dx : mb == 1 ? dy : dz;
+                    const double dax = gax == 0 ? dx : gax == 1 ? dy : dz;
+                    const double u = grad_lane ? wt : da, v = grad_lane ? dqt : db, x = grad_lane ? dax : wt;
+                    const double term = (u * v) * x;
+                    if (lane < 21 && (z || !zdep)) acc = acc + term;
                 }
             }
+            V3<double> gr[5];
+#pragma unroll
+            for (int q = 0; q < 5; q++)
+                gr[q] = v3(__shfl_sync(0xffffffffu, acc, 3 * q), __shfl_sync(0xffffffffu, acc, 3 * q + 1),
+                           __shfl_sync(0xffffffffu, acc, 3 * q + 2));
+            const double a00 = __shfl_sync(0xffffffffu, acc, 15), a01 = __shfl_sync(0xffffffffu, acc, 16),
+                         a11 = __shfl_sync(0xffffffffu, acc, 17), a02 = __shfl_sync(0xffffffffu, acc, 18),
+                         a12 = __shfl_sync(0xffffffffu, acc, 19), a22 = __shfl_sync(0xffffffffu, acc, 20);
             V3<double> m0 = v3(a00, a01, a02), m1 = v3(a01, a11, a12), m2 = v3(a02, a12, a22);
             V3<double> t0 = cross(m1, m2), t1 = cross(m2, m0), t2 = cross(m0, m1);
             double det = dot(m2, t2);
