@@ -299,7 +299,10 @@ def _fp64_peak(torch):
 # DRAM bytes (read + write) per launch of the face stage from ncu captures at
 # the bench sizes (cold caches, ncu's default cache control): the committed
 # summaries in profiles/ give the commands.  Keyed by (workload, nx, form).
-TRAFFIC = {("kh2d", 256, 1): 26_891_008, ("kh2d", 256, 0): 43_228_672}  # profiles/face_stage_traffic_kh256.txt
+# FP32 form: profiles/face_stage_traffic_kh256.txt (k_face_flux32); plain form:
+# profiles/face_stage_fp64_exact_pipes_kh256.txt (k_face_flux + k_face_search +
+# k_face_finish: 43.1 + 47.3 + 47.3 MB, the job queue written once and read twice).
+TRAFFIC = {("kh2d", 256, 1): 26_891_008, ("kh2d", 256, 0): 137_700_000}
 
 
 def _face_kernel_ms(sim, steps):
