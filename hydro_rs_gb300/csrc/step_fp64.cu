@@ -356,25 +356,33 @@ __global__ void __launch_bounds__(kMaxBlock) k_face_flux(KP p) {
 // fills most warps with faces that take the same branches; each face's
 // arithmetic is unchanged.
 constexpr int kJobTile = 128;
+// The branches of fb at the job's pressure (0: below both side pressures, 1:
+// between them, 2: above both); between them, the sampler's side decides
+// whether it meets the shock or the rarefaction, so key 1 splits by the side
+// x/t = 0 is likely to fall on (u* ~ (v_l + v_r) / 2) against which side
+// has the lower pressure: keys 0..3.
 __device__ __forceinline__ int job_branch_key(const BrentJob& J) {
     const double pl = J.q.l.q[4], pr = J.q.r.q[4];
     const double lo = fmin(pl, pr), hi = fmax(pl, pr);
-    return (J.p_guess > lo ? 1 : 0) + (J.p_guess > hi ? 1 : 0);
+    const int pat = (J.p_guess > lo ? 1 : 0) + (J.p_guess > hi ? 1 : 0);
+    if (pat != 1) return pat == 0 ? 0 : 3;
+    return ((pl <= pr) != (J.vl + J.vr < 0.)) ? 1 : 2;
 }
+constexpr int kJobKeys = 4;
 // The index of the job this thread runs in the tile starting at base (or -1);
 // job(t) is job t of the n_jobs the kernel runs.
 template <class Job>
 __device__ __forceinline__ int sorted_job(const Job& job, unsigned int base, unsigned int n_jobs, int* s_count,
                                           int* s_order) {
     const unsigned int j = base + threadIdx.x;
-    const int key = j < n_jobs ? job_branch_key(job(j)) : 3;
-    if (threadIdx.x < 4) s_count[threadIdx.x] = 0;
+    const int key = j < n_jobs ? job_branch_key(job(j)) : kJobKeys;
+    if (threadIdx.x <= kJobKeys) s_count[threadIdx.x] = 0;
     __syncthreads();
     const int rank = atomicAdd(&s_count[key], 1);
     __syncthreads();
     int start = 0;
     for (int k = 0; k < key; k++) start += s_count[k];
-    s_order[start + rank] = key < 3 ? (int)j : -1;
+    s_order[start + rank] = key < kJobKeys ? (int)j : -1;
     __syncthreads();
     const int mine = s_order[threadIdx.x];
     __syncthreads();  // the arrays are reused by the next tile
@@ -539,7 +547,7 @@ __global__ void __launch_bounds__(kSearchBlock, 4) k_face_search(KP p) {
 // run the same code, where in the face kernel only its lanes whose guess was the
 // pressure would have run it.
 __global__ void __launch_bounds__(kJobTile) k_face_finish(KP p) {
-    __shared__ int s_count[4], s_order[kJobTile];
+    __shared__ int s_count[kJobKeys + 1], s_order[kJobTile];
     const Gas<double> g = gas(p);
     const unsigned int n0 = queue_count(p, 0), n1 = queue_count(p, 1), n2 = queue_count(p, 2);
     const unsigned int n_jobs = n0 + n1 + n2;
