@@ -239,23 +239,23 @@ __device__ __forceinline__ St<double> exact_flux_from_p(double pst, const FacePr
                                                         double ar, const Gas<double>& g) {
     const ExSide L = ex_side(q.l.q[0], q.l.q[4], al, g), R = ex_side(q.r.q[0], q.r.q[4], ar, g);
     // star_state_from_pstar's u, its two terms in ex_f's branch-coherent order
-    const bool lo_left = L.p <= R.p;
+    const bool lo_left = cmp64::le(L.p, R.p);
     const double t_lo = ex_fb(pst, lo_left ? L : R, g);
     const double t_hi = ex_fb(pst, lo_left ? R : L, g);
     const double u = 0.5 * (vl + vr) + 0.5 * ((lo_left ? t_hi : t_lo) - (lo_left ? t_lo : t_hi));
     // sample_star (riemann_solver.rs:224-255): u < 0 samples the right side
-    const bool right = u < 0.;
+    const bool right = lt0_64(u);
     const St<double> s = right ? q.r : q.l;
     const ExSide S = right ? R : L;
     const double v = right ? vr : vl;
     const double a = right ? -ar : al;  // the sampler's signed sound speed
     const double sg = right ? -1. : 1.;
     St<double> w;
-    if (pst > s.q[4]) {  // shock
+    if (cmp64::gt(pst, s.q[4])) {  // shock
         const double sp = shock_speed(v, a, pst / s.q[4], g);
-        w = sg * sp < 0. ? sample_middle(ex_middle_density(pst, S, g), u, pst, s, v, q.n) : s;
-    } else if (sg * (v - a) < 0.) {  // rarefaction whose head lies on the other side of x/t = 0
-        if (sg * rarefaction_tail_speed(u, a, pst / s.q[4], g) > 0.) w = sample_rarefaction_fan(s, a, v, q.n, g);
+        w = lt0_64(sg * sp) ? sample_middle(ex_middle_density(pst, S, g), u, pst, s, v, q.n) : s;
+    } else if (lt0_64(sg * (v - a))) {  // rarefaction whose head lies on the other side of x/t = 0
+        if (gt0_64(sg * rarefaction_tail_speed(u, a, pst / s.q[4], g))) w = sample_rarefaction_fan(s, a, v, q.n, g);
         else w = sample_middle(ex_middle_density(pst, S, g), u, pst, s, v, q.n);
     } else {
         w = s;
@@ -892,9 +892,9 @@ __device__ __forceinline__ V3<double> limiter_offset(const KP& p, int i, int f, 
 // not limited and take neither division.  The value is the same, NaN ratios
 // (which fmin passes over) included.
 __device__ __forceinline__ double limit_factor(double d_max, double d_min, double e_max, double e_min) {
-    if (e_max == 0. || e_min == 0.) return 1.;
-    const bool max_ge1 = e_max > 0. && d_max >= e_max;
-    const bool min_ge1 = e_min < 0. && d_min <= e_min;
+    if (is_zero64(e_max) || is_zero64(e_min)) return 1.;  // comparisons on the integer pipe (cmp64.cuh)
+    const bool max_ge1 = gt0_64(e_max) && cmp64::ge(d_max, e_max);
+    const bool min_ge1 = lt0_64(e_min) && cmp64::le(d_min, e_min);
     if (max_ge1 && min_ge1) return 1.;
     if (max_ge1) return m_min(1.0, d_min / e_min);
     if (min_ge1) return m_min(1.0, d_max / e_max);
@@ -955,7 +955,7 @@ __device__ __forceinline__ void gradients_cell(const KP& p, int i, int do_timest
                 // GradientData::collect (gradients.rs:35-41).  When ds.z is
                 // exactly zero (2D meshes) the z terms add +-0 to entries that
                 // are +0 (or 1), which leaves them unchanged, so they are skipped.
-                bool z = ds.z != 0.;
+                bool z = !is_zero64(ds.z);
 #pragma unroll
                 for (int q = 0; q < 5; q++) {
                     double wdq = w * (op.q[q] - prim.q[q]);
@@ -1113,7 +1113,7 @@ __device__ __forceinline__ void gradients_cell_warp(const KP& p, int i, int do_t
                         const double v = __shfl_sync(0xffffffffu, dq[q], t);
                         if (q == gq) dqt = v;
                     }
-                    const bool z = dz != 0.;
+                    const bool z = !is_zero64(dz);
                     const double da = ma == 0 ? dx : ma == 1 ? dy : dz, db = mb == 0 ? dx : mb == 1 ? dy : dz;
                     const double dax = gax == 0 ? dx : gax == 1 ? dy : dz;
                     const double u = grad_lane ? wt : da, v = grad_lane ? dqt : db, x = grad_lane ? dax : wt;
