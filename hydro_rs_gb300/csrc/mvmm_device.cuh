@@ -13,7 +13,6 @@
 #include <stdint.h>
 
 #include "bitconv.cuh"
-#include "cmp64.cuh"
 #include "mvmm_internal.h"
 
 namespace mvmm {
@@ -414,7 +413,7 @@ __device__ __forceinline__ ExSide ex_side(double rho, double p, double a, const 
     return ExSide{rho, p, a, g.tdgp1() / rho, g.gm1dgp1() * p};
 }
 __device__ __forceinline__ double ex_fb(double p, const ExSide& s, const Gas<double>& g) {  // :12-20
-    if (cmp64::gt(p, s.p)) return (p - s.p) * sqrt(s.A / (p + s.B));
+    if (p > s.p) return (p - s.p) * sqrt(s.A / (p + s.B));
     return g.tdgm1() * s.a * (g.pow_e1(p / s.p) - 1.);
 }
 // The two sides' terms are evaluated lower-pressure side first: for a pressure
@@ -424,7 +423,7 @@ __device__ __forceinline__ double ex_fb(double p, const ExSide& s, const Gas<dou
 // (left, right), so the value is the same.
 __device__ __forceinline__ double ex_f(double p, const ExSide& l, const ExSide& r, double vl, double vr,
                                        const Gas<double>& g) {  // :23-34
-    const bool lo_left = cmp64::le(l.p, r.p);
+    const bool lo_left = l.p <= r.p;
     const double t_lo = ex_fb(p, lo_left ? l : r, g);
     const double t_hi = ex_fb(p, lo_left ? r : l, g);
     return (lo_left ? t_lo : t_hi) + (lo_left ? t_hi : t_lo) + (vr - vl);
@@ -439,7 +438,7 @@ __device__ __forceinline__ double ex_f0(const ExSide& l, const ExSide& r, double
     return ex_fb0(l, g) + ex_fb0(r, g) + (vr - vl);
 }
 __device__ __forceinline__ double ex_fprimeb(double p, const ExSide& s, const Gas<double>& g) {  // :37-45
-    if (cmp64::gt(p, s.p)) return (1. - 0.5 * (p - s.p) / (s.B + p)) * sqrt(s.A / (p + s.B));
+    if (p > s.p) return (1. - 0.5 * (p - s.p) / (s.B + p)) * sqrt(s.A / (p + s.B));
     return 1. / s.rho / s.a * g.pow_me1(p / s.p);
 }
 __device__ __forceinline__ double ex_gb(double p, const ExSide& s, const Gas<double>& g) {  // :60-64
@@ -484,16 +483,15 @@ static __device__ __noinline__ double ex_brent(double lower, double upper, doubl
             *err |= 1u;
             break;
         }
-        if (cmp64::ne(fa, fc) && cmp64::ne(fb, fc))
+        if (fa != fc && fb != fc)
             s = a * fb * fc / (fa - fb) / (fa - fc) + b * fa * fc / (fb - fa) / (fb - fc) +
                 c * fa * fb / (fc - fa) / (fc - fb);
         else
             s = b - fb * (b - a) / (fb - fa);
         double tmp = 0.25 * (3. * a + b);
-        if (!((cmp64::gt(s, tmp) && cmp64::lt(s, b)) || (cmp64::lt(s, tmp) && cmp64::gt(s, b))) ||
-            (mflag && cmp64::abs_ge(s - b, 0.5 * fabs(b - c))) || (!mflag && cmp64::abs_ge(s - b, 0.5 * fabs(c - d))) ||
-            (mflag && cmp64::lt(fabs(b - c), 0.5 * tol * (b + c))) ||
-            (!mflag && cmp64::lt(fabs(c - d), 0.5 * tol * (c + d)))) {
+        if (!((s > tmp && s < b) || (s < tmp && s > b)) || (mflag && fabs(s - b) >= (0.5 * fabs(b - c))) ||
+            (!mflag && fabs(s - b) >= (0.5 * fabs(c - d))) || (mflag && fabs(b - c) < 0.5 * tol * (b + c)) ||
+            (!mflag && fabs(c - d) < 0.5 * tol * (c + d))) {
             s = 0.5 * (a + b);
             mflag = true;
         } else {
@@ -557,12 +555,12 @@ struct BrentMachine {
         err = 0;
         done = false;
         phase = 0;
-        if (gt0_64(fa * fb)) {
+        if (fa * fb > 0.) {
             err |= 2u;
             done = true;
             return;
         }
-        if (cmp64::abs_lt(fa, fb)) swap_ab();
+        if (fabs(fa) < fabs(fb)) swap_ab();
         c = a;
         fc = fa;
         mflag = true;
@@ -579,7 +577,7 @@ struct BrentMachine {
     }
     // the loop test, then the iteration's s (or done)
     __device__ __forceinline__ void next_s() {
-        if (!(cmp64::ne(fb, 0.) && cmp64::gt(fabs(a - b), tol * 0.5 * (a + b)))) {
+        if (!(fb != 0. && fabs(a - b) > tol * 0.5 * (a + b))) {
             done = true;
             return;
         }
@@ -589,16 +587,15 @@ struct BrentMachine {
             return;
         }
         double s;
-        if (cmp64::ne(fa, fc) && cmp64::ne(fb, fc))
+        if (fa != fc && fb != fc)
             s = a * fb * fc / (fa - fb) / (fa - fc) + b * fa * fc / (fb - fa) / (fb - fc) +
                 c * fa * fb / (fc - fa) / (fc - fb);
         else
             s = b - fb * (b - a) / (fb - fa);
         double tmp = 0.25 * (3. * a + b);
-        if (!((cmp64::gt(s, tmp) && cmp64::lt(s, b)) || (cmp64::lt(s, tmp) && cmp64::gt(s, b))) ||
-            (mflag && cmp64::abs_ge(s - b, 0.5 * fabs(b - c))) || (!mflag && cmp64::abs_ge(s - b, 0.5 * fabs(c - d))) ||
-            (mflag && cmp64::lt(fabs(b - c), 0.5 * tol * (b + c))) ||
-            (!mflag && cmp64::lt(fabs(c - d), 0.5 * tol * (c + d)))) {
+        if (!((s > tmp && s < b) || (s < tmp && s > b)) || (mflag && fabs(s - b) >= (0.5 * fabs(b - c))) ||
+            (!mflag && fabs(s - b) >= (0.5 * fabs(c - d))) || (mflag && fabs(b - c) < 0.5 * tol * (b + c)) ||
+            (!mflag && fabs(c - d) < 0.5 * tol * (c + d))) {
             s = 0.5 * (a + b);
             mflag = true;
         } else {
@@ -611,7 +608,7 @@ struct BrentMachine {
     // f(x) given
     __device__ __forceinline__ void step(double fx) {
         if (phase == 1) {
-            if (cmp64::ne(fx, 0.) && !lt0_64(fa * fx) && !cmp64::abs_lt(fx, fb)) done = true;
+            if (fx != 0. && !(fa * fx < 0.) && !(fabs(fx) < fabs(fb))) done = true;
             else next_s();
             return;
         }
@@ -619,18 +616,17 @@ struct BrentMachine {
         d = c;
         c = b;
         fc = fb;
-        const bool b_kept = !lt0_64(fa * fs);
-        if (!b_kept) {
+        const bool b_kept = !(fa * fs < 0.);
+        if (fa * fs < 0.) {
             b = s;
             fb = fs;
         } else {
             a = s;
             fa = fs;
         }
-        const bool swapped = cmp64::abs_lt(fa, fb);
+        const bool swapped = fabs(fa) < fabs(fb);
         if (swapped) swap_ab();
-        if (bisected && b_kept && !swapped && cmp64::ne(fb, 0.) && cmp64::gt(fabs(a - b), tol * 0.5 * (a + b)) &&
-            it + 64 <= max_it) {
+        if (bisected && b_kept && !swapped && fb != 0. && fabs(a - b) > tol * 0.5 * (a + b) && it + 64 <= max_it) {
             x = b + copysign(0.125 * tol * fabs(b), a - b);
             phase = 1;
         } else {
@@ -663,17 +659,17 @@ struct NewtonMachine {
         next_x(l, r, g);
     }
     __device__ __forceinline__ void end() {
-        brent = cmp64::gt(fabs(p - pg), 1e-6 * 0.5 * (p + pg)) && gt0_64(fpg);
+        brent = fabs(p - pg) > 1e-6 * 0.5 * (p + pg) && fpg > 0.;
         done = true;
     }
     // the loop test, then the next iterate (or done)
     __device__ __forceinline__ void next_x(const ExSide& l, const ExSide& r, const Gas<double>& g) {
-        if (!(cmp64::gt(fabs(p - pg), 1e-6 * 0.5 * (p + pg)) && lt0_64(fpg))) {
+        if (!(fabs(p - pg) > 1e-6 * 0.5 * (p + pg) && fpg < 0.0)) {
             end();
             return;
         }
         p = pg;
-        const bool lo_left = cmp64::le(l.p, r.p);
+        const bool lo_left = l.p <= r.p;
         const double d_lo = ex_fprimeb(pg, lo_left ? l : r, g);
         const double d_hi = ex_fprimeb(pg, lo_left ? r : l, g);
         pg = pg - fpg / ((lo_left ? d_lo : d_hi) + (lo_left ? d_hi : d_lo));
@@ -694,7 +690,7 @@ struct NewtonMachine {
 
 __device__ __forceinline__ double ex_middle_density(double p, const ExSide& s, const Gas<double>& g) {  // :193-212
     double pdps = p / s.p;
-    if (cmp64::gt(pdps, 1.)) return s.rho * (pdps + g.gm1dgp1()) / (g.gm1dgp1() * pdps + 1.);
+    if (pdps > 1.) return s.rho * (pdps + g.gm1dgp1()) / (g.gm1dgp1() * pdps + 1.);
     return s.rho * g.pow_ginv(pdps);
 }
 // ExactRiemannSolver::solve_for_star_state (exact.rs:241-291), in two parts
@@ -747,9 +743,9 @@ static __device__ __noinline__ int ex_star_start(ExSide l, ExSide r, double vl, 
     *p_guess_out = p_guess;
     *fp_guess_out = fp_guess;
     *fp0_out = fp;
-    const bool apart = cmp64::gt(fabs(p - p_guess), 1e-6 * 0.5 * (p + p_guess));
-    if (cmp64::ge(fp * fp_guess, 0.) && apart && lt0_64(fp_guess)) return EX_NEWTON;
-    return apart && gt0_64(fp_guess) ? EX_BRENT : EX_DONE;
+    const bool apart = fabs(p - p_guess) > 1e-6 * 0.5 * (p + p_guess);
+    if (fp * fp_guess >= 0. && apart && fp_guess < 0.0) return EX_NEWTON;
+    return apart && fp_guess > 0. ? EX_BRENT : EX_DONE;
 }
 // Brent's method on [0, p_guess] as the reference calls it
 __device__ __forceinline__ double ex_star_brent(double p_guess, double fp_guess, const ExSide& l, const ExSide& r,

@@ -4,6 +4,7 @@
 // reference evaluates it.  One CUDA thread per face for the flux stage, one per
 // cell for the cell stages; the flux scatter is a deterministic CSR gather in
 // the reference's face order (no atomics on floating-point data).
+#include "cmp64.cuh"
 #include "face64.cuh"
 #include "mvmm_cellops.cuh"
 
@@ -239,23 +240,23 @@ __device__ __forceinline__ St<double> exact_flux_from_p(double pst, const FacePr
                                                         double ar, const Gas<double>& g) {
     const ExSide L = ex_side(q.l.q[0], q.l.q[4], al, g), R = ex_side(q.r.q[0], q.r.q[4], ar, g);
     // star_state_from_pstar's u, its two terms in ex_f's branch-coherent order
-    const bool lo_left = cmp64::le(L.p, R.p);
+    const bool lo_left = L.p <= R.p;
     const double t_lo = ex_fb(pst, lo_left ? L : R, g);
     const double t_hi = ex_fb(pst, lo_left ? R : L, g);
     const double u = 0.5 * (vl + vr) + 0.5 * ((lo_left ? t_hi : t_lo) - (lo_left ? t_lo : t_hi));
     // sample_star (riemann_solver.rs:224-255): u < 0 samples the right side
-    const bool right = lt0_64(u);
+    const bool right = u < 0.;
     const St<double> s = right ? q.r : q.l;
     const ExSide S = right ? R : L;
     const double v = right ? vr : vl;
     const double a = right ? -ar : al;  // the sampler's signed sound speed
     const double sg = right ? -1. : 1.;
     St<double> w;
-    if (cmp64::gt(pst, s.q[4])) {  // shock
+    if (pst > s.q[4]) {  // shock
         const double sp = shock_speed(v, a, pst / s.q[4], g);
-        w = lt0_64(sg * sp) ? sample_middle(ex_middle_density(pst, S, g), u, pst, s, v, q.n) : s;
-    } else if (lt0_64(sg * (v - a))) {  // rarefaction whose head lies on the other side of x/t = 0
-        if (gt0_64(sg * rarefaction_tail_speed(u, a, pst / s.q[4], g))) w = sample_rarefaction_fan(s, a, v, q.n, g);
+        w = sg * sp < 0. ? sample_middle(ex_middle_density(pst, S, g), u, pst, s, v, q.n) : s;
+    } else if (sg * (v - a) < 0.) {  // rarefaction whose head lies on the other side of x/t = 0
+        if (sg * rarefaction_tail_speed(u, a, pst / s.q[4], g) > 0.) w = sample_rarefaction_fan(s, a, v, q.n, g);
         else w = sample_middle(ex_middle_density(pst, S, g), u, pst, s, v, q.n);
     } else {
         w = s;
