@@ -1,8 +1,8 @@
 """Mesh construction (host side; not part of the hot path).
 
 The reference builds its Voronoi mesh on the host with meshless_voronoi
-(``src/space.rs:571-594``) and the benchmark spec keeps it there: the hot path
-only consumes the face list and the CSR.  1D meshes are analytic here; 2D and
+(``src/space.rs:571-594``), and the mesh stays on the host here too: the hot
+path only consumes the face list and the CSR.  1D meshes are analytic here; 2D and
 3D meshes come from this library's own C++ builder (``csrc/voronoi.cpp``,
 compiled to ``_build/libmvmm_mesh.so`` by :mod:`hydro_rs_gb300.build`).
 

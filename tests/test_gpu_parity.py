@@ -1,6 +1,6 @@
 """GPU parity: the CUDA path, called through the C ABI, against the CPU oracle.
 
-Tolerances (the benchmark spec): plain FP64 path within 1e-12 (norm-wise relative, per
+Tolerances: plain FP64 path within 1e-12 (norm-wise relative, per
 conserved quantity) after the first dt>0 step and 1e-9 at t_end; the FP32-face
 form is checked through its L1 density error against the FP64 oracle.
 """

@@ -63,7 +63,7 @@ def test_gpu_flux_frame_parity_to_t_end(gpu_lib):
 @pytest.mark.gpu
 def test_gpu_fp32_face_l1_at_512_with_flux_frame(gpu_lib):
     """Without the seam's runaway gradients the FP32-face form stays on the
-    plain form's timeline and within the benchmark spec's 1e-5 (L1, density)."""
+    plain form's timeline and within 1e-5 of it (L1, density)."""
     from hydro_rs_gb300 import gpu as G
 
     p = _kh(512, 1)
