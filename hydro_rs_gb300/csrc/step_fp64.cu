@@ -1213,7 +1213,7 @@ __global__ void __launch_bounds__(kMaxBlock, 3) k_gradients(KP p, int do_timeste
     if constexpr (LIST) {
         const int lane = threadIdx.x & 31, n_warps = (gridDim.x * blockDim.x) >> 5;
         for (int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < n_items; w += n_warps)
-            gradients_cell_warp(p, p.cell_list[w], do_timestep, lane);
+            gradients_cell_warp(p, cell_at(p, w), do_timestep, lane);
         return;
     }
     // The cells' loops over their faces have as many trips as the cell has
@@ -1547,10 +1547,21 @@ void launch_update(const KP& p, int do_c2p, cudaStream_t s) {
 void launch_c2p(const KP& p, cudaStream_t s) {
     if (p.n > 0) k_c2p<<<grid(p.n, p.blk_cell), p.blk_cell, 0, s>>>(p);
 }
+// A mesh too small to fill the device with a thread per cell (at most 24 warps'
+// worth of cells per SM) runs a warp per cell, as hierarchical steps do: each
+// cell's FP64 chain is then a warp's, and shorter (the lanes share its faces,
+// each WLS sum is a lane's), where a thread per cell leaves most SMs idle while
+// a few warps run long chains.  The two give the same bits.
 void launch_gradients(const KP& p, int do_timestep, cudaStream_t s) {
     if (p.n <= 0) return;
-    if (p.use_list) k_gradients<true><<<cell_grid(p), p.blk_cell, 0, s>>>(p, do_timestep);
-    else k_gradients<false><<<cell_grid(p), p.blk_cell, 0, s>>>(p, do_timestep);
+    if (p.use_list) {
+        k_gradients<true><<<cell_grid(p), p.blk_cell, 0, s>>>(p, do_timestep);
+    } else if (p.n <= p.n_sms * 24) {
+        const int blocks = (int)(((long long)p.n * 32 + p.blk_cell - 1) / p.blk_cell);
+        k_gradients<true><<<blocks, p.blk_cell, 0, s>>>(p, do_timestep);
+    } else {
+        k_gradients<false><<<cell_grid(p), p.blk_cell, 0, s>>>(p, do_timestep);
+    }
 }
 void launch_timesteps(const KP& p, double* dt_out, cudaStream_t s) {
     if (p.n > 0) k_timesteps<<<grid(p.n, p.blk_cell), p.blk_cell, 0, s>>>(p, dt_out);
