@@ -1547,21 +1547,10 @@ void launch_update(const KP& p, int do_c2p, cudaStream_t s) {
 void launch_c2p(const KP& p, cudaStream_t s) {
     if (p.n > 0) k_c2p<<<grid(p.n, p.blk_cell), p.blk_cell, 0, s>>>(p);
 }
-// A mesh too small to fill the device with a thread per cell (at most 24 warps'
-// worth of cells per SM) runs a warp per cell, as hierarchical steps do: each
-// cell's FP64 chain is then a warp's, and shorter (the lanes share its faces,
-// each WLS sum is a lane's), where a thread per cell leaves most SMs idle while
-// a few warps run long chains.  The two give the same bits.
 void launch_gradients(const KP& p, int do_timestep, cudaStream_t s) {
     if (p.n <= 0) return;
-    if (p.use_list) {
-        k_gradients<true><<<cell_grid(p), p.blk_cell, 0, s>>>(p, do_timestep);
-    } else if (p.n <= p.n_sms * 24) {
-        const int blocks = (int)(((long long)p.n * 32 + p.blk_cell - 1) / p.blk_cell);
-        k_gradients<true><<<blocks, p.blk_cell, 0, s>>>(p, do_timestep);
-    } else {
-        k_gradients<false><<<cell_grid(p), p.blk_cell, 0, s>>>(p, do_timestep);
-    }
+    if (p.use_list) k_gradients<true><<<cell_grid(p), p.blk_cell, 0, s>>>(p, do_timestep);
+    else k_gradients<false><<<cell_grid(p), p.blk_cell, 0, s>>>(p, do_timestep);
 }
 void launch_timesteps(const KP& p, double* dt_out, cudaStream_t s) {
     if (p.n > 0) k_timesteps<<<grid(p.n, p.blk_cell), p.blk_cell, 0, s>>>(p, dt_out);
