@@ -80,10 +80,14 @@ WORKLOADS = {
     # moving mesh: the shear layer with steered generators, host Voronoi rebuild every step
     "kh2d_moving": "kelvin_helmholtz_2d {n}x{n} jittered periodic Voronoi, exact Riemann solver, gamma=5/3, "
                    "steered generators (particle_motion=steer), mesh rebuilt on the host every step",
+    # self-gravity kicks: the shear layer with the direct O(N^2) sum over j > i every step
+    "kh2d_selfgrav": "kelvin_helmholtz_2d {n}x{n} jittered periodic Voronoi, HLLC, gamma=5/3, self-gravity "
+                     "(softening 0.01) accelerations computed and kicked every step",
     # served: Poisson stream (50 req/s) of {n} isentropic-vortex runs, 32^2..512^2, HLLC, t_end=1
     "serve2d": "{n} served isentropic-vortex requests (Poisson 50/s, 32^2..512^2 periodic Voronoi, HLLC, t_end=1)",
 }
 DATA = {
+    "kh2d_selfgrav": "synthetic (seeded jittered lattice, shear-layer ICs)",
     "kh2d": "synthetic (seeded jittered lattice, shear-layer ICs)",
     "kh2d_hllc": "synthetic (seeded jittered lattice, shear-layer ICs)",
     "sod1d": "synthetic (uniform 1D lattice, Sod ICs)",
@@ -91,7 +95,7 @@ DATA = {
     "batch1d": "synthetic (seeded random 1D Riemann problems)",
     "batch1d_pvrs": "synthetic (seeded random 1D Riemann problems)",
 }
-DEFAULT_N = {"kh2d_moving": NX, "kh2d": NX, "kh2d_hllc": 1024, "sod1d": 1000, "blast3d": 128, "batch1d": 512, "batch1d_pvrs": 512, "serve2d": 60}
+DEFAULT_N = {"kh2d_selfgrav": 128, "kh2d_moving": NX, "kh2d": NX, "kh2d_hllc": 1024, "sod1d": 1000, "blast3d": 128, "batch1d": 512, "batch1d_pvrs": 512, "serve2d": 60}
 
 
 def _problem(nx=NX, workload="kh2d"):
@@ -108,8 +112,11 @@ def _problem(nx=NX, workload="kh2d"):
     elif workload == "blast3d":
         p = ics.point_blast_3d(nx, seed=3, riemann=ics.HLLC, t_end=0.05, sync_all=False)
     else:
-        kind = ics.HLLC if workload == "kh2d_hllc" else ics.EXACT
+        kind = ics.HLLC if workload in ("kh2d_hllc", "kh2d_selfgrav") else ics.EXACT
         p = ics.kelvin_helmholtz_2d(nx, seed=2, riemann=kind, t_end=1.5)
+        if workload == "kh2d_selfgrav":
+            p.params.gravity, p.params.gravity_softening = ics.GRAVITY_SELF, 0.01
+            p.params.gravity_accelerations = True
     return p, time.perf_counter() - t0
 
 
@@ -889,6 +896,81 @@ def run_moving(args):
     print(json.dumps(line))
 
 
+# FP64 operations per pair of k_self_gravity's sum: 3 subtractions, 3 products
+# and 2 sums for |d|^2, the square root, + softening, r r r (2), m d (3), the 3
+# divisions and the 3 accumulations (square root and division counted as one).
+SELF_GRAVITY_FLOP_PER_PAIR = 21
+
+
+def run_self_gravity(args):
+    """Self-gravity kicks: SelfGravity::compute_accelerations (gravity.rs:22-43)
+    at the runner's "TODO: gravity" point of every step, then kick2 / kick1.
+    `value` is active-face updates per second of device step time (plain FP64
+    form); `self_gravity` gives the update stage (k_update + k_self_gravity,
+    from event nodes in the step graph) as pairs per second and against the
+    FP64 throughput measured here."""
+    import torch
+
+    from hydro_rs_gb300 import gpu as G
+    from hydro_rs_gb300 import ics
+
+    ws, rank = _dist()
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    if rank != 0:
+        return
+    problem, _ = _problem(args.nx, "kh2d_selfgrav")
+    n = problem.mesh.n_cells
+    stream = torch.cuda.Stream()
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    sim = G.GpuSim(problem, stream=stream.cuda_stream)
+    with _Clocks() as clk:
+        for _ in range(args.warmup):
+            sim.step()
+        f0 = sim.sync_time()[1]
+        ms = _time_steps(sim, args.steps, stream, flush, torch)
+        faces = sim.sync_time()[1] - f0
+        prof = _face_kernel_ms(sim, 3)
+    ev_ms = prof["end"][0] / max(prof["end"][1], 1)
+    upd_ms = max(prof["update"][0] / max(prof["update"][1], 1) - ev_ms, 0.0)
+    pairs = n * (n - 1) // 2
+    fp64_peak = _fp64_peak(torch)
+    ach = SELF_GRAVITY_FLOP_PER_PAIR * pairs / (upd_ms * 1e-3) / 1e12
+    cpu = None
+    if not args.no_cpu:
+        from oracle import oracle as O
+
+        threads = os.cpu_count() or 1
+        osim = O.OracleSim(problem, n_threads=threads)
+        osim.step()
+        f1, t1, k = osim.active_faces, time.perf_counter(), 0
+        while time.perf_counter() - t1 < 15.0 and k < 50:
+            osim.step()
+            k += 1
+        t_cpu = time.perf_counter() - t1
+        cpu = {"value": (osim.active_faces - f1) / t_cpu, "unit": UNIT, "cores": threads, "kind": "port",
+               "pairs_per_s": pairs * k / t_cpu,
+               "sample": f"{k} steps of the same workload on the oracle ({t_cpu:.1f} s)"}
+    line = {
+        "metric": METRIC, "value": faces / (ms * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded jittered lattice, shear-layer ICs)",
+        "config": {"workload": WORKLOADS["kh2d_selfgrav"].format(n=args.nx), "cells": n,
+                   "faces": problem.mesh.n_faces, "precision": PRECISION_FP64,
+                   "l2": "flushed before each step", "parallelism": "replicas x1"},
+        "self_gravity": {"kernel": "k_update + k_self_gravity", "stage_ms": round(upd_ms, 4),
+                         "pairs_per_launch": pairs, "pairs_per_s": pairs / (upd_ms * 1e-3),
+                         "roofline": None if fp64_peak is None else {
+                             "bound": "fp64", "achieved": round(ach, 4), "peak": round(fp64_peak, 3),
+                             "unit": "TFLOP/s", "frac": round(ach / fp64_peak, 4),
+                             "flop_per_pair": SELF_GRAVITY_FLOP_PER_PAIR,
+                             "peak_kind": "measured here: torch.matmul float64 4096^3 (cuBLAS DGEMM), best of 5"}},
+        # predict, face flux, update, self-gravity, gradients, limiter
+        "gpu_launches": args.steps * 6,
+        "cpu_baseline": cpu, "clocks": clk.summary(0),
+    }
+    print(json.dumps(line))
+
+
 def run_reference(args):
     ws, rank = _dist()
     if rank != 0:
@@ -947,6 +1029,8 @@ def main():
         run_serve(args)
     elif args.workload == "kh2d_moving":
         run_moving(args)
+    elif args.workload == "kh2d_selfgrav":
+        run_self_gravity(args)
     elif args.to_end and args.workload in ("batch1d", "batch1d_pvrs"):
         run_batch_to_end(args)
     else:

@@ -75,6 +75,8 @@ struct mvmm_ctx {
     int* inst = nullptr;       // per-cell instance (batches only)
     double* inst_tb = nullptr;  // per-instance time_base, 1/time_base (batches only)
     double* inst_tbi = nullptr;
+    int* inst_end = nullptr;    // per-instance cell end (batches with self-gravity accelerations)
+    double* agrav = nullptr;    // self-gravity: a_grav [3][n]
     unsigned int* face_stamp = nullptr;
     // moving meshes: face capacity, pending geometry of the rebuilt cells
     int nf_cap = 0;
@@ -186,6 +188,8 @@ KP make_kp(mvmm_ctx* c, int stage, int flux_rows) {
     p.n_inst = c->n_inst;
     p.inst_tb = c->inst_tb;
     p.inst_tbi = c->inst_tbi;
+    p.inst_end = c->inst_end;
+    p.agrav = c->agrav;
     // hierarchical steps of a single simulation walk a compacted active-face
     // list; synchronised steps, batches and per-stage calls sweep all faces
     p.use_list = (!stage && !c->prm.sync_all && c->n_inst == 1) ? 1 : 0;
@@ -271,6 +275,11 @@ struct StepHooks {
 // captured into the profiling graph.
 void record_ev(mvmm_ctx* c, int j, cudaStream_t s) { cudaEventRecordWithFlags(c->ev[j], s, cudaEventRecordExternal); }
 
+// Self-gravity accelerations kick: kick2 and cons->prim follow k_self_gravity.
+bool self_gravity_kicks(const mvmm_ctx* c) {
+    return c->prm.gravity == MVMM_GRAVITY_SELF && c->prm.gravity_accelerations;
+}
+
 void enqueue_step_kernels(mvmm_ctx* c, bool with_events, const StepHooks& h = StepHooks()) {
     KP p = make_kp(c, 0, 7);
     p.stale_all = h.stale_all ? 1 : 0;
@@ -290,6 +299,7 @@ void enqueue_step_kernels(mvmm_ctx* c, bool with_events, const StepHooks& h = St
     if (with_events) record_ev(c, 2, s);
     if (h.wait_before_update) cudaStreamWaitEvent(s, h.wait_before_update, 0);
     launch_update(p, 1, s);
+    if (self_gravity_kicks(c)) launch_self_gravity(p, 1, 1, s);  // kick2 and cons->prim after the accelerations
     if (h.after_update) cudaEventRecord(h.after_update, s);
     if (with_events) record_ev(c, 3, s);
     if (c->prm.precision == MVMM_PRECISION_FP32FACE) launch_gradients32(p, s);
@@ -471,8 +481,6 @@ static int create_impl(const mvmm_params* prm, const mvmm_mesh* m, int64_t n_ins
     }
     if (prm->gravity < MVMM_GRAVITY_NONE || prm->gravity > MVMM_GRAVITY_KEPLERIAN)
         return fail(MVMM_E_INVALID, "unknown gravity solver");
-    if (prm->gravity == MVMM_GRAVITY_SELF && prm->gravity_accelerations)
-        return fail(MVMM_E_UNSUPPORTED, "self-gravity accelerations are not computed (external potentials only)");
     if ((prm->gravity == MVMM_GRAVITY_SELF || prm->gravity == MVMM_GRAVITY_KEPLERIAN) &&
         !(prm->gravity_softening >= 0.))
         return fail(MVMM_E_INVALID, "gravity needs a softening_length >= 0");
@@ -567,7 +575,9 @@ static int create_impl(const mvmm_params* prm, const mvmm_mesh* m, int64_t n_ins
         ALLOC(c->inst, n * 4);
         ALLOC(c->inst_tb, c->n_inst * 8);
         ALLOC(c->inst_tbi, c->n_inst * 8);
+        if (prm->gravity == MVMM_GRAVITY_SELF) ALLOC(c->inst_end, c->n_inst * 4);
     }
+    if (prm->gravity == MVMM_GRAVITY_SELF) ALLOC(c->agrav, 3 * n * 8);
 #undef ALLOC
     if (cudaMallocHost((void**)&c->tl_host, sizeof(DevTimeline) * c->n_inst) != cudaSuccess)
         return cleanup(MVMM_E_NOMEM, "cudaMallocHost failed");
@@ -605,6 +615,7 @@ static int create_impl(const mvmm_params* prm, const mvmm_mesh* m, int64_t n_ins
     cudaMemsetAsync(c->fresh, 0, n, s);
     if (c->cf_fresh) cudaMemsetAsync(c->cf_fresh, 0, n, s);
     if (c->extrap_step) cudaMemsetAsync(c->extrap_step, 0, n * 4, s);  // current at step 0
+    if (c->agrav) cudaMemsetAsync(c->agrav, 0, 3 * n * 8, s);  // Particle::new: a_grav = 0
     std::memset(c->tl_host, 0, sizeof(DevTimeline) * c->n_inst);
     for (int k = 0; k < c->n_inst; k++) {
         c->tl_host[k].min_dti = kMax;
@@ -612,6 +623,7 @@ static int create_impl(const mvmm_params* prm, const mvmm_mesh* m, int64_t n_ins
     }
     cudaMemcpyAsync(c->tl, c->tl_host, sizeof(DevTimeline) * c->n_inst, cudaMemcpyHostToDevice, s);
     std::vector<double> tb, tbi;
+    std::vector<int32_t> inst_end_h;
     if (c->n_inst > 1) {
         tb.resize(c->n_inst);
         tbi.resize(c->n_inst);
@@ -622,6 +634,11 @@ static int create_impl(const mvmm_params* prm, const mvmm_mesh* m, int64_t n_ins
         cudaMemcpyAsync(c->inst, inst_h.data(), n * 4, cudaMemcpyHostToDevice, s);
         cudaMemcpyAsync(c->inst_tb, tb.data(), c->n_inst * 8, cudaMemcpyHostToDevice, s);
         cudaMemcpyAsync(c->inst_tbi, tbi.data(), c->n_inst * 8, cudaMemcpyHostToDevice, s);
+        if (c->inst_end) {
+            inst_end_h.resize(c->n_inst);
+            for (int k = 0; k < c->n_inst; k++) inst_end_h[k] = (int32_t)cell_off[k + 1];
+            cudaMemcpyAsync(c->inst_end, inst_end_h.data(), c->n_inst * 4, cudaMemcpyHostToDevice, s);
+        }
     }
     cudaError_t e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return cleanup(MVMM_E_CUDA, std::string("mesh upload: ") + cudaGetErrorString(e));
@@ -669,7 +686,7 @@ int mvmm_ctx_destroy(mvmm_ctx* c) {
                     c->cf, c->timebin, c->tb_tmp, c->active, c->flux, c->flux32, c->geo, c->geo_pos, c->geo_changed, c->snap, c->snap_tb, c->xfer_stored, c->brent_jobs, c->brent_count, c->extrap_step, c->dt_log, c->dtmp, c->face_stamp, c->touch, c->blocks_done, c->cell_list, c->fresh, c->cf_fresh,
                     c->pend_vol, c->pend_cen, c->dirty, c->chg_list,
                     c->face_list, c->tl,
-                    c->inst, c->inst_tb, c->inst_tbi};
+                    c->inst, c->inst_tb, c->inst_tbi, c->inst_end, c->agrav};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (c->tl_host) cudaFreeHost(c->tl_host);
@@ -1358,6 +1375,7 @@ int mvmm_apply_fluxes(mvmm_ctx* c, const double* fluxes, const uint8_t* active) 
         CUDA_TRY(cudaMemcpyAsync(c->flux, fluxes, (size_t)10 * c->nf * 8, cudaMemcpyHostToDevice, c->stream));
     KP p = make_kp(c, 1, 10);
     launch_update(p, 0, c->stream);
+    if (self_gravity_kicks(c)) launch_self_gravity(p, 1, 0, c->stream);
     CUDA_TRY(cudaGetLastError());
     return finish(c);
 }
@@ -1401,9 +1419,14 @@ int mvmm_gravity_timesteps(mvmm_ctx* c, double* dt_out) {
 
 int mvmm_gravity_accelerations(mvmm_ctx* c, double* a_out) {
     if (!c || !a_out) return fail(MVMM_E_INVALID, "null argument");
-    if (c->prm.gravity == MVMM_GRAVITY_SELF)
-        return fail(MVMM_E_UNSUPPORTED, "self-gravity accelerations are not computed (external potentials only)");
     const KP p = make_kp(c, 1, 10);
+    if (c->prm.gravity == MVMM_GRAVITY_SELF) {  // SelfGravity::compute_accelerations sets every a_grav
+        launch_self_gravity(p, 0, 0, c->stream);
+        CUDA_TRY(cudaGetLastError());
+        if (c->n > 0)
+            CUDA_TRY(cudaMemcpyAsync(a_out, c->agrav, (size_t)3 * c->n * 8, cudaMemcpyDeviceToHost, c->stream));
+        return finish(c);
+    }
     for (int a = 0; a < 3; a++) {
         if (c->prm.gravity == MVMM_GRAVITY_NONE) {
             CUDA_TRY(cudaMemsetAsync(c->dtmp, 0, (size_t)c->n * 8, c->stream));

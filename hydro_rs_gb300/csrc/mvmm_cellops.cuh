@@ -163,11 +163,24 @@ __device__ __forceinline__ V3<double> grav_acceleration(const KP& p, V3<double> 
     const double d = r * r2;
     return v3(-dx.x / d, -dx.y / d, -dx.z / d);
 }
+// Cell i's a_grav where the accelerations are computed: self-gravity's from
+// the last SelfGravity::compute_accelerations (k_self_gravity), an external
+// potential's at the generator position.
+__device__ __forceinline__ V3<double> cell_acceleration(const KP& p, int i) {
+    if (p.grav == MVMM_GRAVITY_SELF) return v3(p.agrav[i], p.agrav[p.n + i], p.agrav[2 * p.n + i]);
+    return grav_acceleration(p, C3(p, F_LOC, i));
+}
 // GravitySolver::compute_timesteps of cell i (gravity.rs:45-53, 71-73, 90-95,
-// 119-123).  Only the Keplerian potential sets a limit: self-gravity's
-// accelerations are zero (the runners never compute them), for which it
-// returns INFINITY, as does the constant potential.
+// 119-123).  Self-gravity: sqrt(softening / |a_grav|), INFINITY where a_grav
+// is zero (always, unless its accelerations are computed); the Keplerian
+// potential: eta * r_2D / v_circ; the constant potential: INFINITY.
 __device__ __forceinline__ double grav_timestep(const KP& p, int i) {
+    if (p.grav == MVMM_GRAVITY_SELF) {
+        if (!p.agrav) return INFINITY;
+        const double a2 = len2(v3(p.agrav[i], p.agrav[p.n + i], p.agrav[2 * p.n + i]));
+        if (a2 == 0.) return INFINITY;
+        return sqrt(p.grav_soft / sqrt(a2));
+    }
     if (p.grav != MVMM_GRAVITY_KEPLERIAN) return INFINITY;
     // eta * radius (in 2D whatever the dimensionality) / circular_velocity
     const V3<double> dx = C3(p, F_LOC, i) - v3(p.grav_pos[0], p.grav_pos[1], p.grav_pos[2]);

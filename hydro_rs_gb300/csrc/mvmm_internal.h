@@ -161,6 +161,8 @@ struct KP {
     // acceleration, Keplerian position
     int grav, grav_acc;
     double grav_soft, grav_avec[3], grav_pos[3];
+    double* agrav;           // self-gravity: a_grav [3][n] (SelfGravity::compute_accelerations), or null
+    const int* inst_end;     // batches with self-gravity: each instance's cell end, or null
     int limiter_frame;       // 1: the cell-wise limiter's face offsets in flux_exchange's frame
     uint8_t* dirty;          // or null: 1 for cells whose host rows a kernel rewrote since the
                              //   last mvmm_step_cells_changed stored them (that call's copies back)
@@ -201,6 +203,7 @@ void launch_c2p(const KP& p, cudaStream_t s);
 void launch_gradients(const KP& p, int do_timestep, cudaStream_t s);
 void launch_timesteps(const KP& p, double* dt_out, cudaStream_t s);
 void launch_gravity(const KP& p, int what, double* out, cudaStream_t s);
+void launch_self_gravity(const KP& p, int kick, int do_c2p, cudaStream_t s);
 void launch_limit(const KP& p, cudaStream_t s);
 void launch_compact(const KP& p, cudaStream_t s);
 void launch_end(const KP& p, cudaStream_t s);

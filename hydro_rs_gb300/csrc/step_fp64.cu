@@ -728,6 +728,19 @@ __device__ __forceinline__ void update_cell(const KP& p, int i, int do_c2p) {
     update_finish(p, i, k, act, facc, msv, maor, do_c2p);
 }
 
+// cons->prim of an updated cell, with the FP32 copies the FP32-face form's
+// gradient stage reads.
+__device__ __forceinline__ void c2p_with_copies(const KP& p, int i, const St<double>& cons, unsigned int* err) {
+    c2p(p, i, cons, err);
+    if (p.fp32) {
+#pragma unroll
+        for (int q = 0; q < 5; q++) p.cf[(size_t)(G_PRIM + q) * p.n + i] = f32(C(p, F_PRIM + q, i));
+    }
+}
+// Self-gravity accelerations need every cell's updated mass, so kick2 and
+// cons->prim of the active cells move to k_self_gravity.
+__device__ __forceinline__ bool self_gravity_kicks(const KP& p) { return p.grav == MVMM_GRAVITY_SELF && p.grav_acc; }
+
 // Particle::apply_flux, kick2 and cons->prim of one cell once its faces are summed.
 __device__ __forceinline__ void update_finish(const KP& p, int i, int k, bool act, St<double> facc, double msv,
                                               double maor, int do_c2p) {
@@ -736,20 +749,18 @@ __device__ __forceinline__ void update_finish(const KP& p, int i, int k, bool ac
     if (act) {
         p.fresh[i] = 0;  // prim (here), grad and v_rel (gradient stage) change
         St<double> cons = apply_flux64(C5(p, F_CONS, i), facc, &err);
-        // kick2 (runner/hydrodynamics.rs:51-57); accelerations only where the
-        // external potential's are computed (at the runner's "TODO: gravity")
-        cons = p.grav_acc ? grav_kick64(cons, C(p, F_DT, i), grav_acceleration(p, C3(p, F_LOC, i)))
-                          : zero_kick64(cons);
         facc = st_zero<double>();
-        W5(p, F_CONS, i, cons);
         W(p, F_MSV, i, msv);
         W(p, F_MAOR, i, maor);
-        if (do_c2p) {
-            c2p(p, i, cons, &err);
-            if (p.fp32) {  // FP32 copies read by the FP32-face form's gradient stage
-#pragma unroll
-                for (int q = 0; q < 5; q++) p.cf[(size_t)(G_PRIM + q) * p.n + i] = f32(C(p, F_PRIM + q, i));
-            }
+        if (self_gravity_kicks(p)) {
+            W5(p, F_CONS, i, cons);
+        } else {
+            // kick2 (runner/hydrodynamics.rs:51-57); accelerations only where the
+            // external potential's are computed (at the runner's "TODO: gravity")
+            cons = p.grav_acc ? grav_kick64(cons, C(p, F_DT, i), grav_acceleration(p, C3(p, F_LOC, i)))
+                              : zero_kick64(cons);
+            W5(p, F_CONS, i, cons);
+            if (do_c2p) c2p_with_copies(p, i, cons, &err);
         }
     }
     W5(p, F_FACC, i, facc);
@@ -1253,6 +1264,71 @@ __global__ void __launch_bounds__(kMaxBlock) k_gravity(KP p, int what, double* o
     }
 }
 
+// SelfGravity::compute_accelerations (gravity.rs:22-43): cell i sums, in index
+// order, the pull of the cells after it in its simulation (j > i only, as the
+// reference does):
+//     r = |x_j - x_i| + softening,   a_i += (m_j (x_j - x_i)) / (r r r),
+// with m_j the conserved mass after this step's update.  The block stages the
+// positions and masses of kGravTile cells at a time in shared memory; every
+// thread reads the same entry (a broadcast), so the sum is FP64-pipe bound.
+// Blocks over the first cells have the longest sums and start first.
+// kick: then kick2 and cons->prim (do_c2p) of the active cells, which the
+// update left to this kernel.
+constexpr int kGravTile = 128;
+__global__ void __launch_bounds__(kGravTile) k_self_gravity(KP p, int kick, int do_c2p) {
+    __shared__ double s_x[kGravTile], s_y[kGravTile], s_z[kGravTile], s_m[kGravTile];
+    __shared__ int s_end;
+    const int i0 = blockIdx.x * kGravTile, i = i0 + threadIdx.x;
+    const bool own = i < p.n;
+    const int k = own ? inst_of(p, i) : 0;
+    const int jend = own ? (p.inst_end ? p.inst_end[k] : p.n) : 0;
+    if (threadIdx.x == 0) s_end = 0;
+    __syncthreads();
+    if (own) atomicMax(&s_end, jend);
+    __syncthreads();
+    const int block_end = s_end;
+    const V3<double> xi = own ? C3(p, F_LOC, i) : v3(0., 0., 0.);
+    const double eps = p.grav_soft;
+    double ax = 0., ay = 0., az = 0.;
+    for (int j0 = i0; j0 < block_end; j0 += kGravTile) {
+        const int j = j0 + threadIdx.x;
+        __syncthreads();  // the previous tile is consumed
+        if (j < p.n) {
+            s_x[threadIdx.x] = C(p, F_LOC, j);
+            s_y[threadIdx.x] = C(p, F_LOC + 1, j);
+            s_z[threadIdx.x] = C(p, F_LOC + 2, j);
+            s_m[threadIdx.x] = C(p, F_CONS, j);
+        }
+        __syncthreads();
+        const int lo = max(i + 1 - j0, 0), hi = min(jend - j0, kGravTile);
+#pragma unroll 4
+        for (int t = lo; t < hi; t++) {
+            const double dx = s_x[t] - xi.x, dy = s_y[t] - xi.y, dz = s_z[t] - xi.z;
+            const double r = sqrt(dx * dx + dy * dy + dz * dz) + eps;  // (x_j - x_i).length() + softening
+            const double m = s_m[t], r3 = r * r * r;
+            ax = ax + (m * dx) / r3;
+            ay = ay + (m * dy) / r3;
+            az = az + (m * dz) / r3;
+        }
+    }
+    if (!own) return;
+    p.agrav[i] = ax;
+    p.agrav[p.n + i] = ay;
+    p.agrav[2 * p.n + i] = az;
+    if (!kick || !p.active[i] || p.tl[k].done) return;
+    // kick2 (runner/hydrodynamics.rs:51-57) and cons->prim
+    unsigned int err = 0;
+    const St<double> cons = grav_kick64(C5(p, F_CONS, i), C(p, F_DT, i), v3(ax, ay, az));
+    // Other blocks may still be reading the mass row: grav_kick adds +0 to it,
+    // which changes its bits only from -0 to +0, and a term m_j (x_j - x_i) / r^3
+    // of either zero leaves every sum (which starts at +0) as it is.
+    if (__double_as_longlong(cons.q[0]) != __double_as_longlong(C(p, F_CONS, i))) W(p, F_CONS, i, cons.q[0]);
+#pragma unroll
+    for (int q = 1; q < 5; q++) W(p, F_CONS + q, i, cons.q[q]);
+    if (do_c2p) c2p_with_copies(p, i, cons, &err);
+    if (err) set_err(p, k, err);
+}
+
 // ------------------------------------------------- limiter / sync / end --
 // timestep_sync or timestep_limiter (runner/hydrodynamics.rs:160-191) with
 // Particle::timestep_limit (part.rs:263-297); then reset_extrapolations and
@@ -1315,8 +1391,7 @@ __device__ __forceinline__ void limit_cell(const KP& p, int i, int wakeup = -1) 
         // double x, so the row is left as the update wrote it; only where
         // the external potential's accelerations are computed does it kick,
         // over the new dt.
-        if (p.grav_acc)
-            W5(p, F_CONS, i, grav_kick64(C5(p, F_CONS, i), C(p, F_DT, i), grav_acceleration(p, C3(p, F_LOC, i))));
+        if (p.grav_acc) W5(p, F_CONS, i, grav_kick64(C5(p, F_CONS, i), C(p, F_DT, i), cell_acceleration(p, i)));
     }
 }
 __device__ __forceinline__ void end_instance(const KP& p, int k);
@@ -1554,6 +1629,9 @@ void launch_gradients(const KP& p, int do_timestep, cudaStream_t s) {
 }
 void launch_timesteps(const KP& p, double* dt_out, cudaStream_t s) {
     if (p.n > 0) k_timesteps<<<grid(p.n, p.blk_cell), p.blk_cell, 0, s>>>(p, dt_out);
+}
+void launch_self_gravity(const KP& p, int kick, int do_c2p, cudaStream_t s) {
+    if (p.n > 0) k_self_gravity<<<(p.n + kGravTile - 1) / kGravTile, kGravTile, 0, s>>>(p, kick, do_c2p);
 }
 void launch_gravity(const KP& p, int what, double* out, cudaStream_t s) {
     if (p.n > 0) k_gravity<<<grid(p.n, p.blk_cell), p.blk_cell, 0, s>>>(p, what, out);

@@ -1133,8 +1133,34 @@ static double gravity_timestep(const orc_ctx *c, const particle *pt) {
             return INFINITY;
     }
 }
-/* ExternalPotentialGravity::compute_accelerations (gravity.rs:67-70, 81-86) */
+/* SelfGravity::compute_accelerations (gravity.rs:22-43): particle i sums the
+   pull of the particles after it only (j > i), in index order, with the
+   softening added to the distance; every particle's a_grav is replaced. */
+static void self_gravity_accelerations(orc_ctx *c) {
+    const double eps = c->p.gravity_softening;
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t i = 0; i < c->n; i++) {
+        const vec3 li = c->parts[i].loc;
+        vec3 a = v3(0., 0., 0.);
+        for (int64_t j = i + 1; j < c->n; j++) {
+            const particle *pj = &c->parts[j];
+            double r = vlen(vsub(pj->loc, li)) + eps;
+            vec3 dir = vsub(pj->loc, li);
+            vec3 m = vscale(pj->cons.q[0], dir); /* mass * dir */
+            double r3 = r * r * r;
+            a = vadd(a, v3(m.x / r3, m.y / r3, m.z / r3));
+        }
+        c->parts[i].a_grav = a;
+    }
+}
+
+/* GravitySolver::compute_accelerations: SelfGravity, or
+   ExternalPotentialGravity (gravity.rs:67-70, 81-86) */
 static void gravity_accelerations(orc_ctx *c) {
+    if (c->p.gravity == ORC_GRAVITY_SELF) {
+        self_gravity_accelerations(c);
+        return;
+    }
     if (c->p.gravity != ORC_GRAVITY_CONSTANT && c->p.gravity != ORC_GRAVITY_KEPLERIAN) return;
 #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < c->n; i++) {

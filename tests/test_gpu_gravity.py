@@ -4,11 +4,11 @@ The reference's runners take the gravity solver's timestep per cell where it
 is smaller (runner/hydrodynamics/optimal_order.rs:47-50) but never compute
 accelerations ("TODO: gravity", :33), so a_grav stays zero and the kicks add
 nothing: with the Keplerian potential the timestep limit is the whole effect.
-With gravity_accelerations set, the external potential's accelerations
-(Potential::Constant, KeplerianPotential::acceleration) are computed at that
-point and kick2 / kick1 apply them (Particle::grav_kick, part.rs:303-312).
-Plain FP64 form within 1e-12 of the oracle; the GravitySolver entry points
-within 1e-14.
+With gravity_accelerations set, the accelerations (Potential::Constant,
+KeplerianPotential::acceleration, or SelfGravity's direct sum over j > i) are
+computed at that point and kick2 / kick1 apply them (Particle::grav_kick,
+part.rs:303-312).  Plain FP64 form within 1e-12 of the oracle; the
+GravitySolver entry points within 1e-14, self-gravity's bit for bit.
 """
 import numpy as np
 import pytest
@@ -44,6 +44,8 @@ CASES = {
     # a point mass below the box: accelerations of order one
     "keplerian_kicks": dict(gravity=ics.GRAVITY_KEPLERIAN, gravity_softening=0.05, gravity_position=(0.5, -1.0, 0.5),
                             gravity_accelerations=True),
+    # the direct sum over the cells after each one: its accelerations kick and limit the timestep
+    "self_kicks": dict(gravity=ics.GRAVITY_SELF, gravity_softening=0.02, gravity_accelerations=True),
 }
 
 
@@ -75,10 +77,14 @@ def test_keplerian_timestep_limits_the_step(gpu_lib):
         assert np.array_equal(np.ascontiguousarray(v).view(np.uint8), np.ascontiguousarray(b.arrays[k]).view(np.uint8))
 
 
-@pytest.mark.parametrize("case", ["keplerian_timestep", "constant_kicks", "keplerian_kicks"])
+@pytest.mark.parametrize("case", ["keplerian_timestep", "constant_kicks", "keplerian_kicks", "self_kicks"])
 def test_gravity_solver_entry_points(gpu_lib, case):
     p = _gas_2d(**CASES[case])
     orc, gpu = O.OracleSim(p), G.GpuSim(p)
+    if case == "self_kicks":  # a stepped state: updated masses, and a_grav set by the last step
+        for _ in range(3):
+            orc.step()
+            gpu.step()
     tg, to = gpu.gravity_timesteps(), orc.gravity_timesteps()
     fin = np.isfinite(to)
     assert np.array_equal(np.isfinite(tg), fin)
@@ -90,17 +96,110 @@ def test_gravity_solver_entry_points(gpu_lib, case):
     assert np.array_equal(np.isfinite(ag), ok)
     for a in range(3):
         assert rel_err(ag[a][ok[a]], ao[a][ok[a]]) <= 1e-14, a
+    if case == "self_kicks":
+        # the same sums in the same order with IEEE division and square root
+        assert np.array_equal(ag, ao)
+        assert np.array_equal(gpu.gravity_timesteps(), orc.gravity_timesteps())
+
+
+def test_self_gravity_hierarchical(gpu_lib):
+    """The shear layer 16^2 on hierarchical time bins with self-gravity kicks:
+    the self-gravity timestep sqrt(softening / |a|) spreads the cells over
+    about ten bins; every cell's acceleration is summed each step (as
+    compute_accelerations sets every a_grav), the active ones kick."""
+    p = ics.kelvin_helmholtz_2d(16, riemann=ics.HLLC)
+    p.params.sync_all = False
+    p.params.gravity, p.params.gravity_softening, p.params.gravity_accelerations = ics.GRAVITY_SELF, 0.01, True
+    orc, gpu = O.OracleSim(p), G.GpuSim(p)
+    bins = set()
+    for _ in range(30):
+        orc.step()
+        gpu.step()
+        assert gpu.ti_current == orc.ti_current
+        bins.update(np.unique(orc.state().timebin).tolist())
+    assert len(bins) >= 5, bins
+    assert gpu.active_faces == orc.active_faces
+    a, b = gpu.state(), orc.state()
+    assert np.array_equal(a.timebin, b.timebin)
+    errs = compare_cells(a, b, fields=("cons", "prim", "facc", "dt", "grad"))
+    assert max(errs.values()) <= 1e-10, errs
+    assert gpu.error_bits() == orc.error() == 0
+
+
+def test_self_gravity_flags_as_the_oracle(gpu_lib):
+    """grav_kick is not positivity preserving: it takes (dt/2)^2 |a|^2 m / 2 of
+    internal energy, and the cold background of the point blast goes negative.
+    Both sides flag the negative pressure (MVMM_ERR_NEG_PRIM) at the same step."""
+    p = ics.point_blast_3d(6, riemann=ics.HLLC, sync_all=False, t_end=0.05)
+    p.params.gravity, p.params.gravity_softening, p.params.gravity_accelerations = ics.GRAVITY_SELF, 0.05, True
+    orc, gpu = O.OracleSim(p), G.GpuSim(p)
+    for k in range(25):
+        orc.step()
+        try:
+            gpu.step()
+        except G.MvmmError as e:
+            assert e.code == -3 and e.bits == orc.error() == 0x20, (k, e.bits, orc.error())
+            return
+        assert orc.error() == 0, k
+    raise AssertionError("no step flagged")
+
+
+def test_self_gravity_batch(gpu_lib):
+    """Batched 1D problems with self-gravity kicks: each simulation sums over its
+    own cells only, so it is the same alone and in the batch, bit for bit, and
+    matches the oracle."""
+    probs = ics.riemann_batch_1d(3, seed=5, n_min=50, n_max=120, riemann=ics.HLLC, t_end=0.01)
+    for q in probs:  # the softening keeps the kicks within what the cold states take (no flags)
+        q.params.gravity, q.params.gravity_softening, q.params.gravity_accelerations = ics.GRAVITY_SELF, 0.1, True
+    packed, off, te = ics.pack(probs)
+    sim = G.GpuSim(packed, cell_offsets=off, t_end=te)
+    sim.run(max_steps=40)
+    parts = ics.unpack_cells(sim.state(), off)
+    st = sim.batch_state()
+    for k, q in enumerate(probs):
+        alone, orc = G.GpuSim(q), O.OracleSim(q)
+        for _ in range(int(st["steps"][k])):
+            alone.step()
+            orc.step()
+        a = alone.state()
+        for f in ("cons", "prim", "grad", "dt"):
+            assert np.array_equal(parts[k].arrays[f], a.arrays[f]), (k, f)
+        errs = compare_cells(a, orc.state(), fields=("cons", "prim", "dt"))
+        assert max(errs.values()) <= 1e-12, (k, errs)
+
+
+def test_self_gravity_fp32_face_form(gpu_lib):
+    """The FP32-face form with self-gravity kicks (kick2 and the FP32 copies of
+    the primitives after the FP64 accumulation) stays close to the FP64
+    oracle."""
+    p = _gas_2d(**CASES["self_kicks"])
+    orc, gpu = O.OracleSim(p), G.GpuSim(p, precision=1)
+    for _ in range(10):
+        orc.step()
+        gpu.step()
+    a, b = gpu.state(), orc.state()
+    l1 = np.abs(a.prim[0] - b.prim[0]).sum() / np.abs(b.prim[0]).sum()
+    assert l1 <= 1e-5, l1
+
+
+def test_self_gravity_stage_apply_fluxes(gpu_lib):
+    """FiniteVolumeSolver::apply_fluxes per stage with self-gravity kicks:
+    accelerations from the updated masses, then kick2 of the active cells."""
+    p = _gas_2d(**CASES["self_kicks"])
+    orc = O.OracleSim(p)
+    for _ in range(2):
+        orc.step()
+    p2 = ics.Problem(p.name, p.params, p.mesh, orc.state())
+    gpu, o2 = G.GpuSim(p2), O.OracleSim(p2)
+    active = (np.random.default_rng(3).random(p.mesh.n_cells) < 0.6).astype(np.uint8)
+    fo, _ = o2.compute_fluxes(active)
+    gpu.apply_fluxes(fo, active)
+    o2.apply_fluxes(fo, active)
+    assert max(compare_cells(gpu.state(), o2.state(), fields=("cons", "facc")).values()) <= 1e-14
+    assert np.array_equal(gpu.gravity_accelerations(), o2.gravity_accelerations())
 
 
 def test_gravity_rejections(gpu_lib):
-    p = _gas_2d(gravity=ics.GRAVITY_SELF, gravity_softening=0.01, gravity_accelerations=True)
-    with pytest.raises(G.MvmmError) as e:
-        G.GpuSim(p)
-    assert e.value.code == -5  # MVMM_E_UNSUPPORTED
-    p = _gas_2d(**CASES["self_timestep"])
-    with pytest.raises(G.MvmmError) as e:
-        G.GpuSim(p).gravity_accelerations()
-    assert e.value.code == -5
     p = _gas_2d(**CASES["constant_kicks"])
     sim = G.GpuSim(p)
     with pytest.raises(G.MvmmError) as e:
