@@ -54,8 +54,8 @@ class Params:
     isothermal_internal_energy: float = 0.0   # the Isothermal payload
     # gravity solver (bin/main.rs:643-662): GRAVITY_* kind, softening_length,
     # Potential::Constant acceleration, KeplerianPotential position, and whether
-    # the external potential's accelerations are computed at the runner's
-    # "TODO: gravity" point (the reference never computes them)
+    # the accelerations (external potential or self-gravity) are computed at the
+    # runner's "TODO: gravity" point (the reference never computes them)
     gravity: int = 0
     gravity_softening: float = 0.0
     gravity_acceleration: tuple = (0.0, 0.0, 0.0)

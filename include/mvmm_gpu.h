@@ -100,15 +100,16 @@ typedef struct mvmm_params {
      * its timestep per cell where smaller (optimal_order.rs:47-50,
      * godunov.rs:41-44).  They never compute accelerations (the "TODO: gravity"
      * at optimal_order.rs:33), so a_grav stays zero and the kicks kick2 / kick1
-     * add nothing; gravity_accelerations = 1 computes the external potential's
-     * accelerations at that point instead, and the kicks apply them
+     * add nothing; gravity_accelerations = 1 computes the accelerations at
+     * that point instead (the external potential's, or self-gravity's direct
+     * sum over j > i, gravity.rs:22-43), and the kicks apply them
      * (Particle::grav_kick, part.rs:303-312). */
     int gravity;                     /* MVMM_GRAVITY_* */
     double gravity_softening;        /* SelfGravity / KeplerianPotential softening_length */
     double gravity_acceleration[3];  /* Potential::Constant acceleration */
     double gravity_position[3];      /* KeplerianPotential position */
-    int gravity_accelerations;       /* 0: as the reference; 1: external potentials kick (not for
-                                        MVMM_GRAVITY_SELF, nor through mvmm_step_cells) */
+    int gravity_accelerations;       /* 0: as the reference; 1: the accelerations kick (not
+                                        through mvmm_step_cells) */
     /* The cell-wise limiter's extrapolation to a face.  0 (the reference,
      * runner/hydrodynamics.rs:119): face centroid - centroid - shift for the
      * left cell, + shift for the right one.  flux_exchange puts the face
@@ -191,9 +192,10 @@ int mvmm_compute_timesteps(mvmm_ctx *ctx, const uint8_t *active, double *dt_out)
  * 90-95, 119-123): dt_out host double[n]; INFINITY where the solver sets no
  * limit (self-gravity with zero accelerations, a constant potential). */
 int mvmm_gravity_timesteps(mvmm_ctx *ctx, double *dt_out);
-/* compute_accelerations(&self, particles) of ExternalPotentialGravity
- * (gravity.rs:67-70, 81-86, 110-136): a_out host double[3][n].  Self-gravity
- * returns MVMM_E_UNSUPPORTED. */
+/* compute_accelerations(&self, particles) (gravity.rs:22-43, 67-70, 81-86,
+ * 110-136): a_out host double[3][n].  Self-gravity sums over the current
+ * masses and positions and, as the reference's &mut form does, replaces the
+ * stored a_grav the self-gravity timestep and kicks read. */
 int mvmm_gravity_accelerations(mvmm_ctx *ctx, double *a_out);
 
 /* ---- runner free functions (runner/hydrodynamics.rs) ----------------- */
