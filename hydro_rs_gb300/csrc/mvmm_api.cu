@@ -473,8 +473,6 @@ static int create_impl(const mvmm_params* prm, const mvmm_mesh* m, int64_t n_ins
     if (prm->particle_motion < MVMM_MOTION_FIXED || prm->particle_motion > MVMM_MOTION_FLUID)
         return fail(MVMM_E_INVALID, "unknown particle motion");
     if (prm->particle_motion != MVMM_MOTION_FIXED) {
-        if (prm->boundary != MVMM_BOUNDARY_PERIODIC)
-            return fail(MVMM_E_UNSUPPORTED, "moving meshes need a periodic box (walls reflect or remove generators)");
         if (n_inst > 1) return fail(MVMM_E_UNSUPPORTED, "moving meshes are stepped one simulation at a time");
         for (int a = 0; a < prm->dimensionality; a++)
             if (!(prm->box_size[a] > 0.)) return fail(MVMM_E_INVALID, "moving meshes need box_size > 0");
@@ -581,6 +579,10 @@ static int create_impl(const mvmm_params* prm, const mvmm_mesh* m, int64_t n_ins
 #undef ALLOC
     if (cudaMallocHost((void**)&c->tl_host, sizeof(DevTimeline) * c->n_inst) != cudaSuccess)
         return cleanup(MVMM_E_NOMEM, "cudaMallocHost failed");
+    if (prm->gravity == MVMM_GRAVITY_SELF) {
+        cudaError_t e = setup_self_gravity();
+        if (e != cudaSuccess) return cleanup(MVMM_E_CUDA, std::string("self-gravity kernel: ") + cudaGetErrorString(e));
+    }
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
         return cleanup(MVMM_E_CUDA, "cudaStreamCreate failed");
     c->own_stream = true;

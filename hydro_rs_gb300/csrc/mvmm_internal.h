@@ -203,6 +203,8 @@ void launch_c2p(const KP& p, cudaStream_t s);
 void launch_gradients(const KP& p, int do_timestep, cudaStream_t s);
 void launch_timesteps(const KP& p, double* dt_out, cudaStream_t s);
 void launch_gravity(const KP& p, int what, double* out, cudaStream_t s);
+// k_self_gravity's shared memory (over the default 48 KB); once per process, before a launch
+cudaError_t setup_self_gravity();
 void launch_self_gravity(const KP& p, int kick, int do_c2p, cudaStream_t s);
 void launch_limit(const KP& p, cudaStream_t s);
 void launch_compact(const KP& p, cudaStream_t s);

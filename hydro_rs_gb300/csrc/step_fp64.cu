@@ -1268,50 +1268,97 @@ __global__ void __launch_bounds__(kMaxBlock) k_gravity(KP p, int what, double* o
 // order, the pull of the cells after it in its simulation (j > i only, as the
 // reference does):
 //     r = |x_j - x_i| + softening,   a_i += (m_j (x_j - x_i)) / (r r r),
-// with m_j the conserved mass after this step's update.  The block stages the
-// positions and masses of kGravTile cells at a time in shared memory; every
-// thread reads the same entry (a broadcast), so the sum is FP64-pipe bound.
-// Blocks over the first cells have the longest sums and start first.
+// with m_j the conserved mass after this step's update.  Each a_i is a
+// sequential sum, so its rounding fixes the order of the additions; the terms
+// are independent.  A block takes a row group of kGravRows cells (one per
+// lane) and walks the cells after it in rounds of kGravRound: the round's
+// positions and masses are staged in shared memory, each warp forms the terms
+// of its 32 of them for the whole row group, and then three warps add the
+// round's terms, one component each, in index order.  So the four warps share
+// the FP64 work of the longest rows, which would otherwise run on one
+// scheduler, and blocks over the first cells (the longest sums) start first.
+// Where a displacement component is zero (every pair of a 2D or 1D problem)
+// its term is +0, which leaves the sum as it is (a sum that starts at +0 is
+// never -0), so the component's division and addition are skipped; r^2 skips
+// its +0 square the same way.
 // kick: then kick2 and cons->prim (do_c2p) of the active cells, which the
 // update left to this kernel.
-constexpr int kGravTile = 128;
-__global__ void __launch_bounds__(kGravTile) k_self_gravity(KP p, int kick, int do_c2p) {
-    __shared__ double s_x[kGravTile], s_y[kGravTile], s_z[kGravTile], s_m[kGravTile];
-    __shared__ int s_end;
-    const int i0 = blockIdx.x * kGravTile, i = i0 + threadIdx.x;
+constexpr int kGravRows = 32, kGravWarps = 4, kGravRound = 32 * kGravWarps;
+struct GravSmem {
+    double x[kGravRound], y[kGravRound], z[kGravRound], m[kGravRound];
+    double t[3][kGravRound][kGravRows];  // the round's terms, [component][j][row]
+    double acc[3][kGravRows];
+    int end;      // the row group's last j + 1
+    int any[3];   // components with a term other than +0 in this round
+};
+__global__ void __launch_bounds__(kGravRound) k_self_gravity(KP p, int kick, int do_c2p) {
+    extern __shared__ __align__(16) unsigned char grav_smem[];
+    GravSmem& S = *reinterpret_cast<GravSmem*>(grav_smem);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int i0 = blockIdx.x * kGravRows, i = i0 + lane;
     const bool own = i < p.n;
     const int k = own ? inst_of(p, i) : 0;
     const int jend = own ? (p.inst_end ? p.inst_end[k] : p.n) : 0;
-    if (threadIdx.x == 0) s_end = 0;
+    if (threadIdx.x == 0) S.end = 0;
     __syncthreads();
-    if (own) atomicMax(&s_end, jend);
+    if (w == 0 && own) atomicMax(&S.end, jend);
     __syncthreads();
-    const int block_end = s_end;
+    const int block_end = S.end;
     const V3<double> xi = own ? C3(p, F_LOC, i) : v3(0., 0., 0.);
     const double eps = p.grav_soft;
-    double ax = 0., ay = 0., az = 0.;
-    for (int j0 = i0; j0 < block_end; j0 += kGravTile) {
-        const int j = j0 + threadIdx.x;
-        __syncthreads();  // the previous tile is consumed
-        if (j < p.n) {
-            s_x[threadIdx.x] = C(p, F_LOC, j);
-            s_y[threadIdx.x] = C(p, F_LOC + 1, j);
-            s_z[threadIdx.x] = C(p, F_LOC + 2, j);
-            s_m[threadIdx.x] = C(p, F_CONS, j);
+    double acc = 0.;  // warps 0-2: component w of a_i
+    for (int jr = i0 + 1; jr < block_end; jr += kGravRound) {
+        const int jt = jr + threadIdx.x;
+        if (jt < p.n) {
+            S.x[threadIdx.x] = C(p, F_LOC, jt);
+            S.y[threadIdx.x] = C(p, F_LOC + 1, jt);
+            S.z[threadIdx.x] = C(p, F_LOC + 2, jt);
+            S.m[threadIdx.x] = C(p, F_CONS, jt);
         }
+        if (threadIdx.x < 3) S.any[threadIdx.x] = threadIdx.x == 0;
         __syncthreads();
-        const int lo = max(i + 1 - j0, 0), hi = min(jend - j0, kGravTile);
-#pragma unroll 4
-        for (int t = lo; t < hi; t++) {
-            const double dx = s_x[t] - xi.x, dy = s_y[t] - xi.y, dz = s_z[t] - xi.z;
-            const double r = sqrt(dx * dx + dy * dy + dz * dz) + eps;  // (x_j - x_i).length() + softening
-            const double m = s_m[t], r3 = r * r * r;
-            ax = ax + (m * dx) / r3;
-            ay = ay + (m * dy) / r3;
-            az = az + (m * dz) / r3;
+        bool any_y = false, any_z = false;
+        for (int u = 0; u < 32; u++) {
+            const int t = 32 * w + u, j = jr + t;
+            double tx = 0., ty = 0., tz = 0.;
+            if (j > i && j < jend) {
+                const double dx = S.x[t] - xi.x, dy = S.y[t] - xi.y, dz = S.z[t] - xi.z;
+                // the tests on the integer pipe (cmp64): FP64 comparisons take FP64-pipe issue slots
+                const bool ny = cmp64::ne(dy, 0.), nz = cmp64::ne(dz, 0.);
+                double r2 = dx * dx;
+                if (ny) r2 = r2 + dy * dy;
+                if (nz) r2 = r2 + dz * dz;
+                const double r = sqrt(r2) + eps;  // (x_j - x_i).length() + softening
+                const double m = S.m[t], r3 = r * r * r;
+                // m * 0 / r3 is a zero for a finite m and r3 > 0
+                const bool zero_ok = (cmp64::bits(m) & cmp64::kMag) < cmp64::kInf && cmp64::gt(r3, 0.);
+                tx = (m * dx) / r3;
+                if (ny || !zero_ok) {
+                    ty = (m * dy) / r3;
+                    any_y = true;
+                }
+                if (nz || !zero_ok) {
+                    tz = (m * dz) / r3;
+                    any_z = true;
+                }
+            }
+            S.t[0][t][lane] = tx;
+            S.t[1][t][lane] = ty;
+            S.t[2][t][lane] = tz;
         }
+        if (any_y) S.any[1] = 1;
+        if (any_z) S.any[2] = 1;
+        __syncthreads();
+        if (w < 3 && S.any[w]) {
+            const int t0 = max(i + 1 - jr, 0), t1 = min(jend - jr, kGravRound);
+            for (int t = t0; t < t1; t++) acc = acc + S.t[w][t][lane];
+        }
+        __syncthreads();  // the round's rows are consumed
     }
-    if (!own) return;
+    if (w < 3) S.acc[w][lane] = acc;
+    __syncthreads();
+    if (w != 0 || !own) return;
+    const double ax = S.acc[0][lane], ay = S.acc[1][lane], az = S.acc[2][lane];
     p.agrav[i] = ax;
     p.agrav[p.n + i] = ay;
     p.agrav[2 * p.n + i] = az;
@@ -1452,9 +1499,42 @@ __device__ __forceinline__ void end_instance(const KP& p, int k) {
     tl->n_alist = 0;
 }
 
-// Space::drift (space.rs:833-854) with Particle::drift (part.rs:107-119) and,
-// for a generator that left the periodic box, Particle::box_wrap (part.rs:449-455,
-// utils.rs:23-32).
+// Particle::reflect_quantities and reflect_gradients (part.rs:385-428) about
+// the unit normal n, the reference's steps as they are: State::reflect of the
+// primitive velocity (physical_quantities.rs:239-242); the density gradient
+// reflected, the pressure gradient with the density gradient's reflected
+// normal component; the velocity gradients first take the velocity's sign
+// change, then are reflected themselves.  Gradient rows: F_GRAD + 3 q + axis.
+__device__ void reflect_cell(const KP& p, int i, const V3<double> n) {
+    V3<double> vel = C3(p, F_PRIM + 1, i);
+    vel = vel - (2. * dot(vel, n)) * n;
+    W(p, F_PRIM + 1, i, vel.x);
+    W(p, F_PRIM + 2, i, vel.y);
+    W(p, F_PRIM + 3, i, vel.z);
+    V3<double> g[5];
+#pragma unroll
+    for (int q = 0; q < 5; q++) g[q] = C3(p, F_GRAD + 3 * q, i);
+    g[0] = g[0] - (2. * dot(g[0], n)) * n;
+    g[4] = g[4] - (2. * dot(g[0], n)) * n;
+    const V3<double> twice = 2. * v3(dot(v3(g[1].x, g[2].x, g[3].x), n), dot(v3(g[1].y, g[2].y, g[3].y), n),
+                                     dot(v3(g[1].z, g[2].z, g[3].z), n));
+    g[1] = g[1] - n.x * twice;
+    g[2] = g[2] - n.y * twice;
+    g[3] = g[3] - n.z * twice;
+#pragma unroll
+    for (int q = 1; q <= 3; q++) g[q] = g[q] - (2. * dot(g[q], n)) * n;
+#pragma unroll
+    for (int q = 0; q < 5; q++) {
+        W(p, F_GRAD + 3 * q, i, g[q].x);
+        W(p, F_GRAD + 3 * q + 1, i, g[q].y);
+        W(p, F_GRAD + 3 * q + 2, i, g[q].z);
+    }
+}
+
+// Space::drift (space.rs:833-854) with Particle::drift (part.rs:107-119): every
+// generator by v dt; outside the box it is wrapped (Particle::box_wrap,
+// part.rs:449-455, utils.rs:23-32) or reflected (reflective walls); in an open
+// or vacuum box it stays where it drifted and the host removes it.
 __global__ void __launch_bounds__(kMaxBlock) k_drift(KP p, double dt) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
@@ -1477,7 +1557,23 @@ __global__ void __launch_bounds__(kMaxBlock) k_drift(KP p, double dt) {
     } else {
         bool inside = true;
         for (int a = 0; a < p.dim; a++) inside = inside && loc[a] >= 0. && loc[a] < p.box[a];
-        if (!inside) {
+        if (!inside && p.boundary == MVMM_BOUNDARY_REFLECTIVE) {
+            // Particle::box_reflect (part.rs:457-469), utils.rs box_reflect (:34-43):
+            // mirrored into the box; loc alone moves
+            const V3<double> old = v3(loc[0], loc[1], loc[2]);
+            for (int a = 0; a < p.dim; a++) {
+                if (loc[a] < 0.) loc[a] -= 2. * loc[a];
+                if (loc[a] > p.box[a]) loc[a] -= 2. * (loc[a] - p.box[a]);
+            }
+            bool back = true;  // assert!(contains(..)) after the reflection
+            for (int a = 0; a < p.dim; a++) back = back && loc[a] >= 0. && loc[a] < p.box[a];
+            if (!back) set_err(p, k, 1u << 4);
+            const V3<double> shift = v3(loc[0], loc[1], loc[2]) - old;
+            if (len2(shift) > 0.) {
+                reflect_cell(p, i, (1. / len(shift)) * shift);  // shift * shift.length_recip()
+                p.fresh[i] = 0;  // prim and grad changed: the derived face-stage rows are stale
+            }
+        } else if (!inside && p.boundary == MVMM_BOUNDARY_PERIODIC) {
             double old[3] = {loc[0], loc[1], loc[2]};
             for (int a = 0; a < p.dim; a++) {
                 // one box length per pass, as the reference's loops (bounded: a
@@ -1630,8 +1726,12 @@ void launch_gradients(const KP& p, int do_timestep, cudaStream_t s) {
 void launch_timesteps(const KP& p, double* dt_out, cudaStream_t s) {
     if (p.n > 0) k_timesteps<<<grid(p.n, p.blk_cell), p.blk_cell, 0, s>>>(p, dt_out);
 }
+cudaError_t setup_self_gravity() {
+    return cudaFuncSetAttribute(k_self_gravity, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(GravSmem));
+}
 void launch_self_gravity(const KP& p, int kick, int do_c2p, cudaStream_t s) {
-    if (p.n > 0) k_self_gravity<<<(p.n + kGravTile - 1) / kGravTile, kGravTile, 0, s>>>(p, kick, do_c2p);
+    if (p.n > 0)
+        k_self_gravity<<<(p.n + kGravRows - 1) / kGravRows, kGravRound, sizeof(GravSmem), s>>>(p, kick, do_c2p);
 }
 void launch_gravity(const KP& p, int what, double* out, cudaStream_t s) {
     if (p.n > 0) k_gravity<<<grid(p.n, p.blk_cell), p.blk_cell, 0, s>>>(p, what, out);

@@ -181,6 +181,7 @@ class GpuSim:
         self.problem = problem
         self.mesh = problem.mesh
         prec = p.precision if precision is None else precision
+        self.precision, self.stream = prec, stream
         self._p = make_params(p, prec, problem.mesh.box)
         self._mv = self.mesh.cview()
         h = ctypes.c_void_p(0)
@@ -244,8 +245,25 @@ class GpuSim:
 
     # ---- moving meshes (host-driven: drift, rebuild the Voronoi mesh, step)
     def drift(self, dt: float):
-        """Space::drift of every generator by v*dt (periodic wrap)."""
+        """Space::drift of every generator by v*dt: wrapped in a periodic box,
+        mirrored back into a reflective one; in an open or vacuum box a
+        generator that left stays outside for the host to remove."""
         _check(load_library().mvmm_drift(self.h, float(dt)), self.h)
+
+    def rebuilt(self, keep, mesh) -> "GpuSim":
+        """A context over the cells ``keep`` (indices into this one, in order)
+        with this one's parameters, form, stream and timeline, created with
+        ``mesh`` over them: the removal of generators that left an open or
+        vacuum box (a context's cell count is fixed)."""
+        from .ics import Problem
+
+        st = self.state()
+        cells = Cells(n=len(keep), arrays={k: np.ascontiguousarray(v[..., keep]) for k, v in st.arrays.items()})
+        new = GpuSim(Problem(self.problem.name, self.problem.params, mesh, cells), precision=self.precision,
+                     stream=self.stream)
+        new.ti_current, new.ti_old, new.steps = self.ti_current, self.ti_old, self.steps
+        new.active_faces, new.finished = self.active_faces, self.finished
+        return new
 
     def positions(self) -> np.ndarray:
         loc = np.zeros((3, self.mesh.n_cells))

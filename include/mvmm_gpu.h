@@ -51,9 +51,10 @@ enum {
                                    integer timeline FP64 */
 };
 /* Particle motion: engine.rs:7-13, Particle::set_particle_velocity
- * (part.rs:328-372).  The moving modes need a periodic box: the host rebuilds
- * the Voronoi mesh from the drifted generators (mvmm_drift, mvmm_get_positions,
- * mvmm_set_mesh) before each step. */
+ * (part.rs:328-372).  For the moving modes the host rebuilds the Voronoi mesh
+ * from the drifted generators (mvmm_drift, mvmm_get_positions, mvmm_set_mesh)
+ * before each step; in an open or vacuum box it also removes the generators
+ * that left (space.rs:840-853) and creates a context over the others. */
 enum { MVMM_MOTION_FIXED = 0, MVMM_MOTION_STEER = 1, MVMM_MOTION_STEER_PAKMOR = 2, MVMM_MOTION_FLUID = 3 };
 
 /* ---- status codes / error bits --------------------------------------- */
@@ -211,9 +212,12 @@ int mvmm_gradients(mvmm_ctx *ctx, const uint8_t *active);
 int mvmm_step(mvmm_ctx *ctx, uint64_t ti_current, uint64_t ti_old, uint64_t *ti_next, int64_t *n_active_faces);
 /* ---- moving meshes ------------------------------------------------------ */
 /* Space::drift (space.rs:833-854, part.rs:107-119): every cell's generator,
- * centroid and gradients centroid move by v*dt; generators that leave the
- * periodic box are wrapped (part.rs:449-455).  Engine::run calls it between
- * sync points (engine.rs:164-176). */
+ * centroid and gradients centroid move by v*dt; generators that leave a
+ * periodic box are wrapped (part.rs:449-455), those that leave a reflective
+ * box are mirrored back with their primitive velocity and gradients reflected
+ * (Particle::box_reflect, part.rs:457-469); in an open or vacuum box they stay
+ * outside for the host to remove.  Engine::run calls it between sync points
+ * (engine.rs:164-176). */
 int mvmm_drift(mvmm_ctx *ctx, double dt);
 /* The generator positions loc [3][n] (what Space::volume_calculation feeds the
  * Voronoi builder, space.rs:236-263). */

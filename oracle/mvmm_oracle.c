@@ -1321,6 +1321,58 @@ orc_ctx *orc_create(const orc_params *p, const orc_mesh *m) {
 }
 
 /* Space::drift (space.rs:833-854), Particle::drift (part.rs:107-119), box_wrap (part.rs:449-455) */
+/* Particle::reflect_gradients (part.rs:390-428), the reference's steps as
+   they are: the pressure gradient is reflected with the density gradient's
+   already reflected normal component, and the velocity gradients first take
+   the velocity's sign change, then are reflected themselves. */
+static grads grads_reflect(grads g, vec3 n) {
+    g.g[0] = vsub(g.g[0], vscale(2. * vdot(g.g[0], n), n));
+    g.g[4] = vsub(g.g[4], vscale(2. * vdot(g.g[0], n), n));
+    const vec3 dv_dx = v3(g.g[1].x, g.g[2].x, g.g[3].x);
+    const vec3 dv_dy = v3(g.g[1].y, g.g[2].y, g.g[3].y);
+    const vec3 dv_dz = v3(g.g[1].z, g.g[2].z, g.g[3].z);
+    const vec3 twice = vscale(2., v3(vdot(dv_dx, n), vdot(dv_dy, n), vdot(dv_dz, n)));
+    g.g[1] = vsub(g.g[1], vscale(n.x, twice));
+    g.g[2] = vsub(g.g[2], vscale(n.y, twice));
+    g.g[3] = vsub(g.g[3], vscale(n.z, twice));
+    for (int q = 1; q <= 3; q++) g.g[q] = vsub(g.g[q], vscale(2. * vdot(g.g[q], n), n));
+    return g;
+}
+
+/* utils.rs contains (:15-21) */
+static int box_contains(const orc_ctx *c, vec3 pos) {
+    const double *p3[3] = {&pos.x, &pos.y, &pos.z};
+    int in = 1;
+    for (int a = 0; a < c->p.dimensionality; a++) in = in && *p3[a] >= 0. && *p3[a] < c->p.box_size[a];
+    return in;
+}
+
+/* Particle::box_reflect (part.rs:457-469) with utils.rs box_reflect
+   (:34-43): the generator is mirrored into the box; where it moved, its
+   primitive velocity and its gradients are reflected about the direction of
+   the move.  Only loc moves (centroid and gradients_centroid stay).  A
+   generator still outside (exactly on the upper face, or more than a box
+   length out) fails the reference's assert. */
+static void part_box_reflect(orc_ctx *c, particle *pt) {
+    const vec3 old = pt->loc;
+    double *loc[3] = {&pt->loc.x, &pt->loc.y, &pt->loc.z};
+    for (int a = 0; a < c->p.dimensionality; a++) {
+        if (*loc[a] < 0.) *loc[a] -= 2. * *loc[a];
+        if (*loc[a] > c->p.box_size[a]) *loc[a] -= 2. * (*loc[a] - c->p.box_size[a]);
+    }
+    if (!box_contains(c, pt->loc)) c->err |= ORC_ERR_NONFINITE;
+    const vec3 shift = vsub(pt->loc, old);
+    if (vlen2(shift) > 0.) {
+        const vec3 n = vscale(1. / vlen(shift), shift); /* shift * shift.length_recip() */
+        pt->prim = prim_reflect(pt->prim, n);
+        pt->grad = grads_reflect(pt->grad, n);
+    }
+}
+
+/* Space::drift (space.rs:833-854) of every particle.  Outside the box a
+   generator is wrapped (periodic) or reflected (reflective); in an open or
+   vacuum box it stays where it drifted and the host removes it (orc_outside
+   lists them). */
 void orc_drift(orc_ctx *c, double dt) {
     int dim = c->p.dimensionality;
     for (int64_t i = 0; i < c->n; i++) {
@@ -1338,9 +1390,12 @@ void orc_drift(orc_ctx *c, double dt) {
             c->err |= ORC_ERR_NONFINITE;
             continue;
         }
-        int inside = 1;
-        for (int a = 0; a < dim; a++) inside = inside && *loc[a] >= 0. && *loc[a] < c->p.box_size[a];
-        if (inside) continue;
+        if (box_contains(c, pt->loc)) continue;
+        if (c->p.boundary == ORC_REFLECTIVE) {
+            part_box_reflect(c, pt);
+            continue;
+        }
+        if (c->p.boundary != ORC_PERIODIC) continue; /* removed by the host */
         vec3 old = pt->loc;
         for (int a = 0; a < dim; a++) {
             while (*loc[a] < 0.) *loc[a] += c->p.box_size[a];

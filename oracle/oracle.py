@@ -96,6 +96,7 @@ class OracleSim:
     def __init__(self, problem, n_threads: int = 0):
         p = problem.params
         self.problem = problem
+        self.n_threads = n_threads
         self.mesh = problem.mesh
         self.cells = problem.cells.copy()
         thr, adv = p.solver_extras()
@@ -157,6 +158,20 @@ class OracleSim:
 
     def positions(self) -> np.ndarray:
         return self.state().loc.copy()
+
+    def rebuilt(self, keep, mesh) -> "OracleSim":
+        """An oracle over the particles ``keep`` with this one's parameters and
+        timeline, on ``mesh`` (the removal of generators that left an open or
+        vacuum box)."""
+        from hydro_rs_gb300.ics import Problem
+        from hydro_rs_gb300.layout import Cells
+
+        st = self.state()
+        cells = Cells(n=len(keep), arrays={k: np.ascontiguousarray(v[..., keep]) for k, v in st.arrays.items()})
+        new = OracleSim(Problem(self.problem.name, self.problem.params, mesh, cells), n_threads=self.n_threads)
+        new.ti_current, new.ti_old, new.steps, new.active_faces = (self.ti_current, self.ti_old, self.steps,
+                                                                   self.active_faces)
+        return new
 
     def set_mesh(self, mesh):
         self._mv = mesh.cview()

@@ -44,9 +44,9 @@ def test_invalid_params_rejected_on_host(lib):
     rc = lib.mvmm_ctx_create(ctypes.byref(prm), ctypes.byref(mv), ctypes.byref(h))
     assert rc == -1 and h.value is None
     assert b"gamma" in lib.mvmm_last_error()
-    prm = G._Params(5 / 3, 0, 0.0, 0.3, 0, 1, 1, 1, 0.2, 1000, 0, 1)  # moving mesh
+    prm = G._Params(5 / 3, 0, 0.0, 0.3, 0, 1, 1, 1, 0.2, 1000, 0, 1)  # moving mesh without a box size
     rc = lib.mvmm_ctx_create(ctypes.byref(prm), ctypes.byref(mv), ctypes.byref(h))
-    assert rc == -5
+    assert rc == -1 and b"box_size" in lib.mvmm_last_error()
 
 
 def test_bad_mesh_rejected_on_host(lib):

@@ -94,3 +94,93 @@ def test_oracle_galilean_invariance_first_cycle():
     grad = d.pop("grad")
     assert a.ti_current == b.ti_current and max(d.values()) <= 1e-10, d
     assert max(d.values()) < 1e-13 < grad  # states agree to rounding, the limited gradients do not
+
+
+def test_removal_keep_restates_the_index_shift():
+    """space.rs:851-853 removes the collected indices one by one from the
+    particle vector: after the first removal each later index names the
+    particle after the intended one, and an index past the end panics."""
+    from hydro_rs_gb300.moving import RemovalError, removal_keep
+
+    assert removal_keep(10, [3]).tolist() == [0, 1, 2, 4, 5, 6, 7, 8, 9]
+    assert removal_keep(10, [3, 7]).tolist() == [0, 1, 2, 4, 5, 6, 7, 9]
+    with pytest.raises(RemovalError):
+        removal_keep(10, [8, 9])
+
+
+def _reflect_ref(s, dt, box=(1.0, 1.0)):
+    """Space::drift of a reflective box in numpy, the reference's steps
+    (part.rs:107-119, 385-428, 457-469; utils.rs:34-43;
+    physical_quantities.rs:239-242): loc, prim and grad after the drift."""
+    loc = s.loc.copy()
+    for a in range(2):
+        loc[a] = loc[a] + s.v[a] * dt
+    prim, grad = s.prim.copy(), s.grad.copy()
+    for i in range(loc.shape[1]):
+        x = loc[:, i].copy()
+        if all(0.0 <= x[a] < box[a] for a in range(2)):
+            continue
+        old = x.copy()
+        for a in range(2):
+            if x[a] < 0.0:
+                x[a] -= 2.0 * x[a]
+            if x[a] > box[a]:
+                x[a] -= 2.0 * (x[a] - box[a])
+        loc[:, i] = x
+        sh = x - old
+        l2 = sh[0] * sh[0] + sh[1] * sh[1] + sh[2] * sh[2]
+        if not l2 > 0.0:
+            continue
+        n = sh * (1.0 / np.sqrt(l2))
+        dot = lambda u, w: u[0] * w[0] + u[1] * w[1] + u[2] * w[2]
+        v = prim[1:4, i].copy()
+        prim[1:4, i] = v - (2.0 * dot(v, n)) * n
+        g = [grad[3 * q:3 * q + 3, i].copy() for q in range(5)]
+        g[0] = g[0] - (2.0 * dot(g[0], n)) * n
+        g[4] = g[4] - (2.0 * dot(g[0], n)) * n
+        dvn = np.array([dot(np.array([g[1][c], g[2][c], g[3][c]]), n) for c in range(3)])
+        for q, c in ((1, 0), (2, 1), (3, 2)):
+            g[q] = g[q] - (2.0 * dvn) * n[c]
+        for q in (1, 2, 3):
+            g[q] = g[q] - (2.0 * dot(g[q], n)) * n
+        for q in range(5):
+            grad[3 * q:3 * q + 3, i] = g[q]
+    return loc, prim, grad
+
+
+def test_reflective_drift_restated():
+    """A drift long enough to carry generators through the walls: the oracle's
+    Particle::box_reflect against the numpy restatement, bit for bit; only
+    loc moves (centroid and gradients_centroid are not shifted)."""
+    p = ics.wall_flow_2d(16, boundary=ics.REFLECTIVE, v=(4.0, 1.0))
+    o = O.OracleSim(p)
+    st = MovingMeshStepper(o, p.mesh)
+    st.step()
+    st.step()  # gradients and particle velocities of a stepped state
+    s0 = o.state()
+    dt = 0.02
+    o.drift(dt)
+    s1 = o.state()
+    loc, prim, grad = _reflect_ref(s0, dt)
+    moved = (s0.loc[0] + s0.v[0] * dt >= 1.0) | (s0.loc[1] + s0.v[1] * dt >= 1.0) | \
+            (s0.loc[0] + s0.v[0] * dt < 0.0) | (s0.loc[1] + s0.v[1] * dt < 0.0)
+    assert moved.sum() >= 10 and (np.abs(s0.grad[:, moved]) > 0).any()
+    assert np.array_equal(s1.loc, loc)
+    assert np.array_equal(s1.prim, prim)
+    assert np.array_equal(s1.grad, grad)
+    assert o.error() == 0
+    for a in range(2):  # centroid drifts by v dt, with no reflection
+        assert np.array_equal(s1.centroid[a], s0.centroid[a] + s0.v[a] * dt)
+
+
+@pytest.mark.parametrize("boundary", [ics.OPEN, ics.VACUUM])
+def test_open_box_removes_the_generators_that_left(boundary):
+    p = ics.wall_flow_2d(16, boundary=boundary)
+    o = O.OracleSim(p)
+    st = MovingMeshStepper(o, p.mesh)
+    for _ in range(10):
+        st.step()
+    assert st.removed == 1 and st.sim.mesh.n_cells == p.mesh.n_cells - 1
+    assert st.sim.error() == 0 and st.sim.steps == 10
+    s = st.sim.state()
+    assert (s.loc[0] >= 0).all() and (s.loc[0] < 1).all() and (s.loc[1] >= 0).all() and (s.loc[1] < 1).all()
