@@ -219,24 +219,27 @@ def kelvin_helmholtz_2d(nx: int = 256, seed: int = 2, riemann: int = EXACT, t_en
 
 
 def wall_flow_2d(nx: int = 32, boundary: int = REFLECTIVE, v=(1.5, 0.4), seed: int = 11, riemann: int = HLLC,
-                 t_end: float = 0.5, jitter: float = 0.1, cfl: float = 0.3) -> Problem:
-    """2D flow into the walls of the unit square (seeded +-jitter lattice, no
-    periodic images): density 1 + 0.3 sin(2 pi x) sin(2 pi y), pressure 1,
-    velocity v plus 0.2 sin(2 pi y) along x, generators moving with the fluid.
-    Generators next to the walls the flow heads for leave the box: a reflective
-    box mirrors them back, an open or vacuum box loses them."""
-    params = Params(gamma=5.0 / 3.0, cfl=cfl, riemann=riemann, boundary=boundary, dimensionality=2,
+                 t_end: float = 0.5, jitter: float = 0.1, cfl: float = 0.3, dim: int = 2) -> Problem:
+    """Flow into the walls of the unit square (cube for dim=3; seeded +-jitter
+    lattice of nx per side, no periodic images): density 1 + 0.3 sin(2 pi x)
+    sin(2 pi y), pressure 1, velocity v (v[2] = 0.3 v[1] in 3D) plus 0.2 sin(2 pi
+    y) along x, generators moving with the fluid.  Generators next to the walls
+    the flow heads for leave the box: a reflective box mirrors them back, an
+    open or vacuum box loses them."""
+    params = Params(gamma=5.0 / 3.0, cfl=cfl, riemann=riemann, boundary=boundary, dimensionality=dim,
                     sync_all=True, t_end=t_end, particle_motion=FLUID)
     rng = np.random.default_rng(seed)
-    x, box, vpp, _ = lattice((1.0, 1.0, 1.0), nx * nx, 2, jitter, rng)
-    mesh = mesh_voronoi(x, 2, box, False)
+    x, box, vpp, _ = lattice((1.0, 1.0, 1.0), nx ** dim, dim, jitter, rng)
+    mesh = mesh_voronoi(x, dim, box, False)
     rho = 1.0 + 0.3 * np.sin(2.0 * math.pi * x[0]) * np.sin(2.0 * math.pi * x[1])
     vel = np.zeros_like(x)
     vel[0] = v[0] + 0.2 * np.sin(2.0 * math.pi * x[1])
     vel[1] = v[1]
+    if dim == 3:
+        vel[2] = 0.3 * v[1]
     u = gas_internal_energy_from_pressure(params.gamma, np.ones(x.shape[1]), 1.0 / rho)
     cells = cells_from_ic(mesh, x, rho * mesh.volume, vel, u, params.gamma)
-    return Problem("wall_flow_2d", params, mesh, cells)
+    return Problem(f"wall_flow_{dim}d", params, mesh, cells)
 
 
 def point_blast_3d(n1d: int = 128, seed: int = 3, riemann: int = HLLC, t_end: float = 0.05,

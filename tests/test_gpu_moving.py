@@ -61,11 +61,12 @@ def test_moving_mesh_rejections(gpu_lib):
         sim.run(max_steps=2)  # a moving mesh is stepped from the host
 
 
-def test_reflective_drift_bitwise(gpu_lib):
+@pytest.mark.parametrize("dim", [2, 3])
+def test_reflective_drift_bitwise(gpu_lib, dim):
     """The device drift of a reflective box against the oracle's from the same
     state: Particle::box_reflect mirrors the generators that crossed a wall and
     reflects their primitive velocity and gradients, bit for bit."""
-    p = ics.wall_flow_2d(16, boundary=ics.REFLECTIVE, v=(4.0, 1.0))
+    p = ics.wall_flow_2d(16 if dim == 2 else 6, boundary=ics.REFLECTIVE, v=(4.0, 1.0), dim=dim)
     orc = O.OracleSim(p)
     st = MovingMeshStepper(orc, p.mesh)
     st.step()
@@ -77,8 +78,8 @@ def test_reflective_drift_bitwise(gpu_lib):
     orc.drift(dt)
     gpu.drift(dt)
     a, b = gpu.state(), orc.state()
-    crossed = (s0.loc[0] + s0.v[0] * dt >= 1.0) | (s0.loc[1] + s0.v[1] * dt >= 1.0)
-    assert crossed.sum() >= 10
+    ahead = s0.loc[:dim] + s0.v[:dim] * dt
+    assert ((ahead >= 1.0) | (ahead < 0.0)).any(axis=0).sum() >= 10
     for f in ("loc", "prim", "grad", "centroid", "gc"):
         assert np.array_equal(a.arrays[f], b.arrays[f]), f
     assert gpu.error_bits() == orc.error() == 0
@@ -120,3 +121,18 @@ def test_open_box_moving_parity(gpu_lib, boundary):
     errs = compare_cells(a, b, fields=("cons", "prim", "loc", "centroid", "volume", "v", "grad"))
     assert max(errs.values()) <= 1e-10, errs
     assert sg.sim.error_bits() == so.sim.error() == 0
+
+
+def test_open_box_fp32_face_form(gpu_lib):
+    """The FP32-face form in an open box: the same generator leaves and the
+    state stays close to the FP64 oracle."""
+    p = ics.wall_flow_2d(16, boundary=ics.OPEN)
+    orc, gpu = O.OracleSim(p), G.GpuSim(p, precision=1)
+    so, sg = MovingMeshStepper(orc, p.mesh), MovingMeshStepper(gpu, p.mesh)
+    for _ in range(10):
+        so.step()
+        sg.step()
+    assert sg.removed == so.removed == 1 and sg.sim.precision == 1
+    a, b = sg.sim.state(), so.sim.state()
+    l1 = np.abs(a.prim[0] - b.prim[0]).sum() / np.abs(b.prim[0]).sum()
+    assert l1 <= 1e-5, l1

@@ -108,20 +108,20 @@ def test_removal_keep_restates_the_index_shift():
         removal_keep(10, [8, 9])
 
 
-def _reflect_ref(s, dt, box=(1.0, 1.0)):
+def _reflect_ref(s, dt, box=(1.0, 1.0), dim=2):
     """Space::drift of a reflective box in numpy, the reference's steps
     (part.rs:107-119, 385-428, 457-469; utils.rs:34-43;
     physical_quantities.rs:239-242): loc, prim and grad after the drift."""
     loc = s.loc.copy()
-    for a in range(2):
+    for a in range(dim):
         loc[a] = loc[a] + s.v[a] * dt
     prim, grad = s.prim.copy(), s.grad.copy()
     for i in range(loc.shape[1]):
         x = loc[:, i].copy()
-        if all(0.0 <= x[a] < box[a] for a in range(2)):
+        if all(0.0 <= x[a] < box[a] for a in range(dim)):
             continue
         old = x.copy()
-        for a in range(2):
+        for a in range(dim):
             if x[a] < 0.0:
                 x[a] -= 2.0 * x[a]
             if x[a] > box[a]:
@@ -148,11 +148,12 @@ def _reflect_ref(s, dt, box=(1.0, 1.0)):
     return loc, prim, grad
 
 
-def test_reflective_drift_restated():
+@pytest.mark.parametrize("dim", [2, 3])
+def test_reflective_drift_restated(dim):
     """A drift long enough to carry generators through the walls: the oracle's
     Particle::box_reflect against the numpy restatement, bit for bit; only
     loc moves (centroid and gradients_centroid are not shifted)."""
-    p = ics.wall_flow_2d(16, boundary=ics.REFLECTIVE, v=(4.0, 1.0))
+    p = ics.wall_flow_2d(16 if dim == 2 else 6, boundary=ics.REFLECTIVE, v=(4.0, 1.0), dim=dim)
     o = O.OracleSim(p)
     st = MovingMeshStepper(o, p.mesh)
     st.step()
@@ -161,15 +162,15 @@ def test_reflective_drift_restated():
     dt = 0.02
     o.drift(dt)
     s1 = o.state()
-    loc, prim, grad = _reflect_ref(s0, dt)
-    moved = (s0.loc[0] + s0.v[0] * dt >= 1.0) | (s0.loc[1] + s0.v[1] * dt >= 1.0) | \
-            (s0.loc[0] + s0.v[0] * dt < 0.0) | (s0.loc[1] + s0.v[1] * dt < 0.0)
+    loc, prim, grad = _reflect_ref(s0, dt, box=(1.0, 1.0, 1.0), dim=dim)
+    ahead = s0.loc[:dim] + s0.v[:dim] * dt
+    moved = ((ahead >= 1.0) | (ahead < 0.0)).any(axis=0)
     assert moved.sum() >= 10 and (np.abs(s0.grad[:, moved]) > 0).any()
     assert np.array_equal(s1.loc, loc)
     assert np.array_equal(s1.prim, prim)
     assert np.array_equal(s1.grad, grad)
     assert o.error() == 0
-    for a in range(2):  # centroid drifts by v dt, with no reflection
+    for a in range(dim):  # centroid drifts by v dt, with no reflection
         assert np.array_equal(s1.centroid[a], s0.centroid[a] + s0.v[a] * dt)
 
 
