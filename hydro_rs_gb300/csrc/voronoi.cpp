@@ -141,10 +141,20 @@ void for_ring(const Grid& gr, const int b[3], int r, Fn&& fn) {
 }
 
 // ----------------------------------------------------------------- 2D ----
+// A convex polygon in fixed storage: a 2D Voronoi cell has a few dozen
+// vertices at most, and the clipping below then allocates nothing.
+constexpr int kMaxPoly2 = 128;
 struct Poly2 {
-    std::vector<P3> v;        // vertices (z unused)
-    std::vector<int64_t> lab; // label of edge v[k] -> v[k+1]
-    std::vector<int> sh;      // packed shift of that edge's neighbour
+    int n = 0;
+    P3 v[kMaxPoly2];        // vertices (z unused)
+    int64_t lab[kMaxPoly2]; // label of edge v[k] -> v[k+1]
+    int sh[kMaxPoly2];      // packed shift of that edge's neighbour
+    void push(P3 p, int64_t l, int s) {
+        v[n] = p;
+        lab[n] = l;
+        sh[n] = s;
+        n++;
+    }
 };
 
 inline int pack_shift(const int s[3]) { return (s[0] + 8) | ((s[1] + 8) << 4) | ((s[2] + 8) << 8); }
@@ -154,97 +164,108 @@ inline void unpack_shift(int p, int s[3]) {
     s[2] = ((p >> 8) & 15) - 8;
 }
 
-void clip2(Poly2& P, P3 m, P3 d, int64_t lab, int sh, double eps) {
-    size_t nv = P.v.size();
-    std::vector<double> h(nv);
+// Clips P by the half-space dot(x - m, d) <= eps into Q (Q = P if nothing is
+// cut); false when Q would exceed its storage.  Returns with *changed set
+// when the polygon changed.
+bool clip2(const Poly2& P, Poly2& Q, P3 m, P3 d, int64_t lab, int sh, double eps, bool* changed) {
+    const int nv = P.n;
+    double h[kMaxPoly2];
     bool any_out = false;
-    for (size_t k = 0; k < nv; k++) {
+    for (int k = 0; k < nv; k++) {
         h[k] = dot(P.v[k] - m, d);
         if (h[k] > eps) any_out = true;
     }
-    if (!any_out) return;
-    Poly2 Q;
-    for (size_t k = 0; k < nv; k++) {
-        size_t k1 = (k + 1) % nv;
-        P3 a = P.v[k], b = P.v[k1];
-        bool ain = h[k] <= eps, bin = h[k1] <= eps;
+    *changed = any_out;
+    if (!any_out) return true;
+    Q.n = 0;
+    for (int k = 0; k < nv; k++) {
+        if (Q.n + 2 > kMaxPoly2) return false;
+        const int k1 = k + 1 == nv ? 0 : k + 1;
+        const P3 a = P.v[k], b = P.v[k1];
+        const bool ain = h[k] <= eps, bin = h[k1] <= eps;
         if (ain) {
-            Q.v.push_back(a);
             if (bin) {
-                Q.lab.push_back(P.lab[k]);
-                Q.sh.push_back(P.sh[k]);
+                Q.push(a, P.lab[k], P.sh[k]);
+            } else if (h[k] >= -eps) {
+                // leaving with a on the plane: the new edge starts at a itself
+                Q.push(a, lab, sh);
             } else {
                 // leaving: a -> cut point keeps the old label, cut -> next entry is new
-                double t = h[k] / (h[k] - h[k1]);
-                P3 p = a + t * (b - a);
-                if (h[k] >= -eps) {
-                    // a is on the plane: the new edge starts at a itself
-                    Q.lab.push_back(lab);
-                    Q.sh.push_back(sh);
-                } else {
-                    Q.lab.push_back(P.lab[k]);
-                    Q.sh.push_back(P.sh[k]);
-                    Q.v.push_back(p);
-                    Q.lab.push_back(lab);
-                    Q.sh.push_back(sh);
-                }
+                const double t = h[k] / (h[k] - h[k1]);
+                Q.push(a, P.lab[k], P.sh[k]);
+                Q.push(a + t * (b - a), lab, sh);
             }
         } else if (bin) {
             // entering: cut point -> b keeps the old label
             if (h[k1] >= -eps) continue;  // b on the plane: b itself is the entry point
-            double t = h[k] / (h[k] - h[k1]);
-            P3 p = a + t * (b - a);
-            Q.v.push_back(p);
-            Q.lab.push_back(P.lab[k]);
-            Q.sh.push_back(P.sh[k]);
+            const double t = h[k] / (h[k] - h[k1]);
+            Q.push(a + t * (b - a), P.lab[k], P.sh[k]);
         }
     }
-    P = std::move(Q);
+    return true;
 }
 
 CellOut build_cell2(int64_t i, int64_t n, const double* g, const Grid& gr) {
     CellOut out;
     P3 gi{g[i], g[n + i], 0.0};
-    Poly2 P;
+    Poly2 buf[2];
+    Poly2* P = &buf[0];
+    Poly2* Q = &buf[1];
     double L0 = gr.box[0], L1 = gr.box[1];
+    int zero3[3] = {0, 0, 0};
+    const int sh0 = pack_shift(zero3);
     if (!gr.periodic) {
-        P.v = {{0, 0, 0}, {L0, 0, 0}, {L0, L1, 0}, {0, L1, 0}};
-        P.lab = {-3, -2, -4, -1};
+        P->push({0, 0, 0}, -3, sh0);
+        P->push({L0, 0, 0}, -2, sh0);
+        P->push({L0, L1, 0}, -4, sh0);
+        P->push({0, L1, 0}, -1, sh0);
     } else {
         double hx = 0.5 * L0, hy = 0.5 * L1;
-        P.v = {{gi.x - hx, gi.y - hy, 0}, {gi.x + hx, gi.y - hy, 0}, {gi.x + hx, gi.y + hy, 0}, {gi.x - hx, gi.y + hy, 0}};
-        P.lab = {kInvalid, kInvalid, kInvalid, kInvalid};
+        P->push({gi.x - hx, gi.y - hy, 0}, kInvalid, sh0);
+        P->push({gi.x + hx, gi.y - hy, 0}, kInvalid, sh0);
+        P->push({gi.x + hx, gi.y + hy, 0}, kInvalid, sh0);
+        P->push({gi.x - hx, gi.y + hy, 0}, kInvalid, sh0);
     }
-    int zero3[3] = {0, 0, 0};
-    P.sh.assign(4, pack_shift(zero3));
+    // the largest squared vertex distance from the generator, kept current
+    auto reach2 = [&]() {
+        double r2 = 0;
+        for (int k = 0; k < P->n; k++) r2 = std::max(r2, dot(P->v[k] - gi, P->v[k] - gi));
+        return r2;
+    };
+    double r2 = reach2();
     int b[3] = {std::min(std::max(int(std::floor(gi.x / gr.bw[0])), 0), gr.nb[0] - 1),
                 std::min(std::max(int(std::floor(gi.y / gr.bw[1])), 0), gr.nb[1] - 1), 0};
     double eps = 1e-13 * gr.minbw * gr.minbw;
     int rmax = std::max(gr.nb[0], gr.nb[1]) + 1;
     for (int r = 0; r <= rmax; r++) {
-        double r2max = 0;
-        for (auto& v : P.v) r2max = std::max(r2max, dot(v - gi, v - gi));
         double reach = (r - 1) * gr.minbw;
-        if (r >= 1 && reach > 0 && reach * reach >= 4.0 * r2max) break;
+        if (r >= 1 && reach > 0 && reach * reach >= 4.0 * r2) break;
         for_ring(gr, b, r, [&](int32_t j, const int s[3]) {
             if (j == i && s[0] == 0 && s[1] == 0) return;
             P3 gj{g[j] + s[0] * L0, g[n + j] + s[1] * L1, 0.0};
             P3 d = gj - gi;
             double dd = dot(d, d);
-            double r2 = 0;
-            for (auto& v : P.v) r2 = std::max(r2, dot(v - gi, v - gi));
             if (dd >= 4.0 * r2) return;
             if (j == i) { out.error = 2; return; }
             P3 m = 0.5 * (gi + gj);
-            clip2(P, m, d, j, pack_shift(s), eps * std::sqrt(dd));
+            bool changed = false;
+            if (!clip2(*P, *Q, m, d, j, pack_shift(s), eps * std::sqrt(dd), &changed)) {
+                out.error = 3;
+                return;
+            }
+            if (changed) {
+                std::swap(P, Q);
+                r2 = reach2();
+            }
         });
+        if (out.error) return out;
     }
-    size_t nv = P.v.size();
+    const int nv = P->n;
     // polygon area / centroid relative to the generator
     double A = 0, cx = 0, cy = 0;
     double per = 0;
-    for (size_t k = 0; k < nv; k++) {
-        P3 a = P.v[k] - gi, c = P.v[(k + 1) % nv] - gi;
+    for (int k = 0; k < nv; k++) {
+        P3 a = P->v[k] - gi, c = P->v[(k + 1) % nv] - gi;
         double cr = a.x * c.y - c.x * a.y;
         A += cr;
         cx += (a.x + c.x) * cr;
@@ -255,15 +276,16 @@ CellOut build_cell2(int64_t i, int64_t n, const double* g, const Grid& gr) {
     double Lz = gr.box[2];
     out.volume = A * Lz;
     out.centroid = {gi.x + cx / (6 * A), gi.y + cy / (6 * A), 0.5 * Lz};
-    for (size_t k = 0; k < nv; k++) {
-        if (P.lab[k] == kInvalid) { out.error = 1; continue; }
-        P3 a = P.v[k], c = P.v[(k + 1) % nv];
+    out.faces.reserve(nv);
+    for (int k = 0; k < nv; k++) {
+        if (P->lab[k] == kInvalid) { out.error = 1; continue; }
+        P3 a = P->v[k], c = P->v[(k + 1) % nv];
         double len = norm(c - a);
         if (len <= 1e-12 * per) continue;
         FaceOut f;
-        f.nb = P.lab[k];
+        f.nb = P->lab[k];
         int s[3];
-        unpack_shift(P.sh[k], s);
+        unpack_shift(P->sh[k], s);
         f.sx = s[0]; f.sy = s[1]; f.sz = s[2];
         f.area = len * Lz;
         f.centroid = {0.5 * (a.x + c.x), 0.5 * (a.y + c.y), 0.5 * Lz};
@@ -492,67 +514,91 @@ int mvmm_voronoi_build(int dim, int64_t n, const double* gen, const double* box,
         err |= cells[i].error;
     }
     if (err) return -10 - err;
+    // Faces are owned by the lower cell index (or are walls) and numbered in
+    // owner order, then in the owner's own order; every cell lists its faces
+    // in increasing index.  Each part runs over the cells in parallel.
     Built* B = new Built();
     B->n = n;
     B->volume.resize(n);
     B->cell_centroid.resize(3 * n);
-    std::vector<std::vector<int32_t>> incid(n);
-    int64_t nf = 0;
+    std::vector<int64_t> first(n + 1, 0);  // the first face each cell owns
+#pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < n; i++) {
         B->volume[i] = cells[i].volume;
         B->cell_centroid[i] = cells[i].centroid.x;
         B->cell_centroid[n + i] = cells[i].centroid.y;
         B->cell_centroid[2 * n + i] = cells[i].centroid.z;
+        int64_t c = 0;
         for (auto& f : cells[i].faces)
-            if (f.nb < 0 || f.nb > i) nf++;
+            if (f.nb < 0 || f.nb > i) c++;
+        first[i + 1] = c;
     }
-    B->left.reserve(nf); B->right.reserve(nf); B->area.reserve(nf);
-    std::vector<P3> nrm, cen, shf;
-    nrm.reserve(nf); cen.reserve(nf); shf.reserve(nf);
+    for (int64_t i = 0; i < n; i++) first[i + 1] += first[i];
+    const int64_t nf = first[n];
+    B->left.resize(nf);
+    B->right.resize(nf);
+    B->area.resize(nf);
+    B->normal.resize(3 * nf);
+    B->centroid.resize(3 * nf);
+    B->shift.resize(3 * nf);
+    std::vector<int32_t> deg(n, 0);  // faces per cell
+#pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < n; i++) {
         P3 gi{gen[i], gen[n + i], gen[2 * n + i]};
+        int64_t idx = first[i];
         for (auto& f : cells[i].faces) {
             if (f.nb >= 0 && f.nb <= i) continue;
-            int32_t idx = int32_t(B->left.size());
-            B->left.push_back(int32_t(i));
-            B->area.push_back(f.area);
-            cen.push_back(f.centroid);
-            incid[i].push_back(idx);
+            B->left[idx] = int32_t(i);
+            B->area[idx] = f.area;
+            B->centroid[idx] = f.centroid.x;
+            B->centroid[nf + idx] = f.centroid.y;
+            B->centroid[2 * nf + idx] = f.centroid.z;
+            P3 nn{0, 0, 0}, s{0, 0, 0};
             if (f.nb >= 0) {
                 int64_t j = f.nb;
-                P3 s{f.sx * box[0], f.sy * box[1], f.sz * box[2]};
+                s = P3{f.sx * box[0], f.sy * box[1], f.sz * box[2]};
                 P3 gj{gen[j] + s.x, gen[n + j] + s.y, gen[2 * n + j] + s.z};
                 P3 d = gj - gi;
-                nrm.push_back((1.0 / norm(d)) * d);
-                shf.push_back(s);
-                B->right.push_back(int32_t(j));
-                incid[j].push_back(idx);
+                nn = (1.0 / norm(d)) * d;
+                B->right[idx] = int32_t(j);
+#pragma omp atomic
+                deg[j]++;
             } else {
-                P3 nn{0, 0, 0};
                 if (f.nb == -1) nn.x = -1; else if (f.nb == -2) nn.x = 1;
                 else if (f.nb == -3) nn.y = -1; else if (f.nb == -4) nn.y = 1;
                 else if (f.nb == -5) nn.z = -1; else nn.z = 1;
-                nrm.push_back(nn);
-                shf.push_back({0, 0, 0});
-                B->right.push_back(-1);
+                B->right[idx] = -1;
             }
+            B->normal[idx] = nn.x;
+            B->normal[nf + idx] = nn.y;
+            B->normal[2 * nf + idx] = nn.z;
+            B->shift[idx] = s.x;
+            B->shift[nf + idx] = s.y;
+            B->shift[2 * nf + idx] = s.z;
+            idx++;
         }
-    }
-    nf = int64_t(B->left.size());
-    B->normal.resize(3 * nf); B->centroid.resize(3 * nf); B->shift.resize(3 * nf);
-    for (int64_t f = 0; f < nf; f++) {
-        B->normal[f] = nrm[f].x; B->normal[nf + f] = nrm[f].y; B->normal[2 * nf + f] = nrm[f].z;
-        B->centroid[f] = cen[f].x; B->centroid[nf + f] = cen[f].y; B->centroid[2 * nf + f] = cen[f].z;
-        B->shift[f] = shf[f].x; B->shift[nf + f] = shf[f].y; B->shift[2 * nf + f] = shf[f].z;
     }
     B->csr_off.resize(n + 1);
     B->csr_off[0] = 0;
-    for (int64_t i = 0; i < n; i++) {
-        std::sort(incid[i].begin(), incid[i].end());
-        B->csr_off[i + 1] = B->csr_off[i] + int32_t(incid[i].size());
+    for (int64_t i = 0; i < n; i++)
+        B->csr_off[i + 1] = B->csr_off[i] + int32_t(first[i + 1] - first[i]) + deg[i];
+    B->csr_face.resize(B->csr_off[n]);
+    std::vector<int32_t> fill(B->csr_off.begin(), B->csr_off.end() - 1);
+#pragma omp parallel for schedule(static)
+    for (int64_t f = 0; f < nf; f++) {
+        int32_t slot;
+#pragma omp atomic capture
+        slot = fill[B->left[f]]++;
+        B->csr_face[slot] = int32_t(f);
+        const int32_t j = B->right[f];
+        if (j >= 0) {
+#pragma omp atomic capture
+            slot = fill[j]++;
+            B->csr_face[slot] = int32_t(f);
+        }
     }
-    B->csr_face.reserve(B->csr_off[n]);
-    for (int64_t i = 0; i < n; i++) B->csr_face.insert(B->csr_face.end(), incid[i].begin(), incid[i].end());
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; i++) std::sort(B->csr_face.begin() + B->csr_off[i], B->csr_face.begin() + B->csr_off[i + 1]);
     *n_faces = nf;
     *handle = B;
     return 0;
