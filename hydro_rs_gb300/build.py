@@ -28,7 +28,7 @@ NVCC_COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "
 CU_SOURCES = {
     "step_fp64.cu": ["-fmad=false"],
     "step_fp32.cu": ["-fmad=true", "-prec-div=false", "-prec-sqrt=false"],
-    "mvmm_api.cu": [],
+    "mvmm_api.cu": ["-Xcompiler", "-fopenmp"],
     "noalloc.cu": ["-fmad=false"],
 }
 HEADERS = ["mvmm_device.cuh", "mvmm_internal.h", "mvmm_cellops.cuh", "bitconv.cuh", "face64.cuh"]
@@ -76,7 +76,7 @@ def build_gpu(verbose: bool = False) -> str:
         list(ex.map(lambda j: _run(*j), jobs))
     lib = os.path.join(OUT, "libmvmm_gpu.so")
     if _stale(lib, objs):
-        _run([nvcc] + ARCH + ["-shared", "-o", lib] + objs + ["-lcudart"])
+        _run([nvcc] + ARCH + ["-shared", "-o", lib] + objs + ["-lcudart", "-lgomp"])
     return lib
 
 

@@ -410,29 +410,52 @@ int check_mesh(const mvmm_mesh* m, int boundary) {
         return fail(MVMM_E_INVALID, "mesh: null pointer");
     int64_t n = m->n_cells, nf = m->n_faces;
     if (m->csr_off[0] != 0) return fail(MVMM_E_INVALID, "mesh: csr_off[0] != 0");
-    std::vector<int32_t> deg(n, 0);
+    // every index is checked before anything reads through it; the checks run
+    // over the host's cores (a moving mesh passes every step)
+    int bad = 0;
+#pragma omp parallel for schedule(static) reduction(| : bad)
     for (int64_t f = 0; f < nf; f++) {
-        int32_t l = m->left[f], r = m->right[f];
-        if (l < 0 || l >= n) return fail(MVMM_E_INVALID, "mesh: face left index out of range");
-        if (r >= n || r < -1) return fail(MVMM_E_INVALID, "mesh: face right index out of range");
-        if (r < 0 && boundary == MVMM_BOUNDARY_PERIODIC)
-            return fail(MVMM_E_INVALID, "mesh: boundary face with periodic boundary conditions");
-        deg[l]++;
-        if (r >= 0) deg[r]++;
+        const int32_t l = m->left[f], r = m->right[f];
+        if (l < 0 || l >= n) bad |= 1;
+        if (r >= n || r < -1) bad |= 2;
+        if (r < 0 && boundary == MVMM_BOUNDARY_PERIODIC) bad |= 4;
     }
-    for (int64_t i = 0; i < n; i++) {
-        if (m->csr_off[i + 1] < m->csr_off[i]) return fail(MVMM_E_INVALID, "mesh: csr_off not monotone");
-        if (m->csr_off[i + 1] - m->csr_off[i] != deg[i]) return fail(MVMM_E_INVALID, "mesh: csr does not match faces");
-    }
-    for (int64_t k = 0; k < m->csr_off[n]; k++) {
-        int32_t f = m->csr_face[k];
-        if (f < 0 || f >= nf) return fail(MVMM_E_INVALID, "mesh: csr face index out of range");
-    }
+    if (bad & 1) return fail(MVMM_E_INVALID, "mesh: face left index out of range");
+    if (bad & 2) return fail(MVMM_E_INVALID, "mesh: face right index out of range");
+    if (bad & 4) return fail(MVMM_E_INVALID, "mesh: boundary face with periodic boundary conditions");
+#pragma omp parallel for schedule(static) reduction(| : bad)
     for (int64_t i = 0; i < n; i++)
-        for (int32_t k = m->csr_off[i]; k < m->csr_off[i + 1]; k++) {
-            int32_t f = m->csr_face[k];
-            if (m->left[f] != i && m->right[f] != i) return fail(MVMM_E_INVALID, "mesh: csr lists a face not touching the cell");
+        if (m->csr_off[i + 1] < m->csr_off[i]) bad |= 8;
+    if (bad & 8) return fail(MVMM_E_INVALID, "mesh: csr_off not monotone");
+    const int64_t ncsr = m->csr_off[n];
+#pragma omp parallel for schedule(static) reduction(| : bad)
+    for (int64_t k = 0; k < ncsr; k++) {
+        const int32_t f = m->csr_face[k];
+        if (f < 0 || f >= nf) bad |= 16;
+    }
+    if (bad & 16) return fail(MVMM_E_INVALID, "mesh: csr face index out of range");
+    // each cell lists exactly the faces that touch it: every listed face
+    // touches the cell, and the list lengths add up to the faces' ends
+    std::vector<int32_t> deg(n, 0);
+#pragma omp parallel for schedule(static)
+    for (int64_t f = 0; f < nf; f++) {
+#pragma omp atomic
+        deg[m->left[f]]++;
+        if (m->right[f] >= 0) {
+#pragma omp atomic
+            deg[m->right[f]]++;
         }
+    }
+#pragma omp parallel for schedule(static) reduction(| : bad)
+    for (int64_t i = 0; i < n; i++) {
+        if (m->csr_off[i + 1] - m->csr_off[i] != deg[i]) bad |= 32;
+        for (int32_t k = m->csr_off[i]; k < m->csr_off[i + 1]; k++) {
+            const int32_t f = m->csr_face[k];
+            if (m->left[f] != i && m->right[f] != i) bad |= 64;
+        }
+    }
+    if (bad & 32) return fail(MVMM_E_INVALID, "mesh: csr does not match faces");
+    if (bad & 64) return fail(MVMM_E_INVALID, "mesh: csr lists a face not touching the cell");
     return MVMM_OK;
 }
 
@@ -1599,6 +1622,23 @@ int mvmm_set_mesh(mvmm_ctx* c, const mvmm_mesh* m, const double* volume, const d
     c->geo_built = false;  // new face arrays
     drop_graphs(c);  // kernel parameters hold the face count and pointers
     CUDA_TRY(cudaStreamSynchronize(s));
+    return MVMM_OK;
+}
+
+int mvmm_host_alloc(size_t bytes, void** ptr) {
+    if (!ptr) return fail(MVMM_E_INVALID, "null argument");
+    *ptr = nullptr;
+    if (bytes == 0) return MVMM_OK;
+    cudaError_t e = cudaHostAlloc(ptr, bytes, cudaHostAllocDefault);
+    if (e != cudaSuccess) {
+        *ptr = nullptr;
+        return fail(MVMM_E_NOMEM, std::string("cudaHostAlloc: ") + cudaGetErrorString(e));
+    }
+    return MVMM_OK;
+}
+
+int mvmm_host_free(void* ptr) {
+    if (ptr) CUDA_TRY(cudaFreeHost(ptr));
     return MVMM_OK;
 }
 

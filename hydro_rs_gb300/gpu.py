@@ -27,7 +27,8 @@ EXPORTED = (
     "mvmm_profile_read", "mvmm_riemann_flux", "mvmm_riemann_sample", "mvmm_get_stats",
     "mvmm_ctx_create_batched", "mvmm_batch_state", "mvmm_autotune", "mvmm_riemann_flux_p", "mvmm_riemann_sample_p",
     "mvmm_step_cells", "mvmm_drift", "mvmm_get_positions", "mvmm_set_mesh", "mvmm_flush_deferred",
-    "mvmm_gravity_timesteps", "mvmm_gravity_accelerations", "mvmm_step_cells_changed",
+    "mvmm_gravity_timesteps", "mvmm_gravity_accelerations", "mvmm_step_cells_changed", "mvmm_host_alloc",
+    "mvmm_host_free",
 )
 
 
@@ -105,6 +106,8 @@ def load_library(path: str = LIB_PATH):
         "mvmm_flush_deferred": (i32, [vp]),
         "mvmm_get_positions": (i32, [vp, vp]),
         "mvmm_set_mesh": (i32, [vp, vp, vp, vp]),
+        "mvmm_host_alloc": (i32, [ctypes.c_size_t, ctypes.POINTER(vp)]),
+        "mvmm_host_free": (i32, [vp]),
         "mvmm_riemann_sample_p": (i32, [vp, i64, vp, vp, vp, vp]),
         "mvmm_get_stats": (i32, [vp, vp]),
         "mvmm_ctx_create_batched": (i32, [vp, vp, i64, vp, vp, ctypes.POINTER(vp)]),
@@ -167,6 +170,47 @@ def riemann_sample(kind: int, gamma: float, left, right, normal, precision: int 
         _check(L.mvmm_riemann_sample_p(ctypes.byref(prm), n, left.ctypes.data, right.ctypes.data, normal.ctypes.data,
                                        out.ctypes.data))
     return out
+
+
+class _HostBlock:
+    """A page-locked host block (mvmm_host_alloc), freed when the last array
+    viewing it goes (the arrays hold it as their base)."""
+
+    def __init__(self, nbytes: int):
+        p = ctypes.c_void_p(0)
+        _check(load_library().mvmm_host_alloc(nbytes, ctypes.byref(p)))
+        self.ptr, self.nbytes = p.value, nbytes
+        self.__array_interface__ = {"data": (self.ptr, False), "shape": (nbytes,), "typestr": "|u1", "version": 3}
+
+    def __del__(self):
+        ptr = getattr(self, "ptr", None)
+        if ptr:
+            self.ptr = None
+            try:
+                load_library().mvmm_host_free(ctypes.c_void_p(ptr))
+            except Exception:
+                pass
+
+
+class PinnedArrays:
+    """``arrays(specs)`` for :func:`mesh.mesh_voronoi`: the arrays of one call
+    carved from one page-locked block, which is kept and reused by the next
+    call (grown when too small), so a caller alternates two of these to keep
+    the previous result intact while it builds the next."""
+
+    def __init__(self):
+        self.block = None
+
+    def __call__(self, specs):
+        sizes = [int(np.prod(shape)) * np.dtype(dt).itemsize for shape, dt in specs]
+        offs, total = [], 0
+        for b in sizes:
+            offs.append(total)
+            total += (b + 63) // 64 * 64
+        if self.block is None or self.block.nbytes < total:
+            self.block = _HostBlock(max(total + total // 4, 64))
+        raw = np.asarray(self.block)
+        return [raw[o:o + b].view(dt).reshape(shape) for (shape, dt), o, b in zip(specs, offs, sizes)]
 
 
 class GpuSim:
@@ -264,6 +308,11 @@ class GpuSim:
         new.ti_current, new.ti_old, new.steps = self.ti_current, self.ti_old, self.steps
         new.active_faces, new.finished = self.active_faces, self.finished
         return new
+
+    def host_arrays(self) -> PinnedArrays:
+        """Page-locked output arrays for the host mesh builder: mvmm_set_mesh
+        then copies the mesh at the link's speed."""
+        return PinnedArrays()
 
     def positions(self) -> np.ndarray:
         loc = np.zeros((3, self.mesh.n_cells))

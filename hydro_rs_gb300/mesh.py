@@ -98,8 +98,12 @@ def mesh_1d(x: np.ndarray, box=(1.0, 1.0, 1.0), periodic: bool = False) -> Mesh:
     return m
 
 
-def mesh_voronoi(gen: np.ndarray, dim: int, box, periodic: bool, n_threads: int = 0) -> Mesh:
-    """2D/3D Voronoi mesh of generators ``gen`` ([3][n]) with the C++ builder."""
+def mesh_voronoi(gen: np.ndarray, dim: int, box, periodic: bool, n_threads: int = 0, arrays=None) -> Mesh:
+    """2D/3D Voronoi mesh of generators ``gen`` ([3][n]) with the C++ builder.
+
+    arrays: optional ``arrays(specs) -> list of ndarrays`` that provides the
+    output arrays for a list of (shape, dtype), e.g. page-locked host memory
+    (``gpu.PinnedArrays``) from which the mesh uploads at the link's speed."""
     lib = _mesh_lib()
     gen = np.ascontiguousarray(gen, dtype=np.float64)
     n = gen.shape[1]
@@ -112,18 +116,14 @@ def mesh_voronoi(gen: np.ndarray, dim: int, box, periodic: bool, n_threads: int 
         raise RuntimeError(f"Voronoi construction failed (code {rc})")
     f = nf.value
     try:
-        left = np.empty(f, np.int32)
-        right = np.empty(f, np.int32)
-        area = np.empty(f)
-        normal = np.empty((3, f))
-        centroid = np.empty((3, f))
-        shift = np.empty((3, f))
-        csr_off = np.empty(n + 1, np.int32)
-        volume = np.empty(n)
-        cc = np.empty((3, n))
-        # two passes: csr size is 2F - (#walls)
-        n_csr = 2 * f
-        csr_face = np.empty(n_csr, np.int32)
+        # csr_face holds 2F - (#walls) entries: room for 2F, trimmed below
+        specs = [(f, np.int32), (f, np.int32), (f, np.float64), ((3, f), np.float64), ((3, f), np.float64),
+                 ((3, f), np.float64), (n + 1, np.int32), (n, np.float64), ((3, n), np.float64), (2 * f, np.int32)]
+        if arrays is None:
+            out = [np.empty(shape, dt) for shape, dt in specs]
+        else:
+            out = arrays(specs)
+        left, right, area, normal, centroid, shift, csr_off, volume, cc, csr_face = out
         lib.mvmm_voronoi_fetch(h, left.ctypes.data, right.ctypes.data, area.ctypes.data, normal.ctypes.data,
                                centroid.ctypes.data, shift.ctypes.data, csr_off.ctypes.data, csr_face.ctypes.data,
                                volume.ctypes.data, cc.ctypes.data)

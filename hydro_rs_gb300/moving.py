@@ -69,6 +69,10 @@ class MovingMeshStepper:
         self.n_threads = n_threads
         self.seconds = {"drift": 0.0, "positions": 0.0, "mesh_build": 0.0, "mesh_upload": 0.0, "step": 0.0}
         self.removed = 0  # generators that left an open or vacuum box
+        # the GPU context's meshes are built into two alternating page-locked
+        # blocks (the one the context holds stays intact while the next is built)
+        self._arrays = [sim.host_arrays(), sim.host_arrays()] if hasattr(sim, "host_arrays") else None
+        self._turn = 0
 
     def step(self) -> bool:
         sim, s = self.sim, self.seconds
@@ -87,7 +91,11 @@ class MovingMeshStepper:
                 self.removed += loc.shape[1] - keep.size
                 loc = np.ascontiguousarray(loc[:, keep])
         t2 = time.perf_counter()
-        mesh = mesh_voronoi(loc, self.dim, self.box, self.periodic, self.n_threads)
+        arrays = None
+        if self._arrays is not None:
+            arrays = self._arrays[self._turn]
+            self._turn ^= 1
+        mesh = mesh_voronoi(loc, self.dim, self.box, self.periodic, self.n_threads, arrays=arrays)
         t3 = time.perf_counter()
         if keep is not None:  # a simulation over the particles kept
             sim = self.sim = sim.rebuilt(keep, mesh)

@@ -227,6 +227,12 @@ int mvmm_get_positions(mvmm_ctx *ctx, double *loc);
  * cells are applied to the active cells of the next step after its predict
  * stage (Particle::update_geometry, part.rs:151-158). */
 int mvmm_set_mesh(mvmm_ctx *ctx, const mvmm_mesh *mesh, const double *volume, const double *centroid);
+/* Page-locked host memory (cudaHostAlloc) for arrays a host hands to the
+ * copying calls (mvmm_set_mesh, mvmm_step_cells, the uploads and downloads):
+ * copies from and to it run at the link's speed instead of through a staging
+ * buffer.  No counterpart in the reference (its state lives on the host). */
+int mvmm_host_alloc(size_t bytes, void **ptr);
+int mvmm_host_free(void *ptr);
 
 /* Runner::step(&mut Space, ..) on host-resident state (runner.rs:6-22): uploads
  * `in`, runs one step (OptimalOrderRunner or GodunovHydroRunner) of a fixed
