@@ -295,118 +295,167 @@ CellOut build_cell2(int64_t i, int64_t n, const double* g, const Grid& gr) {
 }
 
 // ----------------------------------------------------------------- 3D ----
+// A convex polyhedron in fixed storage: vertices, and each face a loop of
+// vertex indices (counter-clockwise seen from outside) in one index array.
+constexpr int kMaxV3 = 512, kMaxF3 = 160, kMaxI3 = 2048;
 struct Poly3 {
-    std::vector<P3> v;
-    std::vector<std::vector<int>> f;  // vertex loops, CCW seen from outside
-    std::vector<int64_t> lab;
-    std::vector<int> sh;
+    int nv = 0, nf = 0;
+    P3 v[kMaxV3];
+    int fo[kMaxF3 + 1];  // face k's loop is idx[fo[k] .. fo[k + 1])
+    int idx[kMaxI3];
+    int64_t lab[kMaxF3];
+    int sh[kMaxF3];
 };
 
 void box3(Poly3& P, P3 lo, P3 hi, bool invalid) {
-    P.v = {{lo.x, lo.y, lo.z}, {hi.x, lo.y, lo.z}, {hi.x, hi.y, lo.z}, {lo.x, hi.y, lo.z},
-           {lo.x, lo.y, hi.z}, {hi.x, lo.y, hi.z}, {hi.x, hi.y, hi.z}, {lo.x, hi.y, hi.z}};
-    P.f = {{0, 3, 2, 1}, {4, 5, 6, 7}, {0, 1, 5, 4}, {2, 3, 7, 6}, {0, 4, 7, 3}, {1, 2, 6, 5}};
-    if (invalid) P.lab = {kInvalid, kInvalid, kInvalid, kInvalid, kInvalid, kInvalid};
-    else P.lab = {-5, -6, -3, -4, -1, -2};
+    const P3 v[8] = {{lo.x, lo.y, lo.z}, {hi.x, lo.y, lo.z}, {hi.x, hi.y, lo.z}, {lo.x, hi.y, lo.z},
+                     {lo.x, lo.y, hi.z}, {hi.x, lo.y, hi.z}, {hi.x, hi.y, hi.z}, {lo.x, hi.y, hi.z}};
+    const int f[6][4] = {{0, 3, 2, 1}, {4, 5, 6, 7}, {0, 1, 5, 4}, {2, 3, 7, 6}, {0, 4, 7, 3}, {1, 2, 6, 5}};
+    const int64_t walls[6] = {-5, -6, -3, -4, -1, -2};
     int z[3] = {0, 0, 0};
-    P.sh.assign(6, pack_shift(z));
+    P.nv = 8;
+    for (int k = 0; k < 8; k++) P.v[k] = v[k];
+    P.nf = 6;
+    for (int k = 0; k < 6; k++) {
+        P.fo[k] = 4 * k;
+        for (int j = 0; j < 4; j++) P.idx[4 * k + j] = f[k][j];
+        P.lab[k] = invalid ? kInvalid : walls[k];
+        P.sh[k] = pack_shift(z);
+    }
+    P.fo[6] = 24;
 }
 
-void clip3(Poly3& P, P3 m, P3 d, int64_t lab, int sh, double eps) {
-    size_t nv = P.v.size();
-    std::vector<double> h(nv);
+// Clips P by the half-space dot(x - m, d) <= eps into Q.  Returns 0 when
+// nothing is cut (Q untouched), 1 when Q holds the clipped polyhedron, -1 when
+// it would not fit.  Each face keeps its inside part; the cut points on the
+// plane, one per crossing edge, are chained into the new face.
+int clip3(const Poly3& P, Poly3& Q, P3 m, P3 d, int64_t lab, int sh, double eps) {
+    const int nv = P.nv;
+    double h[kMaxV3];
     bool any_out = false;
-    for (size_t k = 0; k < nv; k++) {
+    for (int k = 0; k < nv; k++) {
         h[k] = dot(P.v[k] - m, d);
         if (h[k] > eps) any_out = true;
     }
-    if (!any_out) return;
-    std::unordered_map<uint64_t, int> cut;  // edge -> new vertex
-    std::unordered_map<int, int> next;      // on the cut face: entry -> exit chain
-    auto edge_point = [&](int a, int b) -> int {
-        // a inside, b outside (or reversed); returns the vertex on the plane
-        if (h[a] >= -eps && h[a] <= eps) return a;
-        uint64_t key = (uint64_t(std::min(a, b)) << 32) | uint64_t(std::max(a, b));
-        auto it = cut.find(key);
-        if (it != cut.end()) return it->second;
-        double t = h[a] / (h[a] - h[b]);
-        P3 p = P.v[a] + t * (P.v[b] - P.v[a]);
-        int id = int(P.v.size());
-        P.v.push_back(p);
-        cut[key] = id;
-        return id;
+    if (!any_out) return 0;
+    int newid[kMaxV3];
+    for (int k = 0; k < nv; k++) newid[k] = -1;
+    Q.nv = 0;
+    Q.nf = 0;
+    Q.fo[0] = 0;
+    bool full = false;
+    auto keep = [&](int a) {  // a vertex of P that stays
+        if (newid[a] < 0) {
+            if (Q.nv >= kMaxV3) { full = true; return 0; }
+            newid[a] = Q.nv;
+            Q.v[Q.nv++] = P.v[a];
+        }
+        return newid[a];
     };
-    std::vector<std::vector<int>> nf;
-    std::vector<int64_t> nl;
-    std::vector<int> ns;
-    for (size_t fi = 0; fi < P.f.size(); fi++) {
-        const auto& F = P.f[fi];
-        size_t m_ = F.size();
-        std::vector<int> G;
-        int exitp = -1, entryp = -1;
-        for (size_t k = 0; k < m_; k++) {
-            int a = F[k], b = F[(k + 1) % m_];
-            bool ain = h[a] <= eps, bin = h[b] <= eps;
+    // the cut point of edge (a inside, b outside), one per edge
+    uint64_t cut_key[kMaxF3];
+    int cut_id[kMaxF3], ncut = 0;
+    auto edge_point = [&](int a, int b) -> int {
+        if (h[a] >= -eps && h[a] <= eps) return keep(a);  // a lies on the plane
+        const uint64_t key = (uint64_t(std::min(a, b)) << 32) | uint64_t(std::max(a, b));
+        for (int k = 0; k < ncut; k++)
+            if (cut_key[k] == key) return cut_id[k];
+        if (ncut >= kMaxF3 || Q.nv >= kMaxV3) { full = true; return 0; }
+        const double t = h[a] / (h[a] - h[b]);
+        Q.v[Q.nv] = P.v[a] + t * (P.v[b] - P.v[a]);
+        cut_key[ncut] = key;
+        cut_id[ncut++] = Q.nv;
+        return Q.nv++;
+    };
+    int chain_from[kMaxF3], chain_to[kMaxF3], nchain = 0;  // on the cut plane: entry -> exit
+    for (int fi = 0; fi < P.nf && !full; fi++) {
+        const int f0 = P.fo[fi], mlen = P.fo[fi + 1] - f0;
+        const int start = Q.fo[Q.nf];
+        int len = 0, exitp = -1, entryp = -1;
+        auto push = [&](int x) {
+            if (start + len >= kMaxI3) { full = true; return; }
+            Q.idx[start + len++] = x;
+        };
+        for (int k = 0; k < mlen; k++) {
+            const int a = P.idx[f0 + k], b = P.idx[f0 + (k + 1 == mlen ? 0 : k + 1)];
+            const bool ain = h[a] <= eps, bin = h[b] <= eps;
             if (ain) {
-                G.push_back(a);
+                const int qa = keep(a);
+                push(qa);
                 if (!bin) {
-                    int p = edge_point(a, b);
-                    if (p != a) G.push_back(p);
+                    const int p = edge_point(a, b);
+                    if (p != qa) push(p);
                     exitp = p;
                 }
             } else if (bin) {
-                int p = edge_point(b, a);
-                if (p != b) G.push_back(p);
+                const int p = edge_point(b, a);
+                const bool b_on_plane = h[b] >= -eps && h[b] <= eps;
+                if (!b_on_plane) push(p);
                 entryp = p;
             }
         }
-        if (exitp >= 0 && entryp >= 0 && exitp != entryp) next[entryp] = exitp;
-        if (G.size() >= 3) {
-            nf.push_back(G);
-            nl.push_back(P.lab[fi]);
-            ns.push_back(P.sh[fi]);
+        if (exitp >= 0 && entryp >= 0 && exitp != entryp) {
+            if (nchain >= kMaxF3) { full = true; break; }
+            chain_from[nchain] = entryp;
+            chain_to[nchain++] = exitp;
+        }
+        if (len >= 3) {
+            if (Q.nf >= kMaxF3) { full = true; break; }
+            Q.lab[Q.nf] = P.lab[fi];
+            Q.sh[Q.nf] = P.sh[fi];
+            Q.fo[++Q.nf] = start + len;
         }
     }
-    // chain the new face: each clipped face contributes exit->entry along its
-    // own boundary; the cut face runs entry -> exit in reverse orientation.
-    if (!next.empty()) {
-        std::vector<int> loop;
-        int start = next.begin()->first;
-        int cur = start;
-        for (size_t guard = 0; guard <= next.size() + 1; guard++) {
-            loop.push_back(cur);
-            auto it = next.find(cur);
-            if (it == next.end()) { loop.clear(); break; }
-            cur = it->second;
-            if (cur == start) break;
+    if (full) return -1;
+    // the new face: each clipped face contributes entry -> exit along the cut
+    if (nchain > 0) {
+        const int start = Q.fo[Q.nf];
+        int len = 0;
+        const int first = chain_from[0];
+        int cur = first;
+        bool closed = false;
+        for (int guard = 0; guard <= nchain + 1; guard++) {
+            if (start + len >= kMaxI3) return -1;
+            Q.idx[start + len++] = cur;
+            int nx = -1;
+            for (int k = 0; k < nchain; k++)
+                if (chain_from[k] == cur) { nx = chain_to[k]; break; }
+            if (nx < 0) break;
+            cur = nx;
+            if (cur == first) { closed = true; break; }
         }
-        if (loop.size() >= 3) {
-            nf.push_back(loop);
-            nl.push_back(lab);
-            ns.push_back(sh);
+        if (closed && len >= 3) {
+            if (Q.nf >= kMaxF3) return -1;
+            Q.lab[Q.nf] = lab;
+            Q.sh[Q.nf] = sh;
+            Q.fo[++Q.nf] = start + len;
         }
     }
-    // compact vertices
-    std::vector<int> remap(P.v.size(), -1);
-    std::vector<P3> nvv;
-    for (auto& F : nf)
-        for (auto& x : F) {
-            if (remap[x] < 0) { remap[x] = int(nvv.size()); nvv.push_back(P.v[x]); }
-            x = remap[x];
+    // drop the vertices no face uses (in order: a vertex moves to a lower slot)
+    int used[kMaxV3];
+    for (int k = 0; k < Q.nv; k++) used[k] = -1;
+    const int nidx = Q.fo[Q.nf];
+    for (int k = 0; k < nidx; k++) used[Q.idx[k]] = 0;
+    int nn = 0;
+    for (int k = 0; k < Q.nv; k++)
+        if (used[k] == 0) {
+            used[k] = nn;
+            Q.v[nn++] = Q.v[k];
         }
-    P.v = std::move(nvv);
-    P.f = std::move(nf);
-    P.lab = std::move(nl);
-    P.sh = std::move(ns);
+    Q.nv = nn;
+    for (int k = 0; k < nidx; k++) Q.idx[k] = used[Q.idx[k]];
+    return 1;
 }
 
 CellOut build_cell3(int64_t i, int64_t n, const double* g, const Grid& gr) {
     CellOut out;
     P3 gi{g[i], g[n + i], g[2 * n + i]};
-    Poly3 P;
+    static thread_local Poly3 buf[2];
+    Poly3* P = &buf[0];
+    Poly3* Q = &buf[1];
     double L[3] = {gr.box[0], gr.box[1], gr.box[2]};
-    if (!gr.periodic) box3(P, {0, 0, 0}, {L[0], L[1], L[2]}, false);
-    else box3(P, gi - P3{0.5 * L[0], 0.5 * L[1], 0.5 * L[2]}, gi + P3{0.5 * L[0], 0.5 * L[1], 0.5 * L[2]}, true);
+    if (!gr.periodic) box3(*P, {0, 0, 0}, {L[0], L[1], L[2]}, false);
+    else box3(*P, gi - P3{0.5 * L[0], 0.5 * L[1], 0.5 * L[2]}, gi + P3{0.5 * L[0], 0.5 * L[1], 0.5 * L[2]}, true);
     int b[3];
     for (int k = 0; k < 3; k++) {
         double c = k == 0 ? gi.x : (k == 1 ? gi.y : gi.z);
@@ -414,13 +463,18 @@ CellOut build_cell3(int64_t i, int64_t n, const double* g, const Grid& gr) {
     }
     double eps = 1e-13 * gr.minbw * gr.minbw;
     int rmax = std::max(gr.nb[0], std::max(gr.nb[1], gr.nb[2])) + 1;
-    double r2max = 0;
-    for (auto& v : P.v) r2max = std::max(r2max, dot(v - gi, v - gi));
+    auto reach2 = [&]() {
+        double r2 = 0;
+        for (int k = 0; k < P->nv; k++) r2 = std::max(r2, dot(P->v[k] - gi, P->v[k] - gi));
+        return r2;
+    };
+    double r2max = reach2();
+    static thread_local std::vector<std::pair<double, std::pair<int32_t, int>>> cand;
     for (int r = 0; r <= rmax; r++) {
         double reach = (r - 1) * gr.minbw;
         if (r >= 1 && reach > 0 && reach * reach >= 4.0 * r2max) break;
-        // gather this ring's candidates sorted by distance: nearer planes cut more
-        std::vector<std::pair<double, std::pair<int32_t, int>>> cand;
+        // this ring's candidates sorted by distance: nearer planes cut more
+        cand.clear();
         for_ring(gr, b, r, [&](int32_t j, const int s[3]) {
             if (j == i && s[0] == 0 && s[1] == 0 && s[2] == 0) return;
             P3 gj{g[j] + s[0] * L[0], g[n + j] + s[1] * L[1], g[2 * n + j] + s[2] * L[2]};
@@ -436,24 +490,31 @@ CellOut build_cell3(int64_t i, int64_t n, const double* g, const Grid& gr) {
             if (j == i) { out.error = 2; continue; }
             P3 gj{g[j] + s[0] * L[0], g[n + j] + s[1] * L[1], g[2 * n + j] + s[2] * L[2]};
             P3 d = gj - gi;
-            clip3(P, 0.5 * (gi + gj), d, j, c.second.second, eps * std::sqrt(c.first));
-            r2max = 0;
-            for (auto& v : P.v) r2max = std::max(r2max, dot(v - gi, v - gi));
+            const int rc = clip3(*P, *Q, 0.5 * (gi + gj), d, j, c.second.second, eps * std::sqrt(c.first));
+            if (rc < 0) {
+                out.error = 3;
+                return out;
+            }
+            if (rc > 0) {
+                std::swap(P, Q);
+                r2max = reach2();
+            }
         }
     }
     // integrals: faces by fan triangulation, volume by tetrahedra from gi
     double V = 0;
     P3 C{0, 0, 0};
     double total_area = 0;
-    std::vector<double> fa(P.f.size());
-    std::vector<P3> fc(P.f.size());
-    for (size_t fi = 0; fi < P.f.size(); fi++) {
-        const auto& F = P.f[fi];
-        P3 a0 = P.v[F[0]] - gi;
+    double fa[kMaxF3];
+    P3 fc[kMaxF3];
+    for (int fi = 0; fi < P->nf; fi++) {
+        const int* F = P->idx + P->fo[fi];
+        const int len = P->fo[fi + 1] - P->fo[fi];
+        P3 a0 = P->v[F[0]] - gi;
         double A = 0;
         P3 ac{0, 0, 0};
-        for (size_t k = 1; k + 1 < F.size(); k++) {
-            P3 a1 = P.v[F[k]] - gi, a2 = P.v[F[k + 1]] - gi;
+        for (int k = 1; k + 1 < len; k++) {
+            P3 a1 = P->v[F[k]] - gi, a2 = P->v[F[k + 1]] - gi;
             P3 cr = cross(a1 - a0, a2 - a0);
             double ta = 0.5 * norm(cr);
             A += ta;
@@ -468,13 +529,14 @@ CellOut build_cell3(int64_t i, int64_t n, const double* g, const Grid& gr) {
     }
     out.volume = V;
     out.centroid = gi + (1.0 / V) * C;
-    for (size_t fi = 0; fi < P.f.size(); fi++) {
-        if (P.lab[fi] == kInvalid) { out.error = 1; continue; }
+    out.faces.reserve(P->nf);
+    for (int fi = 0; fi < P->nf; fi++) {
+        if (P->lab[fi] == kInvalid) { out.error = 1; continue; }
         if (fa[fi] <= 1e-12 * total_area) continue;
         FaceOut f;
-        f.nb = P.lab[fi];
+        f.nb = P->lab[fi];
         int s[3];
-        unpack_shift(P.sh[fi], s);
+        unpack_shift(P->sh[fi], s);
         f.sx = s[0]; f.sy = s[1]; f.sz = s[2];
         f.area = fa[fi];
         f.centroid = fc[fi];
