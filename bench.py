@@ -80,6 +80,9 @@ WORKLOADS = {
     # moving mesh: the shear layer with steered generators, host Voronoi rebuild every step
     "kh2d_moving": "kelvin_helmholtz_2d {n}x{n} jittered periodic Voronoi, exact Riemann solver, gamma=5/3, "
                    "steered generators (particle_motion=steer), mesh rebuilt on the host every step",
+    # the shear layer with any of the reference's solvers and runners (--riemann, --runner)
+    "kh2d_solver": "kelvin_helmholtz_2d {n}x{n} jittered periodic Voronoi, {riemann} Riemann solver, {runner} runner, "
+                   "gamma=5/3",
     # self-gravity kicks: the shear layer with the direct O(N^2) sum over j > i every step
     "kh2d_selfgrav": "kelvin_helmholtz_2d {n}x{n} jittered periodic Voronoi, HLLC, gamma=5/3, self-gravity "
                      "(softening 0.01) accelerations computed and kicked every step",
@@ -87,6 +90,7 @@ WORKLOADS = {
     "serve2d": "{n} served isentropic-vortex requests (Poisson 50/s, 32^2..512^2 periodic Voronoi, HLLC, t_end=1)",
 }
 DATA = {
+    "kh2d_solver": "synthetic (seeded jittered lattice, shear-layer ICs)",
     "kh2d_selfgrav": "synthetic (seeded jittered lattice, shear-layer ICs)",
     "kh2d": "synthetic (seeded jittered lattice, shear-layer ICs)",
     "kh2d_hllc": "synthetic (seeded jittered lattice, shear-layer ICs)",
@@ -95,10 +99,19 @@ DATA = {
     "batch1d": "synthetic (seeded random 1D Riemann problems)",
     "batch1d_pvrs": "synthetic (seeded random 1D Riemann problems)",
 }
-DEFAULT_N = {"kh2d_selfgrav": 128, "kh2d_moving": NX, "kh2d": NX, "kh2d_hllc": 1024, "sod1d": 1000, "blast3d": 128, "batch1d": 512, "batch1d_pvrs": 512, "serve2d": 60}
+DEFAULT_N = {"kh2d_solver": NX, "kh2d_selfgrav": 128, "kh2d_moving": NX, "kh2d": NX, "kh2d_hllc": 1024, "sod1d": 1000, "blast3d": 128, "batch1d": 512, "batch1d_pvrs": 512, "serve2d": 60}
 
 
-def _problem(nx=NX, workload="kh2d"):
+# AIRiemannSolver's threshold and LinearAdvection's velocity for the kh2d_solver workload
+AIRS_THRESHOLD = 2.0
+ADVECTION_VELOCITY = (0.7, -0.4, 0.2)
+
+
+def _workload_name(args) -> str:
+    return WORKLOADS[args.workload].format(n=args.nx, riemann=args.riemann, runner=args.runner)
+
+
+def _problem(nx=NX, workload="kh2d", riemann="TSRS", runner="OptimalOrder"):
     from hydro_rs_gb300 import ics
 
     t0 = time.perf_counter()
@@ -111,6 +124,11 @@ def _problem(nx=NX, workload="kh2d"):
         p = ics.sod_1d(nx)
     elif workload == "blast3d":
         p = ics.point_blast_3d(nx, seed=3, riemann=ics.HLLC, t_end=0.05, sync_all=False)
+    elif workload == "kh2d_solver":
+        p = ics.kelvin_helmholtz_2d(nx, seed=2, riemann=ics.SOLVER_NAMES[riemann], t_end=1.5)
+        p.params.runner = ics.RUNNER_NAMES[runner]
+        p.params.airs_threshold = AIRS_THRESHOLD
+        p.params.advection_velocity = ADVECTION_VELOCITY
     else:
         kind = ics.HLLC if workload in ("kh2d_hllc", "kh2d_selfgrav") else ics.EXACT
         p = ics.kelvin_helmholtz_2d(nx, seed=2, riemann=kind, t_end=1.5)
@@ -338,7 +356,7 @@ def run_ours(args):
         dist.init_process_group("nccl")
     from hydro_rs_gb300 import ics
 
-    problem, mesh_s = _problem(args.nx, args.workload)
+    problem, mesh_s = _problem(args.nx, args.workload, args.riemann, args.runner)
     problem.params.limiter_frame = args.limiter_frame
     nf, nc = problem.mesh.n_faces, problem.mesh.n_cells
     stream = torch.cuda.Stream()
@@ -575,7 +593,7 @@ def run_ours(args):
                        "no host-side change is listed, and the cells the step rewrote (32 at a time) are "
                        "written back in place"}
 
-    cpu = _cpu_sample(problem, WORKLOADS[args.workload].format(n=args.nx)) if (ws == 1 and not args.no_cpu) else None
+    cpu = _cpu_sample(problem, _workload_name(args)) if (ws == 1 and not args.no_cpu) else None
     value64 = faces64 / (ms64 * 1e-3)
     value32 = faces32 / (ms32 * 1e-3)
     exact = problem.params.riemann == ics.EXACT
@@ -583,7 +601,7 @@ def run_ours(args):
         "metric": METRIC, "value": value64, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms64 / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": DATA.get(args.workload, "synthetic, seeded"),
-        "config": {"workload": WORKLOADS[args.workload].format(n=args.nx),
+        "config": {"workload": _workload_name(args),
                    "cells": nc, "faces": nf, "precision": PRECISION_FP64,
                    "l2": "flushed (256 MB write) before each timed step", "parallelism": f"replicas x{ws}",
                    "mesh_build_s": round(mesh_s, 3),
@@ -727,7 +745,7 @@ def run_batch_to_end(args):
 
     ws, rank = _dist()
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-    problem, mesh_s = _problem(args.nx, args.workload)
+    problem, mesh_s = _problem(args.nx, args.workload, args.riemann, args.runner)
     problem.params.limiter_frame = args.limiter_frame
     off, te = problem.extra["cell_offsets"], problem.extra["t_end"]
     res = {}
@@ -780,7 +798,7 @@ def run_batch_to_end(args):
         "metric": METRIC, "value": res[0]["faces"] / res[0]["seconds"], "unit": UNIT, "n_gpus": 1,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": DATA.get(args.workload, "synthetic, seeded"),
-        "config": {"workload": WORKLOADS[args.workload].format(n=args.nx) + ", the whole run",
+        "config": {"workload": _workload_name(args) + ", the whole run",
                    "cells": problem.mesh.n_cells, "faces": problem.mesh.n_faces, "precision": PRECISION_FP64,
                    "mesh_build_s": round(mesh_s, 3),
                    "timing": "wall clock around mvmm_run, each form until every simulation finished" +
@@ -975,7 +993,7 @@ def run_reference(args):
     ws, rank = _dist()
     if rank != 0:
         return
-    problem, _ = _problem(args.nx, args.workload)
+    problem, _ = _problem(args.nx, args.workload, args.riemann, args.runner)
     from oracle import oracle as O
 
     threads = os.cpu_count() or 1
@@ -993,7 +1011,7 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded jittered lattice, shear-layer ICs)",
-        "config": {"workload": WORKLOADS[args.workload].format(n=args.nx), "cells": problem.mesh.n_cells,
+        "config": {"workload": _workload_name(args), "cells": problem.mesh.n_cells,
                    "faces": problem.mesh.n_faces, "precision": PRECISION_FP64},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{args.steps} steps after {2 + args.warmup} warm-up steps; the Rust reference "
@@ -1013,6 +1031,11 @@ def main():
                     help="kh2d (the headline), sod1d, blast3d (extra measurements)")
     ap.add_argument("--nx", type=int, default=None, help="lattice side / cell count (default per workload)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg (profiling runs)")
+    ap.add_argument("--riemann", default="TSRS", choices=["HLLC", "Exact", "PVRS", "AIRS", "TSRS", "TRRS",
+                                                           "LinearAdvection"],
+                    help="kh2d_solver: the Riemann solver (bin/main.rs names)")
+    ap.add_argument("--runner", default="OptimalOrder", choices=["OptimalOrder", "Godunov"],
+                    help="kh2d_solver: the runner")
     ap.add_argument("--limiter-frame", type=int, default=0, choices=[0, 1],
                     help="1: the cell-wise limiter's face offsets in flux_exchange's frame (not the reference's)")
     ap.add_argument("--to-end", action="store_true",
