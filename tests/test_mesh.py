@@ -75,3 +75,23 @@ def test_periodic_shift_convention():
     # normal points from left to the (shifted) right generator
     dots = (d * m.normal).sum(axis=0)
     assert np.all(dots > 0)
+
+
+@pytest.mark.parametrize("dim,periodic", [(2, True), (2, False), (3, True), (3, False)])
+def test_builder_is_deterministic_across_thread_counts(dim, periodic):
+    """The cells are clipped in parallel and the face list and CSR assembled in
+    parallel: the mesh is the same bits whatever the number of threads."""
+    rng = np.random.default_rng(17)
+    n1d = 24 if dim == 2 else 7
+    x, box, _, _ = ics.lattice((1.0, 1.0, 1.0), n1d ** dim, dim, 0.3, rng)
+    meshes = [mesh_voronoi(x, dim, box, periodic, n_threads=t) for t in (1, 3, 8)]
+    for m in meshes[1:]:
+        for name in ("left", "right", "area", "normal", "centroid", "shift", "csr_off", "csr_face", "volume",
+                     "cell_centroid"):
+            a, b = getattr(meshes[0], name), getattr(m, name)
+            assert a.shape == b.shape and np.array_equal(a.view(np.uint8), b.view(np.uint8)), name
+    m = meshes[0]
+    for i in range(m.n_cells):  # each cell's faces in increasing index, each touching it
+        fs = m.csr_face[m.csr_off[i]:m.csr_off[i + 1]]
+        assert np.all(np.diff(fs) > 0)
+        assert np.all((m.left[fs] == i) | (m.right[fs] == i))
