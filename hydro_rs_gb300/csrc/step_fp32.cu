@@ -14,6 +14,7 @@
 // Minimum resident 256-thread blocks of k_face_flux32 per SM, i.e. its register
 // budget: 3 caps it at 80 registers (it needs 128 unconstrained); the extra
 // occupancy outweighs the spills (face stage 15% faster at 256^2, 28% at 512^2).
+// 4 (64 registers, ~10% more spill traffic) measured 29.5 us against 29.0 at 256^2.
 #ifndef FACE32_MINB
 #define FACE32_MINB 3
 #endif
